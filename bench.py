@@ -1,0 +1,521 @@
+"""Benchmark: batched FP64 LU with partial pivoting + solve (MatFlat arithmetic) on GB300.
+
+Default workload (the reference's batched LU configuration): 100,000 matrices with n uniform in
+[8, 128], entries N(0,1), lda = n, 4 right-hand sides per matrix, seed 0, all sizes in one
+persistent launch.  A step is one pass of Factorization.Lu + the forward/back solve over the
+whole batch.  Other configurations (--config chol|qr|qr32) are secondary measurements.
+
+Output: one JSON line (rank 0).  `value` = matrices/s with inputs resident in HBM (each step
+restores the input batch with a device-to-device copy, inside the timed region); `e2e` = the same
+through the C ABI from pinned host buffers, copies included; `roofline` for the dominant kernel
+against the FP64 peak measured in this run (cuBLAS DGEMM); `cpu_baseline` = the MatFlat
+restatement (oracle/) on all host cores over a bounded sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config lu]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "lu": dict(workload="batched FP64 LU (partial pivoting, MatFlat order) + 4-RHS solve, "
+                        "100,000 matrices, n~U{8..128}, A~N(0,1), lda=n, seed 0",
+               count=100_000, nmin=8, nmax=128, nrhs=4),
+    "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
+                          "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
+                 count=10_000, n=32, nrhs=1),
+    "qr": dict(workload="batched FP64 Householder QR (MatFlat order) + least squares, 50,000 "
+                        "matrices m~U{64..512}, n~U{16..64}, N(0,1), 1 RHS, seed 0",
+               count=50_000, dtype="f64"),
+    "qr32": dict(workload="batched FP32 Householder QR (MatFlat float overload) + least squares,"
+                          " 50,000 matrices m~U{64..512}, n~U{16..64}, N(0,1), 1 RHS, seed 0",
+                 count=50_000, dtype="f32"),
+}
+
+
+def lu_flops(n, nrhs):
+    """Algorithmic flops of LU (2n^3/3 - n^2/2 - n/6) plus nrhs two-triangle solves (2n^2)."""
+    n = n.astype(np.float64)
+    return float(np.sum(2 * n ** 3 / 3 - n ** 2 / 2 - n / 6 + 2 * n ** 2 * nrhs))
+
+
+def lu_bytes(n, nrhs):
+    """Minimum HBM traffic: read and write A (16 n^2), b (16 n nrhs) and write piv (4 n)."""
+    n = n.astype(np.float64)
+    return float(np.sum(16 * n ** 2 + 16 * n * nrhs + 4 * n))
+
+
+def chol_flops(n, nrhs):
+    n = n.astype(np.float64)
+    return float(np.sum(n ** 3 / 3 + n ** 2 / 2 + n / 6 + 2 * n ** 2 * nrhs))
+
+
+def chol_bytes(n, nrhs):
+    n = n.astype(np.float64)
+    return float(np.sum(16 * n ** 2 + 16 * n * nrhs))
+
+
+def qr_flops(m, n, nrhs):
+    m = m.astype(np.float64)
+    n = n.astype(np.float64)
+    return float(np.sum(2 * m * n ** 2 - 2 * n ** 3 / 3 + nrhs * (4 * m * n - n ** 2)))
+
+
+def qr_bytes(m, n, nrhs, es):
+    m = m.astype(np.float64)
+    n = n.astype(np.float64)
+    return float(np.sum(es * (2 * m * n + n + 2 * m * nrhs)))
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measure_fp64_peak(torch):
+    """FP64 peak of this GPU measured live: cuBLAS DGEMM 4096^3 (torch.matmul), best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def read_traffic(kernel_key):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        line = line.strip()
+        if line.startswith(kernel_key + ":"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def make_inputs(cfg_name, rank):
+    from matflat_gb300 import synth
+    cfg = CONFIGS[cfg_name]
+    if cfg_name == "lu":
+        return synth.lu_batch(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"], seed=rank)
+    if cfg_name == "chol":
+        return synth.spd_batch(cfg["count"], cfg["n"], cfg["nrhs"], seed=rank)
+    return synth.qr_batch(cfg["count"], seed=rank)
+
+
+def cpu_sample_rate(cfg_name, d, budget_s=15.0, threads=None):
+    """Matrices/s of the MatFlat restatement (oracle/) on the host cores over a bounded,
+    evenly strided sample of the same batch."""
+    from oracle import oracle
+    threads = threads or os.cpu_count() or 1
+    count = len(d["n"])
+    # Probe with a small strided sample, then size the sample to the time budget.
+    stride = max(1, count // 512)
+    sample = np.arange(0, count, stride)
+    for _ in range(4):
+        t = run_cpu_sample(cfg_name, d, sample, threads, oracle)
+        if t >= budget_s / 4 or len(sample) >= count:
+            break
+        grow = min(count, int(len(sample) * min(8.0, budget_s / 4 / max(t, 1e-3))))
+        stride = max(1, count // grow)
+        sample = np.arange(0, count, stride)
+    return len(sample) / t, len(sample), threads, t
+
+
+def run_cpu_sample(cfg_name, d, sample, threads, oracle):
+    if cfg_name in ("lu", "chol"):
+        n = d["n"][sample].astype(np.int32)
+        sz = n.astype(np.int64) ** 2
+        a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+        a = np.concatenate([d["a"][d["a_off"][i]:d["a_off"][i] + sz[j]]
+                            for j, i in enumerate(sample)])
+        nrhs = d["nrhs"]
+        bsz = n.astype(np.int64) * nrhs
+        b_off = np.concatenate([[0], np.cumsum(bsz)[:-1]]).astype(np.int64)
+        b = np.concatenate([d["b"][d["b_off"][i]:d["b_off"][i] + bsz[j]]
+                            for j, i in enumerate(sample)])
+        t0 = time.perf_counter()
+        if cfg_name == "lu":
+            piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+            piv = np.zeros(int(n.sum()), np.int32)
+            sign = np.zeros(len(n), np.int32)
+            oracle.lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, threads)
+        else:
+            info = np.zeros(len(n), np.int32)
+            oracle.chol_solve_batched(n, a_off, a, b_off, b, info, threads)
+        return time.perf_counter() - t0
+    m = d["m"][sample].astype(np.int32)
+    n = d["n"][sample].astype(np.int32)
+    sz = m.astype(np.int64) * n
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    dt = np.float32 if cfg_name == "qr32" else np.float64
+    a = np.concatenate([d["a"][d["a_off"][i]:d["a_off"][i] + sz[j]]
+                        for j, i in enumerate(sample)]).astype(dt)
+    b_off = np.concatenate([[0], np.cumsum(m.astype(np.int64))[:-1]]).astype(np.int64)
+    b = np.concatenate([d["b"][d["b_off"][i]:d["b_off"][i] + m[j]]
+                        for j, i in enumerate(sample)]).astype(dt)
+    x_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    x = np.zeros(int(n.sum()), dt)
+    t0 = time.perf_counter()
+    oracle.qr_ls_batched(m, n, a_off, a, b_off, b, x_off, x, threads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, cfg_name):
+    """--impl reference: the MatFlat restatement on all host cores (the reference is C# and
+    cannot run on this machine; the restatement reproduces its arithmetic)."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    d = make_inputs(cfg_name, 0)
+    for _ in range(args.warmup):
+        cpu_sample_rate(cfg_name, d, budget_s=2.0)
+    rates = []
+    sample_n = threads = 0
+    t_all = 0.0
+    for _ in range(args.steps):
+        r, sample_n, threads, t = cpu_sample_rate(cfg_name, d, budget_s=args.ref_budget)
+        rates.append(r)
+        t_all += t
+    value = statistics.median(rates)
+    cfg = CONFIGS[cfg_name]
+    line = {
+        "impl": "reference", "metric": metric_name(cfg_name), "value": value,
+        "unit": "matrices/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_all / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype_name(cfg_name),
+        "data": "synthetic (seeded SplitMix64 + Box-Muller)",
+        "config": {"workload": cfg["workload"], "count": cfg["count"]},
+        "cpu_baseline": {"value": value, "unit": "matrices/s", "cores": threads, "kind": "port",
+                         "sample": "%d matrices evenly strided over the batch per step" % sample_n},
+        "e2e": {"value": value, "unit": "matrices/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def metric_name(cfg_name):
+    return {"lu": "batched FP64 LU+solve matrices/s (MatFlat-exact pivots)",
+            "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
+            "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
+            "qr32": "batched FP32 QR least-squares matrices/s (MatFlat-exact factors)"}[cfg_name]
+
+
+def dtype_name(cfg_name):
+    return "f32" if cfg_name == "qr32" else "f64"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="lu", choices=sorted(CONFIGS))
+    ap.add_argument("--cpu-budget", type=float, default=15.0,
+                    help="seconds of CPU work for the cpu_baseline sample")
+    ap.add_argument("--ref-budget", type=float, default=10.0,
+                    help="seconds of CPU work per step of --impl reference")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: warmup raised to 3", file=sys.stderr)
+        args.warmup = 3
+    cfg_name = args.config
+    if args.impl == "reference":
+        run_reference(args, cfg_name)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import matflat_gb300 as mf
+    from matflat_gb300 import build
+    build.build()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    ctx = mf.context()
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    d = make_inputs(cfg_name, rank)
+    cfg = CONFIGS[cfg_name]
+    count = len(d["n"])
+    if cfg_name in ("qr", "qr32"):
+        dt = torch.float32 if cfg_name == "qr32" else torch.float64
+        npdt = np.float32 if cfg_name == "qr32" else np.float64
+        a_host = torch.from_numpy(d["a"].astype(npdt)).pin_memory()
+        b_host = torch.from_numpy(d["b"].astype(npdt)).pin_memory()
+        plan = mf.QrBatch(d["m"], d["n"], d["a_off"], d["rdiag_off"], nrhs=1, b_off=d["b_off"])
+        a0 = a_host.to("cuda")
+        b0 = b_host.to("cuda")
+        a = torch.empty_like(a0)
+        b = torch.empty_like(b0)
+        rdiag = torch.empty(d["rdiag_total"], dtype=dt, device="cuda")
+        outs_host = [torch.empty_like(a_host).pin_memory(), torch.empty_like(b_host).pin_memory(),
+                     torch.empty(d["rdiag_total"], dtype=dt).pin_memory()]
+
+        def run():
+            plan.run(a, rdiag, b, single=(cfg_name == "qr32"))
+        outs = [a, b, rdiag]
+        flops = qr_flops(d["m"], d["n"], 1)
+        byts = qr_bytes(d["m"], d["n"], 1, 4 if cfg_name == "qr32" else 8)
+        kernel_key = "qr_batched_kernel_" + ("f32" if cfg_name == "qr32" else "f64")
+    else:
+        a_host = torch.from_numpy(d["a"]).pin_memory()
+        b_host = torch.from_numpy(d["b"]).pin_memory()
+        a0 = a_host.to("cuda")
+        b0 = b_host.to("cuda")
+        a = torch.empty_like(a0)
+        b = torch.empty_like(b0)
+        info = torch.zeros(count, dtype=torch.int32, device="cuda")
+        if cfg_name == "lu":
+            plan = mf.LuBatch(d["n"], d["a_off"], d["piv_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+            piv = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
+            sign = torch.zeros(count, dtype=torch.int32, device="cuda")
+
+            def run():
+                plan.run(a, piv, b, sign, info)
+            outs = [a, b, piv, sign, info]
+            flops = lu_flops(d["n"], d["nrhs"])
+            byts = lu_bytes(d["n"], d["nrhs"])
+            kernel_key = "getrf_batched_kernel"
+        else:
+            plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+
+            def run():
+                plan.run(a, b, info)
+            outs = [a, b, info]
+            flops = chol_flops(d["n"], d["nrhs"])
+            byts = chol_bytes(d["n"], d["nrhs"])
+            kernel_key = "potrf_batched_kernel"
+        outs_host = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
+
+    def restore():
+        a.copy_(a0, non_blocking=True)
+        b.copy_(b0, non_blocking=True)
+
+    # ---- device-resident throughput --------------------------------------------------------
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            restore()
+            run()
+        stream.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        kstart = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kend = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            restore()
+            kstart[i].record(stream)
+            run()
+            kend[i].record(stream)
+        t1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        clocks.stop()
+        barrier()
+    total_ms = t0.elapsed_time(t1)
+    kernel_ms = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    value = world * count * args.steps / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI from pinned host memory -------------------------------
+    e2e = None
+    if not args.no_e2e:
+        h2d = a_host.numel() * a_host.element_size() + b_host.numel() * b_host.element_size()
+        d2h = sum(o.numel() * o.element_size() for o in outs)
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                a.copy_(a_host, non_blocking=True)
+                b.copy_(b_host, non_blocking=True)
+                run()
+                for o, oh in zip(outs, outs_host):
+                    oh.copy_(o, non_blocking=True)
+            stream.synchronize()
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                a.copy_(a_host, non_blocking=True)
+                b.copy_(b_host, non_blocking=True)
+                run()
+                for o, oh in zip(outs, outs_host):
+                    oh.copy_(o, non_blocking=True)
+            e1.record(stream)
+            stream.synchronize()
+            barrier()
+        e2e_ms = e0.elapsed_time(e1)
+        if world > 1:
+            tt = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_ms = float(tt.item())
+        e2e = {"value": world * count * args.steps / (e2e_ms / 1e3), "unit": "matrices/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": e2e_ms / args.steps}
+
+    # ---- roofline of the dominant kernel -----------------------------------------------------
+    fp64_peak = measure_fp64_peak(torch)
+    kmed = statistics.median(kernel_ms)
+    achieved_tf = flops / (kmed / 1e3) / 1e12
+    traffic = read_traffic(kernel_key)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    roof = {
+        "bound": "fp64",
+        "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": achieved_tf / fp64_peak,
+        "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 has no entry in "
+                       "MEASURED_PEAKS.json)",
+        "exact_order_ceiling_frac": 0.5,
+        "note": "MatFlat-exact arithmetic issues every multiply and add separately (no FMA), so "
+                "this kernel's own ceiling is half the DFMA peak",
+        "traffic": traffic, "algorithmic_bytes_per_launch": byts,
+        "hbm_achieved_gbs": byts / (kmed / 1e3) / 1e9, "hbm_peak_gbs": hbm,
+        "hbm_frac": byts / (kmed / 1e3) / 1e9 / hbm,
+        "kernel_ms": kmed, "kernel": kernel_key,
+    }
+
+    # ---- CPU baseline (rank 0, N=1 only) ----------------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, sample_n, threads, t = cpu_sample_rate(cfg_name, d, budget_s=args.cpu_budget)
+        cpu = {"value": rate, "unit": "matrices/s", "cores": threads, "kind": "port",
+               "sample": "%d of %d matrices, evenly strided over the batch (%.1f s)"
+                         % (sample_n, count, t)}
+
+    if rank == 0:
+        line = {
+            "metric": metric_name(cfg_name), "value": value, "unit": "matrices/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype_name(cfg_name),
+            "data": "synthetic (seeded SplitMix64 + Box-Muller, identical bytes for CPU and GPU)",
+            "config": {"workload": cfg["workload"], "count": count,
+                       "per_rank_batch": count, "l2": "inputs (%.1f GB) larger than L2"
+                       % (a0.numel() * a0.element_size() / 1e9),
+                       "step_includes": "device-to-device restore of the input batch + the "
+                                        "batched factorization/solve (one graph replay)"},
+            "kernel_ms_per_step": kmed,
+            "gpu_launches": args.steps,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * matflat_gpu.h — C ABI of the GB300 (sm_103a) implementation of MatFlat's factorization path.
+ *
+ * The reference is the pure-C# library MatFlat 0.8.2 (sinshu/matflat).  Its hot path is a set of
+ * `public static unsafe` methods on `MatFlat.Factorization` and `MatFlat.Blas` that take raw
+ * column-major pointers, a leading dimension and CBLAS-valued enums.  Each single-matrix entry
+ * point below replaces one of those methods one for one (cited per function) and keeps its
+ * argument meaning; a C# facade binds them with [LibraryImport] (the binding is shown in the
+ * integration notes of this repository).  The batched entry points are new overloads beside
+ * them: one call factors tens of thousands of matrices of uneven size.
+ *
+ * Conventions shared by every entry point:
+ *  - Column-major storage with an explicit leading dimension, as in MatFlat.
+ *  - Return value: MFG_OK (0); a negative value -i when argument i (1-based, counting the
+ *    context as argument 1) is invalid, checked in the same order MatFlat checks its arguments;
+ *    or one of the MFG_ERR_* codes below.  No exception crosses the ABI.  Numerical failure that
+ *    MatFlat reports by throwing MatrixFactorizationException is reported through an `info`
+ *    output (0 = success, k+1 = first failing column k), never by a failing status.
+ *  - Single-matrix entry points take HOST pointers (the memory MatFlat's callers pass); the library
+ *    stages the data to the device and back and returns after the result is in host memory.
+ *  - Batched entry points take DEVICE pointers and are asynchronous on the context's stream.
+ *  - The plain FP64 path reproduces MatFlat's arithmetic operation by operation (same summation
+ *    trees, no fused multiply-add, IEEE division and square root), so factors, pivots and
+ *    solutions are bit-identical to MatFlat's.
+ *  - A context is not thread-safe; use one context per host thread.  Distinct contexts are
+ *    independent.
+ */
+#ifndef MATFLAT_GPU_H
+#define MATFLAT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define MFG_API __declspec(dllexport)
+#else
+#define MFG_API __attribute__((visibility("default")))
+#endif
+
+/* MatFlat.Uplo (MatFlat/Uplo.cs:13,18) and MatFlat.Transpose (MatFlat/Transpose.cs:13-28);
+ * CBLAS-compatible values. */
+enum mfg_uplo { MFG_UPPER = 121, MFG_LOWER = 122 };
+enum mfg_transpose {
+  MFG_NOTRANS = 111,
+  MFG_TRANS = 112,
+  MFG_CONJTRANS = 113,
+  MFG_CONJNOTRANS = 114
+};
+
+enum mfg_status {
+  MFG_OK = 0,
+  MFG_ERR_CUDA = -1000,        /* a CUDA runtime call failed; see mfg_last_error */
+  MFG_ERR_NO_DEVICE = -1001,   /* no CUDA device, or the kernels are not built for it */
+  MFG_ERR_ALLOC = -1002,       /* device or pinned allocation failed */
+  MFG_ERR_INPLACE = -1003,     /* MulMatMat: a == c or b == c ("In-place operation is not
+                                  supported.", Blas.MulMatMat.cs:301-304) */
+  MFG_ERR_TIMEOUT = -1004,     /* a bounded device-side wait gave up (see mfg_plan_status) */
+  MFG_ERR_UNSUPPORTED = -1005  /* size or option outside what this build supports */
+};
+
+typedef struct mfg_ctx mfg_ctx;
+typedef struct mfg_plan mfg_plan;
+
+/* ---------------------------------------------------------------------------------------------
+ * Context: owns a CUDA stream, a device workspace, the CUDA-graph cache and the tuning table.
+ * ------------------------------------------------------------------------------------------- */
+MFG_API int mfg_create(mfg_ctx** ctx);
+MFG_API int mfg_destroy(mfg_ctx* ctx);
+/* Use `stream` (a cudaStream_t) for all later work; NULL selects the context's own stream. */
+MFG_API int mfg_set_stream(mfg_ctx* ctx, void* stream);
+MFG_API int mfg_synchronize(mfg_ctx* ctx);
+/* Text of the last failure on this context (empty when none).  Valid until the next call. */
+MFG_API const char* mfg_last_error(mfg_ctx* ctx);
+/* Library version, e.g. "0.1.0"; the MatFlat version whose arithmetic it reproduces is 0.8.2. */
+MFG_API const char* mfg_version(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Single-matrix drop-ins (host pointers).  Same argument meaning as the MatFlat method cited.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Factorization.Lu(int m, int n, double* a, int lda, int* piv) -> pivot sign
+ * (MatFlat/Factorization.Lu.cs:122-161; LuCore :296-350).  piv has m entries and is a
+ * permutation vector: row i of P*A is row piv[i] of A.  *sign receives Lu's return value.
+ * Like MatFlat, a zero pivot is not an error (the column is left undivided). */
+MFG_API int mfg_dgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign);
+
+/* Factorization.Cholesky(int n, double* a, int lda) (MatFlat/Factorization.Cholesky.cs:114-168).
+ * Reads the upper triangle, writes L to the lower triangle and zeroes the strict upper triangle.
+ * *info = 0 on success, or k+1 when the matrix is not positive definite at column k (where
+ * MatFlat throws MatrixFactorizationException; the content of a is then unspecified). */
+MFG_API int mfg_dpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info);
+
+/* Factorization.Qr(int m, int n, double* a, int lda, double* rdiag)
+ * (MatFlat/Factorization.Qr.cs:115-172): Householder QR in the Mapack format, m >= n. */
+MFG_API int mfg_dgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag);
+/* Factorization.QrOrthogonalFactor (MatFlat/Factorization.Qr.cs:357-413): thin m-by-n Q. */
+MFG_API int mfg_dorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq);
+/* Factorization.QrUpperTriangularFactor (MatFlat/Factorization.Qr.cs:597-650): n-by-n R. */
+MFG_API int mfg_dqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
+                      const double* rdiag);
+
+/* Float overloads of the three QR routines (MatFlat/Factorization.Qr.cs:32-89, :278-334,
+ * :518-571): float storage, dots and norms summed in double as MatFlat does. */
+MFG_API int mfg_sgeqrf(mfg_ctx* ctx, int m, int n, float* a, int lda, float* rdiag);
+MFG_API int mfg_sorgqr(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* q, int ldq);
+MFG_API int mfg_sqr_r(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* r, int ldr,
+                      const float* rdiag);
+
+/* Blas.SolveTriangular(Uplo, Transpose, int n, double* a, int lda, double* x, int incx)
+ * (MatFlat/Blas.SolveTriangular.cs:162-242): non-unit diagonal, NoTrans or Trans. */
+MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
+                      double* x, int incx);
+
+/* Blas.MulMatMat(Transpose, Transpose, int m, int n, int k, double* a, int lda, double* b,
+ * int ldb, double* c, int ldc) (MatFlat/Blas.MulMatMat.cs:226-368): C = op(A) op(B), C is
+ * overwritten, aliasing of C with A or B is rejected with MFG_ERR_INPLACE. */
+MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
+                      int lda, const double* b, int ldb, double* c, int ldc);
+
+/* Factorization.LuInverse(int n, double* a, int lda, int* piv)
+ * (MatFlat/Factorization.LuInverse.cs:123-199): overwrites the LU factors with A^-1.
+ * *info = 1 when a diagonal entry of U is zero (MatFlat throws "The matrix is not invertible."),
+ * in which case a is left unchanged. */
+MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched overloads (new).  A plan fixes the shapes of a batch once: the host runtime sorts the
+ * matrices by work (longest first), uploads the descriptors, picks the launch shape from the
+ * tuning table and captures the launch sequence as a CUDA graph on first execution.  Executing a
+ * plan is then a single graph replay on the context's stream, with device pointers only.
+ *
+ * Layout of a batch: matrix i is square of order n[i], stored column-major at
+ * a + a_off[i] with leading dimension lda[i] (lda may be NULL: lda[i] = n[i]); its pivot vector
+ * at piv + piv_off[i] (n[i] ints); its right-hand sides at b + b_off[i], nrhs columns with
+ * leading dimension n[i].  Offsets are in elements.  All descriptor arrays are HOST arrays,
+ * read during plan creation only.
+ * ------------------------------------------------------------------------------------------- */
+
+/* LU with partial pivoting of every matrix (Factorization.Lu), then, when nrhs > 0, the solve
+ * A x = b for nrhs right-hand sides: b' = P b, the unit-lower solve in MatFlat's LuInverse
+ * idiom (MatFlat/Factorization.LuInverse.cs:174-182) and the upper solve
+ * (Blas.SolveTriangular Upper/NoTrans, MatFlat/Blas.SolveTriangular.cs:191-199). */
+MFG_API int mfg_plan_getrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, const int64_t* piv_off,
+                                   int nrhs, const int64_t* b_off);
+/* Executes a getrf plan.  a: in/out factors; piv: out; b: in/out solutions (NULL if nrhs = 0);
+ * sign: out, one per matrix (Lu's return value); info: out, one per matrix (0, or k+1 for the
+ * first exactly-zero pivot U(k,k), LAPACK's convention; the factorization still completes). */
+MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                               int* info);
+
+/* Cholesky of every matrix (Factorization.Cholesky), then, when nrhs > 0, L y = b
+ * (SolveTriangular Lower/NoTrans) and L^T x = y (SolveTriangular Lower/Trans) per right-hand
+ * side.  info: 0, or k+1 for a matrix that is not positive definite at column k (its b is left
+ * unchanged and its a unspecified). */
+MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, int nrhs,
+                                   const int64_t* b_off);
+MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
+
+/* Householder QR of every tall matrix (Factorization.Qr; m[i] >= n[i], lda[i] >= m[i]), then,
+ * when nrhs > 0, the least-squares solve min ||A x - b|| of nrhs right-hand sides per matrix
+ * (b: nrhs columns of m[i] entries, leading dimension m[i]).  MatFlat has no QR solve; the
+ * solver applies the same reflector updates to b (Qr.cs:160-165) and then solves R x = (Q^T b)
+ * with SolveTriangular Upper/NoTrans (Blas.SolveTriangular.cs:191-199).  On exit b[0:n] holds
+ * x and b[n:m] the residual components; a and rdiag hold the factorization in MatFlat's format.
+ * The same plan runs in double (mfg_dgeqrf_batched) or float (mfg_sgeqrf_batched, MatFlat's
+ * float overload: float storage, double-accumulated dots). */
+MFG_API int mfg_plan_geqrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* m,
+                                   const int* n, const int* lda, const int64_t* a_off,
+                                   const int64_t* rdiag_off, int nrhs, const int64_t* b_off);
+MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b);
+MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b);
+
+MFG_API int mfg_plan_destroy(mfg_plan* plan);
+
+/* Reads back the device-side status word of the last execution of `plan` (synchronizes the
+ * context's stream): MFG_OK, or MFG_ERR_TIMEOUT if a bounded device-side wait gave up. */
+MFG_API int mfg_plan_status(mfg_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MATFLAT_GPU_H */

@@ -1,0 +1,440 @@
+"""ctypes binding of libmatflat_gpu.so and the MatFlat-shaped facade above it."""
+import ctypes
+import enum
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libmatflat_gpu.so")
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+_c_i64_p = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+_I = ctypes.c_int
+
+_SIGS = {
+    "mfg_version": (ctypes.c_char_p, []),
+    "mfg_create": (_I, [ctypes.POINTER(_vp)]),
+    "mfg_destroy": (_I, [_vp]),
+    "mfg_set_stream": (_I, [_vp, _vp]),
+    "mfg_synchronize": (_I, [_vp]),
+    "mfg_last_error": (ctypes.c_char_p, [_vp]),
+    "mfg_dgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_dpotrf": (_I, [_vp, _I, _vp, _I, _c_int_p]),
+    "mfg_dgeqrf": (_I, [_vp, _I, _I, _vp, _I, _vp]),
+    "mfg_dorgqr": (_I, [_vp, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_dqr_r": (_I, [_vp, _I, _I, _vp, _I, _vp, _I, _vp]),
+    "mfg_sgeqrf": (_I, [_vp, _I, _I, _vp, _I, _vp]),
+    "mfg_sorgqr": (_I, [_vp, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_sqr_r": (_I, [_vp, _I, _I, _vp, _I, _vp, _I, _vp]),
+    "mfg_plan_geqrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _vp, _I,
+                                    _vp]),
+    "mfg_dgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_sgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dtrsv": (_I, [_vp, _I, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_dgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
+    "mfg_dgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_plan_getrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _I, _vp]),
+    "mfg_plan_potrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _I, _vp]),
+    "mfg_plan_destroy": (_I, [_vp]),
+    "mfg_plan_status": (_I, [_vp]),
+    "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+}
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def library():
+    """Loads libmatflat_gpu.so (raises if it has not been built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not os.path.exists(_LIB_PATH):
+                raise RuntimeError(
+                    "libmatflat_gpu.so is not built (run `python -c \"import __graft_entry__ as g; "
+                    "g.build()\"` or `python matflat_gb300/build.py`)")
+            lib = ctypes.CDLL(_LIB_PATH)
+            for name, (res, args) in _SIGS.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+# ---------------------------------------------------------------------------------------------
+# MatFlat's exception hierarchy (MatFlat/MatFlatException.cs, MatrixFactorizationException.cs)
+# and the .NET argument exceptions it throws.
+
+class MatFlatException(Exception):
+    """MatFlat.MatFlatException."""
+
+
+class MatrixFactorizationException(MatFlatException):
+    """MatFlat.MatrixFactorizationException: thrown when a factorization fails."""
+
+
+class ArgumentException(ValueError):
+    """System.ArgumentException."""
+
+    def __init__(self, message, param=None):
+        super().__init__(message if param is None else "%s (Parameter '%s')" % (message, param))
+        self.param = param
+
+
+class ArgumentNullException(ArgumentException):
+    """System.ArgumentNullException."""
+
+    def __init__(self, param):
+        super().__init__("Value cannot be null.", param)
+
+
+class Uplo(enum.IntEnum):
+    """MatFlat.Uplo (MatFlat/Uplo.cs:13,18)."""
+    Upper = 121
+    Lower = 122
+
+
+class Transpose(enum.IntEnum):
+    """MatFlat.Transpose (MatFlat/Transpose.cs:13-28)."""
+    NoTrans = 111
+    Trans = 112
+    ConjTrans = 113
+    ConjNoTrans = 114
+
+
+class _Context:
+    def __init__(self):
+        lib = library()
+        h = _vp()
+        rc = lib.mfg_create(ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError("mfg_create failed (%d): no usable CUDA device" % rc)
+        self.h = h
+        self.lib = lib
+
+    def set_stream(self, stream_handle):
+        self.lib.mfg_set_stream(self.h, _vp(stream_handle or 0))
+
+    def synchronize(self):
+        self.check(self.lib.mfg_synchronize(self.h))
+
+    def last_error(self):
+        msg = self.lib.mfg_last_error(self.h)
+        return msg.decode() if msg else ""
+
+    def check(self, rc, what="call"):
+        if rc != 0:
+            raise RuntimeError("%s failed with status %d: %s" % (what, rc, self.last_error()))
+
+
+_ctx = None
+_ctx_lock = threading.Lock()
+
+
+def context():
+    """The process-wide default context (created on first use)."""
+    global _ctx
+    with _ctx_lock:
+        if _ctx is None:
+            _ctx = _Context()
+    return _ctx
+
+
+def _need(arr, count, name, dtype=np.float64):
+    if arr is None:
+        raise ArgumentNullException(name)
+    if not isinstance(arr, np.ndarray) or arr.dtype != dtype or arr.ndim != 1 or not \
+            arr.flags["C_CONTIGUOUS"]:
+        raise TypeError("%s must be a contiguous 1-D numpy array of %s" % (name, np.dtype(dtype)))
+    if arr.size < count:
+        raise ArgumentException("The array is too small (%d < %d elements)." % (arr.size, count),
+                                name)
+
+
+def _dt(a):
+    return np.float32 if isinstance(a, np.ndarray) and a.dtype == np.float32 else np.float64
+
+
+def _span(rows, cols, ld):
+    return 0 if rows <= 0 or cols <= 0 else ld * (cols - 1) + rows
+
+
+def _ptr(arr):
+    return _vp(arr.ctypes.data)
+
+
+def _raise_status(rc, names, ctx):
+    """Maps a negative argument status to the .NET exception MatFlat throws."""
+    msg = ctx.last_error()
+    if rc == -1003:
+        raise ArgumentException("In-place operation is not supported.")
+    if rc < 0 and -rc - 2 < len(names):
+        name = names[-rc - 2]
+        if msg.endswith("is null"):
+            raise ArgumentNullException(name)
+        raise ArgumentException(msg, name)
+    raise RuntimeError("status %d: %s" % (rc, msg))
+
+
+class Factorization:
+    """Mirror of MatFlat.Factorization (double overloads on the GPU)."""
+
+    @staticmethod
+    def Lu(m, n, a, lda, piv):
+        """Factorization.Lu (MatFlat/Factorization.Lu.cs:122-161); returns the pivot sign."""
+        ctx = context()
+        if m > 0 and n > 0 and lda >= m:
+            _need(a, _span(m, n, lda), "a")
+            _need(piv, m, "piv", np.int32)
+        sign = ctypes.c_int(0)
+        rc = ctx.lib.mfg_dgetrf(ctx.h, m, n, None if a is None else _ptr(a), lda,
+                                None if piv is None else _ptr(piv), ctypes.byref(sign))
+        if rc != 0:
+            _raise_status(rc, ["m", "n", "a", "lda", "piv"], ctx)
+        return sign.value
+
+    @staticmethod
+    def Cholesky(n, a, lda):
+        """Factorization.Cholesky (MatFlat/Factorization.Cholesky.cs:114-168)."""
+        ctx = context()
+        if n > 0 and lda >= n:
+            _need(a, _span(n, n, lda), "a")
+        info = ctypes.c_int(0)
+        rc = ctx.lib.mfg_dpotrf(ctx.h, n, None if a is None else _ptr(a), lda, ctypes.byref(info))
+        if rc != 0:
+            _raise_status(rc, ["n", "a", "lda"], ctx)
+        if info.value != 0:
+            raise MatrixFactorizationException(
+                "Cholesky decomposition failed. The matrix must be positive definite.")
+
+    @staticmethod
+    def Qr(m, n, a, lda, rdiag):
+        """Factorization.Qr (MatFlat/Factorization.Qr.cs:115-172 double, :32-89 float)."""
+        ctx = context()
+        dt = _dt(a)
+        if m > 0 and n > 0 and lda >= m and n <= m:
+            _need(a, _span(m, n, lda), "a", dt)
+            _need(rdiag, n, "rdiag", dt)
+        fn = ctx.lib.mfg_sgeqrf if dt == np.float32 else ctx.lib.mfg_dgeqrf
+        rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
+                                None if rdiag is None else _ptr(rdiag))
+        if rc != 0:
+            _raise_status(rc, ["m", "n", "a", "lda", "rdiag"], ctx)
+
+    @staticmethod
+    def QrOrthogonalFactor(m, n, a, lda, q, ldq):
+        """Factorization.QrOrthogonalFactor (MatFlat/Factorization.Qr.cs:357-413, :278-334)."""
+        ctx = context()
+        dt = _dt(a)
+        if m > 0 and n > 0 and lda >= m and ldq >= m and n <= m:
+            _need(a, _span(m, n, lda), "a", dt)
+            _need(q, _span(m, n, ldq), "q", dt)
+        fn = ctx.lib.mfg_sorgqr if dt == np.float32 else ctx.lib.mfg_dorgqr
+        rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
+                                None if q is None else _ptr(q), ldq)
+        if rc != 0:
+            _raise_status(rc, ["m", "n", "a", "lda", "q", "ldq"], ctx)
+
+    @staticmethod
+    def QrUpperTriangularFactor(m, n, a, lda, r, ldr, rdiag):
+        """Factorization.QrUpperTriangularFactor (MatFlat/Factorization.Qr.cs:597-650, :518-571)."""
+        ctx = context()
+        dt = _dt(a)
+        if m > 0 and n > 0 and lda >= m and ldr >= n and n <= m:
+            _need(a, _span(m, n, lda), "a", dt)
+            _need(r, _span(n, n, ldr), "r", dt)
+            _need(rdiag, n, "rdiag", dt)
+        fn = ctx.lib.mfg_sqr_r if dt == np.float32 else ctx.lib.mfg_dqr_r
+        rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
+                               None if r is None else _ptr(r), ldr,
+                               None if rdiag is None else _ptr(rdiag))
+        if rc != 0:
+            _raise_status(rc, ["m", "n", "a", "lda", "r", "ldr", "rdiag"], ctx)
+
+    @staticmethod
+    def LuInverse(n, a, lda, piv):
+        """Factorization.LuInverse (MatFlat/Factorization.LuInverse.cs:123-199)."""
+        ctx = context()
+        if n > 0 and lda >= n:
+            _need(a, _span(n, n, lda), "a")
+            _need(piv, n, "piv", np.int32)
+        info = ctypes.c_int(0)
+        rc = ctx.lib.mfg_dgetri(ctx.h, n, None if a is None else _ptr(a), lda,
+                                None if piv is None else _ptr(piv), ctypes.byref(info))
+        if rc != 0:
+            _raise_status(rc, ["n", "a", "lda", "piv"], ctx)
+        if info.value != 0:
+            raise MatrixFactorizationException("The matrix is not invertible.")
+
+
+class Blas:
+    """Mirror of MatFlat.Blas (double overloads on the GPU)."""
+
+    @staticmethod
+    def SolveTriangular(uplo, transa, n, a, lda, x, incx):
+        """Blas.SolveTriangular (MatFlat/Blas.SolveTriangular.cs:162-242)."""
+        ctx = context()
+        if n > 0 and lda >= n and incx > 0:
+            _need(a, _span(n, n, lda), "a")
+            _need(x, (n - 1) * incx + 1, "x")
+        rc = ctx.lib.mfg_dtrsv(ctx.h, int(uplo), int(transa), n, None if a is None else _ptr(a),
+                               lda, None if x is None else _ptr(x), incx)
+        if rc != 0:
+            _raise_status(rc, ["uplo", "transa", "n", "a", "lda", "x", "incx"], ctx)
+
+    @staticmethod
+    def MulMatMat(transa, transb, m, n, k, a, lda, b, ldb, c, ldc):
+        """Blas.MulMatMat (MatFlat/Blas.MulMatMat.cs:226-368)."""
+        ctx = context()
+        ok = m > 0 and n > 0 and k > 0 and ldc >= m
+        ta, tb = int(transa), int(transb)
+        if ok and ta in (111, 112) and tb in (111, 112):
+            ar, ac = (m, k) if ta == 111 else (k, m)
+            br, bc = (k, n) if tb == 111 else (n, k)
+            if lda >= ar and ldb >= br:
+                _need(a, _span(ar, ac, lda), "a")
+                _need(b, _span(br, bc, ldb), "b")
+                _need(c, _span(m, n, ldc), "c")
+                if a is not None and c is not None and (np.shares_memory(a, c) or
+                                                        np.shares_memory(b, c)):
+                    raise ArgumentException("In-place operation is not supported.")
+        rc = ctx.lib.mfg_dgemm(ctx.h, ta, tb, m, n, k, None if a is None else _ptr(a), lda,
+                               None if b is None else _ptr(b), ldb,
+                               None if c is None else _ptr(c), ldc)
+        if rc != 0:
+            _raise_status(rc, ["transa", "transb", "m", "n", "k", "a", "lda", "b", "ldb", "c",
+                               "ldc"], ctx)
+
+
+# ---------------------------------------------------------------------------------------------
+# Batched overloads.  Arrays are device memory: pass torch CUDA tensors or raw device pointers.
+
+def _dptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return _vp(x)
+    return _vp(x.data_ptr())
+
+
+class _Batch:
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.h = handle
+
+    def close(self):
+        if self.h is not None and self.h.value:
+            self.ctx.lib.mfg_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def status(self):
+        self.ctx.check(self.ctx.lib.mfg_plan_status(self.h), "mfg_plan_status")
+
+
+def _i32(x):
+    return np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+
+
+def _i64(x):
+    return np.ascontiguousarray(np.asarray(x, dtype=np.int64))
+
+
+class LuBatch(_Batch):
+    """Batched Factorization.Lu (+ solve of nrhs right-hand sides) over matrices of uneven n.
+
+    n, a_off, piv_off, b_off are host arrays describing the layout (element offsets into the
+    device buffers passed to `run`); lda defaults to n.
+    """
+
+    def __init__(self, n, a_off, piv_off, nrhs=0, b_off=None, lda=None, ctx=None):
+        ctx = ctx or context()
+        self._n = _i32(n)
+        self._lda = None if lda is None else _i32(lda)
+        self._a_off = _i64(a_off)
+        self._piv_off = _i64(piv_off)
+        self._b_off = None if b_off is None else _i64(b_off)
+        h = _vp()
+        rc = ctx.lib.mfg_plan_getrf_batched(
+            ctx.h, ctypes.byref(h), len(self._n), _ptr(self._n),
+            None if self._lda is None else _ptr(self._lda), _ptr(self._a_off),
+            _ptr(self._piv_off), nrhs, None if self._b_off is None else _ptr(self._b_off))
+        ctx.check(rc, "mfg_plan_getrf_batched")
+        super().__init__(ctx, h)
+        self.count = len(self._n)
+        self.nrhs = nrhs
+
+    def run(self, a, piv, b, sign, info):
+        rc = self.ctx.lib.mfg_dgetrf_batched(self.h, _dptr(a), _dptr(piv), _dptr(b), _dptr(sign),
+                                             _dptr(info))
+        self.ctx.check(rc, "mfg_dgetrf_batched")
+
+
+class CholeskyBatch(_Batch):
+    """Batched Factorization.Cholesky (+ L y = b, L^T x = y) over matrices of uneven n."""
+
+    def __init__(self, n, a_off, nrhs=0, b_off=None, lda=None, ctx=None):
+        ctx = ctx or context()
+        self._n = _i32(n)
+        self._lda = None if lda is None else _i32(lda)
+        self._a_off = _i64(a_off)
+        self._b_off = None if b_off is None else _i64(b_off)
+        h = _vp()
+        rc = ctx.lib.mfg_plan_potrf_batched(
+            ctx.h, ctypes.byref(h), len(self._n), _ptr(self._n),
+            None if self._lda is None else _ptr(self._lda), _ptr(self._a_off), nrhs,
+            None if self._b_off is None else _ptr(self._b_off))
+        ctx.check(rc, "mfg_plan_potrf_batched")
+        super().__init__(ctx, h)
+        self.count = len(self._n)
+        self.nrhs = nrhs
+
+    def run(self, a, b, info):
+        rc = self.ctx.lib.mfg_dpotrf_batched(self.h, _dptr(a), _dptr(b), _dptr(info))
+        self.ctx.check(rc, "mfg_dpotrf_batched")
+
+
+class QrBatch(_Batch):
+    """Batched Factorization.Qr of tall matrices (+ least squares of nrhs right-hand sides).
+
+    m, n, a_off, rdiag_off, b_off are host arrays; lda defaults to m; b has nrhs columns of m
+    entries per matrix.  `run` takes float64 or float32 device buffers (MatFlat's two overloads).
+    """
+
+    def __init__(self, m, n, a_off, rdiag_off, nrhs=0, b_off=None, lda=None, ctx=None):
+        ctx = ctx or context()
+        self._m = _i32(m)
+        self._n = _i32(n)
+        self._lda = None if lda is None else _i32(lda)
+        self._a_off = _i64(a_off)
+        self._rdiag_off = _i64(rdiag_off)
+        self._b_off = None if b_off is None else _i64(b_off)
+        h = _vp()
+        rc = ctx.lib.mfg_plan_geqrf_batched(
+            ctx.h, ctypes.byref(h), len(self._m), _ptr(self._m), _ptr(self._n),
+            None if self._lda is None else _ptr(self._lda), _ptr(self._a_off),
+            _ptr(self._rdiag_off), nrhs, None if self._b_off is None else _ptr(self._b_off))
+        ctx.check(rc, "mfg_plan_geqrf_batched")
+        super().__init__(ctx, h)
+        self.count = len(self._m)
+        self.nrhs = nrhs
+
+    def run(self, a, rdiag, b=None, single=False):
+        fn = self.ctx.lib.mfg_sgeqrf_batched if single else self.ctx.lib.mfg_dgeqrf_batched
+        rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
+        self.ctx.check(rc, "mfg_geqrf_batched")

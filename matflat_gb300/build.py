@@ -1,0 +1,87 @@
+"""Builds the CUDA library libmatflat_gpu.so in-tree (matflat_gb300/_lib/).
+
+Every translation unit is compiled for sm_103a only (GB300), in parallel, then linked into one
+shared object exporting the C ABI declared in include/matflat_gpu.h.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUT, "libmatflat_gpu.so")
+SYNTH_LIB = os.path.join(OUT, "libmatflat_synth.so")
+SOURCES = ["lu.cu", "chol.cu", "blas.cu", "qr.cu", "runtime.cu"]
+HEADERS = ["mf_device.cuh", "mf_solve.cuh", "mf_kernels.h"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+              "--expt-relaxed-constexpr"]
+
+
+def nvcc():
+    path = shutil.which("nvcc")
+    if path:
+        return path
+    cand = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(cand):
+        return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_synth(force=False):
+    """Host-only helper library for seeded synthetic inputs (benchmark and tests)."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(CSRC, "synth.c")
+    if force or _stale(SYNTH_LIB, [src]):
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
+                               "-o", SYNTH_LIB + ".tmp", src, "-lm"])
+        os.replace(SYNTH_LIB + ".tmp", SYNTH_LIB)
+    return SYNTH_LIB
+
+
+def build(force=False, verbose=False, extra_flags=()):
+    os.makedirs(OUT, exist_ok=True)
+    build_synth(force)
+    srcs = [os.path.join(CSRC, s) for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [
+        os.path.join(os.path.dirname(HERE), "include", "matflat_gpu.h")]
+    objs = []
+    jobs = []
+    for s in srcs:
+        o = os.path.join(OUT, os.path.basename(s) + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            cmd = [nvcc()] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", s, "-o", o]
+            jobs.append(cmd)
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            futs = [ex.submit(subprocess.run, cmd, capture_output=True, text=True) for cmd in jobs]
+            for cmd, f in zip(jobs, futs):
+                r = f.result()
+                if verbose or r.returncode != 0:
+                    sys.stderr.write(r.stdout + r.stderr)
+                if r.returncode != 0:
+                    raise RuntimeError("nvcc failed: " + " ".join(cmd))
+    if force or jobs or _stale(LIB, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart_static", "-lrt",
+                                                                        "-ldl", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("link failed")
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

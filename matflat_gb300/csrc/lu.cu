@@ -1,0 +1,250 @@
+// LU with partial pivoting in MatFlat's arithmetic (Factorization.LuCore,
+// MatFlat/Factorization.Lu.cs:296-350), plus the fused solve used by the batched solver.
+//
+// MatFlat is a left-looking "dot product" LU: for column j it computes every entry as
+//     v(i,j) = A'(i,j) - Dot(min(i,j), L(i,0:), U(0:,j))         (Lu.cs:315-320)
+// with Internals.Dot's pairwise tree, picks the pivot by a strict ">" scan over |v|
+// (Lu.cs:323-330), swaps whole rows (Lu.cs:332-337) and divides the sub-diagonal by the pivot
+// (Lu.cs:340-344).  Every entry's value depends only on its own dot, so the entries can be
+// computed in any order that respects data dependencies.  This kernel uses the Crout order:
+// step k finishes row k of U (U(k,j), j > k: dots of length k) and column k+1 of L (dots of
+// length k+1), each dot evaluated with exactly MatFlat's tree, so factors and pivots are
+// bit-identical.  To keep the 32 lanes busy, the long prefix of every column-(k+1) dot (all pairs
+// but the last) runs in the same round as the row-k dots; the last pair, which needs L(:,k) and
+// U(k,k+1), is added afterwards:
+//     Dot(k+1, x, y) = Dot(k-1, x, y) + (x[k-1]*y[k-1] + x[k]*y[k])      (k >= 1)
+//     Dot(1, x, y)   = x[0]*y[0]
+//
+// One warp owns one matrix; the matrix stays in its global buffer (L1/L2 resident while it is
+// being factored): on GB300 the FP64 pipe, not memory, bounds this kernel.
+#include <cuda_runtime.h>
+
+#include "mf_device.cuh"
+#include "mf_kernels.h"
+#include "mf_solve.cuh"
+
+namespace mfg {
+
+// Finishes column c (rows [c, m)) once its dot sums are final, then pivots and scales it.
+//   mode 0: column 0 (no dot: v = A - 0.0 = A, left as is)
+//   mode 1: column 1 (sum = L(i,0) * U(0,1))
+//   mode 2: column c >= 2 (sum = scol[i] + (L(i,c-2)*U(c-2,c) + L(i,c-1)*U(c-1,c)))
+__device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long long lda, int c,
+                                                 int mode, const double* scol, int* piv,
+                                                 int& sign, int& info) {
+  const int lane = threadIdx.x & 31;
+  double* cc = a + (long long)c * lda;
+  unsigned long long bkey = 0ull;
+  int bidx = INT_MAX;
+  bool first_nan = false;
+  if (mode == 0) {
+    for (int i = c + lane; i < m; i += 32) {
+      const double v = cc[i];
+      const unsigned long long key = pivot_key(v);
+      if (key > bkey) {
+        bkey = key;
+        bidx = i;
+      }
+      if (i == c) first_nan = is_nan(v);
+    }
+  } else {
+    const double* l1 = a + (long long)(c - 1) * lda;  // L(:, c-1)
+    const double u1 = cc[c - 1];                       // U(c-1, c)
+    const double* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
+    const double u2 = (mode == 2) ? cc[c - 2] : 0.0;   // U(c-2, c)
+    for (int i = c + lane; i < m; i += 32) {
+      double s;
+      if (mode == 1) {
+        s = __dmul_rn(l1[i], u1);
+      } else {
+        s = __dadd_rn(scol[i], __dadd_rn(__dmul_rn(l2[i], u2), __dmul_rn(l1[i], u1)));
+      }
+      const double v = __dsub_rn(cc[i], s);
+      cc[i] = v;
+      const unsigned long long key = pivot_key(v);
+      if (key > bkey) {
+        bkey = key;
+        bidx = i;
+      }
+      if (i == c) first_nan = is_nan(v);
+    }
+  }
+  int p = warp_argmax(bkey, bidx);
+  // Row c is handled by lane 0; a NaN there can never be displaced by the strict ">" scan.
+  if (__shfl_sync(FULL_MASK, first_nan ? 1 : 0, 0)) p = c;
+  __syncwarp();
+  if (p != c && p < m) {
+    for (int col = lane; col < n; col += 32) {
+      double* base = a + (long long)col * lda;
+      const double t = base[c];
+      base[c] = base[p];
+      base[p] = t;
+    }
+    if (lane == 0) {
+      const int t = piv[c];
+      piv[c] = piv[p];
+      piv[p] = t;
+    }
+    sign = -sign;
+  }
+  __syncwarp();
+  const double diag = cc[c];
+  if (nonzero(diag)) {
+    for (int i = c + 1 + lane; i < m; i += 32) cc[i] = __ddiv_rn(cc[i], diag);
+  } else if (info == 0) {
+    info = c + 1;
+  }
+  __syncwarp();
+}
+
+// Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
+// vector (m entries).  scol: m doubles of per-warp scratch.  Returns Lu's sign in `sign` and in
+// `info` the first zero pivot (k+1), or 0.
+__device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double* scol, int& sign,
+                        int& info) {
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < m; i += 32) piv[i] = i;
+  sign = 1;
+  info = 0;
+  __syncwarp();
+  const int K = m < n ? m : n;
+  lu_finish_column(a, m, n, lda, 0, 0, scol, piv, sign, info);
+  for (int k = 0; k < K; ++k) {
+    const int k1 = k + 1;
+    const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
+    const int C = (k1 < K && k >= 1) ? m - k1 : 0;  // prefixes of column k1 (rows [k1, m))
+    const double* rowk = a + k;               // L(k, t) = rowk[t*lda]
+    const double* colk1 = a + (long long)k1 * lda;
+    for (int d = lane; d < R + C; d += 32) {
+      const bool isrow = d < R;
+      const int idx = isrow ? k1 + d : k1 + (d - R);
+      const double* x = isrow ? rowk : a + idx;
+      const double* y = isrow ? a + (long long)idx * lda : colk1;
+      const int len = isrow ? k : k - 1;
+      const double s = exact_dot(len, x, lda, y, 1);
+      if (isrow) {
+        double* dst = a + (long long)idx * lda + k;
+        *dst = __dsub_rn(*dst, s);
+      } else {
+        scol[idx] = s;
+      }
+    }
+    __syncwarp();
+    if (k1 < K) lu_finish_column(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
+  }
+  // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
+}
+
+// Solves A x = b for nr right-hand sides from the factors of one square matrix:
+// b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
+// upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
+__device__ void getrs_warp(const double* lu, int n, long long lda, const int* piv, double* b,
+                           long long ldb, int nrhs, double* xs, double* acc) {
+  const int lane = threadIdx.x & 31;
+  const int ldx = n | 1;
+  for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
+    const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
+    for (int e = lane; e < nr * n; e += 32) {
+      const int r = e / n;
+      const int i = e - r * n;
+      xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + piv[i]];
+    }
+    __syncwarp();
+    warp_solve_dot(lu, n, 1, lda, true, xs, ldx, acc, nr);
+    warp_solve_sweep(lu, n, lda, 1, xs, ldx, nr);
+    for (int e = lane; e < nr * n; e += 32) {
+      const int r = e / n;
+      const int i = e - r * n;
+      b[(long long)(r0 + r) * ldb + i] = xs[r * ldx + i];
+    }
+    __syncwarp();
+  }
+}
+
+constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) {
+  extern __shared__ double sm_dyn[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    double* a = p.a + p.a_off[mat];
+    int* piv = p.piv + p.piv_off[mat];
+    double* scr = (n <= SMEM_N) ? sm_dyn + warp * SMEM_WARP_DOUBLES
+                                 : p.gscratch + gw * p.gscratch_stride;
+    const int ldx = n | 1;
+    int sign, info;
+    lu_warp(a, n, n, lda, piv, scr, sign, info);
+    if (p.nrhs > 0)
+      getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
+                 scr + n + RHS_CHUNK * ldx);
+    if (lane == 0) {
+      p.sign[mat] = sign;
+      p.info[mat] = info;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(32) getrf_single_kernel(double* a, int m, int n, int lda,
+                                                          int* piv, int* out2, double* scratch) {
+  int sign, info;
+  lu_warp(a, m, n, lda, piv, scratch, sign, info);
+  if (threadIdx.x == 0) {
+    out2[0] = sign;
+    out2[1] = info;
+  }
+}
+
+template <int WARPS>
+static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
+  const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
+  getrf_batched_kernel<WARPS><<<ctas, WARPS * 32, smem, s>>>(args);
+  return cudaGetLastError();
+}
+
+template <int WARPS>
+static cudaError_t set_getrf_attr() {
+  const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
+  return cudaFuncSetAttribute(getrf_batched_kernel<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+// Raises the dynamic shared-memory limit of every variant; called once per device, outside any
+// stream capture.
+cudaError_t init_getrf_attributes() {
+  cudaError_t e;
+  if ((e = set_getrf_attr<1>()) != cudaSuccess) return e;
+  if ((e = set_getrf_attr<2>()) != cudaSuccess) return e;
+  if ((e = set_getrf_attr<4>()) != cudaSuccess) return e;
+  if ((e = set_getrf_attr<8>()) != cudaSuccess) return e;
+  return set_getrf_attr<16>();
+}
+
+cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  switch (warps) {
+    case 1: return launch_getrf_w<1>(args, ctas, s);
+    case 2: return launch_getrf_w<2>(args, ctas, s);
+    case 4: return launch_getrf_w<4>(args, ctas, s);
+    case 8: return launch_getrf_w<8>(args, ctas, s);
+    case 16: return launch_getrf_w<16>(args, ctas, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_getrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
+                                double* scratch, cudaStream_t s) {
+  getrf_single_kernel<<<1, 32, 0, s>>>(a, m, n, lda, piv, out2, scratch);
+  return cudaGetLastError();
+}
+
+}  // namespace mfg

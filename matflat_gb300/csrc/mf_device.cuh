@@ -1,0 +1,106 @@
+// Device-side building blocks shared by the factorization kernels.
+//
+// Numerical contract: MatFlat evaluates every product and every sum separately rounded and never
+// fuses a multiply-add (RyuJIT does not contract), so every floating-point operation here is an
+// explicit round-to-nearest intrinsic (__dmul_rn, __dadd_rn, __dsub_rn, __ddiv_rn, __dsqrt_rn).
+// Those intrinsics are never contracted by nvcc, whatever -fmad says.
+//
+// Hardware note (measured on GB300): FP64 DFMA/DMUL/DADD issue at ~1.66 lane-ops per clock per
+// SM, i.e. one warp-wide FP64 instruction every ~77 cycles per SM sub-partition, and inactive
+// lanes are not skipped.  Integer, shuffle, shared-memory and load instructions are nearly free
+// beside that, so the kernels are organised to keep the FP64 lanes busy, and compare and test
+// floating-point values with integer instructions wherever that is exact.
+#pragma once
+
+#include <cstdint>
+#include <climits>
+
+namespace mfg {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// Internals.Dot (MatFlat/Internals.cs:265-292): for an odd length the first product seeds the
+// sum, then every following pair is added as sum = sum + (x_a*y_a + x_b*y_b); an even length
+// starts from sum = 0.0.  x and y are strided.  Reproduced operation for operation.
+__device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
+                                            const double* y, long long incy) {
+  double s = 0.0;
+  if (len & 1) {
+    s = __dmul_rn(x[0], y[0]);
+    x += incx;
+    y += incy;
+  }
+  const int pairs = len >> 1;
+#pragma unroll 4
+  for (int p = 0; p < pairs; ++p) {
+    const double q = __dadd_rn(__dmul_rn(x[0], y[0]), __dmul_rn(x[incx], y[incy]));
+    s = __dadd_rn(s, q);
+    x += 2 * incx;
+    y += 2 * incy;
+  }
+  return s;
+}
+
+// Same tree, float data widened to double (Internals.cs:236-263).  Products of two widened
+// floats are exact in double.
+__device__ __forceinline__ double exact_dot_f(int len, const float* x, long long incx,
+                                              const float* y, long long incy) {
+  double s = 0.0;
+  if (len & 1) {
+    s = __dmul_rn((double)x[0], (double)y[0]);
+    x += incx;
+    y += incy;
+  }
+  const int pairs = len >> 1;
+#pragma unroll 4
+  for (int p = 0; p < pairs; ++p) {
+    const double q = __dadd_rn(__dmul_rn((double)x[0], (double)y[0]),
+                               __dmul_rn((double)x[incx], (double)y[incy]));
+    s = __dadd_rn(s, q);
+    x += 2 * incx;
+    y += 2 * incy;
+  }
+  return s;
+}
+
+__device__ __forceinline__ unsigned long long dbits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+
+// v != 0.0 (true for NaN), by integer test.
+__device__ __forceinline__ bool nonzero(double v) { return (dbits(v) << 1) != 0ull; }
+
+// v > 0.0 (false for NaN and for both zeros), by integer test.
+__device__ __forceinline__ bool positive(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > 0 && b <= 0x7FF0000000000000LL;
+}
+
+__device__ __forceinline__ bool is_nan(double v) {
+  return (dbits(v) & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+
+// Pivot key.  MatFlat's scan (Factorization.Lu.cs:323-330) keeps p = j and moves to i only when
+// |w_i| > |w_p|.  If w_j is NaN nothing ever beats it; otherwise the winner is the first index
+// attaining the largest |w| among the non-NaN entries.  The key orders |w| by its bit pattern
+// (monotone for non-NaN doubles) and maps NaN below every number; the caller handles a NaN w_j.
+__device__ __forceinline__ unsigned long long pivot_key(double v) {
+  const unsigned long long b = dbits(v) & 0x7FFFFFFFFFFFFFFFull;
+  return b > 0x7FF0000000000000ull ? 0ull : b + 1ull;
+}
+
+// Warp-wide argmax over (key, index): the largest key wins, ties go to the smaller index.
+__device__ __forceinline__ int warp_argmax(unsigned long long key, int idx) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(FULL_MASK, key, off);
+    const int oi = __shfl_xor_sync(FULL_MASK, idx, off);
+    if (ok > key || (ok == key && oi < idx)) {
+      key = ok;
+      idx = oi;
+    }
+  }
+  return idx;
+}
+
+}  // namespace mfg

@@ -1,0 +1,97 @@
+// Host-side declarations of the kernel launchers (implemented in the .cu files beside this one).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mfg {
+
+// Per-warp shared-memory budget of the batched warp kernels: matrices up to SMEM_N keep their
+// per-warp vectors in shared memory; larger ones use a slice of a global scratch buffer.
+constexpr int SMEM_N = 128;
+// Right-hand sides solved together per pass of the warp solvers.
+constexpr int RHS_CHUNK = 4;
+// Doubles of per-warp scratch needed for a matrix of order n (column sums, staged right-hand
+// sides and their accumulators).
+inline long long warp_scratch_doubles(int n) {
+  const long long ld = (long long)(n | 1);
+  return (long long)n + 2LL * RHS_CHUNK * ld + 2;
+}
+
+struct BatchArgs {
+  const int* order;          // execution order (longest first)
+  const int* n;              // order of each matrix
+  const int* lda;            // leading dimension of each matrix
+  const long long* a_off;    // element offset of each matrix
+  const long long* piv_off;  // element offset of each pivot vector (getrf)
+  const long long* b_off;    // element offset of each right-hand-side block
+  double* a;
+  int* piv;
+  double* b;
+  int* sign;
+  int* info;
+  int count;
+  int nrhs;
+  int* queue;                // work counter, zeroed before every launch
+  double* gscratch;          // per-warp scratch for n > SMEM_N
+  long long gscratch_stride; // doubles per warp in gscratch
+};
+
+// Batched Householder QR (+ least-squares solve of nrhs right-hand sides, ldb = m).
+template <typename T>
+struct QrBatchArgs {
+  const int* order;
+  const int* m;
+  const int* n;
+  const int* lda;
+  const long long* a_off;
+  const long long* rdiag_off;
+  const long long* b_off;
+  T* a;
+  T* rdiag;
+  T* b;
+  int count;
+  int nrhs;
+  int* queue;
+  T* gscratch;               // per-warp coefficient scratch when n + nrhs > 256
+  long long gscratch_stride;
+};
+
+template <typename T>
+cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s);
+// Single-matrix QR kernels; scratch: n + 1 elements.
+template <typename T>
+cudaError_t launch_qr_single(T* a, int m, int n, int lda, T* rdiag, T* scratch, cudaStream_t s);
+template <typename T>
+cudaError_t launch_qr_q_single(const T* a, int m, int n, int lda, T* q, int ldq, T* scratch,
+                               cudaStream_t s);
+template <typename T>
+cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const T* rdiag,
+                               cudaStream_t s);
+
+// One-time per-device set-up of kernel attributes (dynamic shared-memory limits).
+cudaError_t init_getrf_attributes();
+cudaError_t init_potrf_attributes();
+
+// Batched LU (+ solve); launched persistent: grid = ctas, WARPS warps per CTA.
+cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+// Batched Cholesky (+ two triangular solves).
+cudaError_t launch_potrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+
+// Single-matrix kernels (device pointers).  scratch: at least warp_scratch_doubles(max(m,n))
+// doubles of device memory.  out2[0] = sign (getrf) / info (potrf); out2[1] = info (getrf).
+cudaError_t launch_getrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
+                                double* scratch, cudaStream_t s);
+cudaError_t launch_potrf_single(double* a, int n, int lda, int* out1, double* scratch,
+                                cudaStream_t s);
+cudaError_t launch_trsv_single(int uplo, int trans, int n, const double* a, int lda, double* x,
+                               int incx, double* scratch, cudaStream_t s);
+cudaError_t launch_gemm_single(int transa, int transb, int m, int n, int k, const double* a,
+                               int lda, const double* b, int ldb, double* c, int ldc,
+                               cudaStream_t s);
+// LuInverse after the zero-diagonal check: a holds the LU factors on entry and A^-1 on exit;
+// work: n*n doubles.  scratch: warps * 2 * RHS_CHUNK * (n|1) doubles.
+cudaError_t launch_getri_single(double* a, int n, int lda, const int* piv, double* work,
+                                double* scratch, int warps, cudaStream_t s);
+
+}  // namespace mfg

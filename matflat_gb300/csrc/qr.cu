@@ -1,0 +1,279 @@
+// Householder QR in MatFlat's arithmetic and Mapack storage format:
+//   Factorization.Qr                     (MatFlat/Factorization.Qr.cs:115-172 double, :32-89 float)
+//   Factorization.QrOrthogonalFactor     (:357-413 double, :278-334 float)
+//   Factorization.QrUpperTriangularFactor (:597-650 double, :518-571 float)
+// and the batched least-squares solver built from them.
+//
+// For every column k MatFlat computes norm = sqrt(pairwise sum of squares) (Internals.Norm), and,
+// if norm != 0, divides the column by it, adds 1 to the diagonal entry (no reflector sign choice)
+// and updates every later column j with s = -Dot(v, a_j) / v[0]; a_j += s * v.  rdiag[k] = -norm.
+// The float overload keeps float storage but sums its dots and norms in double.  Each column's
+// dot is independent of the others, so one warp runs the column dots of a step across its lanes,
+// then the rank-1 update across (row, column) pairs; every value is computed with MatFlat's own
+// operations in MatFlat's order.
+//
+// Least squares: MatFlat has no QR solve.  The batched solver treats each right-hand side b as
+// one more trailing column, so Q^T b is produced by the very same reflector updates, and then
+// solves R x = (Q^T b)[0:n] with MatFlat's Upper/NoTrans column sweep (R = strict upper part of
+// a, diagonal rdiag).  On exit b[0:n] = x and b[n:m] holds the residual components.
+#include <cuda_runtime.h>
+
+#include "mf_device.cuh"
+#include "mf_kernels.h"
+
+namespace mfg {
+
+template <typename T>
+struct QrArith;
+
+template <>
+struct QrArith<double> {
+  // Internals.Norm (Internals.cs:435-460): the Dot tree over x*x, then Math.Sqrt.
+  static __device__ __forceinline__ double norm(int len, const double* x) {
+    return __dsqrt_rn(exact_dot(len, x, 1, x, 1));
+  }
+  static __device__ __forceinline__ double dot(int len, const double* x, const double* y) {
+    return exact_dot(len, x, 1, y, 1);
+  }
+  static __device__ __forceinline__ double div(double x, double y) { return __ddiv_rn(x, y); }
+  static __device__ __forceinline__ double add1(double x) { return __dadd_rn(x, 1.0); }
+  // s = -Dot(...) / colk[k]   (Qr.cs:163, :408)
+  static __device__ __forceinline__ double coef(double d, double v0) { return __ddiv_rn(-d, v0); }
+  // MulAdd: dst += x * s      (Internals.cs:49-73)
+  static __device__ __forceinline__ double muladd(double dst, double x, double s) {
+    return __dadd_rn(dst, __dmul_rn(x, s));
+  }
+  static __device__ __forceinline__ double mulsub(double dst, double x, double s) {
+    return __dsub_rn(dst, __dmul_rn(x, s));
+  }
+  static __device__ __forceinline__ bool nz(double v) { return nonzero(v); }
+};
+
+template <>
+struct QrArith<float> {
+  // (float)Internals.Norm(float*) (Qr.cs:68): double sum of widened squares, sqrt, to float.
+  static __device__ __forceinline__ float norm(int len, const float* x) {
+    return __double2float_rn(__dsqrt_rn(exact_dot_f(len, x, 1, x, 1)));
+  }
+  static __device__ __forceinline__ double dot(int len, const float* x, const float* y) {
+    return exact_dot_f(len, x, 1, y, 1);
+  }
+  static __device__ __forceinline__ float div(float x, float y) { return __fdiv_rn(x, y); }
+  static __device__ __forceinline__ float add1(float x) { return __fadd_rn(x, 1.0f); }
+  // s = -(float)(Dot(...) / colk[k])   (Qr.cs:80, :329)
+  static __device__ __forceinline__ float coef(double d, float v0) {
+    return -__double2float_rn(__ddiv_rn(d, (double)v0));
+  }
+  static __device__ __forceinline__ float muladd(float dst, float x, float s) {
+    return __fadd_rn(dst, __fmul_rn(x, s));
+  }
+  static __device__ __forceinline__ float mulsub(float dst, float x, float s) {
+    return __fsub_rn(dst, __fmul_rn(x, s));
+  }
+  static __device__ __forceinline__ bool nz(float v) { return (__float_as_uint(v) << 1) != 0u; }
+};
+
+// Column j of the factored matrix, or right-hand side j - n when j >= n.
+template <typename T>
+__device__ __forceinline__ T* qr_col(T* a, long long lda, int n, T* b, long long ldb, int j) {
+  return j < n ? a + (long long)j * lda : b + (long long)(j - n) * ldb;
+}
+
+// Factors the m-by-n matrix a (m >= n) in place, applying every reflector also to the nb columns
+// of b (leading dimension ldb).  coefs: n - 1 + nb values of per-warp scratch.
+template <typename T>
+__device__ void qr_warp(T* a, int m, int n, long long lda, T* rdiag, T* b, long long ldb, int nb,
+                        T* coefs) {
+  using A = QrArith<T>;
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < n; ++k) {
+    T* ck = a + (long long)k * lda;
+    const int len = m - k;
+    const T norm = A::norm(len, ck + k);  // every lane, same value
+    if (A::nz(norm)) {
+      for (int r = k + lane; r < m; r += 32) ck[r] = A::div(ck[r], norm);
+      __syncwarp();
+      if (lane == 0) ck[k] = A::add1(ck[k]);
+      __syncwarp();
+      const T v0 = ck[k];
+      const int ncols = (n - k - 1) + nb;
+      for (int c = lane; c < ncols; c += 32) {
+        const T* cj = qr_col(a, lda, n, b, ldb, k + 1 + c);
+        coefs[c] = A::coef(A::dot(len, ck + k, cj + k), v0);
+      }
+      __syncwarp();
+      const long long work = (long long)len * ncols;
+      for (long long e = lane; e < work; e += 32) {
+        const int c = (int)(e / len);
+        const int r = k + (int)(e - (long long)c * len);
+        T* cj = qr_col(a, lda, n, b, ldb, k + 1 + c);
+        cj[r] = A::muladd(cj[r], ck[r], coefs[c]);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) rdiag[k] = -norm;
+    __syncwarp();
+  }
+}
+
+// R x = y for the first n entries of every right-hand side (Blas.SolveTriangular Upper/NoTrans,
+// MatFlat/Blas.SolveTriangular.cs:191-199, against QrUpperTriangularFactor's R).
+template <typename T>
+__device__ void qr_rsolve_warp(const T* a, int n, long long lda, const T* rdiag, T* b,
+                               long long ldb, int nb) {
+  using A = QrArith<T>;
+  const int lane = threadIdx.x & 31;
+  for (int i = n - 1; i >= 0; --i) {
+    for (int c = lane; c < nb; c += 32) {
+      T* x = b + (long long)c * ldb;
+      x[i] = A::div(x[i], rdiag[i]);
+    }
+    __syncwarp();
+    const T* ai = a + (long long)i * lda;
+    for (int e = lane; e < nb * i; e += 32) {
+      const int c = e / i;
+      const int r = e - c * i;
+      T* x = b + (long long)c * ldb;
+      x[r] = A::mulsub(x[r], ai[r], x[i]);
+    }
+    __syncwarp();
+  }
+}
+
+// QrOrthogonalFactor: thin Q by backward accumulation of the reflectors.
+template <typename T>
+__device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long long ldq, T* coefs) {
+  using A = QrArith<T>;
+  const int lane = threadIdx.x & 31;
+  for (int k = n - 1; k >= 0; --k) {
+    T* qk = q + (long long)k * ldq;
+    const T* ak = a + (long long)k * lda;
+    for (int r = lane; r < m; r += 32) qk[r] = (T)0;
+    __syncwarp();
+    if (lane == 0) qk[k] = (T)1;
+    __syncwarp();
+    const T v0 = ak[k];
+    if (A::nz(v0)) {
+      const int len = m - k;
+      const int ncols = n - k;
+      for (int c = lane; c < ncols; c += 32) {
+        const T* qj = q + (long long)(k + c) * ldq;
+        coefs[c] = A::coef(A::dot(len, ak + k, qj + k), v0);
+      }
+      __syncwarp();
+      const long long work = (long long)len * ncols;
+      for (long long e = lane; e < work; e += 32) {
+        const int c = (int)(e / len);
+        const int r = k + (int)(e - (long long)c * len);
+        T* qj = q + (long long)(k + c) * ldq;
+        qj[r] = A::muladd(qj[r], ak[r], coefs[c]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+constexpr int QR_SMEM_COEFS = 256;
+
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) qr_batched_kernel(QrBatchArgs<T> p) {
+  __shared__ T sm[WARPS][QR_SMEM_COEFS];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int m = p.m[mat];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    T* a = p.a + p.a_off[mat];
+    T* rd = p.rdiag + p.rdiag_off[mat];
+    T* b = p.nrhs > 0 ? p.b + p.b_off[mat] : nullptr;
+    T* coefs = (n + p.nrhs <= QR_SMEM_COEFS) ? &sm[warp][0] : p.gscratch + gw * p.gscratch_stride;
+    qr_warp<T>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+    if (p.nrhs > 0) qr_rsolve_warp<T>(a, n, lda, rd, b, m, p.nrhs);
+    __syncwarp();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) qr_single_kernel(T* a, int m, int n, int lda, T* rdiag,
+                                                       T* scratch) {
+  qr_warp<T>(a, m, n, lda, rdiag, (T*)nullptr, 0, 0, scratch);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) qr_q_single_kernel(const T* a, int m, int n, int lda, T* q,
+                                                         int ldq, T* scratch) {
+  qr_q_warp<T>(a, m, n, lda, q, ldq, scratch);
+}
+
+// QrUpperTriangularFactor: R(0:i, i) = a(0:i, i); R(i,i) = rdiag[i]; R(i+1:n, i) = 0.
+template <typename T>
+__global__ void qr_r_single_kernel(const T* a, int n, int lda, T* r, int ldr, const T* rdiag) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  const int i = (int)(e / n);   // column
+  const int row = (int)(e - (long long)i * n);
+  T v;
+  if (row < i) v = a[(long long)i * lda + row];
+  else if (row == i) v = rdiag[i];
+  else v = (T)0;
+  r[(long long)i * ldr + row] = v;
+}
+
+template <typename T>
+cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s) {
+  switch (warps) {
+    case 1: qr_batched_kernel<T, 1><<<ctas, 32, 0, s>>>(args); break;
+    case 2: qr_batched_kernel<T, 2><<<ctas, 64, 0, s>>>(args); break;
+    case 4: qr_batched_kernel<T, 4><<<ctas, 128, 0, s>>>(args); break;
+    case 8: qr_batched_kernel<T, 8><<<ctas, 256, 0, s>>>(args); break;
+    case 16: qr_batched_kernel<T, 16><<<ctas, 512, 0, s>>>(args); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_qr_single(T* a, int m, int n, int lda, T* rdiag, T* scratch, cudaStream_t s) {
+  qr_single_kernel<T><<<1, 32, 0, s>>>(a, m, n, lda, rdiag, scratch);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_qr_q_single(const T* a, int m, int n, int lda, T* q, int ldq, T* scratch,
+                               cudaStream_t s) {
+  qr_q_single_kernel<T><<<1, 32, 0, s>>>(a, m, n, lda, q, ldq, scratch);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const T* rdiag,
+                               cudaStream_t s) {
+  const long long total = (long long)n * n;
+  const int threads = 128;
+  qr_r_single_kernel<T><<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
+      a, n, lda, r, ldr, rdiag);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_qr_batched<double>(const QrBatchArgs<double>&, int, int, cudaStream_t);
+template cudaError_t launch_qr_batched<float>(const QrBatchArgs<float>&, int, int, cudaStream_t);
+template cudaError_t launch_qr_single<double>(double*, int, int, int, double*, double*,
+                                              cudaStream_t);
+template cudaError_t launch_qr_single<float>(float*, int, int, int, float*, float*, cudaStream_t);
+template cudaError_t launch_qr_q_single<double>(const double*, int, int, int, double*, int,
+                                                double*, cudaStream_t);
+template cudaError_t launch_qr_q_single<float>(const float*, int, int, int, float*, int, float*,
+                                               cudaStream_t);
+template cudaError_t launch_qr_r_single<double>(const double*, int, int, double*, int,
+                                                const double*, cudaStream_t);
+template cudaError_t launch_qr_r_single<float>(const float*, int, int, float*, int, const float*,
+                                               cudaStream_t);
+
+}  // namespace mfg

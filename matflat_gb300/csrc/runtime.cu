@@ -1,0 +1,913 @@
+// Host runtime and C ABI (include/matflat_gpu.h): contexts, device workspace, batch plans with
+// longest-first ordering, launch-shape selection and CUDA-graph replay.
+//
+// Argument validation mirrors MatFlat's checks, in MatFlat's order, and reports the 1-based
+// position of the offending argument as a negative status (the context is argument 1).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/matflat_gpu.h"
+#include "mf_kernels.h"
+
+using mfg::BatchArgs;
+
+namespace {
+
+constexpr const char* kVersion = "0.1.0";
+
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+};
+
+int env_int(const char* name, int dflt) {
+  const char* v = std::getenv(name);
+  if (!v || !*v) return dflt;
+  return std::atoi(v);
+}
+
+std::once_flag g_attr_once[64];
+cudaError_t g_attr_err[64];
+
+}  // namespace
+
+struct mfg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  DevBuf work;
+  std::string last_error;
+  bool use_graphs = true;
+};
+
+struct mfg_plan {
+  enum Kind { GETRF, POTRF, GEQRF } kind;
+  mfg_ctx* ctx = nullptr;
+  int count = 0;
+  int nrhs = 0;
+  int max_n = 0;
+  DevBuf meta;      // order | n | lda | a_off | piv_off | b_off | queue
+  DevBuf scratch;   // per-warp scratch for n > SMEM_N
+  BatchArgs args{};
+  mfg::QrBatchArgs<double> qd{};
+  mfg::QrBatchArgs<float> qs{};
+  int qr_float = 0;  // GEQRF: which precision the next launch runs
+  int ctas = 0;
+  int warps = 0;
+  // CUDA graph of the last execution (keyed by the data pointers and the stream).
+  cudaGraphExec_t exec = nullptr;
+  const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+int fail(mfg_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->last_error = buf;
+  }
+  return code;
+}
+
+int cuda_fail(mfg_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, MFG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define MFG_CUDA(ctx, call)                                  \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+cudaError_t init_device_attributes(int device) {
+  const int slot = device & 63;
+  std::call_once(g_attr_once[slot], [slot]() {
+    cudaError_t e = mfg::init_getrf_attributes();
+    if (e == cudaSuccess) e = mfg::init_potrf_attributes();
+    g_attr_err[slot] = e;
+  });
+  return g_attr_err[slot];
+}
+
+// Elements spanned by an m-by-n column-major matrix with leading dimension ld.
+size_t span(long long m, long long n, long long ld) {
+  if (m <= 0 || n <= 0) return 0;
+  return (size_t)(ld * (n - 1) + m);
+}
+
+// Launch shape of a batched plan: WARPS warps per CTA and enough CTAs to hold `warps_per_sm`
+// warps on every SM (persistent: each warp pulls matrices from the queue until it is empty).
+void choose_shape(mfg_plan* p) {
+  const int warps = env_int("MFG_WARPS_PER_CTA", 4);
+  const int wps = env_int("MFG_WARPS_PER_SM", 16);
+  p->warps = warps;
+  const long long total_warps = (long long)p->ctx->sm_count * wps;
+  long long ctas = total_warps / warps;
+  // Never more warps than matrices.
+  const long long need = ((long long)p->count + warps - 1) / warps;
+  if (ctas > need) ctas = need;
+  if (ctas < 1) ctas = 1;
+  p->ctas = (int)ctas;
+}
+
+int plan_launch(mfg_plan* p, cudaStream_t s) {
+  mfg_ctx* ctx = p->ctx;
+  int* queue = p->kind == mfg_plan::GEQRF ? p->qd.queue : p->args.queue;
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
+  if (p->count == 0) return MFG_OK;
+  if (p->kind == mfg_plan::GETRF)
+    e = mfg::launch_getrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::POTRF)
+    e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->qr_float)
+    e = mfg::launch_qr_batched<float>(p->qs, p->ctas, p->warps, s);
+  else
+    e = mfg::launch_qr_batched<double>(p->qd, p->ctas, p->warps, s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
+  return MFG_OK;
+}
+
+// Replays the plan's CUDA graph, capturing it first when the data pointers or the stream changed.
+// The legacy default stream cannot be captured; on it the plan launches directly.
+int plan_execute(mfg_plan* p, const void* k0, const void* k1, const void* k2, const void* k3,
+                 const void* k4) {
+  mfg_ctx* ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  if (!ctx->use_graphs || s == nullptr || s == cudaStreamLegacy) return plan_launch(p, s);
+  const void* key[6] = {k0, k1, k2, k3, k4, (const void*)s};
+  bool hit = p->exec != nullptr;
+  for (int i = 0; i < 6 && hit; i++) hit = (key[i] == p->key[i]);
+  if (!hit) {
+    if (p->exec) {
+      cudaGraphExecDestroy(p->exec);
+      p->exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    MFG_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = plan_launch(p, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &g);
+    if (rc != MFG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ee != cudaSuccess) return cuda_fail(ctx, ee, "cudaStreamEndCapture");
+    ee = cudaGraphInstantiate(&p->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ee != cudaSuccess) {
+      p->exec = nullptr;
+      return cuda_fail(ctx, ee, "cudaGraphInstantiate");
+    }
+    for (int i = 0; i < 6; i++) p->key[i] = key[i];
+  }
+  MFG_CUDA(ctx, cudaGraphLaunch(p->exec, s));
+  return MFG_OK;
+}
+
+// Common plan set-up: validation, longest-first order, descriptor upload, scratch.
+int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, const int* n,
+                const int* lda, const int64_t* a_off, const int64_t* piv_off, int nrhs,
+                const int64_t* b_off) {
+  if (!ctx) return -1;
+  if (!out) return fail(ctx, -2, "plan output pointer is null");
+  *out = nullptr;
+  if (count < 0) return fail(ctx, -3, "count must be >= 0");
+  if (count > 0 && !n) return fail(ctx, -4, "n is null");
+  for (int i = 0; i < count; i++)
+    if (n[i] < 1)
+      return fail(ctx, -4, "n[%d] = %d: the order of the matrix must be >= 1", i, n[i]);
+  if (lda)
+    for (int i = 0; i < count; i++)
+      if (lda[i] < n[i])
+        return fail(ctx, -5, "lda[%d] = %d < n[%d] = %d", i, lda[i], i, n[i]);
+  if (count > 0 && !a_off) return fail(ctx, -6, "a_off is null");
+  for (int i = 0; i < count; i++)
+    if (a_off[i] < 0) return fail(ctx, -6, "a_off[%d] < 0", i);
+  int argi = 7;
+  if (kind == mfg_plan::GETRF) {
+    if (count > 0 && !piv_off) return fail(ctx, -7, "piv_off is null");
+    for (int i = 0; i < count; i++)
+      if (piv_off[i] < 0) return fail(ctx, -7, "piv_off[%d] < 0", i);
+    argi = 8;
+  }
+  if (nrhs < 0) return fail(ctx, -argi, "nrhs must be >= 0");
+  if (nrhs > 0 && count > 0 && !b_off) return fail(ctx, -(argi + 1), "b_off is null");
+  if (nrhs > 0)
+    for (int i = 0; i < count; i++)
+      if (b_off[i] < 0) return fail(ctx, -(argi + 1), "b_off[%d] < 0", i);
+
+  mfg_plan* p = new mfg_plan();
+  p->kind = kind;
+  p->ctx = ctx;
+  p->count = count;
+  p->nrhs = nrhs;
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  // Longest first (work grows as n^3): the persistent warps then finish close together.
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  int max_n = 0;
+  for (int i = 0; i < count; i++) max_n = std::max(max_n, n[i]);
+  p->max_n = max_n;
+
+  const size_t ints = (size_t)count;
+  const size_t bytes_i = ((ints * sizeof(int) + 255) / 256) * 256;
+  const size_t bytes_l = ((ints * sizeof(long long) + 255) / 256) * 256;
+  const size_t total = 3 * bytes_i + 3 * bytes_l + 256;
+  cudaError_t e = p->meta.reserve(total);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMalloc(plan descriptors)");
+  }
+  char* base = (char*)p->meta.ptr;
+  int* d_order = (int*)base;
+  int* d_n = (int*)(base + bytes_i);
+  int* d_lda = (int*)(base + 2 * bytes_i);
+  long long* d_aoff = (long long*)(base + 3 * bytes_i);
+  long long* d_pivoff = (long long*)(base + 3 * bytes_i + bytes_l);
+  long long* d_boff = (long long*)(base + 3 * bytes_i + 2 * bytes_l);
+  int* d_queue = (int*)(base + 3 * bytes_i + 3 * bytes_l);
+
+  std::vector<char> host(total, 0);
+  std::memcpy(host.data(), order.data(), ints * sizeof(int));
+  std::memcpy(host.data() + bytes_i, n, ints * sizeof(int));
+  if (lda)
+    std::memcpy(host.data() + 2 * bytes_i, lda, ints * sizeof(int));
+  else
+    std::memcpy(host.data() + 2 * bytes_i, n, ints * sizeof(int));
+  for (size_t i = 0; i < ints; i++) {
+    ((long long*)(host.data() + 3 * bytes_i))[i] = a_off[i];
+    ((long long*)(host.data() + 3 * bytes_i + bytes_l))[i] =
+        (kind == mfg_plan::GETRF) ? piv_off[i] : 0;
+    ((long long*)(host.data() + 3 * bytes_i + 2 * bytes_l))[i] = nrhs > 0 ? b_off[i] : 0;
+  }
+  e = cudaMemcpy(p->meta.ptr, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
+  }
+  choose_shape(p);
+  long long stride = 0;
+  if (max_n > mfg::SMEM_N) {
+    stride = (mfg::warp_scratch_doubles(max_n) + 31) / 32 * 32;
+    const size_t sbytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps;
+    e = p->scratch.reserve(sbytes);
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_fail(ctx, e, "cudaMalloc(plan scratch)");
+    }
+  }
+  BatchArgs& a = p->args;
+  a.order = d_order;
+  a.n = d_n;
+  a.lda = d_lda;
+  a.a_off = d_aoff;
+  a.piv_off = d_pivoff;
+  a.b_off = d_boff;
+  a.count = count;
+  a.nrhs = nrhs;
+  a.queue = d_queue;
+  a.gscratch = (double*)p->scratch.ptr;
+  a.gscratch_stride = stride;
+  *out = p;
+  return MFG_OK;
+}
+
+
+int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const int* n,
+                   const int* lda, const int64_t* a_off, const int64_t* rdiag_off, int nrhs,
+                   const int64_t* b_off) {
+  if (!ctx) return -1;
+  if (!out) return fail(ctx, -2, "plan output pointer is null");
+  *out = nullptr;
+  if (count < 0) return fail(ctx, -3, "count must be >= 0");
+  if (count > 0 && (!m || !n)) return fail(ctx, !m ? -4 : -5, "m or n is null");
+  for (int i = 0; i < count; i++) {
+    if (m[i] < 1) return fail(ctx, -4, "m[%d] = %d: must be >= 1", i, m[i]);
+    if (n[i] < 1) return fail(ctx, -5, "n[%d] = %d: must be >= 1", i, n[i]);
+    if (n[i] > m[i])
+      return fail(ctx, -5,
+                  "The number of rows must be greater than or equal to the number of columns.");
+  }
+  if (lda)
+    for (int i = 0; i < count; i++)
+      if (lda[i] < m[i]) return fail(ctx, -6, "lda[%d] = %d < m[%d] = %d", i, lda[i], i, m[i]);
+  if (count > 0 && !a_off) return fail(ctx, -7, "a_off is null");
+  if (count > 0 && !rdiag_off) return fail(ctx, -8, "rdiag_off is null");
+  if (nrhs < 0) return fail(ctx, -9, "nrhs must be >= 0");
+  if (nrhs > 0 && count > 0 && !b_off) return fail(ctx, -10, "b_off is null");
+  for (int i = 0; i < count; i++) {
+    if (a_off[i] < 0) return fail(ctx, -7, "a_off[%d] < 0", i);
+    if (rdiag_off[i] < 0) return fail(ctx, -8, "rdiag_off[%d] < 0", i);
+    if (nrhs > 0 && b_off[i] < 0) return fail(ctx, -10, "b_off[%d] < 0", i);
+  }
+  mfg_plan* p = new mfg_plan();
+  p->kind = mfg_plan::GEQRF;
+  p->ctx = ctx;
+  p->count = count;
+  p->nrhs = nrhs;
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<double> work(count);
+  int max_cols = 0;
+  for (int i = 0; i < count; i++) {
+    work[i] = 2.0 * m[i] * (double)n[i] * n[i] - 2.0 / 3.0 * (double)n[i] * n[i] * n[i];
+    max_cols = std::max(max_cols, n[i] + nrhs);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  const size_t ints = (size_t)count;
+  const size_t bi = ((ints * sizeof(int) + 255) / 256) * 256;
+  const size_t bl = ((ints * sizeof(long long) + 255) / 256) * 256;
+  const size_t total = 4 * bi + 3 * bl + 256;
+  cudaError_t e = p->meta.reserve(total);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMalloc(plan descriptors)");
+  }
+  std::vector<char> host(total, 0);
+  std::memcpy(host.data(), order.data(), ints * sizeof(int));
+  std::memcpy(host.data() + bi, m, ints * sizeof(int));
+  std::memcpy(host.data() + 2 * bi, n, ints * sizeof(int));
+  std::memcpy(host.data() + 3 * bi, lda ? lda : m, ints * sizeof(int));
+  for (size_t i = 0; i < ints; i++) {
+    ((long long*)(host.data() + 4 * bi))[i] = a_off[i];
+    ((long long*)(host.data() + 4 * bi + bl))[i] = rdiag_off[i];
+    ((long long*)(host.data() + 4 * bi + 2 * bl))[i] = nrhs > 0 ? b_off[i] : 0;
+  }
+  e = cudaMemcpy(p->meta.ptr, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
+  }
+  choose_shape(p);
+  long long stride = 0;
+  if (max_cols > 256) {
+    stride = (max_cols + 31) / 32 * 32;
+    e = p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps);
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_fail(ctx, e, "cudaMalloc(plan scratch)");
+    }
+  }
+  char* base = (char*)p->meta.ptr;
+  auto fill = [&](auto& q) {
+    q.order = (const int*)base;
+    q.m = (const int*)(base + bi);
+    q.n = (const int*)(base + 2 * bi);
+    q.lda = (const int*)(base + 3 * bi);
+    q.a_off = (const long long*)(base + 4 * bi);
+    q.rdiag_off = (const long long*)(base + 4 * bi + bl);
+    q.b_off = (const long long*)(base + 4 * bi + 2 * bl);
+    q.count = count;
+    q.nrhs = nrhs;
+    q.queue = (int*)(base + 4 * bi + 3 * bl);
+    q.gscratch_stride = stride;
+  };
+  fill(p->qd);
+  fill(p->qs);
+  p->qd.gscratch = (double*)p->scratch.ptr;
+  p->qs.gscratch = (float*)p->scratch.ptr;
+  *out = p;
+  return MFG_OK;
+}
+
+// Single-matrix staging: device workspace carve-up helper.
+struct Carve {
+  char* base;
+  size_t off = 0;
+  explicit Carve(void* b) : base((char*)b) {}
+  template <typename T>
+  T* take(size_t count) {
+    T* r = (T*)(base + off);
+    off += ((count * sizeof(T) + 255) / 256) * 256;
+    return r;
+  }
+  static size_t bytes_for(size_t count, size_t elem) { return ((count * elem + 255) / 256) * 256; }
+};
+
+}  // namespace
+
+extern "C" {
+
+MFG_API const char* mfg_version(void) { return kVersion; }
+
+MFG_API int mfg_create(mfg_ctx** ctx) {
+  if (!ctx) return -1;
+  *ctx = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return MFG_ERR_NO_DEVICE;
+  mfg_ctx* c = new mfg_ctx();
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return MFG_ERR_NO_DEVICE;
+  }
+  c->stream = c->own_stream;
+  c->use_graphs = env_int("MFG_GRAPHS", 1) != 0;
+  e = init_device_attributes(c->device);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    return MFG_ERR_NO_DEVICE;
+  }
+  *ctx = c;
+  return MFG_OK;
+}
+
+MFG_API int mfg_destroy(mfg_ctx* ctx) {
+  if (!ctx) return -1;
+  cudaStreamSynchronize(ctx->stream);
+  ctx->work.release();
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return MFG_OK;
+}
+
+MFG_API int mfg_set_stream(mfg_ctx* ctx, void* stream) {
+  if (!ctx) return -1;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return MFG_OK;
+}
+
+MFG_API int mfg_synchronize(mfg_ctx* ctx) {
+  if (!ctx) return -1;
+  MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MFG_OK;
+}
+
+MFG_API const char* mfg_last_error(mfg_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+// ------------------------------------------------------------------------------------------
+// Single-matrix drop-ins.
+
+MFG_API int mfg_dgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign) {
+  if (!ctx) return -1;
+  // Factorization.Lu argument checks (Factorization.Lu.cs:124-147).
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!piv) return fail(ctx, -6, "piv is null");
+  const int big = std::max(m, n);
+  const size_t na = span(m, n, lda);
+  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(mfg::warp_scratch_doubles(big), 8) +
+                      Carve::bytes_for(m, 4) + Carve::bytes_for(2, 4);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(na);
+  double* d_s = cv.take<double>(mfg::warp_scratch_doubles(big));
+  int* d_piv = cv.take<int>(m);
+  int* d_out = cv.take<int>(2);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)m * 8, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_getrf_single(d_a, m, n, lda, d_piv, d_out, d_s, s));
+  int out[2];
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)m * 8, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  if (sign) *sign = out[0];
+  return MFG_OK;
+}
+
+MFG_API int mfg_dpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
+  if (!ctx) return -1;
+  // Factorization.Cholesky argument checks (Factorization.Cholesky.cs:116-129).
+  if (n <= 0) return fail(ctx, -2, "The order of the matrix must be greater than or equal to one.");
+  if (!a) return fail(ctx, -3, "a is null");
+  if (lda < n)
+    return fail(ctx, -4,
+                "The leading dimension must be greater than or equal to the order of the matrix.");
+  const size_t na = span(n, n, lda);
+  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(mfg::warp_scratch_doubles(n), 8) +
+                      Carve::bytes_for(1, 4);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(na);
+  double* d_s = cv.take<double>(mfg::warp_scratch_doubles(n));
+  int* d_out = cv.take<int>(1);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_potrf_single(d_a, n, lda, d_out, d_s, s));
+  int out = 0;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)n * 8, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  if (info) *info = out;
+  return MFG_OK;
+}
+
+MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
+                      double* x, int incx) {
+  if (!ctx) return -1;
+  // Blas.SolveTriangular argument checks (Blas.SolveTriangular.cs:164-187, enums :189-241).
+  if (n <= 0) return fail(ctx, -4, "The order of the matrix must be greater than or equal to one.");
+  if (!a) return fail(ctx, -5, "a is null");
+  if (lda < n)
+    return fail(ctx, -6,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!x) return fail(ctx, -7, "x is null");
+  if (incx <= 0) return fail(ctx, -8, "The value must be greater than or equal to one.");
+  if (uplo != MFG_UPPER && uplo != MFG_LOWER) return fail(ctx, -2, "Invalid enum value.");
+  if (trans != MFG_NOTRANS && trans != MFG_TRANS) return fail(ctx, -3, "Invalid enum value.");
+  const size_t na = span(n, n, lda);
+  const size_t nx = (size_t)(n - 1) * incx + 1;
+  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(nx, 8) +
+                      Carve::bytes_for(2 * (size_t)(n | 1), 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(na);
+  double* d_x = cv.take<double>(nx);
+  double* d_s = cv.take<double>(2 * (size_t)(n | 1));
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * 8, cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_trsv_single(uplo, trans, n, d_a, lda, d_x, incx, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * 8, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
+                      int lda, const double* b, int ldb, double* c, int ldc) {
+  if (!ctx) return -1;
+  // Blas.MulMatMat argument checks (Blas.MulMatMat.cs:228-304).
+  if (m <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -5, "The value must be greater than or equal to one.");
+  if (k <= 0) return fail(ctx, -6, "The value must be greater than or equal to one.");
+  if (!a) return fail(ctx, -7, "a is null");
+  if (transa == MFG_NOTRANS) {
+    if (lda < m)
+      return fail(ctx, -8,
+                  "The leading dimension must be greater than or equal to the number of rows.");
+  } else if (transa == MFG_TRANS) {
+    if (lda < k)
+      return fail(ctx, -8,
+                  "The leading dimension must be greater than or equal to the number of rows.");
+  } else {
+    return fail(ctx, -2, "Invalid enum value.");
+  }
+  if (!b) return fail(ctx, -9, "b is null");
+  if (transb == MFG_NOTRANS) {
+    if (ldb < k)
+      return fail(ctx, -10,
+                  "The leading dimension must be greater than or equal to the number of rows.");
+  } else if (transb == MFG_TRANS) {
+    if (ldb < n)
+      return fail(ctx, -10,
+                  "The leading dimension must be greater than or equal to the number of rows.");
+  } else {
+    return fail(ctx, -3, "Invalid enum value.");
+  }
+  if (!c) return fail(ctx, -11, "c is null");
+  if (ldc < m)
+    return fail(ctx, -12,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if ((const double*)c == a || (const double*)c == b)
+    return fail(ctx, MFG_ERR_INPLACE, "In-place operation is not supported.");
+  const int ar = transa == MFG_NOTRANS ? m : k, ac = transa == MFG_NOTRANS ? k : m;
+  const int br = transb == MFG_NOTRANS ? k : n, bc = transb == MFG_NOTRANS ? n : k;
+  const size_t na = span(ar, ac, lda), nb = span(br, bc, ldb), nc = span(m, n, ldc);
+  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(nb, 8) + Carve::bytes_for(nc, 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(na);
+  double* d_b = cv.take<double>(nb);
+  double* d_c = cv.take<double>(nc);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)ar * 8, ac,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_b, (size_t)ldb * 8, b, (size_t)ldb * 8, (size_t)br * 8, bc,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_gemm_single(transa, transb, m, n, k, d_a, lda, d_b, ldb, d_c, ldc, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(c, (size_t)ldc * 8, d_c, (size_t)ldc * 8, (size_t)m * 8, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+  if (!ctx) return -1;
+  // Factorization.LuInverse argument checks (Factorization.LuInverse.cs:125-143).
+  if (n <= 0) return fail(ctx, -2, "The order of the matrix must be greater than or equal to one.");
+  if (!a) return fail(ctx, -3, "a is null");
+  if (lda < n)
+    return fail(ctx, -4,
+                "The leading dimension must be greater than or equal to the order of the matrix.");
+  if (!piv) return fail(ctx, -5, "piv is null");
+  // Singularity check before anything is written (LuInverse.cs:145-152).
+  for (int j = 0; j < n; j++) {
+    if (a[(size_t)lda * j + j] == 0.0) {
+      if (info) *info = 1;
+      return MFG_OK;
+    }
+  }
+  for (int j = 0; j < n; j++)
+    if (piv[j] < 0 || piv[j] >= n) return fail(ctx, -5, "piv[%d] = %d is out of range", j, piv[j]);
+  const int warps = 8;
+  const size_t na = span(n, n, lda);
+  const size_t nwork = (size_t)n * n;
+  const size_t nscr = (size_t)warps * 2 * mfg::RHS_CHUNK * (n | 1);
+  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(nwork, 8) +
+                      Carve::bytes_for(nscr, 8) + Carve::bytes_for(n, 4);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(na);
+  double* d_w = cv.take<double>(nwork);
+  double* d_s = cv.take<double>(nscr);
+  int* d_piv = cv.take<int>(n);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_piv, piv, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_getri_single(d_a, n, lda, d_piv, d_w, d_s, warps, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)n * 8, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  if (info) *info = 0;
+  return MFG_OK;
+}
+
+
+// ------------------------------------------------------------------------------------------
+// QR drop-ins (Factorization.Qr / QrOrthogonalFactor / QrUpperTriangularFactor), both precisions.
+
+}  // extern "C"
+
+template <typename T>
+static int qr_single(mfg_ctx* ctx, int m, int n, T* a, int lda, T* rdiag) {
+  if (!ctx) return -1;
+  // Factorization.Qr argument checks (Factorization.Qr.cs:117-145).
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!rdiag) return fail(ctx, -6, "rdiag is null");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  const size_t na = span(m, n, lda);
+  const size_t need = Carve::bytes_for(na, sizeof(T)) + Carve::bytes_for(n, sizeof(T)) +
+                      Carve::bytes_for(n + 1, sizeof(T));
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  T* d_a = cv.take<T>(na);
+  T* d_r = cv.take<T>(n);
+  T* d_s = cv.take<T>(n + 1);
+  cudaStream_t s = ctx->stream;
+  const size_t es = sizeof(T);
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_qr_single<T>(d_a, m, n, lda, d_r, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * es, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+template <typename T>
+static int qr_q_single(mfg_ctx* ctx, int m, int n, const T* a, int lda, T* q, int ldq) {
+  if (!ctx) return -1;
+  // QrOrthogonalFactor argument checks (Factorization.Qr.cs:359-392).
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!q) return fail(ctx, -6, "q is null");
+  if (ldq < m)
+    return fail(ctx, -7,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  const size_t na = span(m, n, lda), nq = span(m, n, ldq);
+  const size_t need = Carve::bytes_for(na, sizeof(T)) + Carve::bytes_for(nq, sizeof(T)) +
+                      Carve::bytes_for(n + 1, sizeof(T));
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  T* d_a = cv.take<T>(na);
+  T* d_q = cv.take<T>(nq);
+  T* d_s = cv.take<T>(n + 1);
+  cudaStream_t s = ctx->stream;
+  const size_t es = sizeof(T);
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_qr_q_single<T>(d_a, m, n, lda, d_q, ldq, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(q, (size_t)ldq * es, d_q, (size_t)ldq * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+template <typename T>
+static int qr_r_single(mfg_ctx* ctx, int m, int n, const T* a, int lda, T* r, int ldr,
+                       const T* rdiag) {
+  if (!ctx) return -1;
+  // QrUpperTriangularFactor argument checks (Factorization.Qr.cs:599-632).
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!r) return fail(ctx, -6, "r is null");
+  if (ldr < n)
+    return fail(ctx, -7,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  if (!rdiag) return fail(ctx, -8, "rdiag is null");
+  const size_t na = span(n, n, lda), nr = span(n, n, ldr);
+  const size_t need = Carve::bytes_for(na, sizeof(T)) + Carve::bytes_for(nr, sizeof(T)) +
+                      Carve::bytes_for(n, sizeof(T));
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  T* d_a = cv.take<T>(na);
+  T* d_r = cv.take<T>(nr);
+  T* d_d = cv.take<T>(n);
+  cudaStream_t s = ctx->stream;
+  const size_t es = sizeof(T);
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * es, cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_qr_r_single<T>(d_a, n, lda, d_r, ldr, d_d, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(r, (size_t)ldr * es, d_r, (size_t)ldr * es, (size_t)n * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+extern "C" {
+
+MFG_API int mfg_dgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
+  return qr_single<double>(ctx, m, n, a, lda, rdiag);
+}
+MFG_API int mfg_sgeqrf(mfg_ctx* ctx, int m, int n, float* a, int lda, float* rdiag) {
+  return qr_single<float>(ctx, m, n, a, lda, rdiag);
+}
+MFG_API int mfg_dorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq) {
+  return qr_q_single<double>(ctx, m, n, a, lda, q, ldq);
+}
+MFG_API int mfg_sorgqr(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* q, int ldq) {
+  return qr_q_single<float>(ctx, m, n, a, lda, q, ldq);
+}
+MFG_API int mfg_dqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
+                      const double* rdiag) {
+  return qr_r_single<double>(ctx, m, n, a, lda, r, ldr, rdiag);
+}
+MFG_API int mfg_sqr_r(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* r, int ldr,
+                      const float* rdiag) {
+  return qr_r_single<float>(ctx, m, n, a, lda, r, ldr, rdiag);
+}
+
+MFG_API int mfg_plan_geqrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* m,
+                                   const int* n, const int* lda, const int64_t* a_off,
+                                   const int64_t* rdiag_off, int nrhs, const int64_t* b_off) {
+  return plan_create_qr(ctx, plan, count, m, n, lda, a_off, rdiag_off, nrhs, b_off);
+}
+
+MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!rdiag) return fail(ctx, -3, "rdiag is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  }
+  plan->qr_float = 0;
+  plan->qd.a = a;
+  plan->qd.rdiag = rdiag;
+  plan->qd.b = b;
+  return plan_execute(plan, a, rdiag, b, (const void*)1, nullptr);
+}
+
+MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!rdiag) return fail(ctx, -3, "rdiag is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  }
+  plan->qr_float = 1;
+  plan->qs.a = a;
+  plan->qs.rdiag = rdiag;
+  plan->qs.b = b;
+  return plan_execute(plan, a, rdiag, b, (const void*)2, nullptr);
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched plans.
+
+MFG_API int mfg_plan_getrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, const int64_t* piv_off,
+                                   int nrhs, const int64_t* b_off) {
+  return plan_create(ctx, plan, mfg_plan::GETRF, count, n, lda, a_off, piv_off, nrhs, b_off);
+}
+
+MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, int nrhs,
+                                   const int64_t* b_off) {
+  return plan_create(ctx, plan, mfg_plan::POTRF, count, n, lda, a_off, nullptr, nrhs, b_off);
+}
+
+MFG_API int mfg_plan_destroy(mfg_plan* plan) {
+  if (!plan) return -1;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  cudaStreamSynchronize(plan->ctx->stream);
+  plan->meta.release();
+  plan->scratch.release();
+  delete plan;
+  return MFG_OK;
+}
+
+MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                               int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!piv) return fail(ctx, -3, "piv is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+    if (!sign) return fail(ctx, -5, "sign is null");
+    if (!info) return fail(ctx, -6, "info is null");
+  }
+  plan->args.a = a;
+  plan->args.piv = piv;
+  plan->args.b = b;
+  plan->args.sign = sign;
+  plan->args.info = info;
+  return plan_execute(plan, a, piv, b, sign, info);
+}
+
+MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -3, "b is null");
+    if (!info) return fail(ctx, -4, "info is null");
+  }
+  plan->args.a = a;
+  plan->args.piv = nullptr;
+  plan->args.b = b;
+  plan->args.sign = nullptr;
+  plan->args.info = info;
+  return plan_execute(plan, a, b, info, nullptr, nullptr);
+}
+
+MFG_API int mfg_plan_status(mfg_plan* plan) {
+  if (!plan) return -1;
+  MFG_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
+  MFG_CUDA(plan->ctx, cudaGetLastError());
+  return MFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+"""Seeded synthetic batches with the shapes of the reference's benchmark configurations.
+
+Host-side generation (libmatflat_synth.so, counter-based SplitMix64 + Box-Muller), so the GPU
+path and the CPU oracle see identical bytes.  Every batch is packed: matrix i is column-major with
+leading dimension equal to its row count, at element offset a_off[i].
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def _synth():
+    global _lib
+    if _lib is None:
+        path = _build.SYNTH_LIB
+        if not os.path.exists(path):
+            path = _build.build_synth()
+        lib = ctypes.CDLL(path)
+        lib.mfs_normal.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
+        lib.mfs_uniform.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
+                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int]
+        _lib = lib
+    return _lib
+
+
+def _threads():
+    return max(1, min(64, os.cpu_count() or 1))
+
+
+def normal(count, seed, stream=0, offset=0, out=None):
+    out = np.empty(count, np.float64) if out is None else out
+    _synth().mfs_normal(out.ctypes.data, count, seed, stream, offset, _threads())
+    return out
+
+
+def uniform(count, seed, stream=0, offset=0, lo=0.0, hi=1.0, out=None):
+    out = np.empty(count, np.float64) if out is None else out
+    _synth().mfs_uniform(out.ctypes.data, count, seed, stream, offset, lo, hi, _threads())
+    return out
+
+
+def packed_offsets(rows, cols):
+    sizes = np.asarray(rows, np.int64) * np.asarray(cols, np.int64)
+    off = np.zeros(len(sizes), np.int64)
+    if len(sizes) > 1:
+        off[1:] = np.cumsum(sizes)[:-1]
+    return off, int(sizes.sum())
+
+
+def lu_batch(count, nmin=8, nmax=128, nrhs=4, seed=0):
+    """LU + solve workload: n ~ U{nmin..nmax}, A ~ N(0,1), nrhs right-hand sides ~ N(0,1)."""
+    n = (np.floor(uniform(count, seed, stream=1) * (nmax - nmin + 1)) + nmin).astype(np.int32)
+    a_off, total = packed_offsets(n, n)
+    a = normal(total, seed, stream=2)
+    piv_off, piv_total = packed_offsets(n, np.ones_like(n))
+    b_off, b_total = packed_offsets(n, np.full_like(n, nrhs))
+    b = normal(b_total, seed, stream=3)
+    return dict(n=n, a_off=a_off, a=a, piv_off=piv_off, piv_total=piv_total, b_off=b_off, b=b,
+                nrhs=nrhs)
+
+
+def spd_batch(count, n=32, nrhs=1, seed=0):
+    """Cholesky + solve workload: A = B B^T + n I with B ~ N(0,1), right-hand sides ~ N(0,1)."""
+    ns = np.full(count, n, np.int32)
+    bmat = normal(count * n * n, seed, stream=4).reshape(count, n, n)
+    a = np.matmul(bmat, np.transpose(bmat, (0, 2, 1)))
+    a += n * np.eye(n)[None, :, :]
+    a = np.ascontiguousarray(np.transpose(a, (0, 2, 1))).reshape(-1)   # column-major per matrix
+    a_off, _ = packed_offsets(ns, ns)
+    b_off, b_total = packed_offsets(ns, np.full_like(ns, nrhs))
+    b = normal(b_total, seed, stream=5)
+    return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=b, nrhs=nrhs)
+
+
+def qr_batch(count, mmin=64, mmax=512, nmin=16, nmax=64, nrhs=1, seed=0):
+    """QR least-squares workload: m ~ U{mmin..mmax}, n ~ U{nmin..nmax} (n <= m), N(0,1) data."""
+    m = (np.floor(uniform(count, seed, stream=6) * (mmax - mmin + 1)) + mmin).astype(np.int32)
+    n = (np.floor(uniform(count, seed, stream=7) * (nmax - nmin + 1)) + nmin).astype(np.int32)
+    n = np.minimum(n, m)
+    a_off, total = packed_offsets(m, n)
+    a = normal(total, seed, stream=8)
+    rdiag_off, rd_total = packed_offsets(n, np.ones_like(n))
+    b_off, b_total = packed_offsets(m, np.full_like(m, nrhs))
+    b = normal(b_total, seed, stream=9)
+    return dict(m=m, n=n, a_off=a_off, a=a, rdiag_off=rdiag_off, rdiag_total=rd_total,
+                b_off=b_off, b=b, nrhs=nrhs)

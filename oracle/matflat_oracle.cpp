@@ -1,0 +1,988 @@
+// MatFlat CPU oracle — TEST INFRASTRUCTURE ONLY.
+//
+// A plain C++ restatement of the arithmetic of MatFlat 0.8.2 (sinshu/matflat, C#) for the
+// factorization hot path: Internals.Dot/Norm/MulAdd/DivInplace/SwapRows, Factorization.Lu,
+// Factorization.Cholesky, Factorization.Qr (+ QrOrthogonalFactor, QrUpperTriangularFactor),
+// Blas.SolveTriangular, Blas.MulMatMat, Blas.MulMatVec and Factorization.LuInverse, for the
+// float, double and Complex overloads.  Every routine cites the reference file:line it follows.
+//
+// It exists to check the CUDA library (tests, the smoke check) and to time the reference
+// algorithm on the host cores (the CPU baseline leg of bench.py).  The product library never
+// links it, calls it or falls back to it.
+//
+// Arithmetic contract.  MatFlat evaluates every product and sum separately rounded (RyuJIT does
+// not contract a*b+c into an FMA), so this file MUST be compiled with -ffp-contract=off and no
+// fast-math; the build recipe next to it does so.  The summation trees below reproduce the C#
+// evaluation order exactly: `sum += x0*y0 + x1*y1` evaluates the right-hand pair first.
+//
+// Parity pin.  The reference is C# and no .NET runtime exists on either machine, so the
+// reference itself cannot be executed.  The restatement is pinned against the reference test
+// suite's own oracle (OpenBLAS LAPACK/BLAS via scipy, at the tolerances and shapes of
+// MatFlatTest/*.cs) and against its literal fixtures; see tests/test_oracle_pin.py.
+
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include <atomic>
+#include <algorithm>
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// .NET System.Numerics.Complex arithmetic, restated (textbook formulas, no FMA):
+//   (a+bi)(c+di) = (ac - bd) + (bc + ad)i ;  division by Smith's algorithm (Smith, CACM 1962),
+//   which is what System.Numerics.Complex.op_Division uses.
+struct cplx {
+  double re, im;
+};
+static inline cplx cadd(cplx x, cplx y) { return {x.re + y.re, x.im + y.im}; }
+static inline cplx csub(cplx x, cplx y) { return {x.re - y.re, x.im - y.im}; }
+static inline cplx cmul(cplx x, cplx y) {
+  return {x.re * y.re - x.im * y.im, x.im * y.re + x.re * y.im};
+}
+static inline cplx cdiv(cplx x, cplx y) {
+  double a = x.re, b = x.im, c = y.re, d = y.im;
+  if (std::fabs(d) < std::fabs(c)) {
+    double doc = d / c;
+    return {(a + b * doc) / (c + d * doc), (b - a * doc) / (c + d * doc)};
+  } else {
+    double cod = c / d;
+    return {(b + a * cod) / (d + c * cod), (-a + b * cod) / (d + c * cod)};
+  }
+}
+static inline cplx cconj(cplx x) { return {x.re, -x.im}; }
+// Internals.MulConj (Internals.cs:22-29): conj(x) * y
+static inline cplx cmulconj(cplx x, cplx y) {
+  double a = x.re, b = -x.im, c = y.re, d = y.im;
+  return {a * c - b * d, a * d + b * c};
+}
+// Internals.MulConjConj (Internals.cs:32-39): conj(x) * conj(y)
+static inline cplx cmulconjconj(cplx x, cplx y) {
+  double a = x.re, b = -x.im, c = y.re, d = -y.im;
+  return {a * c - b * d, a * d + b * c};
+}
+// Internals.FastMagnitude (Internals.cs:16-19)
+static inline double cfastmag(cplx x) { return std::fabs(x.re) + std::fabs(x.im); }
+
+// ---------------------------------------------------------------------------------------------
+// Internals.Dot, strided double (Internals.cs:265-292); the contiguous twin (:178-205) is the
+// same tree with unit strides.
+static double dot_d(int n, const double* x, long incx, const double* y, long incy) {
+  double sum;
+  if (n & 1) {
+    sum = x[0] * y[0];
+    x += incx;
+    y += incy;
+    n--;
+  } else {
+    sum = 0.0;
+  }
+  while (n > 0) {
+    sum += x[0] * y[0] + x[incx] * y[incy];
+    x += 2 * incx;
+    y += 2 * incy;
+    n -= 2;
+  }
+  return sum;
+}
+
+// Internals.Dot, strided float widened to double (Internals.cs:236-263; contiguous :149-176).
+static double dot_s(int n, const float* x, long incx, const float* y, long incy) {
+  double sum;
+  if (n & 1) {
+    sum = (double)x[0] * (double)y[0];
+    x += incx;
+    y += incy;
+    n--;
+  } else {
+    sum = 0.0;
+  }
+  while (n > 0) {
+    sum += (double)x[0] * (double)y[0] + (double)x[incx] * (double)y[incy];
+    x += 2 * incx;
+    y += 2 * incy;
+    n -= 2;
+  }
+  return sum;
+}
+
+// Internals.Dot, Complex (Internals.cs:294-321; contiguous :207-234).
+static cplx dot_z(int n, const cplx* x, long incx, const cplx* y, long incy) {
+  cplx sum;
+  if (n & 1) {
+    sum = cmul(x[0], y[0]);
+    x += incx;
+    y += incy;
+    n--;
+  } else {
+    sum = {0.0, 0.0};
+  }
+  while (n > 0) {
+    sum = cadd(sum, cadd(cmul(x[0], y[0]), cmul(x[incx], y[incy])));
+    x += 2 * incx;
+    y += 2 * incy;
+    n -= 2;
+  }
+  return sum;
+}
+
+// Internals.DotConj, Complex (Internals.cs:352-379; contiguous :323-350): sum conj(x)*y.
+static cplx dotconj_z(int n, const cplx* x, long incx, const cplx* y, long incy) {
+  cplx sum;
+  if (n & 1) {
+    sum = cmulconj(x[0], y[0]);
+    x += incx;
+    y += incy;
+    n--;
+  } else {
+    sum = {0.0, 0.0};
+  }
+  while (n > 0) {
+    sum = cadd(sum, cadd(cmulconj(x[0], y[0]), cmulconj(x[incx], y[incy])));
+    x += 2 * incx;
+    y += 2 * incy;
+    n -= 2;
+  }
+  return sum;
+}
+
+// Internals.Norm (Internals.cs:435-460 double, :381-406 float, :489-514 Complex).
+static double norm_d(int n, const double* x) {
+  double sum;
+  if (n & 1) {
+    sum = x[0] * x[0];
+    x++;
+    n--;
+  } else {
+    sum = 0.0;
+  }
+  while (n > 0) {
+    sum += x[0] * x[0] + x[1] * x[1];
+    x += 2;
+    n -= 2;
+  }
+  return std::sqrt(sum);
+}
+static double norm_s(int n, const float* x) {
+  double sum;
+  if (n & 1) {
+    sum = (double)x[0] * (double)x[0];
+    x++;
+    n--;
+  } else {
+    sum = 0.0;
+  }
+  while (n > 0) {
+    sum += (double)x[0] * (double)x[0] + (double)x[1] * (double)x[1];
+    x += 2;
+    n -= 2;
+  }
+  return std::sqrt(sum);
+}
+static double norm_z(int n, const cplx* x) {
+  double sum;
+  if (n & 1) {
+    sum = x[0].re * x[0].re + x[0].im * x[0].im;
+    x++;
+    n--;
+  } else {
+    sum = 0.0;
+  }
+  while (n > 0) {
+    sum += x[0].re * x[0].re + x[0].im * x[0].im + x[1].re * x[1].re + x[1].im * x[1].im;
+    x += 2;
+    n -= 2;
+  }
+  return std::sqrt(sum);
+}
+
+// Internals.MulAdd (Internals.cs:49-73): dst += x*y element by element (the pairing of the
+// loop does not change any value: every element is updated once).
+template <typename T>
+static void muladd(int n, const T* x, T y, T* dst) {
+  for (int i = 0; i < n; i++) dst[i] += x[i] * y;
+}
+static void muladd_z(int n, const cplx* x, cplx y, cplx* dst) {
+  for (int i = 0; i < n; i++) dst[i] = cadd(dst[i], cmul(x[i], y));
+}
+// Internals.MulConjAdd (Internals.cs:75-99): dst += conj(x) * y[i]
+static void mulconjadd_z(int n, cplx x, const cplx* y, cplx* dst) {
+  for (int i = 0; i < n; i++) dst[i] = cadd(dst[i], cmulconj(x, y[i]));
+}
+
+// Internals.DivInplace (Internals.cs:125-147): true division, element by element.
+template <typename T>
+static void divinplace(int n, T* x, T y) {
+  for (int i = 0; i < n; i++) x[i] /= y;
+}
+static void divinplace_z(int n, cplx* x, cplx y) {
+  for (int i = 0; i < n; i++) x[i] = cdiv(x[i], y);
+}
+
+// Internals.SwapRows (Internals.cs:567-576).
+template <typename T>
+static void swaprows(int n, T* x, T* y, long inc) {
+  for (int c = 0; c < n; c++) {
+    T t = x[c * inc];
+    x[c * inc] = y[c * inc];
+    y[c * inc] = t;
+  }
+}
+
+// Blas.MulSub (Blas.SolveTriangular.cs:397-421): dst -= x*y, element by element.
+template <typename T>
+static void mulsub(int n, const T* x, long incx, T y, T* dst, long incdst) {
+  for (int i = 0; i < n; i++) dst[i * incdst] -= x[i * incx] * y;
+}
+static void mulsub_z(int n, const cplx* x, long incx, cplx y, cplx* dst, long incdst) {
+  for (int i = 0; i < n; i++) dst[i * incdst] = csub(dst[i * incdst], cmul(x[i * incx], y));
+}
+// Blas.MulSubConj (Blas.SolveTriangular.cs:423-447): dst -= conj(x) * y
+static void mulsubconj_z(int n, const cplx* x, long incx, cplx y, cplx* dst, long incdst) {
+  for (int i = 0; i < n; i++)
+    dst[i * incdst] = csub(dst[i * incdst], cmulconj(x[i * incx], y));
+}
+
+}  // namespace
+
+extern "C" {
+
+// =============================================================================================
+// LU with partial pivoting: Factorization.LuCore (Factorization.Lu.cs:296-350 double,
+// :240-294 float, :352-406 Complex).  Returns the pivot sign.  `work` holds m elements.
+int orc_dlu(int m, int n, double* a, int lda, int* piv) {
+  std::vector<double> workv(m);
+  double* work = workv.data();
+  for (int i = 0; i < m; i++) piv[i] = i;
+  int sign = 1;
+  double* colj = a;
+  for (int j = 0; j < n; j++) {
+    std::memcpy(work, colj, sizeof(double) * m);
+    for (int i = 0; i < m; i++) {
+      double s = dot_d(std::min(i, j), a + i, lda, work, 1);
+      colj[i] = work[i] -= s;
+    }
+    int p = j;
+    for (int i = j + 1; i < m; i++)
+      if (std::fabs(work[i]) > std::fabs(work[p])) p = i;
+    if (p != j) {
+      swaprows(n, a + p, a + j, lda);
+      std::swap(piv[p], piv[j]);
+      sign = -sign;
+    }
+    if (j < m) {
+      double diag = colj[j];
+      if (diag != 0.0) divinplace(m - j - 1, colj + j + 1, diag);
+    }
+    colj += lda;
+  }
+  return sign;
+}
+
+int orc_slu(int m, int n, float* a, int lda, int* piv) {
+  std::vector<float> workv(m);
+  float* work = workv.data();
+  for (int i = 0; i < m; i++) piv[i] = i;
+  int sign = 1;
+  float* colj = a;
+  for (int j = 0; j < n; j++) {
+    std::memcpy(work, colj, sizeof(float) * m);
+    for (int i = 0; i < m; i++) {
+      float s = (float)dot_s(std::min(i, j), a + i, lda, work, 1);
+      colj[i] = work[i] -= s;
+    }
+    int p = j;
+    for (int i = j + 1; i < m; i++)
+      if (std::fabs(work[i]) > std::fabs(work[p])) p = i;
+    if (p != j) {
+      swaprows(n, a + p, a + j, lda);
+      std::swap(piv[p], piv[j]);
+      sign = -sign;
+    }
+    if (j < m) {
+      float diag = colj[j];
+      if (diag != 0.0f) divinplace(m - j - 1, colj + j + 1, diag);
+    }
+    colj += lda;
+  }
+  return sign;
+}
+
+int orc_zlu(int m, int n, double* a_, int lda, int* piv) {
+  cplx* a = reinterpret_cast<cplx*>(a_);
+  std::vector<cplx> workv(m);
+  cplx* work = workv.data();
+  for (int i = 0; i < m; i++) piv[i] = i;
+  int sign = 1;
+  cplx* colj = a;
+  for (int j = 0; j < n; j++) {
+    std::memcpy(work, colj, sizeof(cplx) * m);
+    for (int i = 0; i < m; i++) {
+      cplx s = dot_z(std::min(i, j), a + i, lda, work, 1);
+      work[i] = csub(work[i], s);
+      colj[i] = work[i];
+    }
+    int p = j;
+    for (int i = j + 1; i < m; i++)
+      if (cfastmag(work[i]) > cfastmag(work[p])) p = i;
+    if (p != j) {
+      swaprows(n, a + p, a + j, lda);
+      std::swap(piv[p], piv[j]);
+      sign = -sign;
+    }
+    if (j < m) {
+      cplx diag = colj[j];
+      if (!(diag.re == 0.0 && diag.im == 0.0)) divinplace_z(m - j - 1, colj + j + 1, diag);
+    }
+    colj += lda;
+  }
+  return sign;
+}
+
+// =============================================================================================
+// Cholesky A = L*L^H: Factorization.Cholesky (Factorization.Cholesky.cs:114-168 double,
+// :33-87 float, :195-249 Complex).  Reads the upper triangle, writes L to the lower triangle,
+// zeroes the strict upper triangle.  Returns 0, or j+1 for the first column whose pivot is not
+// positive (MatFlat throws MatrixFactorizationException there; the array is left as it was at
+// that point, without the final clearing pass).
+int orc_dcholesky(int n, double* a, int lda) {
+  double* colj = a;
+  for (int j = 0; j < n; j++) {
+    double s = 0.0;
+    double* colk = a;
+    for (int k = 0; k < j; k++) {
+      double t = (colj[k] - dot_d(k, a + j, lda, a + k, lda)) / colk[k];
+      colk[j] = t;
+      s += t * t;
+      colk += lda;
+    }
+    s = colj[j] - s;
+    if (s > 0) {
+      colj[j] = std::sqrt(s);
+    } else {
+      return j + 1;
+    }
+    colj += lda;
+  }
+  colj = a + lda;
+  for (int j = 1; j < n; j++) {
+    std::memset(colj, 0, sizeof(double) * j);
+    colj += lda;
+  }
+  return 0;
+}
+
+int orc_scholesky(int n, float* a, int lda) {
+  float* colj = a;
+  for (int j = 0; j < n; j++) {
+    double s = 0.0;
+    float* colk = a;
+    for (int k = 0; k < j; k++) {
+      double t = ((double)colj[k] - dot_s(k, a + j, lda, a + k, lda)) / (double)colk[k];
+      colk[j] = (float)t;
+      s += t * t;
+      colk += lda;
+    }
+    s = (double)colj[j] - s;
+    if (s > 0) {
+      colj[j] = (float)std::sqrt(s);
+    } else {
+      return j + 1;
+    }
+    colj += lda;
+  }
+  colj = a + lda;
+  for (int j = 1; j < n; j++) {
+    std::memset(colj, 0, sizeof(float) * j);
+    colj += lda;
+  }
+  return 0;
+}
+
+int orc_zcholesky(int n, double* a_, int lda) {
+  cplx* a = reinterpret_cast<cplx*>(a_);
+  cplx* colj = a;
+  for (int j = 0; j < n; j++) {
+    double s = 0.0;
+    cplx* colk = a;
+    for (int k = 0; k < j; k++) {
+      cplx t = cdiv(csub(colj[k], dotconj_z(k, a + j, lda, a + k, lda)), colk[k]);
+      colk[j] = {t.re, -t.im};
+      s += t.re * t.re + t.im * t.im;
+      colk += lda;
+    }
+    s = colj[j].re - s;
+    if (s > 0) {
+      colj[j] = {std::sqrt(s), 0.0};
+    } else {
+      return j + 1;
+    }
+    colj += lda;
+  }
+  colj = a + lda;
+  for (int j = 1; j < n; j++) {
+    std::memset(colj, 0, sizeof(cplx) * j);
+    colj += lda;
+  }
+  return 0;
+}
+
+// =============================================================================================
+// Householder QR in the Mapack format: Factorization.Qr (Factorization.Qr.cs:115-172 double,
+// :32-89 float, :198-255 Complex).  No reflector sign choice; rdiag[k] = -norm.
+void orc_dqr(int m, int n, double* a, int lda, double* rdiag) {
+  double* colk = a;
+  for (int k = 0; k < n; k++) {
+    double norm = norm_d(m - k, colk + k);
+    if (norm != 0.0) {
+      divinplace(m - k, colk + k, norm);
+      colk[k] += 1.0;
+      for (int j = k + 1; j < n; j++) {
+        double* colj = a + (long)lda * j;
+        double s = -dot_d(m - k, colk + k, 1, colj + k, 1) / colk[k];
+        muladd(m - k, colk + k, s, colj + k);
+      }
+    }
+    rdiag[k] = -norm;
+    colk += lda;
+  }
+}
+
+void orc_sqr(int m, int n, float* a, int lda, float* rdiag) {
+  float* colk = a;
+  for (int k = 0; k < n; k++) {
+    float norm = (float)norm_s(m - k, colk + k);
+    if (norm != 0.0f) {
+      divinplace(m - k, colk + k, norm);
+      colk[k] += 1.0f;
+      for (int j = k + 1; j < n; j++) {
+        float* colj = a + (long)lda * j;
+        float s = -(float)(dot_s(m - k, colk + k, 1, colj + k, 1) / (double)colk[k]);
+        muladd(m - k, colk + k, s, colj + k);
+      }
+    }
+    rdiag[k] = -norm;
+    colk += lda;
+  }
+}
+
+void orc_zqr(int m, int n, double* a_, int lda, double* rdiag) {
+  cplx* a = reinterpret_cast<cplx*>(a_);
+  cplx* colk = a;
+  for (int k = 0; k < n; k++) {
+    double norm = norm_z(m - k, colk + k);
+    if (norm != 0.0) {
+      // DivInplace<Complex>(…, norm): Complex / Complex(norm, 0).
+      divinplace_z(m - k, colk + k, cplx{norm, 0.0});
+      colk[k] = cadd(colk[k], cplx{1.0, 0.0});
+      for (int j = k + 1; j < n; j++) {
+        cplx* colj = a + (long)lda * j;
+        cplx d = dotconj_z(m - k, colk + k, 1, colj + k, 1);
+        cplx s = cdiv(cplx{-d.re, -d.im}, colk[k]);
+        muladd_z(m - k, colk + k, s, colj + k);
+      }
+    }
+    rdiag[k] = -norm;
+    colk += lda;
+  }
+}
+
+// QrOrthogonalFactor (Factorization.Qr.cs:357-413 double, :278-334 float, :436-492 Complex).
+void orc_dqr_q(int m, int n, const double* a, int lda, double* q, int ldq) {
+  for (int k = n - 1; k >= 0; k--) {
+    double* qColk = q + (long)ldq * k;
+    const double* aColk = a + (long)lda * k;
+    std::memset(qColk, 0, sizeof(double) * m);
+    qColk[k] = 1.0;
+    for (int j = k; j < n; j++) {
+      double* qColj = q + (long)ldq * j;
+      if (aColk[k] != 0) {
+        double s = -dot_d(m - k, aColk + k, 1, qColj + k, 1) / aColk[k];
+        muladd(m - k, aColk + k, s, qColj + k);
+      }
+    }
+  }
+}
+
+void orc_sqr_q(int m, int n, const float* a, int lda, float* q, int ldq) {
+  for (int k = n - 1; k >= 0; k--) {
+    float* qColk = q + (long)ldq * k;
+    const float* aColk = a + (long)lda * k;
+    std::memset(qColk, 0, sizeof(float) * m);
+    qColk[k] = 1.0f;
+    for (int j = k; j < n; j++) {
+      float* qColj = q + (long)ldq * j;
+      if (aColk[k] != 0) {
+        float s = -(float)(dot_s(m - k, aColk + k, 1, qColj + k, 1) / (double)aColk[k]);
+        muladd(m - k, aColk + k, s, qColj + k);
+      }
+    }
+  }
+}
+
+void orc_zqr_q(int m, int n, const double* a_, int lda, double* q_, int ldq) {
+  const cplx* a = reinterpret_cast<const cplx*>(a_);
+  cplx* q = reinterpret_cast<cplx*>(q_);
+  for (int k = n - 1; k >= 0; k--) {
+    cplx* qColk = q + (long)ldq * k;
+    const cplx* aColk = a + (long)lda * k;
+    std::memset(qColk, 0, sizeof(cplx) * m);
+    qColk[k] = {1.0, 0.0};
+    for (int j = k; j < n; j++) {
+      cplx* qColj = q + (long)ldq * j;
+      if (!(aColk[k].re == 0.0 && aColk[k].im == 0.0)) {
+        // Factorization.Qr.cs:487-488: s = -DotConj(qColj, aColk) / aColk[k];
+        // MulConjAdd(s, aColk, qColj): q += conj(s) * a.
+        cplx d = dotconj_z(m - k, qColj + k, 1, aColk + k, 1);
+        cplx s = cdiv(cplx{-d.re, -d.im}, aColk[k]);
+        mulconjadd_z(m - k, s, aColk + k, qColj + k);
+      }
+    }
+  }
+}
+
+// QrUpperTriangularFactor (Factorization.Qr.cs:597-650 double, :518-571 float, :677-730 Complex).
+void orc_dqr_r(int m, int n, const double* a, int lda, double* r, int ldr, const double* rdiag) {
+  (void)m;
+  for (int i = 0; i < n; i++) {
+    std::memcpy(r + (long)ldr * i, a + (long)lda * i, sizeof(double) * i);
+    r[(long)ldr * i + i] = rdiag[i];
+    std::memset(r + (long)ldr * i + i + 1, 0, sizeof(double) * (n - i - 1));
+  }
+}
+void orc_sqr_r(int m, int n, const float* a, int lda, float* r, int ldr, const float* rdiag) {
+  (void)m;
+  for (int i = 0; i < n; i++) {
+    std::memcpy(r + (long)ldr * i, a + (long)lda * i, sizeof(float) * i);
+    r[(long)ldr * i + i] = rdiag[i];
+    std::memset(r + (long)ldr * i + i + 1, 0, sizeof(float) * (n - i - 1));
+  }
+}
+void orc_zqr_r(int m, int n, const double* a_, int lda, double* r_, int ldr, const double* rdiag) {
+  (void)m;
+  const cplx* a = reinterpret_cast<const cplx*>(a_);
+  cplx* r = reinterpret_cast<cplx*>(r_);
+  for (int i = 0; i < n; i++) {
+    std::memcpy(r + (long)ldr * i, a + (long)lda * i, sizeof(cplx) * i);
+    r[(long)ldr * i + i] = {rdiag[i], 0.0};
+    std::memset(r + (long)ldr * i + i + 1, 0, sizeof(cplx) * (n - i - 1));
+  }
+}
+
+// =============================================================================================
+// Triangular solve, non-unit diagonal: Blas.SolveTriangular (Blas.SolveTriangular.cs:162-242
+// double, :44-124 float, :280-395 Complex).  uplo: 121 Upper, 122 Lower.  trans: 111 NoTrans,
+// 112 Trans, 113 ConjTrans, 114 ConjNoTrans.  Returns 0, or -1 for an invalid enum.
+enum { UPPER = 121, LOWER = 122, NOTRANS = 111, TRANS = 112, CONJTRANS = 113, CONJNOTRANS = 114 };
+
+int orc_dtrsv(int uplo, int trans, int n, const double* a, int lda, double* x, int incx) {
+  if (uplo == UPPER) {
+    if (trans == NOTRANS) {
+      for (int i = n - 1; i >= 0; i--) {
+        long p = (long)incx * i;
+        const double* aColi = a + (long)lda * i;
+        x[p] /= aColi[i];
+        mulsub(i, aColi, 1, x[p], x, incx);
+      }
+    } else if (trans == TRANS) {
+      for (int j = 0; j < n; j++) {
+        long p = (long)incx * j;
+        x[p] = (x[p] - dot_d(j, a + (long)lda * j, 1, x, incx)) / a[(long)lda * j + j];
+      }
+    } else {
+      return -1;
+    }
+  } else if (uplo == LOWER) {
+    if (trans == NOTRANS) {
+      for (int i = 0; i < n; i++) {
+        long p = (long)incx * i;
+        x[p] = (x[p] - dot_d(i, a + i, lda, x, incx)) / a[(long)lda * i + i];
+      }
+    } else if (trans == TRANS) {
+      for (int j = n - 1; j >= 0; j--) {
+        long p = (long)incx * j;
+        x[p] /= a[(long)j * lda + j];
+        mulsub(j, a + j, lda, x[p], x, incx);
+      }
+    } else {
+      return -1;
+    }
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+int orc_strsv(int uplo, int trans, int n, const float* a, int lda, float* x, int incx) {
+  if (uplo == UPPER) {
+    if (trans == NOTRANS) {
+      for (int i = n - 1; i >= 0; i--) {
+        long p = (long)incx * i;
+        const float* aColi = a + (long)lda * i;
+        x[p] /= aColi[i];
+        mulsub(i, aColi, 1, x[p], x, incx);
+      }
+    } else if (trans == TRANS) {
+      for (int j = 0; j < n; j++) {
+        long p = (long)incx * j;
+        x[p] = (float)(((double)x[p] - dot_s(j, a + (long)lda * j, 1, x, incx)) /
+                       (double)a[(long)lda * j + j]);
+      }
+    } else {
+      return -1;
+    }
+  } else if (uplo == LOWER) {
+    if (trans == NOTRANS) {
+      for (int i = 0; i < n; i++) {
+        long p = (long)incx * i;
+        x[p] = (float)(((double)x[p] - dot_s(i, a + i, lda, x, incx)) / (double)a[(long)lda * i + i]);
+      }
+    } else if (trans == TRANS) {
+      for (int j = n - 1; j >= 0; j--) {
+        long p = (long)incx * j;
+        x[p] /= a[(long)j * lda + j];
+        mulsub(j, a + j, lda, x[p], x, incx);
+      }
+    } else {
+      return -1;
+    }
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+int orc_ztrsv(int uplo, int trans, int n, const double* a_, int lda, double* x_, int incx) {
+  const cplx* a = reinterpret_cast<const cplx*>(a_);
+  cplx* x = reinterpret_cast<cplx*>(x_);
+  if (uplo == UPPER) {
+    if (trans == NOTRANS) {
+      for (int i = n - 1; i >= 0; i--) {
+        long p = (long)incx * i;
+        const cplx* aColi = a + (long)lda * i;
+        x[p] = cdiv(x[p], aColi[i]);
+        mulsub_z(i, aColi, 1, x[p], x, incx);
+      }
+    } else if (trans == TRANS) {
+      for (int j = 0; j < n; j++) {
+        long p = (long)incx * j;
+        x[p] = cdiv(csub(x[p], dot_z(j, a + (long)lda * j, 1, x, incx)), a[(long)lda * j + j]);
+      }
+    } else if (trans == CONJNOTRANS) {
+      for (int i = n - 1; i >= 0; i--) {
+        long p = (long)incx * i;
+        const cplx* aColi = a + (long)lda * i;
+        x[p] = cdiv(x[p], cconj(aColi[i]));
+        mulsubconj_z(i, aColi, 1, x[p], x, incx);
+      }
+    } else if (trans == CONJTRANS) {
+      for (int j = 0; j < n; j++) {
+        long p = (long)incx * j;
+        x[p] = cdiv(csub(x[p], dotconj_z(j, a + (long)lda * j, 1, x, incx)),
+                    cconj(a[(long)lda * j + j]));
+      }
+    } else {
+      return -1;
+    }
+  } else if (uplo == LOWER) {
+    if (trans == NOTRANS) {
+      for (int i = 0; i < n; i++) {
+        long p = (long)incx * i;
+        x[p] = cdiv(csub(x[p], dot_z(i, a + i, lda, x, incx)), a[(long)lda * i + i]);
+      }
+    } else if (trans == TRANS) {
+      for (int j = n - 1; j >= 0; j--) {
+        long p = (long)incx * j;
+        x[p] = cdiv(x[p], a[(long)j * lda + j]);
+        mulsub_z(j, a + j, lda, x[p], x, incx);
+      }
+    } else if (trans == CONJNOTRANS) {
+      for (int i = 0; i < n; i++) {
+        long p = (long)incx * i;
+        x[p] = cdiv(csub(x[p], dotconj_z(i, a + i, lda, x, incx)), cconj(a[(long)lda * i + i]));
+      }
+    } else if (trans == CONJTRANS) {
+      for (int j = n - 1; j >= 0; j--) {
+        long p = (long)incx * j;
+        x[p] = cdiv(x[p], cconj(a[(long)j * lda + j]));
+        mulsubconj_z(j, a + j, lda, x[p], x, incx);
+      }
+    } else {
+      return -1;
+    }
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+// =============================================================================================
+// C = op(A) * op(B), no alpha/beta: Blas.MulMatMat (Blas.MulMatMat.cs:226-368 double,
+// :45-187 float).  Each element is one Internals.Dot of length k.
+int orc_dgemm(int transa, int transb, int m, int n, int k, const double* a, int lda,
+              const double* b, int ldb, double* c, int ldc) {
+  if ((transa != NOTRANS && transa != TRANS) || (transb != NOTRANS && transb != TRANS)) return -1;
+  for (int j = 0; j < n; j++) {
+    for (int i = 0; i < m; i++) {
+      const double* x;
+      long incx;
+      const double* y;
+      long incy;
+      if (transa == NOTRANS) {
+        x = a + i;
+        incx = lda;
+      } else {
+        x = a + (long)lda * i;
+        incx = 1;
+      }
+      if (transb == NOTRANS) {
+        y = b + (long)ldb * j;
+        incy = 1;
+      } else {
+        y = b + j;
+        incy = ldb;
+      }
+      c[(long)ldc * j + i] = dot_d(k, x, incx, y, incy);
+    }
+  }
+  return 0;
+}
+
+int orc_sgemm(int transa, int transb, int m, int n, int k, const float* a, int lda,
+              const float* b, int ldb, float* c, int ldc) {
+  if ((transa != NOTRANS && transa != TRANS) || (transb != NOTRANS && transb != TRANS)) return -1;
+  for (int j = 0; j < n; j++) {
+    for (int i = 0; i < m; i++) {
+      const float* x;
+      long incx;
+      const float* y;
+      long incy;
+      if (transa == NOTRANS) {
+        x = a + i;
+        incx = lda;
+      } else {
+        x = a + (long)lda * i;
+        incx = 1;
+      }
+      if (transb == NOTRANS) {
+        y = b + (long)ldb * j;
+        incy = 1;
+      } else {
+        y = b + j;
+        incy = ldb;
+      }
+      c[(long)ldc * j + i] = (float)dot_s(k, x, incx, y, incy);
+    }
+  }
+  return 0;
+}
+
+// Complex MulMatMat (Blas.MulMatMat.cs:407-575) with its unpaired sequential dots
+// Dot_NN/CN/NC/CC (:598-648).
+int orc_zgemm(int transa, int transb, int m, int n, int k, const double* a_, int lda,
+              const double* b_, int ldb, double* c_, int ldc) {
+  const cplx* a = reinterpret_cast<const cplx*>(a_);
+  const cplx* b = reinterpret_cast<const cplx*>(b_);
+  cplx* c = reinterpret_cast<cplx*>(c_);
+  auto valid = [](int t) { return t == NOTRANS || t == TRANS || t == CONJTRANS || t == CONJNOTRANS; };
+  if (!valid(transa) || !valid(transb)) return -1;
+  bool ca = (transa == CONJNOTRANS || transa == CONJTRANS);
+  bool cb = (transb == CONJNOTRANS || transb == CONJTRANS);
+  bool ta = (transa == TRANS || transa == CONJTRANS);
+  bool tb = (transb == TRANS || transb == CONJTRANS);
+  for (int j = 0; j < n; j++) {
+    for (int i = 0; i < m; i++) {
+      const cplx* x = ta ? a + (long)lda * i : a + i;
+      long incx = ta ? 1 : lda;
+      const cplx* y = tb ? b + j : b + (long)ldb * j;
+      long incy = tb ? ldb : 1;
+      cplx sum = {0.0, 0.0};
+      for (int t = 0; t < k; t++) {
+        cplx xv = x[t * incx], yv = y[t * incy];
+        cplx p;
+        if (ca && cb) p = cmulconjconj(xv, yv);
+        else if (ca) p = cmulconj(xv, yv);
+        else if (cb) p = cmulconj(yv, xv);
+        else p = cmul(xv, yv);
+        sum = cadd(sum, p);
+      }
+      c[(long)ldc * j + i] = sum;
+    }
+  }
+  return 0;
+}
+
+// y = op(A) x: Blas.MulMatVec (Blas.MulMatVec.cs:138-236), used to form Q^T b for the
+// least-squares composition Qr -> QrOrthogonalFactor -> MulMatVec(Trans) -> SolveTriangular.
+int orc_dgemv(int trans, int m, int n, const double* a, int lda, const double* x, int incx,
+              double* y, int incy) {
+  if (trans == NOTRANS) {
+    for (int i = 0; i < m; i++) y[(long)incy * i] = dot_d(n, a + i, lda, x, incx);
+  } else if (trans == TRANS) {
+    for (int i = 0; i < n; i++) y[(long)incy * i] = dot_d(m, a + (long)lda * i, 1, x, incx);
+  } else {
+    return -1;
+  }
+  return 0;
+}
+int orc_sgemv(int trans, int m, int n, const float* a, int lda, const float* x, int incx,
+              float* y, int incy) {
+  if (trans == NOTRANS) {
+    for (int i = 0; i < m; i++) y[(long)incy * i] = (float)dot_s(n, a + i, lda, x, incx);
+  } else if (trans == TRANS) {
+    for (int i = 0; i < n; i++) y[(long)incy * i] = (float)dot_s(m, a + (long)lda * i, 1, x, incx);
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+// =============================================================================================
+// Factorization.LuInverse (Factorization.LuInverse.cs:123-199): A^-1 from the LU factors.
+// Returns 0, or 1 when a diagonal entry of U is zero (MatFlat throws there, before writing).
+int orc_dlu_inverse(int n, double* a, int lda, const int* piv) {
+  for (int j = 0; j < n; j++)
+    if (a[(long)lda * j + j] == 0.0) return 1;
+  std::vector<double> workv((size_t)n * n + n);
+  double* work = workv.data();
+  double* diag = work + (size_t)n * n;
+  for (int j = 0; j < n; j++) {
+    double* aColj = a + (long)lda * j;
+    std::memcpy(work + (size_t)n * j, aColj, sizeof(double) * n);
+    diag[j] = aColj[j];
+    std::memset(aColj, 0, sizeof(double) * n);
+  }
+  for (int j = 0; j < n; j++) a[(long)lda * piv[j] + j] = 1.0;
+  for (int j = 0; j < n; j++) work[(size_t)n * j + j] = 1.0;
+  for (int j = 0; j < n; j++) orc_dtrsv(LOWER, NOTRANS, n, work, n, a + (long)lda * j, 1);
+  for (int j = 0; j < n; j++) work[(size_t)n * j + j] = diag[j];
+  for (int j = 0; j < n; j++) orc_dtrsv(UPPER, NOTRANS, n, work, n, a + (long)lda * j, 1);
+  return 0;
+}
+
+// =============================================================================================
+// Composite per-matrix workloads of the batched paths.  Each composes the routines above in
+// the order MatFlat's own idioms give.
+
+// Solve A x = b from the LU factors of one square matrix, for nrhs right-hand sides stored
+// column after column with leading dimension ldb.  P*b first (b'[i] = b[piv[i]]), then the
+// unit-lower solve in MatFlat's LuInverse idiom (trsv Lower/NoTrans against L with its diagonal
+// set to 1.0, Factorization.LuInverse.cs:174-182 — dividing by 1.0 is exact, so this equals a
+// solve that skips the division), then trsv Upper/NoTrans against U (:184-192).
+void orc_dlu_solve(int n, const double* lu, int lda, const int* piv, int nrhs, double* b, int ldb) {
+  std::vector<double> l((size_t)n * n);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) l[(size_t)j * n + i] = lu[(long)lda * j + i];
+  for (int j = 0; j < n; j++) l[(size_t)j * n + j] = 1.0;
+  std::vector<double> tmp(n);
+  for (int r = 0; r < nrhs; r++) {
+    double* x = b + (long)ldb * r;
+    for (int i = 0; i < n; i++) tmp[i] = x[piv[i]];
+    std::memcpy(x, tmp.data(), sizeof(double) * n);
+    orc_dtrsv(LOWER, NOTRANS, n, l.data(), n, x, 1);
+    orc_dtrsv(UPPER, NOTRANS, n, lu, lda, x, 1);
+  }
+}
+
+// Least squares min ||A x - b|| for one tall matrix (m >= n), composed from MatFlat's own
+// routines since MatFlat has no QR solve: Qr, QrOrthogonalFactor, MulMatVec(Trans) for Q^T b,
+// QrUpperTriangularFactor, SolveTriangular(Upper, NoTrans).  a is overwritten by the QR factors;
+// x receives n entries.
+void orc_dqr_ls(int m, int n, double* a, int lda, const double* b, double* x) {
+  std::vector<double> rdiag(n), q((size_t)m * n), r((size_t)n * n);
+  orc_dqr(m, n, a, lda, rdiag.data());
+  orc_dqr_q(m, n, a, lda, q.data(), m);
+  orc_dgemv(TRANS, m, n, q.data(), m, b, 1, x, 1);
+  orc_dqr_r(m, n, a, lda, r.data(), n, rdiag.data());
+  orc_dtrsv(UPPER, NOTRANS, n, r.data(), n, x, 1);
+}
+void orc_sqr_ls(int m, int n, float* a, int lda, const float* b, float* x) {
+  std::vector<float> rdiag(n), q((size_t)m * n), r((size_t)n * n);
+  orc_sqr(m, n, a, lda, rdiag.data());
+  orc_sqr_q(m, n, a, lda, q.data(), m);
+  orc_sgemv(TRANS, m, n, q.data(), m, b, 1, x, 1);
+  orc_sqr_r(m, n, a, lda, r.data(), n, rdiag.data());
+  orc_strsv(UPPER, NOTRANS, n, r.data(), n, x, 1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched drivers over std::thread.  Matrices are packed: matrix i starts at a + a_off[i]
+// (elements), has order n[i] and leading dimension n[i]; vectors start at b + b_off[i].
+// Work is split by an atomic counter over the batch (dynamic chunks), which balances uneven n.
+
+}  // extern "C"
+
+template <typename F>
+static void parallel_for(long count, int nthreads, F f) {
+  if (nthreads <= 1) {
+    for (long i = 0; i < count; i++) f(i);
+    return;
+  }
+  std::atomic<long> next(0);
+  const long chunk = 16;
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; t++) {
+    th.emplace_back([&]() {
+      for (;;) {
+        long s = next.fetch_add(chunk);
+        if (s >= count) break;
+        long e = std::min(count, s + chunk);
+        for (long i = s; i < e; i++) f(i);
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+}
+
+extern "C" {
+
+// Config "Cholesky then SolveTriangular": per matrix, Cholesky; then L y = b (Lower/NoTrans)
+// and L^T x = y (Lower/Trans).  info[i] = Cholesky return code; b is left untouched on failure.
+void orc_dchol_solve_batched(long count, const int* n, const int64_t* a_off, double* a,
+                             const int64_t* b_off, double* b, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    int ni = n[i];
+    double* ai = a + a_off[i];
+    int r = orc_dcholesky(ni, ai, ni);
+    info[i] = r;
+    if (r == 0) {
+      orc_dtrsv(LOWER, NOTRANS, ni, ai, ni, b + b_off[i], 1);
+      orc_dtrsv(LOWER, TRANS, ni, ai, ni, b + b_off[i], 1);
+    }
+  });
+}
+
+// Config "LU + forward/back solve": per matrix, Lu then the solve above for nrhs columns
+// (ldb = n[i]).  sign[i] receives Lu's return value.
+void orc_dlu_solve_batched(long count, const int* n, const int64_t* a_off, double* a,
+                           const int64_t* piv_off, int* piv, const int64_t* b_off, double* b,
+                           int nrhs, int* sign, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    int ni = n[i];
+    double* ai = a + a_off[i];
+    int* pi = piv + piv_off[i];
+    sign[i] = orc_dlu(ni, ni, ai, ni, pi);
+    if (nrhs > 0) orc_dlu_solve(ni, ai, ni, pi, nrhs, b + b_off[i], ni);
+  });
+}
+
+// Config "QR + least squares": a_off/m/n per matrix (lda = m), b has m entries, x has n.
+void orc_dqr_ls_batched(long count, const int* m, const int* n, const int64_t* a_off, double* a,
+                        const int64_t* b_off, const double* b, const int64_t* x_off, double* x,
+                        int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    orc_dqr_ls(m[i], n[i], a + a_off[i], m[i], b + b_off[i], x + x_off[i]);
+  });
+}
+void orc_sqr_ls_batched(long count, const int* m, const int* n, const int64_t* a_off, float* a,
+                        const int64_t* b_off, const float* b, const int64_t* x_off, float* x,
+                        int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    orc_sqr_ls(m[i], n[i], a + a_off[i], m[i], b + b_off[i], x + x_off[i]);
+  });
+}
+
+}  // extern "C"
