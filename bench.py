@@ -302,6 +302,8 @@ def main():
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--ref-budget", type=float, default=10.0,
                     help="seconds of CPU work per step of --impl reference")
+    ap.add_argument("--count", type=int, default=None,
+                    help="override the batch size (small cases for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -309,6 +311,8 @@ def main():
         print("note: warmup raised to 3", file=sys.stderr)
         args.warmup = 3
     cfg_name = args.config
+    if args.count:
+        CONFIGS[cfg_name]["count"] = args.count
     if args.impl == "reference":
         run_reference(args, cfg_name)
         return

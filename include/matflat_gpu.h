@@ -181,6 +181,13 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan);
  * context's stream): MFG_OK, or MFG_ERR_TIMEOUT if a bounded device-side wait gave up. */
 MFG_API int mfg_plan_status(mfg_plan* plan);
 
+/* Diagnostics (no MatFlat counterpart): out[i] = a[i] * b[i] computed by the integer-pipe
+ * product the dot products use, for n elements (device pointers, asynchronous on the context's
+ * stream).  It must equal the IEEE round-to-nearest product bit for bit; the tests check it on
+ * random and edge-case operands. */
+MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
+                              int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@ from ._api import (  # noqa: F401
     context,
     library,
     library_path,
+    selftest_dmul,
 )
 
 __version__ = "0.1.0"

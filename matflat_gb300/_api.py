@@ -43,6 +43,7 @@ _SIGS = {
     "mfg_plan_status": (_I, [_vp]),
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
 }
 
 _lib = None
@@ -438,3 +439,10 @@ class QrBatch(_Batch):
         fn = self.ctx.lib.mfg_sgeqrf_batched if single else self.ctx.lib.mfg_dgeqrf_batched
         rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
         self.ctx.check(rc, "mfg_geqrf_batched")
+
+
+def selftest_dmul(a, b, out):
+    """out = a * b through the integer-pipe product (device tensors of float64)."""
+    ctx = context()
+    ctx.check(ctx.lib.mfg_selftest_dmul(ctx.h, _dptr(a), _dptr(b), _dptr(out), a.numel()),
+              "mfg_selftest_dmul")

@@ -113,6 +113,21 @@ __global__ void getri_single_kernel(double* a, int n, int lda, const int* piv, d
   }
 }
 
+__global__ void selftest_mul_kernel(const double* a, const double* b, double* out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = imul_rn(a[i], b[i]);
+}
+
+cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  selftest_mul_kernel<<<(unsigned)blocks, 256, 0, s>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_trsv_single(int uplo, int trans, int n, const double* a, int lda, double* x,
                                int incx, double* scratch, cudaStream_t s) {
   trsv_single_kernel<<<1, 32, 0, s>>>(uplo, trans, n, a, lda, x, incx, scratch);

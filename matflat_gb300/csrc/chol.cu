@@ -20,6 +20,7 @@ namespace mfg {
 
 // Factors the n-by-n matrix a (leading dimension lda) in place.  dsum: n doubles of per-warp
 // scratch.  Returns 0, or k+1 when A is not positive definite at column k.
+template <bool IM>
 __device__ int potrf_warp(double* a, int n, long long lda, double* dsum) {
   const int lane = threadIdx.x & 31;
   for (int j = lane; j < n; j += 32) dsum[j] = 0.0;
@@ -33,7 +34,7 @@ __device__ int potrf_warp(double* a, int n, long long lda, double* dsum) {
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += 32) {
       // Dot(k, a + j, lda, a + k, lda): row j of L against row k of L.
-      const double d = exact_dot(k, a + j, lda, a + k, lda);
+      const double d = exact_dot<IM>(k, a + j, lda, a + k, lda);
       const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], d), lkk);
       colk[j] = t;
       dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
@@ -76,7 +77,7 @@ __device__ void potrs_warp(const double* l, int n, long long lda, double* b, lon
 
 constexpr int SMEM_WARP_DOUBLES_C = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 
-template <int WARPS>
+template <int WARPS, bool IM>
 __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   const int warp = threadIdx.x >> 5;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
     double* scr = (n <= SMEM_N) ? sm_dyn + warp * SMEM_WARP_DOUBLES_C
                                  : p.gscratch + gw * p.gscratch_stride;
     const int ldx = n | 1;
-    const int info = potrf_warp(a, n, lda, scr);
+    const int info = potrf_warp<IM>(a, n, lda, scr);
     if (info == 0 && p.nrhs > 0)
       potrs_warp(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, scr + n, scr + n + RHS_CHUNK * ldx);
     if (lane == 0) p.info[mat] = info;
@@ -104,22 +105,28 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
 
 __global__ void __launch_bounds__(32) potrf_single_kernel(double* a, int n, int lda, int* out1,
                                                           double* scratch) {
-  const int info = potrf_warp(a, n, lda, scratch);
+  const int info = potrf_warp<true>(a, n, lda, scratch);
   if (threadIdx.x == 0) out1[0] = info;
 }
 
 template <int WARPS>
 static cudaError_t launch_potrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES_C * WARPS;
-  potrf_batched_kernel<WARPS><<<ctas, WARPS * 32, smem, s>>>(args);
+  if (args.hw_mul)
+    potrf_batched_kernel<WARPS, false><<<ctas, WARPS * 32, smem, s>>>(args);
+  else
+    potrf_batched_kernel<WARPS, true><<<ctas, WARPS * 32, smem, s>>>(args);
   return cudaGetLastError();
 }
 
 template <int WARPS>
 static cudaError_t set_potrf_attr() {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES_C * WARPS;
-  return cudaFuncSetAttribute(potrf_batched_kernel<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(potrf_batched_kernel<WARPS, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 // Raises the dynamic shared-memory limit of every variant; called once per device, outside any

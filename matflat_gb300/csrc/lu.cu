@@ -100,6 +100,7 @@ __device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long l
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m doubles of per-warp scratch.  Returns Lu's sign in `sign` and in
 // `info` the first zero pivot (k+1), or 0.
+template <bool IM>
 __device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double* scol, int& sign,
                         int& info) {
   const int lane = threadIdx.x & 31;
@@ -121,7 +122,7 @@ __device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double
       const double* x = isrow ? rowk : a + idx;
       const double* y = isrow ? a + (long long)idx * lda : colk1;
       const int len = isrow ? k : k - 1;
-      const double s = exact_dot(len, x, lda, y, 1);
+      const double s = exact_dot<IM>(len, x, lda, y, 1);
       if (isrow) {
         double* dst = a + (long long)idx * lda + k;
         *dst = __dsub_rn(*dst, s);
@@ -163,7 +164,7 @@ __device__ void getrs_warp(const double* lu, int n, long long lda, const int* pi
 
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 
-template <int WARPS>
+template <int WARPS, bool IM>
 __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   const int warp = threadIdx.x >> 5;
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
                                  : p.gscratch + gw * p.gscratch_stride;
     const int ldx = n | 1;
     int sign, info;
-    lu_warp(a, n, n, lda, piv, scr, sign, info);
+    lu_warp<IM>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
 __global__ void __launch_bounds__(32) getrf_single_kernel(double* a, int m, int n, int lda,
                                                           int* piv, int* out2, double* scratch) {
   int sign, info;
-  lu_warp(a, m, n, lda, piv, scratch, sign, info);
+  lu_warp<true>(a, m, n, lda, piv, scratch, sign, info);
   if (threadIdx.x == 0) {
     out2[0] = sign;
     out2[1] = info;
@@ -208,15 +209,21 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(double* a, int m, int 
 template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
-  getrf_batched_kernel<WARPS><<<ctas, WARPS * 32, smem, s>>>(args);
+  if (args.hw_mul)
+    getrf_batched_kernel<WARPS, false><<<ctas, WARPS * 32, smem, s>>>(args);
+  else
+    getrf_batched_kernel<WARPS, true><<<ctas, WARPS * 32, smem, s>>>(args);
   return cudaGetLastError();
 }
 
 template <int WARPS>
 static cudaError_t set_getrf_attr() {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
-  return cudaFuncSetAttribute(getrf_batched_kernel<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(getrf_batched_kernel<WARPS, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 // Raises the dynamic shared-memory limit of every variant; called once per device, outside any

@@ -19,28 +19,6 @@ namespace mfg {
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
-// Internals.Dot (MatFlat/Internals.cs:265-292): for an odd length the first product seeds the
-// sum, then every following pair is added as sum = sum + (x_a*y_a + x_b*y_b); an even length
-// starts from sum = 0.0.  x and y are strided.  Reproduced operation for operation.
-__device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
-                                            const double* y, long long incy) {
-  double s = 0.0;
-  if (len & 1) {
-    s = __dmul_rn(x[0], y[0]);
-    x += incx;
-    y += incy;
-  }
-  const int pairs = len >> 1;
-#pragma unroll 4
-  for (int p = 0; p < pairs; ++p) {
-    const double q = __dadd_rn(__dmul_rn(x[0], y[0]), __dmul_rn(x[incx], y[incy]));
-    s = __dadd_rn(s, q);
-    x += 2 * incx;
-    y += 2 * incy;
-  }
-  return s;
-}
-
 // Same tree, float data widened to double (Internals.cs:236-263).  Products of two widened
 // floats are exact in double.
 __device__ __forceinline__ double exact_dot_f(int len, const float* x, long long incx,
@@ -103,4 +81,76 @@ __device__ __forceinline__ int warp_argmax(unsigned long long key, int idx) {
   return idx;
 }
 
+// Internals.Dot (MatFlat/Internals.cs:265-292): for an odd length the first product seeds the
+// sum, then every following pair is added as sum = sum + (x_a*y_a + x_b*y_b); an even length
+// starts from sum = 0.0.  x and y are strided.  Reproduced operation for operation.
+//
+// The operands usually come from L2, so the loop is software-pipelined: the loads of the next
+// block of DOT_BLOCK pairs are issued before the arithmetic of the current block, which keeps
+// 2*DOT_BLOCK loads per operand in flight while the (slow) FP64 pipe works.
+constexpr int DOT_BLOCK = 4;
+
+// The product used by the dot trees: the hardware DMUL (IM = false) or the integer-pipe product
+// imul_rn (IM = true); both return the correctly rounded product, bit for bit.
+template <bool IM>
+__device__ __forceinline__ double xmul(double a, double b);
+
+template <bool IM = true>
+__device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
+                                            const double* y, long long incy) {
+  double s = 0.0;
+  if (len & 1) {
+    s = xmul<IM>(x[0], y[0]);
+    x += incx;
+    y += incy;
+  }
+  const int pairs = len >> 1;
+  const int blocks = pairs / DOT_BLOCK;
+  if (blocks > 0) {
+    double xa[2 * DOT_BLOCK], ya[2 * DOT_BLOCK];
+#pragma unroll
+    for (int u = 0; u < 2 * DOT_BLOCK; ++u) {
+      xa[u] = x[u * incx];
+      ya[u] = y[u * incy];
+    }
+    x += 2 * DOT_BLOCK * incx;
+    y += 2 * DOT_BLOCK * incy;
+    for (int blk = 0; blk < blocks; ++blk) {
+      double xb[2 * DOT_BLOCK], yb[2 * DOT_BLOCK];
+      const bool more = blk + 1 < blocks;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 2 * DOT_BLOCK; ++u) {
+          xb[u] = x[u * incx];
+          yb[u] = y[u * incy];
+        }
+        x += 2 * DOT_BLOCK * incx;
+        y += 2 * DOT_BLOCK * incy;
+      }
+#pragma unroll
+      for (int u = 0; u < DOT_BLOCK; ++u) {
+        const double q = __dadd_rn(xmul<IM>(xa[2 * u], ya[2 * u]),
+                                   xmul<IM>(xa[2 * u + 1], ya[2 * u + 1]));
+        s = __dadd_rn(s, q);
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 2 * DOT_BLOCK; ++u) {
+          xa[u] = xb[u];
+          ya[u] = yb[u];
+        }
+      }
+    }
+  }
+  for (int p = blocks * DOT_BLOCK; p < pairs; ++p) {
+    const double q = __dadd_rn(xmul<IM>(x[0], y[0]), xmul<IM>(x[incx], y[incy]));
+    s = __dadd_rn(s, q);
+    x += 2 * incx;
+    y += 2 * incy;
+  }
+  return s;
+}
+
 }  // namespace mfg
+
+#include "mf_imul.cuh"

@@ -1,0 +1,62 @@
+// Correctly rounded double-precision product on the integer pipes.
+//
+// Why: on GB300 the FP64 pipe issues one warp-wide DMUL/DADD every ~77 cycles per SM
+// sub-partition (1/73 of the FP32 rate), while 32-bit integer multiply-add runs ~38x faster.
+// MatFlat's exact operation order needs two separately rounded FP64 instructions per multiply-add
+// (no FMA), so moving the multiplies to the integer pipes lets both pipes work at once.
+//
+// Method: IEEE 754 round-to-nearest-even multiplication from its definition.  For normal a, b
+// with significands Ma, Mb in [2^52, 2^53), P = Ma*Mb is an exact 105/106-bit integer; the result
+// significand is P's top 53 bits, rounded up when the next bit (round) is 1 and either any lower
+// bit (sticky) is 1 or the kept significand is odd.  The exponent is ea + eb - 1023 (+1 when
+// P >= 2^105); a carry out of the rounding is absorbed by adding the significand, implicit bit
+// included, onto (exponent - 1) << 52.  Operands or results outside the normal range (zeros,
+// subnormals, infinities, NaN, overflow, underflow) take the hardware __dmul_rn instead, so the
+// function returns exactly __dmul_rn(a, b) for every input.  The low 64 bits of the 128-bit
+// product are needed only to break a possible tie, so they are computed only then.
+#pragma once
+
+#include "mf_device.cuh"
+
+namespace mfg {
+
+__device__ __forceinline__ double imul_rn(double a, double b) {
+  const unsigned long long A = dbits(a), B = dbits(b);
+  const int ea = (int)((A >> 52) & 0x7FF);
+  const int eb = (int)((B >> 52) & 0x7FF);
+  const int e = ea + eb - 1023;
+  // Fast path: ea, eb in [1, 2046] and e in [1, 2044] (so e + 1 + rounding carry <= 2046).
+  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(e - 1) >= 2044u)
+    return __dmul_rn(a, b);
+  const unsigned long long ma = (A << 11) | 0x8000000000000000ull;  // Ma << 11
+  const unsigned long long mb = (B << 11) | 0x8000000000000000ull;  // Mb << 11
+  const unsigned long long hi = __umul64hi(ma, mb);                 // P >> 42
+  const unsigned top = (unsigned)(hi >> 63);                         // P >= 2^105
+  const unsigned sh = 10u + top;
+  unsigned long long mant = hi >> sh;                                // 53 bits
+  const unsigned long long below = hi & ((1ull << sh) - 1ull);       // round bit + high sticky
+  const unsigned long long half = 1ull << (sh - 1u);
+  bool up;
+  if (below != half) {
+    up = below > half;
+  } else {
+    // Round bit set and the sticky bits inside hi clear: the rest of P decides.
+    const unsigned long long lo = ma * mb;                           // (P << 22) mod 2^64
+    up = (lo != 0ull) || (mant & 1ull);
+  }
+  mant += up ? 1ull : 0ull;
+  const unsigned long long r = ((A ^ B) & 0x8000000000000000ull) |
+                               ((((unsigned long long)(e + (int)top - 1)) << 52) + mant);
+  return __longlong_as_double((long long)r);
+}
+
+template <>
+__device__ __forceinline__ double xmul<false>(double a, double b) {
+  return __dmul_rn(a, b);
+}
+template <>
+__device__ __forceinline__ double xmul<true>(double a, double b) {
+  return imul_rn(a, b);
+}
+
+}  // namespace mfg

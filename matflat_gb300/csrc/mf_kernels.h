@@ -35,6 +35,8 @@ struct BatchArgs {
   int* queue;                // work counter, zeroed before every launch
   double* gscratch;          // per-warp scratch for n > SMEM_N
   long long gscratch_stride; // doubles per warp in gscratch
+  int hw_mul;                // 1: dot products multiply on the FP64 pipe (DMUL) instead of the
+                             // integer pipes; both give identical bits
 };
 
 // Batched Householder QR (+ least-squares solve of nrhs right-hand sides, ldb = m).
@@ -68,6 +70,10 @@ cudaError_t launch_qr_q_single(const T* a, int m, int n, int lda, T* q, int ldq,
 template <typename T>
 cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const T* rdiag,
                                cudaStream_t s);
+
+// Diagnostics: out[i] = the integer-pipe product of a[i] and b[i] (device pointers).
+cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
+                                cudaStream_t s);
 
 // One-time per-device set-up of kernel attributes (dynamic shared-memory limits).
 cudaError_t init_getrf_attributes();

@@ -102,7 +102,11 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, T* rdiag, T* b, long 
         coefs[c] = A::coef(A::dot(len, ck + k, cj + k), v0);
       }
       __syncwarp();
-      const long long work = (long long)len * ncols;
+      // Right-hand sides skip a degenerate reflector (v[0] == 0 means v == 0 and the reflector
+      // is the identity), as QrOrthogonalFactor does for the columns of Q (Qr.cs:406); the
+      // factored columns follow Qr itself, which does not skip.
+      const int upd = A::nz(v0) ? ncols : (n - k - 1);
+      const long long work = (long long)len * upd;
       for (long long e = lane; e < work; e += 32) {
         const int c = (int)(e / len);
         const int r = k + (int)(e - (long long)c * len);

@@ -123,11 +123,32 @@ size_t span(long long m, long long n, long long ld) {
   return (size_t)(ld * (n - 1) + m);
 }
 
+// Execution order of a batch.  Pure longest-first puts thousands of the largest matrices in
+// flight at once, whose combined working set (up to 128 KB each) overflows the 129 MB L2 and turns
+// every re-read of L and U into a DRAM access.  The "snake" order pairs the i-th largest with the
+// i-th smallest matrix (L0 S0 L1 S1 ...), so the matrices in flight average out, and the
+// mid-sized ones come last, which keeps the tail short.  MFG_ORDER=lpt selects longest-first.
+std::vector<int> snake_order(int count, const int* n) {
+  std::vector<int> sorted(count);
+  std::iota(sorted.begin(), sorted.end(), 0);
+  std::stable_sort(sorted.begin(), sorted.end(), [&](int x, int y) { return n[x] > n[y]; });
+  const char* mode = std::getenv("MFG_ORDER");
+  if (mode && std::strcmp(mode, "lpt") == 0) return sorted;
+  std::vector<int> out;
+  out.reserve(count);
+  int lo = 0, hi = count - 1;
+  while (lo <= hi) {
+    out.push_back(sorted[lo++]);
+    if (lo <= hi) out.push_back(sorted[hi--]);
+  }
+  return out;
+}
+
 // Launch shape of a batched plan: WARPS warps per CTA and enough CTAs to hold `warps_per_sm`
 // warps on every SM (persistent: each warp pulls matrices from the queue until it is empty).
 void choose_shape(mfg_plan* p) {
   const int warps = env_int("MFG_WARPS_PER_CTA", 4);
-  const int wps = env_int("MFG_WARPS_PER_SM", 16);
+  const int wps = env_int("MFG_WARPS_PER_SM", 8);
   p->warps = warps;
   const long long total_warps = (long long)p->ctx->sm_count * wps;
   long long ctas = total_warps / warps;
@@ -229,10 +250,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   p->ctx = ctx;
   p->count = count;
   p->nrhs = nrhs;
-  std::vector<int> order(count);
-  std::iota(order.begin(), order.end(), 0);
-  // Longest first (work grows as n^3): the persistent warps then finish close together.
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  std::vector<int> order = snake_order(count, n);
   int max_n = 0;
   for (int i = 0; i < count; i++) max_n = std::max(max_n, n[i]);
   p->max_n = max_n;
@@ -296,6 +314,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.queue = d_queue;
   a.gscratch = (double*)p->scratch.ptr;
   a.gscratch_stride = stride;
+  a.hw_mul = env_int("MFG_HW_MUL", 0);
   *out = p;
   return MFG_OK;
 }
@@ -901,6 +920,15 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) 
   plan->args.sign = nullptr;
   plan->args.info = info;
   return plan_execute(plan, a, b, info, nullptr, nullptr);
+}
+
+MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
+                              int64_t n) {
+  if (!ctx) return -1;
+  if (n < 0) return fail(ctx, -5, "n must be >= 0");
+  if (n > 0 && (!a || !b || !out)) return fail(ctx, !a ? -2 : (!b ? -3 : -4), "null pointer");
+  MFG_CUDA(ctx, mfg::launch_selftest_mul(a, b, out, n, ctx->stream));
+  return MFG_OK;
 }
 
 MFG_API int mfg_plan_status(mfg_plan* plan) {

@@ -1,0 +1,51 @@
+"""The integer-pipe double product (used by every dot product of the factorizations) must equal
+the IEEE 754 round-to-nearest-even product bit for bit, on every class of operand."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _operands(rng, n):
+    parts = []
+    # ordinary values
+    parts.append((rng.standard_normal(n), rng.standard_normal(n)))
+    # uniformly random bit patterns: every exponent, subnormals, infinities, NaNs
+    parts.append((rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64),
+                  rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64)))
+    # short significands: products with <= 54 significant bits hit exact halfway cases
+    def short(k):
+        bits = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+        bits &= ~np.uint64((1 << (52 - k)) - 1)
+        bits = (bits & np.uint64(0x800FFFFFFFFFFFFF)) | np.uint64(0x3FF0000000000000)
+        return bits.view(np.float64) * rng.choice([1.0, -1.0, 2.0 ** 40, 2.0 ** -40], n)
+    parts.append((short(26), short(27)))
+    parts.append((short(20), short(33)))
+    # exponents at the edges of the normal range (overflow / underflow / subnormal results)
+    e1 = rng.integers(-1100, 1100, n).astype(np.float64)
+    e2 = -e1 + rng.integers(-60, 60, n)
+    parts.append((np.ldexp(1.0 + rng.random(n), e1.astype(int)),
+                  np.ldexp(1.0 + rng.random(n), np.clip(e2, -1100, 1100).astype(int))))
+    a = np.concatenate([p[0] for p in parts] + [np.array([0.0, -0.0, np.inf, -np.inf, np.nan,
+                                                          5e-324, 1.0, 2.0 ** 1023, 2.0 ** -1022])])
+    b = np.concatenate([p[1] for p in parts] + [np.array([3.0, -2.0, 0.0, -1.0, 1.0, 0.5, 5e-324,
+                                                          2.0, 0.5])])
+    return a, b
+
+
+def test_integer_product_is_ieee(mf):
+    import torch
+    rng = np.random.default_rng(99)
+    a, b = _operands(rng, 1 << 20)
+    da = torch.from_numpy(a).cuda()
+    db = torch.from_numpy(b).cuda()
+    out = torch.empty_like(da)
+    mf.selftest_dmul(da, db, out)
+    mf.context().synchronize()
+    got = out.cpu().numpy()
+    with np.errstate(all="ignore"):
+        exp = a * b          # host IEEE multiply, round to nearest even
+    gn, en = np.isnan(got), np.isnan(exp)
+    np.testing.assert_array_equal(gn, en)
+    bad = np.nonzero(got.view(np.uint64)[~gn] != exp.view(np.uint64)[~en])[0]
+    assert bad.size == 0, (a[~gn][bad[:5]], b[~gn][bad[:5]], got[~gn][bad[:5]], exp[~en][bad[:5]])
