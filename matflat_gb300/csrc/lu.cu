@@ -100,7 +100,7 @@ __device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long l
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m doubles of per-warp scratch.  Returns Lu's sign in `sign` and in
 // `info` the first zero pivot (k+1), or 0.
-template <bool IM>
+template <bool IM, int DB = DOT_BLOCK>
 __device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double* scol, int& sign,
                         int& info) {
   const int lane = threadIdx.x & 31;
@@ -122,7 +122,7 @@ __device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double
       const double* x = isrow ? rowk : a + idx;
       const double* y = isrow ? a + (long long)idx * lda : colk1;
       const int len = isrow ? k : k - 1;
-      const double s = exact_dot<IM>(len, x, lda, y, 1);
+      const double s = exact_dot<IM, DB>(len, x, lda, y, 1);
       if (isrow) {
         double* dst = a + (long long)idx * lda + k;
         *dst = __dsub_rn(*dst, s);
@@ -164,7 +164,7 @@ __device__ void getrs_warp(const double* lu, int n, long long lda, const int* pi
 
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 
-template <int WARPS, bool IM>
+template <int WARPS, bool IM, int DB>
 __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   const int warp = threadIdx.x >> 5;
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
                                  : p.gscratch + gw * p.gscratch_stride;
     const int ldx = n | 1;
     int sign, info;
-    lu_warp<IM>(a, n, n, lda, piv, scr, sign, info);
+    lu_warp<IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);
@@ -210,19 +210,29 @@ template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
   if (args.hw_mul)
-    getrf_batched_kernel<WARPS, false><<<ctas, WARPS * 32, smem, s>>>(args);
+    getrf_batched_kernel<WARPS, false, 4><<<ctas, WARPS * 32, smem, s>>>(args);
+  else if (args.dot_block == 8)
+    getrf_batched_kernel<WARPS, true, 8><<<ctas, WARPS * 32, smem, s>>>(args);
+  else if (args.dot_block == 2)
+    getrf_batched_kernel<WARPS, true, 2><<<ctas, WARPS * 32, smem, s>>>(args);
   else
-    getrf_batched_kernel<WARPS, true><<<ctas, WARPS * 32, smem, s>>>(args);
+    getrf_batched_kernel<WARPS, true, 4><<<ctas, WARPS * 32, smem, s>>>(args);
   return cudaGetLastError();
 }
 
 template <int WARPS>
 static cudaError_t set_getrf_attr() {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
-  cudaError_t e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true>,
+  cudaError_t e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 4>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(getrf_batched_kernel<WARPS, false>,
+  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 8>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 2>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(getrf_batched_kernel<WARPS, false, 4>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 

@@ -95,7 +95,7 @@ constexpr int DOT_BLOCK = 4;
 template <bool IM>
 __device__ __forceinline__ double xmul(double a, double b);
 
-template <bool IM = true>
+template <bool IM = true, int DOT_BLOCK = mfg::DOT_BLOCK>
 __device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
                                             const double* y, long long incy) {
   double s = 0.0;

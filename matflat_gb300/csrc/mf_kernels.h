@@ -37,6 +37,8 @@ struct BatchArgs {
   long long gscratch_stride; // doubles per warp in gscratch
   int hw_mul;                // 1: dot products multiply on the FP64 pipe (DMUL) instead of the
                              // integer pipes; both give identical bits
+  int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
+  int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4, 8)
 };
 
 // Batched Householder QR (+ least-squares solve of nrhs right-hand sides, ldb = m).

@@ -148,7 +148,7 @@ std::vector<int> snake_order(int count, const int* n) {
 // warps on every SM (persistent: each warp pulls matrices from the queue until it is empty).
 void choose_shape(mfg_plan* p) {
   const int warps = env_int("MFG_WARPS_PER_CTA", 4);
-  const int wps = env_int("MFG_WARPS_PER_SM", 8);
+  const int wps = env_int("MFG_WARPS_PER_SM", 16);
   p->warps = warps;
   const long long total_warps = (long long)p->ctx->sm_count * wps;
   long long ctas = total_warps / warps;
@@ -292,10 +292,19 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
   }
   choose_shape(p);
+  // Cholesky runs G lanes per matrix (32/G matrices per warp); small orders use small groups so
+  // the per-column square root and the serial solve steps are shared by several matrices.
+  int group = 32;
+  if (kind == mfg_plan::POTRF) {
+    group = env_int("MFG_CHOL_GROUP", max_n <= 16 ? 4 : max_n <= 32 ? 8 : max_n <= 64 ? 16 : 32);
+    if (group != 4 && group != 8 && group != 16 && group != 32) group = 32;
+  }
+  const int smem_n = kind == mfg_plan::POTRF ? 4 * group : mfg::SMEM_N;
   long long stride = 0;
-  if (max_n > mfg::SMEM_N) {
+  if (max_n > smem_n) {
     stride = (mfg::warp_scratch_doubles(max_n) + 31) / 32 * 32;
-    const size_t sbytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps;
+    const size_t sbytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps *
+                          (size_t)(32 / group);
     e = p->scratch.reserve(sbytes);
     if (e != cudaSuccess) {
       delete p;
@@ -315,6 +324,8 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.gscratch = (double*)p->scratch.ptr;
   a.gscratch_stride = stride;
   a.hw_mul = env_int("MFG_HW_MUL", 0);
+  a.group = group;
+  a.dot_block = env_int("MFG_DOT_BLOCK", 4);
   *out = p;
   return MFG_OK;
 }
