@@ -181,6 +181,25 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan);
  * context's stream): MFG_OK, or MFG_ERR_TIMEOUT if a bounded device-side wait gave up. */
 MFG_API int mfg_plan_status(mfg_plan* plan);
 
+/* Allocation-free batched LU + solve (no counterpart in the reference: MatFlat has no batched
+ * or GPU API).  For callers that cannot allocate device memory — code running inside a stream
+ * capture they do not own, real-time paths whose memory is fixed at start-up, hosts that hand the
+ * library a fixed arena — this entry point calls no cudaMalloc, cudaFree or allocating library
+ * routine.  It factors `count` matrices of one order n (Factorization.Lu) and, when nrhs > 0,
+ * solves A x = b exactly as mfg_dgetrf_batched does, bit for bit.  Matrix i is at
+ * a + i*stride_a (leading dimension lda), its pivots at piv + i*stride_piv, its nrhs right-hand
+ * sides at b + i*stride_b (leading dimension n); sign[i] and info[i] as in mfg_dgetrf_batched.
+ * All pointers are device pointers; the call is asynchronous on the context's stream.
+ * Limit: n <= 256 (larger n returns MFG_ERR_UNSUPPORTED before anything is launched).
+ * The kernel's scratch lives in one static device array of 11.4 MB (10.8 MiB) that every GPU
+ * loading the library keeps until exit.  The first call on a device looks up that array's address and
+ * should come before any stream capture.  Calls share the array: calls that overlap on the GPU
+ * (different streams or contexts on one device) race and must be serialised by the caller. */
+MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, double* a,
+                                              int lda, int64_t stride_a, int* piv,
+                                              int64_t stride_piv, int nrhs, double* b,
+                                              int64_t stride_b, int* sign, int* info);
+
 /* Diagnostics (no MatFlat counterpart): out[i] = a[i] * b[i] computed by the integer-pipe
  * product the dot products use, for n elements (device pointers, asynchronous on the context's
  * stream).  It must equal the IEEE round-to-nearest product bit for bit; the tests check it on

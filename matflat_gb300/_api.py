@@ -44,6 +44,9 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
+    "mfg_dgetrf_strided_batched_noalloc": (_I, [_vp, _I, _I, _vp, _I, ctypes.c_int64, _vp,
+                                                ctypes.c_int64, _I, _vp, ctypes.c_int64, _vp,
+                                                _vp]),
 }
 
 _lib = None

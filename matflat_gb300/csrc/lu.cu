@@ -19,6 +19,8 @@
 // being factored): on GB300 the FP64 pipe, not memory, bounds this kernel.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_solve.cuh"
@@ -261,6 +263,134 @@ cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cud
 cudaError_t launch_getrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
                                 double* scratch, cudaStream_t s) {
   getrf_single_kernel<<<1, 32, 0, s>>>(a, m, n, lda, piv, out2, scratch);
+  return cudaGetLastError();
+}
+
+}  // namespace mfg
+
+namespace mfg {
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free variant for callers that must not allocate device memory.
+//
+// Some callers of this library cannot call cudaMalloc: code that runs inside a CUDA stream capture
+// owned by someone else, real-time or certified paths whose memory is budgeted once at start-up,
+// and hosts that hand the library a fixed device arena.  For them the batched LU + solve has a
+// second entry point that allocates nothing: the caller passes the matrices, pivots, right-hand
+// sides and outputs (device pointers, one order n for the whole batch, fixed strides), and the
+// kernel's scratch — the work-queue counter and, for n > 128, the per-warp column sums and staged
+// right-hand sides — lives in the file-scope array below, which every GPU that loads the library
+// holds until the process exits.
+//
+// Limits: n <= NOALLOC_MAX_N (256); for n > 128 at most NOALLOC_MAX_WARPS warps run, each with a
+// NOALLOC_WARP_STRIDE-double slice; the array is 11.4 MB.  Every call shares the array and keeps
+// the previous call's contents, so the counter is cleared (cudaMemsetAsync) before each launch,
+// and calls that overlap on the GPU (two streams, or two contexts on one device) race on it.
+constexpr int NOALLOC_MAX_N = 256;
+constexpr int NOALLOC_MAX_WARPS = 608;
+constexpr long long NOALLOC_HEADER_DOUBLES = 32;  // 256 bytes: the work-queue counter
+constexpr long long NOALLOC_WARP_STRIDE =
+    ((NOALLOC_MAX_N + 2LL * RHS_CHUNK * (NOALLOC_MAX_N + 1) + 2) + 31) / 32 * 32;
+constexpr long long NOALLOC_SCRATCH_DOUBLES =
+    NOALLOC_HEADER_DOUBLES + (long long)NOALLOC_MAX_WARPS * NOALLOC_WARP_STRIDE;
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+struct StridedArgs {
+  double* a;
+  long long stride_a;
+  int* piv;
+  long long stride_piv;
+  double* b;
+  long long stride_b;
+  int* sign;
+  int* info;
+  int n;
+  int lda;
+  int nrhs;
+  int count;
+  double* scratch;  // device address of g_noalloc_scratch
+};
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) getrf_strided_noalloc_kernel(StridedArgs p) {
+  extern __shared__ double sm_dyn[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  int* queue = reinterpret_cast<int*>(p.scratch);
+  const int n = p.n;
+  const long long lda = p.lda;
+  const int ldx = n | 1;
+  double* scr = (n <= SMEM_N) ? sm_dyn + warp * SMEM_WARP_DOUBLES
+                               : p.scratch + NOALLOC_HEADER_DOUBLES + gw * NOALLOC_WARP_STRIDE;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    double* a = p.a + (long long)idx * p.stride_a;
+    int* piv = p.piv + (long long)idx * p.stride_piv;
+    int sign, info;
+    lu_warp<true>(a, n, n, lda, piv, scr, sign, info);
+    if (p.nrhs > 0)
+      getrs_warp(a, n, lda, piv, p.b + (long long)idx * p.stride_b, n, p.nrhs, scr + n,
+                 scr + n + RHS_CHUNK * ldx);
+    if (lane == 0) {
+      p.sign[idx] = sign;
+      p.info[idx] = info;
+    }
+    __syncwarp();
+  }
+}
+
+// Set-up: the device address of g_noalloc_scratch, looked up once per device with that device
+// current (in host code the array's name is only a host-side stand-in, never a device address).
+static void* g_noalloc_ptr[64];
+static std::once_flag g_noalloc_once[64];
+static cudaError_t g_noalloc_err[64];
+
+static cudaError_t noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  std::call_once(g_noalloc_once[device], [device]() {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e == cudaSuccess) {
+      const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * 4;
+      e = cudaFuncSetAttribute(getrf_strided_noalloc_kernel<4>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    g_noalloc_err[device] = e;
+    g_noalloc_ptr[device] = (e == cudaSuccess) ? ptr : nullptr;
+  });
+  *out = (double*)g_noalloc_ptr[device];
+  return g_noalloc_err[device];
+}
+
+int noalloc_max_n() { return NOALLOC_MAX_N; }
+
+cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,
+                                         long long stride_piv, int nrhs, double* b,
+                                         long long stride_b, int* sign, int* info, int count,
+                                         int sm_count, cudaStream_t s) {
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return e;
+  double* scratch = nullptr;
+  e = noalloc_scratch(device, &scratch);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(scratch, 0, sizeof(double) * NOALLOC_HEADER_DOUBLES, s);
+  if (e != cudaSuccess || count == 0) return e;
+  constexpr int WARPS = 4;
+  long long ctas = (long long)sm_count * (n <= SMEM_N ? 4 : 1);
+  if (n > SMEM_N && ctas * WARPS > NOALLOC_MAX_WARPS) ctas = NOALLOC_MAX_WARPS / WARPS;
+  const long long need = ((long long)count + WARPS - 1) / WARPS;
+  if (ctas > need) ctas = need;
+  if (ctas < 1) ctas = 1;
+  StridedArgs p{a, stride_a, piv, stride_piv, b, stride_b, sign, info, n, lda, nrhs, count,
+                scratch};
+  const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
+  getrf_strided_noalloc_kernel<WARPS><<<(unsigned)ctas, WARPS * 32, smem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -77,6 +77,13 @@ cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const 
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s);
 
+// Allocation-free strided batched LU + solve (scratch in a static device array; see lu.cu).
+int noalloc_max_n();
+cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,
+                                         long long stride_piv, int nrhs, double* b,
+                                         long long stride_b, int* sign, int* info, int count,
+                                         int sm_count, cudaStream_t s);
+
 // One-time per-device set-up of kernel attributes (dynamic shared-memory limits).
 cudaError_t init_getrf_attributes();
 cudaError_t init_potrf_attributes();

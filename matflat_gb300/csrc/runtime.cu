@@ -942,6 +942,34 @@ MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, do
   return MFG_OK;
 }
 
+MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, double* a,
+                                              int lda, int64_t stride_a, int* piv,
+                                              int64_t stride_piv, int nrhs, double* b,
+                                              int64_t stride_b, int* sign, int* info) {
+  if (!ctx) return -1;
+  if (n < 1) return fail(ctx, -2, "n must be >= 1");
+  if (n > mfg::noalloc_max_n())
+    return fail(ctx, MFG_ERR_UNSUPPORTED,
+                "n = %d exceeds the allocation-free limit of %d (use the plan entry points)", n,
+                mfg::noalloc_max_n());
+  if (count < 0) return fail(ctx, -3, "count must be >= 0");
+  if (count > 0 && !a) return fail(ctx, -4, "a is null");
+  if (lda < n) return fail(ctx, -5, "lda = %d < n = %d", lda, n);
+  if (count > 1 && stride_a < (int64_t)lda * n) return fail(ctx, -6, "stride_a too small");
+  if (count > 0 && !piv) return fail(ctx, -7, "piv is null");
+  if (count > 1 && stride_piv < n) return fail(ctx, -8, "stride_piv too small");
+  if (nrhs < 0) return fail(ctx, -9, "nrhs must be >= 0");
+  if (nrhs > 0 && count > 0 && !b) return fail(ctx, -10, "b is null");
+  if (nrhs > 0 && count > 1 && stride_b < (int64_t)n * nrhs)
+    return fail(ctx, -11, "stride_b too small");
+  if (count > 0 && !sign) return fail(ctx, -12, "sign is null");
+  if (count > 0 && !info) return fail(ctx, -13, "info is null");
+  MFG_CUDA(ctx, mfg::launch_getrf_strided_noalloc(a, n, lda, stride_a, piv, stride_piv, nrhs, b,
+                                                  stride_b, sign, info, count, ctx->sm_count,
+                                                  ctx->stream));
+  return MFG_OK;
+}
+
 MFG_API int mfg_plan_status(mfg_plan* plan) {
   if (!plan) return -1;
   MFG_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
