@@ -34,6 +34,10 @@ CONFIGS = {
     "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
                           "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
                  count=10_000, n=32, nrhs=1),
+    "grad": dict(workload="differentiable Cholesky/log-det/solve: loss y^T K^-1 y + log det K and "
+                          "its gradient K^-1 - alpha alpha^T, 4,096 RBF kernel matrices n=128 "
+                          "(x~U[0,1]^3, length 0.3, jitter 1e-6), y~N(0,1), seed 0",
+                 count=4096, n=128),
     "qr": dict(workload="batched FP64 Householder QR (MatFlat order) + least squares, 50,000 "
                         "matrices m~U{64..512}, n~U{16..64}, N(0,1), 1 RHS, seed 0",
                count=50_000, dtype="f64"),
@@ -63,6 +67,18 @@ def chol_flops(n, nrhs):
 def chol_bytes(n, nrhs):
     n = n.astype(np.float64)
     return float(np.sum(16 * n ** 2 + 16 * n * nrhs))
+
+
+def grad_flops(n):
+    """Cholesky forward (n^3/3) plus the adjoint (2n^3/3): n^3 per matrix."""
+    n = n.astype(np.float64)
+    return float(np.sum(n ** 3))
+
+
+def grad_bytes(n):
+    """Read K and y, write L, the gradient, alpha and the loss."""
+    n = n.astype(np.float64)
+    return float(np.sum(24 * n ** 2 + 16 * n + 8))
 
 
 def qr_flops(m, n, nrhs):
@@ -118,7 +134,15 @@ class ClockSampler:
 
     def summary(self):
         if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+            # Timed region shorter than one sampling period: one reading right after it.
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index),
+                                      "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=20).stdout
+                self.samples = [[x.strip() for x in out.strip().split(",")]]
+            except (OSError, subprocess.SubprocessError):
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = []
         mx = None
         reasons = set()
@@ -186,6 +210,8 @@ def make_inputs(cfg_name, rank):
         return synth.lu_batch(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"], seed=rank)
     if cfg_name == "chol":
         return synth.spd_batch(cfg["count"], cfg["n"], cfg["nrhs"], seed=rank)
+    if cfg_name == "grad":
+        return synth.rbf_batch(cfg["count"], cfg["n"], seed=rank)
     return synth.qr_batch(cfg["count"], seed=rank)
 
 
@@ -209,7 +235,7 @@ def cpu_sample_rate(cfg_name, d, budget_s=15.0, threads=None):
 
 
 def run_cpu_sample(cfg_name, d, sample, threads, oracle):
-    if cfg_name in ("lu", "chol"):
+    if cfg_name in ("lu", "chol", "grad"):
         n = d["n"][sample].astype(np.int32)
         sz = n.astype(np.int64) ** 2
         a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
@@ -226,9 +252,15 @@ def run_cpu_sample(cfg_name, d, sample, threads, oracle):
             piv = np.zeros(int(n.sum()), np.int32)
             sign = np.zeros(len(n), np.int32)
             oracle.lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, threads)
-        else:
+        elif cfg_name == "chol":
             info = np.zeros(len(n), np.int32)
             oracle.chol_solve_batched(n, a_off, a, b_off, b, info, threads)
+        else:
+            info = np.zeros(len(n), np.int32)
+            loss = np.zeros(len(n))
+            g = np.zeros_like(a)
+            t0 = time.perf_counter()
+            oracle.chol_grad_batched(n, a_off, a, b_off, b, loss, g, info, threads)
         return time.perf_counter() - t0
     m = d["m"][sample].astype(np.int32)
     n = d["n"][sample].astype(np.int32)
@@ -283,6 +315,7 @@ def run_reference(args, cfg_name):
 def metric_name(cfg_name):
     return {"lu": "batched FP64 LU+solve matrices/s (MatFlat-exact pivots)",
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
+            "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
             "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
             "qr32": "batched FP32 QR least-squares matrices/s (MatFlat-exact factors)"}[cfg_name]
 
@@ -379,7 +412,7 @@ def main():
             flops = lu_flops(d["n"], d["nrhs"])
             byts = lu_bytes(d["n"], d["nrhs"])
             kernel_key = "getrf_batched_kernel"
-        else:
+        elif cfg_name == "chol":
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
 
             def run():
@@ -388,6 +421,17 @@ def main():
             flops = chol_flops(d["n"], d["nrhs"])
             byts = chol_bytes(d["n"], d["nrhs"])
             kernel_key = "potrf_batched_kernel"
+        else:
+            plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
+            loss = torch.zeros(count, dtype=torch.float64, device="cuda")
+            grad = torch.empty_like(a0)
+
+            def run():
+                plan.loss_and_grad(a, b, loss, grad, info, keep_factor=True)
+            outs = [a, b, loss, grad, info]
+            flops = grad_flops(d["n"])
+            byts = grad_bytes(d["n"])
+            kernel_key = "chol_grad_batched_kernel"
         outs_host = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
 
     def restore():

@@ -175,6 +175,23 @@ MFG_API int mfg_plan_geqrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
 MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b);
 MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b);
 
+/* Differentiable Cholesky / log-determinant / solve over a potrf plan with nrhs = 1 (n <= 128).
+ * For every SPD matrix K (upper triangle read, as Factorization.Cholesky) and vector y:
+ *   loss[i] = y^T K^-1 y + log det K,
+ *   grad    = d loss / d K = K^-1 - alpha alpha^T (full symmetric n-by-n, same layout as k),
+ *   y       <- alpha = K^-1 y.
+ * Built from MatFlat's own routines in MatFlat's arithmetic: L = Cholesky(K)
+ * (Factorization.Cholesky.cs:114-168), z = SolveTriangular(Lower, NoTrans), alpha =
+ * SolveTriangular(Lower, Trans) (Blas.SolveTriangular.cs:216-231), K^-1 by the same two solves on
+ * the columns of the identity (the LuInverse idiom, Factorization.LuInverse.cs:174-192), taken
+ * from its upper triangle and mirrored; log det K = 2 * sum log L_ii.
+ * keep_factor = 1: k is overwritten with L.  keep_factor = 0: k is left untouched and L is
+ * recomputed inside grad's storage (no extra memory for the factor).
+ * info[i] = 0, or j+1 when K is not positive definite at column j (loss NaN, grad unspecified). */
+MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, double* y,
+                                                double* loss, double* grad, int* info,
+                                                int keep_factor);
+
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 
 /* Reads back the device-side status word of the last execution of `plan` (synchronizes the

@@ -44,6 +44,7 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
+    "mfg_dpotrf_logdet_solve_grad_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrf_strided_batched_noalloc": (_I, [_vp, _I, _I, _vp, _I, ctypes.c_int64, _vp,
                                                 ctypes.c_int64, _I, _vp, ctypes.c_int64, _vp,
                                                 _vp]),
@@ -411,6 +412,14 @@ class CholeskyBatch(_Batch):
     def run(self, a, b, info):
         rc = self.ctx.lib.mfg_dpotrf_batched(self.h, _dptr(a), _dptr(b), _dptr(info))
         self.ctx.check(rc, "mfg_dpotrf_batched")
+
+    def loss_and_grad(self, k, y, loss, grad, info, keep_factor=True):
+        """loss = y^T K^-1 y + log det K and grad = K^-1 - alpha alpha^T per matrix; y becomes
+        alpha = K^-1 y; with keep_factor, k becomes the Cholesky factor L."""
+        rc = self.ctx.lib.mfg_dpotrf_logdet_solve_grad_batched(
+            self.h, _dptr(k), _dptr(y), _dptr(loss), _dptr(grad), _dptr(info),
+            1 if keep_factor else 0)
+        self.ctx.check(rc, "mfg_dpotrf_logdet_solve_grad_batched")
 
 
 class QrBatch(_Batch):

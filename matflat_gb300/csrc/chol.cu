@@ -198,3 +198,138 @@ cudaError_t launch_potrf_single(double* a, int n, int lda, int* out1, double* sc
 }
 
 }  // namespace mfg
+
+namespace mfg {
+
+// ---------------------------------------------------------------------------------------------
+// Differentiable Cholesky / log-determinant / solve.
+//
+// For each SPD matrix K and vector y the kernel evaluates
+//     loss = y^T K^-1 y + log det K
+// and its gradient with respect to K,
+//     dloss/dK = K^-1 - alpha alpha^T,   alpha = K^-1 y,
+// which is what reverse mode through K = L L^T, z = L^-1 y, loss = z^T z + 2 sum log L_ii gives
+// (L-bar = diag(2/L_ii) - 2 tril(alpha z^T), K-bar = L^-T Phi(L^T L-bar) L^-1, symmetrised).
+// Every quantity is built from MatFlat's own routines, in MatFlat's arithmetic: L by Cholesky,
+// z by SolveTriangular(Lower, NoTrans), alpha by SolveTriangular(Lower, Trans), z^T z by the
+// Internals.Dot tree, and K^-1 column by column by the same two solves applied to the columns of
+// the identity (MatFlat's LuInverse idiom).  K^-1 is taken from its upper triangle (entries i <= j
+// of column j) and mirrored, so the gradient is exactly symmetric; log det K = 2 * sum log L_ii,
+// summed in index order.
+//
+// keep_factor = 1: K is overwritten with L (as Cholesky does) and G receives the gradient.
+// keep_factor = 0: K is left untouched and the factor is recomputed inside G's lower triangle
+// (no buffer for L), K^-1's strict upper triangle goes to G's strict upper triangle and its
+// diagonal to shared memory, and G is completed at the end.
+constexpr int GRAD_SMEM_DOUBLES = 2 * 128 + 2 * RHS_CHUNK * 129 + 8;
+
+__device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double* y, double* loss,
+                               int* info_out, int keep_factor, double* smem) {
+  const int lane = threadIdx.x & 31;
+  double* dsum = smem;                 // n
+  double* kdiag = smem + n;            // n
+  const int ldx = n | 1;
+  double* xs = smem + 2 * n;           // RHS_CHUNK * ldx
+  double* acc = xs + RHS_CHUNK * ldx;  // RHS_CHUNK * ldx
+  double* L;
+  if (keep_factor) {
+    L = K;
+  } else {
+    // Copy K's upper triangle into G and factor there.
+    for (int c = 0; c < n; ++c)
+      for (int r = lane; r <= c; r += 32) G[(long long)c * ld + r] = K[(long long)c * ld + r];
+    __syncwarp();
+    L = G;
+  }
+  // Cholesky in place; for keep_factor = 0 the strict upper triangle of G is cleared by potrf,
+  // which is fine: it is overwritten below.
+  const int info = potrf_group<32, true>(L, n, ld, dsum);
+  if (info != 0) {
+    if (lane == 0) {
+      *info_out = info;
+      *loss = __longlong_as_double(0x7FF8000000000000LL);
+    }
+    __syncwarp();
+    return;
+  }
+  // z = L^-1 y (Lower/NoTrans), quad = z^T z, alpha = L^-T z (Lower/Trans).
+  for (int i = lane; i < n; i += 32) xs[i] = y[i];
+  __syncwarp();
+  warp_solve_dot<32>(L, n, 1, ld, false, xs, ldx, acc, 1);
+  const double quad = exact_dot<true>(n, xs, 1, xs, 1);
+  double logsum = 0.0;
+  for (int i = 0; i < n; ++i) logsum = __dadd_rn(logsum, log(L[(long long)i * ld + i]));
+  warp_solve_sweep<32>(L, n, 1, ld, xs, ldx, 1);
+  for (int i = lane; i < n; i += 32) y[i] = xs[i];  // alpha
+  __syncwarp();
+  if (lane == 0) {
+    *loss = __dadd_rn(quad, __dmul_rn(2.0, logsum));
+    *info_out = 0;
+  }
+  // K^-1 by columns of the identity, RHS_CHUNK at a time; keep entries i <= c of column c.
+  for (int c0 = 0; c0 < n; c0 += RHS_CHUNK) {
+    const int nr = n - c0 < RHS_CHUNK ? n - c0 : RHS_CHUNK;
+    for (int e = lane; e < nr * n; e += 32) {
+      const int r = e / n;
+      const int i = e - r * n;
+      xs[r * ldx + i] = (i == c0 + r) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    warp_solve_dot<32>(L, n, 1, ld, false, xs, ldx, acc, nr);
+    warp_solve_sweep<32>(L, n, 1, ld, xs, ldx, nr);
+    for (int e = lane; e < nr * n; e += 32) {
+      const int r = e / n;
+      const int i = e - r * n;
+      const int c = c0 + r;
+      if (i > c) continue;
+      const double v = xs[r * ldx + i];
+      if (i == c) {
+        kdiag[c] = v;
+      } else {
+        G[(long long)c * ld + i] = v;             // strict upper triangle of G
+      }
+    }
+    __syncwarp();
+  }
+  // G = K^-1 - alpha alpha^T (alpha is in y), symmetric.
+  for (int c = 0; c < n; ++c) {
+    for (int r = lane; r <= c; r += 32) {
+      const double kinv = (r == c) ? kdiag[c] : G[(long long)c * ld + r];
+      const double g = __dsub_rn(kinv, __dmul_rn(y[r], y[c]));
+      G[(long long)c * ld + r] = g;
+    }
+  }
+  __syncwarp();
+  for (int c = 0; c < n; ++c)
+    for (int r = c + 1 + lane; r < n; r += 32) G[(long long)c * ld + r] = G[(long long)r * ld + c];
+  __syncwarp();
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) chol_grad_batched_kernel(BatchArgs p, double* loss,
+                                                                        double* grad,
+                                                                        int keep_factor) {
+  __shared__ double sm[WARPS][GRAD_SMEM_DOUBLES];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    chol_grad_warp(p.a + p.a_off[mat], grad + p.a_off[mat], n, lda, p.b + p.b_off[mat],
+                   loss + mat, p.info + mat, keep_factor, &sm[warp][0]);
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
+                                     int keep_factor, int ctas, cudaStream_t s) {
+  chol_grad_batched_kernel<4><<<ctas, 128, 0, s>>>(args, loss, grad, keep_factor);
+  return cudaGetLastError();
+}
+
+}  // namespace mfg

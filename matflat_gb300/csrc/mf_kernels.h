@@ -77,6 +77,11 @@ cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const 
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s);
 
+// Batched loss = y^T K^-1 y + log det K and its gradient K^-1 - alpha alpha^T (n <= 128; see
+// chol.cu).  Uses args.a (K), args.b (y -> alpha), args.info.
+cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
+                                     int keep_factor, int ctas, cudaStream_t s);
+
 // Allocation-free strided batched LU + solve (scratch in a static device array; see lu.cu).
 int noalloc_max_n();
 cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,

@@ -970,6 +970,38 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
   return MFG_OK;
 }
 
+MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, double* y,
+                                                double* loss, double* grad, int* info,
+                                                int keep_factor) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->nrhs != 1) return fail(ctx, -1, "the plan must have nrhs = 1 (the vector y)");
+  if (plan->max_n > 128)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "matrix order %d > 128 is not supported here",
+                plan->max_n);
+  if (plan->count > 0) {
+    if (!k) return fail(ctx, -2, "k is null");
+    if (!y) return fail(ctx, -3, "y is null");
+    if (!loss) return fail(ctx, -4, "loss is null");
+    if (!grad) return fail(ctx, -5, "grad is null");
+    if (!info) return fail(ctx, -6, "info is null");
+    if ((void*)grad == (void*)k) return fail(ctx, -5, "grad must not alias k");
+  }
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemsetAsync(plan->args.queue, 0, sizeof(int), s));
+  if (plan->count == 0) return MFG_OK;
+  BatchArgs a = plan->args;
+  a.a = k;
+  a.b = y;
+  a.info = info;
+  const long long ctas = std::min<long long>((long long)ctx->sm_count * 4,
+                                             ((long long)plan->count + 3) / 4);
+  MFG_CUDA(ctx, mfg::launch_chol_grad_batched(a, loss, grad, keep_factor ? 1 : 0,
+                                              (int)std::max<long long>(1, ctas), s));
+  return MFG_OK;
+}
+
 MFG_API int mfg_plan_status(mfg_plan* plan) {
   if (!plan) return -1;
   MFG_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));

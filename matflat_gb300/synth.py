@@ -91,3 +91,18 @@ def qr_batch(count, mmin=64, mmax=512, nmin=16, nmax=64, nrhs=1, seed=0):
     b = normal(b_total, seed, stream=9)
     return dict(m=m, n=n, a_off=a_off, a=a, rdiag_off=rdiag_off, rdiag_total=rd_total,
                 b_off=b_off, b=b, nrhs=nrhs)
+
+
+def rbf_batch(count, n=128, length=0.3, jitter=1e-6, seed=0):
+    """Differentiable-Cholesky workload: K_ij = exp(-|x_i - x_j|^2 / (2 length^2)) + jitter
+    delta_ij with x_i ~ U[0,1]^3, and y ~ N(0,1); column-major K per matrix, lda = n."""
+    ns = np.full(count, n, np.int32)
+    x = uniform(count * n * 3, seed, stream=10).reshape(count, n, 3)
+    d2 = ((x[:, :, None, :] - x[:, None, :, :]) ** 2).sum(-1)
+    k = np.exp(-d2 / (2.0 * length * length))
+    k += jitter * np.eye(n)[None, :, :]
+    a = np.ascontiguousarray(np.transpose(k, (0, 2, 1))).reshape(-1)
+    a_off, _ = packed_offsets(ns, ns)
+    b_off, b_total = packed_offsets(ns, np.ones_like(ns))
+    y = normal(b_total, seed, stream=11)
+    return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=y, nrhs=1)

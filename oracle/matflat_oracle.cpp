@@ -908,6 +908,36 @@ void orc_sqr_ls(int m, int n, float* a, int lda, const float* b, float* x) {
   orc_strsv(UPPER, NOTRANS, n, r.data(), n, x, 1);
 }
 
+// Differentiable Cholesky / log-determinant / solve, composed from MatFlat's routines:
+// L = Cholesky(K); z = L^-1 y (SolveTriangular Lower/NoTrans); quad = Internals.Dot(z, z);
+// log det K = 2 * sum_i log L_ii; alpha = L^-T z (SolveTriangular Lower/Trans);
+// K^-1 column c = the same two solves applied to e_c (the LuInverse idiom), upper triangle kept;
+// grad = K^-1 - alpha alpha^T, mirrored to a full symmetric matrix (leading dimension lda).
+// On exit k holds L, y holds alpha.  Returns Cholesky's code (0 = success).
+int orc_dchol_grad(int n, double* k, int lda, double* y, double* loss, double* g) {
+  int info = orc_dcholesky(n, k, lda);
+  if (info != 0) {
+    *loss = std::nan("");
+    return info;
+  }
+  orc_dtrsv(LOWER, NOTRANS, n, k, lda, y, 1);
+  const double quad = dot_d(n, y, 1, y, 1);
+  double logsum = 0.0;
+  for (int i = 0; i < n; i++) logsum = logsum + std::log(k[(long)i * lda + i]);
+  orc_dtrsv(LOWER, TRANS, n, k, lda, y, 1);
+  *loss = quad + 2.0 * logsum;
+  std::vector<double> e(n);
+  for (int c = 0; c < n; c++) {
+    for (int i = 0; i < n; i++) e[i] = (i == c) ? 1.0 : 0.0;
+    orc_dtrsv(LOWER, NOTRANS, n, k, lda, e.data(), 1);
+    orc_dtrsv(LOWER, TRANS, n, k, lda, e.data(), 1);
+    for (int i = 0; i <= c; i++) g[(long)c * lda + i] = e[i] - y[i] * y[c];
+  }
+  for (int c = 0; c < n; c++)
+    for (int r = c + 1; r < n; r++) g[(long)c * lda + r] = g[(long)r * lda + c];
+  return 0;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Batched drivers over std::thread.  Matrices are packed: matrix i starts at a + a_off[i]
 // (elements), has order n[i] and leading dimension n[i]; vectors start at b + b_off[i].
@@ -966,6 +996,15 @@ void orc_dlu_solve_batched(long count, const int* n, const int64_t* a_off, doubl
     int* pi = piv + piv_off[i];
     sign[i] = orc_dlu(ni, ni, ai, ni, pi);
     if (nrhs > 0) orc_dlu_solve(ni, ai, ni, pi, nrhs, b + b_off[i], ni);
+  });
+}
+
+// Config "differentiable Cholesky": per matrix orc_dchol_grad (lda = n); g has the layout of a.
+void orc_dchol_grad_batched(long count, const int* n, const int64_t* a_off, double* a,
+                            const int64_t* b_off, double* y, double* loss, double* g, int* info,
+                            int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    info[i] = orc_dchol_grad(n[i], a + a_off[i], n[i], y + b_off[i], loss + i, g + a_off[i]);
   });
 }
 

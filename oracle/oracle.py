@@ -59,6 +59,8 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_dchol_grad": (_I, [_I, _d, _I, _d, _d, _d]),
+            "orc_dchol_grad_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _d, _i, _I]),
             "orc_dqr_ls_batched": (None, [_L, _i, _i, _l, _d, _l, _d, _l, _d, _I]),
             "orc_sqr_ls_batched": (None, [_L, _i, _i, _l, _f, _l, _f, _l, _f, _I]),
         }
@@ -160,3 +162,17 @@ def qr_ls_batched(m, n, a_off, a, b_off, b, x_off, x, nthreads=1):
     fn = lib().orc_dqr_ls_batched if a.dtype == np.float64 else lib().orc_sqr_ls_batched
     fn(len(m), _p(m, ctypes.c_int), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
        _p(b_off, ctypes.c_int64), _fp(b), _p(x_off, ctypes.c_int64), _fp(x), nthreads)
+
+
+def chol_grad(n, k, lda, y, g):
+    """loss = y^T K^-1 y + log det K and grad K^-1 - alpha alpha^T from MatFlat's routines;
+    k -> L, y -> alpha, g -> grad.  Returns (info, loss)."""
+    loss = ctypes.c_double(0.0)
+    info = lib().orc_dchol_grad(n, _fp(k), lda, _fp(y), ctypes.byref(loss), _fp(g))
+    return info, loss.value
+
+
+def chol_grad_batched(n, a_off, a, b_off, y, loss, g, info, nthreads=1):
+    lib().orc_dchol_grad_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+                                 _p(b_off, ctypes.c_int64), _fp(y), _fp(loss), _fp(g),
+                                 _p(info, ctypes.c_int), nthreads)
