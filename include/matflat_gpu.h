@@ -109,6 +109,35 @@ MFG_API int mfg_sorgqr(mfg_ctx* ctx, int m, int n, const float* a, int lda, floa
 MFG_API int mfg_sqr_r(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* r, int ldr,
                       const float* rdiag);
 
+/* Float and Complex overloads of Lu, Cholesky, Qr, SolveTriangular and MulMatMat, with the
+ * reference arithmetic of each overload: float storage with dots accumulated in double
+ * (Internals.cs:149-176, 236-263); Complex = System.Numerics.Complex as interleaved (re, im)
+ * doubles, every product and sum separately rounded, division by Smith's algorithm, LU pivots by
+ * FastMagnitude |re| + |im| (Internals.cs:16-19).  Complex transposes also accept ConjTrans and
+ * ConjNoTrans.
+ *   Factorization.Lu (Factorization.Lu.cs:45-84 float, :199-238 Complex)
+ *   Factorization.Cholesky (Factorization.Cholesky.cs:33-87 float, :195-249 Complex: A = L L^H)
+ *   Factorization.Qr / QrOrthogonalFactor / QrUpperTriangularFactor Complex
+ *     (Factorization.Qr.cs:198-255, :436-492, :677-730; rdiag is real)
+ *   Blas.SolveTriangular (Blas.SolveTriangular.cs:44-124 float, :280-395 Complex)
+ *   Blas.MulMatMat (Blas.MulMatMat.cs:45-187 float, :407-648 Complex) */
+MFG_API int mfg_sgetrf(mfg_ctx* ctx, int m, int n, float* a, int lda, int* piv, int* sign);
+MFG_API int mfg_zgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign);
+MFG_API int mfg_spotrf(mfg_ctx* ctx, int n, float* a, int lda, int* info);
+MFG_API int mfg_zpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info);
+MFG_API int mfg_zgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag);
+MFG_API int mfg_zorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq);
+MFG_API int mfg_zqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
+                      const double* rdiag);
+MFG_API int mfg_strsv(mfg_ctx* ctx, int uplo, int trans, int n, const float* a, int lda, float* x,
+                      int incx);
+MFG_API int mfg_ztrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
+                      double* x, int incx);
+MFG_API int mfg_sgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const float* a,
+                      int lda, const float* b, int ldb, float* c, int ldc);
+MFG_API int mfg_zgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
+                      int lda, const double* b, int ldb, double* c, int ldc);
+
 /* Blas.SolveTriangular(Uplo, Transpose, int n, double* a, int lda, double* x, int incx)
  * (MatFlat/Blas.SolveTriangular.cs:162-242): non-unit diagonal, NoTrans or Trans. */
 MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,

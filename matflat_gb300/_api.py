@@ -35,6 +35,17 @@ _SIGS = {
     "mfg_dgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dtrsv": (_I, [_vp, _I, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_sgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_zgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_spotrf": (_I, [_vp, _I, _vp, _I, _c_int_p]),
+    "mfg_zpotrf": (_I, [_vp, _I, _vp, _I, _c_int_p]),
+    "mfg_zgeqrf": (_I, [_vp, _I, _I, _vp, _I, _vp]),
+    "mfg_zorgqr": (_I, [_vp, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_zqr_r": (_I, [_vp, _I, _I, _vp, _I, _vp, _I, _vp]),
+    "mfg_strsv": (_I, [_vp, _I, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_ztrsv": (_I, [_vp, _I, _I, _I, _vp, _I, _vp, _I]),
+    "mfg_sgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
+    "mfg_zgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
     "mfg_dgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
     "mfg_dgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_plan_getrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _I, _vp]),
@@ -167,7 +178,16 @@ def _need(arr, count, name, dtype=np.float64):
 
 
 def _dt(a):
-    return np.float32 if isinstance(a, np.ndarray) and a.dtype == np.float32 else np.float64
+    if isinstance(a, np.ndarray) and a.dtype in (np.float32, np.complex128):
+        return a.dtype.type
+    return np.float64
+
+
+def _pfx(dt):
+    return {np.float64: "d", np.float32: "s", np.complex128: "z"}[dt]
+
+
+_RDIAG_DT = {np.float64: np.float64, np.float32: np.float32, np.complex128: np.float64}
 
 
 def _span(rows, cols, ld):
@@ -192,17 +212,19 @@ def _raise_status(rc, names, ctx):
 
 
 class Factorization:
-    """Mirror of MatFlat.Factorization (double overloads on the GPU)."""
+    """Mirror of MatFlat.Factorization: float32, float64 and complex128 arrays select MatFlat's
+    float, double and Complex overloads."""
 
     @staticmethod
     def Lu(m, n, a, lda, piv):
         """Factorization.Lu (MatFlat/Factorization.Lu.cs:122-161); returns the pivot sign."""
         ctx = context()
+        dt = _dt(a)
         if m > 0 and n > 0 and lda >= m:
-            _need(a, _span(m, n, lda), "a")
+            _need(a, _span(m, n, lda), "a", dt)
             _need(piv, m, "piv", np.int32)
         sign = ctypes.c_int(0)
-        rc = ctx.lib.mfg_dgetrf(ctx.h, m, n, None if a is None else _ptr(a), lda,
+        rc = getattr(ctx.lib, "mfg_%sgetrf" % _pfx(dt))(ctx.h, m, n, None if a is None else _ptr(a), lda,
                                 None if piv is None else _ptr(piv), ctypes.byref(sign))
         if rc != 0:
             _raise_status(rc, ["m", "n", "a", "lda", "piv"], ctx)
@@ -212,10 +234,11 @@ class Factorization:
     def Cholesky(n, a, lda):
         """Factorization.Cholesky (MatFlat/Factorization.Cholesky.cs:114-168)."""
         ctx = context()
+        dt = _dt(a)
         if n > 0 and lda >= n:
-            _need(a, _span(n, n, lda), "a")
+            _need(a, _span(n, n, lda), "a", dt)
         info = ctypes.c_int(0)
-        rc = ctx.lib.mfg_dpotrf(ctx.h, n, None if a is None else _ptr(a), lda, ctypes.byref(info))
+        rc = getattr(ctx.lib, "mfg_%spotrf" % _pfx(dt))(ctx.h, n, None if a is None else _ptr(a), lda, ctypes.byref(info))
         if rc != 0:
             _raise_status(rc, ["n", "a", "lda"], ctx)
         if info.value != 0:
@@ -229,8 +252,8 @@ class Factorization:
         dt = _dt(a)
         if m > 0 and n > 0 and lda >= m and n <= m:
             _need(a, _span(m, n, lda), "a", dt)
-            _need(rdiag, n, "rdiag", dt)
-        fn = ctx.lib.mfg_sgeqrf if dt == np.float32 else ctx.lib.mfg_dgeqrf
+            _need(rdiag, n, "rdiag", _RDIAG_DT[dt])
+        fn = getattr(ctx.lib, "mfg_%sgeqrf" % _pfx(dt))
         rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
                                 None if rdiag is None else _ptr(rdiag))
         if rc != 0:
@@ -244,7 +267,7 @@ class Factorization:
         if m > 0 and n > 0 and lda >= m and ldq >= m and n <= m:
             _need(a, _span(m, n, lda), "a", dt)
             _need(q, _span(m, n, ldq), "q", dt)
-        fn = ctx.lib.mfg_sorgqr if dt == np.float32 else ctx.lib.mfg_dorgqr
+        fn = getattr(ctx.lib, "mfg_%sorgqr" % _pfx(dt))
         rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
                                 None if q is None else _ptr(q), ldq)
         if rc != 0:
@@ -258,8 +281,8 @@ class Factorization:
         if m > 0 and n > 0 and lda >= m and ldr >= n and n <= m:
             _need(a, _span(m, n, lda), "a", dt)
             _need(r, _span(n, n, ldr), "r", dt)
-            _need(rdiag, n, "rdiag", dt)
-        fn = ctx.lib.mfg_sqr_r if dt == np.float32 else ctx.lib.mfg_dqr_r
+            _need(rdiag, n, "rdiag", _RDIAG_DT[dt])
+        fn = getattr(ctx.lib, "mfg_%sqr_r" % _pfx(dt))
         rc = fn(ctx.h, m, n, None if a is None else _ptr(a), lda,
                                None if r is None else _ptr(r), ldr,
                                None if rdiag is None else _ptr(rdiag))
@@ -283,16 +306,17 @@ class Factorization:
 
 
 class Blas:
-    """Mirror of MatFlat.Blas (double overloads on the GPU)."""
+    """Mirror of MatFlat.Blas: float32, float64 and complex128 overloads."""
 
     @staticmethod
     def SolveTriangular(uplo, transa, n, a, lda, x, incx):
         """Blas.SolveTriangular (MatFlat/Blas.SolveTriangular.cs:162-242)."""
         ctx = context()
+        dt = _dt(a)
         if n > 0 and lda >= n and incx > 0:
-            _need(a, _span(n, n, lda), "a")
-            _need(x, (n - 1) * incx + 1, "x")
-        rc = ctx.lib.mfg_dtrsv(ctx.h, int(uplo), int(transa), n, None if a is None else _ptr(a),
+            _need(a, _span(n, n, lda), "a", dt)
+            _need(x, (n - 1) * incx + 1, "x", dt)
+        rc = getattr(ctx.lib, "mfg_%strsv" % _pfx(dt))(ctx.h, int(uplo), int(transa), n, None if a is None else _ptr(a),
                                lda, None if x is None else _ptr(x), incx)
         if rc != 0:
             _raise_status(rc, ["uplo", "transa", "n", "a", "lda", "x", "incx"], ctx)
@@ -301,19 +325,21 @@ class Blas:
     def MulMatMat(transa, transb, m, n, k, a, lda, b, ldb, c, ldc):
         """Blas.MulMatMat (MatFlat/Blas.MulMatMat.cs:226-368)."""
         ctx = context()
+        dt = _dt(a)
         ok = m > 0 and n > 0 and k > 0 and ldc >= m
         ta, tb = int(transa), int(transb)
-        if ok and ta in (111, 112) and tb in (111, 112):
-            ar, ac = (m, k) if ta == 111 else (k, m)
-            br, bc = (k, n) if tb == 111 else (n, k)
+        modes = (111, 112, 113, 114) if dt == np.complex128 else (111, 112)
+        if ok and ta in modes and tb in modes:
+            ar, ac = (m, k) if ta in (111, 114) else (k, m)
+            br, bc = (k, n) if tb in (111, 114) else (n, k)
             if lda >= ar and ldb >= br:
-                _need(a, _span(ar, ac, lda), "a")
-                _need(b, _span(br, bc, ldb), "b")
-                _need(c, _span(m, n, ldc), "c")
+                _need(a, _span(ar, ac, lda), "a", dt)
+                _need(b, _span(br, bc, ldb), "b", dt)
+                _need(c, _span(m, n, ldc), "c", dt)
                 if a is not None and c is not None and (np.shares_memory(a, c) or
                                                         np.shares_memory(b, c)):
                     raise ArgumentException("In-place operation is not supported.")
-        rc = ctx.lib.mfg_dgemm(ctx.h, ta, tb, m, n, k, None if a is None else _ptr(a), lda,
+        rc = getattr(ctx.lib, "mfg_%sgemm" % _pfx(dt))(ctx.h, ta, tb, m, n, k, None if a is None else _ptr(a), lda,
                                None if b is None else _ptr(b), ldb,
                                None if c is None else _ptr(c), ldc)
         if rc != 0:

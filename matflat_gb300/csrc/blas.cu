@@ -6,6 +6,7 @@
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_scalar.cuh"
 #include "mf_solve.cuh"
 
 namespace mfg {
@@ -125,6 +126,115 @@ cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, l
   long long blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   selftest_mul_kernel<<<(unsigned)blocks, 256, 0, s>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
+// Float and Complex overloads of SolveTriangular (Blas.SolveTriangular.cs:44-124, :280-395).
+// TrP: plain element arithmetic, TrC: the Conj modes (Complex only; float uses TrP for both).
+template <class TrP, class TrC>
+__global__ void __launch_bounds__(32) trsv_t_kernel(int uplo, int trans, int n,
+                                                    const typename TrP::T* a, int lda,
+                                                    typename TrP::T* x, int incx, void* scratch) {
+  using T = typename TrP::T;
+  using Acc = typename TrP::Acc;
+  const int lane = threadIdx.x & 31;
+  const int ldx = n | 1;
+  Acc* acc = (Acc*)scratch;
+  T* xs = (T*)(acc + ldx);
+  for (int i = lane; i < n; i += 32) xs[i] = x[(long long)i * incx];
+  __syncwarp();
+  const long long l = lda;
+  const bool conj = trans == 113 || trans == 114;
+  const bool tr = trans == 112 || trans == 113;   // Trans, ConjTrans
+  if (uplo == 121) {   // Upper
+    if (!tr) {         // NoTrans / ConjNoTrans: column sweep over the columns of U
+      if (conj) warp_solve_sweep<32, TrC>(a, n, l, 1, xs, ldx, 1);
+      else warp_solve_sweep<32, TrP>(a, n, l, 1, xs, ldx, 1);
+    } else {           // Trans / ConjTrans: dot form over the columns of U
+      if (conj) warp_solve_dot<32, TrC>(a, n, l, 1, false, xs, ldx, acc, 1);
+      else warp_solve_dot<32, TrP>(a, n, l, 1, false, xs, ldx, acc, 1);
+    }
+  } else {             // Lower
+    if (!tr) {         // NoTrans / ConjNoTrans: dot form over the rows of L
+      if (conj) warp_solve_dot<32, TrC>(a, n, 1, l, false, xs, ldx, acc, 1);
+      else warp_solve_dot<32, TrP>(a, n, 1, l, false, xs, ldx, acc, 1);
+    } else {           // Trans / ConjTrans: column sweep over the rows of L
+      if (conj) warp_solve_sweep<32, TrC>(a, n, 1, l, xs, ldx, 1);
+      else warp_solve_sweep<32, TrP>(a, n, 1, l, xs, ldx, 1);
+    }
+  }
+  for (int i = lane; i < n; i += 32) x[(long long)i * incx] = xs[i];
+}
+
+// Float MulMatMat (Blas.MulMatMat.cs:45-187): c = (float)Dot with the double tree.
+__global__ void sgemm_single_kernel(int transa, int transb, int m, int n, int k, const float* a,
+                                    int lda, const float* b, int ldb, float* c, int ldc) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)m * n) return;
+  const int j = (int)(e / m);
+  const int i = (int)(e - (long long)j * m);
+  const float* x = transa == 111 ? a + i : a + (long long)lda * i;
+  const long long incx = transa == 111 ? lda : 1;
+  const float* y = transb == 111 ? b + (long long)ldb * j : b + j;
+  const long long incy = transb == 111 ? 1 : ldb;
+  c[(long long)ldc * j + i] = __double2float_rn(exact_dot_f(k, x, incx, y, incy));
+}
+
+// Complex MulMatMat (Blas.MulMatMat.cs:407-575): unpaired sequential sums Dot_NN/CN/NC/CC
+// (:598-648) starting from Complex.Zero.
+__global__ void zgemm_single_kernel(int transa, int transb, int m, int n, int k, const zdouble* a,
+                                    int lda, const zdouble* b, int ldb, zdouble* c, int ldc) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)m * n) return;
+  const int j = (int)(e / m);
+  const int i = (int)(e - (long long)j * m);
+  const bool ca = transa == 113 || transa == 114, cb = transb == 113 || transb == 114;
+  const bool ta = transa == 112 || transa == 113, tb = transb == 112 || transb == 113;
+  const zdouble* x = ta ? a + (long long)lda * i : a + i;
+  const long long incx = ta ? 1 : lda;
+  const zdouble* y = tb ? b + j : b + (long long)ldb * j;
+  const long long incy = tb ? ldb : 1;
+  zdouble sum = zmake(0.0, 0.0);
+  for (int t = 0; t < k; ++t) {
+    const zdouble xv = x[t * incx], yv = y[t * incy];
+    zdouble p;
+    if (ca && cb) p = zmulconjconj(xv, yv);
+    else if (ca) p = zmulconj(xv, yv);
+    else if (cb) p = zmulconj(yv, xv);
+    else p = zmul(xv, yv);
+    sum = zadd(sum, p);
+  }
+  c[(long long)ldc * j + i] = sum;
+}
+
+cudaError_t launch_strsv_single(int uplo, int trans, int n, const float* a, int lda, float* x,
+                                int incx, double* scratch, cudaStream_t s) {
+  trsv_t_kernel<SSolve, SSolve><<<1, 32, 0, s>>>(uplo, trans, n, a, lda, x, incx, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ztrsv_single(int uplo, int trans, int n, const double* a, int lda, double* x,
+                                int incx, double* scratch, cudaStream_t s) {
+  trsv_t_kernel<ZSolve<false>, ZSolve<true>><<<1, 32, 0, s>>>(
+      uplo, trans, n, (const zdouble*)a, lda, (zdouble*)x, incx, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sgemm_single(int transa, int transb, int m, int n, int k, const float* a,
+                                int lda, const float* b, int ldb, float* c, int ldc,
+                                cudaStream_t s) {
+  const long long total = (long long)m * n;
+  sgemm_single_kernel<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(transa, transb, m, n, k, a,
+                                                                      lda, b, ldb, c, ldc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zgemm_single(int transa, int transb, int m, int n, int k, const double* a,
+                                int lda, const double* b, int ldb, double* c, int ldc,
+                                cudaStream_t s) {
+  const long long total = (long long)m * n;
+  zgemm_single_kernel<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+      transa, transb, m, n, k, (const zdouble*)a, lda, (const zdouble*)b, ldb, (zdouble*)c, ldc);
   return cudaGetLastError();
 }
 

@@ -14,6 +14,7 @@
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_scalar.cuh"
 #include "mf_solve.cuh"
 
 namespace mfg {
@@ -329,6 +330,89 @@ __global__ void __launch_bounds__(WARPS * 32) chol_grad_batched_kernel(BatchArgs
 cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
                                      int keep_factor, int ctas, cudaStream_t s) {
   chol_grad_batched_kernel<4><<<ctas, 128, 0, s>>>(args, loss, grad, keep_factor);
+  return cudaGetLastError();
+}
+
+}  // namespace mfg
+
+namespace mfg {
+
+// Float overload of Factorization.Cholesky (MatFlat/Factorization.Cholesky.cs:33-87): float
+// storage; t = ((double)A(k,j) - Dot) / (double)L(k,k) in double, stored as (float)t; the
+// diagonal sum s += t*t stays in double with the unrounded t; L(j,j) = (float)sqrt(s).
+__global__ void __launch_bounds__(32) spotrf_single_kernel(float* a, int n, int lda, int* out1,
+                                                           double* dsum) {
+  const int lane = threadIdx.x & 31;
+  for (int j = lane; j < n; j += 32) dsum[j] = 0.0;
+  __syncwarp();
+  int info = 0;
+  for (int k = 0; k < n && info == 0; ++k) {
+    float* colk = a + (long long)k * lda;
+    const double s = __dsub_rn((double)colk[k], dsum[k]);
+    if (!positive(s)) {
+      info = k + 1;
+      break;
+    }
+    const float lkk = __double2float_rn(__dsqrt_rn(s));
+    __syncwarp();
+    if (lane == 0) colk[k] = lkk;
+    for (int j = k + 1 + lane; j < n; j += 32) {
+      const double d = exact_dot_f(k, a + j, lda, a + k, lda);
+      const double t = __ddiv_rn(__dsub_rn((double)a[(long long)j * lda + k], d), (double)lkk);
+      colk[j] = __double2float_rn(t);
+      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
+    }
+    __syncwarp();
+  }
+  if (info == 0) {
+    for (int c = 1; c < n; ++c)
+      for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = 0.0f;
+  }
+  if (lane == 0) out1[0] = info;
+}
+
+// Complex overload (Factorization.Cholesky.cs:195-249): t = (A(k,j) - DotConj(L(j,:), L(k,:)))
+// / L(k,k); L(j,k) = conj(t); s += t.re^2 + t.im^2; L(j,j) = Complex(sqrt(A(j,j).re - s), 0).
+__global__ void __launch_bounds__(32) zpotrf_single_kernel(zdouble* a, int n, int lda, int* out1,
+                                                           double* dsum) {
+  const int lane = threadIdx.x & 31;
+  for (int j = lane; j < n; j += 32) dsum[j] = 0.0;
+  __syncwarp();
+  int info = 0;
+  for (int k = 0; k < n; ++k) {
+    zdouble* colk = a + (long long)k * lda;
+    const double s = __dsub_rn(colk[k].re, dsum[k]);
+    if (!positive(s)) {
+      info = k + 1;
+      break;
+    }
+    const zdouble lkk = zmake(__dsqrt_rn(s), 0.0);
+    __syncwarp();
+    if (lane == 0) colk[k] = lkk;
+    for (int j = k + 1 + lane; j < n; j += 32) {
+      const zdouble d = zdot<true>(k, a + j, lda, a + k, lda);
+      const zdouble t = zdiv(zsub(a[(long long)j * lda + k], d), lkk);
+      colk[j] = zconj(t);
+      dsum[j] = __dadd_rn(dsum[j], __dadd_rn(__dmul_rn(t.re, t.re), __dmul_rn(t.im, t.im)));
+    }
+    __syncwarp();
+  }
+  if (info == 0) {
+    for (int c = 1; c < n; ++c)
+      for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = zmake(0.0, 0.0);
+  }
+  if (lane == 0) out1[0] = info;
+}
+
+cudaError_t launch_spotrf_single(float* a, int n, int lda, int* out1, double* scratch,
+                                 cudaStream_t s) {
+  spotrf_single_kernel<<<1, 32, 0, s>>>(a, n, lda, out1, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zpotrf_single(double* a, int n, int lda, int* out1, double* scratch,
+                                 cudaStream_t s) {
+  zpotrf_single_kernel<<<1, 32, 0, s>>>((zdouble*)a, n, lda, out1, scratch);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_scalar.cuh"
 #include "mf_solve.cuh"
 
 namespace mfg {
@@ -31,44 +32,49 @@ namespace mfg {
 //   mode 0: column 0 (no dot: v = A - 0.0 = A, left as is)
 //   mode 1: column 1 (sum = L(i,0) * U(0,1))
 //   mode 2: column c >= 2 (sum = scol[i] + (L(i,c-2)*U(c-2,c) + L(i,c-1)*U(c-1,c)))
-__device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long long lda, int c,
-                                                 int mode, const double* scol, int* piv,
+// Tr supplies the element type's arithmetic (double, float or Complex overload).
+template <class Tr>
+__device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n, long long lda,
+                                                 int c, int mode,
+                                                 const typename Tr::Acc* scol, int* piv,
                                                  int& sign, int& info) {
+  using T = typename Tr::T;
+  using Acc = typename Tr::Acc;
   const int lane = threadIdx.x & 31;
-  double* cc = a + (long long)c * lda;
+  T* cc = a + (long long)c * lda;
   unsigned long long bkey = 0ull;
   int bidx = INT_MAX;
   bool first_nan = false;
   if (mode == 0) {
     for (int i = c + lane; i < m; i += 32) {
-      const double v = cc[i];
-      const unsigned long long key = pivot_key(v);
+      const T v = cc[i];
+      const unsigned long long key = Tr::key(v);
       if (key > bkey) {
         bkey = key;
         bidx = i;
       }
-      if (i == c) first_nan = is_nan(v);
+      if (i == c) first_nan = Tr::nan0(v);
     }
   } else {
-    const double* l1 = a + (long long)(c - 1) * lda;  // L(:, c-1)
-    const double u1 = cc[c - 1];                       // U(c-1, c)
-    const double* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
-    const double u2 = (mode == 2) ? cc[c - 2] : 0.0;   // U(c-2, c)
+    const T* l1 = a + (long long)(c - 1) * lda;  // L(:, c-1)
+    const T u1 = cc[c - 1];                       // U(c-1, c)
+    const T* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
+    const T u2 = (mode == 2) ? cc[c - 2] : u1;    // U(c-2, c)
     for (int i = c + lane; i < m; i += 32) {
-      double s;
+      Acc s;
       if (mode == 1) {
-        s = __dmul_rn(l1[i], u1);
+        s = Tr::prod(l1[i], u1);
       } else {
-        s = __dadd_rn(scol[i], __dadd_rn(__dmul_rn(l2[i], u2), __dmul_rn(l1[i], u1)));
+        s = Tr::pair(scol[i], l2[i], u2, l1[i], u1);
       }
-      const double v = __dsub_rn(cc[i], s);
+      const T v = Tr::fin(cc[i], s);
       cc[i] = v;
-      const unsigned long long key = pivot_key(v);
+      const unsigned long long key = Tr::key(v);
       if (key > bkey) {
         bkey = key;
         bidx = i;
       }
-      if (i == c) first_nan = is_nan(v);
+      if (i == c) first_nan = Tr::nan0(v);
     }
   }
   int p = warp_argmax(bkey, bidx);
@@ -77,8 +83,8 @@ __device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long l
   __syncwarp();
   if (p != c && p < m) {
     for (int col = lane; col < n; col += 32) {
-      double* base = a + (long long)col * lda;
-      const double t = base[c];
+      T* base = a + (long long)col * lda;
+      const T t = base[c];
       base[c] = base[p];
       base[p] = t;
     }
@@ -90,9 +96,9 @@ __device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long l
     sign = -sign;
   }
   __syncwarp();
-  const double diag = cc[c];
-  if (nonzero(diag)) {
-    for (int i = c + 1 + lane; i < m; i += 32) cc[i] = __ddiv_rn(cc[i], diag);
+  const T diag = cc[c];
+  if (Tr::nz(diag)) {
+    for (int i = c + 1 + lane; i < m; i += 32) cc[i] = Tr::div(cc[i], diag);
   } else if (info == 0) {
     info = c + 1;
   }
@@ -100,40 +106,42 @@ __device__ __forceinline__ void lu_finish_column(double* a, int m, int n, long l
 }
 
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
-// vector (m entries).  scol: m doubles of per-warp scratch.  Returns Lu's sign in `sign` and in
-// `info` the first zero pivot (k+1), or 0.
-template <bool IM, int DB = DOT_BLOCK>
-__device__ void lu_warp(double* a, int m, int n, long long lda, int* piv, double* scol, int& sign,
-                        int& info) {
+// vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
+// and in `info` the first zero pivot (k+1), or 0.
+template <class Tr, bool IM, int DB = DOT_BLOCK>
+__device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
+                        typename Tr::Acc* scol, int& sign, int& info) {
+  using T = typename Tr::T;
+  using Acc = typename Tr::Acc;
   const int lane = threadIdx.x & 31;
   for (int i = lane; i < m; i += 32) piv[i] = i;
   sign = 1;
   info = 0;
   __syncwarp();
   const int K = m < n ? m : n;
-  lu_finish_column(a, m, n, lda, 0, 0, scol, piv, sign, info);
+  lu_finish_column<Tr>(a, m, n, lda, 0, 0, scol, piv, sign, info);
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
     const int C = (k1 < K && k >= 1) ? m - k1 : 0;  // prefixes of column k1 (rows [k1, m))
-    const double* rowk = a + k;               // L(k, t) = rowk[t*lda]
-    const double* colk1 = a + (long long)k1 * lda;
+    const T* rowk = a + k;                    // L(k, t) = rowk[t*lda]
+    const T* colk1 = a + (long long)k1 * lda;
     for (int d = lane; d < R + C; d += 32) {
       const bool isrow = d < R;
       const int idx = isrow ? k1 + d : k1 + (d - R);
-      const double* x = isrow ? rowk : a + idx;
-      const double* y = isrow ? a + (long long)idx * lda : colk1;
+      const T* x = isrow ? rowk : a + idx;
+      const T* y = isrow ? a + (long long)idx * lda : colk1;
       const int len = isrow ? k : k - 1;
-      const double s = exact_dot<IM, DB>(len, x, lda, y, 1);
+      const Acc s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
       if (isrow) {
-        double* dst = a + (long long)idx * lda + k;
-        *dst = __dsub_rn(*dst, s);
+        T* dst = a + (long long)idx * lda + k;
+        *dst = Tr::fin(*dst, s);
       } else {
         scol[idx] = s;
       }
     }
     __syncwarp();
-    if (k1 < K) lu_finish_column(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
+    if (k1 < K) lu_finish_column<Tr>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
   }
   // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
 }
@@ -186,7 +194,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
                                  : p.gscratch + gw * p.gscratch_stride;
     const int ldx = n | 1;
     int sign, info;
-    lu_warp<IM, DB>(a, n, n, lda, piv, scr, sign, info);
+    lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);
@@ -198,10 +206,11 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
   }
 }
 
-__global__ void __launch_bounds__(32) getrf_single_kernel(double* a, int m, int n, int lda,
-                                                          int* piv, int* out2, double* scratch) {
+template <class Tr>
+__global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int m, int n, int lda,
+                                                          int* piv, int* out2, void* scratch) {
   int sign, info;
-  lu_warp<true>(a, m, n, lda, piv, scratch, sign, info);
+  lu_warp<Tr, true>(a, m, n, lda, piv, (typename Tr::Acc*)scratch, sign, info);
   if (threadIdx.x == 0) {
     out2[0] = sign;
     out2[1] = info;
@@ -262,7 +271,19 @@ cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cud
 
 cudaError_t launch_getrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
                                 double* scratch, cudaStream_t s) {
-  getrf_single_kernel<<<1, 32, 0, s>>>(a, m, n, lda, piv, out2, scratch);
+  getrf_single_kernel<DTraits><<<1, 32, 0, s>>>(a, m, n, lda, piv, out2, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sgetrf_single(float* a, int m, int n, int lda, int* piv, int* out2,
+                                 double* scratch, cudaStream_t s) {
+  getrf_single_kernel<STraits><<<1, 32, 0, s>>>(a, m, n, lda, piv, out2, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zgetrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
+                                 double* scratch, cudaStream_t s) {
+  getrf_single_kernel<ZTraits><<<1, 32, 0, s>>>((zdouble*)a, m, n, lda, piv, out2, scratch);
   return cudaGetLastError();
 }
 
@@ -332,7 +353,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_strided_noalloc_kernel(Strid
     double* a = p.a + (long long)idx * p.stride_a;
     int* piv = p.piv + (long long)idx * p.stride_piv;
     int sign, info;
-    lu_warp<true>(a, n, n, lda, piv, scr, sign, info);
+    lu_warp<DTraits, true>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + (long long)idx * p.stride_b, n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);

@@ -104,6 +104,35 @@ cudaError_t launch_getrf_single(double* a, int m, int n, int lda, int* piv, int*
                                 double* scratch, cudaStream_t s);
 cudaError_t launch_potrf_single(double* a, int n, int lda, int* out1, double* scratch,
                                 cudaStream_t s);
+// Float and Complex overloads (Complex as interleaved re/im doubles).  LU scratch: m doubles
+// (float) or 2m doubles (Complex).
+cudaError_t launch_sgetrf_single(float* a, int m, int n, int lda, int* piv, int* out2,
+                                 double* scratch, cudaStream_t s);
+cudaError_t launch_zgetrf_single(double* a, int m, int n, int lda, int* piv, int* out2,
+                                 double* scratch, cudaStream_t s);
+// Complex QR (interleaved re/im doubles; rdiag real).  Scratch: 2(n+1) doubles.
+cudaError_t launch_zqr_single(double* a, int m, int n, int lda, double* rdiag, double* scratch,
+                              cudaStream_t s);
+cudaError_t launch_zqr_q_single(const double* a, int m, int n, int lda, double* q, int ldq,
+                                double* scratch, cudaStream_t s);
+cudaError_t launch_zqr_r_single(const double* a, int n, int lda, double* r, int ldr,
+                                const double* rdiag, cudaStream_t s);
+// Triangular solve scratch: 4 * (n|1) doubles.
+cudaError_t launch_strsv_single(int uplo, int trans, int n, const float* a, int lda, float* x,
+                                int incx, double* scratch, cudaStream_t s);
+cudaError_t launch_ztrsv_single(int uplo, int trans, int n, const double* a, int lda, double* x,
+                                int incx, double* scratch, cudaStream_t s);
+cudaError_t launch_sgemm_single(int transa, int transb, int m, int n, int k, const float* a,
+                                int lda, const float* b, int ldb, float* c, int ldc,
+                                cudaStream_t s);
+cudaError_t launch_zgemm_single(int transa, int transb, int m, int n, int k, const double* a,
+                                int lda, const double* b, int ldb, double* c, int ldc,
+                                cudaStream_t s);
+// Cholesky scratch: n doubles.
+cudaError_t launch_spotrf_single(float* a, int n, int lda, int* out1, double* scratch,
+                                 cudaStream_t s);
+cudaError_t launch_zpotrf_single(double* a, int n, int lda, int* out1, double* scratch,
+                                 cudaStream_t s);
 cudaError_t launch_trsv_single(int uplo, int trans, int n, const double* a, int lda, double* x,
                                int incx, double* scratch, cudaStream_t s);
 cudaError_t launch_gemm_single(int transa, int transb, int m, int n, int k, const double* a,

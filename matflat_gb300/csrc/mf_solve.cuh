@@ -15,6 +15,7 @@
 #pragma once
 
 #include "mf_device.cuh"
+#include "mf_scalar.cuh"
 
 namespace mfg {
 
@@ -32,27 +33,92 @@ __device__ __forceinline__ unsigned group_mask() {
   }
 }
 
+// Element arithmetic of the solves (Blas.SolveTriangular's double, float and Complex overloads).
+//   prod/pair  the dot-form accumulation (Internals.Dot / DotConj tree, in the dot's type)
+//   fin        x[i] = (x[i] - dot) / diag      (float: computed in double, then rounded)
+//   fin0       the same for i = 0, where Dot(0) = 0.0 and x - 0.0 = x
+//   sdiv/msub  the column sweep: x[i] /= diag; x[r] -= a(r,i) * x[i]
+struct DSolve {
+  using T = double;
+  using Acc = double;
+  static __device__ __forceinline__ Acc zero() { return 0.0; }
+  static __device__ __forceinline__ Acc prod(T a, T x) { return __dmul_rn(a, x); }
+  static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
+    return __dadd_rn(s, __dadd_rn(__dmul_rn(a0, x0), __dmul_rn(a1, x1)));
+  }
+  static __device__ __forceinline__ T fin(T x, Acc s, T d, bool unit) {
+    const T v = __dsub_rn(x, s);
+    return unit ? v : __ddiv_rn(v, d);
+  }
+  static __device__ __forceinline__ T fin0(T x, T d, bool unit) { return unit ? x : __ddiv_rn(x, d); }
+  static __device__ __forceinline__ T sdiv(T x, T d) { return __ddiv_rn(x, d); }
+  static __device__ __forceinline__ T msub(T x, T a, T xi) { return __dsub_rn(x, __dmul_rn(a, xi)); }
+};
+
+struct SSolve {
+  using T = float;
+  using Acc = double;
+  static __device__ __forceinline__ Acc zero() { return 0.0; }
+  static __device__ __forceinline__ Acc prod(T a, T x) { return __dmul_rn((double)a, (double)x); }
+  static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
+    return __dadd_rn(s, __dadd_rn(__dmul_rn((double)a0, (double)x0),
+                                  __dmul_rn((double)a1, (double)x1)));
+  }
+  static __device__ __forceinline__ T fin(T x, Acc s, T d, bool unit) {
+    const double v = __dsub_rn((double)x, s);
+    return __double2float_rn(unit ? v : __ddiv_rn(v, (double)d));
+  }
+  static __device__ __forceinline__ T fin0(T x, T d, bool unit) {
+    return unit ? x : __double2float_rn(__ddiv_rn((double)x, (double)d));
+  }
+  static __device__ __forceinline__ T sdiv(T x, T d) { return __fdiv_rn(x, d); }
+  static __device__ __forceinline__ T msub(T x, T a, T xi) { return __fsub_rn(x, __fmul_rn(a, xi)); }
+};
+
+// CONJ: the ConjNoTrans / ConjTrans modes (DotConj, MulSubConj, division by conj(diag)).
+template <bool CONJ>
+struct ZSolve {
+  using T = zdouble;
+  using Acc = zdouble;
+  static __device__ __forceinline__ zdouble m(zdouble a, zdouble x) {
+    return CONJ ? zmulconj(a, x) : zmul(a, x);
+  }
+  static __device__ __forceinline__ zdouble dg(zdouble d) { return CONJ ? zconj(d) : d; }
+  static __device__ __forceinline__ Acc zero() { return zmake(0.0, 0.0); }
+  static __device__ __forceinline__ Acc prod(T a, T x) { return m(a, x); }
+  static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
+    return zadd(s, zadd(m(a0, x0), m(a1, x1)));
+  }
+  static __device__ __forceinline__ T fin(T x, Acc s, T d, bool unit) {
+    const zdouble v = zsub(x, s);
+    return unit ? v : zdiv(v, dg(d));
+  }
+  static __device__ __forceinline__ T fin0(T x, T d, bool unit) { return unit ? x : zdiv(x, dg(d)); }
+  static __device__ __forceinline__ T sdiv(T x, T d) { return zdiv(x, dg(d)); }
+  static __device__ __forceinline__ T msub(T x, T a, T xi) { return zsub(x, m(a, xi)); }
+};
+
 // Dot form.  Element (i, t), t < i, of the triangular operand is at a[i*si + t*st] and the
 // diagonal at a[i*si + i*st].  With unit = true the division is skipped: MatFlat's unit-lower
 // idiom divides by an explicit 1.0 (Factorization.LuInverse.cs:174-182), which is exact.
-template <int G = 32>
-__device__ __forceinline__ void warp_solve_dot(const double* a, int n, long long si, long long st,
-                                               bool unit, double* xs, int ldx, double* acc,
-                                               int nr) {
+template <int G = 32, class Tr = DSolve>
+__device__ __forceinline__ void warp_solve_dot(const typename Tr::T* a, int n, long long si,
+                                               long long st, bool unit, typename Tr::T* xs,
+                                               int ldx, typename Tr::Acc* acc, int nr) {
+  using T = typename Tr::T;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int e = lane; e < nr * n; e += G) {
     const int r = e / n;
-    acc[r * ldx + (e - r * n)] = 0.0;
+    acc[r * ldx + (e - r * n)] = Tr::zero();
   }
   __syncwarp(gm);
   for (int t = 0; t < n; ++t) {
     // x[t] is final: its last pair was added at step t-1.
     for (int r = lane; r < nr; r += G) {
-      double v = xs[r * ldx + t];
-      if (t > 0) v = __dsub_rn(v, acc[r * ldx + t]);
-      if (!unit) v = __ddiv_rn(v, a[t * si + t * st]);
-      xs[r * ldx + t] = v;
+      const T v = xs[r * ldx + t];
+      const T d = a[t * si + t * st];
+      xs[r * ldx + t] = (t > 0) ? Tr::fin(v, acc[r * ldx + t], d, unit) : Tr::fin0(v, d, unit);
     }
     __syncwarp(gm);
     // Rows i = t+1, t+3, ... close a pair at t (or, at t = 0, take their lone first product).
@@ -61,14 +127,12 @@ __device__ __forceinline__ void warp_solve_dot(const double* a, int n, long long
       const int q = e / nr;
       const int r = e - q * nr;
       const int i = t + 1 + 2 * q;
-      double* ap = acc + r * ldx + i;
-      const double* ai = a + i * si;
+      typename Tr::Acc* ap = acc + r * ldx + i;
+      const T* ai = a + i * si;
       if (t == 0) {
-        *ap = __dmul_rn(ai[0], xs[r * ldx]);
+        *ap = Tr::prod(ai[0], xs[r * ldx]);
       } else {
-        const double q2 = __dadd_rn(__dmul_rn(ai[(t - 1) * st], xs[r * ldx + t - 1]),
-                                    __dmul_rn(ai[t * st], xs[r * ldx + t]));
-        *ap = __dadd_rn(*ap, q2);
+        *ap = Tr::pair(*ap, ai[(t - 1) * st], xs[r * ldx + t - 1], ai[t * st], xs[r * ldx + t]);
       }
     }
     __syncwarp(gm);
@@ -77,22 +141,23 @@ __device__ __forceinline__ void warp_solve_dot(const double* a, int n, long long
 
 // Column sweep.  Element (r, i), r < i, is at a[i*si + r*sr]; the diagonal at a[i*si + i*sr], or
 // at diag[i] when diag is given (the R factor of QR keeps its diagonal apart, in rdiag).
-template <int G = 32>
-__device__ __forceinline__ void warp_solve_sweep(const double* a, int n, long long si,
-                                                 long long sr, double* xs, int ldx, int nr,
-                                                 const double* diag = nullptr) {
+template <int G = 32, class Tr = DSolve>
+__device__ __forceinline__ void warp_solve_sweep(const typename Tr::T* a, int n, long long si,
+                                                 long long sr, typename Tr::T* xs, int ldx,
+                                                 int nr, const typename Tr::T* diag = nullptr) {
+  using T = typename Tr::T;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int i = n - 1; i >= 0; --i) {
-    const double* ai = a + i * si;
-    const double d = diag ? diag[i] : ai[i * sr];
-    for (int r = lane; r < nr; r += G) xs[r * ldx + i] = __ddiv_rn(xs[r * ldx + i], d);
+    const T* ai = a + i * si;
+    const T d = diag ? diag[i] : ai[i * sr];
+    for (int r = lane; r < nr; r += G) xs[r * ldx + i] = Tr::sdiv(xs[r * ldx + i], d);
     __syncwarp(gm);
     for (int e = lane; e < nr * i; e += G) {
       const int q = e / nr;
       const int r = e - q * nr;
-      double* xp = xs + r * ldx + q;
-      *xp = __dsub_rn(*xp, __dmul_rn(ai[q * sr], xs[r * ldx + i]));
+      T* xp = xs + r * ldx + q;
+      *xp = Tr::msub(*xp, ai[q * sr], xs[r * ldx + i]);
     }
     __syncwarp(gm);
   }

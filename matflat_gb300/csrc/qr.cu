@@ -20,6 +20,7 @@
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_scalar.cuh"
 
 namespace mfg {
 
@@ -28,6 +29,7 @@ struct QrArith;
 
 template <>
 struct QrArith<double> {
+  using R = double;  // type of the norm and of rdiag
   // Internals.Norm (Internals.cs:435-460): the Dot tree over x*x, then Math.Sqrt.
   static __device__ __forceinline__ double norm(int len, const double* x) {
     return __dsqrt_rn(exact_dot(len, x, 1, x, 1));
@@ -47,10 +49,22 @@ struct QrArith<double> {
     return __dsub_rn(dst, __dmul_rn(x, s));
   }
   static __device__ __forceinline__ bool nz(double v) { return nonzero(v); }
+  static __device__ __forceinline__ bool nzr(double v) { return nonzero(v); }
+  static __device__ __forceinline__ double divn(double x, double norm) { return __ddiv_rn(x, norm); }
+  static __device__ __forceinline__ double neg_r(double norm) { return -norm; }
+  // QrOrthogonalFactor's dot and update (Qr.cs:408-409)
+  static __device__ __forceinline__ double qdot(int len, const double* a, const double* q) {
+    return exact_dot(len, a, 1, q, 1);
+  }
+  static __device__ __forceinline__ double qmuladd(double q, double a, double s) {
+    return __dadd_rn(q, __dmul_rn(a, s));
+  }
+  static __device__ __forceinline__ double rdiag_elem(double r) { return r; }
 };
 
 template <>
 struct QrArith<float> {
+  using R = float;
   // (float)Internals.Norm(float*) (Qr.cs:68): double sum of widened squares, sqrt, to float.
   static __device__ __forceinline__ float norm(int len, const float* x) {
     return __double2float_rn(__dsqrt_rn(exact_dot_f(len, x, 1, x, 1)));
@@ -71,6 +85,65 @@ struct QrArith<float> {
     return __fsub_rn(dst, __fmul_rn(x, s));
   }
   static __device__ __forceinline__ bool nz(float v) { return (__float_as_uint(v) << 1) != 0u; }
+  static __device__ __forceinline__ bool nzr(float v) { return nz(v); }
+  static __device__ __forceinline__ float divn(float x, float norm) { return __fdiv_rn(x, norm); }
+  static __device__ __forceinline__ float neg_r(float norm) { return -norm; }
+  static __device__ __forceinline__ double qdot(int len, const float* a, const float* q) {
+    return exact_dot_f(len, a, 1, q, 1);
+  }
+  static __device__ __forceinline__ float qmuladd(float q, float a, float s) {
+    return __fadd_rn(q, __fmul_rn(a, s));
+  }
+  static __device__ __forceinline__ float rdiag_elem(float r) { return r; }
+};
+
+// Complex overload (Factorization.Qr.cs:198-255, :436-492, :677-730): the norm is real
+// (Internals.Norm over re^2 + im^2, Internals.cs:489-514), the column is divided by
+// Complex(norm, 0), the dots are DotConj, and QrOrthogonalFactor uses
+// s = -DotConj(q_j, v) / v[0] with MulConjAdd (q += conj(s) * v).
+template <>
+struct QrArith<zdouble> {
+  using R = double;
+  static __device__ __forceinline__ double norm(int len, const zdouble* x) {
+    double s;
+    int i = 0;
+    if (len & 1) {
+      s = __dadd_rn(__dmul_rn(x[0].re, x[0].re), __dmul_rn(x[0].im, x[0].im));
+      i = 1;
+    } else {
+      s = 0.0;
+    }
+    for (; i < len; i += 2) {
+      // sum += x0.re*x0.re + x0.im*x0.im + x1.re*x1.re + x1.im*x1.im  (left to right)
+      double t = __dadd_rn(__dmul_rn(x[i].re, x[i].re), __dmul_rn(x[i].im, x[i].im));
+      t = __dadd_rn(t, __dmul_rn(x[i + 1].re, x[i + 1].re));
+      t = __dadd_rn(t, __dmul_rn(x[i + 1].im, x[i + 1].im));
+      s = __dadd_rn(s, t);
+    }
+    return __dsqrt_rn(s);
+  }
+  static __device__ __forceinline__ zdouble dot(int len, const zdouble* x, const zdouble* y) {
+    return zdot<true>(len, x, 1, y, 1);
+  }
+  static __device__ __forceinline__ zdouble div(zdouble x, zdouble y) { return zdiv(x, y); }
+  static __device__ __forceinline__ zdouble divn(zdouble x, double norm) {
+    return zdiv(x, zmake(norm, 0.0));
+  }
+  static __device__ __forceinline__ zdouble add1(zdouble x) { return zadd(x, zmake(1.0, 0.0)); }
+  static __device__ __forceinline__ zdouble coef(zdouble d, zdouble v0) { return zdiv(zneg(d), v0); }
+  static __device__ __forceinline__ zdouble muladd(zdouble dst, zdouble x, zdouble s) {
+    return zadd(dst, zmul(x, s));
+  }
+  static __device__ __forceinline__ bool nz(zdouble v) { return znonzero(v); }
+  static __device__ __forceinline__ bool nzr(double v) { return nonzero(v); }
+  static __device__ __forceinline__ double neg_r(double norm) { return -norm; }
+  static __device__ __forceinline__ zdouble qdot(int len, const zdouble* a, const zdouble* q) {
+    return zdot<true>(len, q, 1, a, 1);
+  }
+  static __device__ __forceinline__ zdouble qmuladd(zdouble q, zdouble a, zdouble s) {
+    return zadd(q, zmulconj(s, a));
+  }
+  static __device__ __forceinline__ zdouble rdiag_elem(double r) { return zmake(r, 0.0); }
 };
 
 // Column j of the factored matrix, or right-hand side j - n when j >= n.
@@ -82,16 +155,17 @@ __device__ __forceinline__ T* qr_col(T* a, long long lda, int n, T* b, long long
 // Factors the m-by-n matrix a (m >= n) in place, applying every reflector also to the nb columns
 // of b (leading dimension ldb).  coefs: n - 1 + nb values of per-warp scratch.
 template <typename T>
-__device__ void qr_warp(T* a, int m, int n, long long lda, T* rdiag, T* b, long long ldb, int nb,
-                        T* coefs) {
+__device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag, T* b,
+                        long long ldb, int nb, T* coefs) {
   using A = QrArith<T>;
+  using R = typename A::R;
   const int lane = threadIdx.x & 31;
   for (int k = 0; k < n; ++k) {
     T* ck = a + (long long)k * lda;
     const int len = m - k;
-    const T norm = A::norm(len, ck + k);  // every lane, same value
-    if (A::nz(norm)) {
-      for (int r = k + lane; r < m; r += 32) ck[r] = A::div(ck[r], norm);
+    const R norm = A::norm(len, ck + k);  // every lane, same value
+    if (A::nzr(norm)) {
+      for (int r = k + lane; r < m; r += 32) ck[r] = A::divn(ck[r], norm);
       __syncwarp();
       if (lane == 0) ck[k] = A::add1(ck[k]);
       __syncwarp();
@@ -115,7 +189,7 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, T* rdiag, T* b, long 
       }
     }
     __syncwarp();
-    if (lane == 0) rdiag[k] = -norm;
+    if (lane == 0) rdiag[k] = A::neg_r(norm);
     __syncwarp();
   }
 }
@@ -152,9 +226,9 @@ __device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long lo
   for (int k = n - 1; k >= 0; --k) {
     T* qk = q + (long long)k * ldq;
     const T* ak = a + (long long)k * lda;
-    for (int r = lane; r < m; r += 32) qk[r] = (T)0;
+    for (int r = lane; r < m; r += 32) qk[r] = A::rdiag_elem((typename A::R)0);
     __syncwarp();
-    if (lane == 0) qk[k] = (T)1;
+    if (lane == 0) qk[k] = A::rdiag_elem((typename A::R)1);
     __syncwarp();
     const T v0 = ak[k];
     if (A::nz(v0)) {
@@ -162,7 +236,7 @@ __device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long lo
       const int ncols = n - k;
       for (int c = lane; c < ncols; c += 32) {
         const T* qj = q + (long long)(k + c) * ldq;
-        coefs[c] = A::coef(A::dot(len, ak + k, qj + k), v0);
+        coefs[c] = A::coef(A::qdot(len, ak + k, qj + k), v0);
       }
       __syncwarp();
       const long long work = (long long)len * ncols;
@@ -170,7 +244,7 @@ __device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long lo
         const int c = (int)(e / len);
         const int r = k + (int)(e - (long long)c * len);
         T* qj = q + (long long)(k + c) * ldq;
-        qj[r] = A::muladd(qj[r], ak[r], coefs[c]);
+        qj[r] = A::qmuladd(qj[r], ak[r], coefs[c]);
       }
     }
     __syncwarp();
@@ -205,8 +279,8 @@ __global__ void __launch_bounds__(WARPS * 32) qr_batched_kernel(QrBatchArgs<T> p
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32) qr_single_kernel(T* a, int m, int n, int lda, T* rdiag,
-                                                       T* scratch) {
+__global__ void __launch_bounds__(32) qr_single_kernel(T* a, int m, int n, int lda,
+                                                       typename QrArith<T>::R* rdiag, T* scratch) {
   qr_warp<T>(a, m, n, lda, rdiag, (T*)nullptr, 0, 0, scratch);
 }
 
@@ -218,15 +292,16 @@ __global__ void __launch_bounds__(32) qr_q_single_kernel(const T* a, int m, int 
 
 // QrUpperTriangularFactor: R(0:i, i) = a(0:i, i); R(i,i) = rdiag[i]; R(i+1:n, i) = 0.
 template <typename T>
-__global__ void qr_r_single_kernel(const T* a, int n, int lda, T* r, int ldr, const T* rdiag) {
+__global__ void qr_r_single_kernel(const T* a, int n, int lda, T* r, int ldr,
+                                   const typename QrArith<T>::R* rdiag) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (long long)n * n) return;
   const int i = (int)(e / n);   // column
   const int row = (int)(e - (long long)i * n);
   T v;
   if (row < i) v = a[(long long)i * lda + row];
-  else if (row == i) v = rdiag[i];
-  else v = (T)0;
+  else if (row == i) v = QrArith<T>::rdiag_elem(rdiag[i]);
+  else v = QrArith<T>::rdiag_elem(0);
   r[(long long)i * ldr + row] = v;
 }
 
@@ -263,6 +338,27 @@ cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const 
   const int threads = 128;
   qr_r_single_kernel<T><<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
       a, n, lda, r, ldr, rdiag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zqr_single(double* a, int m, int n, int lda, double* rdiag, double* scratch,
+                              cudaStream_t s) {
+  qr_single_kernel<zdouble><<<1, 32, 0, s>>>((zdouble*)a, m, n, lda, rdiag, (zdouble*)scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zqr_q_single(const double* a, int m, int n, int lda, double* q, int ldq,
+                                double* scratch, cudaStream_t s) {
+  qr_q_single_kernel<zdouble><<<1, 32, 0, s>>>((const zdouble*)a, m, n, lda, (zdouble*)q, ldq,
+                                               (zdouble*)scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zqr_r_single(const double* a, int n, int lda, double* r, int ldr,
+                                const double* rdiag, cudaStream_t s) {
+  const long long total = (long long)n * n;
+  qr_r_single_kernel<zdouble><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+      (const zdouble*)a, n, lda, (zdouble*)r, ldr, rdiag);
   return cudaGetLastError();
 }
 

@@ -871,6 +871,346 @@ MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b)
   return plan_execute(plan, a, rdiag, b, (const void*)2, nullptr);
 }
 
+
+// ------------------------------------------------------------------------------------------
+// Float and Complex overloads of the single-matrix drop-ins.  Complex arrays are interleaved
+// (re, im) doubles, the layout of System.Numerics.Complex; es is the element size in bytes.
+
+}  // extern "C"
+
+namespace {
+
+int getrf_t(mfg_ctx* ctx, int m, int n, void* a, int lda, int* piv, int* sign, size_t es,
+            cudaError_t (*launch)(void*, int, int, int, int*, int*, double*, cudaStream_t)) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!piv) return fail(ctx, -6, "piv is null");
+  const size_t na = span(m, n, lda);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(2 * (size_t)m + 2, 8) +
+                      Carve::bytes_for(m, 4) + Carve::bytes_for(2, 4);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  char* d_a = cv.take<char>(na * es);
+  double* d_s = cv.take<double>(2 * (size_t)m + 2);
+  int* d_piv = cv.take<int>(m);
+  int* d_out = cv.take<int>(2);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, launch(d_a, m, n, lda, d_piv, d_out, d_s, s));
+  int out[2];
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  if (sign) *sign = out[0];
+  return MFG_OK;
+}
+
+int potrf_t(mfg_ctx* ctx, int n, void* a, int lda, int* info, size_t es,
+            cudaError_t (*launch)(void*, int, int, int*, double*, cudaStream_t)) {
+  if (!ctx) return -1;
+  if (n <= 0) return fail(ctx, -2, "The order of the matrix must be greater than or equal to one.");
+  if (!a) return fail(ctx, -3, "a is null");
+  if (lda < n)
+    return fail(ctx, -4,
+                "The leading dimension must be greater than or equal to the order of the matrix.");
+  const size_t na = span(n, n, lda);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(n, 8) + Carve::bytes_for(1, 4);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  char* d_a = cv.take<char>(na * es);
+  double* d_s = cv.take<double>(n);
+  int* d_out = cv.take<int>(1);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, launch(d_a, n, lda, d_out, d_s, s));
+  int out = 0;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)n * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  if (info) *info = out;
+  return MFG_OK;
+}
+
+int trsv_t(mfg_ctx* ctx, int uplo, int trans, int n, const void* a, int lda, void* x, int incx,
+           size_t es, bool complex_modes,
+           cudaError_t (*launch)(int, int, int, const void*, int, void*, int, double*,
+                                 cudaStream_t)) {
+  if (!ctx) return -1;
+  if (n <= 0) return fail(ctx, -4, "The order of the matrix must be greater than or equal to one.");
+  if (!a) return fail(ctx, -5, "a is null");
+  if (lda < n)
+    return fail(ctx, -6,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!x) return fail(ctx, -7, "x is null");
+  if (incx <= 0) return fail(ctx, -8, "The value must be greater than or equal to one.");
+  if (uplo != MFG_UPPER && uplo != MFG_LOWER) return fail(ctx, -2, "Invalid enum value.");
+  const bool okt = trans == MFG_NOTRANS || trans == MFG_TRANS ||
+                   (complex_modes && (trans == MFG_CONJTRANS || trans == MFG_CONJNOTRANS));
+  if (!okt) return fail(ctx, -3, "Invalid enum value.");
+  const size_t na = span(n, n, lda);
+  const size_t nx = (size_t)(n - 1) * incx + 1;
+  const size_t nscr = 4 * (size_t)(n | 1);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(nx, es) + Carve::bytes_for(nscr, 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  char* d_a = cv.take<char>(na * es);
+  char* d_x = cv.take<char>(nx * es);
+  double* d_s = cv.take<double>(nscr);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * es, cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, launch(uplo, trans, n, d_a, lda, d_x, incx, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * es, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+int gemm_t(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const void* a, int lda,
+           const void* b, int ldb, void* c, int ldc, size_t es, bool complex_modes,
+           cudaError_t (*launch)(int, int, int, int, int, const void*, int, const void*, int,
+                                 void*, int, cudaStream_t)) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -5, "The value must be greater than or equal to one.");
+  if (k <= 0) return fail(ctx, -6, "The value must be greater than or equal to one.");
+  if (!a) return fail(ctx, -7, "a is null");
+  auto valid = [&](int t) {
+    return t == MFG_NOTRANS || t == MFG_TRANS ||
+           (complex_modes && (t == MFG_CONJTRANS || t == MFG_CONJNOTRANS));
+  };
+  auto is_t = [](int t) { return t == MFG_TRANS || t == MFG_CONJTRANS; };
+  if (!valid(transa)) return fail(ctx, -2, "Invalid enum value.");
+  if (lda < (is_t(transa) ? k : m))
+    return fail(ctx, -8, "The leading dimension must be greater than or equal to the number of rows.");
+  if (!b) return fail(ctx, -9, "b is null");
+  if (!valid(transb)) return fail(ctx, -3, "Invalid enum value.");
+  if (ldb < (is_t(transb) ? n : k))
+    return fail(ctx, -10, "The leading dimension must be greater than or equal to the number of rows.");
+  if (!c) return fail(ctx, -11, "c is null");
+  if (ldc < m)
+    return fail(ctx, -12, "The leading dimension must be greater than or equal to the number of rows.");
+  if (c == a || c == b) return fail(ctx, MFG_ERR_INPLACE, "In-place operation is not supported.");
+  const int ar = is_t(transa) ? k : m, ac = is_t(transa) ? m : k;
+  const int br = is_t(transb) ? n : k, bc = is_t(transb) ? k : n;
+  const size_t na = span(ar, ac, lda), nb = span(br, bc, ldb), nc = span(m, n, ldc);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(nb, es) + Carve::bytes_for(nc, es);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  char* d_a = cv.take<char>(na * es);
+  char* d_b = cv.take<char>(nb * es);
+  char* d_c = cv.take<char>(nc * es);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)ar * es, ac,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_b, (size_t)ldb * es, b, (size_t)ldb * es, (size_t)br * es, bc,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, launch(transa, transb, m, n, k, d_a, lda, d_b, ldb, d_c, ldc, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(c, (size_t)ldc * es, d_c, (size_t)ldc * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+// Launch adapters from the typeless helpers to the typed kernels.
+cudaError_t sgetrf_l(void* a, int m, int n, int lda, int* piv, int* o, double* s, cudaStream_t st) {
+  return mfg::launch_sgetrf_single((float*)a, m, n, lda, piv, o, s, st);
+}
+cudaError_t zgetrf_l(void* a, int m, int n, int lda, int* piv, int* o, double* s, cudaStream_t st) {
+  return mfg::launch_zgetrf_single((double*)a, m, n, lda, piv, o, s, st);
+}
+cudaError_t spotrf_l(void* a, int n, int lda, int* o, double* s, cudaStream_t st) {
+  return mfg::launch_spotrf_single((float*)a, n, lda, o, s, st);
+}
+cudaError_t zpotrf_l(void* a, int n, int lda, int* o, double* s, cudaStream_t st) {
+  return mfg::launch_zpotrf_single((double*)a, n, lda, o, s, st);
+}
+cudaError_t strsv_l(int u, int t, int n, const void* a, int lda, void* x, int incx, double* s,
+                    cudaStream_t st) {
+  return mfg::launch_strsv_single(u, t, n, (const float*)a, lda, (float*)x, incx, s, st);
+}
+cudaError_t ztrsv_l(int u, int t, int n, const void* a, int lda, void* x, int incx, double* s,
+                    cudaStream_t st) {
+  return mfg::launch_ztrsv_single(u, t, n, (const double*)a, lda, (double*)x, incx, s, st);
+}
+cudaError_t sgemm_l(int ta, int tb, int m, int n, int k, const void* a, int lda, const void* b,
+                    int ldb, void* c, int ldc, cudaStream_t st) {
+  return mfg::launch_sgemm_single(ta, tb, m, n, k, (const float*)a, lda, (const float*)b, ldb,
+                                  (float*)c, ldc, st);
+}
+cudaError_t zgemm_l(int ta, int tb, int m, int n, int k, const void* a, int lda, const void* b,
+                    int ldb, void* c, int ldc, cudaStream_t st) {
+  return mfg::launch_zgemm_single(ta, tb, m, n, k, (const double*)a, lda, (const double*)b, ldb,
+                                  (double*)c, ldc, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+MFG_API int mfg_sgetrf(mfg_ctx* ctx, int m, int n, float* a, int lda, int* piv, int* sign) {
+  return getrf_t(ctx, m, n, a, lda, piv, sign, sizeof(float), sgetrf_l);
+}
+MFG_API int mfg_zgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign) {
+  return getrf_t(ctx, m, n, a, lda, piv, sign, 2 * sizeof(double), zgetrf_l);
+}
+MFG_API int mfg_spotrf(mfg_ctx* ctx, int n, float* a, int lda, int* info) {
+  return potrf_t(ctx, n, a, lda, info, sizeof(float), spotrf_l);
+}
+MFG_API int mfg_zpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
+  return potrf_t(ctx, n, a, lda, info, 2 * sizeof(double), zpotrf_l);
+}
+MFG_API int mfg_strsv(mfg_ctx* ctx, int uplo, int trans, int n, const float* a, int lda, float* x,
+                      int incx) {
+  return trsv_t(ctx, uplo, trans, n, a, lda, x, incx, sizeof(float), false, strsv_l);
+}
+MFG_API int mfg_ztrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
+                      double* x, int incx) {
+  return trsv_t(ctx, uplo, trans, n, a, lda, x, incx, 2 * sizeof(double), true, ztrsv_l);
+}
+MFG_API int mfg_sgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const float* a,
+                      int lda, const float* b, int ldb, float* c, int ldc) {
+  return gemm_t(ctx, transa, transb, m, n, k, a, lda, b, ldb, c, ldc, sizeof(float), false,
+                sgemm_l);
+}
+MFG_API int mfg_zgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
+                      int lda, const double* b, int ldb, double* c, int ldc) {
+  return gemm_t(ctx, transa, transb, m, n, k, a, lda, b, ldb, c, ldc, 2 * sizeof(double), true,
+                zgemm_l);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Complex QR staging (the QR template above is keyed on float/double; Complex uses these).
+int zqr_single(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!rdiag) return fail(ctx, -6, "rdiag is null");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  const size_t es = 16;
+  const size_t na = span(m, n, lda);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(n, 8) +
+                      Carve::bytes_for(2 * (size_t)(n + 1), 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(2 * na);
+  double* d_r = cv.take<double>(n);
+  double* d_s = cv.take<double>(2 * (size_t)(n + 1));
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_zqr_single(d_a, m, n, lda, d_r, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * 8, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+int zqr_q_single(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!q) return fail(ctx, -6, "q is null");
+  if (ldq < m)
+    return fail(ctx, -7,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  const size_t es = 16;
+  const size_t na = span(m, n, lda), nq = span(m, n, ldq);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(nq, es) +
+                      Carve::bytes_for(2 * (size_t)(n + 1), 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(2 * na);
+  double* d_q = cv.take<double>(2 * nq);
+  double* d_s = cv.take<double>(2 * (size_t)(n + 1));
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_zqr_q_single(d_a, m, n, lda, d_q, ldq, d_s, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(q, (size_t)ldq * es, d_q, (size_t)ldq * es, (size_t)m * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+int zqr_r_single(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
+                 const double* rdiag) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -4, "a is null");
+  if (lda < m)
+    return fail(ctx, -5,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!r) return fail(ctx, -6, "r is null");
+  if (ldr < n)
+    return fail(ctx, -7,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (n > m)
+    return fail(ctx, -3,
+                "The number of rows must be greater than or equal to the number of columns.");
+  if (!rdiag) return fail(ctx, -8, "rdiag is null");
+  const size_t es = 16;
+  const size_t na = span(n, n, lda), nr = span(n, n, ldr);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(nr, es) + Carve::bytes_for(n, 8);
+  MFG_CUDA(ctx, ctx->work.reserve(need));
+  Carve cv(ctx->work.ptr);
+  double* d_a = cv.take<double>(2 * na);
+  double* d_r = cv.take<double>(2 * nr);
+  double* d_d = cv.take<double>(n);
+  cudaStream_t s = ctx->stream;
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
+                                  cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * 8, cudaMemcpyHostToDevice, s));
+  MFG_CUDA(ctx, mfg::launch_zqr_r_single(d_a, n, lda, d_r, ldr, d_d, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(r, (size_t)ldr * es, d_r, (size_t)ldr * es, (size_t)n * es, n,
+                                  cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MFG_API int mfg_zgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
+  return zqr_single(ctx, m, n, a, lda, rdiag);
+}
+MFG_API int mfg_zorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq) {
+  return zqr_q_single(ctx, m, n, a, lda, q, ldq);
+}
+MFG_API int mfg_zqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
+                      const double* rdiag) {
+  return zqr_r_single(ctx, m, n, a, lda, r, ldr, rdiag);
+}
+
 // ------------------------------------------------------------------------------------------
 // Batched plans.
 

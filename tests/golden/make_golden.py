@@ -75,6 +75,12 @@ def random_single(seed, count):
         np.float32)
 
 
+def random_complex(seed, count):
+    """Matrix.RandomComplex (MatFlatTest/Matrix.cs:23-28): re and im in [-1, 1) from one stream."""
+    v = 2.0 * np.random.default_rng(seed).random(2 * count) - 1.0
+    return v[0::2] + 1j * v[1::2]
+
+
 def fmat(flat, m, n, ld):
     """m-by-n Fortran view (copy) of a column-major flat array with leading dimension ld."""
     return np.array(flat[:ld * n].reshape(n, ld).T[:m, :], order="F")
@@ -236,6 +242,120 @@ def main():
         rc = oracle.lu_inverse(n, inv, lda, piv)
         assert rc == 0
         g[key + "/oracle"] = inv
+
+    # ---- Complex LU (LuTests.cs:194-286; LAPACK pivots by |re| + |im| too) -----------------
+    for (m, n, lda) in LU_SHAPES:
+        a = random_complex(42, n * lda)
+        key = "lu_z/%d_%d_%d" % (m, n, lda)
+        g[key + "/in"] = a
+        lu_ = a.copy()
+        piv = np.zeros(m, np.int32)
+        sign = oracle.lu(m, n, lu_, lda, piv)
+        g[key + "/oracle"] = lu_
+        g[key + "/oracle_piv"] = piv
+        g[key + "/oracle_sign"] = np.array([sign], np.int32)
+        lu_l, ipiv, info = slapack.zgetrf(fmat(a, m, n, lda))
+        g[key + "/lapack"] = put(a, lu_l, lda)
+
+    # ---- float and Complex Cholesky (CholeskyTests.cs:12-92, :178-260) ----------------------
+    for (n, lda) in CHOL_SHAPES:
+        for prec in ("s", "z"):
+            for kind in ("general", "maybe"):
+                if prec == "s":
+                    a = random_single(42, n * lda)
+                else:
+                    a = random_complex(42, n * lda)
+                if kind == "general":
+                    am = fmat(a, n, n, lda)
+                    sm = am @ am.conj().T
+                    for j in range(n):
+                        for i in range(n):
+                            a[j * lda + i] = sm[i, j] if j >= i else np.nan
+                else:
+                    for j in range(n):
+                        for i in range(j + 1, n):
+                            a[j * lda + i] = np.nan
+                key = "chol_%s/%s_%d_%d" % (prec, kind, n, lda)
+                g[key + "/in"] = a
+                c = a.copy()
+                g[key + "/oracle_info"] = np.array([oracle.cholesky(n, c, lda)], np.int32)
+                g[key + "/oracle"] = c
+                up = np.triu(np.nan_to_num(fmat(a, n, n, lda)))
+                f = slapack.spotrf if prec == "s" else slapack.zpotrf
+                r, linfo = f(up, lower=0)
+                g[key + "/lapack_info"] = np.array([linfo], np.int32)
+                g[key + "/lapack"] = put(a.copy(), np.tril(r.conj().T), lda)
+
+    # ---- Complex QR ------------------------------------------------------------------------
+    for (m, n, lda, ldq, ldr) in QR_SHAPES:
+        a = random_complex(42, n * lda)
+        key = "qr_z/%d_%d_%d_%d_%d" % (m, n, lda, ldq, ldr)
+        g[key + "/in"] = a
+        g[key + "/q_in"] = random_complex(57, n * ldq)
+        g[key + "/r_in"] = random_complex(58, n * ldr)
+        qa = a.copy()
+        rd = np.zeros(n)
+        oracle.qr(m, n, qa, lda, rd)
+        q = g[key + "/q_in"].copy()
+        oracle.qr_q(m, n, qa, lda, q, ldq)
+        r = g[key + "/r_in"].copy()
+        oracle.qr_r(m, n, qa, lda, r, ldr, rd)
+        g[key + "/oracle"], g[key + "/oracle_rdiag"] = qa, rd
+        g[key + "/oracle_q"], g[key + "/oracle_r"] = q, r
+
+    # ---- float and Complex triangular solves (SolveTriangularSingle/Complex.cs) --------------
+    CT, CN = 113, 114
+    for (n, lda, incx) in TRSV_SHAPES:
+        for prec, modes in (("s", (NT, T)), ("z", (NT, T, CT, CN))):
+            for uplo in (U, L):
+                for trans in modes:
+                    if prec == "s":
+                        a = random_single(42, n * lda)
+                        x = random_single(57, (n - 1) * incx + 1)
+                    else:
+                        a = random_complex(42, n * lda)
+                        x = random_complex(57, (n - 1) * incx + 1)
+                    for j in range(n):
+                        for i in range(n):
+                            if (uplo == U and i > j) or (uplo == L and i < j):
+                                a[j * lda + i] = 0.0
+                    key = "trsv_%s/%d_%d_%d_%d_%d" % (prec, uplo, trans, n, lda, incx)
+                    g[key + "/a"], g[key + "/x"] = a, x
+                    xo = x.copy()
+                    oracle.trsv(uplo, trans, n, a, lda, xo, incx)
+                    g[key + "/oracle"] = xo
+                    am = fmat(a, n, n, lda).astype(np.complex128 if prec == "z" else np.float64)
+                    op = {NT: am, T: am.T, CT: am.conj().T, CN: am.conj()}[trans]
+                    xe = x.astype(np.complex128 if prec == "z" else np.float64)
+                    sol = np.linalg.solve(op, xe[::incx][:n])
+                    xe[::incx][:n] = sol
+                    g[key + "/lapack"] = xe
+
+    # ---- float and Complex MulMatMat (MulMatMatSingle/Complex.cs, four conj conditions) ------
+    for mode, shapes in GEMM_SHAPES.items():
+        for prec in ("s", "z"):
+            conds = [(False, False)] if prec == "s" else [(False, False), (True, False),
+                                                         (False, True), (True, True)]
+            for (ca, cb) in conds:
+                ta = (CN if ca else NT) if mode[0] == "N" else (CT if ca else T)
+                tb = (CN if cb else NT) if mode[1] == "N" else (CT if cb else T)
+                for (m, n, k, lda, ldb, ldc) in shapes:
+                    ar, ac = (m, k) if mode[0] == "N" else (k, m)
+                    br, bc = (k, n) if mode[1] == "N" else (n, k)
+                    rnd = random_single if prec == "s" else random_complex
+                    a, b, c = rnd(42, ac * lda), rnd(57, bc * ldb), rnd(0, n * ldc)
+                    key = "gemm_%s/%d_%d_%d_%d_%d_%d_%d_%d" % (prec, ta, tb, m, n, k, lda, ldb, ldc)
+                    g[key + "/a"], g[key + "/b"], g[key + "/c"] = a, b, c
+                    co = c.copy()
+                    oracle.gemm(ta, tb, m, n, k, a, lda, b, ldb, co, ldc)
+                    g[key + "/oracle"] = co
+                    am = fmat(a, ar, ac, lda).astype(np.complex128 if prec == "z" else np.float64)
+                    bm = fmat(b, br, bc, ldb).astype(np.complex128 if prec == "z" else np.float64)
+                    am = am if mode[0] == "N" else am.T
+                    bm = bm if mode[1] == "N" else bm.T
+                    am = am.conj() if ca else am
+                    bm = bm.conj() if cb else bm
+                    g[key + "/lapack"] = put(c.astype(am.dtype), am @ bm, ldc)
 
     np.savez_compressed(OUT, **g)
     print("wrote %s (%d arrays, %.1f KB)" % (OUT, len(g), os.path.getsize(OUT) / 1024))

@@ -212,3 +212,81 @@ def test_batched_oracle_matches_single():
     X = b5.reshape(2, ni).T
     B = b[b_off[i]:b_off[i] + 2 * ni].reshape(2, ni).T
     assert np.max(np.abs(A @ X - B)) <= 1e-9 * max(1, np.max(np.abs(X)))
+
+
+# ---- float and Complex overloads --------------------------------------------------------------
+
+def test_lu_complex_oracle_pin(golden):
+    keys = cases(golden, "lu_z/")
+    assert keys
+    for key in keys:
+        m, n, lda = map(int, key.split("/")[1].split("_"))
+        a = golden[key + "/in"].copy()
+        piv = np.zeros(m, np.int32)
+        oracle.lu(m, n, a, lda, piv)
+        np.testing.assert_array_equal(a.view(np.uint8), golden[key + "/oracle"].view(np.uint8))
+        assert np.max(np.abs(a - golden[key + "/lapack"])) <= 1e-12, key   # LuTests.cs:234-235
+
+
+@pytest.mark.parametrize("prec,tol", [("s", 1e-5), ("z", 1e-12)])
+def test_cholesky_float_complex_oracle_pin(golden, prec, tol):
+    keys = cases(golden, "chol_%s/" % prec)
+    assert keys
+    for key in keys:
+        _, n, lda = key.split("/")[1].split("_")
+        n, lda = int(n), int(lda)
+        a = golden[key + "/in"].copy()
+        info = oracle.cholesky(n, a, lda)
+        assert info == golden[key + "/oracle_info"][0]
+        assert (info == 0) == (golden[key + "/lapack_info"][0] == 0), key
+        if info == 0:
+            np.testing.assert_array_equal(a.view(np.uint8), golden[key + "/oracle"].view(np.uint8))
+            exp = golden[key + "/lapack"]
+            for j in range(n):
+                col = slice(j * lda, j * lda + n)
+                assert np.max(np.abs(a[col] - exp[col])) <= tol, key
+
+
+def test_qr_complex_oracle_pin(golden):
+    for key in cases(golden, "qr_z/"):
+        m, n, lda, ldq, ldr = map(int, key.split("/")[1].split("_"))
+        a = golden[key + "/in"].copy()
+        rd = np.zeros(n)
+        oracle.qr(m, n, a, lda, rd)
+        q = golden[key + "/q_in"].copy()
+        oracle.qr_q(m, n, a, lda, q, ldq)
+        r = golden[key + "/r_in"].copy()
+        oracle.qr_r(m, n, a, lda, r, ldr, rd)
+        for got, name in ((a, "oracle"), (rd, "oracle_rdiag"), (q, "oracle_q"), (r, "oracle_r")):
+            np.testing.assert_array_equal(got.view(np.uint8), golden[key + "/" + name].view(np.uint8))
+        A = golden[key + "/in"][:n * lda].reshape(n, lda).T[:m]
+        Q = q[:n * ldq].reshape(n, ldq).T[:m]
+        R = r[:n * ldr].reshape(n, ldr).T[:n]
+        assert np.max(np.abs(Q @ R - A)) <= 1e-12, key                        # QrTests.cs:452-470
+        assert np.max(np.abs(Q.conj().T @ Q - np.eye(n))) <= 1e-12, key
+
+
+@pytest.mark.parametrize("prec,tol", [("s", 1e-3), ("z", 1e-11)])
+def test_trsv_float_complex_oracle_pin(golden, prec, tol):
+    keys = cases(golden, "trsv_%s/" % prec)
+    assert len(keys) == (40 if prec == "s" else 80)
+    for key in keys:
+        uplo, trans, n, lda, incx = map(int, key.split("/")[1].split("_"))
+        x = golden[key + "/x"].copy()
+        assert oracle.trsv(uplo, trans, n, golden[key + "/a"], lda, x, incx) == 0
+        np.testing.assert_array_equal(x.view(np.uint8), golden[key + "/oracle"].view(np.uint8))
+        exp = golden[key + "/lapack"]
+        assert np.max(np.abs(x - exp)) <= tol * max(1.0, np.max(np.abs(exp))), key
+
+
+@pytest.mark.parametrize("prec,tol", [("s", 1e-6), ("z", 1e-12)])
+def test_gemm_float_complex_oracle_pin(golden, prec, tol):
+    keys = cases(golden, "gemm_%s/" % prec)
+    assert len(keys) == (39 if prec == "s" else 156)
+    for key in keys:
+        ta, tb, m, n, k, lda, ldb, ldc = map(int, key.split("/")[1].split("_"))
+        c = golden[key + "/c"].copy()
+        assert oracle.gemm(ta, tb, m, n, k, golden[key + "/a"], lda, golden[key + "/b"], ldb,
+                           c, ldc) == 0
+        np.testing.assert_array_equal(c.view(np.uint8), golden[key + "/oracle"].view(np.uint8))
+        assert np.max(np.abs(c - golden[key + "/lapack"])) <= tol, key
