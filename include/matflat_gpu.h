@@ -221,6 +221,23 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
                                                 double* loss, double* grad, int* info,
                                                 int keep_factor);
 
+/* Mixed-precision LU solve with FP64 iterative refinement (new; no MatFlat counterpart).
+ * A plan for `count` systems of one order n (a multiple of 32, at most 1024); matrices packed
+ * column-major with lda = n at stride n*n, right-hand sides and solutions at stride n.
+ * The solver factors FP32 copies of A with partial pivoting (trailing updates on the tensor cores
+ * in TF32 or BF16 with FP32 accumulation, or on the FP32 cores), then refines in FP64:
+ * r = b - A x, d = (LU)^-1 r in FP32, x += d, until the normwise backward error
+ * berr = |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) <= tol, stalls, or max_iter sweeps pass.
+ * Systems that do not converge are solved again with the exact FP64 LU (Factorization.Lu's
+ * arithmetic).  Outputs per system: x, berr, iters (refinement sweeps), info (0 refined to tol,
+ * 1 solved by the FP64 fallback, 2 singular).  a, b, x, berr, iters and info are device
+ * pointers; the call returns after the results are complete. */
+enum mfg_lowp { MFG_LOWP_FP32 = 0, MFG_LOWP_TF32 = 1, MFG_LOWP_BF16 = 2 };
+MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n);
+MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const double* b, double* x,
+                                    int lowp, int max_iter, double tol, double* berr, int* iters,
+                                    int* info);
+
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 
 /* Reads back the device-side status word of the last execution of `plan` (synchronizes the

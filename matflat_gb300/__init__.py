@@ -22,6 +22,7 @@ from ._api import (  # noqa: F401
     LuBatch,
     MatFlatException,
     MatrixFactorizationException,
+    MixedSolveBatch,
     QrBatch,
     Transpose,
     Uplo,

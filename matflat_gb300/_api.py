@@ -55,6 +55,9 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
+    "mfg_plan_gesv_mixed_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _I]),
+    "mfg_dgesv_mixed_batched": (_I, [_vp, _vp, _vp, _vp, _I, _I, ctypes.c_double, _vp, _vp,
+                                     _vp]),
     "mfg_dpotrf_logdet_solve_grad_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrf_strided_batched_noalloc": (_I, [_vp, _I, _I, _vp, _I, ctypes.c_int64, _vp,
                                                 ctypes.c_int64, _I, _vp, ctypes.c_int64, _vp,
@@ -484,3 +487,26 @@ def selftest_dmul(a, b, out):
     ctx = context()
     ctx.check(ctx.lib.mfg_selftest_dmul(ctx.h, _dptr(a), _dptr(b), _dptr(out), a.numel()),
               "mfg_selftest_dmul")
+
+
+LOWP = {"fp32": 0, "tf32": 1, "bf16": 2}
+
+
+class MixedSolveBatch(_Batch):
+    """Mixed-precision LU solve with FP64 iterative refinement for `count` systems of order n
+    (device buffers: a count*n*n, b and x count*n, berr/iters/info count)."""
+
+    def __init__(self, count, n, ctx=None):
+        ctx = ctx or context()
+        h = _vp()
+        ctx.check(ctx.lib.mfg_plan_gesv_mixed_batched(ctx.h, ctypes.byref(h), count, n),
+                  "mfg_plan_gesv_mixed_batched")
+        super().__init__(ctx, h)
+        self.count = count
+        self.n = n
+
+    def run(self, a, b, x, berr, iters, info, lowp="tf32", max_iter=10, tol=1e-12):
+        rc = self.ctx.lib.mfg_dgesv_mixed_batched(self.h, _dptr(a), _dptr(b), _dptr(x),
+                                                  LOWP[lowp], max_iter, tol, _dptr(berr),
+                                                  _dptr(iters), _dptr(info))
+        self.ctx.check(rc, "mfg_dgesv_mixed_batched")

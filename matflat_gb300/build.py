@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libmatflat_gpu.so")
 SYNTH_LIB = os.path.join(OUT, "libmatflat_synth.so")
-SOURCES = ["lu.cu", "chol.cu", "blas.cu", "qr.cu", "runtime.cu"]
+SOURCES = ["lu.cu", "chol.cu", "blas.cu", "qr.cu", "mixed.cu", "runtime.cu"]
 HEADERS = ["mf_device.cuh", "mf_solve.cuh", "mf_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
@@ -73,8 +73,8 @@ def build(force=False, verbose=False, extra_flags=()):
                 if r.returncode != 0:
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart_static", "-lrt",
-                                                                        "-ldl", "-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcublas", "-lcudart_static",
+                                                                        "-lrt", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -89,6 +89,20 @@ cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long st
                                          long long stride_b, int* sign, int* info, int count,
                                          int sm_count, cudaStream_t s);
 
+// Mixed-precision LU solve with FP64 refinement (mixed.cu).
+int mx_panel_width();
+cudaError_t mx_panel_attr(int nmax);
+cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t s);
+cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
+                     cudaStream_t s);
+cudaError_t mx_update_fp32(float* a32, int n, int k, const int* active, int count,
+                           cudaStream_t s);
+cudaError_t mx_bf16_operands(const float* a32, int n, int k, void* l21, void* u12,
+                             const int* active, int count, cudaStream_t s);
+cudaError_t mx_refine(const double* a, const double* b, double* x, const float* lu,
+                      const int* ipiv, int n, int count, int iter, double tol, double* berr,
+                      int* iters, int* state, double* anorm, int* active, cudaStream_t s);
+
 // One-time per-device set-up of kernel attributes (dynamic shared-memory limits).
 cudaError_t init_getrf_attributes();
 cudaError_t init_potrf_attributes();

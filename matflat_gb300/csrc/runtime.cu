@@ -3,6 +3,7 @@
 //
 // Argument validation mirrors MatFlat's checks, in MatFlat's order, and reports the 1-based
 // position of the offending argument as a negative status (the context is argument 1).
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -55,6 +56,7 @@ cudaError_t g_attr_err[64];
 }  // namespace
 
 struct mfg_ctx {
+  cublasHandle_t cublas = nullptr;  // created on first use (mixed-precision trailing updates)
   int device = 0;
   int sm_count = 0;
   cudaStream_t own_stream = nullptr;
@@ -65,7 +67,7 @@ struct mfg_ctx {
 };
 
 struct mfg_plan {
-  enum Kind { GETRF, POTRF, GEQRF } kind;
+  enum Kind { GETRF, POTRF, GEQRF, MIXED } kind;
   mfg_ctx* ctx = nullptr;
   int count = 0;
   int nrhs = 0;
@@ -76,6 +78,8 @@ struct mfg_plan {
   mfg::QrBatchArgs<double> qd{};
   mfg::QrBatchArgs<float> qs{};
   int qr_float = 0;  // GEQRF: which precision the next launch runs
+  int mx_n = 0;      // MIXED: order of every matrix
+  DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
   int ctas = 0;
   int warps = 0;
   // CUDA graph of the last execution (keyed by the data pointers and the stream).
@@ -477,6 +481,7 @@ MFG_API int mfg_create(mfg_ctx** ctx) {
 MFG_API int mfg_destroy(mfg_ctx* ctx) {
   if (!ctx) return -1;
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->cublas) cublasDestroy(ctx->cublas);
   ctx->work.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -1232,6 +1237,7 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   cudaStreamSynchronize(plan->ctx->stream);
   plan->meta.release();
   plan->scratch.release();
+  plan->mx_work.release();
   delete plan;
   return MFG_OK;
 }
@@ -1339,6 +1345,187 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
                                              ((long long)plan->count + 3) / 4);
   MFG_CUDA(ctx, mfg::launch_chol_grad_batched(a, loss, grad, keep_factor ? 1 : 0,
                                               (int)std::max<long long>(1, ctas), s));
+  return MFG_OK;
+}
+
+
+// ------------------------------------------------------------------------------------------
+// Mixed-precision LU solve with FP64 iterative refinement.
+
+MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n) {
+  if (!ctx) return -1;
+  if (!plan) return fail(ctx, -2, "plan output pointer is null");
+  *plan = nullptr;
+  if (count < 0) return fail(ctx, -3, "count must be >= 0");
+  const int nb = mfg::mx_panel_width();
+  if (n < nb || n > 1024 || n % nb != 0)
+    return fail(ctx, -4, "n = %d: the mixed solver takes multiples of %d up to 1024", n, nb);
+  mfg_plan* p = new mfg_plan();
+  p->kind = mfg_plan::MIXED;
+  p->ctx = ctx;
+  p->count = count;
+  p->nrhs = 1;
+  p->mx_n = n;
+  p->max_n = n;
+  const size_t nn = (size_t)n * n * count;
+  const size_t bytes = Carve::bytes_for(nn, 4) + Carve::bytes_for((size_t)n * count, 4) +
+                       2 * Carve::bytes_for((size_t)n * nb * count, 2) +
+                       Carve::bytes_for(count, 8) + 3 * Carve::bytes_for(count, 4) + 256;
+  cudaError_t e = p->mx_work.reserve(bytes);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMalloc(mixed workspace)");
+  }
+  e = p->meta.reserve(256);
+  if (e == cudaSuccess) e = mfg::mx_panel_attr(1024);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "mixed plan set-up");
+  }
+  p->args.queue = (int*)p->meta.ptr;
+  *plan = p;
+  return MFG_OK;
+}
+
+MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const double* b, double* x,
+                                    int lowp, int max_iter, double tol, double* berr,
+                                    int* iters, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::MIXED) return fail(ctx, -1, "plan is not a mixed-precision plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!b) return fail(ctx, -3, "b is null");
+  if (!x) return fail(ctx, -4, "x is null");
+  if (lowp != MFG_LOWP_FP32 && lowp != MFG_LOWP_TF32 && lowp != MFG_LOWP_BF16)
+    return fail(ctx, -5, "unknown low precision %d", lowp);
+  if (max_iter < 0) return fail(ctx, -6, "max_iter must be >= 0");
+  if (!(tol > 0)) return fail(ctx, -7, "tol must be > 0");
+  if (!berr) return fail(ctx, -8, "berr is null");
+  if (!iters) return fail(ctx, -9, "iters is null");
+  if (!info) return fail(ctx, -10, "info is null");
+  const int n = plan->mx_n, count = plan->count, nb = mfg::mx_panel_width();
+  cudaStream_t s = ctx->stream;
+  Carve cv(plan->mx_work.ptr);
+  float* a32 = cv.take<float>((size_t)n * n * count);
+  int* ipiv = cv.take<int>((size_t)n * count);
+  void* l21 = cv.take<uint16_t>((size_t)n * nb * count);
+  void* u12 = cv.take<uint16_t>((size_t)n * nb * count);
+  double* anorm = cv.take<double>(count);
+  int* state = cv.take<int>(count);
+  int* active = cv.take<int>(count);
+  if (lowp != MFG_LOWP_FP32 && !ctx->cublas) {
+    if (cublasCreate(&ctx->cublas) != CUBLAS_STATUS_SUCCESS)
+      return fail(ctx, MFG_ERR_CUDA, "cublasCreate failed");
+  }
+  if (ctx->cublas) {
+    cublasSetStream(ctx->cublas, s);
+    cublasSetMathMode(ctx->cublas, lowp == MFG_LOWP_TF32 ? CUBLAS_TF32_TENSOR_OP_MATH
+                                                         : CUBLAS_DEFAULT_MATH);
+  }
+  MFG_CUDA(ctx, mfg::mx_round(a, a32, (long long)n * n * count, s));
+  const long long sa = (long long)n * n;
+  const float alpha = -1.0f, beta = 1.0f;
+  for (int k = 0; k < n; k += nb) {
+    MFG_CUDA(ctx, mfg::mx_panel(a32, n, k, ipiv, nullptr, count, s));
+    const int m2 = n - k - nb;
+    if (m2 <= 0) continue;
+    float* L21 = a32 + (long long)k * n + k + nb;
+    float* U12 = a32 + (long long)(k + nb) * n + k;
+    float* A22 = a32 + (long long)(k + nb) * n + k + nb;
+    if (lowp == MFG_LOWP_FP32) {
+      MFG_CUDA(ctx, mfg::mx_update_fp32(a32, n, k, nullptr, count, s));
+    } else if (lowp == MFG_LOWP_TF32) {
+      cublasStatus_t st = cublasGemmStridedBatchedEx(
+          ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m2, m2, nb, &alpha, L21, CUDA_R_32F, n, sa, U12,
+          CUDA_R_32F, n, sa, &beta, A22, CUDA_R_32F, n, sa, count, CUBLAS_COMPUTE_32F_FAST_TF32,
+          CUBLAS_GEMM_DEFAULT);
+      if (st != CUBLAS_STATUS_SUCCESS)
+        return fail(ctx, MFG_ERR_CUDA, "TF32 trailing update failed (cuBLAS %d)", (int)st);
+    } else {
+      MFG_CUDA(ctx, mfg::mx_bf16_operands(a32, n, k, l21, u12, nullptr, count, s));
+      cublasStatus_t st = cublasGemmStridedBatchedEx(
+          ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m2, m2, nb, &alpha, l21, CUDA_R_16BF, m2,
+          (long long)n * nb, u12, CUDA_R_16BF, nb, (long long)n * nb, &beta, A22, CUDA_R_32F, n,
+          sa, count, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+      if (st != CUBLAS_STATUS_SUCCESS)
+        return fail(ctx, MFG_ERR_CUDA, "BF16 trailing update failed (cuBLAS %d)", (int)st);
+    }
+  }
+  MFG_CUDA(ctx, cudaMemsetAsync(active, 0xFF, sizeof(int) * count, s));
+  MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, -1, tol, berr, iters, state, anorm,
+                               active, s));
+  for (int it = 0; it <= max_iter; ++it)
+    MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, it, tol, berr, iters, state,
+                                 anorm, active, s));
+  // Systems that did not converge (stalled, diverged, out of iterations, singular FP32 factor)
+  // are solved again with the exact FP64 LU.
+  std::vector<int> hstate(count);
+  MFG_CUDA(ctx, cudaMemcpyAsync(hstate.data(), state, sizeof(int) * count, cudaMemcpyDeviceToHost,
+                                s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+  std::vector<int> hinfo(count, 0), redo;
+  for (int i = 0; i < count; i++)
+    if (hstate[i] != 1) redo.push_back(i);
+  if (!redo.empty()) {
+    const int r = (int)redo.size();
+    DevBuf tmp;
+    const size_t need = Carve::bytes_for((size_t)r * n * n, 8) + Carve::bytes_for((size_t)r * n, 8) +
+                        Carve::bytes_for((size_t)r * n, 4) + 2 * Carve::bytes_for(r, 4);
+    MFG_CUDA(ctx, tmp.reserve(need));
+    Carve tv(tmp.ptr);
+    double* ta = tv.take<double>((size_t)r * n * n);
+    double* tb = tv.take<double>((size_t)r * n);
+    int* tpiv = tv.take<int>((size_t)r * n);
+    int* tsign = tv.take<int>(r);
+    int* tinfo = tv.take<int>(r);
+    for (int q = 0; q < r; q++) {
+      const int i = redo[q];
+      MFG_CUDA(ctx, cudaMemcpyAsync(ta + (size_t)q * n * n, a + (size_t)i * n * n,
+                                    sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s));
+      MFG_CUDA(ctx, cudaMemcpyAsync(tb + (size_t)q * n, b + (size_t)i * n, sizeof(double) * n,
+                                    cudaMemcpyDeviceToDevice, s));
+    }
+    std::vector<int> nn(r, n);
+    std::vector<int64_t> aoff(r), poff(r);
+    for (int q = 0; q < r; q++) {
+      aoff[q] = (int64_t)q * n * n;
+      poff[q] = (int64_t)q * n;
+    }
+    mfg_plan* fp = nullptr;
+    int rc = plan_create(ctx, &fp, mfg_plan::GETRF, r, nn.data(), nullptr, aoff.data(),
+                         poff.data(), 1, poff.data());
+    if (rc != MFG_OK) return rc;
+    fp->args.a = ta;
+    fp->args.piv = tpiv;
+    fp->args.b = tb;
+    fp->args.sign = tsign;
+    fp->args.info = tinfo;
+    rc = plan_launch(fp, s);
+    if (rc != MFG_OK) {
+      mfg_plan_destroy(fp);
+      return rc;
+    }
+    std::vector<int> finfo(r);
+    MFG_CUDA(ctx, cudaMemcpyAsync(finfo.data(), tinfo, sizeof(int) * r, cudaMemcpyDeviceToHost,
+                                  s));
+    for (int q = 0; q < r; q++) {
+      const int i = redo[q];
+      MFG_CUDA(ctx, cudaMemcpyAsync(x + (size_t)i * n, tb + (size_t)q * n, sizeof(double) * n,
+                                    cudaMemcpyDeviceToDevice, s));
+    }
+    MFG_CUDA(ctx, cudaStreamSynchronize(s));
+    mfg_plan_destroy(fp);
+    for (int q = 0; q < r; q++) hinfo[redo[q]] = finfo[q] != 0 ? 2 : 1;
+    // Backward error of the FP64 solutions: one measuring sweep (no correction) over them.
+    MFG_CUDA(ctx, cudaMemcpyAsync(state, hinfo.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
+                                  s));
+    MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, -2, tol, berr, iters, state,
+                                 anorm, active, s));
+  }
+  MFG_CUDA(ctx, cudaMemcpyAsync(info, hinfo.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
+                                s));
+  MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
 

@@ -106,3 +106,40 @@ def rbf_batch(count, n=128, length=0.3, jitter=1e-6, seed=0):
     b_off, b_total = packed_offsets(ns, np.ones_like(ns))
     y = normal(b_total, seed, stream=11)
     return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=y, nrhs=1)
+
+
+def conditioned_batch(count, n, cond, seed=0):
+    """Mixed-precision workload (host, numpy): A = U diag(sigma) V^T with U, V the Q factors of
+    N(0,1) matrices and sigma log-spaced from 1 down to 1/cond; x_true ~ N(0,1); b = A x_true.
+    Returns column-major A (count*n*n), b, x_true."""
+    g = normal(count * n * n * 2 + count * n, seed, stream=12)
+    a = np.empty((count, n, n))
+    xt = g[2 * count * n * n:].reshape(count, n)
+    sigma = np.logspace(0.0, -np.log10(cond), n)
+    for i in range(count):
+        u = np.linalg.qr(g[(2 * i) * n * n:(2 * i + 1) * n * n].reshape(n, n))[0]
+        v = np.linalg.qr(g[(2 * i + 1) * n * n:(2 * i + 2) * n * n].reshape(n, n))[0]
+        a[i] = (u * sigma) @ v.T
+    b = np.einsum("kij,kj->ki", a, xt)
+    return np.ascontiguousarray(np.transpose(a, (0, 2, 1))).reshape(-1), b.reshape(-1), xt
+
+
+def conditioned_batch_device(count, n, cond, seed=0):
+    """The same distribution generated on the GPU with torch (for the large benchmark batch):
+    returns device tensors a (count*n*n, column-major per matrix), b, x_true."""
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    sigma = torch.logspace(0.0, -float(np.log10(cond)), n, dtype=torch.float64, device="cuda")
+    a = torch.empty((count, n, n), dtype=torch.float64, device="cuda")
+    chunk = 256
+    for s in range(0, count, chunk):
+        c = min(chunk, count - s)
+        u = torch.linalg.qr(torch.randn((c, n, n), dtype=torch.float64, device="cuda",
+                                        generator=gen))[0]
+        v = torch.linalg.qr(torch.randn((c, n, n), dtype=torch.float64, device="cuda",
+                                        generator=gen))[0]
+        a[s:s + c] = (u * sigma) @ v.transpose(1, 2)
+    xt = torch.randn((count, n), dtype=torch.float64, device="cuda", generator=gen)
+    b = torch.bmm(a, xt.unsqueeze(2)).squeeze(2)
+    return a.transpose(1, 2).contiguous().reshape(-1), b.reshape(-1).contiguous(), xt
