@@ -31,6 +31,10 @@ CONFIGS = {
     "lu": dict(workload="batched FP64 LU (partial pivoting, MatFlat order) + 4-RHS solve, "
                         "100,000 matrices, n~U{8..128}, A~N(0,1), lda=n, seed 0",
                count=100_000, nmin=8, nmax=128, nrhs=4),
+    "inv": dict(workload="batched FP64 LuInverse (MatFlat order) of the LU factors of 100,000 "
+                         "matrices, n~U{8..128}, A~N(0,1), lda=n, seed 0 (factored once on the "
+                         "GPU before timing)",
+                count=100_000, nmin=8, nmax=128, nrhs=0),
     "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
                           "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
                  count=10_000, n=32, nrhs=1),
@@ -62,6 +66,19 @@ def lu_bytes(n, nrhs):
     """Minimum HBM traffic: read and write A (16 n^2), b (16 n nrhs) and write piv (4 n)."""
     n = n.astype(np.float64)
     return float(np.sum(16 * n ** 2 + 16 * n * nrhs + 4 * n))
+
+
+def inv_flops(n):
+    """Algorithmic flops of the inverse from LU factors (LAPACK's getri count 4n^3/3 - n^2 +
+    5n/3; MatFlat's own sequence issues 2n^3, the GPU kernel about 4n^3/3)."""
+    n = n.astype(np.float64)
+    return float(np.sum(4 * n ** 3 / 3 - n ** 2 + 5 * n / 3))
+
+
+def inv_bytes(n):
+    """Read the factors and pivots, write the inverse."""
+    n = n.astype(np.float64)
+    return float(np.sum(16 * n ** 2 + 4 * n))
 
 
 def chol_flops(n, nrhs):
@@ -211,7 +228,7 @@ def read_traffic(kernel_key):
 def make_inputs(cfg_name, rank):
     from matflat_gb300 import synth
     cfg = CONFIGS[cfg_name]
-    if cfg_name == "lu":
+    if cfg_name in ("lu", "inv"):
         return synth.lu_batch(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"], seed=rank)
     if cfg_name == "chol":
         return synth.spd_batch(cfg["count"], cfg["n"], cfg["nrhs"], seed=rank)
@@ -240,6 +257,25 @@ def cpu_sample_rate(cfg_name, d, budget_s=15.0, threads=None):
 
 
 def run_cpu_sample(cfg_name, d, sample, threads, oracle):
+    if cfg_name == "inv":
+        n = d["n"][sample].astype(np.int32)
+        sz = n.astype(np.int64) ** 2
+        a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+        piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+        src = d.get("a_fac", d["a"])
+        a = np.concatenate([src[d["a_off"][i]:d["a_off"][i] + sz[j]]
+                            for j, i in enumerate(sample)])
+        info = np.zeros(len(n), np.int32)
+        if "piv" in d:
+            piv = np.concatenate([d["piv"][d["piv_off"][i]:d["piv_off"][i] + n[j]]
+                                  for j, i in enumerate(sample)])
+        else:   # no GPU factors (reference arm): factor the sample first, untimed
+            piv = np.zeros(int(n.sum()), np.int32)
+            sign = np.zeros(len(n), np.int32)
+            oracle.lu_solve_batched(n, a_off, a, piv_off, piv, a_off, a, 0, sign, threads)
+        t0 = time.perf_counter()
+        oracle.lu_inverse_batched(n, a_off, a, piv_off, piv, info, threads)
+        return time.perf_counter() - t0
     if cfg_name in ("lu", "chol", "grad"):
         n = d["n"][sample].astype(np.int32)
         sz = n.astype(np.int64) ** 2
@@ -319,6 +355,7 @@ def run_reference(args, cfg_name):
 
 def metric_name(cfg_name):
     return {"mixed": "mixed-precision LU+IR solves/s at 1e-12 backward error","lu": "batched FP64 LU+solve matrices/s (MatFlat-exact pivots)",
+            "inv": "batched FP64 LuInverse matrices/s (MatFlat-exact)",
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
             "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
@@ -538,7 +575,27 @@ def main():
         a = torch.empty_like(a0)
         b = torch.empty_like(b0)
         info = torch.zeros(count, dtype=torch.int32, device="cuda")
-        if cfg_name == "lu":
+        if cfg_name == "inv":
+            # Factor once, untimed; the pivots travel as the step's second input.
+            piv0 = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
+            sign = torch.zeros(count, dtype=torch.int32, device="cuda")
+            mf.LuBatch(d["n"], d["a_off"], d["piv_off"]).run(a0, piv0, None, sign, info)
+            torch.cuda.synchronize()
+            a_host.copy_(a0)
+            b_host = piv0.cpu().pin_memory()
+            b0 = piv0
+            b = torch.empty_like(b0)
+            d["a_fac"] = a_host.numpy()
+            d["piv"] = b_host.numpy()
+            plan = mf.LuInverseBatch(d["n"], d["a_off"], d["piv_off"])
+
+            def run():
+                plan.run(a, b, info)
+            outs = [a, info]
+            flops = inv_flops(d["n"])
+            byts = inv_bytes(d["n"])
+            kernel_key = "getri_batched_kernel"
+        elif cfg_name == "lu":
             plan = mf.LuBatch(d["n"], d["a_off"], d["piv_off"], nrhs=d["nrhs"], b_off=d["b_off"])
             piv = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
             sign = torch.zeros(count, dtype=torch.int32, device="cuda")

@@ -190,6 +190,15 @@ MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
                                    const int64_t* b_off);
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
 
+/* Batched Factorization.LuInverse (Factorization.LuInverse.cs:123-199): replaces every matrix's
+ * LU factors (as left by mfg_dgetrf_batched / Factorization.Lu) with A^-1, bit-identical to
+ * MatFlat.  piv at piv + piv_off[i] is the matrix's pivot vector (read only).  info: 0, or j+1
+ * when U(j,j) == 0 for the first such j (MatFlat throws "The matrix is not invertible."), or -1
+ * when piv is not a permutation of 0..n-1; in both cases that matrix is left unchanged. */
+MFG_API int mfg_plan_getri_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, const int64_t* piv_off);
+MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info);
+
 /* Householder QR of every tall matrix (Factorization.Qr; m[i] >= n[i], lda[i] >= m[i]), then,
  * when nrhs > 0, the least-squares solve min ||A x - b|| of nrhs right-hand sides per matrix
  * (b: nrhs columns of m[i] entries, leading dimension m[i]).  MatFlat has no QR solve; the

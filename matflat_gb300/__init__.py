@@ -9,7 +9,8 @@ tests and the benchmark:
     numpy array holding the column-major data with its leading dimension, and work in place.
   * MatFlat's exceptions are mirrored: ArgumentException, ArgumentNullException,
     MatrixFactorizationException (with MatFlat's messages).
-  * `LuBatch` / `CholeskyBatch` are the batched overloads (device-resident batches).
+  * `LuBatch` / `LuInverseBatch` / `CholeskyBatch` are the batched overloads (device-resident
+    batches).
 
 There is no CPU fallback: if the CUDA library is missing or no GPU is present, every call raises.
 """
@@ -20,6 +21,7 @@ from ._api import (  # noqa: F401
     CholeskyBatch,
     Factorization,
     LuBatch,
+    LuInverseBatch,
     MatFlatException,
     MatrixFactorizationException,
     MixedSolveBatch,

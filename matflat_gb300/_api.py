@@ -54,6 +54,8 @@ _SIGS = {
     "mfg_plan_status": (_I, [_vp]),
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_plan_getri_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp]),
+    "mfg_dgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
     "mfg_plan_gesv_mixed_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _I]),
     "mfg_dgesv_mixed_batched": (_I, [_vp, _vp, _vp, _vp, _I, _I, ctypes.c_double, _vp, _vp,
@@ -417,6 +419,34 @@ class LuBatch(_Batch):
         rc = self.ctx.lib.mfg_dgetrf_batched(self.h, _dptr(a), _dptr(piv), _dptr(b), _dptr(sign),
                                              _dptr(info))
         self.ctx.check(rc, "mfg_dgetrf_batched")
+
+
+class LuInverseBatch(_Batch):
+    """Batched Factorization.LuInverse: every matrix's LU factors (from LuBatch) become A^-1.
+
+    info per matrix: 0, j+1 when U(j,j) == 0 (MatFlat's "The matrix is not invertible."), or -1
+    when its pivot vector is not a permutation; such matrices are left unchanged.
+    """
+
+    def __init__(self, n, a_off, piv_off, lda=None, ctx=None):
+        ctx = ctx or context()
+        self._n = _i32(n)
+        self._lda = None if lda is None else _i32(lda)
+        self._a_off = _i64(a_off)
+        self._piv_off = _i64(piv_off)
+        h = _vp()
+        rc = ctx.lib.mfg_plan_getri_batched(
+            ctx.h, ctypes.byref(h), len(self._n), _ptr(self._n),
+            None if self._lda is None else _ptr(self._lda), _ptr(self._a_off),
+            _ptr(self._piv_off))
+        if rc != 0:
+            _raise_status(rc, ["plan", "count", "n", "lda", "a_off", "piv_off"], ctx)
+        super().__init__(ctx, h)
+        self.count = len(self._n)
+
+    def run(self, a, piv, info):
+        rc = self.ctx.lib.mfg_dgetri_batched(self.h, _dptr(a), _dptr(piv), _dptr(info))
+        self.ctx.check(rc, "mfg_dgetri_batched")
 
 
 class CholeskyBatch(_Batch):

@@ -114,10 +114,15 @@ __global__ void getri_single_kernel(double* a, int n, int lda, const int* piv, d
   }
 }
 
+// Both variants of the integer-pipe product must agree bit for bit; a disagreement is reported
+// as a NaN in the output, which the IEEE comparison then flags.
 __global__ void selftest_mul_kernel(const double* a, const double* b, double* out, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    out[i] = imul_rn(a[i], b[i]);
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r0 = imul_rn<false>(a[i], b[i]);
+    const double r1 = imul_rn<true>(a[i], b[i]);
+    out[i] = dbits(r0) == dbits(r1) ? r0 : __longlong_as_double(0x7FF8DEAD0000DEADll);
+  }
 }
 
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,

@@ -106,6 +106,13 @@ cudaError_t mx_refine(const double* a, const double* b, double* x, const float* 
 // One-time per-device set-up of kernel attributes (dynamic shared-memory limits).
 cudaError_t init_getrf_attributes();
 cudaError_t init_potrf_attributes();
+// Batched LuInverse (getri.cu): per-warp global scratch of getri_scratch_doubles(max n),
+// getri_warps_per_cta() warps per CTA, getri_ctas_per_sm() resident CTAs per SM.
+long long getri_scratch_doubles(int n);
+int getri_warps_per_cta();
+int getri_ctas_per_sm();
+cudaError_t init_getri_attributes();
+cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s);
 
 // Batched LU (+ solve); launched persistent: grid = ctas, WARPS warps per CTA.
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);

@@ -67,7 +67,7 @@ struct mfg_ctx {
 };
 
 struct mfg_plan {
-  enum Kind { GETRF, POTRF, GEQRF, MIXED } kind;
+  enum Kind { GETRF, POTRF, GEQRF, MIXED, GETRI } kind;
   mfg_ctx* ctx = nullptr;
   int count = 0;
   int nrhs = 0;
@@ -116,6 +116,7 @@ cudaError_t init_device_attributes(int device) {
   std::call_once(g_attr_once[slot], [slot]() {
     cudaError_t e = mfg::init_getrf_attributes();
     if (e == cudaSuccess) e = mfg::init_potrf_attributes();
+    if (e == cudaSuccess) e = mfg::init_getri_attributes();
     g_attr_err[slot] = e;
   });
   return g_attr_err[slot];
@@ -138,6 +139,32 @@ std::vector<int> snake_order(int count, const int* n) {
   std::stable_sort(sorted.begin(), sorted.end(), [&](int x, int y) { return n[x] > n[y]; });
   const char* mode = std::getenv("MFG_ORDER");
   if (mode && std::strcmp(mode, "lpt") == 0) return sorted;
+  if (mode && std::strcmp(mode, "shuffle") == 0) {
+    // Deterministic shuffle of the first 95% of the work (so the matrices in flight have the
+    // batch's average size), longest-first for the rest (a short tail).
+    std::vector<int> out = sorted;
+    double total = 0, acc = 0;
+    for (int i = 0; i < count; i++) total += (double)n[i] * n[i] * n[i];
+    int cut = count;
+    for (int i = count - 1; i >= 0; i--) {
+      acc += (double)n[sorted[i]] * n[sorted[i]] * n[sorted[i]];
+      if (acc >= 0.05 * total) {
+        cut = i;
+        break;
+      }
+    }
+    std::vector<int> head(sorted.begin(), sorted.begin() + cut), tail(sorted.begin() + cut,
+                                                                      sorted.end());
+    unsigned long long st = 0x9E3779B97F4A7C15ull;
+    for (int i = (int)head.size() - 1; i > 0; i--) {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      const int j = (int)((st >> 33) % (unsigned long long)(i + 1));
+      std::swap(head[i], head[j]);
+    }
+    out.assign(head.begin(), head.end());
+    out.insert(out.end(), tail.begin(), tail.end());
+    return out;
+  }
   std::vector<int> out;
   out.reserve(count);
   int lo = 0, hi = count - 1;
@@ -151,11 +178,18 @@ std::vector<int> snake_order(int count, const int* n) {
 // Launch shape of a batched plan: WARPS warps per CTA and enough CTAs to hold `warps_per_sm`
 // warps on every SM (persistent: each warp pulls matrices from the queue until it is empty).
 void choose_shape(mfg_plan* p) {
-  const int warps = env_int("MFG_WARPS_PER_CTA", 4);
-  const int wps = env_int("MFG_WARPS_PER_SM", 16);
+  const bool inv = p->kind == mfg_plan::GETRI;
+  // LuInverse stages 32 columns per warp in shared memory: its CTA shape is fixed and the grid
+  // holds as many CTAs as fit on an SM.
+  const int warps = inv ? mfg::getri_warps_per_cta() : env_int("MFG_WARPS_PER_CTA", 4);
   p->warps = warps;
-  const long long total_warps = (long long)p->ctx->sm_count * wps;
-  long long ctas = total_warps / warps;
+  long long ctas;
+  if (inv) {
+    ctas = (long long)p->ctx->sm_count * mfg::getri_ctas_per_sm();
+  } else {
+    const int wps = env_int("MFG_WARPS_PER_SM", 16);
+    ctas = (long long)p->ctx->sm_count * wps / warps;
+  }
   // Never more warps than matrices.
   const long long need = ((long long)p->count + warps - 1) / warps;
   if (ctas > need) ctas = need;
@@ -171,6 +205,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   if (p->count == 0) return MFG_OK;
   if (p->kind == mfg_plan::GETRF)
     e = mfg::launch_getrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::GETRI)
+    e = mfg::launch_getri_batched(p->args, p->ctas, s);
   else if (p->kind == mfg_plan::POTRF)
     e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->qr_float)
@@ -237,7 +273,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   for (int i = 0; i < count; i++)
     if (a_off[i] < 0) return fail(ctx, -6, "a_off[%d] < 0", i);
   int argi = 7;
-  if (kind == mfg_plan::GETRF) {
+  if (kind == mfg_plan::GETRF || kind == mfg_plan::GETRI) {
     if (count > 0 && !piv_off) return fail(ctx, -7, "piv_off is null");
     for (int i = 0; i < count; i++)
       if (piv_off[i] < 0) return fail(ctx, -7, "piv_off[%d] < 0", i);
@@ -287,7 +323,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   for (size_t i = 0; i < ints; i++) {
     ((long long*)(host.data() + 3 * bytes_i))[i] = a_off[i];
     ((long long*)(host.data() + 3 * bytes_i + bytes_l))[i] =
-        (kind == mfg_plan::GETRF) ? piv_off[i] : 0;
+        (kind == mfg_plan::GETRF || kind == mfg_plan::GETRI) ? piv_off[i] : 0;
     ((long long*)(host.data() + 3 * bytes_i + 2 * bytes_l))[i] = nrhs > 0 ? b_off[i] : 0;
   }
   e = cudaMemcpy(p->meta.ptr, host.data(), total, cudaMemcpyHostToDevice);
@@ -305,7 +341,16 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   }
   const int smem_n = kind == mfg_plan::POTRF ? 4 * group : mfg::SMEM_N;
   long long stride = 0;
-  if (max_n > smem_n) {
+  if (kind == mfg_plan::GETRI) {
+    // The inverse keeps a packed copy of the factors per warp (A is overwritten column by column).
+    stride = mfg::getri_scratch_doubles(max_n);
+    const size_t sbytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps;
+    e = p->scratch.reserve(sbytes);
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_fail(ctx, e, "cudaMalloc(plan scratch)");
+    }
+  } else if (max_n > smem_n) {
     stride = (mfg::warp_scratch_doubles(max_n) + 31) / 32 * 32;
     const size_t sbytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps *
                           (size_t)(32 / group);
@@ -327,7 +372,10 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.queue = d_queue;
   a.gscratch = (double*)p->scratch.ptr;
   a.gscratch_stride = stride;
-  a.hw_mul = env_int("MFG_HW_MUL", 0);
+  // LuInverse's per-lane solves multiply on the FP64 pipe by default: measured faster there than
+  // the integer-pipe product, whose long dependency chains one or two warps per scheduler cannot
+  // hide.
+  a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
   a.group = group;
   a.dot_block = env_int("MFG_DOT_BLOCK", 4);
   *out = p;
@@ -1229,6 +1277,28 @@ MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
                                    const int* lda, const int64_t* a_off, int nrhs,
                                    const int64_t* b_off) {
   return plan_create(ctx, plan, mfg_plan::POTRF, count, n, lda, a_off, nullptr, nrhs, b_off);
+}
+
+MFG_API int mfg_plan_getri_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                   const int* lda, const int64_t* a_off, const int64_t* piv_off) {
+  return plan_create(ctx, plan, mfg_plan::GETRI, count, n, lda, a_off, piv_off, 0, nullptr);
+}
+
+MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRI) return fail(ctx, -1, "plan is not a getri plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!piv) return fail(ctx, -3, "piv is null");
+    if (!info) return fail(ctx, -4, "info is null");
+  }
+  plan->args.a = a;
+  plan->args.piv = const_cast<int*>(piv);
+  plan->args.b = nullptr;
+  plan->args.sign = nullptr;
+  plan->args.info = info;
+  return plan_execute(plan, a, piv, info, nullptr, nullptr);
 }
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan) {

@@ -999,6 +999,21 @@ void orc_dlu_solve_batched(long count, const int* n, const int64_t* a_off, doubl
   });
 }
 
+// Batched Factorization.LuInverse over LU factors (lda = n): info[i] = 0, or j+1 for the first
+// zero diagonal entry of U (LuInverse.cs:145-152 throws there; the matrix is left unchanged).
+void orc_dlu_inverse_batched(long count, const int* n, const int64_t* a_off, double* a,
+                             const int64_t* piv_off, const int* piv, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    double* ai = a + a_off[i];
+    int bad = 0;
+    for (int j = 0; j < ni && !bad; j++)
+      if (ai[(long)ni * j + j] == 0.0) bad = j + 1;
+    info[i] = bad;
+    if (!bad) orc_dlu_inverse(ni, ai, ni, piv + piv_off[i]);
+  });
+}
+
 // Config "differentiable Cholesky": per matrix orc_dchol_grad (lda = n); g has the layout of a.
 void orc_dchol_grad_batched(long count, const int* n, const int64_t* a_off, double* a,
                             const int64_t* b_off, double* y, double* loss, double* g, int* info,

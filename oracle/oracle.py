@@ -59,6 +59,7 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
             "orc_dchol_grad": (_I, [_I, _d, _I, _d, _d, _d]),
             "orc_dchol_grad_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _d, _i, _I]),
             "orc_dqr_ls_batched": (None, [_L, _i, _i, _l, _d, _l, _d, _l, _d, _I]),
@@ -156,6 +157,13 @@ def lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, nthreads=1
                                 _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int),
                                 _p(b_off, ctypes.c_int64), _fp(b), nrhs,
                                 _p(sign, ctypes.c_int), nthreads)
+
+
+def lu_inverse_batched(n, a_off, a, piv_off, piv, info, nthreads=1):
+    """Factorization.LuInverse per matrix (lda = n); info = j+1 for the first zero U(j,j)."""
+    lib().orc_dlu_inverse_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+                                  _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int),
+                                  _p(info, ctypes.c_int), nthreads)
 
 
 def qr_ls_batched(m, n, a_off, a, b_off, b, x_off, x, nthreads=1):

@@ -1,5 +1,7 @@
 """The integer-pipe double product (used by every dot product of the factorizations) must equal
-the IEEE 754 round-to-nearest-even product bit for bit, on every class of operand."""
+the IEEE 754 round-to-nearest-even product bit for bit, on every class of operand.  Both variants
+(with and without the integer path for exact zeros) are checked: the self-test kernel turns any
+disagreement between them into a NaN."""
 import numpy as np
 import pytest
 
@@ -21,6 +23,11 @@ def _operands(rng, n):
         return bits.view(np.float64) * rng.choice([1.0, -1.0, 2.0 ** 40, 2.0 ** -40], n)
     parts.append((short(26), short(27)))
     parts.append((short(20), short(33)))
+    # signed zeros against every class of operand (the zero-aware variant's integer path)
+    z = rng.choice([0.0, -0.0], n)
+    other = rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64)
+    parts.append((z, other))
+    parts.append((other, z))
     # exponents at the edges of the normal range (overflow / underflow / subnormal results)
     e1 = rng.integers(-1100, 1100, n).astype(np.float64)
     e2 = -e1 + rng.integers(-60, 60, n)
