@@ -30,6 +30,8 @@ namespace mfg {
 constexpr int INV_WARPS = 6;  // 6 x 33.8 KB of staged columns per CTA, one CTA per SM
 constexpr int INV_LDX = 33;     // row stride (doubles) of the staged columns
 constexpr int INV_SMEM_N = 128; // orders whose staged columns fit in shared memory
+constexpr int INV_SMEM_WARP = INV_LDX * INV_SMEM_N + 2 * INV_SMEM_N;  // doubles per warp
+constexpr int INV_MAX_N = INV_SMEM_WARP / 2;  // largest order (two factor buffers in smem)
 
 long long getri_scratch_doubles(int n) {
   long long d = (long long)n * n;                         // packed L rows + packed U columns
@@ -39,21 +41,37 @@ long long getri_scratch_doubles(int n) {
 
 int getri_warps_per_cta() { return INV_WARPS; }
 
-size_t getri_smem_bytes() { return sizeof(double) * INV_WARPS * INV_LDX * INV_SMEM_N; }
+size_t getri_smem_bytes() { return sizeof(double) * INV_WARPS * INV_SMEM_WARP; }
+
+int getri_max_n() { return INV_MAX_N; }
 
 // Products of the solves: exact zeros are frequent here (the unit right-hand sides), so the
 // integer-pipe product keeps them on the integer path.
-template <bool IM>
+template <int IM>
 __device__ __forceinline__ double zmul_(double a, double b) {
-  if constexpr (IM) return imul_rn<true>(a, b);
+  if constexpr (IM == 1) return imul_rn<true>(a, b);
   else return __dmul_rn(a, b);
+}
+
+// Copies src[k0..k1) to dst[k0..k1) (shared memory) with asynchronous 8-byte copies, one element
+// per lane per round; stage_wait() completes this lane's copies and syncs the warp.
+__device__ __forceinline__ void stage_async(double* dst, const double* src, int k0, int k1) {
+  for (int k = k0 + (int)(threadIdx.x & 31); k < k1; k += 32) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + k);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src + k) : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncwarp();
 }
 
 // One matrix.  lp: packed rows of the strict lower factor (row i at i(i-1)/2, i entries);
 // up: packed columns of U (column i at i(i+1)/2, i+1 entries, diagonal last).
-template <bool IM>
+template <int IM>
 __device__ void getri_warp(double* a, int n, long long lda, const int* piv, double* lp,
-                           double* xs, int* info_out) {
+                           double* xs, double* vb, int* info_out) {
   const int lane = threadIdx.x & 31;
   double* up = lp + (long long)n * (n - 1) / 2;
 
@@ -110,9 +128,15 @@ __device__ void getri_warp(double* a, int n, long long lda, const int* piv, doub
     for (int i = 0; i < n; i++) x[i * INV_LDX] = (i == t) ? 1.0 : 0.0;
 
     // Unit lower solve, dot form: x_i = x_i - Dot(i, L(i,:), x) (the division by 1.0 is exact).
+    // Row i of L (entries k0..i-1) is read from shared memory while the next row streams in.
     // Blocks of 4 pairs: 8 independent products, then the sum's own chain in MatFlat's order.
+    if (k0 + 1 < n) {
+      stage_async(vb + ((k0 + 1) & 1) * n, lp + (long long)(k0 + 1) * k0 / 2, k0, k0 + 1);
+      stage_wait();
+    }
     for (int i = k0 + 1; i < n; i++) {
-      const double* li = lp + (long long)i * (i - 1) / 2;
+      const double* li = vb + (i & 1) * n;
+      if (i + 1 < n) stage_async(vb + ((i + 1) & 1) * n, lp + (long long)(i + 1) * i / 2, k0, i + 1);
       double s = 0.0;
       int k = k0;
       if ((i - k0) & 1) {
@@ -137,47 +161,31 @@ __device__ void getri_warp(double* a, int n, long long lda, const int* piv, doub
         s = __dadd_rn(s, q);
       }
       x[i * INV_LDX] = __dsub_rn(x[i * INV_LDX], s);
+      stage_wait();
     }
-    // Upper solve, column sweep: x_i /= U(i,i); x_k -= U(k,i) * x_i (k < i).  Blocks of 8 rows:
-    // the next block's loads are issued before the current block's stores, so the independent
-    // updates overlap.
+    // Upper solve, column sweep: x_i /= U(i,i); x_k -= U(k,i) * x_i (k < i), column i of U from
+    // shared memory while column i-1 streams in.  Blocks of 8 independent updates.
+    stage_async(vb + ((n - 1) & 1) * n, up + (long long)(n - 1) * n / 2, 0, n);
+    stage_wait();
     for (int i = n - 1; i >= 0; i--) {
-      const double* ui = up + (long long)i * (i + 1) / 2;
+      const double* ui = vb + (i & 1) * n;
+      if (i > 0) stage_async(vb + ((i - 1) & 1) * n, up + (long long)(i - 1) * i / 2, 0, i);
       const double xi = __ddiv_rn(x[i * INV_LDX], ui[i]);
       x[i * INV_LDX] = xi;
-      const int nb = i >> 3;
-      double u[8], v[8];
-      if (nb > 0) {
+      int k = 0;
+      for (; k + 8 <= i; k += 8) {
+        double u[8], v[8], pr[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) {
-          u[r] = ui[r];
-          v[r] = x[r * INV_LDX];
+          u[r] = ui[k + r];
+          v[r] = x[(k + r) * INV_LDX];
         }
-      }
-      for (int b = 0; b < nb; b++) {
-        const int k = b * 8;
-        double pr[8];
         mul_block_s<IM, 8, true>(u, xi, pr);
 #pragma unroll
-        for (int r = 0; r < 8; r++) v[r] = __dsub_rn(v[r], pr[r]);
-        double un[8], vn[8];
-        if (b + 1 < nb) {
-#pragma unroll
-          for (int r = 0; r < 8; r++) {
-            un[r] = ui[k + 8 + r];
-            vn[r] = x[(k + 8 + r) * INV_LDX];
-          }
-        }
-#pragma unroll
-        for (int r = 0; r < 8; r++) x[(k + r) * INV_LDX] = v[r];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          u[r] = un[r];
-          v[r] = vn[r];
-        }
+        for (int r = 0; r < 8; r++) x[(k + r) * INV_LDX] = __dsub_rn(v[r], pr[r]);
       }
-      for (int k = nb * 8; k < i; k++)
-        x[k * INV_LDX] = __dsub_rn(x[k * INV_LDX], zmul_<IM>(ui[k], xi));
+      for (; k < i; k++) x[k * INV_LDX] = __dsub_rn(x[k * INV_LDX], zmul_<IM>(ui[k], xi));
+      stage_wait();
     }
     __syncwarp();
     // Column piv[t] of A^-1 is the staged column of lane t - j0; write it back coalesced.
@@ -191,7 +199,7 @@ __device__ void getri_warp(double* a, int n, long long lda, const int* piv, doub
   if (lane == 0) *info_out = 0;
 }
 
-template <bool IM>
+template <int IM>
 __global__ void __launch_bounds__(INV_WARPS * 32) getri_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_inv[];
   const int warp = threadIdx.x >> 5;
@@ -205,27 +213,33 @@ __global__ void __launch_bounds__(INV_WARPS * 32) getri_batched_kernel(BatchArgs
     if (idx >= p.count) break;
     const int mat = p.order[idx];
     const int n = p.n[mat];
-    double* xs = n <= INV_SMEM_N ? sm_inv + warp * INV_LDX * INV_SMEM_N
-                                 : scr + (long long)n * n;
-    getri_warp<IM>(p.a + p.a_off[mat], n, p.lda[mat], p.piv + p.piv_off[mat], scr, xs,
+    // Shared memory per warp: the staged columns (n <= 128), then two factor rows/columns.  For
+    // larger n the staged columns live in global scratch and the smem holds the two buffers.
+    double* wsm = sm_inv + warp * INV_SMEM_WARP;
+    double* xs = n <= INV_SMEM_N ? wsm : scr + (long long)n * n;
+    double* vb = n <= INV_SMEM_N ? wsm + INV_LDX * INV_SMEM_N : wsm;
+    getri_warp<IM>(p.a + p.a_off[mat], n, p.lda[mat], p.piv + p.piv_off[mat], scr, xs, vb,
                    p.info + mat);
     __syncwarp();
   }
 }
 
 cudaError_t init_getri_attributes() {
-  cudaError_t e = cudaFuncSetAttribute(getri_batched_kernel<true>,
+  cudaError_t e = cudaFuncSetAttribute(getri_batched_kernel<1>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)getri_smem_bytes());
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(getri_batched_kernel<false>,
+  e = cudaFuncSetAttribute(getri_batched_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)getri_smem_bytes());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(getri_batched_kernel<0>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)getri_smem_bytes());
 }
 
 int getri_ctas_per_sm() {
   int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, getri_batched_kernel<true>,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, getri_batched_kernel<1>,
                                                     INV_WARPS * 32, getri_smem_bytes()) !=
       cudaSuccess)
     return 1;
@@ -233,10 +247,12 @@ int getri_ctas_per_sm() {
 }
 
 cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s) {
-  if (args.hw_mul)
-    getri_batched_kernel<false><<<ctas, INV_WARPS * 32, getri_smem_bytes(), s>>>(args);
+  if (args.hw_mul == 2)
+    getri_batched_kernel<2><<<ctas, INV_WARPS * 32, getri_smem_bytes(), s>>>(args);
+  else if (args.hw_mul)
+    getri_batched_kernel<0><<<ctas, INV_WARPS * 32, getri_smem_bytes(), s>>>(args);
   else
-    getri_batched_kernel<true><<<ctas, INV_WARPS * 32, getri_smem_bytes(), s>>>(args);
+    getri_batched_kernel<1><<<ctas, INV_WARPS * 32, getri_smem_bytes(), s>>>(args);
   return cudaGetLastError();
 }
 

@@ -108,7 +108,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
 // and in `info` the first zero pivot (k+1), or 0.
-template <class Tr, bool IM, int DB = DOT_BLOCK>
+template <class Tr, int IM, int DB = DOT_BLOCK>
 __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
                         typename Tr::Acc* scol, int& sign, int& info) {
   using T = typename Tr::T;
@@ -174,7 +174,7 @@ __device__ void getrs_warp(const double* lu, int n, long long lda, const int* pi
 
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 
-template <int WARPS, bool IM, int DB>
+template <int WARPS, int IM, int DB>
 __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   const int warp = threadIdx.x >> 5;
@@ -220,8 +220,10 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
 template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
-  if (args.hw_mul)
-    getrf_batched_kernel<WARPS, false, 4><<<ctas, WARPS * 32, smem, s>>>(args);
+  if (args.hw_mul == 2)
+    getrf_batched_kernel<WARPS, 2, 4><<<ctas, WARPS * 32, smem, s>>>(args);
+  else if (args.hw_mul)
+    getrf_batched_kernel<WARPS, 0, 4><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.dot_block == 8)
     getrf_batched_kernel<WARPS, true, 8><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.dot_block == 2)
@@ -241,6 +243,9 @@ static cudaError_t set_getrf_attr() {
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 2>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, 2, 4>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(getrf_batched_kernel<WARPS, false, 4>,

@@ -91,16 +91,18 @@ __device__ __forceinline__ int warp_argmax(unsigned long long key, int idx) {
 constexpr int DOT_BLOCK = 4;
 
 // The product used by the dot trees: the hardware DMUL (IM = false) or the integer-pipe product
-// imul_rn (IM = true); both return the correctly rounded product, bit for bit.
+// imul_rn (IM = true); both return the correctly rounded product, bit for bit.  exact_dot's IM is
+// 0 (DMUL), 1 (integer path) or 2 (the first product of each pair on the integer path, the
+// second on DMUL, splitting the work between the two pipes).
 template <bool IM>
 __device__ __forceinline__ double xmul(double a, double b);
 
-template <bool IM = true, int DOT_BLOCK = mfg::DOT_BLOCK>
+template <int IM = 1, int DOT_BLOCK = mfg::DOT_BLOCK>
 __device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
                                             const double* y, long long incy) {
   double s = 0.0;
   if (len & 1) {
-    s = xmul<IM>(x[0], y[0]);
+    s = xmul<IM != 0>(x[0], y[0]);
     x += incx;
     y += incy;
   }
@@ -129,8 +131,8 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
       }
 #pragma unroll
       for (int u = 0; u < DOT_BLOCK; ++u) {
-        const double q = __dadd_rn(xmul<IM>(xa[2 * u], ya[2 * u]),
-                                   xmul<IM>(xa[2 * u + 1], ya[2 * u + 1]));
+        const double q = __dadd_rn(xmul<IM != 0>(xa[2 * u], ya[2 * u]),
+                                   xmul<IM == 1>(xa[2 * u + 1], ya[2 * u + 1]));
         s = __dadd_rn(s, q);
       }
       if (more) {
@@ -143,7 +145,7 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
     }
   }
   for (int p = blocks * DOT_BLOCK; p < pairs; ++p) {
-    const double q = __dadd_rn(xmul<IM>(x[0], y[0]), xmul<IM>(x[incx], y[incy]));
+    const double q = __dadd_rn(xmul<IM != 0>(x[0], y[0]), xmul<IM == 1>(x[incx], y[incy]));
     s = __dadd_rn(s, q);
     x += 2 * incx;
     y += 2 * incy;

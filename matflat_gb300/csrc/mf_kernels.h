@@ -35,8 +35,8 @@ struct BatchArgs {
   int* queue;                // work counter, zeroed before every launch
   double* gscratch;          // per-warp scratch for n > SMEM_N
   long long gscratch_stride; // doubles per warp in gscratch
-  int hw_mul;                // 1: dot products multiply on the FP64 pipe (DMUL) instead of the
-                             // integer pipes; both give identical bits
+  int hw_mul;                // getrf/potrf: 0 products on the integer pipes, 1 on the FP64 pipe
+                             // (DMUL), 2 (getrf) alternating; all give identical bits
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4, 8)
 };
@@ -111,6 +111,7 @@ cudaError_t init_potrf_attributes();
 long long getri_scratch_doubles(int n);
 int getri_warps_per_cta();
 int getri_ctas_per_sm();
+int getri_max_n();
 cudaError_t init_getri_attributes();
 cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s);
 

@@ -103,7 +103,7 @@ __device__ __forceinline__ bool nonzero_f(float v) { return (__float_as_uint(v) 
 struct DTraits {
   using T = double;
   using Acc = double;
-  template <bool IM, int DB>
+  template <int IM, int DB>
   static __device__ __forceinline__ Acc dot(int len, const T* x, long long incx, const T* y,
                                             long long incy) {
     return exact_dot<IM, DB>(len, x, incx, y, incy);
@@ -122,7 +122,7 @@ struct DTraits {
 struct STraits {
   using T = float;
   using Acc = double;
-  template <bool IM, int DB>
+  template <int IM, int DB>
   static __device__ __forceinline__ Acc dot(int len, const T* x, long long incx, const T* y,
                                             long long incy) {
     return exact_dot_f(len, x, incx, y, incy);
@@ -142,7 +142,7 @@ struct STraits {
 struct ZTraits {
   using T = zdouble;
   using Acc = zdouble;
-  template <bool IM, int DB>
+  template <int IM, int DB>
   static __device__ __forceinline__ Acc dot(int len, const T* x, long long incx, const T* y,
                                             long long incy) {
     return zdot<false>(len, x, incx, y, incy);

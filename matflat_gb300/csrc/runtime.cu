@@ -269,6 +269,11 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     for (int i = 0; i < count; i++)
       if (lda[i] < n[i])
         return fail(ctx, -5, "lda[%d] = %d < n[%d] = %d", i, lda[i], i, n[i]);
+  if (kind == mfg_plan::GETRI)
+    for (int i = 0; i < count; i++)
+      if (n[i] > mfg::getri_max_n())
+        return fail(ctx, -4, "n[%d] = %d: the batched inverse supports orders up to %d", i, n[i],
+                    mfg::getri_max_n());
   if (count > 0 && !a_off) return fail(ctx, -6, "a_off is null");
   for (int i = 0; i < count; i++)
     if (a_off[i] < 0) return fail(ctx, -6, "a_off[%d] < 0", i);
