@@ -222,16 +222,108 @@ namespace mfg {
 // keep_factor = 0: K is left untouched and the factor is recomputed inside G's lower triangle
 // (no buffer for L), K^-1's strict upper triangle goes to G's strict upper triangle and its
 // diagonal to shared memory, and G is completed at the end.
-constexpr int GRAD_SMEM_DOUBLES = 2 * 128 + 2 * RHS_CHUNK * 129 + 8;
+// Per-warp shared memory of the gradient kernel: the 32 staged columns of the identity solves
+// (row stride 33), two staged rows of L, the Cholesky diagonal sums and K^-1's diagonal.
+constexpr int GRAD_LDX = 33;
+constexpr int GRAD_MAX_N = 128;
+constexpr int GRAD_SMEM_DOUBLES = GRAD_LDX * GRAD_MAX_N + 4 * GRAD_MAX_N;
+constexpr int GRAD_WARPS = 6;   // 6 x 37.9 KB per CTA, one CTA per SM
+
+// K^-1 = L^-T L^-1 column by column, MatFlat's two solves applied to the columns of the identity
+// (SolveTriangular Lower/NoTrans, Blas.SolveTriangular.cs:215-222, then Lower/Trans, :224-238,
+// MulSub :397-421), one lane per column: lane l of chunk j0 solves column c = j0 + l.  Keeps the
+// entries i < c of column c in G's strict upper triangle and K^-1(c,c) in kdiag.
+//   Forward, dot form: x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i).  For i < c, x_i = +0 exactly
+//   (0 minus a signed-zero dot, divided by L(i,i) > 0), so with a finite L the dots of a chunk
+//   start at k0 = j0 (the same argument as in the batched LuInverse: the skipped terms are
+//   signed zeros); otherwise they start at 0.
+//   Backward, column sweep: x_j /= L(j,j); x_k -= L(j,k) * x_j (k < j), j = n-1 .. 0.
+// Rows of L are staged in shared memory one ahead of their use.  The products use the FP64
+// pipe: with one CTA of six warps per SM the integer-pipe product's latency is not hidden.
+__device__ void chol_inverse_lanes(const double* L, int n, long long ld, double* G, double* kdiag,
+                                   double* xs, double* vb) {
+  const int lane = threadIdx.x & 31;
+  int nonfinite = 0;
+  for (int c = 0; c < n; ++c)
+    for (int r = c + 1 + lane; r < n; r += 32)
+      nonfinite |= ((dbits(L[(long long)c * ld + r]) >> 52) & 0x7FF) == 0x7FF;
+  nonfinite = __any_sync(FULL_MASK, nonfinite);
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int t = j0 + lane < n ? j0 + lane : j0;  // lanes past n repeat lane 0's column
+    const int k0 = nonfinite ? 0 : j0;
+    double* x = xs + lane;
+    for (int i = 0; i < n; i++) x[i * GRAD_LDX] = (i == t) ? 1.0 : 0.0;
+    // Forward: row i of L, entries k0..i (diagonal last), staged one row ahead.
+    stage_async(vb + (k0 & 1) * n, L + k0, k0, k0 + 1, ld);
+    stage_wait();
+    for (int i = k0; i < n; i++) {
+      const double* li = vb + (i & 1) * n;
+      if (i + 1 < n) stage_async(vb + ((i + 1) & 1) * n, L + i + 1, k0, i + 2, ld);
+      double s = 0.0;
+      int k = k0;
+      if ((i - k0) & 1) {
+        s = __dmul_rn(li[k0], x[k0 * GRAD_LDX]);
+        k = k0 + 1;
+      }
+      for (; k + 8 <= i; k += 8) {
+        double l8[8], v8[8], pr[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          l8[r] = li[k + r];
+          v8[r] = x[(k + r) * GRAD_LDX];
+        }
+        mul_block<0, 8, false>(l8, v8, pr);
+#pragma unroll
+        for (int r = 0; r < 4; r++) s = __dadd_rn(s, __dadd_rn(pr[2 * r], pr[2 * r + 1]));
+      }
+      for (; k < i; k += 2)
+        s = __dadd_rn(s, __dadd_rn(__dmul_rn(li[k], x[k * GRAD_LDX]),
+                                   __dmul_rn(li[k + 1], x[(k + 1) * GRAD_LDX])));
+      x[i * GRAD_LDX] = __ddiv_rn(__dsub_rn(x[i * GRAD_LDX], s), li[i]);
+      stage_wait();
+    }
+    // Backward: row j of L, entries 0..j (diagonal last), staged one row ahead.
+    stage_async(vb + ((n - 1) & 1) * n, L + (n - 1), 0, n, ld);
+    stage_wait();
+    for (int j = n - 1; j >= 0; j--) {
+      const double* lj = vb + (j & 1) * n;
+      if (j > 0) stage_async(vb + ((j - 1) & 1) * n, L + (j - 1), 0, j, ld);
+      const double xj = __ddiv_rn(x[j * GRAD_LDX], lj[j]);
+      x[j * GRAD_LDX] = xj;
+      int k = 0;
+      for (; k + 8 <= j; k += 8) {
+        double l8[8], v8[8], pr[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          l8[r] = lj[k + r];
+          v8[r] = x[(k + r) * GRAD_LDX];
+        }
+        mul_block_s<0, 8, false>(l8, xj, pr);
+#pragma unroll
+        for (int r = 0; r < 8; r++) x[(k + r) * GRAD_LDX] = __dsub_rn(v8[r], pr[r]);
+      }
+      for (; k < j; k++) x[k * GRAD_LDX] = __dsub_rn(x[k * GRAD_LDX], __dmul_rn(lj[k], xj));
+      stage_wait();
+    }
+    // Column c = j0 + l: entries i < c to G's strict upper triangle, i = c to kdiag.
+    const int nc = min(32, n - j0);
+    for (int l = 0; l < nc; l++) {
+      const int c = j0 + l;
+      double* col = G + (long long)c * ld;
+      for (int i = lane; i < c; i += 32) col[i] = xs[i * GRAD_LDX + l];
+      if (lane == 0) kdiag[c] = xs[c * GRAD_LDX + l];
+    }
+    __syncwarp();
+  }
+}
 
 __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double* y, double* loss,
                                int* info_out, int keep_factor, double* smem) {
   const int lane = threadIdx.x & 31;
-  double* dsum = smem;                 // n
-  double* kdiag = smem + n;            // n
-  const int ldx = n | 1;
-  double* xs = smem + 2 * n;           // RHS_CHUNK * ldx
-  double* acc = xs + RHS_CHUNK * ldx;  // RHS_CHUNK * ldx
+  double* xs = smem;                                 // GRAD_LDX * n
+  double* vb = smem + GRAD_LDX * GRAD_MAX_N;         // 2n
+  double* dsum = vb + 2 * GRAD_MAX_N;                // n
+  double* kdiag = dsum + GRAD_MAX_N;                 // n
   double* L;
   if (keep_factor) {
     L = K;
@@ -254,6 +346,8 @@ __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double
     return;
   }
   // z = L^-1 y (Lower/NoTrans), quad = z^T z, alpha = L^-T z (Lower/Trans).
+  const int ldx = n | 1;
+  double* acc = xs + ldx;
   for (int i = lane; i < n; i += 32) xs[i] = y[i];
   __syncwarp();
   warp_solve_dot<32>(L, n, 1, ld, false, xs, ldx, acc, 1);
@@ -267,31 +361,7 @@ __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double
     *loss = __dadd_rn(quad, __dmul_rn(2.0, logsum));
     *info_out = 0;
   }
-  // K^-1 by columns of the identity, RHS_CHUNK at a time; keep entries i <= c of column c.
-  for (int c0 = 0; c0 < n; c0 += RHS_CHUNK) {
-    const int nr = n - c0 < RHS_CHUNK ? n - c0 : RHS_CHUNK;
-    for (int e = lane; e < nr * n; e += 32) {
-      const int r = e / n;
-      const int i = e - r * n;
-      xs[r * ldx + i] = (i == c0 + r) ? 1.0 : 0.0;
-    }
-    __syncwarp();
-    warp_solve_dot<32>(L, n, 1, ld, false, xs, ldx, acc, nr);
-    warp_solve_sweep<32>(L, n, 1, ld, xs, ldx, nr);
-    for (int e = lane; e < nr * n; e += 32) {
-      const int r = e / n;
-      const int i = e - r * n;
-      const int c = c0 + r;
-      if (i > c) continue;
-      const double v = xs[r * ldx + i];
-      if (i == c) {
-        kdiag[c] = v;
-      } else {
-        G[(long long)c * ld + i] = v;             // strict upper triangle of G
-      }
-    }
-    __syncwarp();
-  }
+  chol_inverse_lanes(L, n, ld, G, kdiag, xs, vb);
   // G = K^-1 - alpha alpha^T (alpha is in y), symmetric.
   for (int c = 0; c < n; ++c) {
     for (int r = lane; r <= c; r += 32) {
@@ -306,11 +376,11 @@ __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double
   __syncwarp();
 }
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) chol_grad_batched_kernel(BatchArgs p, double* loss,
-                                                                        double* grad,
-                                                                        int keep_factor) {
-  __shared__ double sm[WARPS][GRAD_SMEM_DOUBLES];
+__global__ void __launch_bounds__(GRAD_WARPS * 32) chol_grad_batched_kernel(BatchArgs p,
+                                                                             double* loss,
+                                                                             double* grad,
+                                                                             int keep_factor) {
+  extern __shared__ double sm_grad[];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   for (;;) {
@@ -322,14 +392,34 @@ __global__ void __launch_bounds__(WARPS * 32) chol_grad_batched_kernel(BatchArgs
     const int n = p.n[mat];
     const long long lda = p.lda[mat];
     chol_grad_warp(p.a + p.a_off[mat], grad + p.a_off[mat], n, lda, p.b + p.b_off[mat],
-                   loss + mat, p.info + mat, keep_factor, &sm[warp][0]);
+                   loss + mat, p.info + mat, keep_factor, sm_grad + warp * GRAD_SMEM_DOUBLES);
     __syncwarp();
   }
 }
 
+static size_t grad_smem_bytes() { return sizeof(double) * GRAD_WARPS * GRAD_SMEM_DOUBLES; }
+
+cudaError_t init_grad_attributes() {
+  return cudaFuncSetAttribute(chol_grad_batched_kernel,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)grad_smem_bytes());
+}
+
+int grad_ctas_per_sm() {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, chol_grad_batched_kernel,
+                                                    GRAD_WARPS * 32, grad_smem_bytes()) !=
+      cudaSuccess)
+    return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int grad_warps_per_cta() { return GRAD_WARPS; }
+
 cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
                                      int keep_factor, int ctas, cudaStream_t s) {
-  chol_grad_batched_kernel<4><<<ctas, 128, 0, s>>>(args, loss, grad, keep_factor);
+  chol_grad_batched_kernel<<<ctas, GRAD_WARPS * 32, grad_smem_bytes(), s>>>(args, loss, grad,
+                                                                             keep_factor);
   return cudaGetLastError();
 }
 

@@ -53,20 +53,6 @@ __device__ __forceinline__ double zmul_(double a, double b) {
   else return __dmul_rn(a, b);
 }
 
-// Copies src[k0..k1) to dst[k0..k1) (shared memory) with asynchronous 8-byte copies, one element
-// per lane per round; stage_wait() completes this lane's copies and syncs the warp.
-__device__ __forceinline__ void stage_async(double* dst, const double* src, int k0, int k1) {
-  for (int k = k0 + (int)(threadIdx.x & 31); k < k1; k += 32) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + k);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src + k) : "memory");
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void stage_wait() {
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  __syncwarp();
-}
-
 // One matrix.  lp: packed rows of the strict lower factor (row i at i(i-1)/2, i entries);
 // up: packed columns of U (column i at i(i+1)/2, i+1 entries, diagonal last).
 template <int IM>

@@ -153,6 +153,24 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
   return s;
 }
 
+// Copies src[k*stride] to dst[k] (shared memory) for k in [k0, k1) with asynchronous 8-byte
+// copies, one element per lane per round (cp.async, completed by stage_wait): a warp stages the
+// next row or column of a factor while it computes with the current one.
+__device__ __forceinline__ void stage_async(double* dst, const double* src, int k0, int k1,
+                                            long long stride = 1) {
+  for (int k = k0 + (int)(threadIdx.x & 31); k < k1; k += 32) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + k);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src + k * stride)
+                 : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// Completes this lane's staged copies and makes every lane's copies visible to the warp.
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncwarp();
+}
+
 }  // namespace mfg
 
 #include "mf_imul.cuh"

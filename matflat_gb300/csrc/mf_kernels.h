@@ -81,6 +81,9 @@ cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, l
 // chol.cu).  Uses args.a (K), args.b (y -> alpha), args.info.
 cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
                                      int keep_factor, int ctas, cudaStream_t s);
+cudaError_t init_grad_attributes();
+int grad_ctas_per_sm();
+int grad_warps_per_cta();
 
 // Allocation-free strided batched LU + solve (scratch in a static device array; see lu.cu).
 int noalloc_max_n();

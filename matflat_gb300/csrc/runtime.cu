@@ -117,6 +117,7 @@ cudaError_t init_device_attributes(int device) {
     cudaError_t e = mfg::init_getrf_attributes();
     if (e == cudaSuccess) e = mfg::init_potrf_attributes();
     if (e == cudaSuccess) e = mfg::init_getri_attributes();
+    if (e == cudaSuccess) e = mfg::init_grad_attributes();
     g_attr_err[slot] = e;
   });
   return g_attr_err[slot];
@@ -1416,8 +1417,9 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
   a.a = k;
   a.b = y;
   a.info = info;
-  const long long ctas = std::min<long long>((long long)ctx->sm_count * 4,
-                                             ((long long)plan->count + 3) / 4);
+  const int wpc = mfg::grad_warps_per_cta();
+  const long long ctas = std::min<long long>((long long)ctx->sm_count * mfg::grad_ctas_per_sm(),
+                                             ((long long)plan->count + wpc - 1) / wpc);
   MFG_CUDA(ctx, mfg::launch_chol_grad_batched(a, loss, grad, keep_factor ? 1 : 0,
                                               (int)std::max<long long>(1, ctas), s));
   return MFG_OK;
