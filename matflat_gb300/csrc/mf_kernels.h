@@ -57,9 +57,12 @@ struct QrBatchArgs {
   int count;
   int nrhs;
   int* queue;
-  T* gscratch;               // per-warp coefficient scratch when n + nrhs > 256
+  T* gscratch;               // per-group coefficient scratch when n + nrhs > qr_smem_coefs
   long long gscratch_stride;
+  int group;                 // lanes per matrix: 32 (one warp) or 16, 8, 4
 };
+// Shared-memory coefficients per matrix of the batched QR for a group size.
+int qr_smem_coefs(int group);
 
 template <typename T>
 cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s);

@@ -21,6 +21,7 @@
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
+#include "mf_solve.cuh"
 
 namespace mfg {
 
@@ -153,68 +154,73 @@ __device__ __forceinline__ T* qr_col(T* a, long long lda, int n, T* b, long long
 }
 
 // Factors the m-by-n matrix a (m >= n) in place, applying every reflector also to the nb columns
-// of b (leading dimension ldb).  coefs: n - 1 + nb values of per-warp scratch.
-template <typename T>
+// of b (leading dimension ldb).  coefs: n - 1 + nb values of scratch.  G lanes work on the matrix
+// (a whole warp for G = 32; 32/G matrices per warp otherwise): the norm is one sequential dot
+// (every lane of the group evaluates it), the trailing-column dots are spread one per lane, and
+// the rank-1 update over (row, column) pairs.
+template <typename T, int G = 32>
 __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag, T* b,
                         long long ldb, int nb, T* coefs) {
   using A = QrArith<T>;
   using R = typename A::R;
-  const int lane = threadIdx.x & 31;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
   for (int k = 0; k < n; ++k) {
     T* ck = a + (long long)k * lda;
     const int len = m - k;
-    const R norm = A::norm(len, ck + k);  // every lane, same value
+    const R norm = A::norm(len, ck + k);  // every lane of the group, same value
     if (A::nzr(norm)) {
-      for (int r = k + lane; r < m; r += 32) ck[r] = A::divn(ck[r], norm);
-      __syncwarp();
+      for (int r = k + lane; r < m; r += G) ck[r] = A::divn(ck[r], norm);
+      __syncwarp(gm);
       if (lane == 0) ck[k] = A::add1(ck[k]);
-      __syncwarp();
+      __syncwarp(gm);
       const T v0 = ck[k];
       const int ncols = (n - k - 1) + nb;
-      for (int c = lane; c < ncols; c += 32) {
+      for (int c = lane; c < ncols; c += G) {
         const T* cj = qr_col(a, lda, n, b, ldb, k + 1 + c);
         coefs[c] = A::coef(A::dot(len, ck + k, cj + k), v0);
       }
-      __syncwarp();
+      __syncwarp(gm);
       // Right-hand sides skip a degenerate reflector (v[0] == 0 means v == 0 and the reflector
       // is the identity), as QrOrthogonalFactor does for the columns of Q (Qr.cs:406); the
       // factored columns follow Qr itself, which does not skip.
       const int upd = A::nz(v0) ? ncols : (n - k - 1);
       const long long work = (long long)len * upd;
-      for (long long e = lane; e < work; e += 32) {
+      for (long long e = lane; e < work; e += G) {
         const int c = (int)(e / len);
         const int r = k + (int)(e - (long long)c * len);
         T* cj = qr_col(a, lda, n, b, ldb, k + 1 + c);
         cj[r] = A::muladd(cj[r], ck[r], coefs[c]);
       }
     }
-    __syncwarp();
+    __syncwarp(gm);
     if (lane == 0) rdiag[k] = A::neg_r(norm);
-    __syncwarp();
+    __syncwarp(gm);
   }
 }
 
 // R x = y for the first n entries of every right-hand side (Blas.SolveTriangular Upper/NoTrans,
 // MatFlat/Blas.SolveTriangular.cs:191-199, against QrUpperTriangularFactor's R).
-template <typename T>
+template <typename T, int G = 32>
 __device__ void qr_rsolve_warp(const T* a, int n, long long lda, const T* rdiag, T* b,
                                long long ldb, int nb) {
   using A = QrArith<T>;
-  const int lane = threadIdx.x & 31;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
   for (int i = n - 1; i >= 0; --i) {
-    for (int c = lane; c < nb; c += 32) {
+    for (int c = lane; c < nb; c += G) {
       T* x = b + (long long)c * ldb;
       x[i] = A::div(x[i], rdiag[i]);
     }
-    __syncwarp();
+    __syncwarp(gm);
     const T* ai = a + (long long)i * lda;
-    for (int e = lane; e < nb * i; e += 32) {
+    for (int e = lane; e < nb * i; e += G) {
       const int c = e / i;
       const int r = e - c * i;
       T* x = b + (long long)c * ldb;
       x[r] = A::mulsub(x[r], ai[r], x[i]);
     }
-    __syncwarp();
+    __syncwarp(gm);
   }
 }
 
@@ -251,29 +257,41 @@ __device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long lo
   }
 }
 
-constexpr int QR_SMEM_COEFS = 256;
+constexpr int QR_SMEM_COEFS = 256;   // shared coefficients per warp (G = 32)
+constexpr int QR_GROUP_COEFS = 128;  // shared coefficients per group (G < 32)
 
-template <typename T, int WARPS>
+int qr_smem_coefs(int group) { return group == 32 ? QR_SMEM_COEFS : QR_GROUP_COEFS; }
+
+// Persistent batched QR (+ least squares): each group of G lanes takes the next matrix from the
+// queue (a warp takes 32/G consecutive ones, which the plan orders to have equal n).
+template <typename T, int WARPS, int G>
 __global__ void __launch_bounds__(WARPS * 32) qr_batched_kernel(QrBatchArgs<T> p) {
-  __shared__ T sm[WARPS][QR_SMEM_COEFS];
+  constexpr int GPW = 32 / G;
+  constexpr int CO = G == 32 ? QR_SMEM_COEFS : QR_GROUP_COEFS;
+  __shared__ T sm[WARPS][GPW][CO];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int g = lane / G;
   const long long gw = (long long)blockIdx.x * WARPS + warp;
   for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(p.queue, 1);
-    idx = __shfl_sync(FULL_MASK, idx, 0);
-    if (idx >= p.count) break;
-    const int mat = p.order[idx];
-    const int m = p.m[mat];
-    const int n = p.n[mat];
-    const long long lda = p.lda[mat];
-    T* a = p.a + p.a_off[mat];
-    T* rd = p.rdiag + p.rdiag_off[mat];
-    T* b = p.nrhs > 0 ? p.b + p.b_off[mat] : nullptr;
-    T* coefs = (n + p.nrhs <= QR_SMEM_COEFS) ? &sm[warp][0] : p.gscratch + gw * p.gscratch_stride;
-    qr_warp<T>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
-    if (p.nrhs > 0) qr_rsolve_warp<T>(a, n, lda, rd, b, m, p.nrhs);
+    int idx0 = 0;
+    if (lane == 0) idx0 = atomicAdd(p.queue, GPW);
+    idx0 = __shfl_sync(FULL_MASK, idx0, 0);
+    if (idx0 >= p.count) break;
+    const int idx = idx0 + g;
+    if (idx < p.count) {
+      const int mat = p.order[idx];
+      const int m = p.m[mat];
+      const int n = p.n[mat];
+      const long long lda = p.lda[mat];
+      T* a = p.a + p.a_off[mat];
+      T* rd = p.rdiag + p.rdiag_off[mat];
+      T* b = p.nrhs > 0 ? p.b + p.b_off[mat] : nullptr;
+      T* coefs = (n + p.nrhs <= CO) ? &sm[warp][g][0]
+                                    : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
+      qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+      if (p.nrhs > 0) qr_rsolve_warp<T, G>(a, n, lda, rd, b, m, p.nrhs);
+    }
     __syncwarp();
   }
 }
@@ -307,13 +325,21 @@ __global__ void qr_r_single_kernel(const T* a, int n, int lda, T* r, int ldr,
 
 template <typename T>
 cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s) {
-  switch (warps) {
-    case 1: qr_batched_kernel<T, 1><<<ctas, 32, 0, s>>>(args); break;
-    case 2: qr_batched_kernel<T, 2><<<ctas, 64, 0, s>>>(args); break;
-    case 4: qr_batched_kernel<T, 4><<<ctas, 128, 0, s>>>(args); break;
-    case 8: qr_batched_kernel<T, 8><<<ctas, 256, 0, s>>>(args); break;
-    case 16: qr_batched_kernel<T, 16><<<ctas, 512, 0, s>>>(args); break;
-    default: return cudaErrorInvalidValue;
+  if (args.group == 16) {
+    qr_batched_kernel<T, 4, 16><<<ctas, 128, 0, s>>>(args);
+  } else if (args.group == 8) {
+    qr_batched_kernel<T, 4, 8><<<ctas, 128, 0, s>>>(args);
+  } else if (args.group == 4) {
+    qr_batched_kernel<T, 4, 4><<<ctas, 128, 0, s>>>(args);
+  } else {
+    switch (warps) {
+      case 1: qr_batched_kernel<T, 1, 32><<<ctas, 32, 0, s>>>(args); break;
+      case 2: qr_batched_kernel<T, 2, 32><<<ctas, 64, 0, s>>>(args); break;
+      case 4: qr_batched_kernel<T, 4, 32><<<ctas, 128, 0, s>>>(args); break;
+      case 8: qr_batched_kernel<T, 8, 32><<<ctas, 256, 0, s>>>(args); break;
+      case 16: qr_batched_kernel<T, 16, 32><<<ctas, 512, 0, s>>>(args); break;
+      default: return cudaErrorInvalidValue;
+    }
   }
   return cudaGetLastError();
 }

