@@ -180,6 +180,11 @@ MFG_API int mfg_plan_getrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
  * first exactly-zero pivot U(k,k), LAPACK's convention; the factorization still completes). */
 MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                int* info);
+/* Solve only, with factors and pivots already in a and piv (from mfg_dgetrf_batched or
+ * Factorization.Lu): b' = P b, the unit-lower solve (LuInverse idiom, Factorization.LuInverse.cs:
+ * 174-182) and the upper solve (Blas.SolveTriangular.cs:191-199), for the plan's nrhs (>= 1)
+ * right-hand sides; bit-identical to the fused path.  a and piv are read only. */
+MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b);
 
 /* Cholesky of every matrix (Factorization.Cholesky), then, when nrhs > 0, L y = b
  * (SolveTriangular Lower/NoTrans) and L^T x = y (SolveTriangular Lower/Trans) per right-hand
@@ -189,6 +194,10 @@ MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
                                    const int* lda, const int64_t* a_off, int nrhs,
                                    const int64_t* b_off);
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
+/* Solve only with Cholesky factors already in a (lower triangle): L y = b, L^T x = y
+ * (Blas.SolveTriangular Lower/NoTrans then Lower/Trans, Blas.SolveTriangular.cs:215-238) for the
+ * plan's nrhs (>= 1) right-hand sides. */
+MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b);
 
 /* Batched Factorization.LuInverse (Factorization.LuInverse.cs:123-199): replaces every matrix's
  * LU factors (as left by mfg_dgetrf_batched / Factorization.Lu) with A^-1, bit-identical to
@@ -212,6 +221,11 @@ MFG_API int mfg_plan_geqrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
                                    const int64_t* rdiag_off, int nrhs, const int64_t* b_off);
 MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b);
 MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b);
+/* Least-squares solve only, with the factorization already in a and rdiag (Factorization.Qr's
+ * format): the stored reflectors applied to b in the factorization's order (Qr.cs:160-165), then
+ * R x = Q^T b (Blas.SolveTriangular.cs:191-199); bit-identical to the fused path.  nrhs >= 1. */
+MFG_API int mfg_dgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b);
+MFG_API int mfg_sgeqrs_batched(mfg_plan* plan, const float* a, const float* rdiag, float* b);
 
 /* Differentiable Cholesky / log-determinant / solve over a potrf plan with nrhs = 1 (n <= 128).
  * For every SPD matrix K (upper triangle read, as Factorization.Cholesky) and vector y:

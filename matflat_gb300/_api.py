@@ -54,6 +54,10 @@ _SIGS = {
     "mfg_plan_status": (_I, [_vp]),
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
+    "mfg_dgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_sgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_getri_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp]),
     "mfg_dgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
@@ -420,6 +424,11 @@ class LuBatch(_Batch):
                                              _dptr(info))
         self.ctx.check(rc, "mfg_dgetrf_batched")
 
+    def solve(self, a, piv, b):
+        """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b)."""
+        rc = self.ctx.lib.mfg_dgetrs_batched(self.h, _dptr(a), _dptr(piv), _dptr(b))
+        self.ctx.check(rc, "mfg_dgetrs_batched")
+
 
 class LuInverseBatch(_Batch):
     """Batched Factorization.LuInverse: every matrix's LU factors (from LuBatch) become A^-1.
@@ -472,6 +481,11 @@ class CholeskyBatch(_Batch):
         rc = self.ctx.lib.mfg_dpotrf_batched(self.h, _dptr(a), _dptr(b), _dptr(info))
         self.ctx.check(rc, "mfg_dpotrf_batched")
 
+    def solve(self, a, b):
+        """Solves with Cholesky factors already in a (the plan's nrhs columns of b)."""
+        rc = self.ctx.lib.mfg_dpotrs_batched(self.h, _dptr(a), _dptr(b))
+        self.ctx.check(rc, "mfg_dpotrs_batched")
+
     def loss_and_grad(self, k, y, loss, grad, info, keep_factor=True):
         """loss = y^T K^-1 y + log det K and grad = K^-1 - alpha alpha^T per matrix; y becomes
         alpha = K^-1 y; with keep_factor, k becomes the Cholesky factor L."""
@@ -510,6 +524,12 @@ class QrBatch(_Batch):
         fn = self.ctx.lib.mfg_sgeqrf_batched if single else self.ctx.lib.mfg_dgeqrf_batched
         rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
         self.ctx.check(rc, "mfg_geqrf_batched")
+
+    def solve(self, a, rdiag, b, single=False):
+        """Least squares with the factorization already in a and rdiag (nrhs columns of b)."""
+        fn = self.ctx.lib.mfg_sgeqrs_batched if single else self.ctx.lib.mfg_dgeqrs_batched
+        rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
+        self.ctx.check(rc, "mfg_geqrs_batched")
 
 
 def selftest_dmul(a, b, out):

@@ -114,11 +114,11 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* a = p.a + p.a_off[mat];
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
-      const int info = potrf_group<G, IM>(a, n, lda, scr);
+      const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
       if (info == 0 && p.nrhs > 0)
         potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                        scr + n + RHS_CHUNK * ldx);
-      if ((lane & (G - 1)) == 0) p.info[mat] = info;
+      if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
     }
     __syncwarp();
   }

@@ -193,12 +193,12 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
     double* scr = (n <= SMEM_N) ? sm_dyn + warp * SMEM_WARP_DOUBLES
                                  : p.gscratch + gw * p.gscratch_stride;
     const int ldx = n | 1;
-    int sign, info;
-    lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
+    int sign = 1, info = 0;
+    if (!p.solve_only) lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);
-    if (lane == 0) {
+    if (lane == 0 && !p.solve_only) {
       p.sign[mat] = sign;
       p.info[mat] = info;
     }

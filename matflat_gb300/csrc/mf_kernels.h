@@ -39,6 +39,7 @@ struct BatchArgs {
                              // (DMUL), 2 (getrf) alternating; all give identical bits
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4, 8)
+  int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
 };
 
 // Batched Householder QR (+ least-squares solve of nrhs right-hand sides, ldb = m).
@@ -60,6 +61,7 @@ struct QrBatchArgs {
   T* gscratch;               // per-group coefficient scratch when n + nrhs > qr_smem_coefs
   long long gscratch_stride;
   int group;                 // lanes per matrix: 32 (one warp) or 16, 8, 4
+  int solve_only;            // a and rdiag hold the factorization; only solve the b blocks
 };
 // Shared-memory coefficients per matrix of the batched QR for a group size.
 int qr_smem_coefs(int group);

@@ -199,6 +199,38 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::
   }
 }
 
+// Applies the stored reflectors of a factored matrix to the nb columns of b, in the order and
+// arithmetic the factorization applies them (the right-hand-side branch of qr_warp): reflector k
+// exists when rdiag[k] != 0 (the column norm was nonzero) and acts when v[0] != 0.
+template <typename T, int G = 32>
+__device__ void qr_apply_warp(const T* a, int m, int n, long long lda,
+                              const typename QrArith<T>::R* rdiag, T* b, long long ldb, int nb,
+                              T* coefs) {
+  using A = QrArith<T>;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  for (int k = 0; k < n; ++k) {
+    const T* ck = a + (long long)k * lda;
+    const T v0 = ck[k];
+    if (A::nzr(rdiag[k]) && A::nz(v0)) {
+      const int len = m - k;
+      for (int c = lane; c < nb; c += G) {
+        const T* bj = b + (long long)c * ldb;
+        coefs[c] = A::coef(A::dot(len, ck + k, bj + k), v0);
+      }
+      __syncwarp(gm);
+      const long long work = (long long)len * nb;
+      for (long long e = lane; e < work; e += G) {
+        const int c = (int)(e / len);
+        const int r = k + (int)(e - (long long)c * len);
+        T* bj = b + (long long)c * ldb;
+        bj[r] = A::muladd(bj[r], ck[r], coefs[c]);
+      }
+    }
+    __syncwarp(gm);
+  }
+}
+
 // R x = y for the first n entries of every right-hand side (Blas.SolveTriangular Upper/NoTrans,
 // MatFlat/Blas.SolveTriangular.cs:191-199, against QrUpperTriangularFactor's R).
 template <typename T, int G = 32>
@@ -289,7 +321,10 @@ __global__ void __launch_bounds__(WARPS * 32) qr_batched_kernel(QrBatchArgs<T> p
       T* b = p.nrhs > 0 ? p.b + p.b_off[mat] : nullptr;
       T* coefs = (n + p.nrhs <= CO) ? &sm[warp][g][0]
                                     : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
-      qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+      if (p.solve_only)
+        qr_apply_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+      else
+        qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       if (p.nrhs > 0) qr_rsolve_warp<T, G>(a, n, lda, rd, b, m, p.nrhs);
     }
     __syncwarp();

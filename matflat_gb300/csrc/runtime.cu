@@ -926,6 +926,7 @@ MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double*
   plan->qd.a = a;
   plan->qd.rdiag = rdiag;
   plan->qd.b = b;
+  plan->qd.solve_only = 0;
   return plan_execute(plan, a, rdiag, b, (const void*)1, nullptr);
 }
 
@@ -942,7 +943,42 @@ MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b)
   plan->qs.a = a;
   plan->qs.rdiag = rdiag;
   plan->qs.b = b;
+  plan->qs.solve_only = 0;
   return plan_execute(plan, a, rdiag, b, (const void*)2, nullptr);
+}
+
+}  // extern "C"
+
+// Least-squares solve with an existing factorization (the plan's nrhs right-hand sides).
+template <typename T>
+static int geqrs_batched(mfg_plan* plan, const T* a, const T* rdiag, T* b, int single) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!rdiag) return fail(ctx, -3, "rdiag is null");
+    if (!b) return fail(ctx, -4, "b is null");
+  }
+  plan->qr_float = single;
+  mfg::QrBatchArgs<T>& q = *reinterpret_cast<mfg::QrBatchArgs<T>*>(single ? (void*)&plan->qs
+                                                                           : (void*)&plan->qd);
+  q.a = const_cast<T*>(a);
+  q.rdiag = const_cast<T*>(rdiag);
+  q.b = b;
+  q.solve_only = 1;
+  return plan_execute(plan, a, rdiag, b, (const void*)(intptr_t)(single ? 2 : 1), (const void*)3);
+}
+
+extern "C" {
+
+MFG_API int mfg_dgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b) {
+  return geqrs_batched<double>(plan, a, rdiag, b, 0);
+}
+
+MFG_API int mfg_sgeqrs_batched(mfg_plan* plan, const float* a, const float* rdiag, float* b) {
+  return geqrs_batched<float>(plan, a, rdiag, b, 1);
 }
 
 
@@ -1350,7 +1386,27 @@ MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, i
   plan->args.b = b;
   plan->args.sign = sign;
   plan->args.info = info;
+  plan->args.solve_only = 0;
   return plan_execute(plan, a, piv, b, sign, info);
+}
+
+MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
+  if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!piv) return fail(ctx, -3, "piv is null");
+    if (!b) return fail(ctx, -4, "b is null");
+  }
+  plan->args.a = const_cast<double*>(a);
+  plan->args.piv = const_cast<int*>(piv);
+  plan->args.b = b;
+  plan->args.sign = nullptr;
+  plan->args.info = nullptr;
+  plan->args.solve_only = 1;
+  return plan_execute(plan, a, piv, b, nullptr, (const void*)3);
 }
 
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
@@ -1367,7 +1423,26 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) 
   plan->args.b = b;
   plan->args.sign = nullptr;
   plan->args.info = info;
+  plan->args.solve_only = 0;
   return plan_execute(plan, a, b, info, nullptr, nullptr);
+}
+
+MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!b) return fail(ctx, -3, "b is null");
+  }
+  plan->args.a = const_cast<double*>(a);
+  plan->args.piv = nullptr;
+  plan->args.b = b;
+  plan->args.sign = nullptr;
+  plan->args.info = nullptr;
+  plan->args.solve_only = 1;
+  return plan_execute(plan, a, b, nullptr, (const void*)3, nullptr);
 }
 
 MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
