@@ -511,6 +511,8 @@ def main():
     ap.add_argument("--lowp", default="tf32", choices=["fp32", "tf32", "bf16"],
                     help="mixed: precision of the factorization")
     ap.add_argument("--n", type=int, default=None, help="mixed: order of the systems")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="lu/chol: keep the default launch shape instead of autotuning the plan")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -552,6 +554,7 @@ def main():
     d = make_inputs(cfg_name, rank)
     cfg = CONFIGS[cfg_name]
     count = len(d["n"])
+    tuned = None
     if cfg_name in ("qr", "qr32"):
         dt = torch.float32 if cfg_name == "qr32" else torch.float64
         npdt = np.float32 if cfg_name == "qr32" else np.float64
@@ -602,6 +605,8 @@ def main():
             kernel_key = "getri_batched_kernel"
         elif cfg_name == "lu":
             plan = mf.LuBatch(d["n"], d["a_off"], d["piv_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+            if not args.no_autotune:
+                tuned = plan.autotune()
             piv = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
             sign = torch.zeros(count, dtype=torch.int32, device="cuda")
 
@@ -613,6 +618,8 @@ def main():
             kernel_key = "getrf_batched_kernel"
         elif cfg_name == "chol":
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+            if not args.no_autotune:
+                tuned = plan.autotune()
 
             def run():
                 plan.run(a, b, info)
@@ -758,6 +765,9 @@ def main():
                        "step_includes": "device-to-device restore of the input batch + the "
                                         "batched factorization/solve (one graph replay)"},
             "kernel_ms_per_step": kmed,
+            "launch_shape": None if tuned is None else dict(
+                zip(["warps_per_cta", "warps_per_sm", "lanes_per_matrix", "mul_mode"], tuned),
+                source="mfg_plan_autotune at plan creation (outside the timed region)"),
             "gpu_launches": args.steps,
             "roofline": roof,
             "cpu_baseline": cpu,

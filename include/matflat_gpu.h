@@ -261,6 +261,17 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
                                     int lowp, int max_iter, double tol, double* berr, int* iters,
                                     int* info);
 
+/* Launch-shape autotuner (no counterpart in the reference) for getrf and potrf plans.  Times
+ * candidate shapes — warps per CTA and per SM, lanes per matrix (potrf) and which pipe does the
+ * multiplies — on a synthetic batch of up to 20,000 matrices with the plan's size mix (sampled
+ * evenly), installs the fastest in the plan and records it in the context's tuning table under the
+ * plan's size bucket (kind, largest order, batch size), so later plans of that bucket on this
+ * context start from it.  Synchronous; allocates and frees its own buffers; every shape gives the
+ * same bits.  config (may be NULL) receives {warps per CTA, warps per SM, lanes per matrix,
+ * multiply mode}.  Environment overrides of the shape (MFG_WARPS_PER_*, MFG_HW_MUL,
+ * MFG_CHOL_GROUP) take precedence over the table for new plans. */
+MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
+
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 
 /* Reads back the device-side status word of the last execution of `plan` (synchronizes the

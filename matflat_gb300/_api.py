@@ -54,6 +54,7 @@ _SIGS = {
     "mfg_plan_status": (_I, [_vp]),
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
     "mfg_dgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -385,6 +386,15 @@ class _Batch:
 
     def status(self):
         self.ctx.check(self.ctx.lib.mfg_plan_status(self.h), "mfg_plan_status")
+
+    def autotune(self):
+        """Times candidate launch shapes on a synthetic batch with this plan's size mix and keeps
+        the fastest (getrf and potrf plans); returns (warps per CTA, warps per SM, lanes per
+        matrix, multiply mode)."""
+        cfg = (ctypes.c_int * 4)()
+        rc = self.ctx.lib.mfg_plan_autotune(self.h, cfg)
+        self.ctx.check(rc, "mfg_plan_autotune")
+        return tuple(cfg)
 
 
 def _i32(x):

@@ -90,6 +90,9 @@ cudaError_t init_grad_attributes();
 int grad_ctas_per_sm();
 int grad_warps_per_cta();
 
+// Fills args.a (and args.b when nrhs > 0) with the autotuner's synthetic batch (tune.cu).
+cudaError_t launch_tune_fill(const BatchArgs& args, int spd, cudaStream_t s);
+
 // Allocation-free strided batched LU + solve (scratch in a static device array; see lu.cu).
 int noalloc_max_n();
 cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,

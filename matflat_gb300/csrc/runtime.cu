@@ -7,10 +7,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -64,6 +66,8 @@ struct mfg_ctx {
   DevBuf work;
   std::string last_error;
   bool use_graphs = true;
+  // Autotuner results: launch shape per (plan kind, size bucket), used by later plans.
+  std::map<long long, std::array<int, 4>> tune;
 };
 
 struct mfg_plan {
@@ -82,6 +86,7 @@ struct mfg_plan {
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
   int ctas = 0;
   int warps = 0;
+  std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
   // CUDA graph of the last execution (keyed by the data pointers and the stream).
   cudaGraphExec_t exec = nullptr;
   const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -197,6 +202,57 @@ void choose_shape(mfg_plan* p, int fixed_warps = 0) {
   if (ctas > need) ctas = need;
   if (ctas < 1) ctas = 1;
   p->ctas = (int)ctas;
+}
+
+// Re-shapes a getrf/potrf plan: warps per CTA (1, 2, 4, 8 or 16), warps per SM, lanes per
+// matrix (potrf) and the multiply mode; grows the per-warp scratch when the new shape keeps more
+// matrices in flight, and drops the cached graph.
+int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul) {
+  mfg_ctx* ctx = p->ctx;
+  long long ctas = (long long)ctx->sm_count * wps / warps;
+  const long long need = ((long long)p->count + warps - 1) / warps;
+  if (ctas > need) ctas = need;
+  if (ctas < 1) ctas = 1;
+  const int g = p->kind == mfg_plan::POTRF ? group : 32;
+  const int smem_n = p->kind == mfg_plan::POTRF ? 4 * g : mfg::SMEM_N;
+  long long stride = 0;
+  if (p->max_n > smem_n) {
+    stride = (mfg::warp_scratch_doubles(p->max_n) + 31) / 32 * 32;
+    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the scratch may be in use
+    MFG_CUDA(ctx, p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)ctas * warps *
+                                     (size_t)(32 / g)));
+  }
+  p->warps = warps;
+  p->ctas = (int)ctas;
+  p->args.gscratch = (double*)p->scratch.ptr;
+  p->args.gscratch_stride = stride;
+  p->args.group = g;
+  p->args.hw_mul = mul;
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return MFG_OK;
+}
+
+// Tuning-table key: plan kind, bucket of the largest order (16, 32, 64, 128, 256, more) and
+// the batch size's power of two.
+long long tune_key(int kind, int max_n, int count) {
+  const int nb = max_n <= 16 ? 0 : max_n <= 32 ? 1 : max_n <= 64 ? 2 : max_n <= 128 ? 3
+               : max_n <= 256 ? 4 : 5;
+  int cb = 0;
+  while (cb < 40 && (1LL << (cb + 1)) <= count) cb++;
+  return (long long)kind * 10000 + nb * 100 + cb;
+}
+
+// A shape forced through the environment wins over the tuning table.
+bool tune_env_override() {
+  const char* names[] = {"MFG_WARPS_PER_CTA", "MFG_WARPS_PER_SM", "MFG_HW_MUL", "MFG_CHOL_GROUP"};
+  for (const char* n : names) {
+    const char* v = std::getenv(n);
+    if (v && *v) return true;
+  }
+  return false;
 }
 
 int plan_launch(mfg_plan* p, cudaStream_t s) {
@@ -385,6 +441,20 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
   a.group = group;
   a.dot_block = env_int("MFG_DOT_BLOCK", 4);
+  if (kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) {
+    p->hn.assign(n, n + count);
+    if (!tune_env_override()) {
+      auto it = ctx->tune.find(tune_key((int)kind, max_n, count));
+      if (it != ctx->tune.end()) {
+        const auto& c = it->second;
+        const int rc = plan_reshape(p, c[0], c[1], c[2], c[3]);
+        if (rc != MFG_OK) {
+          delete p;
+          return rc;
+        }
+      }
+    }
+  }
   *out = p;
   return MFG_OK;
 }
@@ -1356,6 +1426,111 @@ MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* i
   plan->args.sign = nullptr;
   plan->args.info = info;
   return plan_execute(plan, a, piv, info, nullptr, nullptr);
+}
+
+MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRF && plan->kind != mfg_plan::POTRF)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "autotune: getrf and potrf plans only");
+  if (plan->count == 0) return MFG_OK;
+  cudaStream_t s = ctx->stream;
+  // A sample of up to 20,000 matrices spread evenly over the batch keeps its size mix.
+  const int cap = 20000;
+  const int step = (plan->count + cap - 1) / cap;
+  std::vector<int> sn;
+  for (int i = 0; i < plan->count; i += step) sn.push_back(plan->hn[i]);
+  const int cnt = (int)sn.size();
+  const int nrhs = plan->nrhs;
+  std::vector<int64_t> aoff(cnt), poff(cnt), boff(cnt);
+  long long at = 0, pt = 0, bt = 0;
+  for (int i = 0; i < cnt; i++) {
+    aoff[i] = at;
+    at += (long long)sn[i] * sn[i];
+    poff[i] = pt;
+    pt += sn[i];
+    boff[i] = bt;
+    bt += (long long)sn[i] * nrhs;
+  }
+  mfg_plan* tp = nullptr;
+  int rc = plan_create(ctx, &tp, plan->kind, cnt, sn.data(), nullptr, aoff.data(), poff.data(),
+                       nrhs, nrhs > 0 ? boff.data() : nullptr);
+  if (rc != MFG_OK) return rc;
+  DevBuf buf;
+  const size_t need = Carve::bytes_for(at, 8) * 2 + Carve::bytes_for(bt + 1, 8) * 2 +
+                      Carve::bytes_for(pt, 4) + 2 * Carve::bytes_for(cnt, 4);
+  cudaError_t ce = buf.reserve(need);
+  if (ce != cudaSuccess) {
+    mfg_plan_destroy(tp);
+    return cuda_fail(ctx, ce, "cudaMalloc(autotune batch)");
+  }
+  Carve cv(buf.ptr);
+  double* a = cv.take<double>(at);
+  double* a0 = cv.take<double>(at);
+  double* b = cv.take<double>(bt + 1);
+  double* b0 = cv.take<double>(bt + 1);
+  int* piv = cv.take<int>(pt);
+  int* sign = cv.take<int>(cnt);
+  int* info = cv.take<int>(cnt);
+  tp->args.a = a;
+  tp->args.b = nrhs > 0 ? b : nullptr;
+  tp->args.piv = plan->kind == mfg_plan::GETRF ? piv : nullptr;
+  tp->args.sign = plan->kind == mfg_plan::GETRF ? sign : nullptr;
+  tp->args.info = info;
+  tp->args.solve_only = 0;
+  std::vector<std::array<int, 4>> cands;
+  if (plan->kind == mfg_plan::GETRF) {
+    for (int w : {4, 8})
+      for (int wps : {8, 12, 16, 20})
+        for (int mul : {0, 2}) cands.push_back({w, wps, 32, mul});
+  } else {
+    for (int g : {4, 8, 16, 32})
+      for (int wps : {8, 16})
+        for (int mul : {0, 1}) cands.push_back({4, wps, g, mul});
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::array<int, 4> best = cands[0];
+  float best_ms = 3.0e38f;
+  ce = mfg::launch_tune_fill(tp->args, plan->kind == mfg_plan::POTRF ? 1 : 0, s);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(a0, a, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(b0, b, sizeof(double) * (bt + 1), cudaMemcpyDeviceToDevice, s);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  for (size_t c = 0; ce == cudaSuccess && rc == MFG_OK && c < cands.size(); c++) {
+    const auto& k = cands[c];
+    rc = plan_reshape(tp, k[0], k[1], k[2], k[3]);
+    float tmin = 3.0e38f;
+    for (int rep = 0; rc == MFG_OK && ce == cudaSuccess && rep < 2; rep++) {
+      ce = cudaMemcpyAsync(a, a0, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
+      if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(b, b0, sizeof(double) * (bt + 1), cudaMemcpyDeviceToDevice, s);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+      if (ce == cudaSuccess) rc = plan_launch(tp, s);
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == MFG_OK && ce == cudaSuccess) tmin = std::min(tmin, ms);
+    }
+    if (tmin < best_ms) {
+      best_ms = tmin;
+      best = k;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(s);
+  buf.release();
+  mfg_plan_destroy(tp);
+  if (rc != MFG_OK) return rc;
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "autotune");
+  rc = plan_reshape(plan, best[0], best[1], best[2], best[3]);
+  if (rc != MFG_OK) return rc;
+  ctx->tune[tune_key((int)plan->kind, plan->max_n, plan->count)] = best;
+  if (config)
+    for (int i = 0; i < 4; i++) config[i] = best[i];
+  return MFG_OK;
 }
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan) {
