@@ -16,8 +16,10 @@
  *    or one of the MFG_ERR_* codes below.  No exception crosses the ABI.  Numerical failure that
  *    MatFlat reports by throwing MatrixFactorizationException is reported through an `info`
  *    output (0 = success, k+1 = first failing column k), never by a failing status.
- *  - Single-matrix entry points take HOST pointers (the memory MatFlat's callers pass); the library
- *    stages the data to the device and back and returns after the result is in host memory.
+ *  - Single-matrix entry points take the arrays MatFlat's callers pass in HOST memory, or the
+ *    same arrays in DEVICE memory (told apart through unified addressing); the library stages
+ *    them through its workspace and returns after the result is in place.  Scalar outputs
+ *    (sign, info) are host pointers.
  *  - Batched entry points take DEVICE pointers and are asynchronous on the context's stream.
  *  - The plain FP64 path reproduces MatFlat's arithmetic operation by operation (same summation
  *    trees, no fused multiply-add, IEEE division and square root), so factors, pivots and
@@ -78,7 +80,8 @@ MFG_API const char* mfg_last_error(mfg_ctx* ctx);
 MFG_API const char* mfg_version(void);
 
 /* ---------------------------------------------------------------------------------------------
- * Single-matrix drop-ins (host pointers).  Same argument meaning as the MatFlat method cited.
+ * Single-matrix drop-ins (host or device arrays).  Same argument meaning as the MatFlat method
+ * cited.
  * ------------------------------------------------------------------------------------------- */
 
 /* Factorization.Lu(int m, int n, double* a, int lda, int* piv) -> pivot sign

@@ -666,13 +666,13 @@ MFG_API int mfg_dgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv,
   int* d_out = cv.take<int>(2);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)m * 8, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_getrf_single(d_a, m, n, lda, d_piv, d_out, d_s, s));
   int out[2];
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)m * 8, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (sign) *sign = out[0];
   return MFG_OK;
@@ -696,12 +696,12 @@ MFG_API int mfg_dpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
   int* d_out = cv.take<int>(1);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_potrf_single(d_a, n, lda, d_out, d_s, s));
   int out = 0;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)n * 8, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (info) *info = out;
   return MFG_OK;
@@ -731,10 +731,10 @@ MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a,
   double* d_s = cv.take<double>(2 * (size_t)(n | 1));
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
-                                  cudaMemcpyHostToDevice, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * 8, cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * 8, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_trsv_single(uplo, trans, n, d_a, lda, d_x, incx, d_s, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * 8, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * 8, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -787,12 +787,12 @@ MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k,
   double* d_c = cv.take<double>(nc);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)ar * 8, ac,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_b, (size_t)ldb * 8, b, (size_t)ldb * 8, (size_t)br * 8, bc,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_gemm_single(transa, transb, m, n, k, d_a, lda, d_b, ldb, d_c, ldc, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(c, (size_t)ldc * 8, d_c, (size_t)ldc * 8, (size_t)m * 8, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -806,15 +806,22 @@ MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, 
     return fail(ctx, -4,
                 "The leading dimension must be greater than or equal to the order of the matrix.");
   if (!piv) return fail(ctx, -5, "piv is null");
-  // Singularity check before anything is written (LuInverse.cs:145-152).
+  // Singularity check before anything is written (LuInverse.cs:145-152), on host copies of the
+  // diagonal and the pivots (a and piv may be device arrays).
+  std::vector<double> diag(n);
+  std::vector<int> hpiv(n);
+  MFG_CUDA(ctx, cudaMemcpy2D(diag.data(), sizeof(double), a, (size_t)(lda + 1) * sizeof(double),
+                             sizeof(double), n, cudaMemcpyDefault));
+  MFG_CUDA(ctx, cudaMemcpy(hpiv.data(), piv, sizeof(int) * n, cudaMemcpyDefault));
   for (int j = 0; j < n; j++) {
-    if (a[(size_t)lda * j + j] == 0.0) {
+    if (diag[j] == 0.0) {
       if (info) *info = 1;
       return MFG_OK;
     }
   }
   for (int j = 0; j < n; j++)
-    if (piv[j] < 0 || piv[j] >= n) return fail(ctx, -5, "piv[%d] = %d is out of range", j, piv[j]);
+    if (hpiv[j] < 0 || hpiv[j] >= n)
+      return fail(ctx, -5, "piv[%d] = %d is out of range", j, hpiv[j]);
   const int warps = 8;
   const size_t na = span(n, n, lda);
   const size_t nwork = (size_t)n * n;
@@ -829,11 +836,11 @@ MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, 
   int* d_piv = cv.take<int>(n);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
-                                  cudaMemcpyHostToDevice, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(d_piv, piv, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_piv, piv, sizeof(int) * n, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_getri_single(d_a, n, lda, d_piv, d_w, d_s, warps, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)n * 8, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (info) *info = 0;
   return MFG_OK;
@@ -870,11 +877,11 @@ static int qr_single(mfg_ctx* ctx, int m, int n, T* a, int lda, T* rdiag) {
   cudaStream_t s = ctx->stream;
   const size_t es = sizeof(T);
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_qr_single<T>(d_a, m, n, lda, d_r, d_s, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * es, cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * es, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -907,10 +914,10 @@ static int qr_q_single(mfg_ctx* ctx, int m, int n, const T* a, int lda, T* q, in
   cudaStream_t s = ctx->stream;
   const size_t es = sizeof(T);
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_qr_q_single<T>(d_a, m, n, lda, d_q, ldq, d_s, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(q, (size_t)ldq * es, d_q, (size_t)ldq * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -945,11 +952,11 @@ static int qr_r_single(mfg_ctx* ctx, int m, int n, const T* a, int lda, T* r, in
   cudaStream_t s = ctx->stream;
   const size_t es = sizeof(T);
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
-                                  cudaMemcpyHostToDevice, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * es, cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * es, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_qr_r_single<T>(d_a, n, lda, d_r, ldr, d_d, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(r, (size_t)ldr * es, d_r, (size_t)ldr * es, (size_t)n * es, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -1081,13 +1088,13 @@ int getrf_t(mfg_ctx* ctx, int m, int n, void* a, int lda, int* piv, int* sign, s
   int* d_out = cv.take<int>(2);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, launch(d_a, m, n, lda, d_piv, d_out, d_s, s));
   int out[2];
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(piv, d_piv, sizeof(int) * m, cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (sign) *sign = out[0];
   return MFG_OK;
@@ -1110,12 +1117,12 @@ int potrf_t(mfg_ctx* ctx, int n, void* a, int lda, int* info, size_t es,
   int* d_out = cv.take<int>(1);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, launch(d_a, n, lda, d_out, d_s, s));
   int out = 0;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)n * es, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (info) *info = out;
   return MFG_OK;
@@ -1148,10 +1155,10 @@ int trsv_t(mfg_ctx* ctx, int uplo, int trans, int n, const void* a, int lda, voi
   double* d_s = cv.take<double>(nscr);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
-                                  cudaMemcpyHostToDevice, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * es, cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_x, x, nx * es, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, launch(uplo, trans, n, d_a, lda, d_x, incx, d_s, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * es, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(x, d_x, nx * es, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -1192,12 +1199,12 @@ int gemm_t(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const void
   char* d_c = cv.take<char>(nc * es);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)ar * es, ac,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_b, (size_t)ldb * es, b, (size_t)ldb * es, (size_t)br * es, bc,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, launch(transa, transb, m, n, k, d_a, lda, d_b, ldb, d_c, ldc, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(c, (size_t)ldc * es, d_c, (size_t)ldc * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -1297,11 +1304,11 @@ int zqr_single(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
   double* d_s = cv.take<double>(2 * (size_t)(n + 1));
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_zqr_single(d_a, m, n, lda, d_r, d_s, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * 8, cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(rdiag, d_r, n * 8, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -1332,10 +1339,10 @@ int zqr_q_single(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q
   double* d_s = cv.take<double>(2 * (size_t)(n + 1));
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)m * es, n,
-                                  cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_zqr_q_single(d_a, m, n, lda, d_q, ldq, d_s, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(q, (size_t)ldq * es, d_q, (size_t)ldq * es, (size_t)m * es, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
@@ -1367,11 +1374,11 @@ int zqr_r_single(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r
   double* d_d = cv.take<double>(n);
   cudaStream_t s = ctx->stream;
   MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
-                                  cudaMemcpyHostToDevice, s));
-  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * 8, cudaMemcpyHostToDevice, s));
+                                  cudaMemcpyDefault, s));
+  MFG_CUDA(ctx, cudaMemcpyAsync(d_d, rdiag, n * 8, cudaMemcpyDefault, s));
   MFG_CUDA(ctx, mfg::launch_zqr_r_single(d_a, n, lda, d_r, ldr, d_d, s));
   MFG_CUDA(ctx, cudaMemcpy2DAsync(r, (size_t)ldr * es, d_r, (size_t)ldr * es, (size_t)n * es, n,
-                                  cudaMemcpyDeviceToHost, s));
+                                  cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   return MFG_OK;
 }
