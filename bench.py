@@ -408,6 +408,39 @@ def run_mixed(args, torch, mf, world, rank, local):
         clocks.stop()
     ms = t0.elapsed_time(t1) / args.steps
     value = world * count / (ms / 1e3)
+
+    # End to end through the C ABI: A and b from pinned host memory, x, berr, iters and info
+    # back to pinned host memory, every step.
+    e2e = None
+    if not args.no_e2e:
+        ins = [a, b]
+        outs = [x, berr, iters, info]
+        ins_h = [t.cpu().pin_memory() for t in ins]
+        outs_h = [torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in outs]
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                for t, th in zip(ins, ins_h):
+                    t.copy_(th, non_blocking=True)
+                run()
+                for t, th in zip(outs, outs_h):
+                    th.copy_(t, non_blocking=True)
+            stream.synchronize()
+            q0 = torch.cuda.Event(enable_timing=True)
+            q1 = torch.cuda.Event(enable_timing=True)
+            q0.record(stream)
+            for _ in range(args.steps):
+                for t, th in zip(ins, ins_h):
+                    t.copy_(th, non_blocking=True)
+                run()
+                for t, th in zip(outs, outs_h):
+                    th.copy_(t, non_blocking=True)
+            q1.record(stream)
+            stream.synchronize()
+        e2e_ms = q0.elapsed_time(q1) / args.steps
+        e2e = {"value": world * count / (e2e_ms / 1e3), "unit": "solves/s",
+               "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in ins)),
+               "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in outs)),
+               "ms_per_step": e2e_ms}
     be = berr.cpu().numpy()
     it = iters.cpu().numpy()
     inf = info.cpu().numpy()
@@ -489,6 +522,7 @@ def run_mixed(args, torch, mf, world, rank, local):
                                  "factorization's 2n^3/3; the panel and refinement sweeps, not "
                                  "the tensor-core GEMMs, dominate at n=512"},
             "cpu_baseline": cpu,
+            "e2e": e2e,
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -750,6 +784,10 @@ def main():
         cpu = {"value": rate, "unit": "matrices/s", "cores": threads, "kind": "port",
                "sample": "%d matrices (batch of %d, evenly strided, repeated if smaller than "
                          "the budget; %.1f s)" % (sample_n, count, t)}
+        rate1, n1, _, t1s = cpu_sample_rate(cfg_name, d, budget_s=max(1.0, args.cpu_budget / 4),
+                                            threads=1)
+        cpu["single_thread"] = {"value": rate1, "sample": "%d matrices, 1 thread (%.1f s)"
+                                                          % (n1, t1s)}
 
     if rank == 0:
         line = {

@@ -229,19 +229,16 @@ constexpr int GRAD_MAX_N = 128;
 constexpr int GRAD_SMEM_DOUBLES = GRAD_LDX * GRAD_MAX_N + 4 * GRAD_MAX_N;
 constexpr int GRAD_WARPS = 6;   // 6 x 37.9 KB per CTA, one CTA per SM
 
-// K^-1 = L^-T L^-1 column by column, MatFlat's two solves applied to the columns of the identity
-// (SolveTriangular Lower/NoTrans, Blas.SolveTriangular.cs:215-222, then Lower/Trans, :224-238,
-// MulSub :397-421), one lane per column: lane l of chunk j0 solves column c = j0 + l.  Keeps the
-// entries i < c of column c in G's strict upper triangle and K^-1(c,c) in kdiag.
-//   Forward, dot form: x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i).  For i < c, x_i = +0 exactly
-//   (0 minus a signed-zero dot, divided by L(i,i) > 0), so with a finite L the dots of a chunk
-//   start at k0 = j0 (the same argument as in the batched LuInverse: the skipped terms are
-//   signed zeros); otherwise they start at 0.
-//   Backward, column sweep: x_j /= L(j,j); x_k -= L(j,k) * x_j (k < j), j = n-1 .. 0.
-// Rows of L are staged in shared memory one ahead of their use.  The products use the FP64
-// pipe: with one CTA of six warps per SM the integer-pipe product's latency is not hidden.
-__device__ void chol_inverse_lanes(const double* L, int n, long long ld, double* G, double* kdiag,
-                                   double* xs, double* vb) {
+// W = L^-1, column by column: MatFlat's SolveTriangular(Lower, NoTrans) (Blas.SolveTriangular.cs:
+// 215-222) applied to the columns of the identity, one lane per column (lane l of chunk j0 solves
+// column c = j0 + l): x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i).  For i < c, x_i = +0 exactly (0
+// minus a signed-zero dot, divided by L(i,i) > 0), so with a finite L the dots of a chunk start at
+// k0 = j0 (as in the batched LuInverse: the skipped terms are signed zeros); otherwise at 0.  Rows
+// of L are staged in shared memory one ahead of use; products on the FP64 pipe.
+// Output layout (G is free above its diagonal): W(i,c), i > c, goes to G(c,i) = G[i*ld + c] (a
+// coalesced row of lanes), W(c,c) to wdiag[c].
+__device__ void chol_w_lanes(const double* L, int n, long long ld, double* G, double* wdiag,
+                             double* xs, double* vb) {
   const int lane = threadIdx.x & 31;
   int nonfinite = 0;
   for (int c = 0; c < n; ++c)
@@ -249,11 +246,11 @@ __device__ void chol_inverse_lanes(const double* L, int n, long long ld, double*
       nonfinite |= ((dbits(L[(long long)c * ld + r]) >> 52) & 0x7FF) == 0x7FF;
   nonfinite = __any_sync(FULL_MASK, nonfinite);
   for (int j0 = 0; j0 < n; j0 += 32) {
-    const int t = j0 + lane < n ? j0 + lane : j0;  // lanes past n repeat lane 0's column
+    const bool active = j0 + lane < n;
+    const int t = active ? j0 + lane : j0;  // lanes past n repeat lane 0's column
     const int k0 = nonfinite ? 0 : j0;
     double* x = xs + lane;
     for (int i = 0; i < n; i++) x[i * GRAD_LDX] = (i == t) ? 1.0 : 0.0;
-    // Forward: row i of L, entries k0..i (diagonal last), staged one row ahead.
     stage_async(vb + (k0 & 1) * n, L + k0, k0, k0 + 1, ld);
     stage_wait();
     for (int i = k0; i < n; i++) {
@@ -282,39 +279,100 @@ __device__ void chol_inverse_lanes(const double* L, int n, long long ld, double*
       x[i * GRAD_LDX] = __ddiv_rn(__dsub_rn(x[i * GRAD_LDX], s), li[i]);
       stage_wait();
     }
-    // Backward: row j of L, entries 0..j (diagonal last), staged one row ahead.
-    stage_async(vb + ((n - 1) & 1) * n, L + (n - 1), 0, n, ld);
-    stage_wait();
-    for (int j = n - 1; j >= 0; j--) {
-      const double* lj = vb + (j & 1) * n;
-      if (j > 0) stage_async(vb + ((j - 1) & 1) * n, L + (j - 1), 0, j, ld);
-      const double xj = __ddiv_rn(x[j * GRAD_LDX], lj[j]);
-      x[j * GRAD_LDX] = xj;
-      int k = 0;
-      for (; k + 8 <= j; k += 8) {
-        double l8[8], v8[8], pr[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          l8[r] = lj[k + r];
-          v8[r] = x[(k + r) * GRAD_LDX];
-        }
-        mul_block_s<0, 8, false>(l8, xj, pr);
-#pragma unroll
-        for (int r = 0; r < 8; r++) x[(k + r) * GRAD_LDX] = __dsub_rn(v8[r], pr[r]);
-      }
-      for (; k < j; k++) x[k * GRAD_LDX] = __dsub_rn(x[k * GRAD_LDX], __dmul_rn(lj[k], xj));
-      stage_wait();
-    }
-    // Column c = j0 + l: entries i < c to G's strict upper triangle, i = c to kdiag.
-    const int nc = min(32, n - j0);
-    for (int l = 0; l < nc; l++) {
-      const int c = j0 + l;
-      double* col = G + (long long)c * ld;
-      for (int i = lane; i < c; i += 32) col[i] = xs[i * GRAD_LDX + l];
-      if (lane == 0) kdiag[c] = xs[c * GRAD_LDX + l];
-    }
+    if (active) wdiag[t] = x[t * GRAD_LDX];
+    for (int i = j0 + 1; i < n; i++)          // one coalesced row segment per i
+      if (active && i > t) G[(long long)i * ld + t] = x[i * GRAD_LDX];
     __syncwarp();
   }
+}
+
+// Entry (k, c) of W in the layout chol_w_lanes leaves (W is lower triangular; its structural
+// zeros are +0, as the solve produces them).
+__device__ __forceinline__ double w_at(const double* G, long long ld, const double* wdiag, int k,
+                                       int c) {
+  return k == c ? wdiag[c] : (k > c ? G[(long long)k * ld + c] : 0.0);
+}
+
+// C(i,j) = Internals.Dot(n, W(:,i), W(:,j)), i <= j, in MatFlat's pairwise order (MulMatMat's
+// dot).  W(k,j) = +0 for k < j, so the sum starts at k = j: an even offset from the first pair
+// starts with pair (j, j+1), an odd one seeds with the product at j (its pair partner is a zero).
+// The skipped terms are signed zeros, which can only change the sign of a zero result; a zero
+// result is therefore recomputed over all n terms.
+__device__ double wtw_dot(const double* G, long long ld, const double* wdiag, int n, int i, int j) {
+  const int p0 = n & 1;
+  double s = 0.0;
+  int k;
+  if (j == 0 && p0) {
+    s = __dmul_rn(w_at(G, ld, wdiag, 0, i), w_at(G, ld, wdiag, 0, j));
+    k = 1;
+  } else if (((j - p0) & 1) == 0) {
+    k = j;
+  } else {
+    s = __dmul_rn(w_at(G, ld, wdiag, j, i), wdiag[j]);
+    k = j + 1;
+  }
+  // Pairs (k, k+1) ... (n-2, n-1); here k > j >= i, so both factors are stored entries (k > i).
+  if (k == j && k + 1 < n) {
+    // First pair holds the diagonal of column j (and of column i when i == j).
+    const double a0 = w_at(G, ld, wdiag, j, i), b0 = wdiag[j];
+    const double a1 = G[(long long)(j + 1) * ld + i], b1 = G[(long long)(j + 1) * ld + j];
+    s = __dadd_rn(s, __dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)));
+    k += 2;
+  }
+  for (; k + 8 <= n; k += 8) {
+    double a8[8], b8[8], pr[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      a8[r] = G[(long long)(k + r) * ld + i];
+      b8[r] = G[(long long)(k + r) * ld + j];
+    }
+    mul_block<0, 8, false>(a8, b8, pr);
+#pragma unroll
+    for (int r = 0; r < 4; r++) s = __dadd_rn(s, __dadd_rn(pr[2 * r], pr[2 * r + 1]));
+  }
+  for (; k + 1 < n; k += 2)
+    s = __dadd_rn(s, __dadd_rn(__dmul_rn(G[(long long)k * ld + i], G[(long long)k * ld + j]),
+                               __dmul_rn(G[(long long)(k + 1) * ld + i],
+                                         G[(long long)(k + 1) * ld + j])));
+  if (!nonzero(s)) {
+    // The sign of a zero sum depends on the skipped terms: MatFlat's full dot.
+    s = 0.0;
+    k = 0;
+    if (p0) {
+      s = __dmul_rn(w_at(G, ld, wdiag, 0, i), w_at(G, ld, wdiag, 0, j));
+      k = 1;
+    }
+    for (; k < n; k += 2)
+      s = __dadd_rn(s, __dadd_rn(__dmul_rn(w_at(G, ld, wdiag, k, i), w_at(G, ld, wdiag, k, j)),
+                                 __dmul_rn(w_at(G, ld, wdiag, k + 1, i),
+                                           w_at(G, ld, wdiag, k + 1, j))));
+  }
+  return s;
+}
+
+// K^-1 = W^T W (MatFlat's MulMatMat(Trans, NoTrans)) for the upper triangle i <= j, one entry per
+// lane over the triangle flattened column by column.  C(i,j), i < j, goes to G(j,i) = G[i*ld + j]
+// (below G's diagonal: L, if it lived there, is no longer needed), C(j,j) to kdiag[j].
+__device__ void chol_wtw_lanes(double* G, int n, long long ld, const double* wdiag, double* kdiag) {
+  const int lane = threadIdx.x & 31;
+  const long long total = (long long)n * (n + 1) / 2;
+  // entry e of column j is (i, j) with e = j(j+1)/2 + i
+  int j = 0;
+  while ((long long)(j + 1) * (j + 2) / 2 <= lane) j++;
+  int i = lane - j * (j + 1) / 2;
+  for (long long e = lane; e < total; e += 32) {
+    const double c = wtw_dot(G, ld, wdiag, n, i, j);
+    if (i == j)
+      kdiag[j] = c;
+    else
+      G[(long long)i * ld + j] = c;
+    i += 32;
+    while (i > j) {
+      i -= j + 1;
+      j++;
+    }
+  }
+  __syncwarp();
 }
 
 __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double* y, double* loss,
@@ -361,18 +419,20 @@ __device__ void chol_grad_warp(double* K, double* G, int n, long long ld, double
     *loss = __dadd_rn(quad, __dmul_rn(2.0, logsum));
     *info_out = 0;
   }
-  chol_inverse_lanes(L, n, ld, G, kdiag, xs, vb);
-  // G = K^-1 - alpha alpha^T (alpha is in y), symmetric.
+  // W = L^-1 above G's diagonal (and in wdiag, reusing the Cholesky sums' space), then
+  // K^-1 = W^T W below it (and in kdiag).
+  double* wdiag = dsum;
+  chol_w_lanes(L, n, ld, G, wdiag, xs, vb);
+  chol_wtw_lanes(G, n, ld, wdiag, kdiag);
+  // G = K^-1 - alpha alpha^T (alpha is in y), written to both triangles.
   for (int c = 0; c < n; ++c) {
     for (int r = lane; r <= c; r += 32) {
-      const double kinv = (r == c) ? kdiag[c] : G[(long long)c * ld + r];
+      const double kinv = (r == c) ? kdiag[c] : G[(long long)r * ld + c];
       const double g = __dsub_rn(kinv, __dmul_rn(y[r], y[c]));
       G[(long long)c * ld + r] = g;
+      G[(long long)r * ld + c] = g;
     }
   }
-  __syncwarp();
-  for (int c = 0; c < n; ++c)
-    for (int r = c + 1 + lane; r < n; r += 32) G[(long long)c * ld + r] = G[(long long)r * ld + c];
   __syncwarp();
 }
 

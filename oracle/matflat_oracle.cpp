@@ -911,8 +911,10 @@ void orc_sqr_ls(int m, int n, float* a, int lda, const float* b, float* x) {
 // Differentiable Cholesky / log-determinant / solve, composed from MatFlat's routines:
 // L = Cholesky(K); z = L^-1 y (SolveTriangular Lower/NoTrans); quad = Internals.Dot(z, z);
 // log det K = 2 * sum_i log L_ii; alpha = L^-T z (SolveTriangular Lower/Trans);
-// K^-1 column c = the same two solves applied to e_c (the LuInverse idiom), upper triangle kept;
-// grad = K^-1 - alpha alpha^T, mirrored to a full symmetric matrix (leading dimension lda).
+// W = L^-1 column by column (SolveTriangular Lower/NoTrans applied to e_c);
+// K^-1 = W^T W (Blas.MulMatMat(Trans, NoTrans), Blas.MulMatMat.cs:226-368, which is exactly
+// symmetric: C[i,j] and C[j,i] are the same dot); grad = K^-1 - alpha alpha^T, upper triangle
+// computed and mirrored to a full symmetric matrix (leading dimension lda).
 // On exit k holds L, y holds alpha.  Returns Cholesky's code (0 = success).
 int orc_dchol_grad(int n, double* k, int lda, double* y, double* loss, double* g) {
   int info = orc_dcholesky(n, k, lda);
@@ -926,15 +928,17 @@ int orc_dchol_grad(int n, double* k, int lda, double* y, double* loss, double* g
   for (int i = 0; i < n; i++) logsum = logsum + std::log(k[(long)i * lda + i]);
   orc_dtrsv(LOWER, TRANS, n, k, lda, y, 1);
   *loss = quad + 2.0 * logsum;
-  std::vector<double> e(n);
-  for (int c = 0; c < n; c++) {
-    for (int i = 0; i < n; i++) e[i] = (i == c) ? 1.0 : 0.0;
-    orc_dtrsv(LOWER, NOTRANS, n, k, lda, e.data(), 1);
-    orc_dtrsv(LOWER, TRANS, n, k, lda, e.data(), 1);
-    for (int i = 0; i <= c; i++) g[(long)c * lda + i] = e[i] - y[i] * y[c];
+  std::vector<double> w((size_t)n * n), c((size_t)n * n);
+  for (int j = 0; j < n; j++) {
+    double* wj = w.data() + (size_t)n * j;
+    for (int i = 0; i < n; i++) wj[i] = (i == j) ? 1.0 : 0.0;
+    orc_dtrsv(LOWER, NOTRANS, n, k, lda, wj, 1);
   }
-  for (int c = 0; c < n; c++)
-    for (int r = c + 1; r < n; r++) g[(long)c * lda + r] = g[(long)r * lda + c];
+  orc_dgemm(TRANS, NOTRANS, n, n, n, w.data(), n, w.data(), n, c.data(), n);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i <= j; i++) g[(long)j * lda + i] = c[(size_t)n * j + i] - y[i] * y[j];
+  for (int j = 0; j < n; j++)
+    for (int r = j + 1; r < n; r++) g[(long)j * lda + r] = g[(long)r * lda + j];
   return 0;
 }
 

@@ -94,3 +94,53 @@ def test_grad_rbf_central_differences(mf):
         fd = (run(K + h * E)[0] - run(K - h * E)[0]) / (2 * h)
         an = G[i, j] * (1 if i == j else 2)
         assert abs(fd - an) <= 1e-2 * abs(an), (i, j, fd, an)
+
+
+@pytest.mark.parametrize("keep_factor", [True, False])
+def test_grad_structured_zeros(mf, keep_factor):
+    """Exact zeros in L^-1, K^-1 and alpha (diagonal, block-diagonal and arrow matrices, y with
+    zeros): the gradient's signed zeros match the oracle bit for bit."""
+    import torch
+    rng = np.random.default_rng(22)
+    n = np.array([5, 33, 64, 97, 128, 7], np.int32)
+    mats, ys = [], []
+    for i, ni in enumerate(n):
+        if i % 3 == 0:
+            s = np.diag(rng.uniform(1.0, 3.0, ni))
+        elif i % 3 == 1:
+            s = np.zeros((ni, ni))
+            h = ni // 2
+            for lo, hi in ((0, h), (h, ni)):
+                b = rng.standard_normal((hi - lo, hi - lo))
+                s[lo:hi, lo:hi] = b @ b.T + (hi - lo) * np.eye(hi - lo)
+        else:
+            s = np.eye(ni) * ni
+            s[0, 1:] = s[1:, 0] = rng.choice([-1.0, 0.0, 1.0], ni - 1)
+        mats.append(s.reshape(-1, order="F"))
+        yy = rng.standard_normal(ni)
+        yy[rng.random(ni) < 0.3] = 0.0
+        yy[rng.random(ni) < 0.1] = -0.0
+        ys.append(yy)
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]])
+    a = np.concatenate(mats)
+    b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]])
+    y = np.concatenate(ys)
+    batch = mf.CholeskyBatch(n, a_off, nrhs=1, b_off=b_off)
+    dk = torch.from_numpy(a.copy()).cuda()
+    dy = torch.from_numpy(y.copy()).cuda()
+    dloss = torch.zeros(len(n), dtype=torch.float64, device="cuda")
+    dgrad = torch.zeros_like(dk)
+    dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    batch.loss_and_grad(dk, dy, dloss, dgrad, dinfo, keep_factor=keep_factor)
+    mf.context().synchronize()
+    ok, oy, og = a.copy(), y.copy(), np.zeros_like(a)
+    oloss = np.zeros(len(n))
+    oinfo = np.zeros(len(n), np.int32)
+    oracle.chol_grad_batched(n, a_off, ok, b_off, oy, oloss, og, oinfo, 1)
+    assert (oinfo == 0).all()
+    gg = dgrad.cpu().numpy()
+    assert (og == 0).any()
+    for i in range(len(n)):
+        sl = slice(a_off[i], a_off[i] + sz[i])
+        _bits_equal(gg[sl], og[sl], "grad %d" % i)
