@@ -718,7 +718,38 @@ def main():
 
     # ---- end to end through the C ABI from pinned host memory -------------------------------
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and cfg_name == "lu":
+        # The host-buffer entry point (mfg_dgetrf_batched_host): copies and compute pipelined
+        # over chunks inside one synchronous call, timed by the host clock.  The call is in place,
+        # so the host arrays are restored from a pristine pinned copy before each (untimed).
+        io = [torch.empty_like(a_host).pin_memory(), torch.empty_like(b_host).pin_memory()]
+        piv_h = torch.zeros(d["piv_total"], dtype=torch.int32).pin_memory()
+        sign_h = torch.zeros(count, dtype=torch.int32).pin_memory()
+        info_h = torch.zeros(count, dtype=torch.int32).pin_memory()
+        times = []
+        for it in range(2 + args.steps):
+            io[0].copy_(a_host)
+            io[1].copy_(b_host)
+            torch.cuda.synchronize()
+            barrier()
+            t_0 = time.perf_counter()
+            plan.run_host(io[0], piv_h, io[1], sign_h, info_h)
+            t_1 = time.perf_counter()
+            if it >= 2:
+                times.append(t_1 - t_0)
+        e2e_ms = 1e3 * sum(times) / len(times)
+        if world > 1:
+            tt = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_ms = float(tt.item())
+        h2d = a_host.numel() * 8 + b_host.numel() * 8
+        d2h = h2d + piv_h.numel() * 4 + 2 * count * 4
+        e2e = {"value": world * count / (e2e_ms / 1e3), "unit": "matrices/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": e2e_ms,
+               "path": "mfg_dgetrf_batched_host on page-locked host arrays (copies pipelined "
+                       "with compute over chunks of the batch), host wall clock per call"}
+    elif not args.no_e2e:
         h2d = a_host.numel() * a_host.element_size() + b_host.numel() * b_host.element_size()
         d2h = sum(o.numel() * o.element_size() for o in outs)
         with torch.cuda.stream(stream):

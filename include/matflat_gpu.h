@@ -183,6 +183,14 @@ MFG_API int mfg_plan_getrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
  * first exactly-zero pivot U(k,k), LAPACK's convention; the factorization still completes). */
 MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                int* info);
+/* The same factor + solve on HOST buffers (the arrays a C# caller pins), laid out exactly as the
+ * plan describes: the batch is cut into contiguous chunks of about equal work, and each chunk's
+ * upload, factorization and download overlap with its neighbours' on separate streams, so the
+ * copies hide behind the compute.  Synchronous: returns when a, piv, b, sign and info hold the
+ * results (bit-identical to mfg_dgetrf_batched).  Page-locked host memory gives full copy speed.
+ * The first call allocates device mirrors of the arrays and per-chunk plans (kept by the plan). */
+MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                                    int* info);
 /* Solve only, with factors and pivots already in a and piv (from mfg_dgetrf_batched or
  * Factorization.Lu): b' = P b, the unit-lower solve (LuInverse idiom, Factorization.LuInverse.cs:
  * 174-182) and the upper solve (Blas.SolveTriangular.cs:191-199), for the plan's nrhs (>= 1)

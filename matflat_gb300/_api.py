@@ -55,6 +55,7 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
+    "mfg_dgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
     "mfg_dgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -360,6 +361,15 @@ class Blas:
 # ---------------------------------------------------------------------------------------------
 # Batched overloads.  Arrays are device memory: pass torch CUDA tensors or raw device pointers.
 
+def _hptr(x):
+    """Pointer of a host array: numpy array or CPU tensor."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        return _ptr(x)
+    return _vp(x.data_ptr())
+
+
 def _dptr(x):
     if x is None:
         return None
@@ -433,6 +443,13 @@ class LuBatch(_Batch):
         rc = self.ctx.lib.mfg_dgetrf_batched(self.h, _dptr(a), _dptr(piv), _dptr(b), _dptr(sign),
                                              _dptr(info))
         self.ctx.check(rc, "mfg_dgetrf_batched")
+
+    def run_host(self, a, piv, b, sign, info):
+        """Factor + solve on host buffers (numpy arrays or CPU tensors, page-locked for full
+        speed); copies and compute are pipelined over chunks of the batch.  Synchronous."""
+        rc = self.ctx.lib.mfg_dgetrf_batched_host(self.h, _hptr(a), _hptr(piv), _hptr(b),
+                                                  _hptr(sign), _hptr(info))
+        self.ctx.check(rc, "mfg_dgetrf_batched_host")
 
     def solve(self, a, piv, b):
         """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b)."""

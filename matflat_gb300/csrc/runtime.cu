@@ -87,6 +87,19 @@ struct mfg_plan {
   int ctas = 0;
   int warps = 0;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
+  // GETRF: host copies of the layout, and the pipelined host-buffer path (built on first use):
+  // contiguous chunks of the batch, each with its own plan, device mirrors of the user's arrays.
+  std::vector<int> hlda;
+  std::vector<long long> haoff, hpivoff, hboff;
+  struct Pipe {
+    std::vector<mfg_plan*> chunk;
+    std::vector<int> c0, c1;                       // matrix index range of every chunk
+    std::vector<size_t> alo, ahi, plo, phi, blo, bhi;  // element ranges of a, piv, b
+    DevBuf da, dpiv, db, dsign, dinfo;
+    cudaStream_t h2d = nullptr, d2h = nullptr, comp2 = nullptr;
+    std::vector<cudaEvent_t> in, done;
+    bool ready = false;
+  } pipe;
   // CUDA graph of the last execution (keyed by the data pointers and the stream).
   cudaGraphExec_t exec = nullptr;
   const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -441,6 +454,16 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
   a.group = group;
   a.dot_block = env_int("MFG_DOT_BLOCK", 4);
+  if (kind == mfg_plan::GETRF) {
+    p->hlda.resize(count);
+    p->haoff.assign(a_off, a_off + count);
+    p->hpivoff.assign(piv_off, piv_off + count);
+    p->hboff.resize(count);
+    for (int i = 0; i < count; i++) {
+      p->hlda[i] = lda ? lda[i] : n[i];
+      p->hboff[i] = nrhs > 0 ? b_off[i] : 0;
+    }
+  }
   if (kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) {
     p->hn.assign(n, n + count);
     if (!tune_env_override()) {
@@ -1544,6 +1567,20 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   if (!plan) return -1;
   if (plan->exec) cudaGraphExecDestroy(plan->exec);
   cudaStreamSynchronize(plan->ctx->stream);
+  auto& pp = plan->pipe;
+  for (mfg_plan* c : pp.chunk) mfg_plan_destroy(c);
+  for (cudaEvent_t e : pp.in) cudaEventDestroy(e);
+  for (cudaEvent_t e : pp.done) cudaEventDestroy(e);
+  for (cudaStream_t st : {pp.h2d, pp.d2h, pp.comp2})
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  pp.da.release();
+  pp.dpiv.release();
+  pp.db.release();
+  pp.dsign.release();
+  pp.dinfo.release();
   plan->meta.release();
   plan->scratch.release();
   plan->mx_work.release();
@@ -1589,6 +1626,169 @@ MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, 
   plan->args.info = nullptr;
   plan->args.solve_only = 1;
   return plan_execute(plan, a, piv, b, nullptr, (const void*)3);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Builds the pipelined host-buffer path of a getrf plan: the batch is cut into contiguous chunks
+// of about equal work (sum of n^3), each with its own plan whose offsets address device mirrors of
+// the user's arrays laid out exactly like the host arrays.  A layout whose chunks would share
+// elements (overlapping matrices) gets a single chunk.
+int pipe_build(mfg_plan* p) {
+  mfg_ctx* ctx = p->ctx;
+  auto& pp = p->pipe;
+  const int count = p->count;
+  const int nrhs = p->nrhs;
+  int K = std::max(1, std::min(16, count / 4096));
+  K = env_int("MFG_PIPE_CHUNKS", K);
+  if (K < 1) K = 1;
+  double total = 0;
+  for (int i = 0; i < count; i++) total += (double)p->hn[i] * p->hn[i] * p->hn[i];
+  std::vector<int> cut{0};
+  double acc = 0;
+  for (int i = 0; i < count && (int)cut.size() < K; i++) {
+    acc += (double)p->hn[i] * p->hn[i] * p->hn[i];
+    if (acc >= total * cut.size() / K && i + 1 < count) cut.push_back(i + 1);
+  }
+  cut.push_back(count);
+  auto ranges = [&](int c0, int c1, size_t& alo, size_t& ahi, size_t& plo, size_t& phi,
+                    size_t& blo, size_t& bhi) {
+    alo = plo = blo = SIZE_MAX;
+    ahi = phi = bhi = 0;
+    for (int i = c0; i < c1; i++) {
+      const size_t a0 = (size_t)p->haoff[i];
+      alo = std::min(alo, a0);
+      ahi = std::max(ahi, a0 + span(p->hn[i], p->hn[i], p->hlda[i]));
+      plo = std::min(plo, (size_t)p->hpivoff[i]);
+      phi = std::max(phi, (size_t)p->hpivoff[i] + p->hn[i]);
+      if (nrhs > 0) {
+        blo = std::min(blo, (size_t)p->hboff[i]);
+        bhi = std::max(bhi, (size_t)p->hboff[i] + (size_t)p->hn[i] * nrhs);
+      }
+    }
+    if (nrhs == 0) blo = bhi = 0;
+  };
+  const int nc = (int)cut.size() - 1;
+  pp.c0.assign(cut.begin(), cut.end() - 1);
+  pp.c1.assign(cut.begin() + 1, cut.end());
+  pp.alo.resize(nc); pp.ahi.resize(nc); pp.plo.resize(nc); pp.phi.resize(nc);
+  pp.blo.resize(nc); pp.bhi.resize(nc);
+  for (int c = 0; c < nc; c++)
+    ranges(pp.c0[c], pp.c1[c], pp.alo[c], pp.ahi[c], pp.plo[c], pp.phi[c], pp.blo[c], pp.bhi[c]);
+  // Overlapping element ranges would let one chunk's upload overwrite another's data.
+  bool overlap = false;
+  for (int c = 0; c < nc && !overlap; c++)
+    for (int d = c + 1; d < nc && !overlap; d++)
+      overlap = (pp.alo[c] < pp.ahi[d] && pp.alo[d] < pp.ahi[c]) ||
+                (pp.plo[c] < pp.phi[d] && pp.plo[d] < pp.phi[c]) ||
+                (nrhs > 0 && pp.blo[c] < pp.bhi[d] && pp.blo[d] < pp.bhi[c]);
+  if (overlap && nc > 1) {
+    pp.c0 = {0};
+    pp.c1 = {count};
+    pp.alo.resize(1); pp.ahi.resize(1); pp.plo.resize(1); pp.phi.resize(1);
+    pp.blo.resize(1); pp.bhi.resize(1);
+    ranges(0, count, pp.alo[0], pp.ahi[0], pp.plo[0], pp.phi[0], pp.blo[0], pp.bhi[0]);
+  }
+  size_t aspan = 0, pspan = 0, bspan = 0;
+  for (size_t c = 0; c < pp.c0.size(); c++) {
+    aspan = std::max(aspan, pp.ahi[c]);
+    pspan = std::max(pspan, pp.phi[c]);
+    bspan = std::max(bspan, pp.bhi[c]);
+  }
+  MFG_CUDA(ctx, pp.da.reserve(sizeof(double) * std::max<size_t>(aspan, 1)));
+  MFG_CUDA(ctx, pp.dpiv.reserve(sizeof(int) * std::max<size_t>(pspan, 1)));
+  MFG_CUDA(ctx, pp.db.reserve(sizeof(double) * std::max<size_t>(bspan, 1)));
+  MFG_CUDA(ctx, pp.dsign.reserve(sizeof(int) * count));
+  MFG_CUDA(ctx, pp.dinfo.reserve(sizeof(int) * count));
+  MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.h2d, cudaStreamNonBlocking));
+  MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.d2h, cudaStreamNonBlocking));
+  MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.comp2, cudaStreamNonBlocking));
+  for (size_t c = 0; c < pp.c0.size(); c++) {
+    const int c0 = pp.c0[c], cnt = pp.c1[c] - pp.c0[c];
+    mfg_plan* sub = nullptr;
+    int rc = plan_create(ctx, &sub, mfg_plan::GETRF, cnt, p->hn.data() + c0, p->hlda.data() + c0,
+                         (const int64_t*)p->haoff.data() + c0,
+                         (const int64_t*)p->hpivoff.data() + c0, nrhs,
+                         nrhs > 0 ? (const int64_t*)p->hboff.data() + c0 : nullptr);
+    if (rc != MFG_OK) return rc;
+    // Same launch shape as the parent plan (which the autotuner may have chosen).
+    rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
+                      p->args.group, p->args.hw_mul);
+    if (rc != MFG_OK) return rc;
+    sub->args.a = (double*)pp.da.ptr;
+    sub->args.piv = (int*)pp.dpiv.ptr;
+    sub->args.b = nrhs > 0 ? (double*)pp.db.ptr : nullptr;
+    sub->args.sign = (int*)pp.dsign.ptr + c0;
+    sub->args.info = (int*)pp.dinfo.ptr + c0;
+    sub->args.solve_only = 0;
+    pp.chunk.push_back(sub);
+    cudaEvent_t e1, e2;
+    MFG_CUDA(ctx, cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+    MFG_CUDA(ctx, cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+    pp.in.push_back(e1);
+    pp.done.push_back(e2);
+  }
+  pp.ready = true;
+  return MFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                                    int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!piv) return fail(ctx, -3, "piv is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  if (!sign) return fail(ctx, -5, "sign is null");
+  if (!info) return fail(ctx, -6, "info is null");
+  auto& pp = plan->pipe;
+  if (!pp.ready) {
+    const int rc = pipe_build(plan);
+    if (rc != MFG_OK) return rc;
+  }
+  double* da = (double*)pp.da.ptr;
+  int* dpiv = (int*)pp.dpiv.ptr;
+  double* db = (double*)pp.db.ptr;
+  const int nrhs = plan->nrhs;
+  for (size_t c = 0; c < pp.chunk.size(); c++) {
+    const size_t an = pp.ahi[c] - pp.alo[c], bn = pp.bhi[c] - pp.blo[c];
+    MFG_CUDA(ctx, cudaMemcpyAsync(da + pp.alo[c], a + pp.alo[c], an * 8, cudaMemcpyDefault,
+                                  pp.h2d));
+    if (nrhs > 0)
+      MFG_CUDA(ctx, cudaMemcpyAsync(db + pp.blo[c], b + pp.blo[c], bn * 8, cudaMemcpyDefault,
+                                    pp.h2d));
+    MFG_CUDA(ctx, cudaEventRecord(pp.in[c], pp.h2d));
+    // Alternate two compute streams so one chunk's kernel can fill the SMs left idle by the
+    // previous chunk's last matrices.
+    cudaStream_t sc = (c & 1) ? pp.comp2 : ctx->stream;
+    MFG_CUDA(ctx, cudaStreamWaitEvent(sc, pp.in[c], 0));
+    const int rc = plan_launch(pp.chunk[c], sc);
+    if (rc != MFG_OK) return rc;
+    MFG_CUDA(ctx, cudaEventRecord(pp.done[c], sc));
+    MFG_CUDA(ctx, cudaStreamWaitEvent(pp.d2h, pp.done[c], 0));
+    const int c0 = pp.c0[c], cnt = pp.c1[c] - pp.c0[c];
+    MFG_CUDA(ctx, cudaMemcpyAsync(a + pp.alo[c], da + pp.alo[c], an * 8, cudaMemcpyDefault,
+                                  pp.d2h));
+    MFG_CUDA(ctx, cudaMemcpyAsync(piv + pp.plo[c], dpiv + pp.plo[c],
+                                  (pp.phi[c] - pp.plo[c]) * 4, cudaMemcpyDefault, pp.d2h));
+    if (nrhs > 0)
+      MFG_CUDA(ctx, cudaMemcpyAsync(b + pp.blo[c], db + pp.blo[c], bn * 8, cudaMemcpyDefault,
+                                    pp.d2h));
+    MFG_CUDA(ctx, cudaMemcpyAsync(sign + c0, (int*)pp.dsign.ptr + c0, cnt * 4, cudaMemcpyDefault,
+                                  pp.d2h));
+    MFG_CUDA(ctx, cudaMemcpyAsync(info + c0, (int*)pp.dinfo.ptr + c0, cnt * 4, cudaMemcpyDefault,
+                                  pp.d2h));
+  }
+  MFG_CUDA(ctx, cudaStreamSynchronize(pp.d2h));
+  return MFG_OK;
 }
 
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
