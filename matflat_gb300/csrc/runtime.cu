@@ -530,15 +530,17 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   const int genv = env_int("MFG_QR_GROUP", 0);
   if (genv == 4 || genv == 8 || genv == 16 || genv == 32) group_d = group_s = genv;
   const int group = std::min(group_d, group_s);
-  // Decreasing n, then decreasing m: roughly longest first, and the matrices that share a warp
-  // (group < 32) have the same n and similar m, so they run in lockstep.
-  (void)work;
-  std::stable_sort(order.begin(), order.end(),
+  // One queue order per group size: a whole warp per matrix takes them longest first (by work);
+  // groups of fewer lanes take decreasing n, then decreasing m, so the matrices that share a
+  // warp have the same n and similar m and run in lockstep.
+  std::vector<int> order_g = order;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  std::stable_sort(order_g.begin(), order_g.end(),
                    [&](int x, int y) { return n[x] != n[y] ? n[x] > n[y] : m[x] > m[y]; });
   const size_t ints = (size_t)count;
   const size_t bi = ((ints * sizeof(int) + 255) / 256) * 256;
   const size_t bl = ((ints * sizeof(long long) + 255) / 256) * 256;
-  const size_t total = 4 * bi + 3 * bl + 256;
+  const size_t total = 5 * bi + 3 * bl + 256;
   cudaError_t e = p->meta.reserve(total);
   if (e != cudaSuccess) {
     delete p;
@@ -554,6 +556,7 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
     ((long long*)(host.data() + 4 * bi + bl))[i] = rdiag_off[i];
     ((long long*)(host.data() + 4 * bi + 2 * bl))[i] = nrhs > 0 ? b_off[i] : 0;
   }
+  std::memcpy(host.data() + 4 * bi + 3 * bl + 256, order_g.data(), ints * sizeof(int));
   e = cudaMemcpy(p->meta.ptr, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     delete p;
@@ -588,6 +591,9 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   fill(p->qs);
   p->qd.group = group_d;
   p->qs.group = group_s;
+  const int* order_grouped = (const int*)(base + 4 * bi + 3 * bl + 256);
+  if (group_d < 32) p->qd.order = order_grouped;
+  if (group_s < 32) p->qs.order = order_grouped;
   p->qd.gscratch = (double*)p->scratch.ptr;
   p->qs.gscratch = (float*)p->scratch.ptr;
   *out = p;
