@@ -35,6 +35,10 @@ CONFIGS = {
                          "matrices, n~U{8..128}, A~N(0,1), lda=n, seed 0 (factored once on the "
                          "GPU before timing)",
                 count=100_000, nmin=8, nmax=128, nrhs=0),
+    "gevd": dict(workload="batched front half of the generalized symmetric eigenproblem "
+                          "(Factorization.Gevd up to its eigen-solver): B = L L^T, C = L^-1 A L^-T, "
+                          "10,000 pairs n=64, A = S + S^T, B = M M^T + 64 I, S, M ~ N(0,1), seed 0",
+                 count=10_000, n=64),
     "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
                           "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
                  count=10_000, n=32, nrhs=1),
@@ -79,6 +83,18 @@ def inv_bytes(n):
     """Read the factors and pivots, write the inverse."""
     n = n.astype(np.float64)
     return float(np.sum(16 * n ** 2 + 4 * n))
+
+
+def gevd_flops(n):
+    """Cholesky of B (n^3/3) plus two passes of n triangular solves (n^3 each)."""
+    n = n.astype(np.float64)
+    return float(np.sum(n ** 3 / 3 + 2 * n ** 3))
+
+
+def gevd_bytes(n):
+    """Read A and B, write L and C."""
+    n = n.astype(np.float64)
+    return float(np.sum(32 * n ** 2))
 
 
 def chol_flops(n, nrhs):
@@ -234,6 +250,8 @@ def make_inputs(cfg_name, rank):
         return synth.spd_batch(cfg["count"], cfg["n"], cfg["nrhs"], seed=rank)
     if cfg_name == "grad":
         return synth.rbf_batch(cfg["count"], cfg["n"], seed=rank)
+    if cfg_name == "gevd":
+        return synth.gevd_batch(cfg["count"], cfg["n"], seed=rank)
     return synth.qr_batch(cfg["count"], seed=rank)
 
 
@@ -262,6 +280,17 @@ def cpu_sample_rate(cfg_name, d, budget_s=15.0, threads=None):
 
 
 def run_cpu_sample(cfg_name, d, sample, threads, oracle):
+    if cfg_name == "gevd":
+        n = d["n"][sample].astype(np.int32)
+        sz = n.astype(np.int64) ** 2
+        off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+        a = np.concatenate([d["a"][d["a_off"][i]:d["a_off"][i] + sz[j]] for j, i in enumerate(sample)])
+        b = np.concatenate([d["b"][d["b_off"][i]:d["b_off"][i] + sz[j]] for j, i in enumerate(sample)])
+        c = np.zeros_like(a)
+        info = np.zeros(len(n), np.int32)
+        t0 = time.perf_counter()
+        oracle.gevd_front_batched(n, off, a, off, b, c, info, threads)
+        return time.perf_counter() - t0
     if cfg_name == "inv":
         n = d["n"][sample].astype(np.int32)
         sz = n.astype(np.int64) ** 2
@@ -361,6 +390,7 @@ def run_reference(args, cfg_name):
 def metric_name(cfg_name):
     return {"mixed": "mixed-precision LU+IR solves/s at 1e-12 backward error","lu": "batched FP64 LU+solve matrices/s (MatFlat-exact pivots)",
             "inv": "batched FP64 LuInverse matrices/s (MatFlat-exact)",
+            "gevd": "batched FP64 GEVD front half (Cholesky + C = L^-1 A L^-T) pairs/s (MatFlat-exact)",
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
             "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
@@ -617,7 +647,17 @@ def main():
         a = torch.empty_like(a0)
         b = torch.empty_like(b0)
         info = torch.zeros(count, dtype=torch.int32, device="cuda")
-        if cfg_name == "inv":
+        if cfg_name == "gevd":
+            plan = mf.GevdFrontBatch(d["n"], d["a_off"], d["b_off"], d["a_off"])
+            cmat = torch.empty_like(a0)
+
+            def run():
+                plan.run(a, b, cmat, info)
+            outs = [b, cmat, info]
+            flops = gevd_flops(d["n"])
+            byts = gevd_bytes(d["n"])
+            kernel_key = "gevd_front_batched_kernel"
+        elif cfg_name == "inv":
             # Factor once, untimed; the pivots travel as the step's second input.
             piv0 = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
             sign = torch.zeros(count, dtype=torch.int32, device="cuda")

@@ -210,6 +210,21 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
  * plan's nrhs (>= 1) right-hand sides. */
 MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b);
 
+/* Front half of Factorization.Gevd for a batch of pairs (Factorization.GevdCore,
+ * Factorization.Gevd.cs:330-365; the reference has no batched form): B = L L^T in place
+ * (Factorization.Cholesky), then C = L^-1 A L^-T from A's upper triangle by MatFlat's two passes of
+ * SolveTriangular(Lower, NoTrans) over the rows and then the columns of C, bit-identical.  C is
+ * what the eigen-solver of the back half takes (MatFlat runs its Svd on it; out of scope here).
+ * Pair i: A of order n[i] (<= 128) at a + a_off[i] (leading dimension lda[i], NULL: n), B at
+ * b + b_off[i] (ldb[i]), C at c + c_off[i] (leading dimension n[i]).  info: 0, or k+1 when B is not
+ * positive definite at column k (MatFlat throws "The right-hand side matrix is not positive
+ * definite."; C is then unspecified). */
+MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                        const int* lda, const int64_t* a_off, const int* ldb,
+                                        const int64_t* b_off, const int64_t* c_off);
+MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
+                                    int* info);
+
 /* Batched Factorization.LuInverse (Factorization.LuInverse.cs:123-199): replaces every matrix's
  * LU factors (as left by mfg_dgetrf_batched / Factorization.Lu) with A^-1, bit-identical to
  * MatFlat.  piv at piv + piv_off[i] is the matrix's pivot vector (read only).  info: 0, or j+1

@@ -20,6 +20,7 @@ from ._api import (  # noqa: F401
     Blas,
     CholeskyBatch,
     Factorization,
+    GevdFrontBatch,
     LuBatch,
     LuInverseBatch,
     MatFlatException,

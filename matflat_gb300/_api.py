@@ -55,6 +55,9 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
+    "mfg_plan_gevd_front_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _vp,
+                                         _vp]),
+    "mfg_dgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
@@ -483,6 +486,32 @@ class LuInverseBatch(_Batch):
     def run(self, a, piv, info):
         rc = self.ctx.lib.mfg_dgetri_batched(self.h, _dptr(a), _dptr(piv), _dptr(info))
         self.ctx.check(rc, "mfg_dgetri_batched")
+
+
+class GevdFrontBatch(_Batch):
+    """Front half of Factorization.Gevd over a batch of pairs (A, B): B becomes its Cholesky factor
+    L and C = L^-1 A L^-T (leading dimension n) is written at c_off.  info per pair: 0, or k+1 when
+    B is not positive definite ("The right-hand side matrix is not positive definite.")."""
+
+    def __init__(self, n, a_off, b_off, c_off, lda=None, ldb=None, ctx=None):
+        ctx = ctx or context()
+        self._n = _i32(n)
+        self._lda = None if lda is None else _i32(lda)
+        self._ldb = None if ldb is None else _i32(ldb)
+        self._a_off, self._b_off, self._c_off = _i64(a_off), _i64(b_off), _i64(c_off)
+        h = _vp()
+        rc = ctx.lib.mfg_plan_gevd_front_batched(
+            ctx.h, ctypes.byref(h), len(self._n), _ptr(self._n),
+            None if self._lda is None else _ptr(self._lda), _ptr(self._a_off),
+            None if self._ldb is None else _ptr(self._ldb), _ptr(self._b_off), _ptr(self._c_off))
+        if rc != 0:
+            _raise_status(rc, ["plan", "count", "n", "lda", "a_off", "ldb", "b_off", "c_off"], ctx)
+        super().__init__(ctx, h)
+        self.count = len(self._n)
+
+    def run(self, a, b, c, info):
+        rc = self.ctx.lib.mfg_dgevd_front_batched(self.h, _dptr(a), _dptr(b), _dptr(c), _dptr(info))
+        self.ctx.check(rc, "mfg_dgevd_front_batched")
 
 
 class CholeskyBatch(_Batch):

@@ -229,6 +229,44 @@ constexpr int GRAD_MAX_N = 128;
 constexpr int GRAD_SMEM_DOUBLES = GRAD_LDX * GRAD_MAX_N + 4 * GRAD_MAX_N;
 constexpr int GRAD_WARPS = 6;   // 6 x 37.9 KB per CTA, one CTA per SM
 
+// SolveTriangular(Lower, NoTrans) in MatFlat's dot form (Blas.SolveTriangular.cs:215-222) on
+// every lane's own right-hand side x (x = xs + lane, row stride GRAD_LDX):
+// x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i) for i = k0 .. n-1, the dots starting at k0 (k0 = 0: the
+// full dots; k0 > 0 only where x_0..x_{k0-1} are known to be +0 and L finite, see chol_w_lanes).
+// Rows of L are staged in shared memory (vb, 2n doubles) one ahead of use; products on the FP64
+// pipe, blocks of four pairs.
+__device__ void lanes_lower_solve(const double* L, int n, long long ld, int k0, double* x,
+                                  double* vb) {
+  stage_async(vb + (k0 & 1) * n, L + k0, k0, k0 + 1, ld);
+  stage_wait();
+  for (int i = k0; i < n; i++) {
+    const double* li = vb + (i & 1) * n;
+    if (i + 1 < n) stage_async(vb + ((i + 1) & 1) * n, L + i + 1, k0, i + 2, ld);
+    double s = 0.0;
+    int k = k0;
+    if ((i - k0) & 1) {
+      s = __dmul_rn(li[k0], x[k0 * GRAD_LDX]);
+      k = k0 + 1;
+    }
+    for (; k + 8 <= i; k += 8) {
+      double l8[8], v8[8], pr[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        l8[r] = li[k + r];
+        v8[r] = x[(k + r) * GRAD_LDX];
+      }
+      mul_block<0, 8, false>(l8, v8, pr);
+#pragma unroll
+      for (int r = 0; r < 4; r++) s = __dadd_rn(s, __dadd_rn(pr[2 * r], pr[2 * r + 1]));
+    }
+    for (; k < i; k += 2)
+      s = __dadd_rn(s, __dadd_rn(__dmul_rn(li[k], x[k * GRAD_LDX]),
+                                 __dmul_rn(li[k + 1], x[(k + 1) * GRAD_LDX])));
+    x[i * GRAD_LDX] = __ddiv_rn(__dsub_rn(x[i * GRAD_LDX], s), li[i]);
+    stage_wait();
+  }
+}
+
 // W = L^-1, column by column: MatFlat's SolveTriangular(Lower, NoTrans) (Blas.SolveTriangular.cs:
 // 215-222) applied to the columns of the identity, one lane per column (lane l of chunk j0 solves
 // column c = j0 + l): x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i).  For i < c, x_i = +0 exactly (0
@@ -251,34 +289,7 @@ __device__ void chol_w_lanes(const double* L, int n, long long ld, double* G, do
     const int k0 = nonfinite ? 0 : j0;
     double* x = xs + lane;
     for (int i = 0; i < n; i++) x[i * GRAD_LDX] = (i == t) ? 1.0 : 0.0;
-    stage_async(vb + (k0 & 1) * n, L + k0, k0, k0 + 1, ld);
-    stage_wait();
-    for (int i = k0; i < n; i++) {
-      const double* li = vb + (i & 1) * n;
-      if (i + 1 < n) stage_async(vb + ((i + 1) & 1) * n, L + i + 1, k0, i + 2, ld);
-      double s = 0.0;
-      int k = k0;
-      if ((i - k0) & 1) {
-        s = __dmul_rn(li[k0], x[k0 * GRAD_LDX]);
-        k = k0 + 1;
-      }
-      for (; k + 8 <= i; k += 8) {
-        double l8[8], v8[8], pr[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          l8[r] = li[k + r];
-          v8[r] = x[(k + r) * GRAD_LDX];
-        }
-        mul_block<0, 8, false>(l8, v8, pr);
-#pragma unroll
-        for (int r = 0; r < 4; r++) s = __dadd_rn(s, __dadd_rn(pr[2 * r], pr[2 * r + 1]));
-      }
-      for (; k < i; k += 2)
-        s = __dadd_rn(s, __dadd_rn(__dmul_rn(li[k], x[k * GRAD_LDX]),
-                                   __dmul_rn(li[k + 1], x[(k + 1) * GRAD_LDX])));
-      x[i * GRAD_LDX] = __ddiv_rn(__dsub_rn(x[i * GRAD_LDX], s), li[i]);
-      stage_wait();
-    }
+    lanes_lower_solve(L, n, ld, k0, x, vb);
     if (active) wdiag[t] = x[t * GRAD_LDX];
     for (int i = j0 + 1; i < n; i++)          // one coalesced row segment per i
       if (active && i > t) G[(long long)i * ld + t] = x[i * GRAD_LDX];
@@ -459,10 +470,15 @@ __global__ void __launch_bounds__(GRAD_WARPS * 32) chol_grad_batched_kernel(Batc
 
 static size_t grad_smem_bytes() { return sizeof(double) * GRAD_WARPS * GRAD_SMEM_DOUBLES; }
 
+__global__ void gevd_front_batched_kernel(GevdArgs p);
+
 cudaError_t init_grad_attributes() {
-  return cudaFuncSetAttribute(chol_grad_batched_kernel,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)grad_smem_bytes());
+  const cudaError_t e = cudaFuncSetAttribute(chol_grad_batched_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)grad_smem_bytes());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(gevd_front_batched_kernel,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grad_smem_bytes());
 }
 
 int grad_ctas_per_sm() {
@@ -475,6 +491,82 @@ int grad_ctas_per_sm() {
 }
 
 int grad_warps_per_cta() { return GRAD_WARPS; }
+
+// Front half of the generalized symmetric eigenproblem (Factorization.GevdCore,
+// MatFlat/Factorization.Gevd.cs:330-365) for one pair: B = L L^T in place (Cholesky), C filled
+// symmetrically from A's upper triangle, every row of C solved with L (SolveTriangular Lower/
+// NoTrans at stride n), then every column: C = L^-1 A L^-T (leading dimension n).  One lane per
+// row (first pass) and per column (second pass), each running MatFlat's sequential solve.
+__device__ void gevd_front_warp(const double* A, long long lda, double* B, long long ldb,
+                                double* C, int n, int* info_out, double* smem) {
+  const int lane = threadIdx.x & 31;
+  double* xs = smem;
+  double* vb = smem + GRAD_LDX * GRAD_MAX_N;
+  double* dsum = vb + 2 * GRAD_MAX_N;
+  const int info = potrf_group<32, true>(B, n, ldb, dsum);
+  if (info != 0) {
+    if (lane == 0) *info_out = info;
+    __syncwarp();
+    return;
+  }
+  for (long long e = lane; e < (long long)n * n; e += 32) {
+    const int j = (int)(e / n);
+    const int i = (int)(e - (long long)j * n);
+    C[(long long)j * n + i] = i <= j ? A[(long long)j * lda + i] : A[(long long)i * lda + j];
+  }
+  __syncwarp();
+  // Rows of C: lane l of a pass solves row r0 + l (lanes past n repeat row r0, not written back).
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const bool active = r0 + lane < n;
+    const int r = active ? r0 + lane : r0;
+    double* x = xs + lane;
+    for (int k = 0; k < n; k++) x[k * GRAD_LDX] = C[(long long)k * n + r];
+    lanes_lower_solve(B, n, ldb, 0, x, vb);
+    if (active)
+      for (int k = 0; k < n; k++) C[(long long)k * n + r] = x[k * GRAD_LDX];
+    __syncwarp();
+  }
+  // Columns of C: staged transposed (coalesced reads of each column).
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int nc = min(32, n - c0);
+    for (int l = 0; l < 32; l++) {
+      const double* col = C + (long long)(c0 + (l < nc ? l : 0)) * n;
+      for (int k = lane; k < n; k += 32) xs[k * GRAD_LDX + l] = col[k];
+    }
+    __syncwarp();
+    lanes_lower_solve(B, n, ldb, 0, xs + lane, vb);
+    __syncwarp();
+    for (int l = 0; l < nc; l++) {
+      double* col = C + (long long)(c0 + l) * n;
+      for (int k = lane; k < n; k += 32) col[k] = xs[k * GRAD_LDX + l];
+    }
+    __syncwarp();
+  }
+  if (lane == 0) *info_out = 0;
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(GRAD_WARPS * 32) gevd_front_batched_kernel(GevdArgs p) {
+  extern __shared__ double sm_gevd[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    gevd_front_warp(p.a + p.a_off[mat], p.lda[mat], p.b + p.b_off[mat], p.ldb[mat],
+                    p.c + p.c_off[mat], p.n[mat], p.info + mat, sm_gevd + warp * GRAD_SMEM_DOUBLES);
+  }
+}
+
+cudaError_t launch_gevd_front_batched(const GevdArgs& args, int ctas, cudaStream_t s) {
+  gevd_front_batched_kernel<<<ctas, GRAD_WARPS * 32, grad_smem_bytes(), s>>>(args);
+  return cudaGetLastError();
+}
+
+int gevd_max_n() { return GRAD_MAX_N; }
 
 cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
                                      int keep_factor, int ctas, cudaStream_t s) {

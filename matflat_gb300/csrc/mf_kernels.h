@@ -87,6 +87,25 @@ cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, l
 cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double* grad,
                                      int keep_factor, int ctas, cudaStream_t s);
 cudaError_t init_grad_attributes();
+
+// Batched GEVD front half (chol.cu): B -> L (Cholesky), C = L^-1 A L^-T (leading dimension n).
+struct GevdArgs {
+  const int* order;
+  const int* n;
+  const int* lda;
+  const int* ldb;
+  const long long* a_off;
+  const long long* b_off;
+  const long long* c_off;
+  const double* a;
+  double* b;
+  double* c;
+  int* info;
+  int count;
+  int* queue;
+};
+cudaError_t launch_gevd_front_batched(const GevdArgs& args, int ctas, cudaStream_t s);
+int gevd_max_n();
 int grad_ctas_per_sm();
 int grad_warps_per_cta();
 

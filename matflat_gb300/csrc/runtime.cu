@@ -71,7 +71,7 @@ struct mfg_ctx {
 };
 
 struct mfg_plan {
-  enum Kind { GETRF, POTRF, GEQRF, MIXED, GETRI } kind;
+  enum Kind { GETRF, POTRF, GEQRF, MIXED, GETRI, GEVD } kind;
   mfg_ctx* ctx = nullptr;
   int count = 0;
   int nrhs = 0;
@@ -81,6 +81,7 @@ struct mfg_plan {
   BatchArgs args{};
   mfg::QrBatchArgs<double> qd{};
   mfg::QrBatchArgs<float> qs{};
+  mfg::GevdArgs gv{};  // GEVD: the front half of the generalized eigenproblem
   int qr_float = 0;  // GEQRF: which precision the next launch runs
   int mx_n = 0;      // MIXED: order of every matrix
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
@@ -270,7 +271,9 @@ bool tune_env_override() {
 
 int plan_launch(mfg_plan* p, cudaStream_t s) {
   mfg_ctx* ctx = p->ctx;
-  int* queue = p->kind == mfg_plan::GEQRF ? p->qd.queue : p->args.queue;
+  int* queue = p->kind == mfg_plan::GEQRF  ? p->qd.queue
+               : p->kind == mfg_plan::GEVD ? p->gv.queue
+                                           : p->args.queue;
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
@@ -278,6 +281,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_getrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::GETRI)
     e = mfg::launch_getri_batched(p->args, p->ctas, s);
+  else if (p->kind == mfg_plan::GEVD)
+    e = mfg::launch_gevd_front_batched(p->gv, p->ctas, s);
   else if (p->kind == mfg_plan::POTRF)
     e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->qr_float)
@@ -482,6 +487,89 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   return MFG_OK;
 }
 
+
+// Plan of the batched GEVD front half: pair i is A (order n[i], leading dimension lda[i]) at
+// a_off[i], B (ldb[i]) at b_off[i], and C (leading dimension n[i]) at c_off[i].
+int plan_create_gevd(mfg_ctx* ctx, mfg_plan** out, int count, const int* n, const int* lda,
+                     const int64_t* a_off, const int* ldb, const int64_t* b_off,
+                     const int64_t* c_off) {
+  if (!ctx) return -1;
+  if (!out) return fail(ctx, -2, "plan output pointer is null");
+  *out = nullptr;
+  if (count < 0) return fail(ctx, -3, "count must be >= 0");
+  if (count > 0 && !n) return fail(ctx, -4, "n is null");
+  for (int i = 0; i < count; i++) {
+    if (n[i] < 1)
+      return fail(ctx, -4, "n[%d] = %d: The order of the matrix must be greater than or equal "
+                           "to one.", i, n[i]);
+    if (n[i] > mfg::gevd_max_n())
+      return fail(ctx, -4, "n[%d] = %d: the batched GEVD front half supports orders up to %d", i,
+                  n[i], mfg::gevd_max_n());
+    if (lda && lda[i] < n[i])
+      return fail(ctx, -5, "lda[%d]: The leading dimension must be greater than or equal to the "
+                           "order of the matrix.", i);
+    if (ldb && ldb[i] < n[i])
+      return fail(ctx, -7, "ldb[%d]: The leading dimension must be greater than or equal to the "
+                           "order of the matrix.", i);
+  }
+  if (count > 0 && !a_off) return fail(ctx, -6, "a_off is null");
+  if (count > 0 && !b_off) return fail(ctx, -8, "b_off is null");
+  if (count > 0 && !c_off) return fail(ctx, -9, "c_off is null");
+  for (int i = 0; i < count; i++) {
+    if (a_off[i] < 0) return fail(ctx, -6, "a_off[%d] < 0", i);
+    if (b_off[i] < 0) return fail(ctx, -8, "b_off[%d] < 0", i);
+    if (c_off[i] < 0) return fail(ctx, -9, "c_off[%d] < 0", i);
+  }
+  mfg_plan* p = new mfg_plan();
+  p->kind = mfg_plan::GEVD;
+  p->ctx = ctx;
+  p->count = count;
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  const size_t ints = (size_t)count;
+  const size_t bi = ((ints * sizeof(int) + 255) / 256) * 256;
+  const size_t bl = ((ints * sizeof(long long) + 255) / 256) * 256;
+  const size_t total = 4 * bi + 3 * bl + 256;
+  cudaError_t e = p->meta.reserve(total);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMalloc(plan descriptors)");
+  }
+  std::vector<char> host(total, 0);
+  std::memcpy(host.data(), order.data(), ints * sizeof(int));
+  std::memcpy(host.data() + bi, n, ints * sizeof(int));
+  std::memcpy(host.data() + 2 * bi, lda ? lda : n, ints * sizeof(int));
+  std::memcpy(host.data() + 3 * bi, ldb ? ldb : n, ints * sizeof(int));
+  for (size_t i = 0; i < ints; i++) {
+    ((long long*)(host.data() + 4 * bi))[i] = a_off[i];
+    ((long long*)(host.data() + 4 * bi + bl))[i] = b_off[i];
+    ((long long*)(host.data() + 4 * bi + 2 * bl))[i] = c_off[i];
+  }
+  e = cudaMemcpy(p->meta.ptr, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
+  }
+  // Same shape as the gradient kernel: one CTA of six warps per SM (shared-memory bound).
+  p->warps = mfg::grad_warps_per_cta();
+  long long ctas = (long long)ctx->sm_count * mfg::grad_ctas_per_sm();
+  ctas = std::min<long long>(ctas, ((long long)count + p->warps - 1) / p->warps);
+  p->ctas = (int)std::max<long long>(1, ctas);
+  char* base = (char*)p->meta.ptr;
+  mfg::GevdArgs& g = p->gv;
+  g.order = (const int*)base;
+  g.n = (const int*)(base + bi);
+  g.lda = (const int*)(base + 2 * bi);
+  g.ldb = (const int*)(base + 3 * bi);
+  g.a_off = (const long long*)(base + 4 * bi);
+  g.b_off = (const long long*)(base + 4 * bi + bl);
+  g.c_off = (const long long*)(base + 4 * bi + 2 * bl);
+  g.count = count;
+  g.queue = (int*)(base + 4 * bi + 3 * bl);
+  *out = p;
+  return MFG_OK;
+}
 
 int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const int* n,
                    const int* lda, const int64_t* a_off, const int64_t* rdiag_off, int nrhs,
@@ -1462,6 +1550,30 @@ MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* i
   plan->args.sign = nullptr;
   plan->args.info = info;
   return plan_execute(plan, a, piv, info, nullptr, nullptr);
+}
+
+MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
+                                        const int* lda, const int64_t* a_off, const int* ldb,
+                                        const int64_t* b_off, const int64_t* c_off) {
+  return plan_create_gevd(ctx, plan, count, n, lda, a_off, ldb, b_off, c_off);
+}
+
+MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
+                                    int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEVD) return fail(ctx, -1, "plan is not a gevd plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!b) return fail(ctx, -3, "b is null");
+    if (!c) return fail(ctx, -4, "c is null");
+    if (!info) return fail(ctx, -5, "info is null");
+  }
+  plan->gv.a = a;
+  plan->gv.b = b;
+  plan->gv.c = c;
+  plan->gv.info = info;
+  return plan_execute(plan, a, b, c, info, nullptr);
 }
 
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {

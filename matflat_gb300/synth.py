@@ -79,6 +79,20 @@ def spd_batch(count, n=32, nrhs=1, seed=0):
     return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=b, nrhs=nrhs)
 
 
+def gevd_batch(count, n=64, seed=0):
+    """GEVD front-half workload: A symmetric (A = S + S^T, S ~ N(0,1)) and B = M M^T + n I with
+    M ~ N(0,1), column-major pairs of order n."""
+    ns = np.full(count, n, np.int32)
+    s = normal(count * n * n, seed, stream=8).reshape(count, n, n)
+    a = np.ascontiguousarray(s + np.transpose(s, (0, 2, 1))).reshape(-1)
+    m = normal(count * n * n, seed, stream=9).reshape(count, n, n)
+    b = np.matmul(m, np.transpose(m, (0, 2, 1)))
+    b += n * np.eye(n)[None, :, :]
+    b = np.ascontiguousarray(b).reshape(-1)          # symmetric: row- and column-major agree
+    off, _ = packed_offsets(ns, ns)
+    return dict(n=ns, a_off=off, a=a, b_off=off, b=b, nrhs=0)
+
+
 def qr_batch(count, mmin=64, mmax=512, nmin=16, nmax=64, nrhs=1, seed=0):
     """QR least-squares workload: m ~ U{mmin..mmax}, n ~ U{nmin..nmax} (n <= m), N(0,1) data."""
     m = (np.floor(uniform(count, seed, stream=6) * (mmax - mmin + 1)) + mmin).astype(np.int32)

@@ -942,6 +942,27 @@ int orc_dchol_grad(int n, double* k, int lda, double* y, double* loss, double* g
   return 0;
 }
 
+// Front half of the generalized eigenproblem, double (Factorization.GevdCore, Factorization.Gevd.cs:
+// 330-365): Cholesky(B) in place (:335-343), C filled symmetrically from A's upper triangle
+// (:346-357), every row of C solved with SolveTriangular(Lower, NoTrans) at stride n (:358-361),
+// then every column (:362-365): C = L^-1 A L^-T, leading dimension n.  Returns 0, or Cholesky's
+// k+1 (MatFlat throws "The right-hand side matrix is not positive definite." there).
+int orc_dgevd_front(int n, const double* a, int lda, double* b, int ldb, double* c) {
+  const int info = orc_dcholesky(n, b, ldb);
+  if (info != 0) return info;
+  for (int j = 0; j < n; j++) {
+    const double* aColj = a + (long)lda * j;
+    for (int i = 0; i < j; i++) {
+      c[(long)n * j + i] = aColj[i];
+      c[(long)n * i + j] = aColj[i];
+    }
+    c[(long)n * j + j] = aColj[j];
+  }
+  for (int i = 0; i < n; i++) orc_dtrsv(LOWER, NOTRANS, n, b, ldb, c + i, n);
+  for (int i = 0; i < n; i++) orc_dtrsv(LOWER, NOTRANS, n, b, ldb, c + (long)n * i, 1);
+  return 0;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Batched drivers over std::thread.  Matrices are packed: matrix i starts at a + a_off[i]
 // (elements), has order n[i] and leading dimension n[i]; vectors start at b + b_off[i].
@@ -1015,6 +1036,15 @@ void orc_dlu_inverse_batched(long count, const int* n, const int64_t* a_off, dou
       if (ai[(long)ni * j + j] == 0.0) bad = j + 1;
     info[i] = bad;
     if (!bad) orc_dlu_inverse(ni, ai, ni, piv + piv_off[i]);
+  });
+}
+
+// Batched GEVD front half (lda = ldb = n): pair i is A at a + a_off[i], B at b + b_off[i], and C
+// is written at c + a_off[i].
+void orc_dgevd_front_batched(long count, const int* n, const int64_t* a_off, const double* a,
+                             const int64_t* b_off, double* b, double* c, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    info[i] = orc_dgevd_front(n[i], a + a_off[i], n[i], b + b_off[i], n[i], c + a_off[i]);
   });
 }
 

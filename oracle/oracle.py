@@ -59,6 +59,8 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_dgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
+            "orc_dgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
             "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
             "orc_dchol_grad": (_I, [_I, _d, _I, _d, _d, _d]),
             "orc_dchol_grad_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _d, _i, _I]),
@@ -163,6 +165,18 @@ def lu_inverse_batched(n, a_off, a, piv_off, piv, info, nthreads=1):
     """Factorization.LuInverse per matrix (lda = n); info = j+1 for the first zero U(j,j)."""
     lib().orc_dlu_inverse_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
                                   _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int),
+                                  _p(info, ctypes.c_int), nthreads)
+
+
+def gevd_front(n, a, lda, b, ldb, c):
+    """Factorization.GevdCore's front half (Factorization.Gevd.cs:330-365): B -> L, C = L^-1 A L^-T
+    (leading dimension n); returns 0 or Cholesky's k+1."""
+    return lib().orc_dgevd_front(n, _fp(a), lda, _fp(b), ldb, _fp(c))
+
+
+def gevd_front_batched(n, a_off, a, b_off, b, c, info, nthreads=1):
+    lib().orc_dgevd_front_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+                                  _p(b_off, ctypes.c_int64), _fp(b), _fp(c),
                                   _p(info, ctypes.c_int), nthreads)
 
 
