@@ -210,6 +210,28 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
  * plan's nrhs (>= 1) right-hand sides. */
 MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b);
 
+/* Strided batches of MatFlat's vector building blocks (device pointers, asynchronous on the
+ * context's stream; item b of every operand at base + b*stride), in MatFlat's arithmetic:
+ *   Blas.MulMatVec (Blas.MulMatVec.cs:138-236): y = A x (NoTrans: y_i = Dot(n, A(i,:), x)) or
+ *     A^T x (Trans: y_j = Dot(m, A(:,j), x)); same checks and messages (a or x aliasing y is
+ *     MFG_ERR_INPLACE);
+ *   Blas.Dot (Blas.VectorOperations.cs:143-174) and Blas.L2Norm (:50-60: Math.Sqrt of the same
+ *     tree over x*x): one result per item;
+ *   Blas.Outer (:292-334): a(i,j) = y_j * x_i. */
+MFG_API int mfg_dgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const double* a,
+                                      int lda, int64_t stride_a, const double* x, int incx,
+                                      int64_t stride_x, double* y, int incy, int64_t stride_y,
+                                      int count);
+MFG_API int mfg_ddot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* result, int count);
+MFG_API int mfg_dnrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                      int64_t stride_x, double* result, int count);
+MFG_API int mfg_dger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                     int count);
+
 /* Front half of Factorization.Gevd for a batch of pairs (Factorization.GevdCore,
  * Factorization.Gevd.cs:330-365; the reference has no batched form): B = L L^T in place
  * (Factorization.Cholesky), then C = L^-1 A L^-T from A's upper triangle by MatFlat's two passes of

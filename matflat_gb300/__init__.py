@@ -27,6 +27,7 @@ from ._api import (  # noqa: F401
     MatrixFactorizationException,
     MixedSolveBatch,
     QrBatch,
+    StridedBlas,
     Transpose,
     Uplo,
     context,

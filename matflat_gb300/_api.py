@@ -55,6 +55,13 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
+    "mfg_dgemv_strided_batched": (_I, [_vp, _I, _I, _I, _vp, _I, ctypes.c_int64, _vp, _I,
+                                       ctypes.c_int64, _vp, _I, ctypes.c_int64, _I]),
+    "mfg_ddot_strided_batched": (_I, [_vp, _I, _vp, _I, ctypes.c_int64, _vp, _I, ctypes.c_int64,
+                                      _vp, _I]),
+    "mfg_dnrm2_strided_batched": (_I, [_vp, _I, _vp, _I, ctypes.c_int64, _vp, _I]),
+    "mfg_dger_strided_batched": (_I, [_vp, _I, _I, _vp, _I, ctypes.c_int64, _vp, _I,
+                                      ctypes.c_int64, _vp, _I, ctypes.c_int64, _I]),
     "mfg_plan_gevd_front_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "mfg_dgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
@@ -458,6 +465,48 @@ class LuBatch(_Batch):
         """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b)."""
         rc = self.ctx.lib.mfg_dgetrs_batched(self.h, _dptr(a), _dptr(piv), _dptr(b))
         self.ctx.check(rc, "mfg_dgetrs_batched")
+
+
+class StridedBlas:
+    """Strided batches of Blas.MulMatVec / Dot / L2Norm / Outer on device buffers (torch CUDA
+    tensors or device pointers); item b of each operand starts at base + b * stride."""
+
+    @staticmethod
+    def MulMatVec(trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy, stride_y, count,
+                  ctx=None):
+        ctx = ctx or context()
+        rc = ctx.lib.mfg_dgemv_strided_batched(ctx.h, trans, m, n, _dptr(a), lda, stride_a,
+                                               _dptr(x), incx, stride_x, _dptr(y), incy,
+                                               stride_y, count)
+        if rc != 0:
+            _raise_status(rc, ["trans", "m", "n", "a", "lda", "stride_a", "x", "incx",
+                               "stride_x", "y", "incy", "stride_y", "count"], ctx)
+
+    @staticmethod
+    def Dot(n, x, incx, stride_x, y, incy, stride_y, result, count, ctx=None):
+        ctx = ctx or context()
+        rc = ctx.lib.mfg_ddot_strided_batched(ctx.h, n, _dptr(x), incx, stride_x, _dptr(y), incy,
+                                              stride_y, _dptr(result), count)
+        if rc != 0:
+            _raise_status(rc, ["n", "x", "incx", "stride_x", "y", "incy", "stride_y", "result",
+                               "count"], ctx)
+
+    @staticmethod
+    def L2Norm(n, x, incx, stride_x, result, count, ctx=None):
+        ctx = ctx or context()
+        rc = ctx.lib.mfg_dnrm2_strided_batched(ctx.h, n, _dptr(x), incx, stride_x, _dptr(result),
+                                               count)
+        if rc != 0:
+            _raise_status(rc, ["n", "x", "incx", "stride_x", "result", "count"], ctx)
+
+    @staticmethod
+    def Outer(m, n, x, incx, stride_x, y, incy, stride_y, a, lda, stride_a, count, ctx=None):
+        ctx = ctx or context()
+        rc = ctx.lib.mfg_dger_strided_batched(ctx.h, m, n, _dptr(x), incx, stride_x, _dptr(y),
+                                              incy, stride_y, _dptr(a), lda, stride_a, count)
+        if rc != 0:
+            _raise_status(rc, ["m", "n", "x", "incx", "stride_x", "y", "incy", "stride_y", "a",
+                               "lda", "stride_a", "count"], ctx)
 
 
 class LuInverseBatch(_Batch):

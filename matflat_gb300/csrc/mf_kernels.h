@@ -109,6 +109,17 @@ int gevd_max_n();
 int grad_ctas_per_sm();
 int grad_warps_per_cta();
 
+// Strided batches of MulMatVec / Dot / L2Norm / Outer (vec.cu).
+cudaError_t launch_gemv_strided(int trans, int m, int n, const double* a, int lda, long long sa,
+                                const double* x, int incx, long long sx, double* y, int incy,
+                                long long sy, int count, cudaStream_t s);
+cudaError_t launch_dot_strided(int n, const double* x, int incx, long long sx, const double* y,
+                               int incy, long long sy, double* out, int count, int norm,
+                               cudaStream_t s);
+cudaError_t launch_ger_strided(int m, int n, const double* x, int incx, long long sx,
+                               const double* y, int incy, long long sy, double* a, int lda,
+                               long long sa, int count, cudaStream_t s);
+
 // Fills args.a (and args.b when nrhs > 0) with the autotuner's synthetic batch (tune.cu).
 cudaError_t launch_tune_fill(const BatchArgs& args, int spd, cudaStream_t s);
 

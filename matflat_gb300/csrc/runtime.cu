@@ -1552,6 +1552,81 @@ MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* i
   return plan_execute(plan, a, piv, info, nullptr, nullptr);
 }
 
+MFG_API int mfg_dgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const double* a,
+                                      int lda, int64_t stride_a, const double* x, int incx,
+                                      int64_t stride_x, double* y, int incy, int64_t stride_y,
+                                      int count) {
+  if (!ctx) return -1;
+  // Blas.MulMatVec's checks (Blas.MulMatVec.cs:140-183).
+  if (m <= 0) return fail(ctx, -3, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -4, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -5, "a is null");
+  if (lda < m)
+    return fail(ctx, -6,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!x) return fail(ctx, -8, "x is null");
+  if (incx <= 0) return fail(ctx, -9, "The value must be greater than or equal to one.");
+  if (!y) return fail(ctx, -11, "y is null");
+  if (incy <= 0) return fail(ctx, -12, "The value must be greater than or equal to one.");
+  if ((const void*)a == (const void*)y || (const void*)x == (const void*)y)
+    return fail(ctx, MFG_ERR_INPLACE, "In-place operation is not supported.");
+  if (trans != MFG_NOTRANS && trans != MFG_TRANS) return fail(ctx, -2, "Invalid enum value.");
+  if (count < 0) return fail(ctx, -14, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_gemv_strided(trans, m, n, a, lda, stride_a, x, incx, stride_x, y,
+                                         incy, stride_y, count, ctx->stream));
+  return MFG_OK;
+}
+
+MFG_API int mfg_ddot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* result, int count) {
+  if (!ctx) return -1;
+  if (n <= 0) return fail(ctx, -2, "The length of the vector must be greater than or equal to one.");
+  if (!x) return fail(ctx, -3, "x is null");
+  if (incx <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
+  if (!y) return fail(ctx, -6, "y is null");
+  if (incy <= 0) return fail(ctx, -7, "The value must be greater than or equal to one.");
+  if (!result) return fail(ctx, -9, "result is null");
+  if (count < 0) return fail(ctx, -10, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_dot_strided(n, x, incx, stride_x, y, incy, stride_y, result, count,
+                                        0, ctx->stream));
+  return MFG_OK;
+}
+
+MFG_API int mfg_dnrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                      int64_t stride_x, double* result, int count) {
+  if (!ctx) return -1;
+  if (n <= 0) return fail(ctx, -2, "The length of the vector must be greater than or equal to one.");
+  if (!x) return fail(ctx, -3, "x is null");
+  if (incx <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
+  if (!result) return fail(ctx, -6, "result is null");
+  if (count < 0) return fail(ctx, -7, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_dot_strided(n, x, incx, stride_x, x, incx, stride_x, result, count,
+                                        1, ctx->stream));
+  return MFG_OK;
+}
+
+MFG_API int mfg_dger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                     int count) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!x) return fail(ctx, -4, "x is null");
+  if (incx <= 0) return fail(ctx, -5, "The value must be greater than or equal to one.");
+  if (!y) return fail(ctx, -7, "y is null");
+  if (incy <= 0) return fail(ctx, -8, "The value must be greater than or equal to one.");
+  if (!a) return fail(ctx, -10, "a is null");
+  if (lda < m)
+    return fail(ctx, -11,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (count < 0) return fail(ctx, -13, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_ger_strided(m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
+                                        stride_a, count, ctx->stream));
+  return MFG_OK;
+}
+
 MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                         const int* lda, const int64_t* a_off, const int* ldb,
                                         const int64_t* b_off, const int64_t* c_off) {

@@ -840,6 +840,21 @@ int orc_sgemv(int trans, int m, int n, const float* a, int lda, const float* x, 
   return 0;
 }
 
+// Blas.Dot / Blas.L2Norm / Blas.Outer, double (Blas.VectorOperations.cs:143-174, :50-60,
+// :292-334): Internals.Dot's tree; L2Norm = Math.Sqrt of the same tree over x*x
+// (Internals.Norm, Internals.cs:435-460); Outer a(i,j) = y_j * x_i.
+double orc_ddot(int n, const double* x, int incx, const double* y, int incy) {
+  return dot_d(n, x, incx, y, incy);
+}
+double orc_dnrm2(int n, const double* x, int incx) { return std::sqrt(dot_d(n, x, incx, x, incx)); }
+void orc_dger(int m, int n, const double* x, int incx, const double* y, int incy, double* a,
+              int lda) {
+  for (int j = 0; j < n; j++) {
+    const double t = y[(long)incy * j];
+    for (int i = 0; i < m; i++) a[(long)lda * j + i] = t * x[(long)incx * i];
+  }
+}
+
 // =============================================================================================
 // Factorization.LuInverse (Factorization.LuInverse.cs:123-199): A^-1 from the LU factors.
 // Returns 0, or 1 when a diagonal entry of U is zero (MatFlat throws there, before writing).

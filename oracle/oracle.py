@@ -59,6 +59,9 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_ddot": (ctypes.c_double, [_I, _d, _I, _d, _I]),
+            "orc_dnrm2": (ctypes.c_double, [_I, _d, _I]),
+            "orc_dger": (None, [_I, _I, _d, _I, _d, _I, _d, _I]),
             "orc_dgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
             "orc_dgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
             "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
@@ -132,6 +135,21 @@ def gemm(transa, transb, m, n, k, a, lda, b, ldb, c, ldc):
 def gemv(trans, m, n, a, lda, x, incx, y, incy):
     """Blas.MulMatVec (Blas.MulMatVec.cs:138-236), double."""
     return lib().orc_dgemv(trans, m, n, _fp(a), lda, _fp(x), incx, _fp(y), incy)
+
+
+def dot(n, x, incx, y, incy):
+    """Blas.Dot (Blas.VectorOperations.cs:143-174), double."""
+    return lib().orc_ddot(n, _fp(x), incx, _fp(y), incy)
+
+
+def nrm2(n, x, incx):
+    """Blas.L2Norm (Blas.VectorOperations.cs:50-60), double."""
+    return lib().orc_dnrm2(n, _fp(x), incx)
+
+
+def ger(m, n, x, incx, y, incy, a, lda):
+    """Blas.Outer (Blas.VectorOperations.cs:292-334), double: a(i,j) = y_j * x_i."""
+    lib().orc_dger(m, n, _fp(x), incx, _fp(y), incy, _fp(a), lda)
 
 
 def lu_inverse(n, a, lda, piv):

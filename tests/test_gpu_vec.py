@@ -1,0 +1,75 @@
+"""Strided batches of MulMatVec / Dot / L2Norm / Outer against the oracle, bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests.test_gpu_parity import _dev, _host, assert_bits
+
+pytestmark = pytest.mark.gpu
+
+NT, T = 111, 112
+
+
+@pytest.mark.parametrize("trans", [NT, T])
+def test_gemv_strided(mf, trans):
+    import torch
+    rng = np.random.default_rng(81)
+    m, n, lda, incx, incy, count = 37, 29, 41, 2, 3, 50
+    sa = lda * n + 5
+    lx = (n if trans == NT else m)
+    ly = (m if trans == NT else n)
+    sx, sy = incx * lx + 1, incy * ly + 2
+    a = rng.standard_normal(sa * count)
+    x = rng.standard_normal(sx * count)
+    y0 = rng.standard_normal(sy * count)
+    exp = y0.copy()
+    for b in range(count):
+        oracle.gemv(trans, m, n, a[b * sa:], lda, x[b * sx:], incx, exp[b * sy:], incy)
+    dy = _dev(y0)
+    mf.StridedBlas.MulMatVec(trans, m, n, _dev(a), lda, sa, _dev(x), incx, sx, dy, incy, sy, count)
+    mf.context().synchronize()
+    assert_bits(_host(dy), exp)
+
+
+def test_dot_nrm2_strided(mf):
+    import torch
+    rng = np.random.default_rng(82)
+    for n, inc in ((77, 1), (64, 3), (1, 1)):
+        count = 1000
+        s = n * inc + 7
+        x = rng.standard_normal(s * count)
+        y = rng.standard_normal(s * count)
+        d_out = torch.zeros(count, dtype=torch.float64, device="cuda")
+        mf.StridedBlas.Dot(n, _dev(x), inc, s, _dev(y), inc, s, d_out, count)
+        n_out = torch.zeros(count, dtype=torch.float64, device="cuda")
+        mf.StridedBlas.L2Norm(n, _dev(x), inc, s, n_out, count)
+        mf.context().synchronize()
+        ed = np.array([oracle.dot(n, x[b * s:], inc, y[b * s:], inc) for b in range(count)])
+        en = np.array([oracle.nrm2(n, x[b * s:], inc) for b in range(count)])
+        assert_bits(_host(d_out), ed)
+        assert_bits(_host(n_out), en)
+
+
+def test_ger_strided(mf):
+    rng = np.random.default_rng(83)
+    m, n, lda, count = 13, 9, 15, 20
+    sx, sy, sa = 2 * m, n + 3, lda * n + 1
+    x = rng.standard_normal(sx * count)
+    y = rng.standard_normal(sy * count)
+    a0 = rng.standard_normal(sa * count)
+    exp = a0.copy()
+    for b in range(count):
+        oracle.ger(m, n, x[b * sx:], 2, y[b * sy:], 1, exp[b * sa:], lda)
+    da = _dev(a0)
+    mf.StridedBlas.Outer(m, n, _dev(x), 2, sx, _dev(y), 1, sy, da, lda, sa, count)
+    mf.context().synchronize()
+    assert_bits(_host(da), exp)
+
+
+def test_gemv_in_place_rejected(mf):
+    import torch
+    z = torch.zeros(100, dtype=torch.float64, device="cuda")
+    with pytest.raises(mf.ArgumentException):
+        mf.StridedBlas.MulMatVec(NT, 3, 3, z, 3, 9, z, 1, 3, z, 1, 3, 1)
+    with pytest.raises(mf.ArgumentException):
+        mf.StridedBlas.MulMatVec(NT, 3, 3, z, 2, 9, z[50:], 1, 3, z[80:], 1, 3, 1)
