@@ -757,23 +757,62 @@ def main():
     value = world * count * args.steps / (total_ms / 1e3)
 
     # ---- end to end through the C ABI from pinned host memory -------------------------------
+    # The host-buffer entry points (mfg_*_batched_host): copies and compute pipelined over chunks
+    # of the batch inside one synchronous call, timed by the host clock.  The calls work in
+    # place, so the input arrays are restored from pristine pinned copies before each (untimed).
     e2e = None
-    if not args.no_e2e and cfg_name == "lu":
-        # The host-buffer entry point (mfg_dgetrf_batched_host): copies and compute pipelined
-        # over chunks inside one synchronous call, timed by the host clock.  The call is in place,
-        # so the host arrays are restored from a pristine pinned copy before each (untimed).
-        io = [torch.empty_like(a_host).pin_memory(), torch.empty_like(b_host).pin_memory()]
-        piv_h = torch.zeros(d["piv_total"], dtype=torch.int32).pin_memory()
-        sign_h = torch.zeros(count, dtype=torch.int32).pin_memory()
-        info_h = torch.zeros(count, dtype=torch.int32).pin_memory()
+    if not args.no_e2e:
+        def pinned_like(t, dtype=None):
+            return torch.empty(t.shape, dtype=dtype or t.dtype).pin_memory()
+
+        ins = [a_host, b_host]                       # pristine inputs
+        io = [pinned_like(a_host), pinned_like(b_host)]
+        if cfg_name == "lu":
+            extra = [torch.zeros(d["piv_total"], dtype=torch.int32).pin_memory(),
+                     torch.zeros(count, dtype=torch.int32).pin_memory(),
+                     torch.zeros(count, dtype=torch.int32).pin_memory()]
+            call = lambda: plan.run_host(io[0], extra[0], io[1], extra[1], extra[2])
+            up = [io[0], io[1]]
+            down = [io[0], io[1]] + extra
+        elif cfg_name == "inv":
+            extra = [torch.zeros(count, dtype=torch.int32).pin_memory()]
+            io[1] = b_host                           # the pivots: read only
+            call = lambda: plan.run_host(io[0], io[1], extra[0])
+            up = [io[0], io[1]]
+            down = [io[0]] + extra
+        elif cfg_name == "chol":
+            extra = [torch.zeros(count, dtype=torch.int32).pin_memory()]
+            call = lambda: plan.run_host(io[0], io[1], extra[0])
+            up = [io[0], io[1]]
+            down = [io[0], io[1]] + extra
+        elif cfg_name == "grad":
+            extra = [torch.zeros(count, dtype=torch.float64).pin_memory(), pinned_like(a_host),
+                     torch.zeros(count, dtype=torch.int32).pin_memory()]
+            call = lambda: plan.loss_and_grad_host(io[0], io[1], extra[0], extra[1], extra[2],
+                                                   keep_factor=True)
+            up = [io[0], io[1]]
+            down = [io[0], io[1]] + extra
+        elif cfg_name == "gevd":
+            extra = [pinned_like(a_host), torch.zeros(count, dtype=torch.int32).pin_memory()]
+            io[0] = a_host                           # A: read only
+            call = lambda: plan.run_host(io[0], io[1], extra[0], extra[1])
+            up = [io[0], io[1]]
+            down = [io[1]] + extra
+        else:                                        # qr, qr32
+            extra = [pinned_like(outs_host[2])]
+            single = cfg_name == "qr32"
+            call = lambda: plan.run_host(io[0], extra[0], io[1], single=single)
+            up = [io[0], io[1]]
+            down = [io[0], io[1]] + extra
         times = []
         for it in range(2 + args.steps):
-            io[0].copy_(a_host)
-            io[1].copy_(b_host)
+            for src, dst in zip(ins, io):
+                if dst is not src:
+                    dst.copy_(src)
             torch.cuda.synchronize()
             barrier()
             t_0 = time.perf_counter()
-            plan.run_host(io[0], piv_h, io[1], sign_h, info_h)
+            call()
             t_1 = time.perf_counter()
             if it >= 2:
                 times.append(t_1 - t_0)
@@ -782,45 +821,12 @@ def main():
             tt = torch.tensor([e2e_ms], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             e2e_ms = float(tt.item())
-        h2d = a_host.numel() * 8 + b_host.numel() * 8
-        d2h = h2d + piv_h.numel() * 4 + 2 * count * 4
+        nbytes = lambda ts: int(sum(t.numel() * t.element_size() for t in ts))
         e2e = {"value": world * count / (e2e_ms / 1e3), "unit": "matrices/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "h2d_bytes_per_step": nbytes(up), "d2h_bytes_per_step": nbytes(down),
                "ms_per_step": e2e_ms,
-               "path": "mfg_dgetrf_batched_host on page-locked host arrays (copies pipelined "
+               "path": "host-buffer entry point on page-locked host arrays (copies pipelined "
                        "with compute over chunks of the batch), host wall clock per call"}
-    elif not args.no_e2e:
-        h2d = a_host.numel() * a_host.element_size() + b_host.numel() * b_host.element_size()
-        d2h = sum(o.numel() * o.element_size() for o in outs)
-        with torch.cuda.stream(stream):
-            for _ in range(2):
-                a.copy_(a_host, non_blocking=True)
-                b.copy_(b_host, non_blocking=True)
-                run()
-                for o, oh in zip(outs, outs_host):
-                    oh.copy_(o, non_blocking=True)
-            stream.synchronize()
-            barrier()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
-                a.copy_(a_host, non_blocking=True)
-                b.copy_(b_host, non_blocking=True)
-                run()
-                for o, oh in zip(outs, outs_host):
-                    oh.copy_(o, non_blocking=True)
-            e1.record(stream)
-            stream.synchronize()
-            barrier()
-        e2e_ms = e0.elapsed_time(e1)
-        if world > 1:
-            tt = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_ms = float(tt.item())
-        e2e = {"value": world * count * args.steps / (e2e_ms / 1e3), "unit": "matrices/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": e2e_ms / args.steps}
 
     # ---- roofline of the dominant kernel -----------------------------------------------------
     fp64_peak = measure_fp64_peak(torch)

@@ -191,6 +191,17 @@ MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, i
  * The first call allocates device mirrors of the arrays and per-chunk plans (kept by the plan). */
 MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                     int* info);
+/* The same pipelined host-buffer form of the other batched operations (arguments as in their
+ * device-buffer forms; every array is a HOST array, synchronous, bit-identical results). */
+MFG_API int mfg_dpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info);
+MFG_API int mfg_dgetri_batched_host(mfg_plan* plan, double* a, const int* piv, int* info);
+MFG_API int mfg_dgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b);
+MFG_API int mfg_sgeqrf_batched_host(mfg_plan* plan, float* a, float* rdiag, float* b);
+MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
+                                         int* info);
+MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k, double* y,
+                                                     double* loss, double* grad, int* info,
+                                                     int keep_factor);
 /* Solve only, with factors and pivots already in a and piv (from mfg_dgetrf_batched or
  * Factorization.Lu): b' = P b, the unit-lower solve (LuInverse idiom, Factorization.LuInverse.cs:
  * 174-182) and the upper solve (Blas.SolveTriangular.cs:191-199), for the plan's nrhs (>= 1)

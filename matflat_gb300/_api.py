@@ -66,6 +66,12 @@ _SIGS = {
                                          _vp]),
     "mfg_dgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_dpotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dgetri_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dgeqrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_sgeqrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_dgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
+    "mfg_dpotrf_logdet_solve_grad_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
     "mfg_dgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -536,6 +542,11 @@ class LuInverseBatch(_Batch):
         rc = self.ctx.lib.mfg_dgetri_batched(self.h, _dptr(a), _dptr(piv), _dptr(info))
         self.ctx.check(rc, "mfg_dgetri_batched")
 
+    def run_host(self, a, piv, info):
+        """The inverse on host arrays, copies pipelined with compute.  Synchronous."""
+        rc = self.ctx.lib.mfg_dgetri_batched_host(self.h, _hptr(a), _hptr(piv), _hptr(info))
+        self.ctx.check(rc, "mfg_dgetri_batched_host")
+
 
 class GevdFrontBatch(_Batch):
     """Front half of Factorization.Gevd over a batch of pairs (A, B): B becomes its Cholesky factor
@@ -562,6 +573,12 @@ class GevdFrontBatch(_Batch):
         rc = self.ctx.lib.mfg_dgevd_front_batched(self.h, _dptr(a), _dptr(b), _dptr(c), _dptr(info))
         self.ctx.check(rc, "mfg_dgevd_front_batched")
 
+    def run_host(self, a, b, c, info):
+        """The front half on host arrays, copies pipelined with compute.  Synchronous."""
+        rc = self.ctx.lib.mfg_dgevd_front_batched_host(self.h, _hptr(a), _hptr(b), _hptr(c),
+                                                       _hptr(info))
+        self.ctx.check(rc, "mfg_dgevd_front_batched_host")
+
 
 class CholeskyBatch(_Batch):
     """Batched Factorization.Cholesky (+ L y = b, L^T x = y) over matrices of uneven n."""
@@ -585,6 +602,18 @@ class CholeskyBatch(_Batch):
     def run(self, a, b, info):
         rc = self.ctx.lib.mfg_dpotrf_batched(self.h, _dptr(a), _dptr(b), _dptr(info))
         self.ctx.check(rc, "mfg_dpotrf_batched")
+
+    def run_host(self, a, b, info):
+        """Factor + solve on host arrays, copies pipelined with compute.  Synchronous."""
+        rc = self.ctx.lib.mfg_dpotrf_batched_host(self.h, _hptr(a), _hptr(b), _hptr(info))
+        self.ctx.check(rc, "mfg_dpotrf_batched_host")
+
+    def loss_and_grad_host(self, k, y, loss, grad, info, keep_factor=True):
+        """loss_and_grad on host arrays, copies pipelined with compute.  Synchronous."""
+        rc = self.ctx.lib.mfg_dpotrf_logdet_solve_grad_batched_host(
+            self.h, _hptr(k), _hptr(y), _hptr(loss), _hptr(grad), _hptr(info),
+            1 if keep_factor else 0)
+        self.ctx.check(rc, "mfg_dpotrf_logdet_solve_grad_batched_host")
 
     def solve(self, a, b):
         """Solves with Cholesky factors already in a (the plan's nrhs columns of b)."""
@@ -629,6 +658,12 @@ class QrBatch(_Batch):
         fn = self.ctx.lib.mfg_sgeqrf_batched if single else self.ctx.lib.mfg_dgeqrf_batched
         rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
         self.ctx.check(rc, "mfg_geqrf_batched")
+
+    def run_host(self, a, rdiag, b=None, single=False):
+        """QR (+ least squares) on host arrays, copies pipelined with compute.  Synchronous."""
+        fn = self.ctx.lib.mfg_sgeqrf_batched_host if single else self.ctx.lib.mfg_dgeqrf_batched_host
+        rc = fn(self.h, _hptr(a), _hptr(rdiag), _hptr(b))
+        self.ctx.check(rc, "mfg_geqrf_batched_host")
 
     def solve(self, a, rdiag, b, single=False):
         """Least squares with the factorization already in a and rdiag (nrhs columns of b)."""

@@ -88,18 +88,27 @@ struct mfg_plan {
   int ctas = 0;
   int warps = 0;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
-  // GETRF: host copies of the layout, and the pipelined host-buffer path (built on first use):
-  // contiguous chunks of the batch, each with its own plan, device mirrors of the user's arrays.
-  std::vector<int> hlda;
-  std::vector<long long> haoff, hpivoff, hboff;
+  // Host copies of the layout (every batched kind), for the pipelined host-buffer calls: m (QR),
+  // lda, ldb (GEVD), and the offsets of a, of the second array (piv / rdiag / B), of b and of C.
+  std::vector<int> hm, hlda, hldb;
+  std::vector<long long> haoff, hpivoff, hboff, hcoff;
+  // The pipelined host-buffer path (built on the first host call of an operation): contiguous
+  // chunks of the batch, each with its own plan, and device mirrors of the caller's arrays.
+  struct PipeArray {
+    int dir = 3;                     // 1: uploaded, 2: downloaded, 3: both
+    size_t es = 8;                   // element size
+    std::vector<size_t> beg, end;    // element range of every matrix
+    std::vector<size_t> lo, hi;      // element range of every chunk
+    DevBuf dev;
+  };
   struct Pipe {
+    int op = -1;
+    std::vector<PipeArray> arr;
     std::vector<mfg_plan*> chunk;
-    std::vector<int> c0, c1;                       // matrix index range of every chunk
-    std::vector<size_t> alo, ahi, plo, phi, blo, bhi;  // element ranges of a, piv, b
-    DevBuf da, dpiv, db, dsign, dinfo;
-    cudaStream_t h2d = nullptr, d2h = nullptr, comp2 = nullptr;
+    std::vector<int> c0, c1;
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaStream_t comp[3] = {nullptr, nullptr, nullptr};  // with the context's stream: four
     std::vector<cudaEvent_t> in, done;
-    bool ready = false;
   } pipe;
   // CUDA graph of the last execution (keyed by the data pointers and the stream).
   cudaGraphExec_t exec = nullptr;
@@ -107,6 +116,8 @@ struct mfg_plan {
 };
 
 namespace {
+
+void pipe_release(mfg_plan* p);
 
 int fail(mfg_ctx* ctx, int code, const char* fmt, ...) {
   if (ctx) {
@@ -459,18 +470,17 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
   a.group = group;
   a.dot_block = env_int("MFG_DOT_BLOCK", 4);
-  if (kind == mfg_plan::GETRF) {
-    p->hlda.resize(count);
-    p->haoff.assign(a_off, a_off + count);
-    p->hpivoff.assign(piv_off, piv_off + count);
-    p->hboff.resize(count);
-    for (int i = 0; i < count; i++) {
-      p->hlda[i] = lda ? lda[i] : n[i];
-      p->hboff[i] = nrhs > 0 ? b_off[i] : 0;
-    }
+  p->hn.assign(n, n + count);
+  p->hlda.resize(count);
+  p->haoff.assign(a_off, a_off + count);
+  p->hpivoff.assign(count, 0);
+  p->hboff.assign(count, 0);
+  for (int i = 0; i < count; i++) {
+    p->hlda[i] = lda ? lda[i] : n[i];
+    if (kind == mfg_plan::GETRF || kind == mfg_plan::GETRI) p->hpivoff[i] = piv_off[i];
+    if (nrhs > 0) p->hboff[i] = b_off[i];
   }
   if (kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) {
-    p->hn.assign(n, n + count);
     if (!tune_env_override()) {
       auto it = ctx->tune.find(tune_key((int)kind, max_n, count));
       if (it != ctx->tune.end()) {
@@ -567,6 +577,16 @@ int plan_create_gevd(mfg_ctx* ctx, mfg_plan** out, int count, const int* n, cons
   g.c_off = (const long long*)(base + 4 * bi + 2 * bl);
   g.count = count;
   g.queue = (int*)(base + 4 * bi + 3 * bl);
+  p->hn.assign(n, n + count);
+  p->hlda.resize(count);
+  p->hldb.resize(count);
+  for (int i = 0; i < count; i++) {
+    p->hlda[i] = lda ? lda[i] : n[i];
+    p->hldb[i] = ldb ? ldb[i] : n[i];
+  }
+  p->haoff.assign(a_off, a_off + count);
+  p->hboff.assign(b_off, b_off + count);
+  p->hcoff.assign(c_off, c_off + count);
   *out = p;
   return MFG_OK;
 }
@@ -684,6 +704,16 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   if (group_s < 32) p->qs.order = order_grouped;
   p->qd.gscratch = (double*)p->scratch.ptr;
   p->qs.gscratch = (float*)p->scratch.ptr;
+  p->hm.assign(m, m + count);
+  p->hn.assign(n, n + count);
+  p->hlda.resize(count);
+  p->haoff.assign(a_off, a_off + count);
+  p->hpivoff.assign(rdiag_off, rdiag_off + count);
+  p->hboff.assign(count, 0);
+  for (int i = 0; i < count; i++) {
+    p->hlda[i] = lda ? lda[i] : m[i];
+    if (nrhs > 0) p->hboff[i] = b_off[i];
+  }
   *out = p;
   return MFG_OK;
 }
@@ -1760,20 +1790,7 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   if (!plan) return -1;
   if (plan->exec) cudaGraphExecDestroy(plan->exec);
   cudaStreamSynchronize(plan->ctx->stream);
-  auto& pp = plan->pipe;
-  for (mfg_plan* c : pp.chunk) mfg_plan_destroy(c);
-  for (cudaEvent_t e : pp.in) cudaEventDestroy(e);
-  for (cudaEvent_t e : pp.done) cudaEventDestroy(e);
-  for (cudaStream_t st : {pp.h2d, pp.d2h, pp.comp2})
-    if (st) {
-      cudaStreamSynchronize(st);
-      cudaStreamDestroy(st);
-    }
-  pp.da.release();
-  pp.dpiv.release();
-  pp.db.release();
-  pp.dsign.release();
-  pp.dinfo.release();
+  pipe_release(plan);
   plan->meta.release();
   plan->scratch.release();
   plan->mx_work.release();
@@ -1825,105 +1842,318 @@ MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, 
 
 namespace {
 
-// Builds the pipelined host-buffer path of a getrf plan: the batch is cut into contiguous chunks
-// of about equal work (sum of n^3), each with its own plan whose offsets address device mirrors of
-// the user's arrays laid out exactly like the host arrays.  A layout whose chunks would share
-// elements (overlapping matrices) gets a single chunk.
-int pipe_build(mfg_plan* p) {
+// ---- Pipelined host-buffer calls --------------------------------------------------------------
+// A host call cuts the batch into contiguous chunks of about equal work, each with its own plan
+// whose offsets address device mirrors of the caller's arrays (laid out exactly like the host
+// arrays).  Chunk c's upload (stream h2d), kernel (one of two compute streams) and download
+// (stream d2h) overlap with the neighbouring chunks', so the copies hide behind the compute.
+enum PipeOp { OP_GETRF, OP_POTRF, OP_GRAD, OP_GETRI, OP_GEQRF_D, OP_GEQRF_S, OP_GEVD };
+
+void pipe_release(mfg_plan* p) {
+  auto& pp = p->pipe;
+  for (mfg_plan* c : pp.chunk) mfg_plan_destroy(c);
+  pp.chunk.clear();
+  for (cudaEvent_t e : pp.in) cudaEventDestroy(e);
+  for (cudaEvent_t e : pp.done) cudaEventDestroy(e);
+  pp.in.clear();
+  pp.done.clear();
+  for (cudaStream_t* st : {&pp.h2d, &pp.d2h, &pp.comp[0], &pp.comp[1], &pp.comp[2]})
+    if (*st) {
+      cudaStreamSynchronize(*st);
+      cudaStreamDestroy(*st);
+      *st = nullptr;
+    }
+  for (auto& a : pp.arr) a.dev.release();
+  pp.arr.clear();
+  pp.op = -1;
+}
+
+// The arrays an operation moves: per matrix i, the element range of each array.
+void pipe_arrays(mfg_plan* p, int op, int keep_factor) {
+  auto& arr = p->pipe.arr;
+  const int count = p->count, nrhs = p->nrhs;
+  const bool qr = op == OP_GEQRF_D || op == OP_GEQRF_S;
+  const size_t es = op == OP_GEQRF_S ? 4 : 8;
+  auto add = [&](int dir, size_t esz, auto beg, auto len) {
+    mfg_plan::PipeArray a;
+    a.dir = dir;
+    a.es = esz;
+    a.beg.resize(count);
+    a.end.resize(count);
+    for (int i = 0; i < count; i++) {
+      a.beg[i] = beg(i);
+      a.end[i] = a.beg[i] + len(i);
+    }
+    arr.push_back(std::move(a));
+  };
+  auto rows = [&](int i) { return qr ? p->hm[i] : p->hn[i]; };
+  auto aspan = [&](int i) { return span(rows(i), p->hn[i], p->hlda[i]); };
+  auto self = [](int i) { return (size_t)i; };
+  auto one = [](int) { return (size_t)1; };
+  switch (op) {
+    case OP_GETRF:  // a, b, piv, sign, info
+      add(3, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+          [&](int i) { return (size_t)p->hn[i] * nrhs; });
+      add(2, 4, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
+      add(2, 4, self, one);
+      add(2, 4, self, one);
+      break;
+    case OP_POTRF:  // a, b, info
+      add(3, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+          [&](int i) { return (size_t)p->hn[i] * nrhs; });
+      add(2, 4, self, one);
+      break;
+    case OP_GRAD:  // k, y, loss, grad, info
+      add(keep_factor ? 3 : 1, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
+      add(2, 8, self, one);
+      add(2, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(2, 4, self, one);
+      break;
+    case OP_GETRI:  // a, piv, info
+      add(3, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(1, 4, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
+      add(2, 4, self, one);
+      break;
+    case OP_GEQRF_D:
+    case OP_GEQRF_S:  // a, rdiag, b
+      add(3, es, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(2, es, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
+      add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
+          [&](int i) { return (size_t)p->hm[i] * nrhs; });
+      break;
+    case OP_GEVD:  // a, b, c, info
+      add(1, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+          [&](int i) { return span(p->hn[i], p->hn[i], p->hldb[i]); });
+      add(2, 8, [&](int i) { return (size_t)p->hcoff[i]; },
+          [&](int i) { return (size_t)p->hn[i] * p->hn[i]; });
+      add(2, 4, self, one);
+      break;
+  }
+}
+
+int pipe_build(mfg_plan* p, int op, int keep_factor) {
   mfg_ctx* ctx = p->ctx;
+  pipe_release(p);
   auto& pp = p->pipe;
   const int count = p->count;
-  const int nrhs = p->nrhs;
-  int K = std::max(1, std::min(16, count / 4096));
-  K = env_int("MFG_PIPE_CHUNKS", K);
+  const bool qr = op == OP_GEQRF_D || op == OP_GEQRF_S;
+  pipe_arrays(p, op, keep_factor);
+  // Chunks of about equal work (n^3, or m n^2 for QR), each about two full rounds of the GPU's
+  // resident warps (shorter chunks leave SMs idle in their tails), at least four for batches of
+  // 8,192 matrices or more and two from 2,048 (so that copies overlap compute), at most sixteen;
+  // the sweep over the seven benchmark batches is in the profiles.
+  long long per_wave;
+  if (op == OP_GRAD)
+    per_wave = (long long)ctx->sm_count * mfg::grad_ctas_per_sm() * mfg::grad_warps_per_cta();
+  else if (op == OP_GEQRF_D)
+    per_wave = (long long)p->ctas * p->warps * (32 / p->qd.group);
+  else if (op == OP_GEQRF_S)
+    per_wave = (long long)p->ctas * p->warps * (32 / p->qs.group);
+  else if (p->kind == mfg_plan::POTRF)
+    per_wave = (long long)p->ctas * p->warps * (32 / p->args.group);
+  else
+    per_wave = (long long)p->ctas * p->warps;
+  int K = (int)std::min<long long>(16, count / std::max<long long>(1, 2 * per_wave));
+  if (count >= 8192)
+    K = std::max(K, 4);
+  else if (count >= 2048)
+    K = std::max(K, 2);
+  K = env_int("MFG_PIPE_CHUNKS", std::max(K, 1));
   if (K < 1) K = 1;
+  auto work = [&](int i) {
+    const double n = p->hn[i];
+    return qr ? (double)p->hm[i] * n * n : n * n * n;
+  };
   double total = 0;
-  for (int i = 0; i < count; i++) total += (double)p->hn[i] * p->hn[i] * p->hn[i];
+  for (int i = 0; i < count; i++) total += work(i);
   std::vector<int> cut{0};
   double acc = 0;
   for (int i = 0; i < count && (int)cut.size() < K; i++) {
-    acc += (double)p->hn[i] * p->hn[i] * p->hn[i];
+    acc += work(i);
     if (acc >= total * cut.size() / K && i + 1 < count) cut.push_back(i + 1);
   }
   cut.push_back(count);
-  auto ranges = [&](int c0, int c1, size_t& alo, size_t& ahi, size_t& plo, size_t& phi,
-                    size_t& blo, size_t& bhi) {
-    alo = plo = blo = SIZE_MAX;
-    ahi = phi = bhi = 0;
-    for (int i = c0; i < c1; i++) {
-      const size_t a0 = (size_t)p->haoff[i];
-      alo = std::min(alo, a0);
-      ahi = std::max(ahi, a0 + span(p->hn[i], p->hn[i], p->hlda[i]));
-      plo = std::min(plo, (size_t)p->hpivoff[i]);
-      phi = std::max(phi, (size_t)p->hpivoff[i] + p->hn[i]);
-      if (nrhs > 0) {
-        blo = std::min(blo, (size_t)p->hboff[i]);
-        bhi = std::max(bhi, (size_t)p->hboff[i] + (size_t)p->hn[i] * nrhs);
-      }
+  auto chunk_ranges = [&]() {
+    const int nc = (int)cut.size() - 1;
+    for (auto& a : pp.arr) {
+      a.lo.assign(nc, SIZE_MAX);
+      a.hi.assign(nc, 0);
+      for (int c = 0; c < nc; c++)
+        for (int i = cut[c]; i < cut[c + 1]; i++)
+          if (a.end[i] > a.beg[i]) {
+            a.lo[c] = std::min(a.lo[c], a.beg[i]);
+            a.hi[c] = std::max(a.hi[c], a.end[i]);
+          }
+      for (int c = 0; c < nc; c++)
+        if (a.lo[c] == SIZE_MAX) a.lo[c] = a.hi[c] = 0;
     }
-    if (nrhs == 0) blo = bhi = 0;
   };
-  const int nc = (int)cut.size() - 1;
-  pp.c0.assign(cut.begin(), cut.end() - 1);
-  pp.c1.assign(cut.begin() + 1, cut.end());
-  pp.alo.resize(nc); pp.ahi.resize(nc); pp.plo.resize(nc); pp.phi.resize(nc);
-  pp.blo.resize(nc); pp.bhi.resize(nc);
-  for (int c = 0; c < nc; c++)
-    ranges(pp.c0[c], pp.c1[c], pp.alo[c], pp.ahi[c], pp.plo[c], pp.phi[c], pp.blo[c], pp.bhi[c]);
-  // Overlapping element ranges would let one chunk's upload overwrite another's data.
+  chunk_ranges();
+  // Overlapping chunk ranges would let one chunk's upload overwrite another's data.
   bool overlap = false;
-  for (int c = 0; c < nc && !overlap; c++)
-    for (int d = c + 1; d < nc && !overlap; d++)
-      overlap = (pp.alo[c] < pp.ahi[d] && pp.alo[d] < pp.ahi[c]) ||
-                (pp.plo[c] < pp.phi[d] && pp.plo[d] < pp.phi[c]) ||
-                (nrhs > 0 && pp.blo[c] < pp.bhi[d] && pp.blo[d] < pp.bhi[c]);
-  if (overlap && nc > 1) {
-    pp.c0 = {0};
-    pp.c1 = {count};
-    pp.alo.resize(1); pp.ahi.resize(1); pp.plo.resize(1); pp.phi.resize(1);
-    pp.blo.resize(1); pp.bhi.resize(1);
-    ranges(0, count, pp.alo[0], pp.ahi[0], pp.plo[0], pp.phi[0], pp.blo[0], pp.bhi[0]);
+  for (auto& a : pp.arr)
+    for (size_t c = 0; c < a.lo.size() && !overlap; c++)
+      for (size_t d = c + 1; d < a.lo.size() && !overlap; d++)
+        overlap = a.lo[c] < a.hi[d] && a.lo[d] < a.hi[c];
+  if (overlap) {
+    cut = {0, count};
+    chunk_ranges();
   }
-  size_t aspan = 0, pspan = 0, bspan = 0;
-  for (size_t c = 0; c < pp.c0.size(); c++) {
-    aspan = std::max(aspan, pp.ahi[c]);
-    pspan = std::max(pspan, pp.phi[c]);
-    bspan = std::max(bspan, pp.bhi[c]);
+  for (auto& a : pp.arr) {
+    size_t hi = 1;
+    for (size_t v : a.hi) hi = std::max(hi, v);
+    MFG_CUDA(ctx, a.dev.reserve(a.es * hi));
   }
-  MFG_CUDA(ctx, pp.da.reserve(sizeof(double) * std::max<size_t>(aspan, 1)));
-  MFG_CUDA(ctx, pp.dpiv.reserve(sizeof(int) * std::max<size_t>(pspan, 1)));
-  MFG_CUDA(ctx, pp.db.reserve(sizeof(double) * std::max<size_t>(bspan, 1)));
-  MFG_CUDA(ctx, pp.dsign.reserve(sizeof(int) * count));
-  MFG_CUDA(ctx, pp.dinfo.reserve(sizeof(int) * count));
   MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.h2d, cudaStreamNonBlocking));
   MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.d2h, cudaStreamNonBlocking));
-  MFG_CUDA(ctx, cudaStreamCreateWithFlags(&pp.comp2, cudaStreamNonBlocking));
-  for (size_t c = 0; c < pp.c0.size(); c++) {
-    const int c0 = pp.c0[c], cnt = pp.c1[c] - pp.c0[c];
+  for (auto& st : pp.comp) MFG_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const int nrhs = p->nrhs;
+  for (size_t c = 0; c + 1 < cut.size(); c++) {
+    const int c0 = cut[c], cnt = cut[c + 1] - cut[c];
     mfg_plan* sub = nullptr;
-    int rc = plan_create(ctx, &sub, mfg_plan::GETRF, cnt, p->hn.data() + c0, p->hlda.data() + c0,
-                         (const int64_t*)p->haoff.data() + c0,
-                         (const int64_t*)p->hpivoff.data() + c0, nrhs,
-                         nrhs > 0 ? (const int64_t*)p->hboff.data() + c0 : nullptr);
+    auto at = [c0](const std::vector<long long>& v) {
+      return v.empty() ? (const int64_t*)nullptr : (const int64_t*)v.data() + c0;
+    };
+    const int64_t* aoff = at(p->haoff);
+    const int64_t* poff = at(p->hpivoff);
+    const int64_t* boff = at(p->hboff);
+    int rc;
+    if (qr)
+      rc = plan_create_qr(ctx, &sub, cnt, p->hm.data() + c0, p->hn.data() + c0,
+                          p->hlda.data() + c0, aoff, poff, nrhs, nrhs > 0 ? boff : nullptr);
+    else if (p->kind == mfg_plan::GEVD)
+      rc = plan_create_gevd(ctx, &sub, cnt, p->hn.data() + c0, p->hlda.data() + c0, aoff,
+                            p->hldb.data() + c0, boff, at(p->hcoff));
+    else
+      rc = plan_create(ctx, &sub, p->kind, cnt, p->hn.data() + c0, p->hlda.data() + c0, aoff,
+                       poff, nrhs, nrhs > 0 ? boff : nullptr);
     if (rc != MFG_OK) return rc;
-    // Same launch shape as the parent plan (which the autotuner may have chosen).
-    rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
-                      p->args.group, p->args.hw_mul);
-    if (rc != MFG_OK) return rc;
-    sub->args.a = (double*)pp.da.ptr;
-    sub->args.piv = (int*)pp.dpiv.ptr;
-    sub->args.b = nrhs > 0 ? (double*)pp.db.ptr : nullptr;
-    sub->args.sign = (int*)pp.dsign.ptr + c0;
-    sub->args.info = (int*)pp.dinfo.ptr + c0;
-    sub->args.solve_only = 0;
     pp.chunk.push_back(sub);
+    if (p->kind == mfg_plan::GETRF || p->kind == mfg_plan::POTRF) {
+      // Same launch shape as the parent plan (which the autotuner may have chosen).
+      rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
+                        p->args.group, p->args.hw_mul);
+      if (rc != MFG_OK) return rc;
+    }
+    pp.c0.push_back(c0);
+    pp.c1.push_back(c0 + cnt);
     cudaEvent_t e1, e2;
     MFG_CUDA(ctx, cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
     MFG_CUDA(ctx, cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
     pp.in.push_back(e1);
     pp.done.push_back(e2);
   }
-  pp.ready = true;
+  pp.op = op;
+  return MFG_OK;
+}
+
+// Runs operation op on the caller's host arrays (in the order pipe_arrays lists them).
+int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> host) {
+  mfg_ctx* ctx = p->ctx;
+  auto& pp = p->pipe;
+  if (pp.op != op) {
+    // op % 100 is the operation; the hundreds distinguish variants with other array sets.
+    const int rc = pipe_build(p, op % 100, keep_factor);
+    if (rc != MFG_OK) {
+      pipe_release(p);
+      return rc;
+    }
+    pp.op = op;
+  }
+  std::vector<char*> h;
+  for (void* v : host) h.push_back((char*)v);
+  auto dev = [&](int k) { return (char*)pp.arr[k].dev.ptr; };
+  for (size_t c = 0; c < pp.chunk.size(); c++) {
+    for (size_t k = 0; k < pp.arr.size(); k++) {
+      const auto& a = pp.arr[k];
+      if ((a.dir & 1) && h[k] && a.hi[c] > a.lo[c])
+        MFG_CUDA(ctx, cudaMemcpyAsync(dev((int)k) + a.lo[c] * a.es, h[k] + a.lo[c] * a.es,
+                                      (a.hi[c] - a.lo[c]) * a.es, cudaMemcpyDefault, pp.h2d));
+    }
+    MFG_CUDA(ctx, cudaEventRecord(pp.in[c], pp.h2d));
+    // Four compute streams in turn: the kernels of the next chunks fill the SMs that a chunk's
+    // last matrices leave idle.
+    cudaStream_t sc = (c & 3) ? pp.comp[(c & 3) - 1] : ctx->stream;
+    MFG_CUDA(ctx, cudaStreamWaitEvent(sc, pp.in[c], 0));
+    mfg_plan* sub = pp.chunk[c];
+    const int c0 = pp.c0[c];
+    int rc = MFG_OK;
+    switch (op % 100) {
+      case OP_GETRF:
+        sub->args.a = (double*)dev(0);
+        sub->args.b = p->nrhs > 0 ? (double*)dev(1) : nullptr;
+        sub->args.piv = (int*)dev(2);
+        sub->args.sign = (int*)dev(3) + c0;
+        sub->args.info = (int*)dev(4) + c0;
+        sub->args.solve_only = 0;
+        rc = plan_launch(sub, sc);
+        break;
+      case OP_POTRF:
+        sub->args.a = (double*)dev(0);
+        sub->args.b = p->nrhs > 0 ? (double*)dev(1) : nullptr;
+        sub->args.info = (int*)dev(2) + c0;
+        sub->args.solve_only = 0;
+        rc = plan_launch(sub, sc);
+        break;
+      case OP_GRAD: {
+        BatchArgs a = sub->args;
+        a.a = (double*)dev(0);
+        a.b = (double*)dev(1);
+        a.info = (int*)dev(4) + c0;
+        MFG_CUDA(ctx, cudaMemsetAsync(a.queue, 0, sizeof(int), sc));
+        const int wpc = mfg::grad_warps_per_cta();
+        const long long ctas = std::min<long long>(
+            (long long)ctx->sm_count * mfg::grad_ctas_per_sm(), ((long long)sub->count + wpc - 1) / wpc);
+        MFG_CUDA(ctx, mfg::launch_chol_grad_batched(a, (double*)dev(2) + c0, (double*)dev(3),
+                                                    keep_factor ? 1 : 0,
+                                                    (int)std::max<long long>(1, ctas), sc));
+        break;
+      }
+      case OP_GETRI:
+        sub->args.a = (double*)dev(0);
+        sub->args.piv = (int*)dev(1);
+        sub->args.info = (int*)dev(2) + c0;
+        rc = plan_launch(sub, sc);
+        break;
+      case OP_GEQRF_D:
+        sub->qr_float = 0;
+        sub->qd.a = (double*)dev(0);
+        sub->qd.rdiag = (double*)dev(1);
+        sub->qd.b = p->nrhs > 0 ? (double*)dev(2) : nullptr;
+        sub->qd.solve_only = 0;
+        rc = plan_launch(sub, sc);
+        break;
+      case OP_GEQRF_S:
+        sub->qr_float = 1;
+        sub->qs.a = (float*)dev(0);
+        sub->qs.rdiag = (float*)dev(1);
+        sub->qs.b = p->nrhs > 0 ? (float*)dev(2) : nullptr;
+        sub->qs.solve_only = 0;
+        rc = plan_launch(sub, sc);
+        break;
+      case OP_GEVD:
+        sub->gv.a = (const double*)dev(0);
+        sub->gv.b = (double*)dev(1);
+        sub->gv.c = (double*)dev(2);
+        sub->gv.info = (int*)dev(3) + c0;
+        rc = plan_launch(sub, sc);
+        break;
+    }
+    if (rc != MFG_OK) return rc;
+    MFG_CUDA(ctx, cudaEventRecord(pp.done[c], sc));
+    MFG_CUDA(ctx, cudaStreamWaitEvent(pp.d2h, pp.done[c], 0));
+    for (size_t k = 0; k < pp.arr.size(); k++) {
+      const auto& a = pp.arr[k];
+      if ((a.dir & 2) && h[k] && a.hi[c] > a.lo[c])
+        MFG_CUDA(ctx, cudaMemcpyAsync(h[k] + a.lo[c] * a.es, dev((int)k) + a.lo[c] * a.es,
+                                      (a.hi[c] - a.lo[c]) * a.es, cudaMemcpyDefault, pp.d2h));
+    }
+  }
+  MFG_CUDA(ctx, cudaStreamSynchronize(pp.d2h));
   return MFG_OK;
 }
 
@@ -1942,46 +2172,86 @@ MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double*
   if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
   if (!sign) return fail(ctx, -5, "sign is null");
   if (!info) return fail(ctx, -6, "info is null");
-  auto& pp = plan->pipe;
-  if (!pp.ready) {
-    const int rc = pipe_build(plan);
-    if (rc != MFG_OK) return rc;
-  }
-  double* da = (double*)pp.da.ptr;
-  int* dpiv = (int*)pp.dpiv.ptr;
-  double* db = (double*)pp.db.ptr;
-  const int nrhs = plan->nrhs;
-  for (size_t c = 0; c < pp.chunk.size(); c++) {
-    const size_t an = pp.ahi[c] - pp.alo[c], bn = pp.bhi[c] - pp.blo[c];
-    MFG_CUDA(ctx, cudaMemcpyAsync(da + pp.alo[c], a + pp.alo[c], an * 8, cudaMemcpyDefault,
-                                  pp.h2d));
-    if (nrhs > 0)
-      MFG_CUDA(ctx, cudaMemcpyAsync(db + pp.blo[c], b + pp.blo[c], bn * 8, cudaMemcpyDefault,
-                                    pp.h2d));
-    MFG_CUDA(ctx, cudaEventRecord(pp.in[c], pp.h2d));
-    // Alternate two compute streams so one chunk's kernel can fill the SMs left idle by the
-    // previous chunk's last matrices.
-    cudaStream_t sc = (c & 1) ? pp.comp2 : ctx->stream;
-    MFG_CUDA(ctx, cudaStreamWaitEvent(sc, pp.in[c], 0));
-    const int rc = plan_launch(pp.chunk[c], sc);
-    if (rc != MFG_OK) return rc;
-    MFG_CUDA(ctx, cudaEventRecord(pp.done[c], sc));
-    MFG_CUDA(ctx, cudaStreamWaitEvent(pp.d2h, pp.done[c], 0));
-    const int c0 = pp.c0[c], cnt = pp.c1[c] - pp.c0[c];
-    MFG_CUDA(ctx, cudaMemcpyAsync(a + pp.alo[c], da + pp.alo[c], an * 8, cudaMemcpyDefault,
-                                  pp.d2h));
-    MFG_CUDA(ctx, cudaMemcpyAsync(piv + pp.plo[c], dpiv + pp.plo[c],
-                                  (pp.phi[c] - pp.plo[c]) * 4, cudaMemcpyDefault, pp.d2h));
-    if (nrhs > 0)
-      MFG_CUDA(ctx, cudaMemcpyAsync(b + pp.blo[c], db + pp.blo[c], bn * 8, cudaMemcpyDefault,
-                                    pp.d2h));
-    MFG_CUDA(ctx, cudaMemcpyAsync(sign + c0, (int*)pp.dsign.ptr + c0, cnt * 4, cudaMemcpyDefault,
-                                  pp.d2h));
-    MFG_CUDA(ctx, cudaMemcpyAsync(info + c0, (int*)pp.dinfo.ptr + c0, cnt * 4, cudaMemcpyDefault,
-                                  pp.d2h));
-  }
-  MFG_CUDA(ctx, cudaStreamSynchronize(pp.d2h));
-  return MFG_OK;
+  return pipe_run(plan, OP_GETRF, 0, {a, b, piv, sign, info});
+}
+
+MFG_API int mfg_dpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -3, "b is null");
+  if (!info) return fail(ctx, -4, "info is null");
+  return pipe_run(plan, OP_POTRF, 0, {a, b, info});
+}
+
+MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k, double* y,
+                                                     double* loss, double* grad, int* info,
+                                                     int keep_factor) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->nrhs != 1) return fail(ctx, -1, "the plan must have nrhs = 1 (the vector y)");
+  if (plan->max_n > 128)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "matrix order %d > 128 is not supported here",
+                plan->max_n);
+  if (plan->count == 0) return MFG_OK;
+  if (!k) return fail(ctx, -2, "k is null");
+  if (!y) return fail(ctx, -3, "y is null");
+  if (!loss) return fail(ctx, -4, "loss is null");
+  if (!grad) return fail(ctx, -5, "grad is null");
+  if (!info) return fail(ctx, -6, "info is null");
+  if ((void*)grad == (void*)k) return fail(ctx, -5, "grad must not alias k");
+  // keep_factor changes which arrays come back, hence its own pipe variant.
+  return pipe_run(plan, OP_GRAD + (keep_factor ? 0 : 100), keep_factor ? 1 : 0,
+                  {k, y, loss, grad, info});
+}
+
+MFG_API int mfg_dgetri_batched_host(mfg_plan* plan, double* a, const int* piv, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRI) return fail(ctx, -1, "plan is not a getri plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!piv) return fail(ctx, -3, "piv is null");
+  if (!info) return fail(ctx, -4, "info is null");
+  return pipe_run(plan, OP_GETRI, 0, {a, const_cast<int*>(piv), info});
+}
+
+MFG_API int mfg_dgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!rdiag) return fail(ctx, -3, "rdiag is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  return pipe_run(plan, OP_GEQRF_D, 0, {a, rdiag, b});
+}
+
+MFG_API int mfg_sgeqrf_batched_host(mfg_plan* plan, float* a, float* rdiag, float* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!rdiag) return fail(ctx, -3, "rdiag is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  return pipe_run(plan, OP_GEQRF_S, 0, {a, rdiag, b});
+}
+
+MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
+                                         int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEVD) return fail(ctx, -1, "plan is not a gevd plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!b) return fail(ctx, -3, "b is null");
+  if (!c) return fail(ctx, -4, "c is null");
+  if (!info) return fail(ctx, -5, "info is null");
+  return pipe_run(plan, OP_GEVD, 0, {const_cast<double*>(a), b, c, info});
 }
 
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {

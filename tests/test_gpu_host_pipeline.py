@@ -58,3 +58,87 @@ def test_host_pipeline_matches_device_path(mf, reverse):
         assert_bits(ta.numpy(), ha)
         assert_bits(tb.numpy(), hb)
         np.testing.assert_array_equal(tp.numpy(), hpiv)
+
+
+def _pinned(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x).copy()).pin_memory()
+
+
+def test_host_pipeline_other_operations(mf):
+    """Every batched operation's host-buffer form equals its device-buffer form bit for bit
+    (batches above 8,192 matrices, so the pipeline has at least two chunks)."""
+    import torch
+    from matflat_gb300 import synth
+    count = 9000
+    # Cholesky + solve
+    d = synth.spd_batch(count, 24, nrhs=1, seed=5)
+    plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
+    da, db = _dev(d["a"]), _dev(d["b"])
+    di = torch.zeros(count, dtype=torch.int32, device="cuda")
+    plan.run(da, db, di)
+    ha, hb, hi = _pinned(d["a"]), _pinned(d["b"]), _pinned(np.zeros(count, np.int32))
+    plan.run_host(ha, hb, hi)
+    assert_bits(ha.numpy(), _host(da))
+    assert_bits(hb.numpy(), _host(db))
+    # loss and gradient, both factor modes
+    r = synth.rbf_batch(count, 24, seed=6)
+    gp = mf.CholeskyBatch(r["n"], r["a_off"], nrhs=1, b_off=r["b_off"])
+    for keep in (True, False):
+        dk, dy = _dev(r["a"]), _dev(r["b"])
+        dl = torch.zeros(count, dtype=torch.float64, device="cuda")
+        dg = torch.zeros_like(dk)
+        dinf = torch.zeros(count, dtype=torch.int32, device="cuda")
+        gp.loss_and_grad(dk, dy, dl, dg, dinf, keep_factor=keep)
+        hk, hy = _pinned(r["a"]), _pinned(r["b"])
+        hl = _pinned(np.zeros(count))
+        hg = _pinned(np.zeros_like(r["a"]))
+        hinf = _pinned(np.zeros(count, np.int32))
+        gp.loss_and_grad_host(hk, hy, hl, hg, hinf, keep_factor=keep)
+        assert_bits(hk.numpy(), _host(dk))
+        assert_bits(hy.numpy(), _host(dy))
+        assert_bits(hl.numpy(), _host(dl))
+        assert_bits(hg.numpy(), _host(dg))
+        np.testing.assert_array_equal(hinf.numpy(), _host(dinf))
+    # LuInverse of LU factors
+    lu = synth.lu_batch(count, 4, 40, 0, seed=7)
+    lp = mf.LuBatch(lu["n"], lu["a_off"], lu["piv_off"])
+    fa = _dev(lu["a"])
+    fp = torch.zeros(lu["piv_total"], dtype=torch.int32, device="cuda")
+    lp.run(fa, fp, None, torch.zeros(count, dtype=torch.int32, device="cuda"),
+           torch.zeros(count, dtype=torch.int32, device="cuda"))
+    mf.context().synchronize()
+    fac, piv = _host(fa), _host(fp)
+    ip = mf.LuInverseBatch(lu["n"], lu["a_off"], lu["piv_off"])
+    ia = _dev(fac)
+    iinf = torch.zeros(count, dtype=torch.int32, device="cuda")
+    ip.run(ia, _dev(piv), iinf)
+    ha, hinf = _pinned(fac), _pinned(np.zeros(count, np.int32))
+    ip.run_host(ha, _pinned(piv), hinf)
+    assert_bits(ha.numpy(), _host(ia))
+    np.testing.assert_array_equal(hinf.numpy(), _host(iinf))
+    # QR + least squares, double and float
+    q = synth.qr_batch(count, 16, 96, 4, 16, nrhs=1, seed=8)
+    qp = mf.QrBatch(q["m"], q["n"], q["a_off"], q["rdiag_off"], nrhs=1, b_off=q["b_off"])
+    for dt, single in ((np.float64, False), (np.float32, True)):
+        qa, qb = _dev(q["a"].astype(dt)), _dev(q["b"].astype(dt))
+        qr_ = torch.zeros(q["rdiag_total"], dtype=qa.dtype, device="cuda")
+        qp.run(qa, qr_, qb, single=single)
+        ha, hb = _pinned(q["a"].astype(dt)), _pinned(q["b"].astype(dt))
+        hr = _pinned(np.zeros(q["rdiag_total"], dt))
+        qp.run_host(ha, hr, hb, single=single)
+        assert_bits(ha.numpy(), _host(qa))
+        assert_bits(hr.numpy(), _host(qr_))
+        assert_bits(hb.numpy(), _host(qb))
+    # GEVD front half
+    g = synth.gevd_batch(count, 12, seed=9)
+    vp = mf.GevdFrontBatch(g["n"], g["a_off"], g["b_off"], g["a_off"])
+    va, vb = _dev(g["a"]), _dev(g["b"])
+    vc = torch.zeros_like(va)
+    vi = torch.zeros(count, dtype=torch.int32, device="cuda")
+    vp.run(va, vb, vc, vi)
+    hb, hc, hinf = _pinned(g["b"]), _pinned(np.zeros_like(g["a"])), _pinned(np.zeros(count, np.int32))
+    vp.run_host(_pinned(g["a"]), hb, hc, hinf)
+    assert_bits(hb.numpy(), _host(vb))
+    assert_bits(hc.numpy(), _host(vc))
+    np.testing.assert_array_equal(hinf.numpy(), _host(vi))
