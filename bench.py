@@ -881,7 +881,8 @@ def main():
                                         "batched factorization/solve (one graph replay)"},
             "kernel_ms_per_step": kmed,
             "launch_shape": None if tuned is None else dict(
-                zip(["warps_per_cta", "warps_per_sm", "lanes_per_matrix", "mul_mode"], tuned),
+                zip(["warps_per_cta", "warps_per_sm", "lanes_per_matrix", "mul_mode",
+                     "dot_pairs_per_block"], tuned),
                 source="mfg_plan_autotune at plan creation (outside the timed region)"),
             "gpu_launches": args.steps,
             "roofline": roof,

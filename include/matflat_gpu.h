@@ -326,8 +326,8 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
  * evenly), installs the fastest in the plan and records it in the context's tuning table under the
  * plan's size bucket (kind, largest order, batch size), so later plans of that bucket on this
  * context start from it.  Synchronous; allocates and frees its own buffers; every shape gives the
- * same bits.  config (may be NULL) receives {warps per CTA, warps per SM, lanes per matrix,
- * multiply mode}.  Environment overrides of the shape (MFG_WARPS_PER_*, MFG_HW_MUL,
+ * same bits.  config (may be NULL) receives 5 ints: {warps per CTA, warps per SM, lanes per
+ * matrix, multiply mode, dot-product pairs per pipelined block}.  Environment overrides of the shape (MFG_WARPS_PER_*, MFG_HW_MUL,
  * MFG_CHOL_GROUP) take precedence over the table for new plans. */
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 

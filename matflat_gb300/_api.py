@@ -416,8 +416,8 @@ class _Batch:
     def autotune(self):
         """Times candidate launch shapes on a synthetic batch with this plan's size mix and keeps
         the fastest (getrf and potrf plans); returns (warps per CTA, warps per SM, lanes per
-        matrix, multiply mode)."""
-        cfg = (ctypes.c_int * 4)()
+        matrix, multiply mode, dot pairs per block)."""
+        cfg = (ctypes.c_int * 5)()
         rc = self.ctx.lib.mfg_plan_autotune(self.h, cfg)
         self.ctx.check(rc, "mfg_plan_autotune")
         return tuple(cfg)

@@ -67,7 +67,7 @@ struct mfg_ctx {
   std::string last_error;
   bool use_graphs = true;
   // Autotuner results: launch shape per (plan kind, size bucket), used by later plans.
-  std::map<long long, std::array<int, 4>> tune;
+  std::map<long long, std::array<int, 5>> tune;
 };
 
 struct mfg_plan {
@@ -232,7 +232,7 @@ void choose_shape(mfg_plan* p, int fixed_warps = 0) {
 // Re-shapes a getrf/potrf plan: warps per CTA (1, 2, 4, 8 or 16), warps per SM, lanes per
 // matrix (potrf) and the multiply mode; grows the per-warp scratch when the new shape keeps more
 // matrices in flight, and drops the cached graph.
-int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul) {
+int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_block = 0) {
   mfg_ctx* ctx = p->ctx;
   long long ctas = (long long)ctx->sm_count * wps / warps;
   const long long need = ((long long)p->count + warps - 1) / warps;
@@ -253,6 +253,7 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul) {
   p->args.gscratch_stride = stride;
   p->args.group = g;
   p->args.hw_mul = mul;
+  if (dot_block > 0) p->args.dot_block = dot_block;
   if (p->exec) {
     cudaGraphExecDestroy(p->exec);
     p->exec = nullptr;
@@ -485,7 +486,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
       auto it = ctx->tune.find(tune_key((int)kind, max_n, count));
       if (it != ctx->tune.end()) {
         const auto& c = it->second;
-        const int rc = plan_reshape(p, c[0], c[1], c[2], c[3]);
+        const int rc = plan_reshape(p, c[0], c[1], c[2], c[3], c[4]);
         if (rc != MFG_OK) {
           delete p;
           return rc;
@@ -1731,18 +1732,20 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   tp->args.sign = plan->kind == mfg_plan::GETRF ? sign : nullptr;
   tp->args.info = info;
   tp->args.solve_only = 0;
-  std::vector<std::array<int, 4>> cands;
+  std::vector<std::array<int, 5>> cands;
   if (plan->kind == mfg_plan::GETRF) {
+    // Four-pair dot blocks need ~100 registers (up to 20 warps/SM), two-pair blocks ~80.
     for (int w : {4, 8})
       for (int wps : {8, 12, 16, 20})
-        for (int mul : {0, 2}) cands.push_back({w, wps, 32, mul});
+        for (int mul : {0, 2}) cands.push_back({w, wps, 32, mul, 4});
+    for (int wps : {20, 24}) cands.push_back({4, wps, 32, 0, 2});
   } else {
     for (int g : {4, 8, 16, 32})
       for (int wps : {8, 16})
-        for (int mul : {0, 1}) cands.push_back({4, wps, g, mul});
+        for (int mul : {0, 1}) cands.push_back({4, wps, g, mul, 4});
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  std::array<int, 4> best = cands[0];
+  std::array<int, 5> best = cands[0];
   float best_ms = 3.0e38f;
   ce = mfg::launch_tune_fill(tp->args, plan->kind == mfg_plan::POTRF ? 1 : 0, s);
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(a0, a, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
@@ -1752,7 +1755,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
   for (size_t c = 0; ce == cudaSuccess && rc == MFG_OK && c < cands.size(); c++) {
     const auto& k = cands[c];
-    rc = plan_reshape(tp, k[0], k[1], k[2], k[3]);
+    rc = plan_reshape(tp, k[0], k[1], k[2], k[3], k[4]);
     float tmin = 3.0e38f;
     for (int rep = 0; rc == MFG_OK && ce == cudaSuccess && rep < 2; rep++) {
       ce = cudaMemcpyAsync(a, a0, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
@@ -1778,11 +1781,11 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   mfg_plan_destroy(tp);
   if (rc != MFG_OK) return rc;
   if (ce != cudaSuccess) return cuda_fail(ctx, ce, "autotune");
-  rc = plan_reshape(plan, best[0], best[1], best[2], best[3]);
+  rc = plan_reshape(plan, best[0], best[1], best[2], best[3], best[4]);
   if (rc != MFG_OK) return rc;
   ctx->tune[tune_key((int)plan->kind, plan->max_n, plan->count)] = best;
   if (config)
-    for (int i = 0; i < 4; i++) config[i] = best[i];
+    for (int i = 0; i < 5; i++) config[i] = best[i];
   return MFG_OK;
 }
 
@@ -2036,7 +2039,7 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     if (p->kind == mfg_plan::GETRF || p->kind == mfg_plan::POTRF) {
       // Same launch shape as the parent plan (which the autotuner may have chosen).
       rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
-                        p->args.group, p->args.hw_mul);
+                        p->args.group, p->args.hw_mul, p->args.dot_block);
       if (rc != MFG_OK) return rc;
     }
     pp.c0.push_back(c0);
