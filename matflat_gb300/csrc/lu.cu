@@ -224,8 +224,6 @@ static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t 
     getrf_batched_kernel<WARPS, 2, 4><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.hw_mul)
     getrf_batched_kernel<WARPS, 0, 4><<<ctas, WARPS * 32, smem, s>>>(args);
-  else if (args.dot_block == 8)
-    getrf_batched_kernel<WARPS, true, 8><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.dot_block == 2)
     getrf_batched_kernel<WARPS, true, 2><<<ctas, WARPS * 32, smem, s>>>(args);
   else
@@ -238,9 +236,6 @@ static cudaError_t set_getrf_attr() {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
   cudaError_t e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 4>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 8>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, true, 2>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

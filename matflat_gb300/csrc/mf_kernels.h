@@ -38,7 +38,7 @@ struct BatchArgs {
   int hw_mul;                // getrf/potrf: 0 products on the integer pipes, 1 on the FP64 pipe
                              // (DMUL), 2 (getrf) alternating; all give identical bits
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
-  int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4, 8)
+  int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4)
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
 };
 
