@@ -846,8 +846,9 @@ def main():
         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 has no entry in "
                        "MEASURED_PEAKS.json)",
         "exact_order_ceiling_frac": 0.5,
-        "note": "MatFlat-exact arithmetic issues every multiply and add separately (no FMA), so "
-                "this kernel's own ceiling is half the DFMA peak",
+        "note": "MatFlat-exact arithmetic issues every multiply and add separately (no FMA): on "
+                "the FP64 pipe alone that caps a kernel at half the DFMA peak; kernels that move "
+                "the multiplies to the integer pipes (getrf, potrf) can pass that ceiling",
         "traffic": traffic, "algorithmic_bytes_per_launch": byts,
         "hbm_achieved_gbs": byts / (kmed / 1e3) / 1e9, "hbm_peak_gbs": hbm,
         "hbm_frac": byts / (kmed / 1e3) / 1e9 / hbm,
