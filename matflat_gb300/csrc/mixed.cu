@@ -129,21 +129,22 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
     }
   }
   __syncthreads();
-  // U12 = L11^-1 A12 (unit lower), one column per thread.
+  // U12 = L11^-1 A12 (unit lower), one column per thread, staged in shared memory after the panel
+  // (us[i * MX_THREADS + tid]: conflict-free).  Column sweep: for every t, u[i] -= L(i,t) u[t]
+  // for i > t, which is the same FMA sequence per entry as the dot form.  A fully unrolled
+  // register version needed more than 255 registers and spilled.
+  float* us = sp + rows * MX_NB + tid;
   for (int c = k + MX_NB + tid; c < n; c += MX_THREADS) {
     float* col = a + (long long)c * n + k;
-    float u[MX_NB];
-#pragma unroll
-    for (int i = 0; i < MX_NB; ++i) u[i] = col[i];
-#pragma unroll
-    for (int i = 1; i < MX_NB; ++i) {
-      float s = u[i];
-#pragma unroll
-      for (int t = 0; t < i; ++t) s = fmaf(-sp[t * ldp + i], u[t], s);
-      u[i] = s;
+    for (int i = 0; i < MX_NB; ++i) us[i * MX_THREADS] = col[i];
+    for (int t = 0; t < MX_NB - 1; ++t) {
+      const float ut = us[t * MX_THREADS];
+      const float* lt = sp + t * ldp;
+#pragma unroll 4
+      for (int i = t + 1; i < MX_NB; ++i)
+        us[i * MX_THREADS] = fmaf(-lt[i], ut, us[i * MX_THREADS]);
     }
-#pragma unroll
-    for (int i = 0; i < MX_NB; ++i) col[i] = u[i];
+    for (int i = 0; i < MX_NB; ++i) col[i] = us[i * MX_THREADS];
   }
 }
 
@@ -244,21 +245,27 @@ __device__ void mx_lu_solve_warp(const float* lu, const int* ip, int n, float* v
   }
 }
 
-// One refinement sweep per matrix (warp per matrix):
+// One refinement sweep per system, one CTA of MX_RT threads per system:
 //   iter == -1: x = (LU)^-1 b                       (initial solve)
 //   iter >= 0 : r = b - A x (FP64), berr; stop on convergence or stall, else x += (LU)^-1 r.
 //   iter == -2: measure only: berr of x for the systems with state != 0 (FP64 fallback).
 // state: 0 active, 1 converged, 2 stalled/diverged, 3 singular low-precision factor.
-__global__ void mx_refine_kernel(const double* a, const double* b, double* x, const float* lu,
-                                 const int* ipiv, int n, int count, int iter, double tol,
-                                 double* berr, int* iters, int* state, double* anorm,
-                                 int* active) {
-  extern __shared__ float sv[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  const int mat = blockIdx.x * wpb + warp;
+// The residual streams A (FP64) once per sweep with all MX_RT threads (thread t owns rows t,
+// t + MX_RT, ...; coalesced column reads); warp 0 then runs the FP32 triangular solves.
+constexpr int MX_RT = 256;       // refinement CTA size
+constexpr int MX_RROWS = 4;      // rows per thread (n <= 1024)
+
+__global__ void __launch_bounds__(MX_RT) mx_refine_kernel(
+    const double* a, const double* b, double* x, const float* lu, const int* ipiv, int n,
+    int count, int iter, double tol, double* berr, int* iters, int* state, double* anorm,
+    int* active) {
+  extern __shared__ double sx[];            // x (n doubles), then v (n floats)
+  __shared__ double red[4][MX_RT / 32];
+  __shared__ int verdict;
+  float* v = reinterpret_cast<float*>(sx + n);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int mat = blockIdx.x;
   if (mat >= count) return;
-  float* v = sv + warp * n;
   const double* A = a + (long long)mat * n * n;
   const double* B = b + (long long)mat * n;
   double* X = x + (long long)mat * n;
@@ -267,14 +274,13 @@ __global__ void mx_refine_kernel(const double* a, const double* b, double* x, co
   const bool measure = iter == -2;
   if (iter == -1) {
     int sing = 0;
-    for (int i = lane; i < n; i += 32) {
+    for (int i = tid; i < n; i += MX_RT) {
       v[i] = (float)B[i];
       if (LU[(long long)i * n + i] == 0.0f) sing = 1;
     }
-    sing = __any_sync(FULL_MASK, sing);
-    __syncwarp();
+    sing = __syncthreads_or(sing);
     if (sing) {
-      if (lane == 0) {
+      if (tid == 0) {
         state[mat] = 3;
         active[mat] = 0;
         berr[mat] = __longlong_as_double(0x7FF8000000000000LL);
@@ -282,9 +288,10 @@ __global__ void mx_refine_kernel(const double* a, const double* b, double* x, co
       }
       return;
     }
-    mx_lu_solve_warp(LU, IP, n, v);
-    for (int i = lane; i < n; i += 32) X[i] = (double)v[i];
-    if (lane == 0) {
+    if (warp == 0) mx_lu_solve_warp(LU, IP, n, v);
+    __syncthreads();
+    for (int i = tid; i < n; i += MX_RT) X[i] = (double)v[i];
+    if (tid == 0) {
       state[mat] = 0;
       iters[mat] = 0;
       berr[mat] = __longlong_as_double(0x7FF0000000000000LL);
@@ -292,36 +299,38 @@ __global__ void mx_refine_kernel(const double* a, const double* b, double* x, co
     return;
   }
   if (measure ? state[mat] == 0 : state[mat] != 0) return;
+  for (int j = tid; j < n; j += MX_RT) sx[j] = X[j];
+  __syncthreads();
   // r = b - A x, with |A|_inf accumulated on the first sweep.
-  constexpr int R = 32;  // rows per lane held in registers (n <= 1024)
-  double r[R], rs[R];
-  const int per = (n + 31) / 32;
+  const bool rowsums = iter == 0 || measure;
+  double r[MX_RROWS], rs[MX_RROWS];
 #pragma unroll
-  for (int q = 0; q < R; ++q) {
-    const int i = lane + 32 * q;
-    r[q] = (q < per && i < n) ? B[i] : 0.0;
+  for (int q = 0; q < MX_RROWS; ++q) {
+    const int i = tid + MX_RT * q;
+    r[q] = i < n ? B[i] : 0.0;
     rs[q] = 0.0;
   }
+#pragma unroll 4
   for (int j = 0; j < n; ++j) {
-    const double xj = X[j];
+    const double xj = sx[j];
     const double* col = A + (long long)j * n;
 #pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const int i = lane + 32 * q;
-      if (q < per && i < n) {
+    for (int q = 0; q < MX_RROWS; ++q) {
+      const int i = tid + MX_RT * q;
+      if (i < n) {
         const double aij = col[i];
         r[q] = fma(-aij, xj, r[q]);
-        if (iter == 0 || measure) rs[q] += fabs(aij);
+        if (rowsums) rs[q] += fabs(aij);
       }
     }
   }
   double rn = 0.0, xn = 0.0, bn = 0.0, an = 0.0;
 #pragma unroll
-  for (int q = 0; q < R; ++q) {
-    const int i = lane + 32 * q;
-    if (q < per && i < n) {
+  for (int q = 0; q < MX_RROWS; ++q) {
+    const int i = tid + MX_RT * q;
+    if (i < n) {
       rn = fmax(rn, fabs(r[q]));
-      xn = fmax(xn, fabs(X[i]));
+      xn = fmax(xn, fabs(sx[i]));
       bn = fmax(bn, fabs(B[i]));
       an = fmax(an, rs[q]);
     }
@@ -332,38 +341,52 @@ __global__ void mx_refine_kernel(const double* a, const double* b, double* x, co
     bn = fmax(bn, __shfl_xor_sync(FULL_MASK, bn, off));
     an = fmax(an, __shfl_xor_sync(FULL_MASK, an, off));
   }
-  if (iter == 0 && lane == 0) anorm[mat] = an;
-  __syncwarp();
-  const double An = (iter == 0 || measure) ? an : anorm[mat];
-  const double be = rn / (An * xn + bn);
-  if (measure) {
-    if (lane == 0) berr[mat] = be;
-    return;
-  }
-  const double prev = berr[mat];
-  int st = 0;
-  if (!(be == be)) st = 2;                 // NaN: diverged
-  else if (be <= tol) st = 1;
-  else if (iter >= 2 && be > 0.5 * prev) st = 2;
   if (lane == 0) {
-    berr[mat] = be;
-    iters[mat] = iter;
+    red[0][warp] = rn;
+    red[1][warp] = xn;
+    red[2][warp] = bn;
+    red[3][warp] = an;
   }
-  if (st != 0) {
-    if (lane == 0) {
-      state[mat] = st;
-      active[mat] = 0;
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < MX_RT / 32; ++w) {
+      rn = fmax(rn, red[0][w]);
+      xn = fmax(xn, red[1][w]);
+      bn = fmax(bn, red[2][w]);
+      an = fmax(an, red[3][w]);
     }
-    return;
+    if (iter == 0) anorm[mat] = an;
+    const double An = rowsums ? an : anorm[mat];
+    const double be = rn / (An * xn + bn);
+    int st = 0;
+    if (measure) {
+      berr[mat] = be;
+      st = -1;
+    } else {
+      const double prev = berr[mat];
+      if (!(be == be)) st = 2;                 // NaN: diverged
+      else if (be <= tol) st = 1;
+      else if (iter >= 2 && be > 0.5 * prev) st = 2;
+      berr[mat] = be;
+      iters[mat] = iter;
+      if (st != 0) {
+        state[mat] = st;
+        active[mat] = 0;
+      }
+    }
+    verdict = st;
   }
+  __syncthreads();
+  if (verdict != 0) return;
 #pragma unroll
-  for (int q = 0; q < R; ++q) {
-    const int i = lane + 32 * q;
-    if (q < per && i < n) v[i] = (float)r[q];
+  for (int q = 0; q < MX_RROWS; ++q) {
+    const int i = tid + MX_RT * q;
+    if (i < n) v[i] = (float)r[q];
   }
-  __syncwarp();
-  mx_lu_solve_warp(LU, IP, n, v);
-  for (int i = lane; i < n; i += 32) X[i] += (double)v[i];
+  __syncthreads();
+  if (warp == 0) mx_lu_solve_warp(LU, IP, n, v);
+  __syncthreads();
+  for (int i = tid; i < n; i += MX_RT) X[i] = sx[i] + (double)v[i];
 }
 
 cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t s) {
@@ -373,14 +396,15 @@ cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t 
 
 cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
                      cudaStream_t s) {
-  const size_t smem = sizeof(float) * (size_t)(n - k) * MX_NB;
+  const size_t smem = sizeof(float) * ((size_t)(n - k) * MX_NB + (size_t)MX_NB * MX_THREADS);
   mx_panel_kernel<<<count, MX_THREADS, smem, s>>>(a32, n, k, ipiv, active);
   return cudaGetLastError();
 }
 
 cudaError_t mx_panel_attr(int nmax) {
-  return cudaFuncSetAttribute(mx_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(sizeof(float) * (size_t)nmax * MX_NB));
+  return cudaFuncSetAttribute(
+      mx_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      (int)(sizeof(float) * ((size_t)nmax * MX_NB + (size_t)MX_NB * MX_THREADS)));
 }
 
 cudaError_t mx_update_fp32(float* a32, int n, int k, const int* active, int count,
@@ -405,10 +429,9 @@ cudaError_t mx_bf16_operands(const float* a32, int n, int k, void* l21, void* u1
 cudaError_t mx_refine(const double* a, const double* b, double* x, const float* lu,
                       const int* ipiv, int n, int count, int iter, double tol, double* berr,
                       int* iters, int* state, double* anorm, int* active, cudaStream_t s) {
-  const int wpb = 4;
-  const size_t smem = sizeof(float) * (size_t)n * wpb;
-  mx_refine_kernel<<<(count + wpb - 1) / wpb, 32 * wpb, smem, s>>>(
-      a, b, x, lu, ipiv, n, count, iter, tol, berr, iters, state, anorm, active);
+  const size_t smem = sizeof(double) * (size_t)n + sizeof(float) * (size_t)n;
+  mx_refine_kernel<<<count, MX_RT, smem, s>>>(a, b, x, lu, ipiv, n, count, iter, tol, berr,
+                                              iters, state, anorm, active);
   return cudaGetLastError();
 }
 
