@@ -1781,6 +1781,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   mfg_plan_destroy(tp);
   if (rc != MFG_OK) return rc;
   if (ce != cudaSuccess) return cuda_fail(ctx, ce, "autotune");
+  pipe_release(plan);  // host-buffer chunk plans are rebuilt with the new shape on next use
   rc = plan_reshape(plan, best[0], best[1], best[2], best[3], best[4]);
   if (rc != MFG_OK) return rc;
   ctx->tune[tune_key((int)plan->kind, plan->max_n, plan->count)] = best;
