@@ -207,6 +207,19 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k,
  * 174-182) and the upper solve (Blas.SolveTriangular.cs:191-199), for the plan's nrhs (>= 1)
  * right-hand sides; bit-identical to the fused path.  a and piv are read only. */
 MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b);
+/* The float and Complex overloads of the batched factor + solve and of the solve alone, on the
+ * same plan (offsets count elements of the type; Complex arrays are interleaved (re, im) doubles,
+ * element e at doubles 2e and 2e+1).  Bit-identical to Factorization.Lu's float / Complex
+ * overloads (MatFlat/Factorization.Lu.cs:240-294 float, :352-406 Complex: float storage with
+ * double dot sums; Complex pivots by FastMagnitude) followed by the unit-lower and upper
+ * SolveTriangular of the same type (MatFlat/Blas.SolveTriangular.cs:44-124 float, :280-395
+ * Complex).  sign, info and piv as in mfg_dgetrf_batched. */
+MFG_API int mfg_sgetrf_batched(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
+                               int* info);
+MFG_API int mfg_zgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                               int* info);
+MFG_API int mfg_sgetrs_batched(mfg_plan* plan, const float* a, const int* piv, float* b);
+MFG_API int mfg_zgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b);
 
 /* Cholesky of every matrix (Factorization.Cholesky), then, when nrhs > 0, L y = b
  * (SolveTriangular Lower/NoTrans) and L^T x = y (SolveTriangular Lower/Trans) per right-hand

@@ -73,6 +73,10 @@ _SIGS = {
     "mfg_dgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_logdet_solve_grad_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_sgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_zgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_sgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dpotrs_batched": (_I, [_vp, _vp, _vp]),
     "mfg_dgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -394,6 +398,22 @@ def _dptr(x):
     return _vp(x.data_ptr())
 
 
+def _elem(a, dtype=None):
+    """BLAS prefix of a batched call: "d", "s" or "z" from `dtype` or from a's element type."""
+    if dtype is not None:
+        if dtype not in ("d", "s", "z"):
+            raise ValueError("dtype must be 'd', 's' or 'z'")
+        return dtype
+    name = str(getattr(a, "dtype", "float64")).replace("torch.", "")
+    if name == "float32":
+        return "s"
+    if name == "complex128":
+        return "z"
+    if name == "float64":
+        return "d"
+    raise TypeError("unsupported element type %s (float64, float32 or complex128)" % name)
+
+
 class _Batch:
     def __init__(self, ctx, handle):
         self.ctx = ctx
@@ -455,10 +475,14 @@ class LuBatch(_Batch):
         self.count = len(self._n)
         self.nrhs = nrhs
 
-    def run(self, a, piv, b, sign, info):
-        rc = self.ctx.lib.mfg_dgetrf_batched(self.h, _dptr(a), _dptr(piv), _dptr(b), _dptr(sign),
-                                             _dptr(info))
-        self.ctx.check(rc, "mfg_dgetrf_batched")
+    def run(self, a, piv, b, sign, info, dtype=None):
+        """Factor (+ solve) device buffers.  The element type follows a's dtype (float64,
+        float32 or complex128 tensors: MatFlat's double, float and Complex overloads); pass
+        dtype="z" for Complex data held as interleaved float64."""
+        name = "mfg_%sgetrf_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(piv), _dptr(b), _dptr(sign),
+                                         _dptr(info))
+        self.ctx.check(rc, name)
 
     def run_host(self, a, piv, b, sign, info):
         """Factor + solve on host buffers (numpy arrays or CPU tensors, page-locked for full
@@ -467,10 +491,12 @@ class LuBatch(_Batch):
                                                   _hptr(sign), _hptr(info))
         self.ctx.check(rc, "mfg_dgetrf_batched_host")
 
-    def solve(self, a, piv, b):
-        """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b)."""
-        rc = self.ctx.lib.mfg_dgetrs_batched(self.h, _dptr(a), _dptr(piv), _dptr(b))
-        self.ctx.check(rc, "mfg_dgetrs_batched")
+    def solve(self, a, piv, b, dtype=None):
+        """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b);
+        element type as in `run`."""
+        name = "mfg_%sgetrs_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(piv), _dptr(b))
+        self.ctx.check(rc, name)
 
 
 class StridedBlas:

@@ -149,8 +149,11 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
 // Solves A x = b for nr right-hand sides from the factors of one square matrix:
 // b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
 // upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
-__device__ void getrs_warp(const double* lu, int n, long long lda, const int* piv, double* b,
-                           long long ldb, int nrhs, double* xs, double* acc) {
+// S: the solve arithmetic of the element type (DSolve, SSolve or ZSolve<false>).
+template <class S = DSolve>
+__device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const int* piv,
+                           typename S::T* b, long long ldb, int nrhs, typename S::T* xs,
+                           typename S::Acc* acc) {
   const int lane = threadIdx.x & 31;
   const int ldx = n | 1;
   for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
@@ -161,8 +164,8 @@ __device__ void getrs_warp(const double* lu, int n, long long lda, const int* pi
       xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + piv[i]];
     }
     __syncwarp();
-    warp_solve_dot(lu, n, 1, lda, true, xs, ldx, acc, nr);
-    warp_solve_sweep(lu, n, lda, 1, xs, ldx, nr);
+    warp_solve_dot<32, S>(lu, n, 1, lda, true, xs, ldx, acc, nr);
+    warp_solve_sweep<32, S>(lu, n, lda, 1, xs, ldx, nr);
     for (int e = lane; e < nr * n; e += 32) {
       const int r = e / n;
       const int i = e - r * n;
@@ -198,6 +201,47 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
                  scr + n + RHS_CHUNK * ldx);
+    if (lane == 0 && !p.solve_only) {
+      p.sign[mat] = sign;
+      p.info[mat] = info;
+    }
+    __syncwarp();
+  }
+}
+
+// The float and Complex overloads of the batched LU + solve.  Same schedule as the double kernel;
+// the per-warp scratch (column sums, staged right-hand sides and their accumulators) takes
+// W = sizeof(Acc)/8 times the double kernel's doubles: 1 for float (float storage, double sums),
+// 2 for Complex.  a and b are the typed arrays behind args.a / args.b; offsets count elements.
+template <int WARPS, class Tr, class S>
+__global__ void __launch_bounds__(WARPS * 32) getrf_batched_t_kernel(BatchArgs p) {
+  using T = typename Tr::T;
+  using Acc = typename Tr::Acc;
+  constexpr int W = sizeof(Acc) / sizeof(double);
+  extern __shared__ double sm_dyn[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  T* abase = reinterpret_cast<T*>(p.a);
+  T* bbase = reinterpret_cast<T*>(p.b);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    T* a = abase + p.a_off[mat];
+    int* piv = p.piv + p.piv_off[mat];
+    double* scr = (n <= SMEM_N) ? sm_dyn + warp * W * SMEM_WARP_DOUBLES
+                                 : p.gscratch + gw * p.gscratch_stride;
+    const int ldx = n | 1;
+    int sign = 1, info = 0;
+    if (!p.solve_only) lu_warp<Tr, 1, DOT_BLOCK>(a, n, n, lda, piv, (Acc*)scr, sign, info);
+    if (p.nrhs > 0)
+      getrs_warp<S>(a, n, lda, piv, bbase + p.b_off[mat], n, p.nrhs, (T*)(scr + W * n),
+                    (Acc*)(scr + W * n + W * RHS_CHUNK * ldx));
     if (lane == 0 && !p.solve_only) {
       p.sign[mat] = sign;
       p.info[mat] = info;
@@ -247,10 +291,64 @@ static cudaError_t set_getrf_attr() {
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// Float / Complex overloads: at most 8 warps per CTA (a Complex warp keeps 18.6 KB of shared
+// scratch); a plan shaped with 16 warps per CTA launches twice the CTAs of 8 warps, so the warp
+// count, and with it the global-scratch slices, stay the same.
+constexpr int GETRF_T_MAX_WARPS = 8;
+
+template <int WARPS, class Tr, class S>
+static cudaError_t launch_getrf_t_w(const BatchArgs& args, int ctas, cudaStream_t s) {
+  constexpr int W = sizeof(typename Tr::Acc) / sizeof(double);
+  const size_t smem = sizeof(double) * W * SMEM_WARP_DOUBLES * WARPS;
+  getrf_batched_t_kernel<WARPS, Tr, S><<<ctas, WARPS * 32, smem, s>>>(args);
+  return cudaGetLastError();
+}
+
+template <class Tr, class S>
+static cudaError_t launch_getrf_t(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  if (warps > GETRF_T_MAX_WARPS) {
+    ctas *= warps / GETRF_T_MAX_WARPS;
+    warps = GETRF_T_MAX_WARPS;
+  }
+  switch (warps) {
+    case 1: return launch_getrf_t_w<1, Tr, S>(args, ctas, s);
+    case 2: return launch_getrf_t_w<2, Tr, S>(args, ctas, s);
+    case 4: return launch_getrf_t_w<4, Tr, S>(args, ctas, s);
+    case 8: return launch_getrf_t_w<8, Tr, S>(args, ctas, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int WARPS, class Tr, class S>
+static cudaError_t set_getrf_t_attr() {
+  constexpr int W = sizeof(typename Tr::Acc) / sizeof(double);
+  const size_t smem = sizeof(double) * W * SMEM_WARP_DOUBLES * WARPS;
+  return cudaFuncSetAttribute(getrf_batched_t_kernel<WARPS, Tr, S>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <class Tr, class S>
+static cudaError_t set_getrf_t_attrs() {
+  cudaError_t e;
+  if ((e = set_getrf_t_attr<1, Tr, S>()) != cudaSuccess) return e;
+  if ((e = set_getrf_t_attr<2, Tr, S>()) != cudaSuccess) return e;
+  if ((e = set_getrf_t_attr<4, Tr, S>()) != cudaSuccess) return e;
+  return set_getrf_t_attr<8, Tr, S>();
+}
+
+cudaError_t launch_sgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  return launch_getrf_t<STraits, SSolve>(args, ctas, warps, s);
+}
+cudaError_t launch_zgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  return launch_getrf_t<ZTraits, ZSolve<false>>(args, ctas, warps, s);
+}
+
 // Raises the dynamic shared-memory limit of every variant; called once per device, outside any
 // stream capture.
 cudaError_t init_getrf_attributes() {
   cudaError_t e;
+  if ((e = set_getrf_t_attrs<STraits, SSolve>()) != cudaSuccess) return e;
+  if ((e = set_getrf_t_attrs<ZTraits, ZSolve<false>>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<1>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<2>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<4>()) != cudaSuccess) return e;

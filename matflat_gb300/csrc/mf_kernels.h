@@ -158,6 +158,11 @@ cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s
 
 // Batched LU (+ solve); launched persistent: grid = ctas, WARPS warps per CTA.
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+// Float and Complex overloads of the batched LU (+ solve): args.a / args.b point at float or
+// interleaved (re, im) double arrays, offsets count elements; per-warp global scratch (orders
+// above SMEM_N) of getrf_t_scratch_doubles(max n, elem) doubles.
+cudaError_t launch_sgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+cudaError_t launch_zgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 // Batched Cholesky (+ two triangular solves).
 cudaError_t launch_potrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 

@@ -83,6 +83,7 @@ struct mfg_plan {
   mfg::QrBatchArgs<float> qs{};
   mfg::GevdArgs gv{};  // GEVD: the front half of the generalized eigenproblem
   int qr_float = 0;  // GEQRF: which precision the next launch runs
+  int elem = 0;      // GETRF: element type of the next launch (0 double, 1 float, 2 Complex)
   int mx_n = 0;      // MIXED: order of every matrix
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
   int ctas = 0;
@@ -112,7 +113,7 @@ struct mfg_plan {
   } pipe;
   // CUDA graph of the last execution (keyed by the data pointers and the stream).
   cudaGraphExec_t exec = nullptr;
-  const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  const void* key[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -289,7 +290,11 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
-  if (p->kind == mfg_plan::GETRF)
+  if (p->kind == mfg_plan::GETRF && p->elem == 1)
+    e = mfg::launch_sgetrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::GETRF && p->elem == 2)
+    e = mfg::launch_zgetrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::GETRF)
     e = mfg::launch_getrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::GETRI)
     e = mfg::launch_getri_batched(p->args, p->ctas, s);
@@ -307,14 +312,15 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
 
 // Replays the plan's CUDA graph, capturing it first when the data pointers or the stream changed.
 // The legacy default stream cannot be captured; on it the plan launches directly.
+// GETRF plans add their element type to the key.
 int plan_execute(mfg_plan* p, const void* k0, const void* k1, const void* k2, const void* k3,
                  const void* k4) {
   mfg_ctx* ctx = p->ctx;
   cudaStream_t s = ctx->stream;
   if (!ctx->use_graphs || s == nullptr || s == cudaStreamLegacy) return plan_launch(p, s);
-  const void* key[6] = {k0, k1, k2, k3, k4, (const void*)s};
+  const void* key[7] = {k0, k1, k2, k3, k4, (const void*)s, (const void*)(intptr_t)p->elem};
   bool hit = p->exec != nullptr;
-  for (int i = 0; i < 6 && hit; i++) hit = (key[i] == p->key[i]);
+  for (int i = 0; i < 7 && hit; i++) hit = (key[i] == p->key[i]);
   if (!hit) {
     if (p->exec) {
       cudaGraphExecDestroy(p->exec);
@@ -335,7 +341,7 @@ int plan_execute(mfg_plan* p, const void* k0, const void* k1, const void* k2, co
       p->exec = nullptr;
       return cuda_fail(ctx, ee, "cudaGraphInstantiate");
     }
-    for (int i = 0; i < 6; i++) p->key[i] = key[i];
+    for (int i = 0; i < 7; i++) p->key[i] = key[i];
   }
   MFG_CUDA(ctx, cudaGraphLaunch(p->exec, s));
   return MFG_OK;
@@ -1802,8 +1808,41 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   return MFG_OK;
 }
 
-MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
-                               int* info) {
+}  // extern "C"
+
+namespace {
+
+// Points a GETRF plan at the element type of the next launch.  Orders above SMEM_N keep their
+// per-warp vectors in the plan's global scratch; Complex needs twice the doubles of double and
+// float, so its first launch grows the scratch (after the stream drains: it may be in use).
+int getrf_set_elem(mfg_plan* p, int elem) {
+  mfg_ctx* ctx = p->ctx;
+  p->elem = elem;
+  if (p->max_n <= mfg::SMEM_N) return MFG_OK;
+  const long long base = (mfg::warp_scratch_doubles(p->max_n) + 31) / 32 * 32;
+  const long long stride = elem == 2 ? 2 * base : base;
+  const size_t need = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+  if (need > p->scratch.bytes) {
+    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MFG_CUDA(ctx, p->scratch.reserve(need));
+    if (p->exec) {
+      cudaGraphExecDestroy(p->exec);
+      p->exec = nullptr;
+    }
+  }
+  if (p->args.gscratch != (double*)p->scratch.ptr || p->args.gscratch_stride != stride) {
+    p->args.gscratch = (double*)p->scratch.ptr;
+    p->args.gscratch_stride = stride;
+    if (p->exec) {
+      cudaGraphExecDestroy(p->exec);
+      p->exec = nullptr;
+    }
+  }
+  return MFG_OK;
+}
+
+int getrf_batched_any(mfg_plan* plan, int elem, void* a, int* piv, void* b, int* sign,
+                      int* info) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
@@ -1814,16 +1853,18 @@ MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, i
     if (!sign) return fail(ctx, -5, "sign is null");
     if (!info) return fail(ctx, -6, "info is null");
   }
-  plan->args.a = a;
+  const int rc = getrf_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->args.a = (double*)a;
   plan->args.piv = piv;
-  plan->args.b = b;
+  plan->args.b = (double*)b;
   plan->args.sign = sign;
   plan->args.info = info;
   plan->args.solve_only = 0;
   return plan_execute(plan, a, piv, b, sign, info);
 }
 
-MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+int getrs_batched_any(mfg_plan* plan, int elem, const void* a, const int* piv, void* b) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
@@ -1833,13 +1874,43 @@ MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, 
     if (!piv) return fail(ctx, -3, "piv is null");
     if (!b) return fail(ctx, -4, "b is null");
   }
-  plan->args.a = const_cast<double*>(a);
+  const int rc = getrf_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->args.a = (double*)const_cast<void*>(a);
   plan->args.piv = const_cast<int*>(piv);
-  plan->args.b = b;
+  plan->args.b = (double*)b;
   plan->args.sign = nullptr;
   plan->args.info = nullptr;
   plan->args.solve_only = 1;
   return plan_execute(plan, a, piv, b, nullptr, (const void*)3);
+}
+
+}  // namespace
+
+extern "C" {
+
+MFG_API int mfg_sgetrf_batched(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
+                               int* info) {
+  return getrf_batched_any(plan, 1, a, piv, b, sign, info);
+}
+MFG_API int mfg_zgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                               int* info) {
+  return getrf_batched_any(plan, 2, a, piv, b, sign, info);
+}
+MFG_API int mfg_sgetrs_batched(mfg_plan* plan, const float* a, const int* piv, float* b) {
+  return getrs_batched_any(plan, 1, a, piv, b);
+}
+MFG_API int mfg_zgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+  return getrs_batched_any(plan, 2, a, piv, b);
+}
+
+MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                               int* info) {
+  return getrf_batched_any(plan, 0, a, piv, b, sign, info);
+}
+
+MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+  return getrs_batched_any(plan, 0, a, piv, b);
 }
 
 }  // extern "C"

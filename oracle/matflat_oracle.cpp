@@ -902,6 +902,47 @@ void orc_dlu_solve(int n, const double* lu, int lda, const int* piv, int nrhs, d
   }
 }
 
+// The same solve for the float and Complex overloads (MatFlat's float / Complex SolveTriangular;
+// Complex arrays are interleaved (re, im) doubles).
+void orc_slu_solve(int n, const float* lu, int lda, const int* piv, int nrhs, float* b, int ldb) {
+  std::vector<float> l((size_t)n * n);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) l[(size_t)j * n + i] = lu[(long)lda * j + i];
+  for (int j = 0; j < n; j++) l[(size_t)j * n + j] = 1.0f;
+  std::vector<float> tmp(n);
+  for (int r = 0; r < nrhs; r++) {
+    float* x = b + (long)ldb * r;
+    for (int i = 0; i < n; i++) tmp[i] = x[piv[i]];
+    std::memcpy(x, tmp.data(), sizeof(float) * n);
+    orc_strsv(LOWER, NOTRANS, n, l.data(), n, x, 1);
+    orc_strsv(UPPER, NOTRANS, n, lu, lda, x, 1);
+  }
+}
+void orc_zlu_solve(int n, const double* lu, int lda, const int* piv, int nrhs, double* b,
+                   int ldb) {
+  std::vector<double> l((size_t)2 * n * n);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) {
+      l[2 * ((size_t)j * n + i)] = lu[2 * ((long)lda * j + i)];
+      l[2 * ((size_t)j * n + i) + 1] = lu[2 * ((long)lda * j + i) + 1];
+    }
+  for (int j = 0; j < n; j++) {
+    l[2 * ((size_t)j * n + j)] = 1.0;
+    l[2 * ((size_t)j * n + j) + 1] = 0.0;
+  }
+  std::vector<double> tmp((size_t)2 * n);
+  for (int r = 0; r < nrhs; r++) {
+    double* x = b + (long)2 * ldb * r;
+    for (int i = 0; i < n; i++) {
+      tmp[2 * i] = x[2 * piv[i]];
+      tmp[2 * i + 1] = x[2 * piv[i] + 1];
+    }
+    std::memcpy(x, tmp.data(), sizeof(double) * 2 * n);
+    orc_ztrsv(LOWER, NOTRANS, n, l.data(), n, x, 1);
+    orc_ztrsv(UPPER, NOTRANS, n, lu, lda, x, 1);
+  }
+}
+
 // Least squares min ||A x - b|| for one tall matrix (m >= n), composed from MatFlat's own
 // routines since MatFlat has no QR solve: Qr, QrOrthogonalFactor, MulMatVec(Trans) for Q^T b,
 // QrUpperTriangularFactor, SolveTriangular(Upper, NoTrans).  a is overwritten by the QR factors;
@@ -1060,6 +1101,27 @@ void orc_dgevd_front_batched(long count, const int* n, const int64_t* a_off, con
                              const int64_t* b_off, double* b, double* c, int* info, int nthreads) {
   parallel_for(count, nthreads, [&](long i) {
     info[i] = orc_dgevd_front(n[i], a + a_off[i], n[i], b + b_off[i], n[i], c + a_off[i]);
+  });
+}
+
+// Float and Complex overloads of the batched LU + solve (offsets in elements of the type).
+void orc_slu_solve_batched(long count, const int* n, const int64_t* a_off, float* a,
+                           const int64_t* piv_off, int* piv, const int64_t* b_off, float* b,
+                           int nrhs, int* sign, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    sign[i] = orc_slu(ni, ni, a + a_off[i], ni, piv + piv_off[i]);
+    if (nrhs > 0) orc_slu_solve(ni, a + a_off[i], ni, piv + piv_off[i], nrhs, b + b_off[i], ni);
+  });
+}
+void orc_zlu_solve_batched(long count, const int* n, const int64_t* a_off, double* a,
+                           const int64_t* piv_off, int* piv, const int64_t* b_off, double* b,
+                           int nrhs, int* sign, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    double* ai = a + 2 * a_off[i];
+    sign[i] = orc_zlu(ni, ni, ai, ni, piv + piv_off[i]);
+    if (nrhs > 0) orc_zlu_solve(ni, ai, ni, piv + piv_off[i], nrhs, b + 2 * b_off[i], ni);
   });
 }
 

@@ -59,6 +59,8 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_slu_solve_batched": (None, [_L, _i, _l, _f, _l, _i, _l, _f, _I, _i, _I]),
+            "orc_zlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
             "orc_ddot": (ctypes.c_double, [_I, _d, _I, _d, _I]),
             "orc_dnrm2": (ctypes.c_double, [_I, _d, _I]),
             "orc_dger": (None, [_I, _I, _d, _I, _d, _I, _d, _I]),
@@ -173,10 +175,11 @@ def chol_solve_batched(n, a_off, a, b_off, b, info, nthreads=1):
 
 
 def lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, nthreads=1):
-    lib().orc_dlu_solve_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
-                                _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int),
-                                _p(b_off, ctypes.c_int64), _fp(b), nrhs,
-                                _p(sign, ctypes.c_int), nthreads)
+    """Batched LU + solve; a (and b) float64, float32 or complex128 select the overload."""
+    fn = getattr(lib(), "orc_%slu_solve_batched" % _pre(a))
+    fn(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+       _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int), _p(b_off, ctypes.c_int64), _fp(b), nrhs,
+       _p(sign, ctypes.c_int), nthreads)
 
 
 def lu_inverse_batched(n, a_off, a, piv_off, piv, info, nthreads=1):
