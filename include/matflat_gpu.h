@@ -233,6 +233,16 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
  * (Blas.SolveTriangular Lower/NoTrans then Lower/Trans, Blas.SolveTriangular.cs:215-238) for the
  * plan's nrhs (>= 1) right-hand sides. */
 MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b);
+/* The float and Complex overloads on the same plan (offsets count elements; Complex arrays are
+ * interleaved (re, im) doubles).  Bit-identical to Factorization.Cholesky's float / Complex
+ * overloads (MatFlat/Factorization.Cholesky.cs:33-87, :195-249; Complex A = L L^H with a real
+ * diagonal) followed by SolveTriangular of the same type: Lower/NoTrans, then Lower/Trans (float)
+ * or Lower/ConjTrans (Complex) (MatFlat/Blas.SolveTriangular.cs:44-124, :280-395).  One warp per
+ * matrix whatever the plan's lanes per matrix; info as in mfg_dpotrf_batched. */
+MFG_API int mfg_spotrf_batched(mfg_plan* plan, float* a, float* b, int* info);
+MFG_API int mfg_zpotrf_batched(mfg_plan* plan, double* a, double* b, int* info);
+MFG_API int mfg_spotrs_batched(mfg_plan* plan, const float* a, float* b);
+MFG_API int mfg_zpotrs_batched(mfg_plan* plan, const double* a, double* b);
 
 /* Strided batches of MatFlat's vector building blocks (device pointers, asynchronous on the
  * context's stream; item b of every operand at base + b*stride), in MatFlat's arithmetic:

@@ -74,6 +74,10 @@ _SIGS = {
     "mfg_dpotrf_logdet_solve_grad_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_spotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_spotrs_batched": (_I, [_vp, _vp, _vp]),
+    "mfg_zpotrs_batched": (_I, [_vp, _vp, _vp]),
     "mfg_zgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_sgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_zgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -625,9 +629,13 @@ class CholeskyBatch(_Batch):
         self.count = len(self._n)
         self.nrhs = nrhs
 
-    def run(self, a, b, info):
-        rc = self.ctx.lib.mfg_dpotrf_batched(self.h, _dptr(a), _dptr(b), _dptr(info))
-        self.ctx.check(rc, "mfg_dpotrf_batched")
+    def run(self, a, b, info, dtype=None):
+        """Factor (+ solve) device buffers; the element type follows a's dtype (float64,
+        float32, complex128; dtype="z" for Complex held as interleaved float64).  Complex
+        solves L y = b, then L^H x = y."""
+        name = "mfg_%spotrf_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(b), _dptr(info))
+        self.ctx.check(rc, name)
 
     def run_host(self, a, b, info):
         """Factor + solve on host arrays, copies pipelined with compute.  Synchronous."""
@@ -641,10 +649,12 @@ class CholeskyBatch(_Batch):
             1 if keep_factor else 0)
         self.ctx.check(rc, "mfg_dpotrf_logdet_solve_grad_batched_host")
 
-    def solve(self, a, b):
-        """Solves with Cholesky factors already in a (the plan's nrhs columns of b)."""
-        rc = self.ctx.lib.mfg_dpotrs_batched(self.h, _dptr(a), _dptr(b))
-        self.ctx.check(rc, "mfg_dpotrs_batched")
+    def solve(self, a, b, dtype=None):
+        """Solves with Cholesky factors already in a (the plan's nrhs columns of b); element
+        type as in `run`."""
+        name = "mfg_%spotrs_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(b))
+        self.ctx.check(rc, name)
 
     def loss_and_grad(self, k, y, loss, grad, info, keep_factor=True):
         """loss = y^T K^-1 y + log det K and grad = K^-1 - alpha alpha^T per matrix; y becomes

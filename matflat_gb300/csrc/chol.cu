@@ -582,19 +582,15 @@ namespace mfg {
 // Float overload of Factorization.Cholesky (MatFlat/Factorization.Cholesky.cs:33-87): float
 // storage; t = ((double)A(k,j) - Dot) / (double)L(k,k) in double, stored as (float)t; the
 // diagonal sum s += t*t stays in double with the unrounded t; L(j,j) = (float)sqrt(s).
-__global__ void __launch_bounds__(32) spotrf_single_kernel(float* a, int n, int lda, int* out1,
-                                                           double* dsum) {
+// One warp per matrix; dsum: n doubles.  Returns 0, or k+1 (not positive definite at column k).
+__device__ int spotrf_warp(float* a, int n, long long lda, double* dsum) {
   const int lane = threadIdx.x & 31;
   for (int j = lane; j < n; j += 32) dsum[j] = 0.0;
   __syncwarp();
-  int info = 0;
-  for (int k = 0; k < n && info == 0; ++k) {
+  for (int k = 0; k < n; ++k) {
     float* colk = a + (long long)k * lda;
     const double s = __dsub_rn((double)colk[k], dsum[k]);
-    if (!positive(s)) {
-      info = k + 1;
-      break;
-    }
+    if (!positive(s)) return k + 1;  // uniform across the warp
     const float lkk = __double2float_rn(__dsqrt_rn(s));
     __syncwarp();
     if (lane == 0) colk[k] = lkk;
@@ -606,28 +602,22 @@ __global__ void __launch_bounds__(32) spotrf_single_kernel(float* a, int n, int 
     }
     __syncwarp();
   }
-  if (info == 0) {
-    for (int c = 1; c < n; ++c)
-      for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = 0.0f;
-  }
-  if (lane == 0) out1[0] = info;
+  for (int c = 1; c < n; ++c)
+    for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = 0.0f;
+  __syncwarp();
+  return 0;
 }
 
 // Complex overload (Factorization.Cholesky.cs:195-249): t = (A(k,j) - DotConj(L(j,:), L(k,:)))
 // / L(k,k); L(j,k) = conj(t); s += t.re^2 + t.im^2; L(j,j) = Complex(sqrt(A(j,j).re - s), 0).
-__global__ void __launch_bounds__(32) zpotrf_single_kernel(zdouble* a, int n, int lda, int* out1,
-                                                           double* dsum) {
+__device__ int zpotrf_warp(zdouble* a, int n, long long lda, double* dsum) {
   const int lane = threadIdx.x & 31;
   for (int j = lane; j < n; j += 32) dsum[j] = 0.0;
   __syncwarp();
-  int info = 0;
   for (int k = 0; k < n; ++k) {
     zdouble* colk = a + (long long)k * lda;
     const double s = __dsub_rn(colk[k].re, dsum[k]);
-    if (!positive(s)) {
-      info = k + 1;
-      break;
-    }
+    if (!positive(s)) return k + 1;
     const zdouble lkk = zmake(__dsqrt_rn(s), 0.0);
     __syncwarp();
     if (lane == 0) colk[k] = lkk;
@@ -639,11 +629,159 @@ __global__ void __launch_bounds__(32) zpotrf_single_kernel(zdouble* a, int n, in
     }
     __syncwarp();
   }
-  if (info == 0) {
-    for (int c = 1; c < n; ++c)
-      for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = zmake(0.0, 0.0);
+  for (int c = 1; c < n; ++c)
+    for (int r = lane; r < c; r += 32) a[(long long)c * lda + r] = zmake(0.0, 0.0);
+  __syncwarp();
+  return 0;
+}
+
+__global__ void __launch_bounds__(32) spotrf_single_kernel(float* a, int n, int lda, int* out1,
+                                                           double* dsum) {
+  const int info = spotrf_warp(a, n, lda, dsum);
+  if (threadIdx.x == 0) out1[0] = info;
+}
+
+__global__ void __launch_bounds__(32) zpotrf_single_kernel(zdouble* a, int n, int lda, int* out1,
+                                                           double* dsum) {
+  const int info = zpotrf_warp(a, n, lda, dsum);
+  if (threadIdx.x == 0) out1[0] = info;
+}
+
+// Element types of the batched float / Complex Cholesky: the factorization, and the solve
+// arithmetic of L y = b (Lower/NoTrans, dot form) and of L^T x = y (float, Lower/Trans) or
+// L^H x = y (Complex, Lower/ConjTrans), both column sweeps over the rows of L.
+struct SChol {
+  using T = float;
+  using Fwd = SSolve;
+  using Bwd = SSolve;
+  static __device__ __forceinline__ int factor(T* a, int n, long long lda, double* dsum) {
+    return spotrf_warp(a, n, lda, dsum);
   }
-  if (lane == 0) out1[0] = info;
+};
+struct ZChol {
+  using T = zdouble;
+  using Fwd = ZSolve<false>;
+  using Bwd = ZSolve<true>;
+  static __device__ __forceinline__ int factor(T* a, int n, long long lda, double* dsum) {
+    return zpotrf_warp(a, n, lda, dsum);
+  }
+};
+
+constexpr int SMEM_WARP_DOUBLES_T = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
+
+// Per-warp scratch, in doubles: dsum (n), staged right-hand sides (W * RHS_CHUNK * (n|1)) and
+// their accumulators (the same), W = 1 (float: double sums) or 2 (Complex); shared memory for
+// n <= SMEM_N, else the warp's slice of global scratch.
+template <int WARPS, class C>
+__global__ void __launch_bounds__(WARPS * 32) potrf_batched_t_kernel(BatchArgs p) {
+  using T = typename C::T;
+  using Acc = typename C::Fwd::Acc;
+  constexpr int W = sizeof(Acc) / sizeof(double);
+  extern __shared__ double sm_dyn[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  T* abase = reinterpret_cast<T*>(p.a);
+  T* bbase = reinterpret_cast<T*>(p.b);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    T* a = abase + p.a_off[mat];
+    double* scr = (n <= SMEM_N) ? sm_dyn + warp * W * SMEM_WARP_DOUBLES_T
+                                 : p.gscratch + gw * p.gscratch_stride;
+    const int ldx = n | 1;
+    const int info = p.solve_only ? 0 : C::factor(a, n, lda, scr);
+    if (info == 0 && p.nrhs > 0) {
+      T* b = bbase + p.b_off[mat];
+      T* xs = (T*)(scr + n);
+      Acc* acc = (Acc*)(scr + n + W * RHS_CHUNK * ldx);
+      for (int r0 = 0; r0 < p.nrhs; r0 += RHS_CHUNK) {
+        const int nr = p.nrhs - r0 < RHS_CHUNK ? p.nrhs - r0 : RHS_CHUNK;
+        for (int e = lane; e < nr * n; e += 32) {
+          const int r = e / n;
+          const int i = e - r * n;
+          xs[r * ldx + i] = b[(long long)(r0 + r) * n + i];
+        }
+        __syncwarp();
+        warp_solve_dot<32, typename C::Fwd>(a, n, 1, lda, false, xs, ldx, acc, nr);
+        warp_solve_sweep<32, typename C::Bwd>(a, n, 1, lda, xs, ldx, nr);
+        for (int e = lane; e < nr * n; e += 32) {
+          const int r = e / n;
+          const int i = e - r * n;
+          b[(long long)(r0 + r) * n + i] = xs[r * ldx + i];
+        }
+        __syncwarp();
+      }
+    }
+    if (lane == 0 && !p.solve_only) p.info[mat] = info;
+    __syncwarp();
+  }
+}
+
+template <int WARPS, class C>
+static size_t potrf_t_smem() {
+  constexpr int W = sizeof(typename C::Fwd::Acc) / sizeof(double);
+  return sizeof(double) * W * SMEM_WARP_DOUBLES_T * WARPS;
+}
+
+template <int WARPS, class C>
+static cudaError_t launch_potrf_t_w(const BatchArgs& args, int ctas, cudaStream_t s) {
+  potrf_batched_t_kernel<WARPS, C><<<ctas, WARPS * 32, potrf_t_smem<WARPS, C>(), s>>>(args);
+  return cudaGetLastError();
+}
+
+// At most 8 warps per CTA; 16-warp plan shapes launch twice the CTAs (same warp count).
+template <class C>
+static cudaError_t launch_potrf_t(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  if (warps > 8) {
+    ctas *= warps / 8;
+    warps = 8;
+  }
+  switch (warps) {
+    case 1: return launch_potrf_t_w<1, C>(args, ctas, s);
+    case 2: return launch_potrf_t_w<2, C>(args, ctas, s);
+    case 4: return launch_potrf_t_w<4, C>(args, ctas, s);
+    case 8: return launch_potrf_t_w<8, C>(args, ctas, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class C>
+static cudaError_t set_potrf_t_attrs() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(potrf_batched_t_kernel<1, C>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)potrf_t_smem<1, C>())) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(potrf_batched_t_kernel<2, C>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)potrf_t_smem<2, C>())) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(potrf_batched_t_kernel<4, C>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)potrf_t_smem<4, C>())) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(potrf_batched_t_kernel<8, C>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)potrf_t_smem<8, C>());
+}
+
+cudaError_t init_potrf_t_attributes() {
+  cudaError_t e = set_potrf_t_attrs<SChol>();
+  if (e != cudaSuccess) return e;
+  return set_potrf_t_attrs<ZChol>();
+}
+
+cudaError_t launch_spotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  return launch_potrf_t<SChol>(args, ctas, warps, s);
+}
+cudaError_t launch_zpotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {
+  return launch_potrf_t<ZChol>(args, ctas, warps, s);
 }
 
 cudaError_t launch_spotrf_single(float* a, int n, int lda, int* out1, double* scratch,

@@ -160,9 +160,15 @@ cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 // Float and Complex overloads of the batched LU (+ solve): args.a / args.b point at float or
 // interleaved (re, im) double arrays, offsets count elements; per-warp global scratch (orders
-// above SMEM_N) of getrf_t_scratch_doubles(max n, elem) doubles.
+// above SMEM_N) of W * warp_scratch_doubles(max n) doubles, W = 1 (float) or 2 (Complex).
 cudaError_t launch_sgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 cudaError_t launch_zgetrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+// Float and Complex overloads of the batched Cholesky (+ L y = b, then L^T x = y or L^H x = y):
+// one warp per matrix; per-warp global scratch (orders above SMEM_N) of W * warp_scratch_doubles
+// doubles, W = 1 (float) or 2 (Complex).
+cudaError_t launch_spotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+cudaError_t launch_zpotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
+cudaError_t init_potrf_t_attributes();
 // Batched Cholesky (+ two triangular solves).
 cudaError_t launch_potrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 

@@ -83,7 +83,8 @@ struct mfg_plan {
   mfg::QrBatchArgs<float> qs{};
   mfg::GevdArgs gv{};  // GEVD: the front half of the generalized eigenproblem
   int qr_float = 0;  // GEQRF: which precision the next launch runs
-  int elem = 0;      // GETRF: element type of the next launch (0 double, 1 float, 2 Complex)
+  int elem = 0;      // GETRF/POTRF: element type of the next launch (0 double, 1 float, 2 Complex)
+  long long dstride = 0;  // GETRF/POTRF: the double kernels' per-group scratch stride
   int mx_n = 0;      // MIXED: order of every matrix
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
   int ctas = 0;
@@ -147,6 +148,7 @@ cudaError_t init_device_attributes(int device) {
   std::call_once(g_attr_once[slot], [slot]() {
     cudaError_t e = mfg::init_getrf_attributes();
     if (e == cudaSuccess) e = mfg::init_potrf_attributes();
+    if (e == cudaSuccess) e = mfg::init_potrf_t_attributes();
     if (e == cudaSuccess) e = mfg::init_getri_attributes();
     if (e == cudaSuccess) e = mfg::init_grad_attributes();
     g_attr_err[slot] = e;
@@ -252,6 +254,8 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
   p->ctas = (int)ctas;
   p->args.gscratch = (double*)p->scratch.ptr;
   p->args.gscratch_stride = stride;
+  p->dstride = stride;
+  p->elem = 0;
   p->args.group = g;
   p->args.hw_mul = mul;
   if (dot_block > 0) p->args.dot_block = dot_block;
@@ -300,6 +304,10 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_getri_batched(p->args, p->ctas, s);
   else if (p->kind == mfg_plan::GEVD)
     e = mfg::launch_gevd_front_batched(p->gv, p->ctas, s);
+  else if (p->kind == mfg_plan::POTRF && p->elem == 1)
+    e = mfg::launch_spotrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::POTRF && p->elem == 2)
+    e = mfg::launch_zpotrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::POTRF)
     e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->qr_float)
@@ -471,6 +479,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   a.queue = d_queue;
   a.gscratch = (double*)p->scratch.ptr;
   a.gscratch_stride = stride;
+  p->dstride = stride;
   // LuInverse's per-lane solves multiply on the FP64 pipe by default: measured faster there than
   // the integer-pipe product, whose long dependency chains one or two warps per scheduler cannot
   // hide.
@@ -1812,22 +1821,25 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
 
 namespace {
 
-// Points a GETRF plan at the element type of the next launch.  Orders above SMEM_N keep their
-// per-warp vectors in the plan's global scratch; Complex needs twice the doubles of double and
-// float, so its first launch grows the scratch (after the stream drains: it may be in use).
-int getrf_set_elem(mfg_plan* p, int elem) {
+// Points a GETRF or POTRF plan at the element type of the next launch.  The double kernels use
+// the scratch stride the plan was shaped with; the float / Complex kernels run one warp per matrix
+// and keep the per-warp vectors of orders above SMEM_N in global scratch, Complex twice the
+// doubles of float, so their first launch may grow the scratch (after the stream drains: it may
+// be in use).  A changed scratch address or stride drops the cached graph.
+int plan_set_elem(mfg_plan* p, int elem) {
   mfg_ctx* ctx = p->ctx;
   p->elem = elem;
-  if (p->max_n <= mfg::SMEM_N) return MFG_OK;
-  const long long base = (mfg::warp_scratch_doubles(p->max_n) + 31) / 32 * 32;
-  const long long stride = elem == 2 ? 2 * base : base;
-  const size_t need = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
-  if (need > p->scratch.bytes) {
-    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    MFG_CUDA(ctx, p->scratch.reserve(need));
-    if (p->exec) {
-      cudaGraphExecDestroy(p->exec);
-      p->exec = nullptr;
+  long long stride = p->dstride;
+  if (elem != 0) {
+    stride = 0;
+    if (p->max_n > mfg::SMEM_N) {
+      const long long base = (mfg::warp_scratch_doubles(p->max_n) + 31) / 32 * 32;
+      stride = elem == 2 ? 2 * base : base;
+      const size_t need = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+      if (need > p->scratch.bytes) {
+        MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        MFG_CUDA(ctx, p->scratch.reserve(need));
+      }
     }
   }
   if (p->args.gscratch != (double*)p->scratch.ptr || p->args.gscratch_stride != stride) {
@@ -1853,7 +1865,7 @@ int getrf_batched_any(mfg_plan* plan, int elem, void* a, int* piv, void* b, int*
     if (!sign) return fail(ctx, -5, "sign is null");
     if (!info) return fail(ctx, -6, "info is null");
   }
-  const int rc = getrf_set_elem(plan, elem);
+  const int rc = plan_set_elem(plan, elem);
   if (rc != MFG_OK) return rc;
   plan->args.a = (double*)a;
   plan->args.piv = piv;
@@ -1874,7 +1886,7 @@ int getrs_batched_any(mfg_plan* plan, int elem, const void* a, const int* piv, v
     if (!piv) return fail(ctx, -3, "piv is null");
     if (!b) return fail(ctx, -4, "b is null");
   }
-  const int rc = getrf_set_elem(plan, elem);
+  const int rc = plan_set_elem(plan, elem);
   if (rc != MFG_OK) return rc;
   plan->args.a = (double*)const_cast<void*>(a);
   plan->args.piv = const_cast<int*>(piv);
@@ -2329,6 +2341,67 @@ MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double
   return pipe_run(plan, OP_GEVD, 0, {const_cast<double*>(a), b, c, info});
 }
 
+}  // extern "C"
+
+namespace {
+
+int potrf_batched_any(mfg_plan* plan, int elem, void* a, void* b, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -3, "b is null");
+    if (!info) return fail(ctx, -4, "info is null");
+  }
+  const int rc = plan_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->args.a = (double*)a;
+  plan->args.piv = nullptr;
+  plan->args.b = (double*)b;
+  plan->args.sign = nullptr;
+  plan->args.info = info;
+  plan->args.solve_only = 0;
+  return plan_execute(plan, a, b, info, nullptr, nullptr);
+}
+
+int potrs_batched_any(mfg_plan* plan, int elem, const void* a, void* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!b) return fail(ctx, -3, "b is null");
+  }
+  const int rc = plan_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->args.a = (double*)const_cast<void*>(a);
+  plan->args.piv = nullptr;
+  plan->args.b = (double*)b;
+  plan->args.sign = nullptr;
+  plan->args.info = nullptr;
+  plan->args.solve_only = 1;
+  return plan_execute(plan, a, b, nullptr, (const void*)3, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+MFG_API int mfg_spotrf_batched(mfg_plan* plan, float* a, float* b, int* info) {
+  return potrf_batched_any(plan, 1, a, b, info);
+}
+MFG_API int mfg_zpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
+  return potrf_batched_any(plan, 2, a, b, info);
+}
+MFG_API int mfg_spotrs_batched(mfg_plan* plan, const float* a, float* b) {
+  return potrs_batched_any(plan, 1, a, b);
+}
+MFG_API int mfg_zpotrs_batched(mfg_plan* plan, const double* a, double* b) {
+  return potrs_batched_any(plan, 2, a, b);
+}
+
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
@@ -2338,6 +2411,8 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) 
     if (plan->nrhs > 0 && !b) return fail(ctx, -3, "b is null");
     if (!info) return fail(ctx, -4, "info is null");
   }
+  const int rc = plan_set_elem(plan, 0);
+  if (rc != MFG_OK) return rc;
   plan->args.a = a;
   plan->args.piv = nullptr;
   plan->args.b = b;
@@ -2356,6 +2431,8 @@ MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b) {
     if (!a) return fail(ctx, -2, "a is null");
     if (!b) return fail(ctx, -3, "b is null");
   }
+  const int rc = plan_set_elem(plan, 0);
+  if (rc != MFG_OK) return rc;
   plan->args.a = const_cast<double*>(a);
   plan->args.piv = nullptr;
   plan->args.b = b;

@@ -1066,6 +1066,39 @@ void orc_dchol_solve_batched(long count, const int* n, const int64_t* a_off, dou
   });
 }
 
+// Float and Complex overloads: Cholesky, then L y = b and L^T x = y (float) or L^H x = y
+// (Complex: Lower/ConjTrans, A = L L^H) for nrhs columns (ldb = n[i]; offsets in elements).
+void orc_schol_solve_batched(long count, const int* n, const int64_t* a_off, float* a,
+                             const int64_t* b_off, float* b, int nrhs, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    float* ai = a + a_off[i];
+    const int r = orc_scholesky(ni, ai, ni);
+    info[i] = r;
+    if (r == 0)
+      for (int c = 0; c < nrhs; c++) {
+        float* x = b + b_off[i] + (long)ni * c;
+        orc_strsv(LOWER, NOTRANS, ni, ai, ni, x, 1);
+        orc_strsv(LOWER, TRANS, ni, ai, ni, x, 1);
+      }
+  });
+}
+void orc_zchol_solve_batched(long count, const int* n, const int64_t* a_off, double* a,
+                             const int64_t* b_off, double* b, int nrhs, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    double* ai = a + 2 * a_off[i];
+    const int r = orc_zcholesky(ni, ai, ni);
+    info[i] = r;
+    if (r == 0)
+      for (int c = 0; c < nrhs; c++) {
+        double* x = b + 2 * (b_off[i] + (long)ni * c);
+        orc_ztrsv(LOWER, NOTRANS, ni, ai, ni, x, 1);
+        orc_ztrsv(LOWER, CONJTRANS, ni, ai, ni, x, 1);
+      }
+  });
+}
+
 // Config "LU + forward/back solve": per matrix, Lu then the solve above for nrhs columns
 // (ldb = n[i]).  sign[i] receives Lu's return value.
 void orc_dlu_solve_batched(long count, const int* n, const int64_t* a_off, double* a,

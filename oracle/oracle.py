@@ -59,6 +59,8 @@ def lib():
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
+            "orc_schol_solve_batched": (None, [_L, _i, _l, _f, _l, _f, _I, _i, _I]),
+            "orc_zchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _I, _i, _I]),
             "orc_slu_solve_batched": (None, [_L, _i, _l, _f, _l, _i, _l, _f, _I, _i, _I]),
             "orc_zlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
             "orc_ddot": (ctypes.c_double, [_I, _d, _I, _d, _I]),
@@ -169,7 +171,14 @@ def qr_ls(m, n, a, lda, b, x):
     getattr(lib(), "orc_%sqr_ls" % _pre(a))(m, n, _fp(a), lda, _fp(b), _fp(x))
 
 
-def chol_solve_batched(n, a_off, a, b_off, b, info, nthreads=1):
+def chol_solve_batched(n, a_off, a, b_off, b, info, nthreads=1, nrhs=1):
+    """Batched Cholesky + solve.  float64: one right-hand side per matrix; float32 and
+    complex128 (MatFlat's float and Complex overloads): nrhs columns, ldb = n."""
+    if a.dtype != np.float64:
+        fn = getattr(lib(), "orc_%schol_solve_batched" % _pre(a))
+        fn(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+           _p(b_off, ctypes.c_int64), _fp(b), nrhs, _p(info, ctypes.c_int), nthreads)
+        return
     lib().orc_dchol_solve_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
                                   _p(b_off, ctypes.c_int64), _fp(b), _p(info, ctypes.c_int), nthreads)
 
