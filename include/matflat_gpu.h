@@ -308,6 +308,14 @@ MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b)
  * R x = Q^T b (Blas.SolveTriangular.cs:191-199); bit-identical to the fused path.  nrhs >= 1. */
 MFG_API int mfg_dgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b);
 MFG_API int mfg_sgeqrs_batched(mfg_plan* plan, const float* a, const float* rdiag, float* b);
+/* The Complex overload of the batched QR (+ least squares) and of the solve alone, on the same
+ * plan: a and b are interleaved (re, im) doubles (offsets count complex elements), rdiag is real
+ * as in Factorization.Qr(Complex) (MatFlat/Factorization.Qr.cs:198-255: DotConj coefficients,
+ * division by Complex(norm, 0)); factors and rdiag bit-identical to it.  The right-hand sides get
+ * Q^H b from the same reflector updates, then R x = y with Complex SolveTriangular Upper/NoTrans
+ * arithmetic (Blas.SolveTriangular.cs:280-395; R's diagonal is Complex(rdiag, 0)). */
+MFG_API int mfg_zgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b);
+MFG_API int mfg_zgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b);
 
 /* Differentiable Cholesky / log-determinant / solve over a potrf plan with nrhs = 1 (n <= 128).
  * For every SPD matrix K (upper triangle read, as Factorization.Cholesky) and vector y:

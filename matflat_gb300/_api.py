@@ -34,6 +34,8 @@ _SIGS = {
                                     _vp]),
     "mfg_dgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zgeqrf_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zgeqrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dtrsv": (_I, [_vp, _I, _I, _I, _vp, _I, _vp, _I]),
     "mfg_sgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_zgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
@@ -690,10 +692,13 @@ class QrBatch(_Batch):
         self.count = len(self._m)
         self.nrhs = nrhs
 
-    def run(self, a, rdiag, b=None, single=False):
-        fn = self.ctx.lib.mfg_sgeqrf_batched if single else self.ctx.lib.mfg_dgeqrf_batched
-        rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
-        self.ctx.check(rc, "mfg_geqrf_batched")
+    def run(self, a, rdiag, b=None, single=False, dtype=None):
+        """QR (+ least squares) of device buffers: float64 (default), float32 (single=True or a
+        float32 tensor) or Complex (a complex128 tensor, or dtype="z" for interleaved float64;
+        rdiag is then float64)."""
+        name = "mfg_%sgeqrf_batched" % ("s" if single else _elem(a, dtype))
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
+        self.ctx.check(rc, name)
 
     def run_host(self, a, rdiag, b=None, single=False):
         """QR (+ least squares) on host arrays, copies pipelined with compute.  Synchronous."""
@@ -701,11 +706,12 @@ class QrBatch(_Batch):
         rc = fn(self.h, _hptr(a), _hptr(rdiag), _hptr(b))
         self.ctx.check(rc, "mfg_geqrf_batched_host")
 
-    def solve(self, a, rdiag, b, single=False):
-        """Least squares with the factorization already in a and rdiag (nrhs columns of b)."""
-        fn = self.ctx.lib.mfg_sgeqrs_batched if single else self.ctx.lib.mfg_dgeqrs_batched
-        rc = fn(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
-        self.ctx.check(rc, "mfg_geqrs_batched")
+    def solve(self, a, rdiag, b, single=False, dtype=None):
+        """Least squares with the factorization already in a and rdiag (nrhs columns of b);
+        element type as in `run`."""
+        name = "mfg_%sgeqrs_batched" % ("s" if single else _elem(a, dtype))
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
+        self.ctx.check(rc, name)
 
 
 def selftest_dmul(a, b, out):

@@ -68,6 +68,13 @@ int qr_smem_coefs(int group);
 
 template <typename T>
 cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s);
+// Complex batched QR (+ least squares): args holds interleaved (re, im) arrays as doubles with
+// complex-element offsets and a real rdiag; one warp per matrix; coefficients of matrices with
+// n + nrhs > zqr_smem_coefs() in global scratch (gscratch_stride doubles per warp, 2 per
+// coefficient).
+int zqr_smem_coefs();
+cudaError_t launch_zqr_batched(const QrBatchArgs<double>& args, int ctas, int warps,
+                               cudaStream_t s);
 // Single-matrix QR kernels; scratch: n + 1 elements.
 template <typename T>
 cudaError_t launch_qr_single(T* a, int m, int n, int lda, T* rdiag, T* scratch, cudaStream_t s);

@@ -341,6 +341,93 @@ __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
   }
 }
 
+// Complex overload of the batched QR + least squares (Factorization.Qr Complex,
+// MatFlat/Factorization.Qr.cs:198-255): one warp per matrix, the same column schedule as the
+// double kernel in complex arithmetic (DotConj coefficients, Complex(norm, 0) divisions); rdiag
+// is real.  The right-hand sides receive Q^H b from the same reflector updates, then R x = y with
+// Complex SolveTriangular Upper/NoTrans arithmetic (x[i] /= Complex(rdiag[i], 0);
+// x[r] -= R(r,i) * x[i]).  args carries the interleaved (re, im) arrays as doubles; offsets count
+// complex elements; gscratch_stride counts doubles (2 per coefficient).
+constexpr int QR_Z_SMEM_COEFS = 128;
+
+__device__ void zqr_rsolve_warp(const zdouble* a, int n, long long lda, const double* rdiag,
+                                zdouble* b, long long ldb, int nb) {
+  const int lane = threadIdx.x & 31;
+  for (int i = n - 1; i >= 0; --i) {
+    const zdouble d = zmake(rdiag[i], 0.0);
+    for (int c = lane; c < nb; c += 32) {
+      zdouble* x = b + (long long)c * ldb;
+      x[i] = zdiv(x[i], d);
+    }
+    __syncwarp();
+    const zdouble* ai = a + (long long)i * lda;
+    for (int e = lane; e < nb * i; e += 32) {
+      const int c = e / i;
+      const int r = e - c * i;
+      zdouble* x = b + (long long)c * ldb;
+      x[r] = zsub(x[r], zmul(ai[r], x[i]));
+    }
+    __syncwarp();
+  }
+}
+
+template <int WARPS, bool SOLVE>
+__global__ void __launch_bounds__(WARPS * 32) zqr_batched_kernel(QrBatchArgs<double> p) {
+  __shared__ zdouble sm[WARPS][QR_Z_SMEM_COEFS];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  zdouble* abase = reinterpret_cast<zdouble*>(p.a);
+  zdouble* bbase = reinterpret_cast<zdouble*>(p.b);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int m = p.m[mat];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    zdouble* a = abase + p.a_off[mat];
+    double* rd = p.rdiag + p.rdiag_off[mat];
+    zdouble* b = p.nrhs > 0 ? bbase + p.b_off[mat] : nullptr;
+    zdouble* coefs = (n + p.nrhs <= QR_Z_SMEM_COEFS)
+                         ? &sm[warp][0]
+                         : reinterpret_cast<zdouble*>(p.gscratch + gw * p.gscratch_stride);
+    if constexpr (SOLVE)
+      qr_apply_warp<zdouble, 32>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+    else
+      qr_warp<zdouble, 32>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+    if (p.nrhs > 0) zqr_rsolve_warp(a, n, lda, rd, b, m, p.nrhs);
+    __syncwarp();
+  }
+}
+
+template <bool SOLVE>
+static cudaError_t launch_zqr_batched_s(const QrBatchArgs<double>& args, int ctas, int warps,
+                                        cudaStream_t s) {
+  if (warps > 8) {
+    ctas *= warps / 8;
+    warps = 8;
+  }
+  switch (warps) {
+    case 1: zqr_batched_kernel<1, SOLVE><<<ctas, 32, 0, s>>>(args); break;
+    case 2: zqr_batched_kernel<2, SOLVE><<<ctas, 64, 0, s>>>(args); break;
+    case 4: zqr_batched_kernel<4, SOLVE><<<ctas, 128, 0, s>>>(args); break;
+    case 8: zqr_batched_kernel<8, SOLVE><<<ctas, 256, 0, s>>>(args); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+int zqr_smem_coefs() { return QR_Z_SMEM_COEFS; }
+
+cudaError_t launch_zqr_batched(const QrBatchArgs<double>& args, int ctas, int warps,
+                               cudaStream_t s) {
+  return args.solve_only ? launch_zqr_batched_s<true>(args, ctas, warps, s)
+                         : launch_zqr_batched_s<false>(args, ctas, warps, s);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(32) qr_single_kernel(T* a, int m, int n, int lda,
                                                        typename QrArith<T>::R* rdiag, T* scratch) {

@@ -82,7 +82,9 @@ struct mfg_plan {
   mfg::QrBatchArgs<double> qd{};
   mfg::QrBatchArgs<float> qs{};
   mfg::GevdArgs gv{};  // GEVD: the front half of the generalized eigenproblem
-  int qr_float = 0;  // GEQRF: which precision the next launch runs
+  mfg::QrBatchArgs<double> qz{};  // GEQRF: the Complex overload (interleaved doubles)
+  int qr_max_cols = 0;             // GEQRF: max over the batch of n + nrhs
+  int qr_float = 0;  // GEQRF: which overload the next launch runs (0 double, 1 float, 2 Complex)
   int elem = 0;      // GETRF/POTRF: element type of the next launch (0 double, 1 float, 2 Complex)
   long long dstride = 0;  // GETRF/POTRF: the double kernels' per-group scratch stride
   int mx_n = 0;      // MIXED: order of every matrix
@@ -310,6 +312,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_zpotrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::POTRF)
     e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->qr_float == 2)
+    e = mfg::launch_zqr_batched(p->qz, p->ctas, p->warps, s);
   else if (p->qr_float)
     e = mfg::launch_qr_batched<float>(p->qs, p->ctas, p->warps, s);
   else
@@ -713,8 +717,12 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   };
   fill(p->qd);
   fill(p->qs);
+  fill(p->qz);
   p->qd.group = group_d;
   p->qs.group = group_s;
+  p->qz.group = 32;
+  p->qz.gscratch_stride = 0;
+  p->qr_max_cols = max_cols;
   const int* order_grouped = (const int*)(base + 4 * bi + 3 * bl + 256);
   if (group_d < 32) p->qd.order = order_grouped;
   if (group_s < 32) p->qs.order = order_grouped;
@@ -1185,6 +1193,74 @@ MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b)
   plan->qs.b = b;
   plan->qs.solve_only = 0;
   return plan_execute(plan, a, rdiag, b, (const void*)2, nullptr);
+}
+
+}  // extern "C"
+
+// The Complex overload keeps 2 doubles per reflector coefficient: matrices whose n + nrhs
+// coefficients do not fit in shared memory use global scratch, grown on first use (after the
+// stream drains: it may be in use; the other overloads follow the new address).
+static int zqr_prepare(mfg_plan* p) {
+  mfg_ctx* ctx = p->ctx;
+  long long stride = 0;
+  if (p->qr_max_cols > mfg::zqr_smem_coefs()) {
+    stride = 2LL * ((p->qr_max_cols + 31) / 32 * 32);
+    const size_t need = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+    if (need > p->scratch.bytes) {
+      MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      MFG_CUDA(ctx, p->scratch.reserve(need));
+      p->qd.gscratch = (double*)p->scratch.ptr;
+      p->qs.gscratch = (float*)p->scratch.ptr;
+      if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+      }
+    }
+  }
+  p->qz.gscratch = (double*)p->scratch.ptr;
+  p->qz.gscratch_stride = stride;
+  return MFG_OK;
+}
+
+extern "C" {
+
+MFG_API int mfg_zgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!rdiag) return fail(ctx, -3, "rdiag is null");
+    if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  }
+  const int rc = zqr_prepare(plan);
+  if (rc != MFG_OK) return rc;
+  plan->qr_float = 2;
+  plan->qz.a = a;
+  plan->qz.rdiag = rdiag;
+  plan->qz.b = b;
+  plan->qz.solve_only = 0;
+  return plan_execute(plan, a, rdiag, b, (const void*)4, nullptr);
+}
+
+MFG_API int mfg_zgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!rdiag) return fail(ctx, -3, "rdiag is null");
+    if (!b) return fail(ctx, -4, "b is null");
+  }
+  const int rc = zqr_prepare(plan);
+  if (rc != MFG_OK) return rc;
+  plan->qr_float = 2;
+  plan->qz.a = const_cast<double*>(a);
+  plan->qz.rdiag = const_cast<double*>(rdiag);
+  plan->qz.b = b;
+  plan->qz.solve_only = 1;
+  return plan_execute(plan, a, rdiag, b, (const void*)4, (const void*)3);
 }
 
 }  // extern "C"

@@ -955,6 +955,16 @@ void orc_dqr_ls(int m, int n, double* a, int lda, const double* b, double* x) {
   orc_dqr_r(m, n, a, lda, r.data(), n, rdiag.data());
   orc_dtrsv(UPPER, NOTRANS, n, r.data(), n, x, 1);
 }
+// Complex: x = R^-1 (Q^H b) with Q^H b from MulMatMat(ConjTrans, NoTrans) (Blas.MulMatMat.cs:
+// 407-575) and R x = y by SolveTriangular(Upper, NoTrans) Complex.
+void orc_zqr_ls(int m, int n, double* a, int lda, const double* b, double* x) {
+  std::vector<double> rdiag(n), q((size_t)2 * m * n), r((size_t)2 * n * n);
+  orc_zqr(m, n, a, lda, rdiag.data());
+  orc_zqr_q(m, n, a, lda, q.data(), m);
+  orc_zgemm(CONJTRANS, NOTRANS, n, 1, m, q.data(), m, b, m, x, n);
+  orc_zqr_r(m, n, a, lda, r.data(), n, rdiag.data());
+  orc_ztrsv(UPPER, NOTRANS, n, r.data(), n, x, 1);
+}
 void orc_sqr_ls(int m, int n, float* a, int lda, const float* b, float* x) {
   std::vector<float> rdiag(n), q((size_t)m * n), r((size_t)n * n);
   orc_sqr(m, n, a, lda, rdiag.data());

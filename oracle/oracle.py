@@ -57,6 +57,7 @@ def lib():
             "orc_dlu_solve": (None, [_I, _d, _I, _i, _I, _d, _I]),
             "orc_dqr_ls": (None, [_I, _I, _d, _I, _d, _d]),
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
+            "orc_zqr_ls": (None, [_I, _I, _d, _I, _d, _d]),
             "orc_dchol_solve_batched": (None, [_L, _i, _l, _d, _l, _d, _i, _I]),
             "orc_dlu_solve_batched": (None, [_L, _i, _l, _d, _l, _i, _l, _d, _I, _i, _I]),
             "orc_schol_solve_batched": (None, [_L, _i, _l, _f, _l, _f, _I, _i, _I]),
@@ -167,7 +168,8 @@ def lu_solve(n, lu_, lda, piv, nrhs, b, ldb):
 
 
 def qr_ls(m, n, a, lda, b, x):
-    """Least squares through Qr, QrOrthogonalFactor, MulMatVec(Trans), SolveTriangular."""
+    """Least squares through Qr, QrOrthogonalFactor, MulMatVec(Trans) (Complex: MulMatMat
+    ConjTrans), QrUpperTriangularFactor and SolveTriangular(Upper, NoTrans)."""
     getattr(lib(), "orc_%sqr_ls" % _pre(a))(m, n, _fp(a), lda, _fp(b), _fp(x))
 
 
