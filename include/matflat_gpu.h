@@ -393,10 +393,6 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
  * random and edge-case operands. */
 MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
                               int64_t n);
-/* Diagnostics: out[i] = a[i] + b[i] by the integer-pipe sum the dot products can use, or a NaN
- * where it differs from the IEEE round-to-nearest sum (NaN results count as equal). */
-MFG_API int mfg_selftest_dadd(mfg_ctx* ctx, const double* a, const double* b, double* out,
-                              int64_t n);
 
 #ifdef __cplusplus
 }

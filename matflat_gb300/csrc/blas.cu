@@ -125,26 +125,6 @@ __global__ void selftest_mul_kernel(const double* a, const double* b, double* ou
   }
 }
 
-// The integer-pipe sum against the hardware one; a disagreement is reported as a NaN.
-__global__ void selftest_add_kernel(const double* a, const double* b, double* out, long long n) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double r0 = iadd_rn(a[i], b[i]);
-    const double r1 = __dadd_rn(a[i], b[i]);
-    const bool same = dbits(r0) == dbits(r1) || (r0 != r0 && r1 != r1);
-    out[i] = same ? r0 : __longlong_as_double(0x7FF8DEAD0000DEADll);
-  }
-}
-
-cudaError_t launch_selftest_add(const double* a, const double* b, double* out, long long n,
-                                cudaStream_t s) {
-  if (n <= 0) return cudaSuccess;
-  long long blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
-  selftest_add_kernel<<<(unsigned)blocks, 256, 0, s>>>(a, b, out, n);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

@@ -264,11 +264,7 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
 template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
-  if (args.hw_mul == 3)
-    getrf_batched_kernel<WARPS, 3, 4><<<ctas, WARPS * 32, smem, s>>>(args);
-  else if (args.hw_mul == 4)
-    getrf_batched_kernel<WARPS, 4, 4><<<ctas, WARPS * 32, smem, s>>>(args);
-  else if (args.hw_mul == 2)
+  if (args.hw_mul == 2)
     getrf_batched_kernel<WARPS, 2, 4><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.hw_mul)
     getrf_batched_kernel<WARPS, 0, 4><<<ctas, WARPS * 32, smem, s>>>(args);
@@ -289,12 +285,6 @@ static cudaError_t set_getrf_attr() {
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, 2, 4>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, 3, 4>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(getrf_batched_kernel<WARPS, 4, 4>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(getrf_batched_kernel<WARPS, false, 4>,

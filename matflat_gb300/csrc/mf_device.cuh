@@ -93,13 +93,9 @@ constexpr int DOT_BLOCK = 4;
 // The product used by the dot trees: the hardware DMUL (IM = false) or the integer-pipe product
 // imul_rn (IM = true); both return the correctly rounded product, bit for bit.  exact_dot's IM is
 // 0 (DMUL), 1 (integer path) or 2 (the first product of each pair on the integer path, the
-// second on DMUL, splitting the work between the two pipes); 3 and 4 also move the pair's own
-// sum x_a*y_a + x_b*y_b to the integer pipes (iadd_rn), for every pair (3) or every other pair
-// of the software-pipelined blocks (4), leaving the FP64 pipe the running sum alone.
+// second on DMUL, splitting the work between the two pipes).
 template <bool IM>
 __device__ __forceinline__ double xmul(double a, double b);
-// The integer-pipe sum (mf_imul.cuh): exactly __dadd_rn(a, b).
-__device__ __forceinline__ double iadd_rn(double a, double b);
 
 template <int IM = 1, int DOT_BLOCK = mfg::DOT_BLOCK>
 __device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
@@ -135,10 +131,8 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
       }
 #pragma unroll
       for (int u = 0; u < DOT_BLOCK; ++u) {
-        const double p0 = xmul<IM != 0>(xa[2 * u], ya[2 * u]);
-        const double p1 = xmul<IM == 1 || IM >= 3>(xa[2 * u + 1], ya[2 * u + 1]);
-        const bool isum = IM == 3 || (IM == 4 && (u & 1) == 0);
-        const double q = isum ? iadd_rn(p0, p1) : __dadd_rn(p0, p1);
+        const double q = __dadd_rn(xmul<IM != 0>(xa[2 * u], ya[2 * u]),
+                                   xmul<IM == 1>(xa[2 * u + 1], ya[2 * u + 1]));
         s = __dadd_rn(s, q);
       }
       if (more) {
@@ -151,9 +145,7 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
     }
   }
   for (int p = blocks * DOT_BLOCK; p < pairs; ++p) {
-    const double p0 = xmul<IM != 0>(x[0], y[0]);
-    const double p1 = xmul<IM == 1 || IM >= 3>(x[incx], y[incy]);
-    const double q = IM == 3 ? iadd_rn(p0, p1) : __dadd_rn(p0, p1);
+    const double q = __dadd_rn(xmul<IM != 0>(x[0], y[0]), xmul<IM == 1>(x[incx], y[incy]));
     s = __dadd_rn(s, q);
     x += 2 * incx;
     y += 2 * incy;

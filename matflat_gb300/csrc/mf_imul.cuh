@@ -85,53 +85,6 @@ __device__ __forceinline__ double imul_nb(double a, double b, bool& ok) {
   return __longlong_as_double((long long)(zero ? (A ^ B) & 0x8000000000000000ull : r));
 }
 
-// Correctly rounded double-precision sum on the integer pipes, from the definition of IEEE 754
-// round-to-nearest-even addition.  With |a| >= |b| (ordered by bit pattern), both significands
-// are scaled to [2^62, 2^63) (10 guard bits); b's is shifted right by the exponent difference d
-// with every shifted-out bit ORed into bit 0 (sticky), so the operand is odd whenever it is
-// inexact and no rounding boundary (a multiple of 2^9) can be hit by an inexact sum.  The sum or
-// difference is renormalised to [2^62, 2^63) (one right shift with sticky after a carry, a left
-// shift by the leading-zero count after cancellation), rounded on bits 9..0, and packed with the
-// larger operand's sign; an exact cancellation gives +0.  Operands that are not normal numbers
-// and results outside the normal range take the hardware __dadd_rn, so the function returns
-// exactly __dadd_rn(a, b) for every input.
-__device__ __forceinline__ double iadd_nb(double a, double b, bool& ok) {
-  const unsigned long long A = dbits(a), B = dbits(b);
-  const unsigned long long ka = A & 0x7FFFFFFFFFFFFFFFull, kb = B & 0x7FFFFFFFFFFFFFFFull;
-  const bool swap = kb > ka;
-  const unsigned long long kbig = swap ? kb : ka, ksml = swap ? ka : kb;
-  const unsigned long long sign = (swap ? B : A) & 0x8000000000000000ull;
-  const int eb = (int)(kbig >> 52), es = (int)(ksml >> 52);
-  const unsigned long long MB = ((kbig & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) << 10;
-  const unsigned long long M0 = ((ksml & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) << 10;
-  const int d = eb - es;
-  unsigned long long MS;
-  if (d >= 64) {
-    MS = 1ull;
-  } else {
-    const bool lost = d > 10 && (M0 << (64 - d)) != 0ull;
-    MS = (M0 >> d) | (lost ? 1ull : 0ull);
-  }
-  const bool sub = ((A ^ B) >> 63) != 0ull;
-  const unsigned long long S = sub ? MB - MS : MB + MS;
-  const int sh = __clzll((long long)S) - 1;  // -1: carry out of the addition
-  const unsigned long long N = sh < 0 ? ((S >> 1) | (S & 1ull)) : (S << sh);
-  const int e = eb - sh;
-  unsigned long long mant = N >> 10;
-  const unsigned low = (unsigned)N & 0x3FFu;
-  mant += (low > 0x200u || (low == 0x200u && (mant & 1ull))) ? 1ull : 0ull;
-  ok = (unsigned)(es - 1) < 2046u && eb <= 2046 && (S == 0ull || (unsigned)(e - 1) < 2046u);
-  const unsigned long long r =
-      S == 0ull ? 0ull : sign | ((((unsigned long long)(e - 1)) << 52) + mant);
-  return __longlong_as_double((long long)r);
-}
-
-__device__ __forceinline__ double iadd_rn(double a, double b) {
-  bool ok;
-  const double r = iadd_nb(a, b, ok);
-  return ok ? r : __dadd_rn(a, b);
-}
-
 // p[r] = a[r] * b[r], correctly rounded, for R products: the integer-path ones first, then one
 // (rarely taken) branch that redoes the out-of-range ones with the hardware multiply.  IM = 0
 // uses the hardware multiply throughout, 1 the integer path, 2 the integer path for even r and

@@ -57,51 +57,3 @@ def test_integer_product_is_ieee(mf):
     np.testing.assert_array_equal(gn, en)
     bad = np.nonzero(got.view(np.uint64)[~gn] != exp.view(np.uint64)[~en])[0]
     assert bad.size == 0, (a[~gn][bad[:5]], b[~gn][bad[:5]], got[~gn][bad[:5]], exp[~en][bad[:5]])
-
-
-def _add_operands(rng, n):
-    parts = []
-    # every exponent difference from 0 to beyond the significand, both signs
-    a = rng.standard_normal(n)
-    parts.append((a, rng.standard_normal(n) * np.ldexp(1.0, rng.integers(-70, 70, n))))
-    # near-cancellation: b = -a (1 + small), the result loses up to 60 leading bits
-    k = rng.integers(0, 62, n)
-    parts.append((a, -a * (1.0 + rng.standard_normal(n) * np.ldexp(1.0, -k))))
-    parts.append((a, -a))
-    parts.append((a, -np.nextafter(a, 2 * a)))
-    # exact halfway and near-halfway cases: b = m * ulp(a)
-    parts.append((a, np.spacing(a) * rng.choice([0.5, 1.5, -0.5, -1.5, 0.25, 0.75, 2.5], n)))
-    # uniformly random bit patterns: every exponent, subnormals, infinities, NaNs
-    parts.append((rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64),
-                  rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64)))
-    # the edges of the normal range: overflow to infinity, subnormal results
-    big = np.ldexp(1.0 + rng.random(n), 1023)
-    parts.append((big, big * rng.choice([1.0, 0.5, 2.0 ** -52, -1.0], n)))
-    tiny = np.ldexp(1.0 + rng.random(n), -1022)
-    parts.append((tiny, -tiny * rng.choice([1.0, 0.5, 0.75, 1.0 + 2.0 ** -52], n)))
-    z = rng.choice([0.0, -0.0], n)
-    parts.append((z, a))
-    parts.append((z, z[::-1]))
-    a = np.concatenate([p[0] for p in parts])
-    b = np.concatenate([p[1] for p in parts])
-    return a, b
-
-
-def test_integer_sum_is_ieee(mf):
-    """The integer-pipe sum (iadd_rn) equals the IEEE round-to-nearest-even sum bit for bit; the
-    self-test kernel also compares it with the hardware sum on the device."""
-    import torch
-    rng = np.random.default_rng(98)
-    a, b = _add_operands(rng, 1 << 18)
-    da = torch.from_numpy(a).cuda()
-    db = torch.from_numpy(b).cuda()
-    out = torch.empty_like(da)
-    mf.selftest_dadd(da, db, out)
-    mf.context().synchronize()
-    got = out.cpu().numpy()
-    with np.errstate(all="ignore"):
-        exp = a + b
-    gn, en = np.isnan(got), np.isnan(exp)
-    np.testing.assert_array_equal(gn, en)
-    bad = np.nonzero(got.view(np.uint64)[~gn] != exp.view(np.uint64)[~en])[0]
-    assert bad.size == 0, (a[~gn][bad[:5]], b[~gn][bad[:5]], got[~gn][bad[:5]], exp[~en][bad[:5]])
