@@ -42,6 +42,10 @@ CONFIGS = {
     "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
                           "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
                  count=10_000, n=32, nrhs=1),
+    "chol100k": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
+                              "100,000 SPD matrices n~U{8..128}, A=S+2n*I, S symmetric with "
+                              "N(0,1) entries, 1 RHS, seed 0",
+                     count=100_000, nmin=8, nmax=128, nrhs=1),
     "grad": dict(workload="differentiable Cholesky/log-det/solve: loss y^T K^-1 y + log det K and "
                           "its gradient K^-1 - alpha alpha^T, 4,096 RBF kernel matrices n=128 "
                           "(x~U[0,1]^3, length 0.3, jitter 1e-6), y~N(0,1), seed 0",
@@ -248,6 +252,9 @@ def make_inputs(cfg_name, rank):
         return synth.lu_batch(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"], seed=rank)
     if cfg_name == "chol":
         return synth.spd_batch(cfg["count"], cfg["n"], cfg["nrhs"], seed=rank)
+    if cfg_name == "chol100k":
+        return synth.spd_batch_uneven(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"],
+                                      seed=rank)
     if cfg_name == "grad":
         return synth.rbf_batch(cfg["count"], cfg["n"], seed=rank)
     if cfg_name == "gevd":
@@ -310,7 +317,7 @@ def run_cpu_sample(cfg_name, d, sample, threads, oracle):
         t0 = time.perf_counter()
         oracle.lu_inverse_batched(n, a_off, a, piv_off, piv, info, threads)
         return time.perf_counter() - t0
-    if cfg_name in ("lu", "chol", "grad"):
+    if cfg_name in ("lu", "chol", "chol100k", "grad"):
         n = d["n"][sample].astype(np.int32)
         sz = n.astype(np.int64) ** 2
         a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
@@ -327,7 +334,7 @@ def run_cpu_sample(cfg_name, d, sample, threads, oracle):
             piv = np.zeros(int(n.sum()), np.int32)
             sign = np.zeros(len(n), np.int32)
             oracle.lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, threads)
-        elif cfg_name == "chol":
+        elif cfg_name in ("chol", "chol100k"):
             info = np.zeros(len(n), np.int32)
             oracle.chol_solve_batched(n, a_off, a, b_off, b, info, threads)
         else:
@@ -392,6 +399,7 @@ def metric_name(cfg_name):
             "inv": "batched FP64 LuInverse matrices/s (MatFlat-exact)",
             "gevd": "batched FP64 GEVD front half (Cholesky + C = L^-1 A L^-T) pairs/s (MatFlat-exact)",
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
+            "chol100k": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
             "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
             "qr32": "batched FP32 QR least-squares matrices/s (MatFlat-exact factors)"}[cfg_name]
@@ -619,6 +627,7 @@ def main():
     cfg = CONFIGS[cfg_name]
     count = len(d["n"])
     tuned = None
+    traffic_key = None
     if cfg_name in ("qr", "qr32"):
         dt = torch.float32 if cfg_name == "qr32" else torch.float64
         npdt = np.float32 if cfg_name == "qr32" else np.float64
@@ -690,7 +699,7 @@ def main():
             flops = lu_flops(d["n"], d["nrhs"])
             byts = lu_bytes(d["n"], d["nrhs"])
             kernel_key = "getrf_batched_kernel"
-        elif cfg_name == "chol":
+        elif cfg_name in ("chol", "chol100k"):
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
             if not args.no_autotune:
                 tuned = plan.autotune()
@@ -701,6 +710,8 @@ def main():
             flops = chol_flops(d["n"], d["nrhs"])
             byts = chol_bytes(d["n"], d["nrhs"])
             kernel_key = "potrf_batched_kernel"
+            if cfg_name == "chol100k":
+                traffic_key = "potrf_batched_kernel_chol100k"
         else:
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
             loss = torch.zeros(count, dtype=torch.float64, device="cuda")
@@ -780,7 +791,7 @@ def main():
             call = lambda: plan.run_host(io[0], io[1], extra[0])
             up = [io[0], io[1]]
             down = [io[0]] + extra
-        elif cfg_name == "chol":
+        elif cfg_name in ("chol", "chol100k"):
             extra = [torch.zeros(count, dtype=torch.int32).pin_memory()]
             call = lambda: plan.run_host(io[0], io[1], extra[0])
             up = [io[0], io[1]]
@@ -832,7 +843,7 @@ def main():
     fp64_peak = measure_fp64_peak(torch)
     kmed = statistics.median(kernel_ms)
     achieved_tf = flops / (kmed / 1e3) / 1e12
-    traffic = read_traffic(kernel_key)
+    traffic = read_traffic(traffic_key or kernel_key)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))

@@ -79,6 +79,30 @@ def spd_batch(count, n=32, nrhs=1, seed=0):
     return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=b, nrhs=nrhs)
 
 
+def spd_batch_uneven(count, nmin=8, nmax=128, nrhs=1, seed=0):
+    """Cholesky + solve workload of uneven orders: n ~ U{nmin..nmax}, A = S + 2n I with S
+    symmetric, S_ij = S_ji ~ N(0,1) (the upper triangle of n^2 draws per matrix, mirrored), so
+    every A is positive definite (the spectrum of S lies within about +-2 sqrt(n)); right-hand
+    sides ~ N(0,1).  O(n^2) per matrix, unlike B B^T, so a 100,000-matrix batch builds in
+    seconds."""
+    ns = (np.floor(uniform(count, seed, stream=6) * (nmax - nmin + 1)) + nmin).astype(np.int32)
+    a_off, total = packed_offsets(ns, ns)
+    a = normal(total, seed, stream=7)
+    for n in np.unique(ns).tolist():
+        idx = np.nonzero(ns == n)[0]
+        lower = np.tril_indices(n, -1)
+        src = lower[1] * n + lower[0]           # (j, i) with i > j: the upper triangle, row-major
+        dst = lower[0] * n + lower[1]           # (i, j): mirrored below the diagonal
+        diag = np.arange(n) * (n + 1)
+        for i in idx.tolist():
+            m = a[a_off[i]:a_off[i] + n * n]
+            m[dst] = m[src]
+            m[diag] += 2.0 * n
+    b_off, b_total = packed_offsets(ns, np.full_like(ns, nrhs))
+    b = normal(b_total, seed, stream=8)
+    return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=b, nrhs=nrhs)
+
+
 def gevd_batch(count, n=64, seed=0):
     """GEVD front-half workload: A symmetric (A = S + S^T, S ~ N(0,1)) and B = M M^T + n I with
     M ~ N(0,1), column-major pairs of order n."""
