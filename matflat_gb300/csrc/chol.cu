@@ -92,6 +92,14 @@ static_assert(chol_group_doubles<32>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 static_assert(4 * chol_group_doubles<8>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 static_assert(8 * chol_group_doubles<4>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 
+// Per-warp shared memory when the solves are staged in global memory (BatchArgs::gsolve): the
+// column sums of the warp's groups only (4G doubles each).
+constexpr int SMEM_WARP_DOUBLES_CG = 4 * 32 + 2;
+
+static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
+  return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
+}
+
 template <int WARPS, bool IM, int G>
 __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
@@ -100,7 +108,12 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
   const int lane = threadIdx.x & 31;
   const int group = lane / G;
   const long long gg = ((long long)blockIdx.x * WARPS + warp) * GPW + group;
-  double* smem_group = sm_dyn + warp * SMEM_WARP_DOUBLES_C + group * chol_group_doubles<G>();
+  const bool gs = p.gsolve != nullptr;
+  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 4 * G
+                          : sm_dyn + warp * SMEM_WARP_DOUBLES_C + group * chol_group_doubles<G>();
+  double* gsol = gs ? p.gsolve + ((long long)blockIdx.x * WARPS + warp) * GSOLVE_STRIDE_C +
+                          group * gsolve_group_doubles(G)
+                    : nullptr;
   for (;;) {
     int base = 0;
     if (lane == 0) base = atomicAdd(p.queue, GPW);
@@ -114,10 +127,10 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* a = p.a + p.a_off[mat];
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
+      double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
       const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
       if (info == 0 && p.nrhs > 0)
-        potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, scr + n,
-                       scr + n + RHS_CHUNK * ldx);
+        potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
     }
     __syncwarp();
@@ -132,7 +145,7 @@ __global__ void __launch_bounds__(32) potrf_single_kernel(double* a, int n, int 
 
 template <int WARPS, int G>
 static cudaError_t launch_potrf_wg(const BatchArgs& args, int ctas, cudaStream_t s) {
-  const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES_C * WARPS;
+  const size_t smem = potrf_smem_bytes(args, WARPS);
   if (args.hw_mul)
     potrf_batched_kernel<WARPS, false, G><<<ctas, WARPS * 32, smem, s>>>(args);
   else

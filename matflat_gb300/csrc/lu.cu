@@ -176,6 +176,12 @@ __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const 
 }
 
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
+// Per-warp shared memory when the solve is staged in global memory (BatchArgs::gsolve).
+constexpr int SMEM_WARP_DOUBLES_G = SMEM_N + 2;
+
+static size_t getrf_smem_bytes(const BatchArgs& args, int warps) {
+  return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_G : SMEM_WARP_DOUBLES) * warps;
+}
 
 template <int WARPS, int IM, int DB>
 __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) {
@@ -193,14 +199,16 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
     const long long lda = p.lda[mat];
     double* a = p.a + p.a_off[mat];
     int* piv = p.piv + p.piv_off[mat];
-    double* scr = (n <= SMEM_N) ? sm_dyn + warp * SMEM_WARP_DOUBLES
+    const bool gs = p.gsolve != nullptr;
+    double* scr = (n <= SMEM_N) ? sm_dyn + warp * (gs ? SMEM_WARP_DOUBLES_G : SMEM_WARP_DOUBLES)
                                  : p.gscratch + gw * p.gscratch_stride;
+    // The solve's staging: after the column sums in the same buffer, or the warp's global slice.
+    double* sol = (n <= SMEM_N && gs) ? p.gsolve + gw * GSOLVE_STRIDE : scr + n;
     const int ldx = n | 1;
     int sign = 1, info = 0;
     if (!p.solve_only) lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
-      getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, scr + n,
-                 scr + n + RHS_CHUNK * ldx);
+      getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
     if (lane == 0 && !p.solve_only) {
       p.sign[mat] = sign;
       p.info[mat] = info;
@@ -263,7 +271,7 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
 
 template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
-  const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * WARPS;
+  const size_t smem = getrf_smem_bytes(args, WARPS);
   if (args.hw_mul == 2)
     getrf_batched_kernel<WARPS, 2, 4><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.hw_mul)

@@ -40,7 +40,24 @@ struct BatchArgs {
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4)
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
+  double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
+                             // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
+                             // sums fit in shared memory, which then holds only those sums and
+                             // leaves the rest of the SM's L1 to the matrices; null: the solves
+                             // are staged in shared memory too
 };
+// Doubles per warp of BatchArgs::gsolve: getrf (one matrix per warp), and potrf (32/G groups of
+// G lanes, each with gsolve_group_doubles(G)).
+constexpr long long GSOLVE_STRIDE = (2LL * RHS_CHUNK * (SMEM_N + 1) + 31) / 32 * 32;
+constexpr long long gsolve_group_doubles(int g) {
+  return (2LL * RHS_CHUNK * (4 * g + 1) + 31) / 32 * 32;
+}
+constexpr long long GSOLVE_STRIDE_C = 1280;
+static_assert(8 * gsolve_group_doubles(4) <= GSOLVE_STRIDE_C &&
+                  4 * gsolve_group_doubles(8) <= GSOLVE_STRIDE_C &&
+                  2 * gsolve_group_doubles(16) <= GSOLVE_STRIDE_C &&
+                  gsolve_group_doubles(32) <= GSOLVE_STRIDE_C,
+              "potrf solve staging");
 
 // Batched Householder QR (+ least-squares solve of nrhs right-hand sides, ldb = m).
 template <typename T>

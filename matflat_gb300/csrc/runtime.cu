@@ -78,6 +78,7 @@ struct mfg_plan {
   int max_n = 0;
   DevBuf meta;      // order | n | lda | a_off | piv_off | b_off | queue
   DevBuf scratch;   // per-warp scratch for n > SMEM_N
+  DevBuf gsolve;    // GETRF: per-warp global staging of the solve (BatchArgs::gsolve)
   BatchArgs args{};
   mfg::QrBatchArgs<double> qd{};
   mfg::QrBatchArgs<float> qs{};
@@ -234,6 +235,11 @@ void choose_shape(mfg_plan* p, int fixed_warps = 0) {
   p->ctas = (int)ctas;
 }
 
+// Doubles per warp of the global solve staging of a getrf / potrf plan.
+long long gsolve_stride(int kind) {
+  return kind == mfg_plan::POTRF ? mfg::GSOLVE_STRIDE_C : mfg::GSOLVE_STRIDE;
+}
+
 // Re-shapes a getrf/potrf plan: warps per CTA (1, 2, 4, 8 or 16), warps per SM, lanes per
 // matrix (potrf) and the multiply mode; grows the per-warp scratch when the new shape keeps more
 // matrices in flight, and drops the cached graph.
@@ -258,6 +264,12 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
   p->args.gscratch_stride = stride;
   p->dstride = stride;
   p->elem = 0;
+  if (p->args.gsolve) {
+    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MFG_CUDA(ctx, p->gsolve.reserve((size_t)gsolve_stride(p->kind) * sizeof(double) *
+                                    (size_t)ctas * warps));
+    p->args.gsolve = (double*)p->gsolve.ptr;
+  }
   p->args.group = g;
   p->args.hw_mul = mul;
   if (dot_block > 0) p->args.dot_block = dot_block;
@@ -488,6 +500,17 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   // the integer-pipe product, whose long dependency chains one or two warps per scheduler cannot
   // hide.
   a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
+  a.gsolve = nullptr;
+  if ((kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) && nrhs > 0 &&
+      env_int("MFG_GSOLVE", 1)) {
+    e = p->gsolve.reserve((size_t)gsolve_stride(kind) * sizeof(double) * (size_t)p->ctas *
+                          p->warps);
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_fail(ctx, e, "cudaMalloc(plan solve staging)");
+    }
+    a.gsolve = (double*)p->gsolve.ptr;
+  }
   a.group = group;
   a.dot_block = env_int("MFG_DOT_BLOCK", 4);
   p->hn.assign(n, n + count);
@@ -1888,6 +1911,7 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   pipe_release(plan);
   plan->meta.release();
   plan->scratch.release();
+  plan->gsolve.release();
   plan->mx_work.release();
   delete plan;
   return MFG_OK;
