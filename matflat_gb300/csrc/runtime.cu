@@ -1854,9 +1854,13 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
         for (int mul : {0, 2}) cands.push_back({w, wps, 32, mul, 4});
     for (int wps : {20, 24}) cands.push_back({4, wps, 32, 0, 2});
   } else {
-    for (int g : {4, 8, 16, 32})
+    // The integer-product variants need ~100 registers (up to 20 warps/SM), the FP64-pipe ones
+    // ~128 (16 warps/SM).
+    for (int g : {4, 8, 16, 32}) {
       for (int wps : {8, 16})
         for (int mul : {0, 1}) cands.push_back({4, wps, g, mul, 4});
+      cands.push_back({4, 20, g, 0, 4});
+    }
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::array<int, 5> best = cands[0];
