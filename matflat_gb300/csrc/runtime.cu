@@ -674,10 +674,13 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
     work[i] = 2.0 * m[i] * (double)n[i] * n[i] - 2.0 / 3.0 * (double)n[i] * n[i] * n[i];
     max_cols = std::max(max_cols, n[i] + nrhs);
   }
-  // Lanes per matrix: a whole warp for the double overload, half a warp for the float one (its
-  // kernel needs few registers, so two matrices per warp keep more of them in flight: measured
-  // 22 % faster on the 50,000-matrix batch); MFG_QR_GROUP = 32, 16, 8 or 4 overrides both.
-  int group_d = 32, group_s = 16;
+  // Lanes per matrix: 8 for both overloads (four matrices per warp).  On the 50,000-matrix
+  // batch (m 64..512, n 16..64) the double kernel measured 194 / 175 / 166 / 263 ms with 32 / 16
+  // / 8 / 4 lanes and the float one 180 / 154 / 210 ms with 16 / 8 / 4: the column dots (one per
+  // lane, n - k of them) fill small groups better, and four times the matrices in flight hide
+  // more of the trailing-matrix streams; 4 lanes leave too few lanes for the rank-1 updates.
+  // MFG_QR_GROUP = 32, 16, 8 or 4 overrides both.
+  int group_d = 8, group_s = 8;
   const int genv = env_int("MFG_QR_GROUP", 0);
   if (genv == 4 || genv == 8 || genv == 16 || genv == 32) group_d = group_s = genv;
   const int group = std::min(group_d, group_s);
