@@ -2151,9 +2151,13 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     per_wave = (long long)p->ctas * p->warps * (32 / p->args.group);
   else
     per_wave = (long long)p->ctas * p->warps;
-  int K = (int)std::min<long long>(16, count / std::max<long long>(1, 2 * per_wave));
+  // QR chunks hold about four rounds and at least two chunks are used: its per-matrix work
+  // spans a 128x range, so shorter chunks end in long tails (the 50,000-matrix batch measured
+  // 236 / 236 / 216 / 210 / 181 / 145 / 119 thousand matrices/s with 1 / 2 / 3 / 4 / 8 / 12 / 16
+  // chunks at 8 lanes per matrix).
+  int K = (int)std::min<long long>(16, count / std::max<long long>(1, (qr ? 4 : 2) * per_wave));
   if (count >= 8192)
-    K = std::max(K, 4);
+    K = std::max(K, qr ? 2 : 4);
   else if (count >= 2048)
     K = std::max(K, 2);
   K = env_int("MFG_PIPE_CHUNKS", std::max(K, 1));
