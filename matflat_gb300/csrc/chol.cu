@@ -54,112 +54,6 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
   return 0;
 }
 
-// Dot(c, x, y2) and Dot(c + 1, x, y3) (c even) in one pass over x: the first has pairs (0,1),
-// (2,3), ..., the second seeds with x0*y3_0 and then adds pairs (1,2), (3,4), ... (Internals.Dot,
-// MatFlat/Internals.cs:265-292).  The two independent sums share every load of x and keep two
-// dependency chains in flight per lane.
-template <bool IM>
-__device__ __forceinline__ void dual_dot(int c, const double* x, const double* y2,
-                                         const double* y3, long long inc, double& s2,
-                                         double& s3) {
-  s2 = 0.0;
-  double xe = x[0];                         // x[2i]
-  s3 = xmul<IM>(xe, y3[0]);
-  const int it = c >> 1;
-  int i = 0;
-  for (; i + 2 <= it; i += 2) {
-    const long long t = 2LL * i;
-    double xv[4], a2[4], a3[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      xv[u] = x[(t + 1 + u) * inc];          // x[2i+1 .. 2i+4]
-      a2[u] = y2[(t + u) * inc];             // y2[2i .. 2i+3]
-      a3[u] = y3[(t + 1 + u) * inc];         // y3[2i+1 .. 2i+4]
-    }
-    s2 = __dadd_rn(s2, __dadd_rn(xmul<IM>(xe, a2[0]), xmul<IM>(xv[0], a2[1])));
-    s3 = __dadd_rn(s3, __dadd_rn(xmul<IM>(xv[0], a3[0]), xmul<IM>(xv[1], a3[1])));
-    s2 = __dadd_rn(s2, __dadd_rn(xmul<IM>(xv[1], a2[2]), xmul<IM>(xv[2], a2[3])));
-    s3 = __dadd_rn(s3, __dadd_rn(xmul<IM>(xv[2], a3[2]), xmul<IM>(xv[3], a3[3])));
-    xe = xv[3];
-  }
-  for (; i < it; ++i) {
-    const long long t = 2LL * i;
-    const double x1 = x[(t + 1) * inc], x2 = x[(t + 2) * inc];
-    s2 = __dadd_rn(s2, __dadd_rn(xmul<IM>(xe, y2[t * inc]), xmul<IM>(x1, y2[(t + 1) * inc])));
-    s3 = __dadd_rn(s3, __dadd_rn(xmul<IM>(x1, y3[(t + 1) * inc]), xmul<IM>(x2, y3[(t + 2) * inc])));
-    xe = x2;
-  }
-}
-
-// The same factorization two columns per step.  Column c (even) and c + 1 finish from prefixes
-// computed one step earlier plus their last pair (Dot(c) = Dot(c - 2) + (x_{c-2} y_{c-2} +
-// x_{c-1} y_{c-1}); Dot(c + 1) = Dot(c - 1) + (x_{c-1} y_{c-1} + x_c y_c); Dot(1) is its lone
-// product), then every row j > c + 2 computes the prefixes of columns c + 2 and c + 3 (Dot(c)
-// against row c + 2 and Dot(c + 1) against row c + 3) in one dual pass over row j.  Every value
-// is formed by MatFlat's tree in MatFlat's order, so the factor is bit-identical to potrf_group's.
-// scratch: 3n doubles (the diagonal sums, then the even and odd prefixes).
-template <int G, bool IM>
-__device__ int potrf_group_ps(double* a, int n, long long lda, double* dsum) {
-  const int lane = group_lane<G>();
-  const unsigned gm = group_mask<G>();
-  double* pe = dsum + n;
-  double* po = dsum + 2 * n;
-  for (int j = lane; j < n; j += G) {
-    dsum[j] = 0.0;
-    pe[j] = 0.0;
-    po[j] = 0.0;
-  }
-  __syncwarp(gm);
-  for (int c = 0; c < n; c += 2) {
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-      const int k = c + h;
-      if (k >= n) break;
-      double* colk = a + (long long)k * lda;
-      const double s = __dsub_rn(colk[k], dsum[k]);
-      if (!positive(s)) return k + 1;  // uniform across the group
-      const double lkk = __dsqrt_rn(s);
-      __syncwarp(gm);
-      if (lane == 0) colk[k] = lkk;
-      const double* pre = h ? po : pe;
-      const double* rowk = a + k;          // L(k, t) = rowk[t * lda]
-      for (int j = k + 1 + lane; j < n; j += G) {
-        double d;
-        if (k == 0) {
-          d = 0.0;
-        } else if (k == 1) {
-          d = xmul<IM>(a[j], rowk[0]);
-        } else {
-          const double* rowj = a + j;
-          const long long t0 = (long long)(k - 2) * lda, t1 = (long long)(k - 1) * lda;
-          d = __dadd_rn(pre[j], __dadd_rn(xmul<IM>(rowj[t0], rowk[t0]),
-                                          xmul<IM>(rowj[t1], rowk[t1])));
-        }
-        const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], d), lkk);
-        colk[j] = t;
-        dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
-      }
-      __syncwarp(gm);
-    }
-    if (c + 2 < n) {
-      const bool odd = c + 3 < n;
-      for (int j = c + 3 + lane; j < n; j += G) {
-        double p2, p3;
-        dual_dot<IM>(c, a + j, a + c + 2, a + (odd ? c + 3 : c + 2), lda, p2, p3);
-        pe[j] = p2;
-        if (odd) po[j] = p3;
-      }
-      __syncwarp(gm);
-    }
-  }
-  for (int c = 1; c < n; ++c) {
-    double* col = a + (long long)c * lda;
-    for (int r = lane; r < c; r += G) col[r] = 0.0;
-  }
-  __syncwarp(gm);
-  return 0;
-}
-
 // L y = b (SolveTriangular Lower/NoTrans) then L^T x = y (Lower/Trans) for nrhs right-hand
 // sides stored column-major with leading dimension ldb.
 template <int G>
@@ -199,8 +93,8 @@ static_assert(4 * chol_group_doubles<8>() <= SMEM_WARP_DOUBLES_C, "smem layout")
 static_assert(8 * chol_group_doubles<4>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 
 // Per-warp shared memory when the solves are staged in global memory (BatchArgs::gsolve): the
-// diagonal sums and the two prefix vectors of the warp's groups only (3 x 4G doubles each).
-constexpr int SMEM_WARP_DOUBLES_CG = 3 * 4 * 32 + 2;
+// column sums of the warp's groups only (4G doubles each).
+constexpr int SMEM_WARP_DOUBLES_CG = 4 * 32 + 2;
 
 static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
@@ -215,7 +109,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
   const int group = lane / G;
   const long long gg = ((long long)blockIdx.x * WARPS + warp) * GPW + group;
   const bool gs = p.gsolve != nullptr;
-  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 3 * 4 * G
+  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 4 * G
                           : sm_dyn + warp * SMEM_WARP_DOUBLES_C + group * chol_group_doubles<G>();
   double* gsol = gs ? p.gsolve + ((long long)blockIdx.x * WARPS + warp) * GSOLVE_STRIDE_C +
                           group * gsolve_group_doubles(G)
@@ -234,9 +128,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
-      const int info = p.solve_only    ? 0
-                       : p.pair_step ? potrf_group_ps<G, IM>(a, n, lda, scr)
-                                     : potrf_group<G, IM>(a, n, lda, scr);
+      const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
       if (info == 0 && p.nrhs > 0)
         potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
