@@ -27,9 +27,29 @@ namespace {
 
 constexpr const char* kVersion = "0.1.0";
 
+// Owning device allocation (freed with its owner; movable, not copyable), so that every early
+// return of a failing set-up releases what it had reserved.
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : ptr(o.ptr), bytes(o.bytes) {
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      ptr = o.ptr;
+      bytes = o.bytes;
+      o.ptr = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   cudaError_t reserve(size_t want) {
     if (want <= bytes) return cudaSuccess;
     if (ptr) cudaFree(ptr);
