@@ -33,6 +33,7 @@ from ._api import (  # noqa: F401
     context,
     library,
     library_path,
+    selftest_ddiv,
     selftest_dmul,
 )
 
