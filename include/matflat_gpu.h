@@ -393,11 +393,6 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
  * random and edge-case operands. */
 MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
                               int64_t n);
-/* Diagnostics: out[i] = a[i] / b[i] by the reciprocal-based division the batched solves use (one
- * reciprocal per diagonal entry, each quotient checked exactly), or a NaN where it differs from
- * the IEEE round-to-nearest quotient (NaN results count as equal). */
-MFG_API int mfg_selftest_ddiv(mfg_ctx* ctx, const double* a, const double* b, double* out,
-                              int64_t n);
 
 #ifdef __cplusplus
 }

@@ -33,7 +33,6 @@ from ._api import (  # noqa: F401
     context,
     library,
     library_path,
-    selftest_ddiv,
     selftest_dmul,
 )
 

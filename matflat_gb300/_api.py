@@ -89,7 +89,6 @@ _SIGS = {
     "mfg_plan_getri_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp]),
     "mfg_dgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
-    "mfg_selftest_ddiv": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
     "mfg_plan_gesv_mixed_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _I]),
     "mfg_dgesv_mixed_batched": (_I, [_vp, _vp, _vp, _vp, _I, _I, ctypes.c_double, _vp, _vp,
                                      _vp]),
@@ -713,14 +712,6 @@ class QrBatch(_Batch):
         name = "mfg_%sgeqrs_batched" % ("s" if single else _elem(a, dtype))
         rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
         self.ctx.check(rc, name)
-
-
-def selftest_ddiv(a, b, out):
-    """out = a / b through the reciprocal-based division of the solves (device tensors of
-    float64); a NaN marks an element where it differs from the hardware division."""
-    ctx = context()
-    ctx.check(ctx.lib.mfg_selftest_ddiv(ctx.h, _dptr(a), _dptr(b), _dptr(out), a.numel()),
-              "mfg_selftest_ddiv")
 
 
 def selftest_dmul(a, b, out):

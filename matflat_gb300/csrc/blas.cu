@@ -125,28 +125,6 @@ __global__ void selftest_mul_kernel(const double* a, const double* b, double* ou
   }
 }
 
-// The reciprocal-based division (div_rn_y) against the hardware one; a disagreement is reported
-// as a NaN (NaN results compare equal).
-__global__ void selftest_div_kernel(const double* a, const double* b, double* out, long long n) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double y = __ddiv_rn(1.0, b[i]);
-    const double r0 = div_rn_y(a[i], b[i], y);
-    const double r1 = __ddiv_rn(a[i], b[i]);
-    const bool same = dbits(r0) == dbits(r1) || (r0 != r0 && r1 != r1);
-    out[i] = same ? r0 : __longlong_as_double(0x7FF8DEAD0000DEADll);
-  }
-}
-
-cudaError_t launch_selftest_div(const double* a, const double* b, double* out, long long n,
-                                cudaStream_t s) {
-  if (n <= 0) return cudaSuccess;
-  long long blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
-  selftest_div_kernel<<<(unsigned)blocks, 256, 0, s>>>(a, b, out, n);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

@@ -56,17 +56,12 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
 
 // L y = b (SolveTriangular Lower/NoTrans) then L^T x = y (Lower/Trans) for nrhs right-hand
 // sides stored column-major with leading dimension ldb.
-// rec: optional n doubles of scratch for the reciprocals of L's diagonal (see getrs_warp).
 template <int G>
 __device__ void potrs_group(const double* l, int n, long long lda, double* b, long long ldb,
-                            int nrhs, double* xs, double* acc, double* rec = nullptr) {
+                            int nrhs, double* xs, double* acc) {
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   const int ldx = n | 1;
-  if (rec) {
-    for (int i = lane; i < n; i += G) rec[i] = __ddiv_rn(1.0, l[(long long)i * lda + i]);
-    __syncwarp(gm);
-  }
   for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
     const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
     for (int e = lane; e < nr * n; e += G) {
@@ -75,8 +70,8 @@ __device__ void potrs_group(const double* l, int n, long long lda, double* b, lo
       xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + i];
     }
     __syncwarp(gm);
-    warp_solve_dot<G>(l, n, 1, lda, false, xs, ldx, acc, nr, rec);
-    warp_solve_sweep<G>(l, n, 1, lda, xs, ldx, nr, nullptr, rec);
+    warp_solve_dot<G>(l, n, 1, lda, false, xs, ldx, acc, nr);
+    warp_solve_sweep<G>(l, n, 1, lda, xs, ldx, nr);
     for (int e = lane; e < nr * n; e += G) {
       const int r = e / n;
       const int i = e - r * n;
@@ -135,8 +130,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
       const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
       if (info == 0 && p.nrhs > 0)
-        potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx,
-                       p.rec_div ? scr : nullptr);
+        potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
     }
     __syncwarp();

@@ -150,20 +150,12 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
 // b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
 // upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
 // S: the solve arithmetic of the element type (DSolve, SSolve or ZSolve<false>).
-// rec (double only): n doubles of scratch for the reciprocals of U's diagonal, computed once
-// here and shared by every right-hand side's divisions (div_rn_y: the same bits as __ddiv_rn).
 template <class S = DSolve>
 __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const int* piv,
                            typename S::T* b, long long ldb, int nrhs, typename S::T* xs,
-                           typename S::Acc* acc, typename S::T* rec = nullptr) {
+                           typename S::Acc* acc) {
   const int lane = threadIdx.x & 31;
   const int ldx = n | 1;
-  if constexpr (S::kRec) {
-    if (rec) {
-      for (int i = lane; i < n; i += 32) rec[i] = __ddiv_rn(1.0, lu[(long long)i * lda + i]);
-      __syncwarp();
-    }
-  }
   for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
     const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
     for (int e = lane; e < nr * n; e += 32) {
@@ -173,7 +165,7 @@ __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const 
     }
     __syncwarp();
     warp_solve_dot<32, S>(lu, n, 1, lda, true, xs, ldx, acc, nr);
-    warp_solve_sweep<32, S>(lu, n, lda, 1, xs, ldx, nr, nullptr, rec);
+    warp_solve_sweep<32, S>(lu, n, lda, 1, xs, ldx, nr);
     for (int e = lane; e < nr * n; e += 32) {
       const int r = e / n;
       const int i = e - r * n;
@@ -216,8 +208,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
     int sign = 1, info = 0;
     if (!p.solve_only) lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
-      getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx,
-                 p.rec_div ? scr : nullptr);
+      getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
     if (lane == 0 && !p.solve_only) {
       p.sign[mat] = sign;
       p.info[mat] = info;

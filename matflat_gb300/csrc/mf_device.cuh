@@ -58,36 +58,6 @@ __device__ __forceinline__ bool is_nan(double v) {
   return (dbits(v) & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
 }
 
-// a / d correctly rounded, given y = RN(1/d) (one __ddiv_rn(1.0, d) per divisor, shared by many
-// quotients).  Markstein's correction step (P. Markstein, "Computation of elementary functions on
-// the IBM RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990) forms the candidate
-// q = RN(q0 + r0 y) from q0 = RN(a y) and r0 = a - q0 d (one FMA each).  The candidate is then
-// checked exactly from its own remainder r = RN(a - q d): q is the correctly rounded quotient
-// when a/d lies strictly inside q's rounding interval, i.e. |a - q d| < |d| ulp(q)/2 on the side
-// away from zero, |d| ulp(q)/4 toward zero when |q| is a power of two (the binade below is twice
-// as fine).  The bound is a representable number and rounding is monotonic, so |r| below it
-// implies the exact |a - q d| below it, whether or not r itself is exact.  Ties, anything the
-// correction step misses, and operands or quotients within 2^64 of the ends of the exponent range
-// take __ddiv_rn, so the result is __ddiv_rn(a, d) for every input.
-__device__ __forceinline__ double div_rn_y(double a, double d, double y) {
-  const double q0 = __dmul_rn(a, y);
-  const double r0 = __fma_rn(-q0, d, a);
-  const double q = __fma_rn(r0, y, q0);
-  const double r = __fma_rn(-q, d, a);
-  const unsigned long long A = dbits(a), D = dbits(d), Q = dbits(q), R = dbits(r);
-  const int ea = (int)((A >> 52) & 0x7FF), ed = (int)((D >> 52) & 0x7FF);
-  const int eq = (int)((Q >> 52) & 0x7FF);
-  // |d| ulp(q) / 2 = |d| 2^(eq - 1076): its exponent field is ed + eq - 1076, about ea - 53.
-  const unsigned long long hup =
-      (D & 0x7FFFFFFFFFFFFFFFull) + ((unsigned long long)(long long)(eq - 1076) << 52);
-  const bool pow2 = (Q & 0x000FFFFFFFFFFFFFull) == 0ull;
-  const bool up = ((R ^ Q ^ D) >> 63) == 0ull;  // a/d lies beyond q, away from zero
-  const unsigned long long bound = (up || !pow2) ? hup : hup - (1ull << 52);
-  const bool ok = (unsigned)(ea - 64) < 1920u && (unsigned)(ed - 64) < 1920u &&
-                  (unsigned)(eq - 64) < 1920u && (R & 0x7FFFFFFFFFFFFFFFull) < bound;
-  return ok ? q : __ddiv_rn(a, d);
-}
-
 // Pivot key.  MatFlat's scan (Factorization.Lu.cs:323-330) keeps p = j and moves to i only when
 // |w_i| > |w_p|.  If w_j is NaN nothing ever beats it; otherwise the winner is the first index
 // attaining the largest |w| among the non-NaN entries.  The key orders |w| by its bit pattern

@@ -40,8 +40,6 @@ struct BatchArgs {
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4)
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
-  int rec_div;               // getrf/potrf: the solves divide through reciprocals of the
-                             // diagonal checked exactly (div_rn_y) instead of full divisions
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and
@@ -106,10 +104,6 @@ cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const 
 
 // Diagnostics: out[i] = the integer-pipe product of a[i] and b[i] (device pointers).
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
-                                cudaStream_t s);
-// Diagnostics: out[i] = a[i] / b[i] through the reciprocal-based division of the solves, or a
-// NaN where it differs from __ddiv_rn.
-cudaError_t launch_selftest_div(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s);
 
 // Batched loss = y^T K^-1 y + log det K and its gradient K^-1 - alpha alpha^T (n <= 128; see

@@ -41,13 +41,6 @@ __device__ __forceinline__ unsigned group_mask() {
 struct DSolve {
   using T = double;
   using Acc = double;
-  // The divisions can use reciprocals of the diagonal computed ahead (div_rn_y: same bits).
-  static constexpr bool kRec = true;
-  static __device__ __forceinline__ T fin_y(T x, Acc s, T d, T y) {
-    return div_rn_y(__dsub_rn(x, s), d, y);
-  }
-  static __device__ __forceinline__ T fin0_y(T x, T d, T y) { return div_rn_y(x, d, y); }
-  static __device__ __forceinline__ T sdiv_y(T x, T d, T y) { return div_rn_y(x, d, y); }
   static __device__ __forceinline__ Acc zero() { return 0.0; }
   static __device__ __forceinline__ Acc prod(T a, T x) { return __dmul_rn(a, x); }
   static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
@@ -65,7 +58,6 @@ struct DSolve {
 struct SSolve {
   using T = float;
   using Acc = double;
-  static constexpr bool kRec = false;
   static __device__ __forceinline__ Acc zero() { return 0.0; }
   static __device__ __forceinline__ Acc prod(T a, T x) { return __dmul_rn((double)a, (double)x); }
   static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
@@ -88,7 +80,6 @@ template <bool CONJ>
 struct ZSolve {
   using T = zdouble;
   using Acc = zdouble;
-  static constexpr bool kRec = false;
   static __device__ __forceinline__ zdouble m(zdouble a, zdouble x) {
     return CONJ ? zmulconj(a, x) : zmul(a, x);
   }
@@ -110,13 +101,10 @@ struct ZSolve {
 // Dot form.  Element (i, t), t < i, of the triangular operand is at a[i*si + t*st] and the
 // diagonal at a[i*si + i*st].  With unit = true the division is skipped: MatFlat's unit-lower
 // idiom divides by an explicit 1.0 (Factorization.LuInverse.cs:174-182), which is exact.
-// rec (double only, optional): rec[i] = RN(1 / diagonal i), so that each division is a
-// reciprocal-based one checked exactly (div_rn_y) instead of a full division.
 template <int G = 32, class Tr = DSolve>
 __device__ __forceinline__ void warp_solve_dot(const typename Tr::T* a, int n, long long si,
                                                long long st, bool unit, typename Tr::T* xs,
-                                               int ldx, typename Tr::Acc* acc, int nr,
-                                               const typename Tr::T* rec = nullptr) {
+                                               int ldx, typename Tr::Acc* acc, int nr) {
   using T = typename Tr::T;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
@@ -130,13 +118,6 @@ __device__ __forceinline__ void warp_solve_dot(const typename Tr::T* a, int n, l
     for (int r = lane; r < nr; r += G) {
       const T v = xs[r * ldx + t];
       const T d = a[t * si + t * st];
-      if constexpr (Tr::kRec) {
-        if (rec && !unit) {
-          xs[r * ldx + t] =
-              (t > 0) ? Tr::fin_y(v, acc[r * ldx + t], d, rec[t]) : Tr::fin0_y(v, d, rec[t]);
-          continue;
-        }
-      }
       xs[r * ldx + t] = (t > 0) ? Tr::fin(v, acc[r * ldx + t], d, unit) : Tr::fin0(v, d, unit);
     }
     __syncwarp(gm);
@@ -159,28 +140,18 @@ __device__ __forceinline__ void warp_solve_dot(const typename Tr::T* a, int n, l
 }
 
 // Column sweep.  Element (r, i), r < i, is at a[i*si + r*sr]; the diagonal at a[i*si + i*sr], or
-// at diag[i] when diag is given (the R factor of QR keeps its diagonal apart, in rdiag); rec as
-// in warp_solve_dot.
+// at diag[i] when diag is given (the R factor of QR keeps its diagonal apart, in rdiag).
 template <int G = 32, class Tr = DSolve>
 __device__ __forceinline__ void warp_solve_sweep(const typename Tr::T* a, int n, long long si,
                                                  long long sr, typename Tr::T* xs, int ldx,
-                                                 int nr, const typename Tr::T* diag = nullptr,
-                                                 const typename Tr::T* rec = nullptr) {
+                                                 int nr, const typename Tr::T* diag = nullptr) {
   using T = typename Tr::T;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int i = n - 1; i >= 0; --i) {
     const T* ai = a + i * si;
     const T d = diag ? diag[i] : ai[i * sr];
-    for (int r = lane; r < nr; r += G) {
-      if constexpr (Tr::kRec) {
-        if (rec) {
-          xs[r * ldx + i] = Tr::sdiv_y(xs[r * ldx + i], d, rec[i]);
-          continue;
-        }
-      }
-      xs[r * ldx + i] = Tr::sdiv(xs[r * ldx + i], d);
-    }
+    for (int r = lane; r < nr; r += G) xs[r * ldx + i] = Tr::sdiv(xs[r * ldx + i], d);
     __syncwarp(gm);
     for (int e = lane; e < nr * i; e += G) {
       const int q = e / nr;

@@ -520,7 +520,6 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   // the integer-pipe product, whose long dependency chains one or two warps per scheduler cannot
   // hide.
   a.hw_mul = kind == mfg_plan::GETRI ? env_int("MFG_INV_HW_MUL", 1) : env_int("MFG_HW_MUL", 0);
-  a.rec_div = env_int("MFG_REC_DIV", 1);
   a.gsolve = nullptr;
   if ((kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) && nrhs > 0 &&
       env_int("MFG_GSOLVE", 1)) {
@@ -2580,15 +2579,6 @@ MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, do
   if (n < 0) return fail(ctx, -5, "n must be >= 0");
   if (n > 0 && (!a || !b || !out)) return fail(ctx, !a ? -2 : (!b ? -3 : -4), "null pointer");
   MFG_CUDA(ctx, mfg::launch_selftest_mul(a, b, out, n, ctx->stream));
-  return MFG_OK;
-}
-
-MFG_API int mfg_selftest_ddiv(mfg_ctx* ctx, const double* a, const double* b, double* out,
-                              int64_t n) {
-  if (!ctx) return -1;
-  if (n < 0) return fail(ctx, -5, "n must be >= 0");
-  if (n > 0 && (!a || !b || !out)) return fail(ctx, !a ? -2 : (!b ? -3 : -4), "null pointer");
-  MFG_CUDA(ctx, mfg::launch_selftest_div(a, b, out, n, ctx->stream));
   return MFG_OK;
 }
 

@@ -57,51 +57,3 @@ def test_integer_product_is_ieee(mf):
     np.testing.assert_array_equal(gn, en)
     bad = np.nonzero(got.view(np.uint64)[~gn] != exp.view(np.uint64)[~en])[0]
     assert bad.size == 0, (a[~gn][bad[:5]], b[~gn][bad[:5]], got[~gn][bad[:5]], exp[~en][bad[:5]])
-
-
-def _div_operands(rng, n):
-    parts = []
-    a = rng.standard_normal(n)
-    parts.append((a * np.ldexp(1.0, rng.integers(-200, 200, n)),
-                  rng.standard_normal(n) * np.ldexp(1.0, rng.integers(-200, 200, n))))
-    # short significands: exact quotients and quotients close to a rounding boundary
-    m1 = rng.integers(1, 2 ** 20, n).astype(np.float64)
-    m2 = rng.integers(1, 2 ** 12, n).astype(np.float64)
-    parts.append((m1 * rng.choice([1.0, -1.0], n), m2))
-    # quotients at and next to powers of two (the binade below is twice as fine)
-    d = rng.standard_normal(n)
-    q = np.ldexp(1.0, rng.integers(-8, 8, n)) * (1 + rng.integers(-3, 4, n) * 2.0 ** -52)
-    prod = d * q
-    parts.append((prod, d))
-    parts.append((np.nextafter(prod, np.inf), d))
-    parts.append((np.nextafter(prod, -np.inf), d))
-    # the edges of the exponent range (the checked path hands these to the hardware division)
-    parts.append((np.ldexp(1.0 + rng.random(n), rng.integers(-1074, 1024, n)),
-                  np.ldexp(1.0 + rng.random(n), rng.integers(-1074, 1024, n))))
-    # zeros, infinities, NaN, random bit patterns
-    parts.append((rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64),
-                  rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(np.float64)))
-    parts.append((rng.choice([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0], n),
-                  rng.choice([0.0, -0.0, np.inf, 3.0, -2.0, 5e-324], n)))
-    return np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts])
-
-
-def test_reciprocal_division_is_ieee(mf):
-    """The solves' division through a precomputed reciprocal (div_rn_y) equals the IEEE
-    round-to-nearest quotient bit for bit; the self-test kernel also compares it with the
-    hardware division on the device."""
-    import torch
-    rng = np.random.default_rng(97)
-    a, b = _div_operands(rng, 1 << 18)
-    da = torch.from_numpy(a).cuda()
-    db = torch.from_numpy(b).cuda()
-    out = torch.empty_like(da)
-    mf.selftest_ddiv(da, db, out)
-    mf.context().synchronize()
-    got = out.cpu().numpy()
-    with np.errstate(all="ignore"):
-        exp = a / b
-    gn, en = np.isnan(got), np.isnan(exp)
-    np.testing.assert_array_equal(gn, en)
-    bad = np.nonzero(got.view(np.uint64)[~gn] != exp.view(np.uint64)[~en])[0]
-    assert bad.size == 0, (a[~gn][bad[:5]], b[~gn][bad[:5]], got[~gn][bad[:5]], exp[~en][bad[:5]])
