@@ -202,6 +202,15 @@ MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double
 MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k, double* y,
                                                      double* loss, double* grad, int* info,
                                                      int keep_factor);
+/* The float and Complex overloads' host-buffer forms (Complex: interleaved (re, im) doubles;
+ * the Complex QR's rdiag is real). */
+MFG_API int mfg_sgetrf_batched_host(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
+                                    int* info);
+MFG_API int mfg_zgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                                    int* info);
+MFG_API int mfg_spotrf_batched_host(mfg_plan* plan, float* a, float* b, int* info);
+MFG_API int mfg_zpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info);
+MFG_API int mfg_zgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b);
 /* Solve only, with factors and pivots already in a and piv (from mfg_dgetrf_batched or
  * Factorization.Lu): b' = P b, the unit-lower solve (LuInverse idiom, Factorization.LuInverse.cs:
  * 174-182) and the upper solve (Blas.SolveTriangular.cs:191-199), for the plan's nrhs (>= 1)

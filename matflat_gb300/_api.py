@@ -72,6 +72,11 @@ _SIGS = {
     "mfg_dgetri_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dgeqrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgeqrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zgeqrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_sgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_zgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mfg_spotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zpotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_logdet_solve_grad_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
@@ -490,12 +495,14 @@ class LuBatch(_Batch):
                                          _dptr(info))
         self.ctx.check(rc, name)
 
-    def run_host(self, a, piv, b, sign, info):
+    def run_host(self, a, piv, b, sign, info, dtype=None):
         """Factor + solve on host buffers (numpy arrays or CPU tensors, page-locked for full
-        speed); copies and compute are pipelined over chunks of the batch.  Synchronous."""
-        rc = self.ctx.lib.mfg_dgetrf_batched_host(self.h, _hptr(a), _hptr(piv), _hptr(b),
-                                                  _hptr(sign), _hptr(info))
-        self.ctx.check(rc, "mfg_dgetrf_batched_host")
+        speed); copies and compute are pipelined over chunks of the batch.  Synchronous.
+        Element type as in `run`."""
+        name = "mfg_%sgetrf_batched_host" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _hptr(a), _hptr(piv), _hptr(b), _hptr(sign),
+                                         _hptr(info))
+        self.ctx.check(rc, name)
 
     def solve(self, a, piv, b, dtype=None):
         """Solves with factors and pivots already in a and piv (the plan's nrhs columns of b);
@@ -639,10 +646,12 @@ class CholeskyBatch(_Batch):
         rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(b), _dptr(info))
         self.ctx.check(rc, name)
 
-    def run_host(self, a, b, info):
-        """Factor + solve on host arrays, copies pipelined with compute.  Synchronous."""
-        rc = self.ctx.lib.mfg_dpotrf_batched_host(self.h, _hptr(a), _hptr(b), _hptr(info))
-        self.ctx.check(rc, "mfg_dpotrf_batched_host")
+    def run_host(self, a, b, info, dtype=None):
+        """Factor + solve on host arrays, copies pipelined with compute.  Synchronous.  Element
+        type as in `run`."""
+        name = "mfg_%spotrf_batched_host" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _hptr(a), _hptr(b), _hptr(info))
+        self.ctx.check(rc, name)
 
     def loss_and_grad_host(self, k, y, loss, grad, info, keep_factor=True):
         """loss_and_grad on host arrays, copies pipelined with compute.  Synchronous."""
@@ -700,11 +709,12 @@ class QrBatch(_Batch):
         rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(rdiag), _dptr(b))
         self.ctx.check(rc, name)
 
-    def run_host(self, a, rdiag, b=None, single=False):
-        """QR (+ least squares) on host arrays, copies pipelined with compute.  Synchronous."""
-        fn = self.ctx.lib.mfg_sgeqrf_batched_host if single else self.ctx.lib.mfg_dgeqrf_batched_host
-        rc = fn(self.h, _hptr(a), _hptr(rdiag), _hptr(b))
-        self.ctx.check(rc, "mfg_geqrf_batched_host")
+    def run_host(self, a, rdiag, b=None, single=False, dtype=None):
+        """QR (+ least squares) on host arrays, copies pipelined with compute.  Synchronous.
+        Element type as in `run`."""
+        name = "mfg_%sgeqrf_batched_host" % ("s" if single else _elem(a, dtype))
+        rc = getattr(self.ctx.lib, name)(self.h, _hptr(a), _hptr(rdiag), _hptr(b))
+        self.ctx.check(rc, name)
 
     def solve(self, a, rdiag, b, single=False, dtype=None):
         """Least squares with the factorization already in a and rdiag (nrhs columns of b);

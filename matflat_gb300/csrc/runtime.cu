@@ -2061,7 +2061,20 @@ namespace {
 // whose offsets address device mirrors of the caller's arrays (laid out exactly like the host
 // arrays).  Chunk c's upload (stream h2d), kernel (one of two compute streams) and download
 // (stream d2h) overlap with the neighbouring chunks', so the copies hide behind the compute.
-enum PipeOp { OP_GETRF, OP_POTRF, OP_GRAD, OP_GETRI, OP_GEQRF_D, OP_GEQRF_S, OP_GEVD };
+enum PipeOp {
+  OP_GETRF, OP_POTRF, OP_GRAD, OP_GETRI, OP_GEQRF_D, OP_GEQRF_S, OP_GEVD,
+  OP_GETRF_S, OP_GETRF_Z, OP_POTRF_S, OP_POTRF_Z, OP_GEQRF_Z
+};
+
+// Element type of an operation's factor arrays: 0 double, 1 float, 2 Complex.
+int pipe_elem(int op) {
+  switch (op) {
+    case OP_GETRF_S: case OP_POTRF_S: case OP_GEQRF_S: return 1;
+    case OP_GETRF_Z: case OP_POTRF_Z: case OP_GEQRF_Z: return 2;
+    default: return 0;
+  }
+}
+bool pipe_qr(int op) { return op == OP_GEQRF_D || op == OP_GEQRF_S || op == OP_GEQRF_Z; }
 
 void pipe_release(mfg_plan* p) {
   auto& pp = p->pipe;
@@ -2086,8 +2099,10 @@ void pipe_release(mfg_plan* p) {
 void pipe_arrays(mfg_plan* p, int op, int keep_factor) {
   auto& arr = p->pipe.arr;
   const int count = p->count, nrhs = p->nrhs;
-  const bool qr = op == OP_GEQRF_D || op == OP_GEQRF_S;
-  const size_t es = op == OP_GEQRF_S ? 4 : 8;
+  const bool qr = pipe_qr(op);
+  const int elem = pipe_elem(op);
+  const size_t es = elem == 1 ? 4 : elem == 2 ? 16 : 8;  // factor and right-hand-side elements
+  const size_t rs = elem == 1 ? 4 : 8;                    // QR's rdiag (real for Complex)
   auto add = [&](int dir, size_t esz, auto beg, auto len) {
     mfg_plan::PipeArray a;
     a.dir = dir;
@@ -2105,17 +2120,21 @@ void pipe_arrays(mfg_plan* p, int op, int keep_factor) {
   auto self = [](int i) { return (size_t)i; };
   auto one = [](int) { return (size_t)1; };
   switch (op) {
-    case OP_GETRF:  // a, b, piv, sign, info
-      add(3, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
-      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+    case OP_GETRF:
+    case OP_GETRF_S:
+    case OP_GETRF_Z:  // a, b, piv, sign, info
+      add(3, es, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
           [&](int i) { return (size_t)p->hn[i] * nrhs; });
       add(2, 4, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
       add(2, 4, self, one);
       add(2, 4, self, one);
       break;
-    case OP_POTRF:  // a, b, info
-      add(3, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
-      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+    case OP_POTRF:
+    case OP_POTRF_S:
+    case OP_POTRF_Z:  // a, b, info
+      add(3, es, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
           [&](int i) { return (size_t)p->hn[i] * nrhs; });
       add(2, 4, self, one);
       break;
@@ -2132,9 +2151,10 @@ void pipe_arrays(mfg_plan* p, int op, int keep_factor) {
       add(2, 4, self, one);
       break;
     case OP_GEQRF_D:
-    case OP_GEQRF_S:  // a, rdiag, b
+    case OP_GEQRF_S:
+    case OP_GEQRF_Z:  // a, rdiag, b
       add(3, es, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
-      add(2, es, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
+      add(2, rs, [&](int i) { return (size_t)p->hpivoff[i]; }, [&](int i) { return (size_t)p->hn[i]; });
       add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
           [&](int i) { return (size_t)p->hm[i] * nrhs; });
       break;
@@ -2154,7 +2174,7 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
   pipe_release(p);
   auto& pp = p->pipe;
   const int count = p->count;
-  const bool qr = op == OP_GEQRF_D || op == OP_GEQRF_S;
+  const bool qr = pipe_qr(op);
   pipe_arrays(p, op, keep_factor);
   // Chunks of about equal work (n^3, or m n^2 for QR), each about two full rounds of the GPU's
   // resident warps (shorter chunks leave SMs idle in their tails), at least four for batches of
@@ -2165,6 +2185,8 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     per_wave = (long long)ctx->sm_count * mfg::grad_ctas_per_sm() * mfg::grad_warps_per_cta();
   else if (op == OP_GEQRF_D)
     per_wave = (long long)p->ctas * p->warps * (32 / p->qd.group);
+  else if (op == OP_GEQRF_Z)
+    per_wave = (long long)p->ctas * p->warps;
   else if (op == OP_GEQRF_S)
     per_wave = (long long)p->ctas * p->warps * (32 / p->qs.group);
   else if (p->kind == mfg_plan::POTRF)
@@ -2252,9 +2274,15 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     if (rc != MFG_OK) return rc;
     pp.chunk.push_back(sub);
     if (p->kind == mfg_plan::GETRF || p->kind == mfg_plan::POTRF) {
-      // Same launch shape as the parent plan (which the autotuner may have chosen).
+      // Same launch shape as the parent plan (which the autotuner may have chosen), then the
+      // element type's scratch.
       rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
                         p->args.group, p->args.hw_mul, p->args.dot_block);
+      if (rc == MFG_OK) rc = plan_set_elem(sub, pipe_elem(op));
+      if (rc != MFG_OK) return rc;
+    }
+    if (op == OP_GEQRF_Z) {
+      rc = zqr_prepare(sub);
       if (rc != MFG_OK) return rc;
     }
     pp.c0.push_back(c0);
@@ -2302,6 +2330,8 @@ int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> 
     int rc = MFG_OK;
     switch (op % 100) {
       case OP_GETRF:
+      case OP_GETRF_S:
+      case OP_GETRF_Z:
         sub->args.a = (double*)dev(0);
         sub->args.b = p->nrhs > 0 ? (double*)dev(1) : nullptr;
         sub->args.piv = (int*)dev(2);
@@ -2311,6 +2341,8 @@ int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> 
         rc = plan_launch(sub, sc);
         break;
       case OP_POTRF:
+      case OP_POTRF_S:
+      case OP_POTRF_Z:
         sub->args.a = (double*)dev(0);
         sub->args.b = p->nrhs > 0 ? (double*)dev(1) : nullptr;
         sub->args.info = (int*)dev(2) + c0;
@@ -2353,6 +2385,14 @@ int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> 
         sub->qs.solve_only = 0;
         rc = plan_launch(sub, sc);
         break;
+      case OP_GEQRF_Z:
+        sub->qr_float = 2;
+        sub->qz.a = (double*)dev(0);
+        sub->qz.rdiag = (double*)dev(1);
+        sub->qz.b = p->nrhs > 0 ? (double*)dev(2) : nullptr;
+        sub->qz.solve_only = 0;
+        rc = plan_launch(sub, sc);
+        break;
       case OP_GEVD:
         sub->gv.a = (const double*)dev(0);
         sub->gv.b = (double*)dev(1);
@@ -2391,6 +2431,56 @@ MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double*
   if (!sign) return fail(ctx, -5, "sign is null");
   if (!info) return fail(ctx, -6, "info is null");
   return pipe_run(plan, OP_GETRF, 0, {a, b, piv, sign, info});
+}
+
+static int getrf_host_any(mfg_plan* plan, int op, void* a, int* piv, void* b, int* sign,
+                          int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!piv) return fail(ctx, -3, "piv is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  if (!sign) return fail(ctx, -5, "sign is null");
+  if (!info) return fail(ctx, -6, "info is null");
+  return pipe_run(plan, op, 0, {a, b, piv, sign, info});
+}
+
+static int potrf_host_any(mfg_plan* plan, int op, void* a, void* b, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -3, "b is null");
+  if (!info) return fail(ctx, -4, "info is null");
+  return pipe_run(plan, op, 0, {a, b, info});
+}
+
+MFG_API int mfg_sgetrf_batched_host(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
+                                    int* info) {
+  return getrf_host_any(plan, OP_GETRF_S, a, piv, b, sign, info);
+}
+MFG_API int mfg_zgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
+                                    int* info) {
+  return getrf_host_any(plan, OP_GETRF_Z, a, piv, b, sign, info);
+}
+MFG_API int mfg_spotrf_batched_host(mfg_plan* plan, float* a, float* b, int* info) {
+  return potrf_host_any(plan, OP_POTRF_S, a, b, info);
+}
+MFG_API int mfg_zpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info) {
+  return potrf_host_any(plan, OP_POTRF_Z, a, b, info);
+}
+MFG_API int mfg_zgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (!rdiag) return fail(ctx, -3, "rdiag is null");
+  if (plan->nrhs > 0 && !b) return fail(ctx, -4, "b is null");
+  return pipe_run(plan, OP_GEQRF_Z, 0, {a, rdiag, b});
 }
 
 MFG_API int mfg_dpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info) {

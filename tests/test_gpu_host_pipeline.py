@@ -142,3 +142,85 @@ def test_host_pipeline_other_operations(mf):
     assert_bits(hb.numpy(), _host(vb))
     assert_bits(hc.numpy(), _host(vc))
     np.testing.assert_array_equal(hinf.numpy(), _host(vi))
+
+
+def _flat(x):
+    return x.view(np.float64) if x.dtype == np.complex128 else x
+
+
+def _draw(rng, k, dt):
+    if dt == np.complex128:
+        return rng.standard_normal(k) + 1j * rng.standard_normal(k)
+    return rng.standard_normal(k).astype(dt)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex128])
+def test_host_pipeline_float_complex(mf, dt):
+    """The float and Complex host-buffer forms of the batched LU, Cholesky and (Complex) QR
+    equal their device-buffer forms bit for bit (orders above 128 use the global scratch)."""
+    import torch
+    rng = np.random.default_rng(66 + (dt == np.complex128))
+    count = 9000
+    n = rng.integers(1, 141, size=count).astype(np.int32)
+    a_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    b_off = np.concatenate([[0], np.cumsum(2 * n.astype(np.int64))[:-1]]).astype(np.int64)
+    atot, ptot, btot = int((n.astype(np.int64) ** 2).sum()), int(n.sum()), int(2 * n.sum())
+    # LU + 2-RHS solve
+    a, b = _draw(rng, atot, dt), _draw(rng, btot, dt)
+    lu = mf.LuBatch(n, a_off, piv_off, nrhs=2, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(ptot, dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(count, dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(count, dtype=torch.int32, device="cuda")
+    lu.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    ha, hb = a.copy(), b.copy()
+    hpiv = np.zeros(ptot, np.int32)
+    hsign = np.zeros(count, np.int32)
+    hinfo = np.zeros(count, np.int32)
+    lu.run_host(ha, hpiv, hb, hsign, hinfo)
+    assert_bits(_flat(ha), _flat(_host(da)))
+    assert_bits(_flat(hb), _flat(_host(db)))
+    np.testing.assert_array_equal(hpiv, _host(dpiv))
+    np.testing.assert_array_equal(hsign, _host(dsign))
+    lu.close()
+    # Cholesky + 2-RHS solve of Hermitian positive definite matrices
+    mats = []
+    for ni in n:                                # (B + B^H) / 2 + 2n I: positive definite
+        m = _draw(rng, int(ni) * int(ni), dt).reshape(ni, ni)
+        mats.append(((m + m.conj().T) / 2 + 2 * ni * np.eye(ni)).astype(dt).flatten(order="F"))
+    s = np.concatenate(mats)
+    ch = mf.CholeskyBatch(n, a_off, nrhs=2, b_off=b_off)
+    ds, db = _dev(s), _dev(b)
+    dinfo = torch.zeros(count, dtype=torch.int32, device="cuda")
+    ch.run(ds, db, dinfo)
+    mf.context().synchronize()
+    hs, hb = s.copy(), b.copy()
+    hinfo = np.zeros(count, np.int32)
+    ch.run_host(hs, hb, hinfo)
+    np.testing.assert_array_equal(hinfo, _host(dinfo))
+    assert_bits(_flat(hs), _flat(_host(ds)))
+    assert_bits(_flat(hb), _flat(_host(db)))
+    ch.close()
+    if dt != np.complex128:
+        return
+    # Complex QR + least squares (rdiag real)
+    qn = rng.integers(1, 40, size=3000).astype(np.int32)
+    qm = (qn + rng.integers(0, 100, size=3000)).astype(np.int32)
+    sz = qm.astype(np.int64) * qn
+    qa_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    r_off = np.concatenate([[0], np.cumsum(qn.astype(np.int64))[:-1]]).astype(np.int64)
+    qb_off = np.concatenate([[0], np.cumsum(qm.astype(np.int64))[:-1]]).astype(np.int64)
+    qa, qb = _draw(rng, int(sz.sum()), dt), _draw(rng, int(qm.sum()), dt)
+    qr = mf.QrBatch(qm, qn, qa_off, r_off, nrhs=1, b_off=qb_off)
+    da, db = _dev(qa), _dev(qb)
+    dr = torch.zeros(int(qn.sum()), dtype=torch.float64, device="cuda")
+    qr.run(da, dr, db)
+    mf.context().synchronize()
+    ha, hb, hr = qa.copy(), qb.copy(), np.zeros(int(qn.sum()))
+    qr.run_host(ha, hr, hb)
+    assert_bits(_flat(ha), _flat(_host(da)))
+    assert_bits(hr, _host(dr))
+    assert_bits(_flat(hb), _flat(_host(db)))
+    qr.close()
