@@ -89,18 +89,24 @@ struct ZSolve {
   static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
     return zadd(s, zadd(m(a0, x0), m(a1, x1)));
   }
+  // A unit diagonal is still divided by: the LuInverse idiom stores Complex(1, 0) there, and
+  // Complex division by (1, 0) is not the identity (a signed zero can flip, an infinite part
+  // turns the other part into NaN).
   static __device__ __forceinline__ T fin(T x, Acc s, T d, bool unit) {
     const zdouble v = zsub(x, s);
-    return unit ? v : zdiv(v, dg(d));
+    return zdiv(v, unit ? zmake(1.0, 0.0) : dg(d));
   }
-  static __device__ __forceinline__ T fin0(T x, T d, bool unit) { return unit ? x : zdiv(x, dg(d)); }
+  static __device__ __forceinline__ T fin0(T x, T d, bool unit) {
+    return zdiv(x, unit ? zmake(1.0, 0.0) : dg(d));
+  }
   static __device__ __forceinline__ T sdiv(T x, T d) { return zdiv(x, dg(d)); }
   static __device__ __forceinline__ T msub(T x, T a, T xi) { return zsub(x, m(a, xi)); }
 };
 
 // Dot form.  Element (i, t), t < i, of the triangular operand is at a[i*si + t*st] and the
-// diagonal at a[i*si + i*st].  With unit = true the division is skipped: MatFlat's unit-lower
-// idiom divides by an explicit 1.0 (Factorization.LuInverse.cs:174-182), which is exact.
+// diagonal at a[i*si + i*st].  With unit = true the diagonal is taken as one: MatFlat's
+// unit-lower idiom divides by an explicit 1.0 (Factorization.LuInverse.cs:174-182), which is
+// exact for double and float (the division is skipped) and done as a division for Complex.
 template <int G = 32, class Tr = DSolve>
 __device__ __forceinline__ void warp_solve_dot(const typename Tr::T* a, int n, long long si,
                                                long long st, bool unit, typename Tr::T* xs,

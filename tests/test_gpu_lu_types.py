@@ -122,3 +122,31 @@ def test_lu_batched_types_share_a_plan(mf):
     assert_bits(_host(da), oa.view(np.float64))
     assert_bits(_host(db), ob.view(np.float64))
     batch.close()
+
+
+def test_complex_unit_lower_divides_by_one(mf):
+    """MatFlat's unit-lower idiom divides by an explicit Complex(1, 0); for Complex that division
+    is not the identity on signed zeros, and the batched solve must reproduce it."""
+    import torch
+    n = np.array([1, 3, 4], np.int32)
+    a_off = np.array([0, 1, 10], np.int64)
+    piv_off = np.array([0, 1, 4], np.int64)
+    b_off = np.array([0, 2, 8], np.int64)
+    a = np.zeros(26, np.complex128)
+    a[0] = 1.0
+    a[1:10] = np.diag([1.0, 2.0, 1.0 + 1.0j]).flatten(order="F")
+    a[10:26] = (np.eye(4) + np.tril(np.full((4, 4), 0.5), -1)).flatten(order="F")
+    b = np.full(16, complex(-0.0, -0.0))
+    b[3] = complex(-0.0, 1.0)
+    b[9] = complex(1.0, -0.0)
+    oa, ob, opiv, osign = _oracle(n, a_off, piv_off, b_off, a, b, 2, 8)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=2, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(8, dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(3, dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(3, dtype=torch.int32, device="cuda")
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    assert_bits(_host(da).view(np.float64), oa.view(np.float64))
+    assert_bits(_host(db).view(np.float64), ob.view(np.float64))
+    assert np.signbit(ob.view(np.float64)).any() and not np.signbit(ob.view(np.float64)).all()
