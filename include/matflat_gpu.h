@@ -157,6 +157,10 @@ MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k,
  * *info = 1 when a diagonal entry of U is zero (MatFlat throws "The matrix is not invertible."),
  * in which case a is left unchanged. */
 MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info);
+/* The float and Complex overloads (MatFlat/Factorization.LuInverse.cs:27-103, :219-295; Complex
+ * as interleaved (re, im) doubles, singular when a diagonal entry is exactly 0 + 0i). */
+MFG_API int mfg_sgetri(mfg_ctx* ctx, int n, float* a, int lda, const int* piv, int* info);
+MFG_API int mfg_zgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info);
 
 /* ---------------------------------------------------------------------------------------------
  * Batched overloads (new).  A plan fixes the shapes of a batch once: the host runtime sorts the

@@ -50,6 +50,8 @@ _SIGS = {
     "mfg_zgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
     "mfg_dgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
     "mfg_dgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_sgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_zgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_plan_getrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _I, _vp]),
     "mfg_plan_potrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _I, _vp]),
     "mfg_plan_destroy": (_I, [_vp]),
@@ -333,14 +335,17 @@ class Factorization:
 
     @staticmethod
     def LuInverse(n, a, lda, piv):
-        """Factorization.LuInverse (MatFlat/Factorization.LuInverse.cs:123-199)."""
+        """Factorization.LuInverse (MatFlat/Factorization.LuInverse.cs:27-295): float32,
+        float64 and complex128 overloads."""
         ctx = context()
+        dt = _dt(a)
         if n > 0 and lda >= n:
-            _need(a, _span(n, n, lda), "a")
+            _need(a, _span(n, n, lda), "a", dt)
             _need(piv, n, "piv", np.int32)
         info = ctypes.c_int(0)
-        rc = ctx.lib.mfg_dgetri(ctx.h, n, None if a is None else _ptr(a), lda,
-                                None if piv is None else _ptr(piv), ctypes.byref(info))
+        fn = getattr(ctx.lib, "mfg_%sgetri" % _pfx(dt))
+        rc = fn(ctx.h, n, None if a is None else _ptr(a), lda,
+                None if piv is None else _ptr(piv), ctypes.byref(info))
         if rc != 0:
             _raise_status(rc, ["n", "a", "lda", "piv"], ctx)
         if info.value != 0:

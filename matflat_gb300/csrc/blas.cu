@@ -69,10 +69,25 @@ __global__ void gemm_single_kernel(int transa, int transb, int m, int n, int k, 
 
 // LuInverse: work <- LU (leading dimension n); a <- the columns of P^T (a[piv[j], ...] pattern
 // of LuInverse.cs:160-172); then every column is solved with the unit lower factor (the LuInverse
-// idiom sets L's diagonal to 1.0, :174-182; dividing by 1.0 is exact, so the unit solve skips it)
-// and then the upper factor (:184-192).  One CTA; warp w solves columns w, w+W, ... in chunks.
-__global__ void getri_single_kernel(double* a, int n, int lda, const int* piv, double* work,
-                                    double* scratch, long long scratch_stride) {
+// idiom sets L's diagonal to 1.0, :174-182; dividing by 1.0 is exact for double and float, so the
+// unit solve skips it, and done as a division for Complex) and then the upper factor (:184-192).
+// One CTA; warp w solves columns w, w+W, ... in chunks.  S: the element type's solve arithmetic
+// (DSolve, SSolve or ZSolve<false>: the double, float and Complex overloads).
+template <class S>
+__device__ __forceinline__ typename S::T elem_of(double v);
+template <>
+__device__ __forceinline__ double elem_of<DSolve>(double v) { return v; }
+template <>
+__device__ __forceinline__ float elem_of<SSolve>(double v) { return (float)v; }
+template <>
+__device__ __forceinline__ zdouble elem_of<ZSolve<false>>(double v) { return zmake(v, 0.0); }
+
+template <class S>
+__global__ void getri_single_kernel(typename S::T* a, int n, int lda, const int* piv,
+                                    typename S::T* work, void* scratch,
+                                    long long scratch_bytes) {
+  using T = typename S::T;
+  using Acc = typename S::Acc;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
   for (long long e = tid; e < (long long)n * n; e += nthreads) {
@@ -84,17 +99,17 @@ __global__ void getri_single_kernel(double* a, int n, int lda, const int* piv, d
   for (long long e = tid; e < (long long)n * n; e += nthreads) {
     const int j = (int)(e / n);
     const int i = (int)(e - (long long)j * n);
-    a[(long long)j * lda + i] = 0.0;
+    a[(long long)j * lda + i] = elem_of<S>(0.0);
   }
   __syncthreads();
-  for (int j = tid; j < n; j += nthreads) a[(long long)lda * piv[j] + j] = 1.0;
+  for (int j = tid; j < n; j += nthreads) a[(long long)lda * piv[j] + j] = elem_of<S>(1.0);
   __syncthreads();
   const int warp = tid >> 5;
   const int lane = tid & 31;
   const int nwarps = nthreads >> 5;
   const int ldx = n | 1;
-  double* xs = scratch + warp * scratch_stride;
-  double* acc = xs + RHS_CHUNK * ldx;
+  Acc* acc = (Acc*)((char*)scratch + warp * scratch_bytes);
+  T* xs = (T*)(acc + RHS_CHUNK * ldx);
   for (int c0 = warp * RHS_CHUNK; c0 < n; c0 += nwarps * RHS_CHUNK) {
     const int nr = n - c0 < RHS_CHUNK ? n - c0 : RHS_CHUNK;
     for (int e = lane; e < nr * n; e += 32) {
@@ -103,8 +118,8 @@ __global__ void getri_single_kernel(double* a, int n, int lda, const int* piv, d
       xs[r * ldx + i] = a[(long long)(c0 + r) * lda + i];
     }
     __syncwarp();
-    warp_solve_dot(work, n, 1, n, true, xs, ldx, acc, nr);
-    warp_solve_sweep(work, n, n, 1, xs, ldx, nr);
+    warp_solve_dot<32, S>(work, n, 1, n, true, xs, ldx, acc, nr);
+    warp_solve_sweep<32, S>(work, n, n, 1, xs, ldx, nr);
     for (int e = lane; e < nr * n; e += 32) {
       const int r = e / n;
       const int i = e - r * n;
@@ -260,10 +275,37 @@ cudaError_t launch_gemm_single(int transa, int transb, int m, int n, int k, cons
   return cudaGetLastError();
 }
 
+// Scratch per warp: RHS_CHUNK * (n|1) accumulators and as many staged entries, 8-byte aligned.
+template <class S>
+static long long getri_single_scratch_bytes(int n) {
+  const long long ld = n | 1;
+  const long long b = RHS_CHUNK * ld * (long long)(sizeof(typename S::Acc) + sizeof(typename S::T));
+  return (b + 15) / 16 * 16;
+}
+
+long long getri_single_scratch_bytes_per_warp(int n, int elem) {
+  return elem == 1 ? getri_single_scratch_bytes<SSolve>(n)
+         : elem == 2 ? getri_single_scratch_bytes<ZSolve<false>>(n)
+                     : getri_single_scratch_bytes<DSolve>(n);
+}
+
 cudaError_t launch_getri_single(double* a, int n, int lda, const int* piv, double* work,
                                 double* scratch, int warps, cudaStream_t s) {
-  const long long stride = 2LL * RHS_CHUNK * (n | 1);
-  getri_single_kernel<<<1, warps * 32, 0, s>>>(a, n, lda, piv, work, scratch, stride);
+  getri_single_kernel<DSolve><<<1, warps * 32, 0, s>>>(a, n, lda, piv, work, scratch,
+                                                       getri_single_scratch_bytes<DSolve>(n));
+  return cudaGetLastError();
+}
+cudaError_t launch_sgetri_single(float* a, int n, int lda, const int* piv, float* work,
+                                 void* scratch, int warps, cudaStream_t s) {
+  getri_single_kernel<SSolve><<<1, warps * 32, 0, s>>>(a, n, lda, piv, work, scratch,
+                                                       getri_single_scratch_bytes<SSolve>(n));
+  return cudaGetLastError();
+}
+cudaError_t launch_zgetri_single(double* a, int n, int lda, const int* piv, double* work,
+                                 void* scratch, int warps, cudaStream_t s) {
+  getri_single_kernel<ZSolve<false>><<<1, warps * 32, 0, s>>>(
+      (zdouble*)a, n, lda, piv, (zdouble*)work, scratch,
+      getri_single_scratch_bytes<ZSolve<false>>(n));
   return cudaGetLastError();
 }
 

@@ -240,5 +240,12 @@ cudaError_t launch_gemm_single(int transa, int transb, int m, int n, int k, cons
 // work: n*n doubles.  scratch: warps * 2 * RHS_CHUNK * (n|1) doubles.
 cudaError_t launch_getri_single(double* a, int n, int lda, const int* piv, double* work,
                                 double* scratch, int warps, cudaStream_t s);
+// Float and Complex overloads (Complex as interleaved doubles; work: n*n elements).  Scratch:
+// warps * getri_single_scratch_bytes_per_warp(n, elem) bytes (elem 0 double, 1 float, 2 Complex).
+long long getri_single_scratch_bytes_per_warp(int n, int elem);
+cudaError_t launch_sgetri_single(float* a, int n, int lda, const int* piv, float* work,
+                                 void* scratch, int warps, cudaStream_t s);
+cudaError_t launch_zgetri_single(double* a, int n, int lda, const int* piv, double* work,
+                                 void* scratch, int warps, cudaStream_t s);
 
 }  // namespace mfg

@@ -1014,24 +1014,38 @@ MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k,
   return MFG_OK;
 }
 
-MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+}  // extern "C"
+
+// Factorization.LuInverse, all three overloads (elem 0 double, 1 float, 2 Complex as interleaved
+// doubles): argument checks in MatFlat's order (Factorization.LuInverse.cs:125-143), then the
+// singularity test before anything is written (:145-152), on host copies of the diagonal and the
+// pivots (a and piv may be device arrays).
+static int getri_single_any(mfg_ctx* ctx, int elem, int n, void* a, int lda, const int* piv,
+                            int* info) {
   if (!ctx) return -1;
-  // Factorization.LuInverse argument checks (Factorization.LuInverse.cs:125-143).
   if (n <= 0) return fail(ctx, -2, "The order of the matrix must be greater than or equal to one.");
   if (!a) return fail(ctx, -3, "a is null");
   if (lda < n)
     return fail(ctx, -4,
                 "The leading dimension must be greater than or equal to the order of the matrix.");
   if (!piv) return fail(ctx, -5, "piv is null");
-  // Singularity check before anything is written (LuInverse.cs:145-152), on host copies of the
-  // diagonal and the pivots (a and piv may be device arrays).
-  std::vector<double> diag(n);
+  const size_t es = elem == 1 ? 4 : elem == 2 ? 16 : 8;
+  std::vector<char> diag((size_t)n * es);
   std::vector<int> hpiv(n);
-  MFG_CUDA(ctx, cudaMemcpy2D(diag.data(), sizeof(double), a, (size_t)(lda + 1) * sizeof(double),
-                             sizeof(double), n, cudaMemcpyDefault));
+  MFG_CUDA(ctx, cudaMemcpy2D(diag.data(), es, a, (size_t)(lda + 1) * es, es, n,
+                             cudaMemcpyDefault));
   MFG_CUDA(ctx, cudaMemcpy(hpiv.data(), piv, sizeof(int) * n, cudaMemcpyDefault));
   for (int j = 0; j < n; j++) {
-    if (diag[j] == 0.0) {
+    bool zero;
+    if (elem == 1) {
+      zero = ((const float*)diag.data())[j] == 0.0f;
+    } else if (elem == 2) {
+      const double* z = (const double*)diag.data() + 2 * j;
+      zero = z[0] == 0.0 && z[1] == 0.0;
+    } else {
+      zero = ((const double*)diag.data())[j] == 0.0;
+    }
+    if (zero) {
       if (info) *info = 1;
       return MFG_OK;
     }
@@ -1042,25 +1056,45 @@ MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, 
   const int warps = 8;
   const size_t na = span(n, n, lda);
   const size_t nwork = (size_t)n * n;
-  const size_t nscr = (size_t)warps * 2 * mfg::RHS_CHUNK * (n | 1);
-  const size_t need = Carve::bytes_for(na, 8) + Carve::bytes_for(nwork, 8) +
-                      Carve::bytes_for(nscr, 8) + Carve::bytes_for(n, 4);
+  const size_t sbytes = (size_t)warps * (size_t)mfg::getri_single_scratch_bytes_per_warp(n, elem);
+  const size_t need = Carve::bytes_for(na, es) + Carve::bytes_for(nwork, es) +
+                      Carve::bytes_for(sbytes, 1) + Carve::bytes_for(n, 4);
   MFG_CUDA(ctx, ctx->work.reserve(need));
   Carve cv(ctx->work.ptr);
-  double* d_a = cv.take<double>(na);
-  double* d_w = cv.take<double>(nwork);
-  double* d_s = cv.take<double>(nscr);
+  char* d_a = cv.take<char>(na * es);
+  char* d_w = cv.take<char>(nwork * es);
+  char* d_s = cv.take<char>(sbytes);
   int* d_piv = cv.take<int>(n);
   cudaStream_t s = ctx->stream;
-  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * 8, a, (size_t)lda * 8, (size_t)n * 8, n,
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(d_a, (size_t)lda * es, a, (size_t)lda * es, (size_t)n * es, n,
                                   cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaMemcpyAsync(d_piv, piv, sizeof(int) * n, cudaMemcpyDefault, s));
-  MFG_CUDA(ctx, mfg::launch_getri_single(d_a, n, lda, d_piv, d_w, d_s, warps, s));
-  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * 8, d_a, (size_t)lda * 8, (size_t)n * 8, n,
+  if (elem == 1)
+    MFG_CUDA(ctx, mfg::launch_sgetri_single((float*)d_a, n, lda, d_piv, (float*)d_w, d_s, warps,
+                                            s));
+  else if (elem == 2)
+    MFG_CUDA(ctx, mfg::launch_zgetri_single((double*)d_a, n, lda, d_piv, (double*)d_w, d_s,
+                                            warps, s));
+  else
+    MFG_CUDA(ctx, mfg::launch_getri_single((double*)d_a, n, lda, d_piv, (double*)d_w,
+                                           (double*)d_s, warps, s));
+  MFG_CUDA(ctx, cudaMemcpy2DAsync(a, (size_t)lda * es, d_a, (size_t)lda * es, (size_t)n * es, n,
                                   cudaMemcpyDefault, s));
   MFG_CUDA(ctx, cudaStreamSynchronize(s));
   if (info) *info = 0;
   return MFG_OK;
+}
+
+extern "C" {
+
+MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+  return getri_single_any(ctx, 0, n, a, lda, piv, info);
+}
+MFG_API int mfg_sgetri(mfg_ctx* ctx, int n, float* a, int lda, const int* piv, int* info) {
+  return getri_single_any(ctx, 1, n, a, lda, piv, info);
+}
+MFG_API int mfg_zgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+  return getri_single_any(ctx, 2, n, a, lda, piv, info);
 }
 
 

@@ -878,6 +878,60 @@ int orc_dlu_inverse(int n, double* a, int lda, const int* piv) {
   return 0;
 }
 
+// The float and Complex overloads (Factorization.LuInverse.cs:27-103, :219-295): the same steps
+// with float SolveTriangular and with Complex SolveTriangular / Complex.One (the zero test is
+// re == 0 && im == 0 for Complex).
+int orc_slu_inverse(int n, float* a, int lda, const int* piv) {
+  for (int j = 0; j < n; j++)
+    if (a[(long)lda * j + j] == 0.0f) return 1;
+  std::vector<float> workv((size_t)n * n + n);
+  float* work = workv.data();
+  float* diag = work + (size_t)n * n;
+  for (int j = 0; j < n; j++) {
+    float* aColj = a + (long)lda * j;
+    std::memcpy(work + (size_t)n * j, aColj, sizeof(float) * n);
+    diag[j] = aColj[j];
+    std::memset(aColj, 0, sizeof(float) * n);
+  }
+  for (int j = 0; j < n; j++) a[(long)lda * piv[j] + j] = 1.0f;
+  for (int j = 0; j < n; j++) work[(size_t)n * j + j] = 1.0f;
+  for (int j = 0; j < n; j++) orc_strsv(LOWER, NOTRANS, n, work, n, a + (long)lda * j, 1);
+  for (int j = 0; j < n; j++) work[(size_t)n * j + j] = diag[j];
+  for (int j = 0; j < n; j++) orc_strsv(UPPER, NOTRANS, n, work, n, a + (long)lda * j, 1);
+  return 0;
+}
+int orc_zlu_inverse(int n, double* a, int lda, const int* piv) {
+  for (int j = 0; j < n; j++) {
+    const double* d = a + 2 * ((long)lda * j + j);
+    if (d[0] == 0.0 && d[1] == 0.0) return 1;
+  }
+  std::vector<double> workv((size_t)2 * ((size_t)n * n + n));
+  double* work = workv.data();
+  double* diag = work + (size_t)2 * n * n;
+  for (int j = 0; j < n; j++) {
+    double* aColj = a + 2 * (long)lda * j;
+    std::memcpy(work + (size_t)2 * n * j, aColj, sizeof(double) * 2 * n);
+    diag[2 * j] = aColj[2 * j];
+    diag[2 * j + 1] = aColj[2 * j + 1];
+    std::memset(aColj, 0, sizeof(double) * 2 * n);
+  }
+  for (int j = 0; j < n; j++) {
+    a[2 * ((long)lda * piv[j] + j)] = 1.0;
+    a[2 * ((long)lda * piv[j] + j) + 1] = 0.0;
+  }
+  for (int j = 0; j < n; j++) {
+    work[2 * ((size_t)n * j + j)] = 1.0;
+    work[2 * ((size_t)n * j + j) + 1] = 0.0;
+  }
+  for (int j = 0; j < n; j++) orc_ztrsv(LOWER, NOTRANS, n, work, n, a + 2 * (long)lda * j, 1);
+  for (int j = 0; j < n; j++) {
+    work[2 * ((size_t)n * j + j)] = diag[2 * j];
+    work[2 * ((size_t)n * j + j) + 1] = diag[2 * j + 1];
+  }
+  for (int j = 0; j < n; j++) orc_ztrsv(UPPER, NOTRANS, n, work, n, a + 2 * (long)lda * j, 1);
+  return 0;
+}
+
 // =============================================================================================
 // Composite per-matrix workloads of the batched paths.  Each composes the routines above in
 // the order MatFlat's own idioms give.

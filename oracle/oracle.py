@@ -54,6 +54,8 @@ def lib():
             "orc_zgemm": (_I, [_I, _I, _I, _I, _I, _d, _I, _d, _I, _d, _I]),
             "orc_dgemv": (_I, [_I, _I, _I, _d, _I, _d, _I, _d, _I]),
             "orc_dlu_inverse": (_I, [_I, _d, _I, _i]),
+            "orc_slu_inverse": (_I, [_I, _f, _I, _i]),
+            "orc_zlu_inverse": (_I, [_I, _d, _I, _i]),
             "orc_dlu_solve": (None, [_I, _d, _I, _i, _I, _d, _I]),
             "orc_dqr_ls": (None, [_I, _I, _d, _I, _d, _d]),
             "orc_sqr_ls": (None, [_I, _I, _f, _I, _f, _f]),
@@ -158,8 +160,9 @@ def ger(m, n, x, incx, y, incy, a, lda):
 
 
 def lu_inverse(n, a, lda, piv):
-    """Factorization.LuInverse (Factorization.LuInverse.cs:123-199), double; 0 or 1 (singular)."""
-    return lib().orc_dlu_inverse(n, _fp(a), lda, _p(piv, ctypes.c_int))
+    """Factorization.LuInverse (Factorization.LuInverse.cs:27-295), the overload a's dtype
+    selects; 0 or 1 (singular)."""
+    return getattr(lib(), "orc_%slu_inverse" % _pre(a))(n, _fp(a), lda, _p(piv, ctypes.c_int))
 
 
 def lu_solve(n, lu_, lda, piv, nrhs, b, ldb):

@@ -121,3 +121,27 @@ def test_qr_complex_large(mf):
     oracle.qr(m, n, b, m, ro)
     _same(a, b)
     _same(rg, ro)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex128])
+@pytest.mark.parametrize("n,lda", [(1, 1), (5, 7), (33, 33), (70, 71)])
+def test_lu_inverse_overloads(mf, dt, n, lda):
+    """Factorization.LuInverse's float and Complex overloads, bit for bit against the oracle,
+    including the singular case (no write, MatrixFactorizationException)."""
+    rng = np.random.default_rng(700 + n)
+    if dt == np.complex128:
+        a0 = rng.standard_normal(lda * n) + 1j * rng.standard_normal(lda * n)
+    else:
+        a0 = rng.standard_normal(lda * n).astype(dt)
+    piv = np.zeros(n, np.int32)
+    oracle.lu(n, n, a0, lda, piv)
+    g, o = a0.copy(), a0.copy()
+    mf.Factorization.LuInverse(n, g, lda, piv)
+    assert oracle.lu_inverse(n, o, lda, piv) == 0
+    _same(g, o, "n=%d" % n)
+    s = a0.copy()
+    s[(n - 1) * lda + n - 1] = 0
+    keep = s.copy()
+    with pytest.raises(mf.MatrixFactorizationException):
+        mf.Factorization.LuInverse(n, s, lda, piv)
+    _same(s, keep)
