@@ -278,6 +278,47 @@ MFG_API int mfg_dger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x
                                      int64_t stride_x, const double* y, int incy,
                                      int64_t stride_y, double* a, int lda, int64_t stride_a,
                                      int count);
+/* The float and Complex overloads of the same strided batches (Complex as interleaved (re, im)
+ * doubles, strides and increments in elements):
+ *   MulMatVec float (Blas.MulMatVec.cs:38-136: the double tree over widened operands, cast to
+ *     float) and Complex (:238-336: Internals.Dot, and DotConj for ConjNoTrans / ConjTrans);
+ *   Dot float (Blas.VectorOperations.cs:110-141), Dot / DotConj Complex (:176-246);
+ *   L2Norm float (:23-48, cast to float) and Complex (:77-108, a double: Internals.Norm's order,
+ *     ((re0^2 + im0^2) + re1^2) + im1^2 per pair);
+ *   Outer float (:248-290), Outer / OuterConj Complex (:336-420: y_j * x_i, conj(y_j) * x_i). */
+MFG_API int mfg_sgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const float* a,
+                                      int lda, int64_t stride_a, const float* x, int incx,
+                                      int64_t stride_x, float* y, int incy, int64_t stride_y,
+                                      int count);
+MFG_API int mfg_zgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const double* a,
+                                      int lda, int64_t stride_a, const double* x, int incx,
+                                      int64_t stride_x, double* y, int incy, int64_t stride_y,
+                                      int count);
+MFG_API int mfg_sdot_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
+                                     int64_t stride_x, const float* y, int incy,
+                                     int64_t stride_y, float* result, int count);
+MFG_API int mfg_zdot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* result, int count);
+MFG_API int mfg_zdotc_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                      int64_t stride_x, const double* y, int incy,
+                                      int64_t stride_y, double* result, int count);
+MFG_API int mfg_snrm2_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
+                                      int64_t stride_x, float* result, int count);
+MFG_API int mfg_dznrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                       int64_t stride_x, double* result, int count);
+MFG_API int mfg_sger_strided_batched(mfg_ctx* ctx, int m, int n, const float* x, int incx,
+                                     int64_t stride_x, const float* y, int incy,
+                                     int64_t stride_y, float* a, int lda, int64_t stride_a,
+                                     int count);
+MFG_API int mfg_zger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                     int count);
+MFG_API int mfg_zgerc_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                      int64_t stride_x, const double* y, int incy,
+                                      int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                      int count);
 
 /* Front half of Factorization.Gevd for a batch of pairs (Factorization.GevdCore,
  * Factorization.Gevd.cs:330-365; the reference has no batched form): B = L L^T in place

@@ -59,6 +59,18 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
+    **{"mfg_%sgemv_strided_batched" % _p: (_I, [_vp, _I, _I, _I, _vp, _I, ctypes.c_int64, _vp,
+                                                 _I, ctypes.c_int64, _vp, _I, ctypes.c_int64, _I])
+       for _p in "sz"},
+    **{_f: (_I, [_vp, _I, _vp, _I, ctypes.c_int64, _vp, _I, ctypes.c_int64, _vp, _I])
+       for _f in ("mfg_sdot_strided_batched", "mfg_zdot_strided_batched",
+                  "mfg_zdotc_strided_batched")},
+    **{_f: (_I, [_vp, _I, _vp, _I, ctypes.c_int64, _vp, _I])
+       for _f in ("mfg_snrm2_strided_batched", "mfg_dznrm2_strided_batched")},
+    **{_f: (_I, [_vp, _I, _I, _vp, _I, ctypes.c_int64, _vp, _I, ctypes.c_int64, _vp, _I,
+                 ctypes.c_int64, _I])
+       for _f in ("mfg_sger_strided_batched", "mfg_zger_strided_batched",
+                  "mfg_zgerc_strided_batched")},
     "mfg_dgemv_strided_batched": (_I, [_vp, _I, _I, _I, _vp, _I, ctypes.c_int64, _vp, _I,
                                        ctypes.c_int64, _vp, _I, ctypes.c_int64, _I]),
     "mfg_ddot_strided_batched": (_I, [_vp, _I, _vp, _I, ctypes.c_int64, _vp, _I, ctypes.c_int64,
@@ -518,45 +530,73 @@ class LuBatch(_Batch):
 
 
 class StridedBlas:
-    """Strided batches of Blas.MulMatVec / Dot / L2Norm / Outer on device buffers (torch CUDA
-    tensors or device pointers); item b of each operand starts at base + b * stride."""
+    """Strided batches of Blas.MulMatVec / Dot / DotConj / L2Norm / Outer / OuterConj on device
+    buffers (torch CUDA tensors or device pointers); item b of each operand starts at base +
+    b * stride (elements).  The overload follows the operand's dtype (float64, float32,
+    complex128), or `dtype` ("d", "s", "z") for raw pointers or interleaved float64."""
 
     @staticmethod
     def MulMatVec(trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy, stride_y, count,
-                  ctx=None):
+                  ctx=None, dtype=None):
         ctx = ctx or context()
-        rc = ctx.lib.mfg_dgemv_strided_batched(ctx.h, trans, m, n, _dptr(a), lda, stride_a,
-                                               _dptr(x), incx, stride_x, _dptr(y), incy,
-                                               stride_y, count)
+        name = "mfg_%sgemv_strided_batched" % _elem(a, dtype)
+        rc = getattr(ctx.lib, name)(ctx.h, trans, m, n, _dptr(a), lda, stride_a, _dptr(x), incx,
+                                    stride_x, _dptr(y), incy, stride_y, count)
         if rc != 0:
             _raise_status(rc, ["trans", "m", "n", "a", "lda", "stride_a", "x", "incx",
                                "stride_x", "y", "incy", "stride_y", "count"], ctx)
 
     @staticmethod
-    def Dot(n, x, incx, stride_x, y, incy, stride_y, result, count, ctx=None):
+    def _dot(name, n, x, incx, stride_x, y, incy, stride_y, result, count, ctx):
         ctx = ctx or context()
-        rc = ctx.lib.mfg_ddot_strided_batched(ctx.h, n, _dptr(x), incx, stride_x, _dptr(y), incy,
-                                              stride_y, _dptr(result), count)
+        rc = getattr(ctx.lib, name)(ctx.h, n, _dptr(x), incx, stride_x, _dptr(y), incy, stride_y,
+                                    _dptr(result), count)
         if rc != 0:
             _raise_status(rc, ["n", "x", "incx", "stride_x", "y", "incy", "stride_y", "result",
                                "count"], ctx)
 
     @staticmethod
-    def L2Norm(n, x, incx, stride_x, result, count, ctx=None):
+    def Dot(n, x, incx, stride_x, y, incy, stride_y, result, count, ctx=None, dtype=None):
+        StridedBlas._dot("mfg_%sdot_strided_batched" % _elem(x, dtype), n, x, incx, stride_x, y,
+                         incy, stride_y, result, count, ctx)
+
+    @staticmethod
+    def DotConj(n, x, incx, stride_x, y, incy, stride_y, result, count, ctx=None):
+        """Complex only: sum of conj(x_i) * y_i (Blas.DotConj)."""
+        StridedBlas._dot("mfg_zdotc_strided_batched", n, x, incx, stride_x, y, incy, stride_y,
+                         result, count, ctx)
+
+    @staticmethod
+    def L2Norm(n, x, incx, stride_x, result, count, ctx=None, dtype=None):
+        """Result dtype: float32 for float32 input, float64 otherwise (Complex norms are real)."""
         ctx = ctx or context()
-        rc = ctx.lib.mfg_dnrm2_strided_batched(ctx.h, n, _dptr(x), incx, stride_x, _dptr(result),
-                                               count)
+        name = {"d": "mfg_dnrm2_strided_batched", "s": "mfg_snrm2_strided_batched",
+                "z": "mfg_dznrm2_strided_batched"}[_elem(x, dtype)]
+        rc = getattr(ctx.lib, name)(ctx.h, n, _dptr(x), incx, stride_x, _dptr(result), count)
         if rc != 0:
             _raise_status(rc, ["n", "x", "incx", "stride_x", "result", "count"], ctx)
 
     @staticmethod
-    def Outer(m, n, x, incx, stride_x, y, incy, stride_y, a, lda, stride_a, count, ctx=None):
+    def _outer(name, m, n, x, incx, stride_x, y, incy, stride_y, a, lda, stride_a, count, ctx):
         ctx = ctx or context()
-        rc = ctx.lib.mfg_dger_strided_batched(ctx.h, m, n, _dptr(x), incx, stride_x, _dptr(y),
-                                              incy, stride_y, _dptr(a), lda, stride_a, count)
+        rc = getattr(ctx.lib, name)(ctx.h, m, n, _dptr(x), incx, stride_x, _dptr(y), incy,
+                                    stride_y, _dptr(a), lda, stride_a, count)
         if rc != 0:
             _raise_status(rc, ["m", "n", "x", "incx", "stride_x", "y", "incy", "stride_y", "a",
                                "lda", "stride_a", "count"], ctx)
+
+    @staticmethod
+    def Outer(m, n, x, incx, stride_x, y, incy, stride_y, a, lda, stride_a, count, ctx=None,
+              dtype=None):
+        StridedBlas._outer("mfg_%sger_strided_batched" % _elem(x, dtype), m, n, x, incx,
+                           stride_x, y, incy, stride_y, a, lda, stride_a, count, ctx)
+
+    @staticmethod
+    def OuterConj(m, n, x, incx, stride_x, y, incy, stride_y, a, lda, stride_a, count,
+                  ctx=None):
+        """Complex only: a(i,j) = conj(y_j) * x_i (Blas.OuterConj)."""
+        StridedBlas._outer("mfg_zgerc_strided_batched", m, n, x, incx, stride_x, y, incy,
+                           stride_y, a, lda, stride_a, count, ctx)
 
 
 class LuInverseBatch(_Batch):

@@ -144,6 +144,18 @@ cudaError_t launch_ger_strided(int m, int n, const double* x, int incx, long lon
                                const double* y, int incy, long long sy, double* a, int lda,
                                long long sa, int count, cudaStream_t s);
 
+// The float (elem 1) and Complex (elem 2, interleaved doubles) overloads of the same strided
+// batches.  Dot mode: 0 Dot, 1 L2Norm (float result for float, double for Complex), 2 DotConj.
+cudaError_t launch_gemv_strided_t(int elem, int trans, int m, int n, const void* a, int lda,
+                                  long long sa, const void* x, int incx, long long sx, void* y,
+                                  int incy, long long sy, int count, cudaStream_t s);
+cudaError_t launch_dot_strided_t(int elem, int n, const void* x, int incx, long long sx,
+                                 const void* y, int incy, long long sy, void* out, int count,
+                                 int mode, cudaStream_t s);
+cudaError_t launch_ger_strided_t(int elem, int m, int n, const void* x, int incx, long long sx,
+                                 const void* y, int incy, long long sy, void* a, int lda,
+                                 long long sa, int count, int conj, cudaStream_t s);
+
 // Fills args.a (and args.b when nrhs > 0) with the autotuner's synthetic batch (tune.cu).
 cudaError_t launch_tune_fill(const BatchArgs& args, int spd, cudaStream_t s);
 

@@ -1829,6 +1829,137 @@ MFG_API int mfg_dger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x
   return MFG_OK;
 }
 
+}  // extern "C"
+
+// The float and Complex strided batches: MatFlat's argument checks, as for the double ones.
+static int gemv_strided_any(mfg_ctx* ctx, int elem, int trans, int m, int n, const void* a,
+                            int lda, int64_t sa, const void* x, int incx, int64_t sx, void* y,
+                            int incy, int64_t sy, int count) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -3, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -4, "The number of columns must be greater than or equal to one.");
+  if (!a) return fail(ctx, -5, "a is null");
+  if (lda < m)
+    return fail(ctx, -6,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (!x) return fail(ctx, -8, "x is null");
+  if (incx <= 0) return fail(ctx, -9, "The value must be greater than or equal to one.");
+  if (!y) return fail(ctx, -11, "y is null");
+  if (incy <= 0) return fail(ctx, -12, "The value must be greater than or equal to one.");
+  if (a == (const void*)y || x == (const void*)y)
+    return fail(ctx, MFG_ERR_INPLACE, "In-place operation is not supported.");
+  const bool ok = trans == MFG_NOTRANS || trans == MFG_TRANS ||
+                  (elem == 2 && (trans == MFG_CONJTRANS || trans == MFG_CONJNOTRANS));
+  if (!ok) return fail(ctx, -2, "Invalid enum value.");
+  if (count < 0) return fail(ctx, -14, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_gemv_strided_t(elem, trans, m, n, a, lda, sa, x, incx, sx, y, incy,
+                                           sy, count, ctx->stream));
+  return MFG_OK;
+}
+
+static int dot_strided_any(mfg_ctx* ctx, int elem, int mode, int n, const void* x, int incx,
+                           int64_t sx, const void* y, int incy, int64_t sy, void* result,
+                           int count) {
+  if (!ctx) return -1;
+  if (n <= 0) return fail(ctx, -2, "The length of the vector must be greater than or equal to one.");
+  if (!x) return fail(ctx, -3, "x is null");
+  if (incx <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
+  if (mode != 1) {
+    if (!y) return fail(ctx, -6, "y is null");
+    if (incy <= 0) return fail(ctx, -7, "The value must be greater than or equal to one.");
+    if (!result) return fail(ctx, -9, "result is null");
+    if (count < 0) return fail(ctx, -10, "count must be >= 0");
+  } else {
+    if (!result) return fail(ctx, -6, "result is null");
+    if (count < 0) return fail(ctx, -7, "count must be >= 0");
+  }
+  MFG_CUDA(ctx, mfg::launch_dot_strided_t(elem, n, x, incx, sx, mode == 1 ? x : y,
+                                          mode == 1 ? incx : incy, mode == 1 ? sx : sy, result,
+                                          count, mode, ctx->stream));
+  return MFG_OK;
+}
+
+static int ger_strided_any(mfg_ctx* ctx, int elem, int conj, int m, int n, const void* x,
+                           int incx, int64_t sx, const void* y, int incy, int64_t sy, void* a,
+                           int lda, int64_t sa, int count) {
+  if (!ctx) return -1;
+  if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
+  if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
+  if (!x) return fail(ctx, -4, "x is null");
+  if (incx <= 0) return fail(ctx, -5, "The value must be greater than or equal to one.");
+  if (!y) return fail(ctx, -7, "y is null");
+  if (incy <= 0) return fail(ctx, -8, "The value must be greater than or equal to one.");
+  if (!a) return fail(ctx, -10, "a is null");
+  if (lda < m)
+    return fail(ctx, -11,
+                "The leading dimension must be greater than or equal to the number of rows.");
+  if (count < 0) return fail(ctx, -13, "count must be >= 0");
+  MFG_CUDA(ctx, mfg::launch_ger_strided_t(elem, m, n, x, incx, sx, y, incy, sy, a, lda, sa,
+                                          count, conj, ctx->stream));
+  return MFG_OK;
+}
+
+extern "C" {
+
+MFG_API int mfg_sgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const float* a,
+                                      int lda, int64_t stride_a, const float* x, int incx,
+                                      int64_t stride_x, float* y, int incy, int64_t stride_y,
+                                      int count) {
+  return gemv_strided_any(ctx, 1, trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy,
+                          stride_y, count);
+}
+MFG_API int mfg_zgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, const double* a,
+                                      int lda, int64_t stride_a, const double* x, int incx,
+                                      int64_t stride_x, double* y, int incy, int64_t stride_y,
+                                      int count) {
+  return gemv_strided_any(ctx, 2, trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy,
+                          stride_y, count);
+}
+MFG_API int mfg_sdot_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
+                                     int64_t stride_x, const float* y, int incy,
+                                     int64_t stride_y, float* result, int count) {
+  return dot_strided_any(ctx, 1, 0, n, x, incx, stride_x, y, incy, stride_y, result, count);
+}
+MFG_API int mfg_zdot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* result, int count) {
+  return dot_strided_any(ctx, 2, 0, n, x, incx, stride_x, y, incy, stride_y, result, count);
+}
+MFG_API int mfg_zdotc_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                      int64_t stride_x, const double* y, int incy,
+                                      int64_t stride_y, double* result, int count) {
+  return dot_strided_any(ctx, 2, 2, n, x, incx, stride_x, y, incy, stride_y, result, count);
+}
+MFG_API int mfg_snrm2_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
+                                      int64_t stride_x, float* result, int count) {
+  return dot_strided_any(ctx, 1, 1, n, x, incx, stride_x, nullptr, 0, 0, result, count);
+}
+MFG_API int mfg_dznrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
+                                       int64_t stride_x, double* result, int count) {
+  return dot_strided_any(ctx, 2, 1, n, x, incx, stride_x, nullptr, 0, 0, result, count);
+}
+MFG_API int mfg_sger_strided_batched(mfg_ctx* ctx, int m, int n, const float* x, int incx,
+                                     int64_t stride_x, const float* y, int incy,
+                                     int64_t stride_y, float* a, int lda, int64_t stride_a,
+                                     int count) {
+  return ger_strided_any(ctx, 1, 0, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
+                         stride_a, count);
+}
+MFG_API int mfg_zger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                     int64_t stride_x, const double* y, int incy,
+                                     int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                     int count) {
+  return ger_strided_any(ctx, 2, 0, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
+                         stride_a, count);
+}
+MFG_API int mfg_zgerc_strided_batched(mfg_ctx* ctx, int m, int n, const double* x, int incx,
+                                      int64_t stride_x, const double* y, int incy,
+                                      int64_t stride_y, double* a, int lda, int64_t stride_a,
+                                      int count) {
+  return ger_strided_any(ctx, 2, 1, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
+                         stride_a, count);
+}
+
 MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                         const int* lda, const int64_t* a_off, const int* ldb,
                                         const int64_t* b_off, const int64_t* c_off) {

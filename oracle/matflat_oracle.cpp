@@ -855,6 +855,76 @@ void orc_dger(int m, int n, const double* x, int incx, const double* y, int incy
   }
 }
 
+// The float and Complex overloads (Blas.MulMatVec.cs:38-136, :238-336; Blas.VectorOperations.cs
+// :23-48, :77-108, :110-141, :176-246, :248-290, :336-420).  Float dots and norms are the double
+// tree over widened operands, cast to float; Complex MulMatVec uses Dot for NoTrans / Trans and
+// DotConj for ConjNoTrans / ConjTrans; the Complex norm is a double.
+int orc_zgemv(int trans, int m, int n, const double* a_, int lda, const double* x_, int incx,
+              double* y_, int incy) {
+  const cplx* a = (const cplx*)a_;
+  const cplx* x = (const cplx*)x_;
+  cplx* y = (cplx*)y_;
+  if (trans == NOTRANS) {
+    for (int i = 0; i < m; i++) y[(long)incy * i] = dot_z(n, a + i, lda, x, incx);
+  } else if (trans == TRANS) {
+    for (int i = 0; i < n; i++) y[(long)incy * i] = dot_z(m, a + (long)lda * i, 1, x, incx);
+  } else if (trans == CONJNOTRANS) {
+    for (int i = 0; i < m; i++) y[(long)incy * i] = dotconj_z(n, a + i, lda, x, incx);
+  } else if (trans == CONJTRANS) {
+    for (int i = 0; i < n; i++) y[(long)incy * i] = dotconj_z(m, a + (long)lda * i, 1, x, incx);
+  } else {
+    return -1;
+  }
+  return 0;
+}
+float orc_sdot(int n, const float* x, int incx, const float* y, int incy) {
+  return (float)dot_s(n, x, incx, y, incy);
+}
+void orc_zdot(int n, const double* x, int incx, const double* y, int incy, int conj,
+              double* out) {
+  const cplx r = conj ? dotconj_z(n, (const cplx*)x, incx, (const cplx*)y, incy)
+                      : dot_z(n, (const cplx*)x, incx, (const cplx*)y, incy);
+  out[0] = r.re;
+  out[1] = r.im;
+}
+float orc_snrm2(int n, const float* x, int incx) {
+  return (float)std::sqrt(dot_s(n, x, incx, x, incx));
+}
+double orc_dznrm2(int n, const double* x_, int incx) {
+  const cplx* x = (const cplx*)x_;
+  double sum = 0.0;
+  if (n & 1) {
+    sum = x[0].re * x[0].re + x[0].im * x[0].im;
+    x += incx;
+    n--;
+  }
+  while (n > 0) {
+    sum += x[0].re * x[0].re + x[0].im * x[0].im + x[incx].re * x[incx].re +
+           x[incx].im * x[incx].im;
+    x += 2 * (long)incx;
+    n -= 2;
+  }
+  return std::sqrt(sum);
+}
+void orc_sger(int m, int n, const float* x, int incx, const float* y, int incy, float* a,
+              int lda) {
+  for (int j = 0; j < n; j++) {
+    const float t = y[(long)incy * j];
+    for (int i = 0; i < m; i++) a[(long)lda * j + i] = t * x[(long)incx * i];
+  }
+}
+void orc_zger(int m, int n, const double* x_, int incx, const double* y_, int incy, double* a_,
+              int lda, int conj) {
+  const cplx* x = (const cplx*)x_;
+  const cplx* y = (const cplx*)y_;
+  cplx* a = (cplx*)a_;
+  for (int j = 0; j < n; j++) {
+    cplx t = y[(long)incy * j];
+    if (conj) t.im = -t.im;
+    for (int i = 0; i < m; i++) a[(long)lda * j + i] = cmul(t, x[(long)incx * i]);
+  }
+}
+
 // =============================================================================================
 // Factorization.LuInverse (Factorization.LuInverse.cs:123-199): A^-1 from the LU factors.
 // Returns 0, or 1 when a diagonal entry of U is zero (MatFlat throws there, before writing).

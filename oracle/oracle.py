@@ -69,6 +69,13 @@ def lib():
             "orc_ddot": (ctypes.c_double, [_I, _d, _I, _d, _I]),
             "orc_dnrm2": (ctypes.c_double, [_I, _d, _I]),
             "orc_dger": (None, [_I, _I, _d, _I, _d, _I, _d, _I]),
+            "orc_zgemv": (_I, [_I, _I, _I, _d, _I, _d, _I, _d, _I]),
+            "orc_sdot": (ctypes.c_float, [_I, _f, _I, _f, _I]),
+            "orc_zdot": (None, [_I, _d, _I, _d, _I, _I, _d]),
+            "orc_snrm2": (ctypes.c_float, [_I, _f, _I]),
+            "orc_dznrm2": (ctypes.c_double, [_I, _d, _I]),
+            "orc_sger": (None, [_I, _I, _f, _I, _f, _I, _f, _I]),
+            "orc_zger": (None, [_I, _I, _d, _I, _d, _I, _d, _I, _I]),
             "orc_dgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
             "orc_dgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
             "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
@@ -140,23 +147,33 @@ def gemm(transa, transb, m, n, k, a, lda, b, ldb, c, ldc):
 
 
 def gemv(trans, m, n, a, lda, x, incx, y, incy):
-    """Blas.MulMatVec (Blas.MulMatVec.cs:138-236), double."""
-    return lib().orc_dgemv(trans, m, n, _fp(a), lda, _fp(x), incx, _fp(y), incy)
+    """Blas.MulMatVec (Blas.MulMatVec.cs:38-336), the overload a's dtype selects."""
+    return getattr(lib(), "orc_%sgemv" % _pre(a))(trans, m, n, _fp(a), lda, _fp(x), incx,
+                                                  _fp(y), incy)
 
 
-def dot(n, x, incx, y, incy):
-    """Blas.Dot (Blas.VectorOperations.cs:143-174), double."""
-    return lib().orc_ddot(n, _fp(x), incx, _fp(y), incy)
+def dot(n, x, incx, y, incy, conj=False):
+    """Blas.Dot / DotConj (Blas.VectorOperations.cs:110-246), the overload x's dtype selects."""
+    if x.dtype == np.complex128:
+        out = np.zeros(2)
+        lib().orc_zdot(n, _fp(x), incx, _fp(y), incy, 1 if conj else 0, _fp(out))
+        return complex(out[0], out[1])
+    return getattr(lib(), "orc_%sdot" % _pre(x))(n, _fp(x), incx, _fp(y), incy)
 
 
 def nrm2(n, x, incx):
-    """Blas.L2Norm (Blas.VectorOperations.cs:50-60), double."""
-    return lib().orc_dnrm2(n, _fp(x), incx)
+    """Blas.L2Norm (Blas.VectorOperations.cs:23-108), the overload x's dtype selects."""
+    name = {"d": "orc_dnrm2", "s": "orc_snrm2", "z": "orc_dznrm2"}[_pre(x)]
+    return getattr(lib(), name)(n, _fp(x), incx)
 
 
-def ger(m, n, x, incx, y, incy, a, lda):
-    """Blas.Outer (Blas.VectorOperations.cs:292-334), double: a(i,j) = y_j * x_i."""
-    lib().orc_dger(m, n, _fp(x), incx, _fp(y), incy, _fp(a), lda)
+def ger(m, n, x, incx, y, incy, a, lda, conj=False):
+    """Blas.Outer / OuterConj (Blas.VectorOperations.cs:248-420): a(i,j) = y_j * x_i (conj(y_j)
+    * x_i), the overload x's dtype selects."""
+    if x.dtype == np.complex128:
+        lib().orc_zger(m, n, _fp(x), incx, _fp(y), incy, _fp(a), lda, 1 if conj else 0)
+    else:
+        getattr(lib(), "orc_%sger" % _pre(x))(m, n, _fp(x), incx, _fp(y), incy, _fp(a), lda)
 
 
 def lu_inverse(n, a, lda, piv):
