@@ -23,11 +23,8 @@ namespace mfg {
 // one warp per matrix; G < 32: 32/G matrices per warp, which amortises the per-column square root
 // and the serial solve steps over several matrices).  dsum: n doubles of per-group scratch.
 // Returns 0, or k+1 when A is not positive definite at column k.
-// stage (optional, n doubles of shared memory): each step first copies row k of L, which every
-// lane of the group reads, into shared memory with one parallel round of loads.
 template <int G, bool IM>
-__device__ int potrf_group(double* a, int n, long long lda, double* dsum,
-                           double* stage = nullptr) {
+__device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int j = lane; j < n; j += G) dsum[j] = 0.0;
@@ -37,18 +34,11 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum,
     const double s = __dsub_rn(colk[k], dsum[k]);
     if (!positive(s)) return k + 1;  // uniform across the group
     const double lkk = __dsqrt_rn(s);
-    const double* rowk = a + k;      // L(k, t) = rowk[t * incr]
-    long long incr = lda;
-    if (stage && k + 1 < n) {
-      for (int t = lane; t < k; t += G) stage[t] = rowk[(long long)t * lda];
-      rowk = stage;
-      incr = 1;
-    }
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += G) {
       // Dot(k, a + j, lda, a + k, lda): row j of L against row k of L.
-      const double d = exact_dot<IM>(k, a + j, lda, rowk, incr);
+      const double d = exact_dot<IM>(k, a + j, lda, a + k, lda);
       const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], d), lkk);
       colk[j] = t;
       dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
@@ -103,8 +93,8 @@ static_assert(4 * chol_group_doubles<8>() <= SMEM_WARP_DOUBLES_C, "smem layout")
 static_assert(8 * chol_group_doubles<4>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 
 // Per-warp shared memory when the solves are staged in global memory (BatchArgs::gsolve): the
-// column sums of the warp's groups and their staged rows (2 x 4G doubles each).
-constexpr int SMEM_WARP_DOUBLES_CG = 2 * 4 * 32 + 2;
+// column sums of the warp's groups only (4G doubles each).
+constexpr int SMEM_WARP_DOUBLES_CG = 4 * 32 + 2;
 
 static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
@@ -119,7 +109,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
   const int group = lane / G;
   const long long gg = ((long long)blockIdx.x * WARPS + warp) * GPW + group;
   const bool gs = p.gsolve != nullptr;
-  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 2 * 4 * G
+  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 4 * G
                           : sm_dyn + warp * SMEM_WARP_DOUBLES_C + group * chol_group_doubles<G>();
   double* gsol = gs ? p.gsolve + ((long long)blockIdx.x * WARPS + warp) * GSOLVE_STRIDE_C +
                           group * gsolve_group_doubles(G)
@@ -138,10 +128,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
-      // The staged row follows the column sums (in the shared layout without global solve
-      // staging it shares the solve's space, used only afterwards).
-      double* stage = (n <= 4 * G && p.stage_bcast) ? scr + 4 * G : nullptr;
-      const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr, stage);
+      const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
       if (info == 0 && p.nrhs > 0)
         potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;

@@ -108,13 +108,9 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
 // and in `info` the first zero pivot (k+1), or 0.
-// stage (optional, 2 * max(m, n) elements of shared memory): every step first copies the two
-// vectors that all lanes read, row k of L (strided in memory) and the head of column k+1 of U,
-// into shared memory with one parallel round of loads; the dots then read them from there.
 template <class Tr, int IM, int DB = DOT_BLOCK>
 __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
-                        typename Tr::Acc* scol, int& sign, int& info,
-                        typename Tr::T* stage = nullptr) {
+                        typename Tr::Acc* scol, int& sign, int& info) {
   using T = typename Tr::T;
   using Acc = typename Tr::Acc;
   const int lane = threadIdx.x & 31;
@@ -123,7 +119,6 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
   info = 0;
   __syncwarp();
   const int K = m < n ? m : n;
-  const int mn = m > n ? m : n;
   lu_finish_column<Tr>(a, m, n, lda, 0, 0, scol, piv, sign, info);
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
@@ -131,24 +126,13 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
     const int C = (k1 < K && k >= 1) ? m - k1 : 0;  // prefixes of column k1 (rows [k1, m))
     const T* rowk = a + k;                    // L(k, t) = rowk[t*lda]
     const T* colk1 = a + (long long)k1 * lda;
-    long long incr = lda;                     // stride of rowk
-    if (stage) {
-      if (R > 0)
-        for (int t = lane; t < k; t += 32) stage[t] = rowk[(long long)t * lda];
-      if (C > 0)
-        for (int t = lane; t < k - 1; t += 32) stage[mn + t] = colk1[t];
-      __syncwarp();
-      rowk = stage;
-      colk1 = stage + mn;
-      incr = 1;
-    }
     for (int d = lane; d < R + C; d += 32) {
       const bool isrow = d < R;
       const int idx = isrow ? k1 + d : k1 + (d - R);
       const T* x = isrow ? rowk : a + idx;
       const T* y = isrow ? a + (long long)idx * lda : colk1;
       const int len = isrow ? k : k - 1;
-      const Acc s = Tr::template dot<IM, DB>(len, x, isrow ? incr : lda, y, 1);
+      const Acc s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
       if (isrow) {
         T* dst = a + (long long)idx * lda + k;
         *dst = Tr::fin(*dst, s);
@@ -193,7 +177,7 @@ __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const 
 
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 // Per-warp shared memory when the solve is staged in global memory (BatchArgs::gsolve).
-constexpr int SMEM_WARP_DOUBLES_G = 3 * SMEM_N + 2;
+constexpr int SMEM_WARP_DOUBLES_G = SMEM_N + 2;
 
 static size_t getrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_G : SMEM_WARP_DOUBLES) * warps;
@@ -220,12 +204,9 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
                                  : p.gscratch + gw * p.gscratch_stride;
     // The solve's staging: after the column sums in the same buffer, or the warp's global slice.
     double* sol = (n <= SMEM_N && gs) ? p.gsolve + gw * GSOLVE_STRIDE : scr + n;
-    // The factorization's staged vectors (2n doubles) follow the column sums; in the shared
-    // layout without global solve staging they share the solve's space (used only afterwards).
-    double* stage = (n <= SMEM_N && p.stage_bcast) ? scr + SMEM_N : nullptr;
     const int ldx = n | 1;
     int sign = 1, info = 0;
-    if (!p.solve_only) lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info, stage);
+    if (!p.solve_only) lu_warp<DTraits, IM, DB>(a, n, n, lda, piv, scr, sign, info);
     if (p.nrhs > 0)
       getrs_warp(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
     if (lane == 0 && !p.solve_only) {

@@ -40,7 +40,6 @@ struct BatchArgs {
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4)
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
-  int stage_bcast;           // getrf/potrf: stage each step's broadcast vectors in shared memory
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and
