@@ -343,6 +343,11 @@ MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, 
 MFG_API int mfg_plan_getri_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                    const int* lda, const int64_t* a_off, const int64_t* piv_off);
 MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info);
+/* The float and Complex overloads on the same plan (Factorization.LuInverse.cs:27-103, :219-295;
+ * Complex as interleaved (re, im) doubles, offsets in elements): bit-identical to MatFlat, info
+ * as above (a diagonal entry counts as zero when it is exactly 0, or 0 + 0i). */
+MFG_API int mfg_sgetri_batched(mfg_plan* plan, float* a, const int* piv, int* info);
+MFG_API int mfg_zgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info);
 
 /* Householder QR of every tall matrix (Factorization.Qr; m[i] >= n[i], lda[i] >= m[i]), then,
  * when nrhs > 0, the least-squares solve min ||A x - b|| of nrhs right-hand sides per matrix

@@ -51,6 +51,8 @@ _SIGS = {
     "mfg_dgemm": (_I, [_vp, _I, _I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I]),
     "mfg_dgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_sgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
+    "mfg_sgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
+    "mfg_zgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_zgetri": (_I, [_vp, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_plan_getrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _I, _vp]),
     "mfg_plan_potrf_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _I, _vp]),
@@ -622,9 +624,11 @@ class LuInverseBatch(_Batch):
         super().__init__(ctx, h)
         self.count = len(self._n)
 
-    def run(self, a, piv, info):
-        rc = self.ctx.lib.mfg_dgetri_batched(self.h, _dptr(a), _dptr(piv), _dptr(info))
-        self.ctx.check(rc, "mfg_dgetri_batched")
+    def run(self, a, piv, info, dtype=None):
+        """Element type as in LuBatch.run (float64, float32 or complex128)."""
+        name = "mfg_%sgetri_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(piv), _dptr(info))
+        self.ctx.check(rc, name)
 
     def run_host(self, a, piv, info):
         """The inverse on host arrays, copies pipelined with compute.  Synchronous."""

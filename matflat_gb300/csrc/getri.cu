@@ -24,6 +24,8 @@
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_scalar.cuh"
+#include "mf_solve.cuh"
 
 namespace mfg {
 
@@ -208,6 +210,121 @@ __global__ void __launch_bounds__(INV_WARPS * 32) getri_batched_kernel(BatchArgs
                    p.info + mat);
     __syncwarp();
   }
+}
+
+// ---- The float and Complex overloads (Factorization.LuInverse.cs:27-103, :219-295) -----------
+// One warp per matrix, the single-matrix algorithm: the zero-diagonal and permutation checks of
+// the double kernel, then the factors are copied to the warp's scratch (leading dimension n), A is
+// set to the columns of P^T and solved RHS_CHUNK columns at a time, unit-lower (the LuInverse
+// idiom; Complex divides by the explicit Complex(1, 0)) then upper, in MatFlat's order.
+// Scratch per warp (getri_t_scratch_bytes): n*n elements, then the staged columns and their
+// accumulators (the permutation check's bitmap reuses the staged columns).
+template <class S>
+__device__ __forceinline__ typename S::T inv_elem(double v);
+template <>
+__device__ __forceinline__ float inv_elem<SSolve>(double v) { return (float)v; }
+template <>
+__device__ __forceinline__ zdouble inv_elem<ZSolve<false>>(double v) { return zmake(v, 0.0); }
+
+__device__ __forceinline__ bool inv_zero(float v) { return v == 0.0f; }
+__device__ __forceinline__ bool inv_zero(zdouble v) { return v.re == 0.0 && v.im == 0.0; }
+
+template <class S>
+__global__ void __launch_bounds__(INV_WARPS * 32) getri_batched_t_kernel(BatchArgs p) {
+  using T = typename S::T;
+  using Acc = typename S::Acc;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * INV_WARPS + warp;
+  char* scr = reinterpret_cast<char*>(p.gscratch + gw * p.gscratch_stride);
+  T* abase = reinterpret_cast<T*>(p.a);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    T* a = abase + p.a_off[mat];
+    const int* piv = p.piv + p.piv_off[mat];
+    const int ldx = n | 1;
+    T* work = reinterpret_cast<T*>(scr);
+    Acc* acc = reinterpret_cast<Acc*>(scr + ((long long)n * n * sizeof(T) + 15) / 16 * 16);
+    T* xs = reinterpret_cast<T*>(acc + RHS_CHUNK * ldx);
+    // First zero diagonal entry (LuInverse.cs:145-152): nothing is written.
+    int bad = INT_MAX;
+    for (int j = lane; j < n; j += 32)
+      if (inv_zero(a[(long long)j * lda + j])) bad = min(bad, j);
+    for (int o = 16; o > 0; o >>= 1) bad = min(bad, __shfl_xor_sync(FULL_MASK, bad, o));
+    if (bad != INT_MAX) {
+      if (lane == 0) p.info[mat] = bad + 1;
+      continue;
+    }
+    unsigned* seen = reinterpret_cast<unsigned*>(xs);
+    for (int w = lane; w < ((n + 31) >> 5); w += 32) seen[w] = 0u;
+    __syncwarp();
+    int badp = 0;
+    for (int t = lane; t < n; t += 32) {
+      const int c = piv[t];
+      if (c < 0 || c >= n)
+        badp = 1;
+      else if (atomicOr(&seen[c >> 5], 1u << (c & 31)) & (1u << (c & 31)))
+        badp = 1;
+    }
+    if (__any_sync(FULL_MASK, badp)) {
+      if (lane == 0) p.info[mat] = -1;
+      continue;
+    }
+    for (long long e = lane; e < (long long)n * n; e += 32) {
+      const int j = (int)(e / n);
+      const int i = (int)(e - (long long)j * n);
+      work[e] = a[(long long)j * lda + i];
+    }
+    __syncwarp();
+    for (long long e = lane; e < (long long)n * n; e += 32) {
+      const int j = (int)(e / n);
+      const int i = (int)(e - (long long)j * n);
+      a[(long long)j * lda + i] = inv_elem<S>(0.0);
+    }
+    __syncwarp();
+    for (int j = lane; j < n; j += 32) a[lda * piv[j] + j] = inv_elem<S>(1.0);
+    __syncwarp();
+    for (int c0 = 0; c0 < n; c0 += RHS_CHUNK) {
+      const int nr = n - c0 < RHS_CHUNK ? n - c0 : RHS_CHUNK;
+      for (int e = lane; e < nr * n; e += 32) {
+        const int r = e / n;
+        const int i = e - r * n;
+        xs[r * ldx + i] = a[(long long)(c0 + r) * lda + i];
+      }
+      __syncwarp();
+      warp_solve_dot<32, S>(work, n, 1, n, true, xs, ldx, acc, nr);
+      warp_solve_sweep<32, S>(work, n, n, 1, xs, ldx, nr);
+      for (int e = lane; e < nr * n; e += 32) {
+        const int r = e / n;
+        const int i = e - r * n;
+        a[(long long)(c0 + r) * lda + i] = xs[r * ldx + i];
+      }
+      __syncwarp();
+    }
+    if (lane == 0) p.info[mat] = 0;
+    __syncwarp();
+  }
+}
+
+long long getri_t_scratch_bytes(int n, int elem) {
+  const long long es = elem == 1 ? 4 : 16, as = elem == 1 ? 8 : 16;
+  const long long ld = n | 1;
+  const long long b = ((long long)n * n * es + 15) / 16 * 16 + RHS_CHUNK * ld * (as + es);
+  return (b + 255) / 256 * 256;
+}
+
+cudaError_t launch_getri_batched_t(const BatchArgs& args, int elem, int ctas, cudaStream_t s) {
+  if (elem == 1)
+    getri_batched_t_kernel<SSolve><<<ctas, INV_WARPS * 32, 0, s>>>(args);
+  else
+    getri_batched_t_kernel<ZSolve<false>><<<ctas, INV_WARPS * 32, 0, s>>>(args);
+  return cudaGetLastError();
 }
 
 cudaError_t init_getri_attributes() {

@@ -191,6 +191,10 @@ int getri_ctas_per_sm();
 int getri_max_n();
 cudaError_t init_getri_attributes();
 cudaError_t launch_getri_batched(const BatchArgs& args, int ctas, cudaStream_t s);
+// Float (elem 1) and Complex (elem 2) batched LuInverse: same plan and launch shape, per-warp
+// global scratch of getri_t_scratch_bytes(max n, elem) bytes (args.gscratch_stride in doubles).
+long long getri_t_scratch_bytes(int n, int elem);
+cudaError_t launch_getri_batched_t(const BatchArgs& args, int elem, int ctas, cudaStream_t s);
 
 // Batched LU (+ solve); launched persistent: grid = ctas, WARPS warps per CTA.
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);

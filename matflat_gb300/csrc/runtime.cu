@@ -143,6 +143,7 @@ struct mfg_plan {
 namespace {
 
 void pipe_release(mfg_plan* p);
+int plan_set_elem(mfg_plan* p, int elem);
 
 int fail(mfg_ctx* ctx, int code, const char* fmt, ...) {
   if (ctx) {
@@ -334,6 +335,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_zgetrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::GETRF)
     e = mfg::launch_getrf_batched(p->args, p->ctas, p->warps, s);
+  else if (p->kind == mfg_plan::GETRI && p->elem != 0)
+    e = mfg::launch_getri_batched_t(p->args, p->elem, p->ctas, s);
   else if (p->kind == mfg_plan::GETRI)
     e = mfg::launch_getri_batched(p->args, p->ctas, s);
   else if (p->kind == mfg_plan::GEVD)
@@ -1737,6 +1740,36 @@ MFG_API int mfg_plan_getri_batched(mfg_ctx* ctx, mfg_plan** plan, int count, con
   return plan_create(ctx, plan, mfg_plan::GETRI, count, n, lda, a_off, piv_off, 0, nullptr);
 }
 
+}  // extern "C"
+
+static int getri_batched_any(mfg_plan* plan, int elem, void* a, const int* piv, int* info) {
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::GETRI) return fail(ctx, -1, "plan is not a getri plan");
+  if (plan->count > 0) {
+    if (!a) return fail(ctx, -2, "a is null");
+    if (!piv) return fail(ctx, -3, "piv is null");
+    if (!info) return fail(ctx, -4, "info is null");
+  }
+  const int rc = plan_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->args.a = (double*)a;
+  plan->args.piv = const_cast<int*>(piv);
+  plan->args.b = nullptr;
+  plan->args.sign = nullptr;
+  plan->args.info = info;
+  return plan_execute(plan, a, piv, info, nullptr, nullptr);
+}
+
+extern "C" {
+
+MFG_API int mfg_sgetri_batched(mfg_plan* plan, float* a, const int* piv, int* info) {
+  return getri_batched_any(plan, 1, a, piv, info);
+}
+MFG_API int mfg_zgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info) {
+  return getri_batched_any(plan, 2, a, piv, info);
+}
+
 MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
@@ -1746,6 +1779,8 @@ MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* i
     if (!piv) return fail(ctx, -3, "piv is null");
     if (!info) return fail(ctx, -4, "info is null");
   }
+  const int rc = plan_set_elem(plan, 0);
+  if (rc != MFG_OK) return rc;
   plan->args.a = a;
   plan->args.piv = const_cast<int*>(piv);
   plan->args.b = nullptr;
@@ -2122,7 +2157,15 @@ int plan_set_elem(mfg_plan* p, int elem) {
   mfg_ctx* ctx = p->ctx;
   p->elem = elem;
   long long stride = p->dstride;
-  if (elem != 0) {
+  if (elem != 0 && p->kind == mfg_plan::GETRI) {
+    // The float / Complex inverse keeps a copy of the factors per warp in global scratch.
+    stride = mfg::getri_t_scratch_bytes(p->max_n, elem) / (long long)sizeof(double);
+    const size_t need = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+    if (need > p->scratch.bytes) {
+      MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      MFG_CUDA(ctx, p->scratch.reserve(need));
+    }
+  } else if (elem != 0) {
     stride = 0;
     if (p->max_n > mfg::SMEM_N) {
       const long long base = (mfg::warp_scratch_doubles(p->max_n) + 31) / 32 * 32;

@@ -1262,6 +1262,34 @@ void orc_dlu_inverse_batched(long count, const int* n, const int64_t* a_off, dou
   });
 }
 
+// The float and Complex overloads of the batched LuInverse (offsets in elements).
+void orc_slu_inverse_batched(long count, const int* n, const int64_t* a_off, float* a,
+                             const int64_t* piv_off, const int* piv, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    float* ai = a + a_off[i];
+    int bad = 0;
+    for (int j = 0; j < ni && !bad; j++)
+      if (ai[(long)ni * j + j] == 0.0f) bad = j + 1;
+    info[i] = bad;
+    if (!bad) orc_slu_inverse(ni, ai, ni, piv + piv_off[i]);
+  });
+}
+void orc_zlu_inverse_batched(long count, const int* n, const int64_t* a_off, double* a,
+                             const int64_t* piv_off, const int* piv, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    const int ni = n[i];
+    double* ai = a + 2 * a_off[i];
+    int bad = 0;
+    for (int j = 0; j < ni && !bad; j++) {
+      const double* d = ai + 2 * ((long)ni * j + j);
+      if (d[0] == 0.0 && d[1] == 0.0) bad = j + 1;
+    }
+    info[i] = bad;
+    if (!bad) orc_zlu_inverse(ni, ai, ni, piv + piv_off[i]);
+  });
+}
+
 // Batched GEVD front half (lda = ldb = n): pair i is A at a + a_off[i], B at b + b_off[i], and C
 // is written at c + a_off[i].
 void orc_dgevd_front_batched(long count, const int* n, const int64_t* a_off, const double* a,

@@ -79,6 +79,8 @@ def lib():
             "orc_dgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
             "orc_dgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
             "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
+            "orc_slu_inverse_batched": (None, [_L, _i, _l, _f, _l, _i, _i, _I]),
+            "orc_zlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
             "orc_dchol_grad": (_I, [_I, _d, _I, _d, _d, _d]),
             "orc_dchol_grad_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _d, _i, _I]),
             "orc_dqr_ls_batched": (None, [_L, _i, _i, _l, _d, _l, _d, _l, _d, _I]),
@@ -215,7 +217,8 @@ def lu_solve_batched(n, a_off, a, piv_off, piv, b_off, b, nrhs, sign, nthreads=1
 
 def lu_inverse_batched(n, a_off, a, piv_off, piv, info, nthreads=1):
     """Factorization.LuInverse per matrix (lda = n); info = j+1 for the first zero U(j,j)."""
-    lib().orc_dlu_inverse_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+    getattr(lib(), "orc_%slu_inverse_batched" % _pre(a))(
+                                  len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
                                   _p(piv_off, ctypes.c_int64), _p(piv, ctypes.c_int),
                                   _p(info, ctypes.c_int), nthreads)
 

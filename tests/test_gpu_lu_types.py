@@ -150,3 +150,50 @@ def test_complex_unit_lower_divides_by_one(mf):
     assert_bits(_host(da).view(np.float64), oa.view(np.float64))
     assert_bits(_host(db).view(np.float64), ob.view(np.float64))
     assert np.signbit(ob.view(np.float64)).any() and not np.signbit(ob.view(np.float64)).all()
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex128])
+def test_lu_inverse_batched_types(mf, dt):
+    """Batched LuInverse, float and Complex: the inverse of the factors of every matrix, bit for
+    bit against the oracle, with singular factors (info) and a double run on the same plan."""
+    import torch
+    rng = np.random.default_rng(330 + (dt == np.complex128))
+    n = rng.integers(1, 150, size=300).astype(np.int32)
+    n[:3] = [1, 129, 149]
+    a_off, atot = _packed(n, n)
+    piv_off, ptot = _packed(n, np.ones_like(n))
+    if dt == np.complex128:
+        a = rng.standard_normal(atot) + 1j * rng.standard_normal(atot)
+    else:
+        a = rng.standard_normal(atot).astype(dt)
+    piv = np.zeros(ptot, np.int32)
+    for i in range(len(n)):
+        ni = int(n[i])
+        ai = a[a_off[i]:a_off[i] + ni * ni]
+        oracle.lu(ni, ni, ai, ni, piv[piv_off[i]:piv_off[i] + ni])
+    a[a_off[5] + int(n[5]) * 2 + 2 if n[5] > 2 else a_off[5]] = 0    # a zero diagonal entry
+    oa = a.copy()
+    oinfo = np.zeros(len(n), np.int32)
+    oracle.lu_inverse_batched(n, a_off, oa, piv_off, piv, oinfo, 4)
+    assert oinfo[5] > 0
+    batch = mf.LuInverseBatch(n, a_off, piv_off)
+    da, dpiv = _dev(a), _dev(piv)
+    dinfo = torch.full((len(n),), -7, dtype=torch.int32, device="cuda")
+    batch.run(da, dpiv, dinfo)
+    mf.context().synchronize()
+    np.testing.assert_array_equal(_host(dinfo), oinfo)
+    assert_bits(_flat(_host(da)), _flat(oa))
+    # The double overload on the same plan afterwards.
+    d = rng.standard_normal(atot)
+    dp = np.zeros(ptot, np.int32)
+    for i in range(len(n)):
+        ni = int(n[i])
+        oracle.lu(ni, ni, d[a_off[i]:a_off[i] + ni * ni], ni, dp[piv_off[i]:piv_off[i] + ni])
+    od = d.copy()
+    oinfo = np.zeros(len(n), np.int32)
+    oracle.lu_inverse_batched(n, a_off, od, piv_off, dp, oinfo, 4)
+    dd = _dev(d)
+    batch.run(dd, _dev(dp), dinfo)
+    mf.context().synchronize()
+    assert_bits(_host(dd), od)
+    batch.close()
