@@ -79,6 +79,8 @@ struct QrBatchArgs {
   long long gscratch_stride;
   int group;                 // lanes per matrix: 32 (one warp) or 16, 8, 4
   int solve_only;            // a and rdiag hold the factorization; only solve the b blocks
+  int fused;                 // one pass per trailing column and step (qr_warp_fused); the
+                             // coefficient scratch then holds 2 (n + nrhs) values
 };
 // Shared-memory coefficients per matrix of the batched QR for a group size.
 int qr_smem_coefs(int group);

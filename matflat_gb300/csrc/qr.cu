@@ -68,6 +68,12 @@ struct QrArith<double> {
     return __dadd_rn(q, __dmul_rn(a, s));
   }
   static __device__ __forceinline__ double rdiag_elem(double r) { return r; }
+  // One term and one pair of Internals.Dot's tree (for loops that fuse the dot with an update).
+  static __device__ __forceinline__ double prod(double x, double y) { return imul_rn(x, y); }
+  static __device__ __forceinline__ double pair(double s, double x0, double y0, double x1,
+                                                double y1) {
+    return __dadd_rn(s, __dadd_rn(imul_rn(x0, y0), imul_rn(x1, y1)));
+  }
 };
 
 template <>
@@ -103,6 +109,13 @@ struct QrArith<float> {
     return __fadd_rn(q, __fmul_rn(a, s));
   }
   static __device__ __forceinline__ float rdiag_elem(float r) { return r; }
+  static __device__ __forceinline__ double prod(float x, float y) {
+    return __dmul_rn((double)x, (double)y);
+  }
+  static __device__ __forceinline__ double pair(double s, float x0, float y0, float x1, float y1) {
+    return __dadd_rn(s, __dadd_rn(__dmul_rn((double)x0, (double)y0),
+                                  __dmul_rn((double)x1, (double)y1)));
+  }
 };
 
 // Complex overload (Factorization.Qr.cs:198-255, :436-492, :677-730): the norm is real
@@ -206,6 +219,94 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::
   }
 }
 
+// The same factorization with every trailing column visited once per step instead of twice: at
+// step k a lane takes a trailing column, applies reflector k-1 to it (cj += v_{k-1} s) and, in the
+// same pass, accumulates reflector k's dot Dot(m-k, v_k, cj) over the updated entries; column k
+// itself is brought up to date first, because v_k is formed from it.  Each entry sees the same
+// operations in the same order as in qr_warp (every update of a column precedes the next dot on
+// it, and the dot's pairwise tree is unchanged), so the factors and rdiag are bit-identical.
+// coefs: 2 (n + nb) values (the previous step's coefficients and the current ones).
+template <typename T, int G = 32>
+__device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag,
+                              T* b, long long ldb, int nb, T* coefs) {
+  using A = QrArith<T>;
+  using R = typename A::R;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  T* pc = coefs;              // coefficients of reflector k-1 (index: column - k)
+  T* nc = coefs + n + nb;     // coefficients of reflector k (index: column - k - 1)
+  const T* pv = nullptr;      // reflector k-1 (column k-1 of a), or null
+  bool pskip = false;         // reflector k-1 is degenerate (v0 == 0): right-hand sides skip it
+  for (int k = 0; k < n; ++k) {
+    T* ck = a + (long long)k * lda;
+    if (pv) {
+      const T s0 = pc[0];
+      for (int r = k - 1 + lane; r < m; r += G) ck[r] = A::muladd(ck[r], pv[r], s0);
+      __syncwarp(gm);
+    }
+    const int len = m - k;
+    const R norm = A::norm(len, ck + k);  // every lane of the group, same value
+    const bool has = A::nzr(norm);
+    T v0{};
+    if (has) {
+      for (int r = k + lane; r < m; r += G) ck[r] = A::divn(ck[r], norm);
+      __syncwarp(gm);
+      if (lane == 0) ck[k] = A::add1(ck[k]);
+      __syncwarp(gm);
+      v0 = ck[k];
+    }
+    const int ncols = (n - k - 1) + nb;
+    for (int c = lane; c < ncols; c += G) {
+      const int j = k + 1 + c;
+      T* cj = qr_col(a, lda, n, b, ldb, j);
+      const bool upd = pv && !(j >= n && pskip);
+      const T sp = upd ? pc[c + 1] : T{};
+      if (upd) cj[k - 1] = A::muladd(cj[k - 1], pv[k - 1], sp);
+      if (has) {
+        // Dot(len, ck + k, cj + k) over the updated entries.
+        int r = k;
+        double d = 0.0;
+        if (len & 1) {
+          const T u = upd ? A::muladd(cj[r], pv[r], sp) : cj[r];
+          cj[r] = u;
+          d = A::prod(ck[r], u);
+          ++r;
+        }
+        for (; r < m; r += 2) {
+          T u0 = cj[r], u1 = cj[r + 1];
+          if (upd) {
+            u0 = A::muladd(u0, pv[r], sp);
+            u1 = A::muladd(u1, pv[r + 1], sp);
+            cj[r] = u0;
+            cj[r + 1] = u1;
+          }
+          d = A::pair(d, ck[r], u0, ck[r + 1], u1);
+        }
+        nc[c] = A::coef(d, v0);
+      } else if (upd) {
+        for (int r = k; r < m; ++r) cj[r] = A::muladd(cj[r], pv[r], sp);
+      }
+    }
+    __syncwarp(gm);
+    if (lane == 0) rdiag[k] = A::neg_r(norm);
+    __syncwarp(gm);
+    pv = has ? ck : nullptr;
+    pskip = has && !A::nz(v0);
+    T* t = pc;
+    pc = nc;
+    nc = t;
+  }
+  // Reflector n-1 still owes its update to the right-hand sides.
+  if (pv && !pskip) {
+    for (int c = lane; c < nb; c += G) {
+      T* cj = b + (long long)c * ldb;
+      const T sp = pc[c];
+      for (int r = n - 1; r < m; ++r) cj[r] = A::muladd(cj[r], pv[r], sp);
+    }
+  }
+  __syncwarp(gm);
+}
+
 // Applies the stored reflectors of a factored matrix to the nb columns of b, in the order and
 // arithmetic the factorization applies them (the right-hand-side branch of qr_warp): reflector k
 // exists when rdiag[k] != 0 (the column norm was nonzero) and acts when v[0] != 0.
@@ -297,7 +398,7 @@ __device__ void qr_q_warp(const T* a, int m, int n, long long lda, T* q, long lo
 }
 
 constexpr int QR_SMEM_COEFS = 256;   // shared coefficients per warp (G = 32)
-constexpr int QR_GROUP_COEFS = 128;  // shared coefficients per group (G < 32)
+constexpr int QR_GROUP_COEFS = 136;  // shared coefficients per group (G < 32): 2 x (64 + 4)
 
 int qr_smem_coefs(int group) { return group == 32 ? QR_SMEM_COEFS : QR_GROUP_COEFS; }
 
@@ -329,10 +430,13 @@ __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
       T* a = p.a + p.a_off[mat];
       T* rd = p.rdiag + p.rdiag_off[mat];
       T* b = p.nrhs > 0 ? p.b + p.b_off[mat] : nullptr;
-      T* coefs = (n + p.nrhs <= CO) ? &sm[warp][g][0]
-                                    : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
+      const int need = p.fused ? 2 * (n + p.nrhs) : n + p.nrhs;
+      T* coefs = (need <= CO) ? &sm[warp][g][0]
+                              : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
       if constexpr (SOLVE)
         qr_apply_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+      else if (p.fused)
+        qr_warp_fused<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       else
         qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       if (p.nrhs > 0) qr_rsolve_warp<T, G>(a, n, lda, rd, b, m, p.nrhs);

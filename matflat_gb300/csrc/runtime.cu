@@ -740,9 +740,12 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
     return cuda_fail(ctx, e, "cudaMemcpy(plan descriptors)");
   }
   choose_shape(p, group == 32 ? 0 : 4);
+  // The fused variant keeps two steps' coefficients.
+  const int fused = env_int("MFG_QR_FUSED", 0) ? 1 : 0;
+  const int coef_need = fused ? 2 * max_cols : max_cols;
   long long stride = 0;
-  if (max_cols > mfg::qr_smem_coefs(group)) {
-    stride = (max_cols + 31) / 32 * 32;
+  if (coef_need > mfg::qr_smem_coefs(group)) {
+    stride = (coef_need + 31) / 32 * 32;
     e = p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)p->ctas * p->warps *
                            (size_t)(32 / group));
     if (e != cudaSuccess) {
@@ -767,6 +770,8 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   fill(p->qd);
   fill(p->qs);
   fill(p->qz);
+  p->qd.fused = p->qs.fused = fused;
+  p->qz.fused = 0;
   p->qd.group = group_d;
   p->qs.group = group_s;
   p->qz.group = 32;
