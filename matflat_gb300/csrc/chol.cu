@@ -54,6 +54,83 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
   return 0;
 }
 
+// The same factorization with every column's dots split in two halves computed one step apart,
+// so that a step's lanes hold twice as many (half as long) dot items.  Column c's dot for row j,
+// Dot(c, L(j,:), L(c,:)), is split at the pair boundary h(c) (about c/2, with c's parity: an odd
+// length keeps its lone first product in the first half); the first half runs at step c-2 (it
+// reads columns below h(c) <= c-2 only), the second half, continued from the first half's sum,
+// at step c-1 right after column c-1 is finished, and column c finishes at step c.  The sums are
+// MatFlat's tree in MatFlat's order, so L is bit-identical to potrf_group's.
+// scratch: 4n doubles (the diagonal sums, the complete dots of the next column, and the
+// first-half sums of the two columns after it, by parity).
+__device__ __forceinline__ int split_point(int c) {
+  return (c & 1) ? ((c >> 1) | 1) : ((c >> 1) & ~1);
+}
+
+template <int G, bool IM>
+__device__ int potrf_group_split(double* a, int n, long long lda, double* dsum) {
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  double* full = dsum + n;   // Dot(k, ...) of the column finished next
+  double* half = dsum + 2 * n;  // first halves, column parity p at half + p * n
+  for (int j = lane; j < n; j += G) {
+    dsum[j] = 0.0;
+    full[j] = 0.0;
+  }
+  __syncwarp(gm);
+  for (int k = 0; k < n; ++k) {
+    double* colk = a + (long long)k * lda;
+    const double s = __dsub_rn(colk[k], dsum[k]);
+    if (!positive(s)) return k + 1;  // uniform across the group
+    const double lkk = __dsqrt_rn(s);
+    __syncwarp(gm);
+    if (lane == 0) colk[k] = lkk;
+    for (int j = k + 1 + lane; j < n; j += G) {
+      const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], full[j]), lkk);
+      colk[j] = t;
+      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
+    }
+    __syncwarp(gm);
+    // Second halves of column c1 = k+1 (rows j > c1) and first halves of c2 = k+2 (rows j > c2).
+    const int c1 = k + 1, c2 = k + 2;
+    const int r1 = c1 < n ? n - c1 - 1 : 0;
+    const int r2 = c2 < n ? n - c2 - 1 : 0;
+    const int h1 = split_point(c1), h2 = split_point(c2);
+    const double* row1 = a + c1;  // L(c1, t) = row1[t * lda]
+    const double* row2 = a + c2;
+    for (int d = lane; d < r1 + r2; d += G) {
+      const bool second = d < r1;
+      const int j = second ? c1 + 1 + d : c2 + 1 + (d - r1);
+      const double* rj = a + j;
+      const double* rc = second ? row1 : row2;
+      double s0;
+      int t0, pairs;
+      double* dst;
+      if (second) {
+        // Dot(1) is its lone product; otherwise continue from the first half's sum.
+        s0 = c1 == 1 ? xmul<IM>(rj[0], rc[0]) : half[(c1 & 1) * n + j];
+        t0 = c1 == 1 ? 1 : h1;
+        pairs = (c1 - t0) >> 1;
+        dst = full + j;
+      } else {
+        s0 = (c2 & 1) ? xmul<IM>(rj[0], rc[0]) : 0.0;
+        t0 = c2 & 1;
+        pairs = (h2 - t0) >> 1;
+        dst = half + (c2 & 1) * n + j;
+      }
+      *dst = exact_dot_pairs<IM>(s0, pairs, rj + (long long)t0 * lda, lda,
+                                 rc + (long long)t0 * lda, lda);
+    }
+    __syncwarp(gm);
+  }
+  for (int c = 1; c < n; ++c) {
+    double* col = a + (long long)c * lda;
+    for (int r = lane; r < c; r += G) col[r] = 0.0;
+  }
+  __syncwarp(gm);
+  return 0;
+}
+
 // L y = b (SolveTriangular Lower/NoTrans) then L^T x = y (Lower/Trans) for nrhs right-hand
 // sides stored column-major with leading dimension ldb.
 template <int G>
@@ -93,14 +170,14 @@ static_assert(4 * chol_group_doubles<8>() <= SMEM_WARP_DOUBLES_C, "smem layout")
 static_assert(8 * chol_group_doubles<4>() <= SMEM_WARP_DOUBLES_C, "smem layout");
 
 // Per-warp shared memory when the solves are staged in global memory (BatchArgs::gsolve): the
-// column sums of the warp's groups only (4G doubles each).
-constexpr int SMEM_WARP_DOUBLES_CG = 4 * 32 + 2;
+// column sums and dot buffers of the warp's groups (4 x 4G doubles each).
+constexpr int SMEM_WARP_DOUBLES_CG = 4 * 4 * 32 + 2;
 
 static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
 }
 
-template <int WARPS, bool IM, int G>
+template <int WARPS, bool IM, int G, bool SPLIT = false>
 __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   constexpr int GPW = 32 / G;  // groups (matrices in flight) per warp
@@ -109,7 +186,7 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
   const int group = lane / G;
   const long long gg = ((long long)blockIdx.x * WARPS + warp) * GPW + group;
   const bool gs = p.gsolve != nullptr;
-  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 4 * G
+  double* smem_group = gs ? sm_dyn + warp * SMEM_WARP_DOUBLES_CG + group * 4 * 4 * G
                           : sm_dyn + warp * SMEM_WARP_DOUBLES_C + group * chol_group_doubles<G>();
   double* gsol = gs ? p.gsolve + ((long long)blockIdx.x * WARPS + warp) * GSOLVE_STRIDE_C +
                           group * gsolve_group_doubles(G)
@@ -128,7 +205,13 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
-      const int info = p.solve_only ? 0 : potrf_group<G, IM>(a, n, lda, scr);
+      int info = 0;
+      if (!p.solve_only) {
+        if constexpr (SPLIT)
+          info = potrf_group_split<G, IM>(a, n, lda, scr);
+        else
+          info = potrf_group<G, IM>(a, n, lda, scr);
+      }
       if (info == 0 && p.nrhs > 0)
         potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
@@ -146,6 +229,12 @@ __global__ void __launch_bounds__(32) potrf_single_kernel(double* a, int n, int 
 template <int WARPS, int G>
 static cudaError_t launch_potrf_wg(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = potrf_smem_bytes(args, WARPS);
+  if constexpr (G == 32) {
+    if (args.split && !args.hw_mul) {
+      potrf_batched_kernel<WARPS, true, G, true><<<ctas, WARPS * 32, smem, s>>>(args);
+      return cudaGetLastError();
+    }
+  }
   if (args.hw_mul)
     potrf_batched_kernel<WARPS, false, G><<<ctas, WARPS * 32, smem, s>>>(args);
   else
@@ -170,6 +259,11 @@ static cudaError_t set_potrf_attr_g() {
   cudaError_t e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  if constexpr (G == 32) {
+    e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   return cudaFuncSetAttribute(potrf_batched_kernel<WARPS, false, G>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }

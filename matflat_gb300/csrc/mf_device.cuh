@@ -97,16 +97,14 @@ constexpr int DOT_BLOCK = 4;
 template <bool IM>
 __device__ __forceinline__ double xmul(double a, double b);
 
+// The pair loop of Internals.Dot continued from a running sum s: s = s + (x_0 y_0 + x_1 y_1),
+// s = s + (x_2 y_2 + x_3 y_3), ... for `pairs` pairs.  A dot split at a pair boundary and
+// evaluated in two calls (the second starting from the first's sum) gives the same bits as one
+// call over the whole length.
 template <int IM = 1, int DOT_BLOCK = mfg::DOT_BLOCK>
-__device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
-                                            const double* y, long long incy) {
-  double s = 0.0;
-  if (len & 1) {
-    s = xmul<IM != 0>(x[0], y[0]);
-    x += incx;
-    y += incy;
-  }
-  const int pairs = len >> 1;
+__device__ __forceinline__ double exact_dot_pairs(double s, int pairs, const double* x,
+                                                  long long incx, const double* y,
+                                                  long long incy) {
   const int blocks = pairs / DOT_BLOCK;
   if (blocks > 0) {
     double xa[2 * DOT_BLOCK], ya[2 * DOT_BLOCK];
@@ -151,6 +149,18 @@ __device__ __forceinline__ double exact_dot(int len, const double* x, long long 
     y += 2 * incy;
   }
   return s;
+}
+
+template <int IM = 1, int DOT_BLOCK = mfg::DOT_BLOCK>
+__device__ __forceinline__ double exact_dot(int len, const double* x, long long incx,
+                                            const double* y, long long incy) {
+  double s = 0.0;
+  if (len & 1) {
+    s = xmul<IM != 0>(x[0], y[0]);
+    x += incx;
+    y += incy;
+  }
+  return exact_dot_pairs<IM, DOT_BLOCK>(s, len >> 1, x, incx, y, incy);
 }
 
 // Copies src[k*stride] to dst[k] (shared memory) for k in [k0, k1) with asynchronous 8-byte

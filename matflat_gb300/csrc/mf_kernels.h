@@ -40,6 +40,8 @@ struct BatchArgs {
   int group;                 // potrf: lanes per matrix (4, 8, 16 or 32)
   int dot_block;             // getrf: pairs per software-pipelined block of the dot loop (2, 4)
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
+  int split;                 // potrf: split every dot in two halves a step apart
+                             // (potrf_group_split; 4n doubles of per-group scratch)
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and
