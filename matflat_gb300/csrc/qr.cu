@@ -68,9 +68,7 @@ struct QrArith<double> {
     return __dadd_rn(q, __dmul_rn(a, s));
   }
   static __device__ __forceinline__ double rdiag_elem(double r) { return r; }
-  // One term and one pair of Internals.Dot's tree (for loops that fuse the dot with an update),
-  // and the norm from its sum of squares.
-  static __device__ __forceinline__ double norm_fin(double s) { return __dsqrt_rn(s); }
+  // One term and one pair of Internals.Dot's tree (for loops that fuse the dot with an update).
   static __device__ __forceinline__ double prod(double x, double y) { return imul_rn(x, y); }
   static __device__ __forceinline__ double pair(double s, double x0, double y0, double x1,
                                                 double y1) {
@@ -111,9 +109,6 @@ struct QrArith<float> {
     return __fadd_rn(q, __fmul_rn(a, s));
   }
   static __device__ __forceinline__ float rdiag_elem(float r) { return r; }
-  static __device__ __forceinline__ float norm_fin(double s) {
-    return __double2float_rn(__dsqrt_rn(s));
-  }
   static __device__ __forceinline__ double prod(float x, float y) {
     return __dmul_rn((double)x, (double)y);
   }
@@ -231,12 +226,9 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::
 // operations in the same order as in qr_warp (every update of a column precedes the next dot on
 // it, and the dot's pairwise tree is unchanged), so the factors and rdiag are bit-identical.
 // coefs: 2 (n + nb) values (the previous step's coefficients and the current ones).
-// NL (lookahead): the lane that owns column k+1 in step k's pass also applies reflector k to it
-// and takes its norm right away (into *nrm), so step k+1 starts without the group-wide norm
-// chain; the norm is the same tree over the same values, so the bits do not change.
-template <typename T, int G = 32, bool NL = false>
+template <typename T, int G = 32>
 __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag,
-                              T* b, long long ldb, int nb, T* coefs, typename QrArith<T>::R* nrm) {
+                              T* b, long long ldb, int nb, T* coefs) {
   using A = QrArith<T>;
   using R = typename A::R;
   const int lane = group_lane<G>();
@@ -247,19 +239,13 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
   bool pskip = false;         // reflector k-1 is degenerate (v0 == 0): right-hand sides skip it
   for (int k = 0; k < n; ++k) {
     T* ck = a + (long long)k * lda;
-    const int len = m - k;
-    R norm;
-    if (NL && k > 0) {
-      // Column k was brought up to date, and its norm taken, by its owner in the last pass.
-      norm = *nrm;
-    } else {
-      if (pv) {
-        const T s0 = pc[0];
-        for (int r = k - 1 + lane; r < m; r += G) ck[r] = A::muladd(ck[r], pv[r], s0);
-        __syncwarp(gm);
-      }
-      norm = A::norm(len, ck + k);  // every lane of the group, same value
+    if (pv) {
+      const T s0 = pc[0];
+      for (int r = k - 1 + lane; r < m; r += G) ck[r] = A::muladd(ck[r], pv[r], s0);
+      __syncwarp(gm);
     }
+    const int len = m - k;
+    const R norm = A::norm(len, ck + k);  // every lane of the group, same value
     const bool has = A::nzr(norm);
     T v0{};
     if (has) {
@@ -276,7 +262,6 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
       const bool upd = pv && !(j >= n && pskip);
       const T sp = upd ? pc[c + 1] : T{};
       if (upd) cj[k - 1] = A::muladd(cj[k - 1], pv[k - 1], sp);
-      T coef{};
       if (has) {
         // Dot(len, ck + k, cj + k) over the updated entries.
         int r = k;
@@ -297,35 +282,9 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
           }
           d = A::pair(d, ck[r], u0, ck[r + 1], u1);
         }
-        coef = A::coef(d, v0);
-        nc[c] = coef;
+        nc[c] = A::coef(d, v0);
       } else if (upd) {
         for (int r = k; r < m; ++r) cj[r] = A::muladd(cj[r], pv[r], sp);
-      }
-      if (NL && c == 0 && j < n) {
-        // Look ahead: apply reflector k to column k+1 now and take its norm over rows
-        // [k+1, m) (Internals.Norm's tree over the updated entries).
-        if (has) cj[k] = A::muladd(cj[k], ck[k], coef);
-        const int ln = m - j;
-        int r = j;
-        double q = 0.0;
-        if (ln & 1) {
-          T u = cj[r];
-          if (has) cj[r] = u = A::muladd(u, ck[r], coef);
-          q = A::prod(u, u);
-          ++r;
-        }
-        for (; r < m; r += 2) {
-          T u0 = cj[r], u1 = cj[r + 1];
-          if (has) {
-            u0 = A::muladd(u0, ck[r], coef);
-            u1 = A::muladd(u1, ck[r + 1], coef);
-            cj[r] = u0;
-            cj[r + 1] = u1;
-          }
-          q = A::pair(q, u0, u0, u1, u1);
-        }
-        *nrm = A::norm_fin(q);
       }
     }
     __syncwarp(gm);
@@ -453,7 +412,6 @@ __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
   constexpr int GPW = 32 / G;
   constexpr int CO = G == 32 ? QR_SMEM_COEFS : QR_GROUP_COEFS;
   __shared__ T sm[WARPS][GPW][CO];
-  __shared__ typename QrArith<T>::R snrm[WARPS][GPW];  // the fused lookahead's next norm
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int g = lane / G;
@@ -477,10 +435,8 @@ __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
                               : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
       if constexpr (SOLVE)
         qr_apply_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
-      else if (p.fused == 2)
-        qr_warp_fused<T, G, true>(a, m, n, lda, rd, b, m, p.nrhs, coefs, &snrm[warp][g]);
       else if (p.fused)
-        qr_warp_fused<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs, &snrm[warp][g]);
+        qr_warp_fused<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       else
         qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       if (p.nrhs > 0) qr_rsolve_warp<T, G>(a, n, lda, rd, b, m, p.nrhs);

@@ -745,7 +745,7 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   choose_shape(p, group == 32 ? 0 : 4);
   // The fused variant (one pass per trailing column and step; default, measured 9 % faster in
   // FP64 and 13 % in FP32 on the 50,000-matrix batch) keeps two steps' coefficients.
-  const int fused = env_int("MFG_QR_FUSED", 1);
+  const int fused = env_int("MFG_QR_FUSED", 1) ? 1 : 0;
   const int coef_need = fused ? 2 * max_cols : max_cols;
   long long stride = 0;
   if (coef_need > mfg::qr_smem_coefs(group)) {
