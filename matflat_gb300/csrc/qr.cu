@@ -272,6 +272,51 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
           d = A::prod(ck[r], u);
           ++r;
         }
+        // Software-pipelined by blocks of QF pairs: the next block's loads are issued before the
+        // current block's stores (the columns are distinct, but the compiler cannot know that).
+        constexpr int QF = 2;
+        const int pairs = (m - r) >> 1;
+        const int blocks = pairs / QF;
+        if (blocks > 0) {
+          T cu[2 * QF], cv[2 * QF], cp[2 * QF];
+#pragma unroll
+          for (int u = 0; u < 2 * QF; ++u) {
+            cu[u] = cj[r + u];
+            cv[u] = ck[r + u];
+            cp[u] = upd ? pv[r + u] : T{};
+          }
+          for (int blk = 0; blk < blocks; ++blk) {
+            T nu[2 * QF], nv[2 * QF], np[2 * QF];
+            const bool more = blk + 1 < blocks;
+            if (more) {
+#pragma unroll
+              for (int u = 0; u < 2 * QF; ++u) {
+                nu[u] = cj[r + 2 * QF + u];
+                nv[u] = ck[r + 2 * QF + u];
+                np[u] = upd ? pv[r + 2 * QF + u] : T{};
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 2 * QF; ++u) {
+              if (upd) {
+                cu[u] = A::muladd(cu[u], cp[u], sp);
+                cj[r + u] = cu[u];
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < QF; ++u)
+              d = A::pair(d, cv[2 * u], cu[2 * u], cv[2 * u + 1], cu[2 * u + 1]);
+            r += 2 * QF;
+            if (more) {
+#pragma unroll
+              for (int u = 0; u < 2 * QF; ++u) {
+                cu[u] = nu[u];
+                cv[u] = nv[u];
+                cp[u] = np[u];
+              }
+            }
+          }
+        }
         for (; r < m; r += 2) {
           T u0 = cj[r], u1 = cj[r + 1];
           if (upd) {
