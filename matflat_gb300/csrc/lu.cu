@@ -82,24 +82,11 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
   if (__shfl_sync(FULL_MASK, first_nan ? 1 : 0, 0)) p = c;
   __syncwarp();
   if (p != c && p < m) {
-    for (int col0 = lane; col0 < n; col0 += 32 * 2) {
-      T tc[2], tp[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int col = col0 + 32 * u;
-        if (col < n) {
-          tc[u] = a[(long long)col * lda + c];
-          tp[u] = a[(long long)col * lda + p];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int col = col0 + 32 * u;
-        if (col < n) {
-          a[(long long)col * lda + c] = tp[u];
-          a[(long long)col * lda + p] = tc[u];
-        }
-      }
+    for (int col = lane; col < n; col += 32) {
+      T* base = a + (long long)col * lda;
+      const T t = base[c];
+      base[c] = base[p];
+      base[p] = t;
     }
     if (lane == 0) {
       const int t = piv[c];
@@ -111,15 +98,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
   __syncwarp();
   const T diag = cc[c];
   if (Tr::nz(diag)) {
-    for (int i0 = c + 1 + lane; i0 < m; i0 += 32 * 2) {
-      T v[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-        if (i0 + 32 * u < m) v[u] = cc[i0 + 32 * u];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-        if (i0 + 32 * u < m) cc[i0 + 32 * u] = Tr::div(v[u], diag);
-    }
+    for (int i = c + 1 + lane; i < m; i += 32) cc[i] = Tr::div(cc[i], diag);
   } else if (info == 0) {
     info = c + 1;
   }
