@@ -60,7 +60,7 @@ enum mfg_status {
   MFG_ERR_INPLACE = -1003,     /* MulMatMat: a == c or b == c ("In-place operation is not
                                   supported.", Blas.MulMatMat.cs:301-304) */
   MFG_ERR_TIMEOUT = -1004,     /* a bounded device-side wait gave up (see mfg_plan_status) */
-  MFG_ERR_UNSUPPORTED = -1005  /* size or option outside what this build supports */
+  MFG_ERR_UNSUPPORTED = -1005  /* size or option outside what the library supports */
 };
 
 typedef struct mfg_ctx mfg_ctx;
