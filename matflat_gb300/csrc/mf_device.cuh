@@ -21,19 +21,36 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // Same tree, float data widened to double (Internals.cs:236-263).  Products of two widened
 // floats are exact in double.
+// (double)x * (double)y on the integer pipes.  The product of two floats' 24-bit significands
+// has at most 48 bits, so the widened product is exact in double: for normal x and y it is the
+// integer product Mx * My (one 32x32->64 multiply) placed under the exponent
+// ex + ey + t + 769 (t = 1 when the product reaches 2^47), with no rounding at all.  Zeros,
+// subnormals, infinities and NaN take the FP64 multiply, which gives the same value for them.
+__device__ __forceinline__ double fmul_wide(float x, float y) {
+  const unsigned X = __float_as_uint(x), Y = __float_as_uint(y);
+  const unsigned ex = (X >> 23) & 0xFFu, ey = (Y >> 23) & 0xFFu;
+  if (ex - 1u >= 254u || ey - 1u >= 254u) return __dmul_rn((double)x, (double)y);
+  const unsigned long long P =
+      (unsigned long long)((X & 0x7FFFFFu) | 0x800000u) * ((Y & 0x7FFFFFu) | 0x800000u);
+  const unsigned t = (unsigned)(P >> 47);
+  const unsigned long long mant = (P << (6u - t)) & 0x000FFFFFFFFFFFFFull;
+  const unsigned long long e = (unsigned long long)(ex + ey + t + 769u);
+  return __longlong_as_double((long long)(((unsigned long long)((X ^ Y) & 0x80000000u) << 32) |
+                                          (e << 52) | mant));
+}
+
 __device__ __forceinline__ double exact_dot_f(int len, const float* x, long long incx,
                                               const float* y, long long incy) {
   double s = 0.0;
   if (len & 1) {
-    s = __dmul_rn((double)x[0], (double)y[0]);
+    s = fmul_wide(x[0], y[0]);
     x += incx;
     y += incy;
   }
   const int pairs = len >> 1;
 #pragma unroll 4
   for (int p = 0; p < pairs; ++p) {
-    const double q = __dadd_rn(__dmul_rn((double)x[0], (double)y[0]),
-                               __dmul_rn((double)x[incx], (double)y[incy]));
+    const double q = __dadd_rn(fmul_wide(x[0], y[0]), fmul_wide(x[incx], y[incy]));
     s = __dadd_rn(s, q);
     x += 2 * incx;
     y += 2 * incy;

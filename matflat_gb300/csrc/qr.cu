@@ -118,12 +118,9 @@ struct QrArith<float> {
     return __fadd_rn(q, __fmul_rn(a, s));
   }
   static __device__ __forceinline__ float rdiag_elem(float r) { return r; }
-  static __device__ __forceinline__ double prod(float x, float y) {
-    return __dmul_rn((double)x, (double)y);
-  }
+  static __device__ __forceinline__ double prod(float x, float y) { return fmul_wide(x, y); }
   static __device__ __forceinline__ double pair(double s, float x0, float y0, float x1, float y1) {
-    return __dadd_rn(s, __dadd_rn(__dmul_rn((double)x0, (double)y0),
-                                  __dmul_rn((double)x1, (double)y1)));
+    return __dadd_rn(s, __dadd_rn(fmul_wide(x0, y0), fmul_wide(x1, y1)));
   }
 };
 
