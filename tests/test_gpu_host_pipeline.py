@@ -105,14 +105,15 @@ def test_host_pipeline_other_operations(mf):
     lp = mf.LuBatch(lu["n"], lu["a_off"], lu["piv_off"])
     fa = _dev(lu["a"])
     fp = torch.zeros(lu["piv_total"], dtype=torch.int32, device="cuda")
-    lp.run(fa, fp, None, torch.zeros(count, dtype=torch.int32, device="cuda"),
-           torch.zeros(count, dtype=torch.int32, device="cuda"))
+    fs = torch.zeros(count, dtype=torch.int32, device="cuda")
+    fi = torch.zeros(count, dtype=torch.int32, device="cuda")
+    lp.run(fa, fp, None, fs, fi)
     mf.context().synchronize()
     fac, piv = _host(fa), _host(fp)
     ip = mf.LuInverseBatch(lu["n"], lu["a_off"], lu["piv_off"])
-    ia = _dev(fac)
+    ia, ipv = _dev(fac), _dev(piv)
     iinf = torch.zeros(count, dtype=torch.int32, device="cuda")
-    ip.run(ia, _dev(piv), iinf)
+    ip.run(ia, ipv, iinf)
     ha, hinf = _pinned(fac), _pinned(np.zeros(count, np.int32))
     ip.run_host(ha, _pinned(piv), hinf)
     assert_bits(ha.numpy(), _host(ia))

@@ -192,8 +192,8 @@ def test_lu_inverse_batched_types(mf, dt):
     od = d.copy()
     oinfo = np.zeros(len(n), np.int32)
     oracle.lu_inverse_batched(n, a_off, od, piv_off, dp, oinfo, 4)
-    dd = _dev(d)
-    batch.run(dd, _dev(dp), dinfo)
+    dd, ddp = _dev(d), _dev(dp)
+    batch.run(dd, ddp, dinfo)
     mf.context().synchronize()
     assert_bits(_host(dd), od)
     batch.close()

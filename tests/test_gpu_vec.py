@@ -25,8 +25,8 @@ def test_gemv_strided(mf, trans):
     exp = y0.copy()
     for b in range(count):
         oracle.gemv(trans, m, n, a[b * sa:], lda, x[b * sx:], incx, exp[b * sy:], incy)
-    dy = _dev(y0)
-    mf.StridedBlas.MulMatVec(trans, m, n, _dev(a), lda, sa, _dev(x), incx, sx, dy, incy, sy, count)
+    dy, da, dx = _dev(y0), _dev(a), _dev(x)   # kept alive until the stream is synchronised
+    mf.StridedBlas.MulMatVec(trans, m, n, da, lda, sa, dx, incx, sx, dy, incy, sy, count)
     mf.context().synchronize()
     assert_bits(_host(dy), exp)
 
@@ -40,9 +40,10 @@ def test_dot_nrm2_strided(mf):
         x = rng.standard_normal(s * count)
         y = rng.standard_normal(s * count)
         d_out = torch.zeros(count, dtype=torch.float64, device="cuda")
-        mf.StridedBlas.Dot(n, _dev(x), inc, s, _dev(y), inc, s, d_out, count)
+        dx, dy = _dev(x), _dev(y)
+        mf.StridedBlas.Dot(n, dx, inc, s, dy, inc, s, d_out, count)
         n_out = torch.zeros(count, dtype=torch.float64, device="cuda")
-        mf.StridedBlas.L2Norm(n, _dev(x), inc, s, n_out, count)
+        mf.StridedBlas.L2Norm(n, dx, inc, s, n_out, count)
         mf.context().synchronize()
         ed = np.array([oracle.dot(n, x[b * s:], inc, y[b * s:], inc) for b in range(count)])
         en = np.array([oracle.nrm2(n, x[b * s:], inc) for b in range(count)])
@@ -60,8 +61,8 @@ def test_ger_strided(mf):
     exp = a0.copy()
     for b in range(count):
         oracle.ger(m, n, x[b * sx:], 2, y[b * sy:], 1, exp[b * sa:], lda)
-    da = _dev(a0)
-    mf.StridedBlas.Outer(m, n, _dev(x), 2, sx, _dev(y), 1, sy, da, lda, sa, count)
+    da, dx, dy = _dev(a0), _dev(x), _dev(y)
+    mf.StridedBlas.Outer(m, n, dx, 2, sx, dy, 1, sy, da, lda, sa, count)
     mf.context().synchronize()
     assert_bits(_host(da), exp)
 
@@ -101,9 +102,8 @@ def test_gemv_strided_types(mf, dt, trans):
         ey = exp[b * sy:]
         oracle.gemv(trans, m, n, a[b * sa:], lda, x[b * sx:], incx, ey, incy)
         exp[b * sy:] = ey
-    dy = _dev(y0)
-    mf.StridedBlas.MulMatVec(trans, m, n, _dev(a), lda, sa, _dev(x), incx, sx, dy, incy, sy,
-                             count)
+    dy, da, dx = _dev(y0), _dev(a), _dev(x)   # kept alive until the stream is synchronised
+    mf.StridedBlas.MulMatVec(trans, m, n, da, lda, sa, dx, incx, sx, dy, incy, sy, count)
     mf.context().synchronize()
     assert_bits(_flat(_host(dy)), _flat(exp))
 
@@ -118,10 +118,11 @@ def test_dot_nrm2_strided_types(mf, dt):
         s = n * inc + 7
         x, y = _draw(rng, s * count, dt), _draw(rng, s * count, dt)
         d_out = torch.zeros(count, dtype=rdt, device="cuda")
-        mf.StridedBlas.Dot(n, _dev(x), inc, s, _dev(y), inc, s, d_out, count)
+        dx, dy = _dev(x), _dev(y)
+        mf.StridedBlas.Dot(n, dx, inc, s, dy, inc, s, d_out, count)
         n_out = torch.zeros(count, dtype=torch.float32 if dt == np.float32 else torch.float64,
                             device="cuda")
-        mf.StridedBlas.L2Norm(n, _dev(x), inc, s, n_out, count)
+        mf.StridedBlas.L2Norm(n, dx, inc, s, n_out, count)
         mf.context().synchronize()
         ed = np.array([oracle.dot(n, x[b * s:], inc, y[b * s:], inc) for b in range(count)],
                       dtype=dt)
@@ -131,7 +132,7 @@ def test_dot_nrm2_strided_types(mf, dt):
         assert_bits(_host(n_out), en)
         if dt == np.complex128:
             c_out = torch.zeros(count, dtype=rdt, device="cuda")
-            mf.StridedBlas.DotConj(n, _dev(x), inc, s, _dev(y), inc, s, c_out, count)
+            mf.StridedBlas.DotConj(n, dx, inc, s, dy, inc, s, c_out, count)
             mf.context().synchronize()
             ec = np.array([oracle.dot(n, x[b * s:], inc, y[b * s:], inc, conj=True)
                            for b in range(count)])
@@ -149,8 +150,8 @@ def test_ger_strided_types(mf, dt, conj):
     for b in range(count):
         ea = exp[b * sa:]
         oracle.ger(m, n, x[b * sx:], 2, y[b * sy:], 1, ea, lda, conj=conj)
-    da = _dev(a0)
+    da, dx, dy = _dev(a0), _dev(x), _dev(y)
     fn = mf.StridedBlas.OuterConj if conj else mf.StridedBlas.Outer
-    fn(m, n, _dev(x), 2, sx, _dev(y), 1, sy, da, lda, sa, count)
+    fn(m, n, dx, 2, sx, dy, 1, sy, da, lda, sa, count)
     mf.context().synchronize()
     assert_bits(_flat(_host(da)), _flat(exp))
