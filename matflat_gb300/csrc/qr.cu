@@ -59,8 +59,9 @@ struct QrArith<double> {
   // s = -Dot(...) / colk[k]   (Qr.cs:163, :408)
   static __device__ __forceinline__ double coef(double d, double v0) { return __ddiv_rn(-d, v0); }
   // MulAdd: dst += x * s      (Internals.cs:49-73)
+  // The product on the integer pipes (imul_rn: the same correctly rounded value as DMUL).
   static __device__ __forceinline__ double muladd(double dst, double x, double s) {
-    return __dadd_rn(dst, __dmul_rn(x, s));
+    return __dadd_rn(dst, imul_rn(x, s));
   }
   static __device__ __forceinline__ double mulsub(double dst, double x, double s) {
     return __dsub_rn(dst, __dmul_rn(x, s));
