@@ -127,10 +127,9 @@ struct STraits {
                                             long long incy) {
     return exact_dot_f(len, x, incx, y, incy);
   }
-  static __device__ __forceinline__ Acc prod(T x, T y) { return __dmul_rn((double)x, (double)y); }
+  static __device__ __forceinline__ Acc prod(T x, T y) { return fmul_wide(x, y); }
   static __device__ __forceinline__ Acc pair(Acc s, T x0, T y0, T x1, T y1) {
-    return __dadd_rn(s, __dadd_rn(__dmul_rn((double)x0, (double)y0),
-                                  __dmul_rn((double)x1, (double)y1)));
+    return __dadd_rn(s, __dadd_rn(fmul_wide(x0, y0), fmul_wide(x1, y1)));
   }
   static __device__ __forceinline__ T fin(T a, Acc s) { return __fsub_rn(a, __double2float_rn(s)); }
   static __device__ __forceinline__ unsigned long long key(T v) { return pivot_key_f(v); }

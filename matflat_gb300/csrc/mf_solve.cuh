@@ -59,10 +59,10 @@ struct SSolve {
   using T = float;
   using Acc = double;
   static __device__ __forceinline__ Acc zero() { return 0.0; }
-  static __device__ __forceinline__ Acc prod(T a, T x) { return __dmul_rn((double)a, (double)x); }
+  // Widened float products are exact in double: formed on the integer pipes (fmul_wide).
+  static __device__ __forceinline__ Acc prod(T a, T x) { return fmul_wide(a, x); }
   static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
-    return __dadd_rn(s, __dadd_rn(__dmul_rn((double)a0, (double)x0),
-                                  __dmul_rn((double)a1, (double)x1)));
+    return __dadd_rn(s, __dadd_rn(fmul_wide(a0, x0), fmul_wide(a1, x1)));
   }
   static __device__ __forceinline__ T fin(T x, Acc s, T d, bool unit) {
     const double v = __dsub_rn((double)x, s);
