@@ -203,6 +203,10 @@ MFG_API int mfg_dgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, do
 MFG_API int mfg_sgeqrf_batched_host(mfg_plan* plan, float* a, float* rdiag, float* b);
 MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
                                          int* info);
+MFG_API int mfg_sgevd_front_batched_host(mfg_plan* plan, const float* a, float* b, float* c,
+                                         int* info);
+MFG_API int mfg_zgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
+                                         int* info);
 MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k, double* y,
                                                      double* loss, double* grad, int* info,
                                                      int keep_factor);
@@ -328,11 +332,21 @@ MFG_API int mfg_zgerc_strided_batched(mfg_ctx* ctx, int m, int n, const double* 
  * Pair i: A of order n[i] (<= 128) at a + a_off[i] (leading dimension lda[i], NULL: n), B at
  * b + b_off[i] (ldb[i]), C at c + c_off[i] (leading dimension n[i]).  info: 0, or k+1 when B is not
  * positive definite at column k (MatFlat throws "The right-hand side matrix is not positive
- * definite."; C is then unspecified). */
+ * definite."; B and C are then unspecified). */
 MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                         const int* lda, const int64_t* a_off, const int* ldb,
                                         const int64_t* b_off, const int64_t* c_off);
 MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
+                                    int* info);
+/* The float and Complex overloads on the same plan (GevdCore float, Factorization.Gevd.cs:282-318;
+ * Complex, :378-422, Complex as interleaved (re, im) doubles).  The float overload computes in
+ * float storage with double dots, as MatFlat's float Cholesky and SolveTriangular do.  The
+ * Complex one factors B = L L^H, fills C Hermitian from A's upper triangle (the diagonal taken as
+ * stored) and solves each row of C conjugated, conjugating the solution back, as MatFlat does:
+ * C = L^-1 A L^-H. */
+MFG_API int mfg_sgevd_front_batched(mfg_plan* plan, const float* a, float* b, float* c,
+                                    int* info);
+MFG_API int mfg_zgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
                                     int* info);
 
 /* Batched Factorization.LuInverse (Factorization.LuInverse.cs:123-199): replaces every matrix's

@@ -83,6 +83,8 @@ _SIGS = {
     "mfg_plan_gevd_front_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "mfg_dgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
+    "mfg_sgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
+    "mfg_zgevd_front_batched": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dgetrf_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dgetri_batched_host": (_I, [_vp, _vp, _vp, _vp]),
@@ -94,6 +96,8 @@ _SIGS = {
     "mfg_spotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_zpotrf_batched_host": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_dgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
+    "mfg_sgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
+    "mfg_zgevd_front_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_logdet_solve_grad_batched_host": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrs_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_sgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
@@ -642,8 +646,10 @@ class LuInverseBatch(_Batch):
 
 class GevdFrontBatch(_Batch):
     """Front half of Factorization.Gevd over a batch of pairs (A, B): B becomes its Cholesky factor
-    L and C = L^-1 A L^-T (leading dimension n) is written at c_off.  info per pair: 0, or k+1 when
-    B is not positive definite ("The right-hand side matrix is not positive definite.")."""
+    L and C = L^-1 A L^-T (L^-1 A L^-H for Complex; leading dimension n) is written at c_off.  info
+    per pair: 0, or k+1 when B is not positive definite ("The right-hand side matrix is not
+    positive definite.").  The double, float and Complex overloads share the plan; the overload
+    follows the arrays' element type, or `dtype` ("d", "s", "z") for Complex held as doubles."""
 
     def __init__(self, n, a_off, b_off, c_off, lda=None, ldb=None, ctx=None):
         ctx = ctx or context()
@@ -661,15 +667,16 @@ class GevdFrontBatch(_Batch):
         super().__init__(ctx, h)
         self.count = len(self._n)
 
-    def run(self, a, b, c, info):
-        rc = self.ctx.lib.mfg_dgevd_front_batched(self.h, _dptr(a), _dptr(b), _dptr(c), _dptr(info))
-        self.ctx.check(rc, "mfg_dgevd_front_batched")
+    def run(self, a, b, c, info, dtype=None):
+        name = "mfg_%sgevd_front_batched" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _dptr(a), _dptr(b), _dptr(c), _dptr(info))
+        self.ctx.check(rc, name)
 
-    def run_host(self, a, b, c, info):
+    def run_host(self, a, b, c, info, dtype=None):
         """The front half on host arrays, copies pipelined with compute.  Synchronous."""
-        rc = self.ctx.lib.mfg_dgevd_front_batched_host(self.h, _hptr(a), _hptr(b), _hptr(c),
-                                                       _hptr(info))
-        self.ctx.check(rc, "mfg_dgevd_front_batched_host")
+        name = "mfg_%sgevd_front_batched_host" % _elem(a, dtype)
+        rc = getattr(self.ctx.lib, name)(self.h, _hptr(a), _hptr(b), _hptr(c), _hptr(info))
+        self.ctx.check(rc, name)
 
 
 class CholeskyBatch(_Batch):

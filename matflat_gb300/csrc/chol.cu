@@ -878,10 +878,145 @@ static cudaError_t set_potrf_t_attrs() {
                               (int)potrf_t_smem<8, C>());
 }
 
+// Float and Complex overloads of the GEVD front half (Factorization.GevdCore, MatFlat/
+// Factorization.Gevd.cs:282-318 float, :378-422 Complex).  MatFlat solves every ROW of C in
+// place at stride n (the Complex overload conjugates the row first and conjugates the solution
+// back, :407-418), then every column.  Here the row pass runs as column solves on C^H: the fill
+// writes C^H (for the real types C itself, which is symmetric), the warp solves its columns
+// a few at a time in MatFlat's dot order (the stride does not change the arithmetic), an
+// in-place conjugate transpose turns the solutions back into rows, and the column pass solves
+// the columns of C directly.  One warp per pair; C is the solve's working storage and the dot
+// accumulators of gevd_rhs columns at a time sit in shared memory (9 KB per warp for either
+// type: three CTAs of eight warps per SM).
+constexpr int GEVD_T_WARPS = 8;
+
+__device__ __forceinline__ float gevd_conj(float v) { return v; }
+__device__ __forceinline__ zdouble gevd_conj(zdouble v) { return zconj(v); }
+
+template <int W>
+constexpr int gevd_rhs() {
+  return 8 / W;
+}
+template <int W>
+constexpr int gevd_t_warp_doubles() {
+  return GRAD_MAX_N + W * gevd_rhs<W>() * GRAD_MAX_N;
+}
+
+template <class C>
+__global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel(GevdArgs p) {
+  using T = typename C::T;
+  using Tr = typename C::Fwd;  // SolveTriangular(Lower, NoTrans): the dot form
+  using Acc = typename Tr::Acc;
+  constexpr int W = sizeof(Acc) / sizeof(double);
+  extern __shared__ double sm_gevd_t[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  double* dsum = sm_gevd_t + warp * gevd_t_warp_doubles<W>();
+  Acc* acc = reinterpret_cast<Acc*>(dsum + GRAD_MAX_N);
+  const T* abase = reinterpret_cast<const T*>(p.a);
+  T* bbase = reinterpret_cast<T*>(p.b);
+  T* cbase = reinterpret_cast<T*>(p.c);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(p.queue, 1);
+    idx = __shfl_sync(FULL_MASK, idx, 0);
+    if (idx >= p.count) break;
+    const int mat = p.order[idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    const long long ldb = p.ldb[mat];
+    const T* A = abase + p.a_off[mat];
+    T* B = bbase + p.b_off[mat];
+    T* Cm = cbase + p.c_off[mat];
+    const int info = C::factor(B, n, ldb, dsum);
+    if (info != 0) {
+      if (lane == 0) p.info[mat] = info;
+      __syncwarp();
+      continue;
+    }
+    // C(i,k) = A(i,k) for i < k, conj(A(k,i)) for i > k, A(i,i) on the diagonal
+    // (Gevd.cs:393-406); stored here is C^H(k,i) = conj(C(i,k)).
+    for (long long e = lane; e < (long long)n * n; e += 32) {
+      const int i = (int)(e / n);
+      const int k = (int)(e - (long long)i * n);
+      T v;
+      if (k < i)
+        v = A[(long long)i * lda + k];
+      else if (k > i)
+        v = gevd_conj(A[(long long)k * lda + i]);
+      else
+        v = gevd_conj(A[(long long)i * lda + i]);
+      Cm[e] = v;
+    }
+    __syncwarp();
+    for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
+      const int nr = min(gevd_rhs<W>(), n - c0);
+      warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
+    }
+    // Back to rows: C(i,k) = conj(C^H(k,i)).
+    for (long long e = lane; e < (long long)n * n; e += 32) {
+      const int j = (int)(e / n);
+      const int i = (int)(e - (long long)j * n);
+      if (i < j) {
+        const T lo = Cm[(long long)i * n + j];
+        const T up = Cm[e];
+        Cm[e] = gevd_conj(lo);
+        Cm[(long long)i * n + j] = gevd_conj(up);
+      } else if (i == j) {
+        Cm[e] = gevd_conj(Cm[e]);
+      }
+    }
+    __syncwarp();
+    for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
+      const int nr = min(gevd_rhs<W>(), n - c0);
+      warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
+    }
+    if (lane == 0) p.info[mat] = 0;
+    __syncwarp();
+  }
+}
+
+template <class C>
+static size_t gevd_t_smem() {
+  constexpr int W = sizeof(typename C::Fwd::Acc) / sizeof(double);
+  return sizeof(double) * gevd_t_warp_doubles<W>() * GEVD_T_WARPS;
+}
+
+cudaError_t launch_gevd_front_batched_t(const GevdArgs& args, int elem, int ctas,
+                                        cudaStream_t s) {
+  if (elem == 1)
+    gevd_front_batched_t_kernel<SChol><<<ctas, GEVD_T_WARPS * 32, gevd_t_smem<SChol>(), s>>>(args);
+  else
+    gevd_front_batched_t_kernel<ZChol><<<ctas, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>(), s>>>(args);
+  return cudaGetLastError();
+}
+
+int gevd_t_ctas_per_sm(int elem) {
+  int blocks = 0;
+  const cudaError_t e =
+      elem == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &blocks, gevd_front_batched_t_kernel<SChol>, GEVD_T_WARPS * 32,
+                      gevd_t_smem<SChol>())
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &blocks, gevd_front_batched_t_kernel<ZChol>, GEVD_T_WARPS * 32,
+                      gevd_t_smem<ZChol>());
+  if (e != cudaSuccess) return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int gevd_t_warps_per_cta() { return GEVD_T_WARPS; }
+
 cudaError_t init_potrf_t_attributes() {
   cudaError_t e = set_potrf_t_attrs<SChol>();
   if (e != cudaSuccess) return e;
-  return set_potrf_t_attrs<ZChol>();
+  e = set_potrf_t_attrs<ZChol>();
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gevd_t_smem<SChol>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)gevd_t_smem<ZChol>());
 }
 
 cudaError_t launch_spotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {

@@ -133,6 +133,10 @@ struct GevdArgs {
   int* queue;
 };
 cudaError_t launch_gevd_front_batched(const GevdArgs& args, int ctas, cudaStream_t s);
+// Float (elem 1) and Complex (elem 2) overloads: a, b and c point at float / interleaved Complex.
+cudaError_t launch_gevd_front_batched_t(const GevdArgs& args, int elem, int ctas, cudaStream_t s);
+int gevd_t_ctas_per_sm(int elem);
+int gevd_t_warps_per_cta();
 int gevd_max_n();
 int grad_ctas_per_sm();
 int grad_warps_per_cta();

@@ -106,7 +106,9 @@ struct mfg_plan {
   mfg::QrBatchArgs<double> qz{};  // GEQRF: the Complex overload (interleaved doubles)
   int qr_max_cols = 0;             // GEQRF: max over the batch of n + nrhs
   int qr_float = 0;  // GEQRF: which overload the next launch runs (0 double, 1 float, 2 Complex)
-  int elem = 0;      // GETRF/POTRF: element type of the next launch (0 double, 1 float, 2 Complex)
+  int elem = 0;      // GETRF/POTRF/GETRI/GEVD: element type of the next launch (0 double, 1 float,
+                     // 2 Complex)
+  int ctas_t = 0;    // GEVD: the grid of the float / Complex kernel
   long long dstride = 0;  // GETRF/POTRF: the double kernels' per-group scratch stride
   int mx_n = 0;      // MIXED: order of every matrix
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
@@ -339,6 +341,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_getri_batched_t(p->args, p->elem, p->ctas, s);
   else if (p->kind == mfg_plan::GETRI)
     e = mfg::launch_getri_batched(p->args, p->ctas, s);
+  else if (p->kind == mfg_plan::GEVD && p->elem != 0)
+    e = mfg::launch_gevd_front_batched_t(p->gv, p->elem, p->ctas_t, s);
   else if (p->kind == mfg_plan::GEVD)
     e = mfg::launch_gevd_front_batched(p->gv, p->ctas, s);
   else if (p->kind == mfg_plan::POTRF && p->elem == 1)
@@ -2010,8 +2014,9 @@ MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count
   return plan_create_gevd(ctx, plan, count, n, lda, a_off, ldb, b_off, c_off);
 }
 
-MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
-                                    int* info) {
+}  // extern "C"
+
+static int gevd_front_any(mfg_plan* plan, int elem, const void* a, void* b, void* c, int* info) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEVD) return fail(ctx, -1, "plan is not a gevd plan");
@@ -2021,11 +2026,28 @@ MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, 
     if (!c) return fail(ctx, -4, "c is null");
     if (!info) return fail(ctx, -5, "info is null");
   }
-  plan->gv.a = a;
-  plan->gv.b = b;
-  plan->gv.c = c;
+  const int rc = plan_set_elem(plan, elem);
+  if (rc != MFG_OK) return rc;
+  plan->gv.a = (const double*)a;
+  plan->gv.b = (double*)b;
+  plan->gv.c = (double*)c;
   plan->gv.info = info;
   return plan_execute(plan, a, b, c, info, nullptr);
+}
+
+extern "C" {
+
+MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
+                                    int* info) {
+  return gevd_front_any(plan, 0, a, b, c, info);
+}
+MFG_API int mfg_sgevd_front_batched(mfg_plan* plan, const float* a, float* b, float* c,
+                                    int* info) {
+  return gevd_front_any(plan, 1, a, b, c, info);
+}
+MFG_API int mfg_zgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
+                                    int* info) {
+  return gevd_front_any(plan, 2, a, b, c, info);
 }
 
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
@@ -2165,6 +2187,17 @@ namespace {
 int plan_set_elem(mfg_plan* p, int elem) {
   mfg_ctx* ctx = p->ctx;
   p->elem = elem;
+  if (p->kind == mfg_plan::GEVD) {
+    // The float / Complex kernel keeps its accumulators in shared memory: only its grid differs.
+    if (elem != 0 && p->ctas_t == 0) {
+      const long long w = mfg::gevd_t_warps_per_cta();
+      const long long ctas = std::min<long long>(
+          (long long)ctx->sm_count * std::min(mfg::gevd_t_ctas_per_sm(1), mfg::gevd_t_ctas_per_sm(2)),
+          ((long long)p->count + w - 1) / w);
+      p->ctas_t = (int)std::max<long long>(1, ctas);
+    }
+    return MFG_OK;
+  }
   long long stride = p->dstride;
   if (elem != 0 && p->kind == mfg_plan::GETRI) {
     // The float / Complex inverse keeps a copy of the factors per warp in global scratch.
@@ -2280,14 +2313,14 @@ namespace {
 // (stream d2h) overlap with the neighbouring chunks', so the copies hide behind the compute.
 enum PipeOp {
   OP_GETRF, OP_POTRF, OP_GRAD, OP_GETRI, OP_GEQRF_D, OP_GEQRF_S, OP_GEVD,
-  OP_GETRF_S, OP_GETRF_Z, OP_POTRF_S, OP_POTRF_Z, OP_GEQRF_Z
+  OP_GETRF_S, OP_GETRF_Z, OP_POTRF_S, OP_POTRF_Z, OP_GEQRF_Z, OP_GEVD_S, OP_GEVD_Z
 };
 
 // Element type of an operation's factor arrays: 0 double, 1 float, 2 Complex.
 int pipe_elem(int op) {
   switch (op) {
-    case OP_GETRF_S: case OP_POTRF_S: case OP_GEQRF_S: return 1;
-    case OP_GETRF_Z: case OP_POTRF_Z: case OP_GEQRF_Z: return 2;
+    case OP_GETRF_S: case OP_POTRF_S: case OP_GEQRF_S: case OP_GEVD_S: return 1;
+    case OP_GETRF_Z: case OP_POTRF_Z: case OP_GEQRF_Z: case OP_GEVD_Z: return 2;
     default: return 0;
   }
 }
@@ -2375,11 +2408,13 @@ void pipe_arrays(mfg_plan* p, int op, int keep_factor) {
       add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
           [&](int i) { return (size_t)p->hm[i] * nrhs; });
       break;
-    case OP_GEVD:  // a, b, c, info
-      add(1, 8, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
-      add(3, 8, [&](int i) { return (size_t)p->hboff[i]; },
+    case OP_GEVD:
+    case OP_GEVD_S:
+    case OP_GEVD_Z:  // a, b, c, info
+      add(1, es, [&](int i) { return (size_t)p->haoff[i]; }, aspan);
+      add(3, es, [&](int i) { return (size_t)p->hboff[i]; },
           [&](int i) { return span(p->hn[i], p->hn[i], p->hldb[i]); });
-      add(2, 8, [&](int i) { return (size_t)p->hcoff[i]; },
+      add(2, es, [&](int i) { return (size_t)p->hcoff[i]; },
           [&](int i) { return (size_t)p->hn[i] * p->hn[i]; });
       add(2, 4, self, one);
       break;
@@ -2498,6 +2533,10 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
       if (rc == MFG_OK) rc = plan_set_elem(sub, pipe_elem(op));
       if (rc != MFG_OK) return rc;
     }
+    if (p->kind == mfg_plan::GEVD) {
+      rc = plan_set_elem(sub, pipe_elem(op));
+      if (rc != MFG_OK) return rc;
+    }
     if (op == OP_GEQRF_Z) {
       rc = zqr_prepare(sub);
       if (rc != MFG_OK) return rc;
@@ -2611,6 +2650,8 @@ int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> 
         rc = plan_launch(sub, sc);
         break;
       case OP_GEVD:
+      case OP_GEVD_S:
+      case OP_GEVD_Z:
         sub->gv.a = (const double*)dev(0);
         sub->gv.b = (double*)dev(1);
         sub->gv.c = (double*)dev(2);
@@ -2766,8 +2807,10 @@ MFG_API int mfg_sgeqrf_batched_host(mfg_plan* plan, float* a, float* rdiag, floa
   return pipe_run(plan, OP_GEQRF_S, 0, {a, rdiag, b});
 }
 
-MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
-                                         int* info) {
+}  // extern "C"
+
+static int gevd_front_host_any(mfg_plan* plan, int op, const void* a, void* b, void* c,
+                               int* info) {
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEVD) return fail(ctx, -1, "plan is not a gevd plan");
@@ -2776,7 +2819,22 @@ MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double
   if (!b) return fail(ctx, -3, "b is null");
   if (!c) return fail(ctx, -4, "c is null");
   if (!info) return fail(ctx, -5, "info is null");
-  return pipe_run(plan, OP_GEVD, 0, {const_cast<double*>(a), b, c, info});
+  return pipe_run(plan, op, 0, {const_cast<void*>(a), b, c, info});
+}
+
+extern "C" {
+
+MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
+                                         int* info) {
+  return gevd_front_host_any(plan, OP_GEVD, a, b, c, info);
+}
+MFG_API int mfg_sgevd_front_batched_host(mfg_plan* plan, const float* a, float* b, float* c,
+                                         int* info) {
+  return gevd_front_host_any(plan, OP_GEVD_S, a, b, c, info);
+}
+MFG_API int mfg_zgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
+                                         int* info) {
+  return gevd_front_host_any(plan, OP_GEVD_Z, a, b, c, info);
 }
 
 }  // extern "C"

@@ -1153,6 +1153,50 @@ int orc_dgevd_front(int n, const double* a, int lda, double* b, int ldb, double*
   return 0;
 }
 
+// Float overload (Factorization.Gevd.cs:282-318): the same steps with float storage, through the
+// float Cholesky and SolveTriangular (double dots, float results).
+int orc_sgevd_front(int n, const float* a, int lda, float* b, int ldb, float* c) {
+  const int info = orc_scholesky(n, b, ldb);
+  if (info != 0) return info;
+  for (int j = 0; j < n; j++) {
+    const float* aColj = a + (long)lda * j;
+    for (int i = 0; i < j; i++) {
+      c[(long)n * j + i] = aColj[i];
+      c[(long)n * i + j] = aColj[i];
+    }
+    c[(long)n * j + j] = aColj[j];
+  }
+  for (int i = 0; i < n; i++) orc_strsv(LOWER, NOTRANS, n, b, ldb, c + i, n);
+  for (int i = 0; i < n; i++) orc_strsv(LOWER, NOTRANS, n, b, ldb, c + (long)n * i, 1);
+  return 0;
+}
+
+// Complex overload (Factorization.Gevd.cs:378-422): B = L L^H; C(i,j) = A(i,j) above the diagonal,
+// conj(A(j,i)) below it, A(j,j) on it (:393-406); each row of C is conjugated, solved at stride n
+// and conjugated back (:407-418); then every column is solved (:419-422).  Interleaved doubles.
+int orc_zgevd_front(int n, const double* a_, int lda, double* b_, int ldb, double* c_) {
+  const int info = orc_zcholesky(n, b_, ldb);
+  if (info != 0) return info;
+  const cplx* a = reinterpret_cast<const cplx*>(a_);
+  cplx* c = reinterpret_cast<cplx*>(c_);
+  for (int j = 0; j < n; j++) {
+    const cplx* aColj = a + (long)lda * j;
+    for (int i = 0; i < j; i++) {
+      c[(long)n * j + i] = aColj[i];
+      c[(long)n * i + j] = cconj(aColj[i]);
+    }
+    c[(long)n * j + j] = aColj[j];
+  }
+  for (int i = 0; i < n; i++) {
+    for (int k = 0; k < n; k++) c[(long)n * k + i] = cconj(c[(long)n * k + i]);
+    orc_ztrsv(LOWER, NOTRANS, n, b_, ldb, reinterpret_cast<double*>(c + i), n);
+    for (int k = 0; k < n; k++) c[(long)n * k + i] = cconj(c[(long)n * k + i]);
+  }
+  for (int i = 0; i < n; i++)
+    orc_ztrsv(LOWER, NOTRANS, n, b_, ldb, reinterpret_cast<double*>(c + (long)n * i), 1);
+  return 0;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Batched drivers over std::thread.  Matrices are packed: matrix i starts at a + a_off[i]
 // (elements), has order n[i] and leading dimension n[i]; vectors start at b + b_off[i].
@@ -1296,6 +1340,20 @@ void orc_dgevd_front_batched(long count, const int* n, const int64_t* a_off, con
                              const int64_t* b_off, double* b, double* c, int* info, int nthreads) {
   parallel_for(count, nthreads, [&](long i) {
     info[i] = orc_dgevd_front(n[i], a + a_off[i], n[i], b + b_off[i], n[i], c + a_off[i]);
+  });
+}
+void orc_sgevd_front_batched(long count, const int* n, const int64_t* a_off, const float* a,
+                             const int64_t* b_off, float* b, float* c, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    info[i] = orc_sgevd_front(n[i], a + a_off[i], n[i], b + b_off[i], n[i], c + a_off[i]);
+  });
+}
+// Complex: offsets in Complex elements, arrays as interleaved doubles.
+void orc_zgevd_front_batched(long count, const int* n, const int64_t* a_off, const double* a,
+                             const int64_t* b_off, double* b, double* c, int* info, int nthreads) {
+  parallel_for(count, nthreads, [&](long i) {
+    info[i] = orc_zgevd_front(n[i], a + 2 * a_off[i], n[i], b + 2 * b_off[i], n[i],
+                              c + 2 * a_off[i]);
   });
 }
 

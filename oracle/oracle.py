@@ -78,6 +78,10 @@ def lib():
             "orc_zger": (None, [_I, _I, _d, _I, _d, _I, _d, _I, _I]),
             "orc_dgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
             "orc_dgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
+            "orc_sgevd_front": (_I, [_I, _f, _I, _f, _I, _f]),
+            "orc_zgevd_front": (_I, [_I, _d, _I, _d, _I, _d]),
+            "orc_sgevd_front_batched": (None, [_L, _i, _l, _f, _l, _f, _f, _i, _I]),
+            "orc_zgevd_front_batched": (None, [_L, _i, _l, _d, _l, _d, _d, _i, _I]),
             "orc_dlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
             "orc_slu_inverse_batched": (None, [_L, _i, _l, _f, _l, _i, _i, _I]),
             "orc_zlu_inverse_batched": (None, [_L, _i, _l, _d, _l, _i, _i, _I]),
@@ -224,15 +228,16 @@ def lu_inverse_batched(n, a_off, a, piv_off, piv, info, nthreads=1):
 
 
 def gevd_front(n, a, lda, b, ldb, c):
-    """Factorization.GevdCore's front half (Factorization.Gevd.cs:330-365): B -> L, C = L^-1 A L^-T
-    (leading dimension n); returns 0 or Cholesky's k+1."""
-    return lib().orc_dgevd_front(n, _fp(a), lda, _fp(b), ldb, _fp(c))
+    """Factorization.GevdCore's front half (Factorization.Gevd.cs:330-365 double, :282-318 float,
+    :378-422 Complex): B -> L, C = L^-1 A L^-T (L^-H for Complex; leading dimension n); returns 0
+    or Cholesky's k+1.  The overload follows a's dtype."""
+    return getattr(lib(), "orc_%sgevd_front" % _pre(a))(n, _fp(a), lda, _fp(b), ldb, _fp(c))
 
 
 def gevd_front_batched(n, a_off, a, b_off, b, c, info, nthreads=1):
-    lib().orc_dgevd_front_batched(len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
-                                  _p(b_off, ctypes.c_int64), _fp(b), _fp(c),
-                                  _p(info, ctypes.c_int), nthreads)
+    getattr(lib(), "orc_%sgevd_front_batched" % _pre(a))(
+        len(n), _p(n, ctypes.c_int), _p(a_off, ctypes.c_int64), _fp(a),
+        _p(b_off, ctypes.c_int64), _fp(b), _fp(c), _p(info, ctypes.c_int), nthreads)
 
 
 def qr_ls_batched(m, n, a_off, a, b_off, b, x_off, x, nthreads=1):
