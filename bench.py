@@ -39,6 +39,13 @@ CONFIGS = {
                           "(Factorization.Gevd up to its eigen-solver): B = L L^T, C = L^-1 A L^-T, "
                           "10,000 pairs n=64, A = S + S^T, B = M M^T + 64 I, S, M ~ N(0,1), seed 0",
                  count=10_000, n=64),
+    "gevd32": dict(workload="batched GEVD front half, MatFlat's float overload (float storage, "
+                            "double dots): the gevd pairs (10,000, n=64, seed 0) rounded to float",
+                   count=10_000, n=64, dtype="f32"),
+    "gevdz": dict(workload="batched GEVD front half, MatFlat's Complex overload: B = L L^H, "
+                           "C = L^-1 A L^-H, 10,000 pairs n=64, A = S + S^T + i (T - T^T), "
+                           "B = M M^T + 64 I + 0.05 i (K - K^T), S, T, M, K ~ N(0,1), seed 0",
+                  count=10_000, n=64, dtype="c128"),
     "chol": dict(workload="batched FP64 Cholesky (MatFlat order) + L and L^T solves, "
                           "10,000 SPD matrices n=32, A=B*B^T+32*I, B~N(0,1), 1 RHS, seed 0",
                  count=10_000, n=32, nrhs=1),
@@ -89,16 +96,17 @@ def inv_bytes(n):
     return float(np.sum(16 * n ** 2 + 4 * n))
 
 
-def gevd_flops(n):
-    """Cholesky of B (n^3/3) plus two passes of n triangular solves (n^3 each)."""
+def gevd_flops(n, cplx=False):
+    """Cholesky of B (n^3/3) plus two passes of n triangular solves (n^3 each); a Complex
+    multiply-add is four real ones."""
     n = n.astype(np.float64)
-    return float(np.sum(n ** 3 / 3 + 2 * n ** 3))
+    return float(np.sum(n ** 3 / 3 + 2 * n ** 3)) * (4 if cplx else 1)
 
 
-def gevd_bytes(n):
-    """Read A and B, write L and C."""
+def gevd_bytes(n, es=8):
+    """Read A and B, write L and C (es bytes per element)."""
     n = n.astype(np.float64)
-    return float(np.sum(32 * n ** 2))
+    return float(np.sum(4 * es * n ** 2))
 
 
 def chol_flops(n, nrhs):
@@ -257,8 +265,8 @@ def make_inputs(cfg_name, rank):
                                       seed=rank)
     if cfg_name == "grad":
         return synth.rbf_batch(cfg["count"], cfg["n"], seed=rank)
-    if cfg_name == "gevd":
-        return synth.gevd_batch(cfg["count"], cfg["n"], seed=rank)
+    if cfg_name.startswith("gevd"):
+        return synth.gevd_batch(cfg["count"], cfg["n"], seed=rank, dtype=cfg.get("dtype", "f64"))
     return synth.qr_batch(cfg["count"], seed=rank)
 
 
@@ -287,7 +295,7 @@ def cpu_sample_rate(cfg_name, d, budget_s=15.0, threads=None):
 
 
 def run_cpu_sample(cfg_name, d, sample, threads, oracle):
-    if cfg_name == "gevd":
+    if cfg_name.startswith("gevd"):
         n = d["n"][sample].astype(np.int32)
         sz = n.astype(np.int64) ** 2
         off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
@@ -398,6 +406,8 @@ def metric_name(cfg_name):
     return {"mixed": "mixed-precision LU+IR solves/s at 1e-12 backward error","lu": "batched FP64 LU+solve matrices/s (MatFlat-exact pivots)",
             "inv": "batched FP64 LuInverse matrices/s (MatFlat-exact)",
             "gevd": "batched FP64 GEVD front half (Cholesky + C = L^-1 A L^-T) pairs/s (MatFlat-exact)",
+            "gevd32": "batched FP32 GEVD front half (Cholesky + C = L^-1 A L^-T) pairs/s (MatFlat-exact)",
+            "gevdz": "batched Complex GEVD front half (Cholesky + C = L^-1 A L^-H) pairs/s (MatFlat-exact)",
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "chol100k": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
@@ -406,7 +416,7 @@ def metric_name(cfg_name):
 
 
 def dtype_name(cfg_name):
-    return "f32" if cfg_name == "qr32" else "f64"
+    return {"qr32": "f32", "gevd32": "f32", "gevdz": "complex128"}.get(cfg_name, "f64")
 
 
 def run_mixed(args, torch, mf, world, rank, local):
@@ -656,16 +666,18 @@ def main():
         a = torch.empty_like(a0)
         b = torch.empty_like(b0)
         info = torch.zeros(count, dtype=torch.int32, device="cuda")
-        if cfg_name == "gevd":
+        if cfg_name.startswith("gevd"):
             plan = mf.GevdFrontBatch(d["n"], d["a_off"], d["b_off"], d["a_off"])
             cmat = torch.empty_like(a0)
 
             def run():
                 plan.run(a, b, cmat, info)
             outs = [b, cmat, info]
-            flops = gevd_flops(d["n"])
-            byts = gevd_bytes(d["n"])
-            kernel_key = "gevd_front_batched_kernel"
+            flops = gevd_flops(d["n"], cplx=cfg_name == "gevdz")
+            byts = gevd_bytes(d["n"], a0.element_size())
+            kernel_key = {"gevd": "gevd_front_batched_kernel",
+                          "gevd32": "gevd_front_batched_t_kernel_f32",
+                          "gevdz": "gevd_front_batched_t_kernel_c128"}[cfg_name]
         elif cfg_name == "inv":
             # Factor once, untimed; the pivots travel as the step's second input.
             piv0 = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
@@ -803,7 +815,7 @@ def main():
                                                    keep_factor=True)
             up = [io[0], io[1]]
             down = [io[0], io[1]] + extra
-        elif cfg_name == "gevd":
+        elif cfg_name.startswith("gevd"):
             extra = [pinned_like(a_host), torch.zeros(count, dtype=torch.int32).pin_memory()]
             io[0] = a_host                           # A: read only
             call = lambda: plan.run_host(io[0], io[1], extra[0], extra[1])

@@ -12,6 +12,8 @@
 // are bit-identical.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
@@ -881,13 +883,17 @@ static cudaError_t set_potrf_t_attrs() {
 // Float and Complex overloads of the GEVD front half (Factorization.GevdCore, MatFlat/
 // Factorization.Gevd.cs:282-318 float, :378-422 Complex).  MatFlat solves every ROW of C in
 // place at stride n (the Complex overload conjugates the row first and conjugates the solution
-// back, :407-418), then every column.  Here the row pass runs as column solves on C^H: the fill
-// writes C^H (for the real types C itself, which is symmetric), the warp solves its columns
-// a few at a time in MatFlat's dot order (the stride does not change the arithmetic), an
-// in-place conjugate transpose turns the solutions back into rows, and the column pass solves
-// the columns of C directly.  One warp per pair; C is the solve's working storage and the dot
-// accumulators of gevd_rhs columns at a time sit in shared memory (9 KB per warp for either
-// type: three CTAs of eight warps per SM).
+// back, :407-418), then every column.  The kernel runs both passes as row solves, one lane per
+// row, so that a warp's loads of the rows' entries are coalesced:
+//   D = conj(C)            the fill (for the real types C itself, which is symmetric)
+//   D <- rows of D solved  MatFlat's row pass, before its conjugation back
+//   E = D^H                row c of E is column c of MatFlat's C after the row pass
+//   E <- rows of E solved  MatFlat's column pass
+//   C = E^T
+// Each row solve is SolveTriangular(Lower, NoTrans) in MatFlat's dot order (the stride does not
+// change the arithmetic), with the rows of L staged in shared memory one ahead of use.  One warp
+// per pair.  MFG_GEVD_LANES=0 selects the earlier form of the same passes, column solves of
+// warp_solve_dot with the accumulators of a few columns in shared memory.
 constexpr int GEVD_T_WARPS = 8;
 
 __device__ __forceinline__ float gevd_conj(float v) { return v; }
@@ -897,12 +903,111 @@ template <int W>
 constexpr int gevd_rhs() {
   return 8 / W;
 }
+// Per-warp shared memory in doubles: the Cholesky sums, then the staged rows of L (lanes form)
+// or the dot accumulators (warp_solve_dot form).
 template <int W>
 constexpr int gevd_t_warp_doubles() {
   return GRAD_MAX_N + W * gevd_rhs<W>() * GRAD_MAX_N;
 }
 
-template <class C>
+// Copies src[k*stride] to dst[k] (shared memory) for k in [k0, k1) asynchronously, in 4-byte
+// (float) or 8-byte (Complex: two per element) pieces, which the arrays' alignment allows.
+template <class T>
+__device__ __forceinline__ void stage_async_t(T* dst, const T* src, int k0, int k1,
+                                              long long stride) {
+  const int lane = threadIdx.x & 31;
+  if constexpr (sizeof(T) == 4) {
+    for (int k = k0 + lane; k < k1; k += 32) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(dst + k);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src + k * stride)
+                   : "memory");
+    }
+  } else {
+    constexpr int P = sizeof(T) / 8;
+    for (int q = lane; q < (k1 - k0) * P; q += 32) {
+      const int k = k0 + q / P;
+      const int h = q - (q / P) * P;
+      const unsigned d =
+          (unsigned)__cvta_generic_to_shared(reinterpret_cast<double*>(dst + k) + h);
+      const double* sp = reinterpret_cast<const double*>(src + k * stride) + h;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(sp) : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Every row of the n-by-n matrix M (leading dimension n) solved in place with the lower factor
+// L (leading dimension ld): x_i = (x_i - Dot(i, L(i,:), x)) / L(i,i), one lane per row.
+// vb: 2n elements of shared memory.
+template <class Tr>
+__device__ void gevd_rows_solve(const typename Tr::T* L, int n, long long ld, typename Tr::T* M,
+                                typename Tr::T* vb) {
+  using T = typename Tr::T;
+  using Acc = typename Tr::Acc;
+  const int lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const bool active = r0 + lane < n;
+    T* x = M + r0 + (active ? lane : 0);
+    stage_async_t(vb, L, 0, 1, ld);
+    stage_wait();
+    for (int i = 0; i < n; i++) {
+      const T* li = vb + (i & 1) * n;
+      if (i + 1 < n) stage_async_t(vb + ((i + 1) & 1) * n, L + i + 1, 0, i + 2, ld);
+      if (active) {
+        const T v = x[(long long)i * n];
+        T out;
+        if (i == 0) {
+          out = Tr::fin0(v, li[0], false);
+        } else {
+          Acc s = Tr::zero();
+          int k = 0;
+          if (i & 1) {
+            s = Tr::prod(li[0], x[0]);
+            k = 1;
+          }
+          for (; k + 8 <= i; k += 8) {
+            T l8[8], v8[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+              l8[r] = li[k + r];
+              v8[r] = x[(long long)(k + r) * n];
+            }
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+              s = Tr::pair(s, l8[2 * r], v8[2 * r], l8[2 * r + 1], v8[2 * r + 1]);
+          }
+          for (; k < i; k += 2)
+            s = Tr::pair(s, li[k], x[(long long)k * n], li[k + 1], x[(long long)(k + 1) * n]);
+          out = Tr::fin(v, s, li[i], false);
+        }
+        x[(long long)i * n] = out;
+      }
+      stage_wait();
+    }
+  }
+}
+
+// M <- M^H (CONJ) or M^T in place (n-by-n, leading dimension n).
+template <bool CONJ, class T>
+__device__ void gevd_transpose(T* M, int n) {
+  const int lane = threadIdx.x & 31;
+  auto cj = [](T v) { return CONJ ? gevd_conj(v) : v; };
+  for (long long e = lane; e < (long long)n * n; e += 32) {
+    const int j = (int)(e / n);
+    const int i = (int)(e - (long long)j * n);
+    if (i < j) {
+      const T lo = M[(long long)i * n + j];
+      const T up = M[e];
+      M[e] = cj(lo);
+      M[(long long)i * n + j] = cj(up);
+    } else if (i == j && CONJ) {
+      M[e] = cj(M[e]);
+    }
+  }
+  __syncwarp();
+}
+
+template <class C, bool LANES>
 __global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel(GevdArgs p) {
   using T = typename C::T;
   using Tr = typename C::Fwd;  // SolveTriangular(Lower, NoTrans): the dot form
@@ -913,6 +1018,7 @@ __global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel
   const int lane = threadIdx.x & 31;
   double* dsum = sm_gevd_t + warp * gevd_t_warp_doubles<W>();
   Acc* acc = reinterpret_cast<Acc*>(dsum + GRAD_MAX_N);
+  T* vb = reinterpret_cast<T*>(dsum + GRAD_MAX_N);
   const T* abase = reinterpret_cast<const T*>(p.a);
   T* bbase = reinterpret_cast<T*>(p.b);
   T* cbase = reinterpret_cast<T*>(p.c);
@@ -934,42 +1040,39 @@ __global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel
       __syncwarp();
       continue;
     }
-    // C(i,k) = A(i,k) for i < k, conj(A(k,i)) for i > k, A(i,i) on the diagonal
-    // (Gevd.cs:393-406); stored here is C^H(k,i) = conj(C(i,k)).
-    for (long long e = lane; e < (long long)n * n; e += 32) {
-      const int i = (int)(e / n);
-      const int k = (int)(e - (long long)i * n);
-      T v;
-      if (k < i)
-        v = A[(long long)i * lda + k];
-      else if (k > i)
-        v = gevd_conj(A[(long long)k * lda + i]);
-      else
-        v = gevd_conj(A[(long long)i * lda + i]);
-      Cm[e] = v;
-    }
-    __syncwarp();
-    for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
-      const int nr = min(gevd_rhs<W>(), n - c0);
-      warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
-    }
-    // Back to rows: C(i,k) = conj(C^H(k,i)).
+    // MatFlat's C (Gevd.cs:393-406): C(i,k) = A(i,k) for i < k, conj(A(k,i)) for i > k, A(i,i)
+    // on the diagonal.  Stored: D = conj(C) (lanes form) or C^H (warp_solve_dot form).
     for (long long e = lane; e < (long long)n * n; e += 32) {
       const int j = (int)(e / n);
       const int i = (int)(e - (long long)j * n);
-      if (i < j) {
-        const T lo = Cm[(long long)i * n + j];
-        const T up = Cm[e];
-        Cm[e] = gevd_conj(lo);
-        Cm[(long long)i * n + j] = gevd_conj(up);
-      } else if (i == j) {
-        Cm[e] = gevd_conj(Cm[e]);
-      }
+      // element (i, j) of the stored matrix, from row r, column c of C, conjugated
+      const int r = LANES ? i : j;
+      const int c = LANES ? j : i;
+      T v;
+      if (r < c)
+        v = gevd_conj(A[(long long)c * lda + r]);
+      else if (r > c)
+        v = A[(long long)r * lda + c];
+      else
+        v = gevd_conj(A[(long long)r * lda + r]);
+      Cm[e] = v;
     }
     __syncwarp();
-    for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
-      const int nr = min(gevd_rhs<W>(), n - c0);
-      warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
+    if constexpr (LANES) {
+      gevd_rows_solve<Tr>(B, n, ldb, Cm, vb);
+      gevd_transpose<true>(Cm, n);
+      gevd_rows_solve<Tr>(B, n, ldb, Cm, vb);
+      gevd_transpose<false>(Cm, n);
+    } else {
+      for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
+        const int nr = min(gevd_rhs<W>(), n - c0);
+        warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
+      }
+      gevd_transpose<true>(Cm, n);   // back to rows: C(i,k) = conj(C^H(k,i))
+      for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
+        const int nr = min(gevd_rhs<W>(), n - c0);
+        warp_solve_dot<32, Tr>(B, n, 1, ldb, false, Cm + (long long)c0 * n, n, acc, nr);
+      }
     }
     if (lane == 0) p.info[mat] = 0;
     __syncwarp();
@@ -982,26 +1085,46 @@ static size_t gevd_t_smem() {
   return sizeof(double) * gevd_t_warp_doubles<W>() * GEVD_T_WARPS;
 }
 
+static bool gevd_lanes() {
+  static const bool on = [] {
+    const char* v = std::getenv("MFG_GEVD_LANES");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 cudaError_t launch_gevd_front_batched_t(const GevdArgs& args, int elem, int ctas,
                                         cudaStream_t s) {
-  if (elem == 1)
-    gevd_front_batched_t_kernel<SChol><<<ctas, GEVD_T_WARPS * 32, gevd_t_smem<SChol>(), s>>>(args);
+  const dim3 blk(GEVD_T_WARPS * 32);
+  if (elem == 1 && gevd_lanes())
+    gevd_front_batched_t_kernel<SChol, true><<<ctas, blk, gevd_t_smem<SChol>(), s>>>(args);
+  else if (elem == 1)
+    gevd_front_batched_t_kernel<SChol, false><<<ctas, blk, gevd_t_smem<SChol>(), s>>>(args);
+  else if (gevd_lanes())
+    gevd_front_batched_t_kernel<ZChol, true><<<ctas, blk, gevd_t_smem<ZChol>(), s>>>(args);
   else
-    gevd_front_batched_t_kernel<ZChol><<<ctas, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>(), s>>>(args);
+    gevd_front_batched_t_kernel<ZChol, false><<<ctas, blk, gevd_t_smem<ZChol>(), s>>>(args);
   return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the float / Complex kernels (the smaller of the two forms).
 int gevd_t_ctas_per_sm(int elem) {
-  int blocks = 0;
-  const cudaError_t e =
-      elem == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                      &blocks, gevd_front_batched_t_kernel<SChol>, GEVD_T_WARPS * 32,
-                      gevd_t_smem<SChol>())
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                      &blocks, gevd_front_batched_t_kernel<ZChol>, GEVD_T_WARPS * 32,
-                      gevd_t_smem<ZChol>());
-  if (e != cudaSuccess) return 1;
-  return blocks < 1 ? 1 : blocks;
+  int b0 = 0, b1 = 0;
+  cudaError_t e0, e1;
+  if (elem == 1) {
+    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b0, gevd_front_batched_t_kernel<SChol, true>, GEVD_T_WARPS * 32, gevd_t_smem<SChol>());
+    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b1, gevd_front_batched_t_kernel<SChol, false>, GEVD_T_WARPS * 32, gevd_t_smem<SChol>());
+  } else {
+    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b0, gevd_front_batched_t_kernel<ZChol, true>, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>());
+    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b1, gevd_front_batched_t_kernel<ZChol, false>, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>());
+  }
+  if (e0 != cudaSuccess || e1 != cudaSuccess) return 1;
+  const int b = b0 < b1 ? b0 : b1;
+  return b < 1 ? 1 : b;
 }
 
 int gevd_t_warps_per_cta() { return GEVD_T_WARPS; }
@@ -1011,12 +1134,18 @@ cudaError_t init_potrf_t_attributes() {
   if (e != cudaSuccess) return e;
   e = set_potrf_t_attrs<ZChol>();
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gevd_t_smem<SChol>());
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)gevd_t_smem<ZChol>());
+  const int ss = (int)gevd_t_smem<SChol>(), zs = (int)gevd_t_smem<ZChol>();
+  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, ss)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, ss)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, zs)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, zs);
 }
 
 cudaError_t launch_spotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {

@@ -103,16 +103,28 @@ def spd_batch_uneven(count, nmin=8, nmax=128, nrhs=1, seed=0):
     return dict(n=ns, a_off=a_off, a=a, b_off=b_off, b=b, nrhs=nrhs)
 
 
-def gevd_batch(count, n=64, seed=0):
+def gevd_batch(count, n=64, seed=0, dtype="f64"):
     """GEVD front-half workload: A symmetric (A = S + S^T, S ~ N(0,1)) and B = M M^T + n I with
-    M ~ N(0,1), column-major pairs of order n."""
+    M ~ N(0,1), column-major pairs of order n.  dtype "f32": the same pairs rounded to float;
+    "c128": Hermitian pairs, A + i (T - T^T) and B + 0.05 i (K - K^T) with T, K ~ N(0,1) (B stays
+    positive definite: the skew part's norm is far below n)."""
     ns = np.full(count, n, np.int32)
+    tr = lambda x: np.transpose(x, (0, 2, 1))
     s = normal(count * n * n, seed, stream=8).reshape(count, n, n)
-    a = np.ascontiguousarray(s + np.transpose(s, (0, 2, 1))).reshape(-1)
+    a = s + tr(s)
     m = normal(count * n * n, seed, stream=9).reshape(count, n, n)
-    b = np.matmul(m, np.transpose(m, (0, 2, 1)))
+    b = np.matmul(m, tr(m))
     b += n * np.eye(n)[None, :, :]
+    if dtype == "c128":
+        t = normal(count * n * n, seed, stream=10).reshape(count, n, n)
+        k = normal(count * n * n, seed, stream=11).reshape(count, n, n)
+        # Column-major storage of a Hermitian X is the row-major storage of X^T = conj(X).
+        a = np.conj(a + 1j * (t - tr(t)))
+        b = np.conj(b + 0.05j * (k - tr(k)))
+    a = np.ascontiguousarray(a).reshape(-1)
     b = np.ascontiguousarray(b).reshape(-1)          # symmetric: row- and column-major agree
+    if dtype == "f32":
+        a, b = a.astype(np.float32), b.astype(np.float32)
     off, _ = packed_offsets(ns, ns)
     return dict(n=ns, a_off=off, a=a, b_off=off, b=b, nrhs=0)
 
