@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <type_traits>
 
 #include "mf_device.cuh"
 #include "mf_kernels.h"
@@ -893,7 +894,9 @@ static cudaError_t set_potrf_t_attrs() {
 // Each row solve is SolveTriangular(Lower, NoTrans) in MatFlat's dot order (the stride does not
 // change the arithmetic), with the rows of L staged in shared memory one ahead of use.  One warp
 // per pair.  MFG_GEVD_LANES=0 selects the earlier form of the same passes, column solves of
-// warp_solve_dot with the accumulators of a few columns in shared memory.
+// warp_solve_dot with the accumulators of a few columns in shared memory; MFG_GEVD_LANES=2 moves
+// the Complex products to the integer pipes (ZSolveIM; measured slower at n=64, 138k against
+// 153k pairs/s, with 116 registers a thread against 80).
 constexpr int GEVD_T_WARPS = 8;
 
 __device__ __forceinline__ float gevd_conj(float v) { return v; }
@@ -1007,10 +1010,12 @@ __device__ void gevd_transpose(T* M, int n) {
   __syncwarp();
 }
 
-template <class C, bool LANES>
+template <class C, int MODE>
 __global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel(GevdArgs p) {
   using T = typename C::T;
   using Tr = typename C::Fwd;  // SolveTriangular(Lower, NoTrans): the dot form
+  using TrRows = std::conditional_t<MODE == 2 && sizeof(T) == 16, ZSolveIM, Tr>;
+  constexpr bool LANES = MODE != 0;
   using Acc = typename Tr::Acc;
   constexpr int W = sizeof(Acc) / sizeof(double);
   extern __shared__ double sm_gevd_t[];
@@ -1059,9 +1064,9 @@ __global__ void __launch_bounds__(GEVD_T_WARPS * 32) gevd_front_batched_t_kernel
     }
     __syncwarp();
     if constexpr (LANES) {
-      gevd_rows_solve<Tr>(B, n, ldb, Cm, vb);
+      gevd_rows_solve<TrRows>(B, n, ldb, Cm, vb);
       gevd_transpose<true>(Cm, n);
-      gevd_rows_solve<Tr>(B, n, ldb, Cm, vb);
+      gevd_rows_solve<TrRows>(B, n, ldb, Cm, vb);
       gevd_transpose<false>(Cm, n);
     } else {
       for (int c0 = 0; c0 < n; c0 += gevd_rhs<W>()) {
@@ -1085,46 +1090,50 @@ static size_t gevd_t_smem() {
   return sizeof(double) * gevd_t_warp_doubles<W>() * GEVD_T_WARPS;
 }
 
-static bool gevd_lanes() {
-  static const bool on = [] {
+// MFG_GEVD_LANES: 0 column solves, 1 (default) row solves, 2 row solves with the Complex
+// products on the integer pipes (float: the same kernel as 1).
+static int gevd_mode() {
+  static const int mode = [] {
     const char* v = std::getenv("MFG_GEVD_LANES");
-    return !(v && v[0] == '0');
+    if (v && v[0] == '0') return 0;
+    if (v && v[0] == '2') return 2;
+    return 1;
   }();
-  return on;
+  return mode;
+}
+
+template <class C, int MODE>
+static cudaError_t gevd_t_launch(const GevdArgs& args, int ctas, cudaStream_t s) {
+  gevd_front_batched_t_kernel<C, MODE><<<ctas, GEVD_T_WARPS * 32, gevd_t_smem<C>(), s>>>(args);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_gevd_front_batched_t(const GevdArgs& args, int elem, int ctas,
                                         cudaStream_t s) {
-  const dim3 blk(GEVD_T_WARPS * 32);
-  if (elem == 1 && gevd_lanes())
-    gevd_front_batched_t_kernel<SChol, true><<<ctas, blk, gevd_t_smem<SChol>(), s>>>(args);
-  else if (elem == 1)
-    gevd_front_batched_t_kernel<SChol, false><<<ctas, blk, gevd_t_smem<SChol>(), s>>>(args);
-  else if (gevd_lanes())
-    gevd_front_batched_t_kernel<ZChol, true><<<ctas, blk, gevd_t_smem<ZChol>(), s>>>(args);
-  else
-    gevd_front_batched_t_kernel<ZChol, false><<<ctas, blk, gevd_t_smem<ZChol>(), s>>>(args);
-  return cudaGetLastError();
+  const int mode = gevd_mode();
+  if (elem == 1) return mode == 0 ? gevd_t_launch<SChol, 0>(args, ctas, s)
+                                  : gevd_t_launch<SChol, 1>(args, ctas, s);
+  return mode == 0   ? gevd_t_launch<ZChol, 0>(args, ctas, s)
+         : mode == 1 ? gevd_t_launch<ZChol, 1>(args, ctas, s)
+                     : gevd_t_launch<ZChol, 2>(args, ctas, s);
 }
 
-// Resident CTAs per SM of the float / Complex kernels (the smaller of the two forms).
-int gevd_t_ctas_per_sm(int elem) {
-  int b0 = 0, b1 = 0;
-  cudaError_t e0, e1;
-  if (elem == 1) {
-    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &b0, gevd_front_batched_t_kernel<SChol, true>, GEVD_T_WARPS * 32, gevd_t_smem<SChol>());
-    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &b1, gevd_front_batched_t_kernel<SChol, false>, GEVD_T_WARPS * 32, gevd_t_smem<SChol>());
-  } else {
-    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &b0, gevd_front_batched_t_kernel<ZChol, true>, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>());
-    e1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &b1, gevd_front_batched_t_kernel<ZChol, false>, GEVD_T_WARPS * 32, gevd_t_smem<ZChol>());
-  }
-  if (e0 != cudaSuccess || e1 != cudaSuccess) return 1;
-  const int b = b0 < b1 ? b0 : b1;
+template <class C, int MODE>
+static int gevd_t_blocks() {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gevd_front_batched_t_kernel<C, MODE>,
+                                                    GEVD_T_WARPS * 32, gevd_t_smem<C>()) !=
+      cudaSuccess)
+    return 1;
   return b < 1 ? 1 : b;
+}
+
+// Resident CTAs per SM of the float / Complex kernel that the current mode launches.
+int gevd_t_ctas_per_sm(int elem) {
+  const int mode = gevd_mode();
+  if (elem == 1) return mode == 0 ? gevd_t_blocks<SChol, 0>() : gevd_t_blocks<SChol, 1>();
+  return mode == 0 ? gevd_t_blocks<ZChol, 0>()
+                   : mode == 1 ? gevd_t_blocks<ZChol, 1>() : gevd_t_blocks<ZChol, 2>();
 }
 
 int gevd_t_warps_per_cta() { return GEVD_T_WARPS; }
@@ -1135,17 +1144,16 @@ cudaError_t init_potrf_t_attributes() {
   e = set_potrf_t_attrs<ZChol>();
   if (e != cudaSuccess) return e;
   const int ss = (int)gevd_t_smem<SChol>(), zs = (int)gevd_t_smem<ZChol>();
-  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, ss)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<SChol, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, ss)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, zs)) != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(gevd_front_batched_t_kernel<ZChol, false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, zs);
+  const void* ks[5] = {(const void*)gevd_front_batched_t_kernel<SChol, 0>,
+                       (const void*)gevd_front_batched_t_kernel<SChol, 1>,
+                       (const void*)gevd_front_batched_t_kernel<ZChol, 0>,
+                       (const void*)gevd_front_batched_t_kernel<ZChol, 1>,
+                       (const void*)gevd_front_batched_t_kernel<ZChol, 2>};
+  for (int i = 0; i < 5; i++)
+    if ((e = cudaFuncSetAttribute(ks[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  i < 2 ? ss : zs)) != cudaSuccess)
+      return e;
+  return cudaSuccess;
 }
 
 cudaError_t launch_spotrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {

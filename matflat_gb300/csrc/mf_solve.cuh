@@ -103,6 +103,19 @@ struct ZSolve {
   static __device__ __forceinline__ T msub(T x, T a, T xi) { return zsub(x, m(a, xi)); }
 };
 
+// ZSolve<false> with the dot's four real products per multiply on the integer pipes (imul_rn,
+// bit-identical to __dmul_rn), which leaves the FP64 pipe the additions only.
+struct ZSolveIM : ZSolve<false> {
+  static __device__ __forceinline__ zdouble m(zdouble a, zdouble x) {
+    return {__dsub_rn(imul_rn(a.re, x.re), imul_rn(a.im, x.im)),
+            __dadd_rn(imul_rn(a.im, x.re), imul_rn(a.re, x.im))};
+  }
+  static __device__ __forceinline__ Acc prod(T a, T x) { return m(a, x); }
+  static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
+    return zadd(s, zadd(m(a0, x0), m(a1, x1)));
+  }
+};
+
 // Dot form.  Element (i, t), t < i, of the triangular operand is at a[i*si + t*st] and the
 // diagonal at a[i*si + i*st].  With unit = true the diagonal is taken as one: MatFlat's
 // unit-lower idiom divides by an explicit 1.0 (Factorization.LuInverse.cs:174-182), which is
