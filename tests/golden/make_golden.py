@@ -60,6 +60,9 @@ GEMM_SHAPES = {
 }
 # MatFlatTest/LuInverseTests.cs:75-84 (n, lda)
 LUINV_SHAPES = [(1, 1), (1, 3), (2, 2), (2, 3), (3, 3), (3, 5), (5, 5), (5, 8), (10, 10), (10, 17)]
+# MatFlatTest/GevdTests.cs:12-21, :96-105, :180-189 (n, lda, ldb)
+GEVD_SHAPES = [(1, 1, 1), (1, 3, 2), (2, 2, 2), (2, 4, 3), (3, 3, 3), (3, 4, 5), (5, 5, 5),
+               (5, 7, 8), (10, 10, 10), (10, 17, 11)]
 
 U, L = 121, 122
 NT, T = 111, 112
@@ -356,6 +359,54 @@ def main():
                     am = am.conj() if ca else am
                     bm = bm.conj() if cb else bm
                     g[key + "/lapack"] = put(c.astype(am.dtype), am @ bm, ldc)
+
+    # ---- float and Complex LuInverse (LuInverseTests.cs:12-72, :138-204) ---------------------
+    for (n, lda) in LUINV_SHAPES:
+        for prec, rnd in (("s", random_single), ("z", random_complex)):
+            a = rnd(42, n * lda)
+            key = "luinv_%s/%d_%d" % (prec, n, lda)
+            g[key + "/in"] = a
+            lu_ = a.copy()
+            piv = np.zeros(n, np.int32)
+            oracle.lu(n, n, lu_, lda, piv)
+            g[key + "/lu"] = lu_
+            g[key + "/piv"] = piv
+            inv = lu_.copy()
+            assert oracle.lu_inverse(n, inv, lda, piv) == 0
+            g[key + "/oracle"] = inv
+            wide = np.complex128 if prec == "z" else np.float64
+            g[key + "/lapack"] = put(a.astype(wide), np.linalg.inv(fmat(a, n, n, lda).astype(wide)),
+                                     lda)
+
+    # ---- GEVD front half (GevdTests.cs:12-94 float, :96-178 double, :180-262 Complex) --------
+    # A and B as the reference's GetDecomposable* helpers build them (X X^T, or X X^H, from a
+    # random X, written over X's leading n-by-n block; :271-364), then the strict lower parts set
+    # to NaN (NanLowerPart, :366-406), as the reference passes them to Factorization.Gevd.  The
+    # LAPACK side: potrf of B and C = L^-1 A L^-T (L^-H) from numpy's LAPACK solves.
+    for (n, lda, ldb) in GEVD_SHAPES:
+        for prec, rnd in (("d", random_double), ("s", random_single), ("z", random_complex)):
+            def decomposable(seed, ld):
+                x = rnd(seed, n * ld)
+                xm = fmat(x, n, n, ld).astype(np.complex128 if prec == "z" else np.float64)
+                sym = xm @ xm.conj().T
+                return put(x, sym.astype(x.dtype), ld)
+            a, b = decomposable(42, lda), decomposable(57, ldb)
+            full_a, full_b = a.copy(), b.copy()
+            for j in range(n):
+                a[j * lda + j + 1:j * lda + n] = np.nan
+                b[j * ldb + j + 1:j * ldb + n] = np.nan
+            key = "gevd_%s/%d_%d_%d" % (prec, n, lda, ldb)
+            g[key + "/a"], g[key + "/b"] = a, b
+            ob, oc = b.copy(), np.zeros(n * n, a.dtype)
+            assert oracle.gevd_front(n, a, lda, ob, ldb, oc) == 0
+            g[key + "/oracle_b"], g[key + "/oracle_c"] = ob, oc
+            wide = np.complex128 if prec == "z" else np.float64
+            Am = fmat(full_a, n, n, lda).astype(wide)
+            Bm = fmat(full_b, n, n, ldb).astype(wide)
+            Lm = np.linalg.cholesky(Bm)
+            Cm = np.linalg.solve(Lm, np.linalg.solve(Lm, Am).conj().T).conj().T
+            g[key + "/lapack_l"] = put(full_b.astype(wide), Lm, ldb)
+            g[key + "/lapack_c"] = Cm.flatten(order="F")
 
     np.savez_compressed(OUT, **g)
     print("wrote %s (%d arrays, %.1f KB)" % (OUT, len(g), os.path.getsize(OUT) / 1024))

@@ -101,12 +101,51 @@ def test_gemm_golden(mf, golden):
         assert_bits(c, golden[key + "/oracle"], key)
 
 
-def test_lu_inverse_golden(mf, golden):
-    for key in cases(golden, "luinv_d/"):
+@pytest.mark.parametrize("prec", ["d", "s", "z"])
+def test_lu_inverse_golden(mf, golden, prec):
+    keys = cases(golden, "luinv_%s/" % prec)
+    assert keys
+    for key in keys:
         n, lda = map(int, key.split("/")[1].split("_"))
         a = golden[key + "/lu"].copy()
         mf.Factorization.LuInverse(n, a, lda, golden[key + "/piv"])
-        assert_bits(a, golden[key + "/oracle"], key)
+        exp = golden[key + "/oracle"]
+        if prec == "z":
+            a, exp = a.view(np.float64), exp.view(np.float64)
+        assert_bits(a, exp, key)
+
+
+@pytest.mark.parametrize("prec", ["d", "s", "z"])
+def test_gevd_front_golden(mf, golden, prec):
+    """The batched GEVD front half on the reference's shapes (GevdTests.cs), all ten pairs in one
+    plan with their own lda and ldb, strict lower parts of A and B NaN as the reference passes
+    them: B (L and padding) and C bit-identical to the oracle fixture."""
+    import torch
+    keys = cases(golden, "gevd_%s/" % prec)
+    dims = [tuple(map(int, k.split("/")[1].split("_"))) for k in keys]
+    n = np.array([d[0] for d in dims], np.int32)
+    lda = np.array([d[1] for d in dims], np.int32)
+    ldb = np.array([d[2] for d in dims], np.int32)
+    a = np.concatenate([golden[k + "/a"] for k in keys])
+    b = np.concatenate([golden[k + "/b"] for k in keys])
+    off = lambda sz: np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    a_off, b_off = off(lda.astype(np.int64) * n), off(ldb.astype(np.int64) * n)
+    c_off = off(n.astype(np.int64) ** 2)
+    flat = (lambda x: x.view(np.float64)) if prec == "z" else (lambda x: x)
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    dc = torch.from_numpy(np.zeros(int((n.astype(np.int64) ** 2).sum()), a.dtype)).cuda()
+    dinfo = torch.full((len(n),), -3, dtype=torch.int32, device="cuda")
+    plan = mf.GevdFrontBatch(n, a_off, b_off, c_off, lda=lda, ldb=ldb)
+    plan.run(da, db, dc, dinfo)
+    mf.context().synchronize()
+    assert (dinfo.cpu().numpy() == 0).all()
+    gb, gc = db.cpu().numpy(), dc.cpu().numpy()
+    for i, k in enumerate(keys):
+        sb = slice(b_off[i], b_off[i] + ldb[i] * n[i])
+        sc = slice(c_off[i], c_off[i] + n[i] * n[i])
+        assert_bits(flat(gb[sb]), flat(golden[k + "/oracle_b"]), k + " B")
+        assert_bits(flat(gc[sc]), flat(golden[k + "/oracle_c"]), k + " C")
+    plan.close()
 
 
 # ------------------------------------------------------------------------------------------

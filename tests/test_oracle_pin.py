@@ -168,6 +168,64 @@ def test_lu_inverse_oracle_pin(golden):
             np.testing.assert_array_equal(inv[j * lda + n:(j + 1) * lda], a0[j * lda + n:(j + 1) * lda])
 
 
+@pytest.mark.parametrize("prec", ["s", "z"])
+def test_lu_inverse_types_oracle_pin(golden, prec):
+    """Float and Complex LuInverse on the reference's shapes (LuInverseTests.cs:12-72,
+    :138-204): bits against the fixture, A X = I at the reference's tolerance (float: 1e-5,
+    :55-59, widened by the first-order bound n eps cond(A) for the one ill-conditioned draw;
+    Complex: 1e-12, :184-190), padding rows unchanged."""
+    keys = cases(golden, "luinv_%s/" % prec)
+    assert keys
+    for key in keys:
+        n, lda = map(int, key.split("/")[1].split("_"))
+        a0 = golden[key + "/in"]
+        inv = golden[key + "/lu"].copy()
+        assert oracle.lu_inverse(n, inv, lda, golden[key + "/piv"]) == 0
+        np.testing.assert_array_equal(inv.view(np.uint8), golden[key + "/oracle"].view(np.uint8),
+                                      err_msg=key)
+        wide = np.complex128 if prec == "z" else np.float64
+        A = a0[:n * lda].reshape(n, lda).T[:n].astype(wide)
+        X = inv[:n * lda].reshape(n, lda).T[:n].astype(wide)
+        if prec == "s":
+            tol = max(1e-5, n * 2.0 ** -24 * np.linalg.cond(A))
+        else:
+            tol = 1e-12
+        assert np.max(np.abs(A @ X - np.eye(n))) <= tol, key
+        for j in range(n):
+            np.testing.assert_array_equal(inv[j * lda + n:(j + 1) * lda],
+                                          a0[j * lda + n:(j + 1) * lda])
+
+
+@pytest.mark.parametrize("prec", ["d", "s", "z"])
+def test_gevd_front_oracle_pin(golden, prec):
+    """The GEVD front half on the reference's shapes (GevdTests.cs:12-21, :96-105, :180-189) with
+    A and B's strict lower parts NaN, as the reference passes them: bits against the fixture,
+    only the upper triangles read (C finite), padding rows of B unchanged, L and
+    C = L^-1 A L^-T (L^-H) against LAPACK to a first-order bound, 10 n eps cond(B), relative to
+    the largest entry."""
+    keys = cases(golden, "gevd_%s/" % prec)
+    assert keys
+    eps = 2.0 ** -24 if prec == "s" else 2.0 ** -53
+    for key in keys:
+        n, lda, ldb = map(int, key.split("/")[1].split("_"))
+        a, b0 = golden[key + "/a"], golden[key + "/b"]
+        b, c = b0.copy(), np.zeros(n * n, a.dtype)
+        assert oracle.gevd_front(n, a, lda, b, ldb, c) == 0
+        np.testing.assert_array_equal(b.view(np.uint8), golden[key + "/oracle_b"].view(np.uint8),
+                                      err_msg=key)
+        np.testing.assert_array_equal(c.view(np.uint8), golden[key + "/oracle_c"].view(np.uint8),
+                                      err_msg=key)
+        assert np.isfinite(c.view(np.float32 if prec == "s" else np.float64)).all(), key
+        for j in range(n):
+            np.testing.assert_array_equal(b[j * ldb + n:(j + 1) * ldb], b0[j * ldb + n:(j + 1) * ldb])
+        ll, lc = golden[key + "/lapack_l"], golden[key + "/lapack_c"]
+        L = np.tril(b[:n * ldb].reshape(n, ldb).T[:n].astype(ll.dtype))
+        LL = np.tril(ll[:n * ldb].reshape(n, ldb).T[:n])
+        tol = 10 * n * eps * np.linalg.cond(LL @ LL.conj().T)
+        assert np.max(np.abs(L - LL)) <= tol * np.max(np.abs(LL)), key
+        assert np.max(np.abs(c - lc)) <= tol * np.max(np.abs(lc)), key
+
+
 def test_oracle_no_fma_contract():
     """A case whose result differs between fused and unfused evaluation: the oracle must not
     contract x0*y0 + x1*y1 into an FMA."""
