@@ -222,9 +222,11 @@ _ctx_lock = threading.Lock()
 def context():
     """The process-wide default context (created on first use).
 
-    Batched calls on device buffers are asynchronous on the context's own stream: keep every
-    tensor passed to them alive (and do not let another stream reuse its memory) until
-    context().synchronize(), or point the context at torch's stream with set_stream."""
+    Batched calls on device buffers are asynchronous on the context's own stream, which does not
+    wait for other streams: finish (or synchronize) the work that fills their inputs on torch's
+    stream before the call, keep every tensor passed to them alive (and do not let another
+    stream reuse its memory) until context().synchronize(), or point the context at torch's
+    stream with set_stream."""
     global _ctx
     with _ctx_lock:
         if _ctx is None:
