@@ -34,6 +34,7 @@ def test_gevd_front_batched(mf):
     dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
     for _ in range(2):          # the second call replays the captured graph
         db.copy_(_dev(b))
+        torch.cuda.synchronize()     # the copy runs on torch's stream, the plan on its own
         plan.run(da, db, dc, dinfo)
         mf.context().synchronize()
     info = _host(dinfo)

@@ -82,6 +82,7 @@ def test_lu_inverse_batched(mf):
     dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
     for _ in range(2):   # twice: the second run replays the captured graph
         da.copy_(_dev(fac))
+        torch.cuda.synchronize()     # the copy runs on torch's stream, the plan on its own
         batch.run(da, dpiv, dinfo)
         mf.context().synchronize()
     info = _host(dinfo)

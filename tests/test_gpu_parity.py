@@ -288,6 +288,7 @@ def test_lu_batched(mf):
     for _ in range(2):   # twice: the second run replays the captured graph
         da.copy_(_dev(a))
         db.copy_(_dev(b))
+        torch.cuda.synchronize()     # the copies run on torch's stream, the plan on its own
         batch.run(da, dpiv, db, dsign, dinfo)
         mf.context().synchronize()
     oa, ob = a.copy(), b.copy()

@@ -38,6 +38,7 @@ def test_getrs_batched_matches_fused(mf):
     b2 = _dev(b)
     for _ in range(2):          # the second call replays the captured graph
         b2.copy_(_dev(b))
+        torch.cuda.synchronize()     # the copy runs on torch's stream, the plan on its own
         batch.solve(da, dpiv, b2)
         mf.context().synchronize()
     assert_bits(_host(b2), fused)
@@ -50,6 +51,7 @@ def test_getrs_batched_matches_fused(mf):
     # factoring again after a solve recaptures the factorization graph
     da.copy_(_dev(a))
     db.copy_(_dev(b))
+    torch.cuda.synchronize()
     batch.run(da, dpiv, db, dsign, dinfo)
     mf.context().synchronize()
     assert_bits(_host(db), fused)
