@@ -116,3 +116,41 @@ def test_gevd_front_types_not_positive_definite(dt):
     b = b.flatten(order="F")
     c = np.zeros(n * n, dt)
     assert oracle.gevd_front(n, a, n, b, n, c) == 4
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32, np.complex128])
+@pytest.mark.parametrize("n", [1, 2, 7, 33])
+def test_gevd_row_form_is_matflats_order(dt, n):
+    """The float / Complex GPU kernel runs MatFlat's two passes as row solves: D = conj(C), its
+    rows solved, E = D^H, its rows solved, C = E^T.  Replayed here with the oracle's own
+    SolveTriangular at stride n, the reformulation reproduces the oracle's GevdCore bit for bit
+    (the stride and the order of the right-hand sides do not change any value)."""
+    LOWER, NOTRANS = 122, 111
+    rng = np.random.default_rng(180 + n)
+    draw = (lambda *s: rng.standard_normal(s) + 1j * rng.standard_normal(s)) \
+        if dt == np.complex128 else (lambda *s: rng.standard_normal(s))
+    A = draw(n, n)
+    M = draw(n, n)
+    B = M @ M.conj().T + n * np.eye(n)
+    a = A.astype(dt).flatten(order="F")
+    b = B.astype(dt).flatten(order="F")
+    ob, oc = b.copy(), np.zeros(n * n, dt)
+    assert oracle.gevd_front(n, a, n, ob, n, oc) == 0
+    lb = b.copy()
+    assert oracle.cholesky(n, lb, n) == 0
+    np.testing.assert_array_equal(lb.view(np.uint8), ob.view(np.uint8))
+    Am = a.reshape(n, n, order="F")
+    U = np.triu(Am, 1)
+    C = U + U.conj().T + np.diag(np.diag(Am))           # MatFlat's C (diagonal as stored)
+    D = np.asfortranarray(np.conj(C)).flatten(order="F")
+    for r in range(n):                                   # rows of D, stride n
+        seg = D[r:].copy()
+        assert oracle.trsv(LOWER, NOTRANS, n, lb, n, seg, n) == 0
+        D[r:] = seg
+    E = np.asfortranarray(D.reshape(n, n, order="F").conj().T).flatten(order="F")
+    for r in range(n):
+        seg = E[r:].copy()
+        assert oracle.trsv(LOWER, NOTRANS, n, lb, n, seg, n) == 0
+        E[r:] = seg
+    got = np.asfortranarray(E.reshape(n, n, order="F").T).flatten(order="F")
+    np.testing.assert_array_equal(got.view(np.uint8), oc.view(np.uint8))
