@@ -254,7 +254,7 @@ def read_traffic(kernel_key):
 
 
 def make_inputs(cfg_name, rank):
-    from matflat_gb300 import synth
+    from workloads import synth
     cfg = CONFIGS[cfg_name]
     if cfg_name in ("lu", "inv"):
         return synth.lu_batch(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"], seed=rank)
@@ -419,17 +419,18 @@ def dtype_name(cfg_name):
     return {"qr32": "f32", "gevd32": "f32", "gevdz": "complex128"}.get(cfg_name, "f64")
 
 
-def run_mixed(args, torch, mf, world, rank, local):
-    """Mixed-precision LU + FP64 refinement vs the exact FP64 LU on the same batch."""
-    from matflat_gb300 import synth
-    cfg = CONFIGS["mixed"]
-    count = cfg["count"]
-    n = args.n or cfg["n"]
-    stream = torch.cuda.Stream()
+def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, local,
+                  with_e2e=True, cpu_sample=0):
+    """Mixed-precision LU + FP64 refinement against the exact FP64 LU on the same systems.
+
+    Returns a dict: solves/s (CUDA events on the solver's stream, L2-sized inputs so no flush is
+    needed: A alone is 8 n^2 count bytes), per-system backward/forward error, the exact FP64 GPU
+    rate on the same systems, optionally the end-to-end rate and a CPU-oracle sample."""
+    from workloads import synth
     ctx = mf.context()
     ctx.set_stream(stream.cuda_stream)
     with torch.cuda.stream(stream):
-        a, b, xt = synth.conditioned_batch_device(count, n, args.cond, seed=rank)
+        a, b, xt = synth.conditioned_batch_device(count, n, cond, seed=seed)
     stream.synchronize()
     x = torch.zeros_like(b)
     berr = torch.zeros(count, dtype=torch.float64, device="cuda")
@@ -438,10 +439,10 @@ def run_mixed(args, torch, mf, world, rank, local):
     solver = mf.MixedSolveBatch(count, n)
 
     def run():
-        solver.run(a, b, x, berr, iters, info, lowp=args.lowp, max_iter=10, tol=1e-12)
+        solver.run(a, b, x, berr, iters, info, lowp=lowp, max_iter=10, tol=1e-12)
 
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             run()
         stream.synchronize()
         clocks = ClockSampler(local)
@@ -449,18 +450,17 @@ def run_mixed(args, torch, mf, world, rank, local):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             run()
         t1.record(stream)
         stream.synchronize()
         clocks.stop()
-    ms = t0.elapsed_time(t1) / args.steps
-    value = world * count / (ms / 1e3)
+    ms = t0.elapsed_time(t1) / steps
 
     # End to end through the C ABI: A and b from pinned host memory, x, berr, iters and info
     # back to pinned host memory, every step.
     e2e = None
-    if not args.no_e2e:
+    if with_e2e:
         ins = [a, b]
         outs = [x, berr, iters, info]
         ins_h = [t.cpu().pin_memory() for t in ins]
@@ -476,7 +476,7 @@ def run_mixed(args, torch, mf, world, rank, local):
             q0 = torch.cuda.Event(enable_timing=True)
             q1 = torch.cuda.Event(enable_timing=True)
             q0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 for t, th in zip(ins, ins_h):
                     t.copy_(th, non_blocking=True)
                 run()
@@ -484,8 +484,8 @@ def run_mixed(args, torch, mf, world, rank, local):
                     th.copy_(t, non_blocking=True)
             q1.record(stream)
             stream.synchronize()
-        e2e_ms = q0.elapsed_time(q1) / args.steps
-        e2e = {"value": world * count / (e2e_ms / 1e3), "unit": "solves/s",
+        e2e_ms = q0.elapsed_time(q1) / steps
+        e2e = {"value": count / (e2e_ms / 1e3), "unit": "solves/s",
                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in ins)),
                "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in outs)),
                "ms_per_step": e2e_ms}
@@ -520,15 +520,14 @@ def run_mixed(args, torch, mf, world, rank, local):
     plain_ms = p0.elapsed_time(p1)
     plain_x = b2.reshape(count, n)
     pfe = ((plain_x - xt).abs().amax(1) / xt.abs().amax(1)).cpu().numpy()
-    flops = count * (2.0 * n ** 3 / 3)
     hist = {int(k): int(v) for k, v in zip(*np.unique(it, return_counts=True))}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if cpu_sample:
         from oracle import oracle
         ah = a.cpu().numpy()
         bh = b.cpu().numpy()
-        k = max(8, min(count, 64))
+        k = max(1, min(count, cpu_sample))
         idx = np.linspace(0, count - 1, k).astype(int)
         n_s = np.full(k, n, np.int32)
         aoff = np.arange(k, dtype=np.int64) * n * n
@@ -547,33 +546,87 @@ def run_mixed(args, torch, mf, world, rank, local):
         ox = bsub.reshape(k, n)
         gx = xv.cpu().numpy()[idx]
         cpu["mixed_vs_oracle_rel_err_max"] = float(np.max(np.abs(gx - ox) / np.abs(ox).max(1, keepdims=True)))
+    del a, b, xt, x, a2, b2
+    torch.cuda.empty_cache()
+    return {
+        "value": count / (ms / 1e3), "unit": "solves/s", "ms": ms, "count": count, "n": n,
+        "cond": cond, "lowp": lowp, "tol": 1e-12, "max_iter": 10,
+        "berr_max": float(np.nanmax(be)), "berr_median": float(np.nanmedian(be)),
+        "fwd_err_max": float(np.max(fe)), "fwd_err_median": float(np.median(fe)),
+        "iters_histogram": hist, "fallback_fp64": int((inf == 1).sum()),
+        "singular": int((inf == 2).sum()),
+        "fp64_plain": {"value": count / (plain_ms / 1e3), "unit": "solves/s", "ms": plain_ms,
+                       "fwd_err_max": float(np.max(pfe))},
+        "speedup_vs_fp64_plain": plain_ms / ms,
+        "flops": count * (2.0 * n ** 3 / 3),
+        "e2e": e2e, "cpu": cpu, "clocks": clocks.summary(),
+    }
 
+
+def run_mixed(args, torch, mf, world, rank, local):
+    """Mixed-precision LU + FP64 refinement vs the exact FP64 LU on the same batch."""
+    cfg = CONFIGS["mixed"]
+    count = cfg["count"]
+    n = args.n or cfg["n"]
+    stream = torch.cuda.Stream()
+    r = measure_mixed(torch, mf, stream, count, n, args.cond, args.lowp, args.steps, args.warmup,
+                      rank, local, with_e2e=not args.no_e2e,
+                      cpu_sample=64 if (rank == 0 and world == 1 and not args.no_cpu_baseline)
+                      else 0)
     if rank == 0:
         line = {
-            "metric": metric_name("mixed"), "value": value, "unit": "solves/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "metric": metric_name("mixed"), "value": world * r["value"], "unit": "solves/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (torch generator on the GPU, seed per rank)",
             "config": {"workload": cfg["workload"], "count": count, "n": n, "cond": args.cond,
                        "lowp": args.lowp, "max_iter": 10, "tol": 1e-12},
             "gpu_launches": 2 * (n // 32) + 12,
-            "berr_max": float(np.nanmax(be)), "berr_median": float(np.nanmedian(be)),
-            "fwd_err_max": float(np.max(fe)), "fwd_err_median": float(np.median(fe)),
-            "iters_histogram": hist, "fallback_fp64": int((inf == 1).sum()),
-            "singular": int((inf == 2).sum()),
-            "fp64_plain": {"value": count / (plain_ms / 1e3), "unit": "solves/s",
-                           "ms": plain_ms, "fwd_err_max": float(np.max(pfe))},
-            "speedup_vs_fp64_plain": plain_ms / ms,
             "roofline": {"bound": "tensor" if args.lowp != "fp32" else "fp32",
-                         "achieved": flops / (ms / 1e3) / 1e12, "unit": "TFLOP/s",
+                         "achieved": r["flops"] / (r["ms"] / 1e3) / 1e12, "unit": "TFLOP/s",
                          "note": "whole solve (factorization + refinement) against the "
                                  "factorization's 2n^3/3; the panel and refinement sweeps, not "
                                  "the tensor-core GEMMs, dominate at n=512"},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "clocks": clocks.summary(),
+            "cpu_baseline": r["cpu"], "e2e": r["e2e"], "clocks": r["clocks"],
         }
+        for k in ("berr_max", "berr_median", "fwd_err_max", "fwd_err_median", "iters_histogram",
+                  "fallback_fp64", "singular", "fp64_plain", "speedup_vs_fp64_plain"):
+            line[k] = r[k]
         print(json.dumps(line), flush=True)
+
+
+def lu_parity(d, a_out, b_out, piv_out, sign_out, info_out):
+    """The oracle (MatFlat's LuCore + solve restated in C++) over the WHOLE timed batch, after
+    the timed region, compared with the GPU's outputs of the last timed step bit for bit."""
+    from oracle import oracle
+    n = d["n"]
+    a = d["a"].copy()
+    b = d["b"].copy()
+    piv = np.zeros(d["piv_total"], np.int32)
+    sign = np.zeros(len(n), np.int32)
+    t = time.perf_counter()
+    oracle.lu_solve_batched(n, d["a_off"], a, d["piv_off"], piv, d["b_off"], b, d["nrhs"], sign,
+                            os.cpu_count() or 1)
+    dt = time.perf_counter() - t
+    ga = a_out.view(np.uint64)
+    gb = b_out.view(np.uint64)
+    bad_piv = bad_a = bad_b = 0
+    a_off, piv_off, b_off = d["a_off"], d["piv_off"], d["b_off"]
+    eq_a = ga == a.view(np.uint64)
+    eq_b = gb == b.view(np.uint64)
+    eq_p = piv_out == piv
+    # per-matrix mismatch counts through the packed offsets
+    ia = np.add.reduceat(~eq_a, a_off) if len(a_off) else np.zeros(0)
+    ip = np.add.reduceat(~eq_p, piv_off) if len(piv_off) else np.zeros(0)
+    ib = np.add.reduceat(~eq_b, b_off) if len(b_off) else np.zeros(0)
+    bad_a, bad_piv, bad_b = int((ia > 0).sum()), int((ip > 0).sum()), int((ib > 0).sum())
+    bad_sign = int((sign_out != sign).sum())
+    return {"checked": int(len(n)), "checker": "oracle (MatFlat LuCore + solve, C++), %.1f s on "
+                                              "%d threads" % (dt, os.cpu_count() or 1),
+            "pivots_identical": bad_piv == 0, "factors_bit_identical": bad_a == 0,
+            "x_bit_identical": bad_b == 0, "signs_identical": bad_sign == 0,
+            "mismatches": {"pivots": bad_piv, "factors": bad_a, "x": bad_b, "sign": bad_sign},
+            "zero_pivot_matrices": int((info_out != 0).sum())}
 
 
 def main():
@@ -597,6 +650,10 @@ def main():
                     help="lu/chol: keep the default launch shape instead of autotuning the plan")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="lu: skip the oracle check of the whole timed batch")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="lu: skip the mixed-precision sub-measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: warmup raised to 3", file=sys.stderr)
@@ -772,6 +829,10 @@ def main():
         barrier()
     total_ms = sum(s.elapsed_time(e) for s, e in zip(sstart, kend))
     kernel_ms = [s.elapsed_time(e) for s, e in zip(kstart, kend)]
+    # The last timed step's outputs, for the parity check against the oracle (after timing).
+    parity_outs = None
+    if cfg_name == "lu" and rank == 0 and not args.no_parity:
+        parity_outs = [t.cpu().numpy() for t in (a, b, piv, sign, info)]
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -890,6 +951,33 @@ def main():
         cpu["single_thread"] = {"value": rate1, "sample": "%d matrices, 1 thread (%.1f s)"
                                                           % (n1, t1s)}
 
+    # ---- parity of the whole timed batch against the oracle (rank 0, after timing) -----------
+    parity = None
+    if parity_outs is not None:
+        parity = lu_parity(d, *parity_outs)
+
+    # ---- the mixed-precision half of the metric (2,048 systems n=512, cond 1e5) --------------
+    mixed = None
+    if cfg_name == "lu" and not args.no_mixed:
+        mcfg = CONFIGS["mixed"]
+        r = measure_mixed(torch, mf, torch.cuda.Stream(), mcfg["count"], mcfg["n"], 1e5,
+                          args.lowp, 3, 3, rank, local, with_e2e=False)
+        if world > 1:
+            tt = torch.tensor([r["ms"], r["fp64_plain"]["ms"]], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            r["ms"], r["fp64_plain"]["ms"] = float(tt[0].item()), float(tt[1].item())
+        mixed = {"workload": mcfg["workload"] + ", cond 1e5", "lowp": args.lowp,
+                 "value": world * mcfg["count"] / (r["ms"] / 1e3), "unit": "solves/s",
+                 "ms_per_solve_batch": r["ms"],
+                 "fp64_plain_value": world * mcfg["count"] / (r["fp64_plain"]["ms"] / 1e3),
+                 "fp64_plain_ms": r["fp64_plain"]["ms"],
+                 "speedup_vs_fp64_plain": r["fp64_plain"]["ms"] / r["ms"],
+                 "berr_max": r["berr_max"], "berr_median": r["berr_median"],
+                 "fwd_err_max": r["fwd_err_max"], "fp64_plain_fwd_err_max": r["fp64_plain"]["fwd_err_max"],
+                 "iters_histogram": r["iters_histogram"], "fallback_fp64": r["fallback_fp64"],
+                 "timing": "CUDA events on the solver's stream, 3 warm-up + 3 timed solves; "
+                           "plain rate: one timed exact FP64 LU + solve of the same systems"}
+
     if rank == 0:
         line = {
             "metric": metric_name(cfg_name), "value": value, "unit": "matrices/s",
@@ -914,6 +1002,10 @@ def main():
             "e2e": e2e,
             "clocks": clocks.summary(),
         }
+        if parity is not None:
+            line["parity"] = parity
+        if mixed is not None:
+            line["mixed"] = mixed
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

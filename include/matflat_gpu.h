@@ -59,7 +59,7 @@ enum mfg_status {
   MFG_ERR_ALLOC = -1002,       /* device or pinned allocation failed */
   MFG_ERR_INPLACE = -1003,     /* MulMatMat: a == c or b == c ("In-place operation is not
                                   supported.", Blas.MulMatMat.cs:301-304) */
-  MFG_ERR_TIMEOUT = -1004,     /* a bounded device-side wait gave up (see mfg_plan_status) */
+  /* -1004 is not used: no kernel of this library waits on another (see mfg_plan_status) */
   MFG_ERR_UNSUPPORTED = -1005  /* size or option outside what the library supports */
 };
 
@@ -74,6 +74,10 @@ MFG_API int mfg_destroy(mfg_ctx* ctx);
 /* Use `stream` (a cudaStream_t) for all later work; NULL selects the context's own stream. */
 MFG_API int mfg_set_stream(mfg_ctx* ctx, void* stream);
 MFG_API int mfg_synchronize(mfg_ctx* ctx);
+/* The CUDA device the context was created on (the device current at mfg_create).  Every later
+ * call on the context makes that device current while it runs and restores the caller's device
+ * before returning, so a thread may switch devices between calls. */
+MFG_API int mfg_get_device(mfg_ctx* ctx, int* device);
 /* Text of the last failure on this context (empty when none).  Valid until the next call. */
 MFG_API const char* mfg_last_error(mfg_ctx* ctx);
 /* Library version, e.g. "0.1.0"; the MatFlat version whose arithmetic it reproduces is 0.8.2. */
@@ -437,8 +441,10 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 
-/* Reads back the device-side status word of the last execution of `plan` (synchronizes the
- * context's stream): MFG_OK, or MFG_ERR_TIMEOUT if a bounded device-side wait gave up. */
+/* Waits for the context's stream and reports an asynchronous CUDA failure of the work queued so
+ * far (including the last execution of `plan`): MFG_OK or MFG_ERR_CUDA (text in mfg_last_error).
+ * Numerical failures are not statuses: they are in the `info` arrays.  No kernel of this library
+ * waits on another, so no call reports a timeout. */
 MFG_API int mfg_plan_status(mfg_plan* plan);
 
 /* Allocation-free batched LU + solve (no counterpart in the reference: MatFlat has no batched
@@ -452,9 +458,12 @@ MFG_API int mfg_plan_status(mfg_plan* plan);
  * All pointers are device pointers; the call is asynchronous on the context's stream.
  * Limit: n <= 256 (larger n returns MFG_ERR_UNSUPPORTED before anything is launched).
  * The kernel's scratch lives in one static device array of 11.4 MB (10.8 MiB) that every GPU
- * loading the library keeps until exit.  The first call on a device looks up that array's address and
- * should come before any stream capture.  Calls share the array: calls that overlap on the GPU
- * (different streams or contexts on one device) race and must be serialised by the caller. */
+ * loading the library keeps until exit.  Every call looks up that array's address on the
+ * context's device (a look-up allocates nothing); the first call on a device may load the
+ * library's kernels onto it and should come before any stream capture.  For n > 128 at most
+ * 608 warps work on the batch, so those orders can run below the plan path's rate on a GPU
+ * with more than 152 SMs.  Calls share the array: calls that overlap on the GPU (different
+ * streams or contexts on one device) race and must be serialised by the caller. */
 MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, double* a,
                                               int lda, int64_t stride_a, int* piv,
                                               int64_t stride_piv, int nrhs, double* b,

@@ -22,6 +22,7 @@ _SIGS = {
     "mfg_set_stream": (_I, [_vp, _vp]),
     "mfg_synchronize": (_I, [_vp]),
     "mfg_last_error": (ctypes.c_char_p, [_vp]),
+    "mfg_get_device": (_I, [_vp, _c_int_p]),
     "mfg_dgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_dpotrf": (_I, [_vp, _I, _vp, _I, _c_int_p]),
     "mfg_dgeqrf": (_I, [_vp, _I, _I, _vp, _I, _vp]),
@@ -205,6 +206,12 @@ class _Context:
 
     def synchronize(self):
         self.check(self.lib.mfg_synchronize(self.h))
+
+    def device(self):
+        """The CUDA device the context runs on (current at its creation)."""
+        d = ctypes.c_int(-1)
+        self.check(self.lib.mfg_get_device(self.h, ctypes.byref(d)), "mfg_get_device")
+        return d.value
 
     def last_error(self):
         msg = self.lib.mfg_last_error(self.h)

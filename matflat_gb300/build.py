@@ -13,7 +13,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libmatflat_gpu.so")
-SYNTH_LIB = os.path.join(OUT, "libmatflat_synth.so")
 SOURCES = ["lu.cu", "chol.cu", "getri.cu", "blas.cu", "qr.cu", "mixed.cu", "tune.cu", "vec.cu", "runtime.cu"]
 HEADERS = ["mf_device.cuh", "mf_imul.cuh", "mf_scalar.cuh", "mf_solve.cuh", "mf_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -38,20 +37,8 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_synth(force=False):
-    """Host-only helper library for seeded synthetic inputs (benchmark and tests)."""
-    os.makedirs(OUT, exist_ok=True)
-    src = os.path.join(CSRC, "synth.c")
-    if force or _stale(SYNTH_LIB, [src]):
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-                               "-o", SYNTH_LIB + ".tmp", src, "-lm"])
-        os.replace(SYNTH_LIB + ".tmp", SYNTH_LIB)
-    return SYNTH_LIB
-
-
 def build(force=False, verbose=False, extra_flags=()):
     os.makedirs(OUT, exist_ok=True)
-    build_synth(force)
     srcs = [os.path.join(CSRC, s) for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [
         os.path.join(os.path.dirname(HERE), "include", "matflat_gpu.h")]

@@ -19,8 +19,6 @@
 // being factored): on GB300 the FP64 pipe, not memory, bounds this kernel.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
@@ -410,7 +408,9 @@ namespace mfg {
 // holds until the process exits.
 //
 // Limits: n <= NOALLOC_MAX_N (256); for n > 128 at most NOALLOC_MAX_WARPS warps run, each with a
-// NOALLOC_WARP_STRIDE-double slice; the array is 11.4 MB.  Every call shares the array and keeps
+// NOALLOC_WARP_STRIDE-double slice (on a GPU with more SMs than NOALLOC_MAX_WARPS / 4 some SMs
+// then get no work, so orders above 128 can run below the plan path's rate); the array is
+// 11.4 MB.  Every call shares the array and keeps
 // the previous call's contents, so the counter is cleared (cudaMemsetAsync) before each launch,
 // and calls that overlap on the GPU (two streams, or two contexts on one device) race on it.
 constexpr int NOALLOC_MAX_N = 256;
@@ -471,40 +471,35 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_strided_noalloc_kernel(Strid
   }
 }
 
-// Set-up: the device address of g_noalloc_scratch, looked up once per device with that device
-// current (in host code the array's name is only a host-side stand-in, never a device address).
-static void* g_noalloc_ptr[64];
-static std::once_flag g_noalloc_once[64];
-static cudaError_t g_noalloc_err[64];
-
+// Set-up: the device address of g_noalloc_scratch, looked up on every call with the context's
+// device current (in host code the array's name is only a host-side stand-in, never a device
+// address).  The look-up allocates nothing; the first one on a device may load this library's
+// kernels onto it, so that first call should come before any stream capture.  Nothing is
+// cached, so a failed look-up is simply retried by the next call and a cudaDeviceReset leaves
+// no stale address behind.  The kernel's 37 KB of dynamic shared memory stay under the default
+// 48 KB limit, so no function attribute has to be set.
 static cudaError_t noalloc_scratch(int device, double** out) {
-  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-  std::call_once(g_noalloc_once[device], [device]() {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e == cudaSuccess) {
-      const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES * 4;
-      e = cudaFuncSetAttribute(getrf_strided_noalloc_kernel<4>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
-    g_noalloc_err[device] = e;
-    g_noalloc_ptr[device] = (e == cudaSuccess) ? ptr : nullptr;
-  });
-  *out = (double*)g_noalloc_ptr[device];
-  return g_noalloc_err[device];
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return e;
+  if (cur != device) return cudaErrorInvalidDevice;
+  void* ptr = nullptr;
+  e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  *out = (double*)ptr;
+  return cudaSuccess;
 }
+static_assert(sizeof(double) * SMEM_WARP_DOUBLES * 4 <= 48 * 1024,
+              "the allocation-free kernel must fit the default shared-memory limit");
 
 int noalloc_max_n() { return NOALLOC_MAX_N; }
 
 cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,
                                          long long stride_piv, int nrhs, double* b,
                                          long long stride_b, int* sign, int* info, int count,
-                                         int sm_count, cudaStream_t s) {
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) return e;
+                                         int device, int sm_count, cudaStream_t s) {
   double* scratch = nullptr;
-  e = noalloc_scratch(device, &scratch);
+  cudaError_t e = noalloc_scratch(device, &scratch);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(scratch, 0, sizeof(double) * NOALLOC_HEADER_DOUBLES, s);
   if (e != cudaSuccess || count == 0) return e;

@@ -172,7 +172,7 @@ int noalloc_max_n();
 cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long stride_a, int* piv,
                                          long long stride_piv, int nrhs, double* b,
                                          long long stride_b, int* sign, int* info, int count,
-                                         int sm_count, cudaStream_t s);
+                                         int device, int sm_count, cudaStream_t s);
 
 // Mixed-precision LU solve with FP64 refinement (mixed.cu).
 int mx_panel_width();

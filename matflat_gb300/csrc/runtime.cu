@@ -90,6 +90,25 @@ struct mfg_ctx {
   std::map<long long, std::array<int, 5>> tune;
 };
 
+// Makes the context's device current for the duration of an entry point and restores the
+// caller's device afterwards, so a host thread that switched devices after mfg_create still
+// launches on the context's device, stream and workspace.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(const mfg_ctx* ctx) {
+    if (!ctx) return;
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != ctx->device &&
+        cudaSetDevice(ctx->device) == cudaSuccess)
+      prev = cur;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 struct mfg_plan {
   enum Kind { GETRF, POTRF, GEQRF, MIXED, GETRI, GEVD } kind;
   mfg_ctx* ctx = nullptr;
@@ -159,8 +178,11 @@ int fail(mfg_ctx* ctx, int code, const char* fmt, ...) {
   return code;
 }
 
+// A failed CUDA call: MFG_ERR_ALLOC when the device (or page-locked host memory) ran out,
+// MFG_ERR_CUDA otherwise; the text names the call.
 int cuda_fail(mfg_ctx* ctx, cudaError_t e, const char* what) {
-  return fail(ctx, MFG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  const int code = e == cudaErrorMemoryAllocation ? MFG_ERR_ALLOC : MFG_ERR_CUDA;
+  return fail(ctx, code, "%s: %s", what, cudaGetErrorString(e));
 }
 
 #define MFG_CUDA(ctx, call)                                  \
@@ -852,6 +874,7 @@ MFG_API int mfg_create(mfg_ctx** ctx) {
 
 MFG_API int mfg_destroy(mfg_ctx* ctx) {
   if (!ctx) return -1;
+  DeviceScope device_scope_(ctx);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   ctx->work.release();
@@ -861,14 +884,23 @@ MFG_API int mfg_destroy(mfg_ctx* ctx) {
 }
 
 MFG_API int mfg_set_stream(mfg_ctx* ctx, void* stream) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   return MFG_OK;
 }
 
 MFG_API int mfg_synchronize(mfg_ctx* ctx) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MFG_OK;
+}
+
+MFG_API int mfg_get_device(mfg_ctx* ctx, int* device) {
+  if (!ctx) return -1;
+  if (!device) return fail(ctx, -2, "device is null");
+  *device = ctx->device;
   return MFG_OK;
 }
 
@@ -878,6 +910,7 @@ MFG_API const char* mfg_last_error(mfg_ctx* ctx) { return ctx ? ctx->last_error.
 // Single-matrix drop-ins.
 
 MFG_API int mfg_dgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   // Factorization.Lu argument checks (Factorization.Lu.cs:124-147).
   if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
@@ -912,6 +945,7 @@ MFG_API int mfg_dgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv,
 }
 
 MFG_API int mfg_dpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   // Factorization.Cholesky argument checks (Factorization.Cholesky.cs:116-129).
   if (n <= 0) return fail(ctx, -2, "The order of the matrix must be greater than or equal to one.");
@@ -942,6 +976,7 @@ MFG_API int mfg_dpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
 
 MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
                       double* x, int incx) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   // Blas.SolveTriangular argument checks (Blas.SolveTriangular.cs:164-187, enums :189-241).
   if (n <= 0) return fail(ctx, -4, "The order of the matrix must be greater than or equal to one.");
@@ -974,6 +1009,7 @@ MFG_API int mfg_dtrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a,
 
 MFG_API int mfg_dgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
                       int lda, const double* b, int ldb, double* c, int ldc) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   // Blas.MulMatMat argument checks (Blas.MulMatMat.cs:228-304).
   if (m <= 0) return fail(ctx, -4, "The value must be greater than or equal to one.");
@@ -1104,12 +1140,15 @@ static int getri_single_any(mfg_ctx* ctx, int elem, int n, void* a, int lda, con
 extern "C" {
 
 MFG_API int mfg_dgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+  DeviceScope device_scope_(ctx);
   return getri_single_any(ctx, 0, n, a, lda, piv, info);
 }
 MFG_API int mfg_sgetri(mfg_ctx* ctx, int n, float* a, int lda, const int* piv, int* info) {
+  DeviceScope device_scope_(ctx);
   return getri_single_any(ctx, 1, n, a, lda, piv, info);
 }
 MFG_API int mfg_zgetri(mfg_ctx* ctx, int n, double* a, int lda, const int* piv, int* info) {
+  DeviceScope device_scope_(ctx);
   return getri_single_any(ctx, 2, n, a, lda, piv, info);
 }
 
@@ -1231,33 +1270,41 @@ static int qr_r_single(mfg_ctx* ctx, int m, int n, const T* a, int lda, T* r, in
 extern "C" {
 
 MFG_API int mfg_dgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
+  DeviceScope device_scope_(ctx);
   return qr_single<double>(ctx, m, n, a, lda, rdiag);
 }
 MFG_API int mfg_sgeqrf(mfg_ctx* ctx, int m, int n, float* a, int lda, float* rdiag) {
+  DeviceScope device_scope_(ctx);
   return qr_single<float>(ctx, m, n, a, lda, rdiag);
 }
 MFG_API int mfg_dorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq) {
+  DeviceScope device_scope_(ctx);
   return qr_q_single<double>(ctx, m, n, a, lda, q, ldq);
 }
 MFG_API int mfg_sorgqr(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* q, int ldq) {
+  DeviceScope device_scope_(ctx);
   return qr_q_single<float>(ctx, m, n, a, lda, q, ldq);
 }
 MFG_API int mfg_dqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
                       const double* rdiag) {
+  DeviceScope device_scope_(ctx);
   return qr_r_single<double>(ctx, m, n, a, lda, r, ldr, rdiag);
 }
 MFG_API int mfg_sqr_r(mfg_ctx* ctx, int m, int n, const float* a, int lda, float* r, int ldr,
                       const float* rdiag) {
+  DeviceScope device_scope_(ctx);
   return qr_r_single<float>(ctx, m, n, a, lda, r, ldr, rdiag);
 }
 
 MFG_API int mfg_plan_geqrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* m,
                                    const int* n, const int* lda, const int64_t* a_off,
                                    const int64_t* rdiag_off, int nrhs, const int64_t* b_off) {
+  DeviceScope device_scope_(ctx);
   return plan_create_qr(ctx, plan, count, m, n, lda, a_off, rdiag_off, nrhs, b_off);
 }
 
 MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -1275,6 +1322,7 @@ MFG_API int mfg_dgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double*
 }
 
 MFG_API int mfg_sgeqrf_batched(mfg_plan* plan, float* a, float* rdiag, float* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -1321,6 +1369,7 @@ static int zqr_prepare(mfg_plan* p) {
 extern "C" {
 
 MFG_API int mfg_zgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -1340,6 +1389,7 @@ MFG_API int mfg_zgeqrf_batched(mfg_plan* plan, double* a, double* rdiag, double*
 }
 
 MFG_API int mfg_zgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -1386,10 +1436,12 @@ static int geqrs_batched(mfg_plan* plan, const T* a, const T* rdiag, T* b, int s
 extern "C" {
 
 MFG_API int mfg_dgeqrs_batched(mfg_plan* plan, const double* a, const double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return geqrs_batched<double>(plan, a, rdiag, b, 0);
 }
 
 MFG_API int mfg_sgeqrs_batched(mfg_plan* plan, const float* a, const float* rdiag, float* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return geqrs_batched<float>(plan, a, rdiag, b, 1);
 }
 
@@ -1581,32 +1633,40 @@ cudaError_t zgemm_l(int ta, int tb, int m, int n, int k, const void* a, int lda,
 extern "C" {
 
 MFG_API int mfg_sgetrf(mfg_ctx* ctx, int m, int n, float* a, int lda, int* piv, int* sign) {
+  DeviceScope device_scope_(ctx);
   return getrf_t(ctx, m, n, a, lda, piv, sign, sizeof(float), sgetrf_l);
 }
 MFG_API int mfg_zgetrf(mfg_ctx* ctx, int m, int n, double* a, int lda, int* piv, int* sign) {
+  DeviceScope device_scope_(ctx);
   return getrf_t(ctx, m, n, a, lda, piv, sign, 2 * sizeof(double), zgetrf_l);
 }
 MFG_API int mfg_spotrf(mfg_ctx* ctx, int n, float* a, int lda, int* info) {
+  DeviceScope device_scope_(ctx);
   return potrf_t(ctx, n, a, lda, info, sizeof(float), spotrf_l);
 }
 MFG_API int mfg_zpotrf(mfg_ctx* ctx, int n, double* a, int lda, int* info) {
+  DeviceScope device_scope_(ctx);
   return potrf_t(ctx, n, a, lda, info, 2 * sizeof(double), zpotrf_l);
 }
 MFG_API int mfg_strsv(mfg_ctx* ctx, int uplo, int trans, int n, const float* a, int lda, float* x,
                       int incx) {
+  DeviceScope device_scope_(ctx);
   return trsv_t(ctx, uplo, trans, n, a, lda, x, incx, sizeof(float), false, strsv_l);
 }
 MFG_API int mfg_ztrsv(mfg_ctx* ctx, int uplo, int trans, int n, const double* a, int lda,
                       double* x, int incx) {
+  DeviceScope device_scope_(ctx);
   return trsv_t(ctx, uplo, trans, n, a, lda, x, incx, 2 * sizeof(double), true, ztrsv_l);
 }
 MFG_API int mfg_sgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const float* a,
                       int lda, const float* b, int ldb, float* c, int ldc) {
+  DeviceScope device_scope_(ctx);
   return gemm_t(ctx, transa, transb, m, n, k, a, lda, b, ldb, c, ldc, sizeof(float), false,
                 sgemm_l);
 }
 MFG_API int mfg_zgemm(mfg_ctx* ctx, int transa, int transb, int m, int n, int k, const double* a,
                       int lda, const double* b, int ldb, double* c, int ldc) {
+  DeviceScope device_scope_(ctx);
   return gemm_t(ctx, transa, transb, m, n, k, a, lda, b, ldb, c, ldc, 2 * sizeof(double), true,
                 zgemm_l);
 }
@@ -1723,13 +1783,16 @@ int zqr_r_single(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r
 extern "C" {
 
 MFG_API int mfg_zgeqrf(mfg_ctx* ctx, int m, int n, double* a, int lda, double* rdiag) {
+  DeviceScope device_scope_(ctx);
   return zqr_single(ctx, m, n, a, lda, rdiag);
 }
 MFG_API int mfg_zorgqr(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* q, int ldq) {
+  DeviceScope device_scope_(ctx);
   return zqr_q_single(ctx, m, n, a, lda, q, ldq);
 }
 MFG_API int mfg_zqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, double* r, int ldr,
                       const double* rdiag) {
+  DeviceScope device_scope_(ctx);
   return zqr_r_single(ctx, m, n, a, lda, r, ldr, rdiag);
 }
 
@@ -1739,17 +1802,20 @@ MFG_API int mfg_zqr_r(mfg_ctx* ctx, int m, int n, const double* a, int lda, doub
 MFG_API int mfg_plan_getrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                    const int* lda, const int64_t* a_off, const int64_t* piv_off,
                                    int nrhs, const int64_t* b_off) {
+  DeviceScope device_scope_(ctx);
   return plan_create(ctx, plan, mfg_plan::GETRF, count, n, lda, a_off, piv_off, nrhs, b_off);
 }
 
 MFG_API int mfg_plan_potrf_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                    const int* lda, const int64_t* a_off, int nrhs,
                                    const int64_t* b_off) {
+  DeviceScope device_scope_(ctx);
   return plan_create(ctx, plan, mfg_plan::POTRF, count, n, lda, a_off, nullptr, nrhs, b_off);
 }
 
 MFG_API int mfg_plan_getri_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                    const int* lda, const int64_t* a_off, const int64_t* piv_off) {
+  DeviceScope device_scope_(ctx);
   return plan_create(ctx, plan, mfg_plan::GETRI, count, n, lda, a_off, piv_off, 0, nullptr);
 }
 
@@ -1777,13 +1843,16 @@ static int getri_batched_any(mfg_plan* plan, int elem, void* a, const int* piv, 
 extern "C" {
 
 MFG_API int mfg_sgetri_batched(mfg_plan* plan, float* a, const int* piv, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getri_batched_any(plan, 1, a, piv, info);
 }
 MFG_API int mfg_zgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getri_batched_any(plan, 2, a, piv, info);
 }
 
 MFG_API int mfg_dgetri_batched(mfg_plan* plan, double* a, const int* piv, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRI) return fail(ctx, -1, "plan is not a getri plan");
@@ -1806,6 +1875,7 @@ MFG_API int mfg_dgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, con
                                       int lda, int64_t stride_a, const double* x, int incx,
                                       int64_t stride_x, double* y, int incy, int64_t stride_y,
                                       int count) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   // Blas.MulMatVec's checks (Blas.MulMatVec.cs:140-183).
   if (m <= 0) return fail(ctx, -3, "The number of rows must be greater than or equal to one.");
@@ -1830,6 +1900,7 @@ MFG_API int mfg_dgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, con
 MFG_API int mfg_ddot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
                                      int64_t stride_x, const double* y, int incy,
                                      int64_t stride_y, double* result, int count) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (n <= 0) return fail(ctx, -2, "The length of the vector must be greater than or equal to one.");
   if (!x) return fail(ctx, -3, "x is null");
@@ -1845,6 +1916,7 @@ MFG_API int mfg_ddot_strided_batched(mfg_ctx* ctx, int n, const double* x, int i
 
 MFG_API int mfg_dnrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
                                       int64_t stride_x, double* result, int count) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (n <= 0) return fail(ctx, -2, "The length of the vector must be greater than or equal to one.");
   if (!x) return fail(ctx, -3, "x is null");
@@ -1860,6 +1932,7 @@ MFG_API int mfg_dger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x
                                      int64_t stride_x, const double* y, int incy,
                                      int64_t stride_y, double* a, int lda, int64_t stride_a,
                                      int count) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (m <= 0) return fail(ctx, -2, "The number of rows must be greater than or equal to one.");
   if (n <= 0) return fail(ctx, -3, "The number of columns must be greater than or equal to one.");
@@ -1953,6 +2026,7 @@ MFG_API int mfg_sgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, con
                                       int lda, int64_t stride_a, const float* x, int incx,
                                       int64_t stride_x, float* y, int incy, int64_t stride_y,
                                       int count) {
+  DeviceScope device_scope_(ctx);
   return gemv_strided_any(ctx, 1, trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy,
                           stride_y, count);
 }
@@ -1960,36 +2034,43 @@ MFG_API int mfg_zgemv_strided_batched(mfg_ctx* ctx, int trans, int m, int n, con
                                       int lda, int64_t stride_a, const double* x, int incx,
                                       int64_t stride_x, double* y, int incy, int64_t stride_y,
                                       int count) {
+  DeviceScope device_scope_(ctx);
   return gemv_strided_any(ctx, 2, trans, m, n, a, lda, stride_a, x, incx, stride_x, y, incy,
                           stride_y, count);
 }
 MFG_API int mfg_sdot_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
                                      int64_t stride_x, const float* y, int incy,
                                      int64_t stride_y, float* result, int count) {
+  DeviceScope device_scope_(ctx);
   return dot_strided_any(ctx, 1, 0, n, x, incx, stride_x, y, incy, stride_y, result, count);
 }
 MFG_API int mfg_zdot_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
                                      int64_t stride_x, const double* y, int incy,
                                      int64_t stride_y, double* result, int count) {
+  DeviceScope device_scope_(ctx);
   return dot_strided_any(ctx, 2, 0, n, x, incx, stride_x, y, incy, stride_y, result, count);
 }
 MFG_API int mfg_zdotc_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
                                       int64_t stride_x, const double* y, int incy,
                                       int64_t stride_y, double* result, int count) {
+  DeviceScope device_scope_(ctx);
   return dot_strided_any(ctx, 2, 2, n, x, incx, stride_x, y, incy, stride_y, result, count);
 }
 MFG_API int mfg_snrm2_strided_batched(mfg_ctx* ctx, int n, const float* x, int incx,
                                       int64_t stride_x, float* result, int count) {
+  DeviceScope device_scope_(ctx);
   return dot_strided_any(ctx, 1, 1, n, x, incx, stride_x, nullptr, 0, 0, result, count);
 }
 MFG_API int mfg_dznrm2_strided_batched(mfg_ctx* ctx, int n, const double* x, int incx,
                                        int64_t stride_x, double* result, int count) {
+  DeviceScope device_scope_(ctx);
   return dot_strided_any(ctx, 2, 1, n, x, incx, stride_x, nullptr, 0, 0, result, count);
 }
 MFG_API int mfg_sger_strided_batched(mfg_ctx* ctx, int m, int n, const float* x, int incx,
                                      int64_t stride_x, const float* y, int incy,
                                      int64_t stride_y, float* a, int lda, int64_t stride_a,
                                      int count) {
+  DeviceScope device_scope_(ctx);
   return ger_strided_any(ctx, 1, 0, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
                          stride_a, count);
 }
@@ -1997,6 +2078,7 @@ MFG_API int mfg_zger_strided_batched(mfg_ctx* ctx, int m, int n, const double* x
                                      int64_t stride_x, const double* y, int incy,
                                      int64_t stride_y, double* a, int lda, int64_t stride_a,
                                      int count) {
+  DeviceScope device_scope_(ctx);
   return ger_strided_any(ctx, 2, 0, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
                          stride_a, count);
 }
@@ -2004,6 +2086,7 @@ MFG_API int mfg_zgerc_strided_batched(mfg_ctx* ctx, int m, int n, const double* 
                                       int64_t stride_x, const double* y, int incy,
                                       int64_t stride_y, double* a, int lda, int64_t stride_a,
                                       int count) {
+  DeviceScope device_scope_(ctx);
   return ger_strided_any(ctx, 2, 1, m, n, x, incx, stride_x, y, incy, stride_y, a, lda,
                          stride_a, count);
 }
@@ -2011,6 +2094,7 @@ MFG_API int mfg_zgerc_strided_batched(mfg_ctx* ctx, int m, int n, const double* 
 MFG_API int mfg_plan_gevd_front_batched(mfg_ctx* ctx, mfg_plan** plan, int count, const int* n,
                                         const int* lda, const int64_t* a_off, const int* ldb,
                                         const int64_t* b_off, const int64_t* c_off) {
+  DeviceScope device_scope_(ctx);
   return plan_create_gevd(ctx, plan, count, n, lda, a_off, ldb, b_off, c_off);
 }
 
@@ -2039,18 +2123,22 @@ extern "C" {
 
 MFG_API int mfg_dgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_any(plan, 0, a, b, c, info);
 }
 MFG_API int mfg_sgevd_front_batched(mfg_plan* plan, const float* a, float* b, float* c,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_any(plan, 1, a, b, c, info);
 }
 MFG_API int mfg_zgevd_front_batched(mfg_plan* plan, const double* a, double* b, double* c,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_any(plan, 2, a, b, c, info);
 }
 
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF && plan->kind != mfg_plan::POTRF)
@@ -2163,6 +2251,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
 }
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   if (plan->exec) cudaGraphExecDestroy(plan->exec);
   cudaStreamSynchronize(plan->ctx->stream);
@@ -2280,25 +2369,31 @@ extern "C" {
 
 MFG_API int mfg_sgetrf_batched(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
                                int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrf_batched_any(plan, 1, a, piv, b, sign, info);
 }
 MFG_API int mfg_zgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrf_batched_any(plan, 2, a, piv, b, sign, info);
 }
 MFG_API int mfg_sgetrs_batched(mfg_plan* plan, const float* a, const int* piv, float* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrs_batched_any(plan, 1, a, piv, b);
 }
 MFG_API int mfg_zgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrs_batched_any(plan, 2, a, piv, b);
 }
 
 MFG_API int mfg_dgetrf_batched(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrf_batched_any(plan, 0, a, piv, b, sign, info);
 }
 
 MFG_API int mfg_dgetrs_batched(mfg_plan* plan, const double* a, const int* piv, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrs_batched_any(plan, 0, a, piv, b);
 }
 
@@ -2554,7 +2649,7 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
 }
 
 // Runs operation op on the caller's host arrays (in the order pipe_arrays lists them).
-int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> host) {
+int pipe_run_body(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> host) {
   mfg_ctx* ctx = p->ctx;
   auto& pp = p->pipe;
   if (pp.op != op) {
@@ -2673,12 +2768,26 @@ int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> 
   return MFG_OK;
 }
 
+// A host-buffer call returns only when none of its copies can still touch the caller's arrays:
+// on a failure part-way through, the copies and kernels queued for earlier chunks are drained
+// first (their own errors are ignored; the first failure is the one reported).
+int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> host) {
+  const int rc = pipe_run_body(p, op, keep_factor, host);
+  if (rc != MFG_OK) {
+    auto& pp = p->pipe;
+    for (cudaStream_t st : {pp.h2d, pp.comp[0], pp.comp[1], pp.comp[2], p->ctx->stream, pp.d2h})
+      if (st) cudaStreamSynchronize(st);
+  }
+  return rc;
+}
+
 }  // namespace
 
 extern "C" {
 
 MFG_API int mfg_dgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
@@ -2718,19 +2827,24 @@ static int potrf_host_any(mfg_plan* plan, int op, void* a, void* b, int* info) {
 
 MFG_API int mfg_sgetrf_batched_host(mfg_plan* plan, float* a, int* piv, float* b, int* sign,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrf_host_any(plan, OP_GETRF_S, a, piv, b, sign, info);
 }
 MFG_API int mfg_zgetrf_batched_host(mfg_plan* plan, double* a, int* piv, double* b, int* sign,
                                     int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return getrf_host_any(plan, OP_GETRF_Z, a, piv, b, sign, info);
 }
 MFG_API int mfg_spotrf_batched_host(mfg_plan* plan, float* a, float* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrf_host_any(plan, OP_POTRF_S, a, b, info);
 }
 MFG_API int mfg_zpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrf_host_any(plan, OP_POTRF_Z, a, b, info);
 }
 MFG_API int mfg_zgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -2742,6 +2856,7 @@ MFG_API int mfg_zgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, do
 }
 
 MFG_API int mfg_dpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
@@ -2755,6 +2870,7 @@ MFG_API int mfg_dpotrf_batched_host(mfg_plan* plan, double* a, double* b, int* i
 MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k, double* y,
                                                      double* loss, double* grad, int* info,
                                                      int keep_factor) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
@@ -2775,6 +2891,7 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched_host(mfg_plan* plan, double* k,
 }
 
 MFG_API int mfg_dgetri_batched_host(mfg_plan* plan, double* a, const int* piv, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRI) return fail(ctx, -1, "plan is not a getri plan");
@@ -2786,6 +2903,7 @@ MFG_API int mfg_dgetri_batched_host(mfg_plan* plan, double* a, const int* piv, i
 }
 
 MFG_API int mfg_dgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -2797,6 +2915,7 @@ MFG_API int mfg_dgeqrf_batched_host(mfg_plan* plan, double* a, double* rdiag, do
 }
 
 MFG_API int mfg_sgeqrf_batched_host(mfg_plan* plan, float* a, float* rdiag, float* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GEQRF) return fail(ctx, -1, "plan is not a geqrf plan");
@@ -2826,14 +2945,17 @@ extern "C" {
 
 MFG_API int mfg_dgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
                                          int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_host_any(plan, OP_GEVD, a, b, c, info);
 }
 MFG_API int mfg_sgevd_front_batched_host(mfg_plan* plan, const float* a, float* b, float* c,
                                          int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_host_any(plan, OP_GEVD_S, a, b, c, info);
 }
 MFG_API int mfg_zgevd_front_batched_host(mfg_plan* plan, const double* a, double* b, double* c,
                                          int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return gevd_front_host_any(plan, OP_GEVD_Z, a, b, c, info);
 }
 
@@ -2886,19 +3008,24 @@ int potrs_batched_any(mfg_plan* plan, int elem, const void* a, void* b) {
 extern "C" {
 
 MFG_API int mfg_spotrf_batched(mfg_plan* plan, float* a, float* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrf_batched_any(plan, 1, a, b, info);
 }
 MFG_API int mfg_zpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrf_batched_any(plan, 2, a, b, info);
 }
 MFG_API int mfg_spotrs_batched(mfg_plan* plan, const float* a, float* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrs_batched_any(plan, 1, a, b);
 }
 MFG_API int mfg_zpotrs_batched(mfg_plan* plan, const double* a, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   return potrs_batched_any(plan, 2, a, b);
 }
 
 MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
@@ -2919,6 +3046,7 @@ MFG_API int mfg_dpotrf_batched(mfg_plan* plan, double* a, double* b, int* info) 
 }
 
 MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
@@ -2940,6 +3068,7 @@ MFG_API int mfg_dpotrs_batched(mfg_plan* plan, const double* a, double* b) {
 
 MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
                               int64_t n) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (n < 0) return fail(ctx, -5, "n must be >= 0");
   if (n > 0 && (!a || !b || !out)) return fail(ctx, !a ? -2 : (!b ? -3 : -4), "null pointer");
@@ -2951,6 +3080,7 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
                                               int lda, int64_t stride_a, int* piv,
                                               int64_t stride_piv, int nrhs, double* b,
                                               int64_t stride_b, int* sign, int* info) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (n < 1) return fail(ctx, -2, "n must be >= 1");
   if (n > mfg::noalloc_max_n())
@@ -2970,14 +3100,15 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
   if (count > 0 && !sign) return fail(ctx, -12, "sign is null");
   if (count > 0 && !info) return fail(ctx, -13, "info is null");
   MFG_CUDA(ctx, mfg::launch_getrf_strided_noalloc(a, n, lda, stride_a, piv, stride_piv, nrhs, b,
-                                                  stride_b, sign, info, count, ctx->sm_count,
-                                                  ctx->stream));
+                                                  stride_b, sign, info, count, ctx->device,
+                                                  ctx->sm_count, ctx->stream));
   return MFG_OK;
 }
 
 MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, double* y,
                                                 double* loss, double* grad, int* info,
                                                 int keep_factor) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
@@ -3013,6 +3144,7 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
 // Mixed-precision LU solve with FP64 iterative refinement.
 
 MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n) {
+  DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
   if (!plan) return fail(ctx, -2, "plan output pointer is null");
   *plan = nullptr;
@@ -3050,6 +3182,7 @@ MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count
 MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const double* b, double* x,
                                     int lowp, int max_iter, double tol, double* berr,
                                     int* iters, int* info) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::MIXED) return fail(ctx, -1, "plan is not a mixed-precision plan");
@@ -3190,6 +3323,7 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
 }
 
 MFG_API int mfg_plan_status(mfg_plan* plan) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   MFG_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
   MFG_CUDA(plan->ctx, cudaGetLastError());

@@ -62,3 +62,26 @@ def test_python_facade_raises_without_device():
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
                          timeout=120)
     assert out.stdout.strip() == "raised", out.stdout + out.stderr
+
+
+def test_every_status_code_is_returned_somewhere():
+    """Each MFG_ERR_* status the header declares is produced by some code path of the library
+    (named in code, not only in comments): the ABI promises no status that can never occur."""
+    header = open(os.path.join(ROOT, "include", "matflat_gpu.h")).read()
+    codes = set(re.findall(r"\b(MFG_ERR_\w+)\s*=", header))
+    assert codes, "no status codes found"
+    src = ""
+    for f in glob.glob(os.path.join(ROOT, "matflat_gb300", "csrc", "*.cu")):
+        text = re.sub(r"/\*.*?\*/", "", open(f).read(), flags=re.S)
+        src += re.sub(r"//[^\n]*", "", text)
+    unused = [c for c in sorted(codes) if not re.search(r"\b%s\b" % c, src)]
+    assert not unused, unused
+
+
+def test_library_package_is_torch_free_and_loads_no_workload_helper():
+    """The product package imports neither torch nor the benchmark's input generator."""
+    for f in glob.glob(os.path.join(ROOT, "matflat_gb300", "*.py")):
+        text = open(f).read()
+        assert not re.search(r"^\s*(import torch|from torch)", text, re.M), f
+        assert not re.search(r"^\s*(import workloads|from workloads)", text, re.M), f
+        assert "libworkloads_synth" not in text, f

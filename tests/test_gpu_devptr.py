@@ -93,3 +93,32 @@ def test_device_arrays_match_host_arrays(mf):
     assert lib.mfg_zgetrf(ctx.h, m, n, _vp(dz), m, _vp(dzp), ctypes.byref(sign)) == 0
     assert_bits(dz.cpu().numpy(), hz.view(np.float64))
     np.testing.assert_array_equal(dzp.cpu().numpy(), hzp)
+
+
+def test_context_runs_on_its_device_and_restores_the_callers(mf):
+    """Every call runs on the context's device and leaves the caller's current device as it
+    was.  With one visible GPU the switch itself cannot be exercised: the test checks the
+    device the context reports, that a call made while another device id was current on the
+    host thread still computes correctly (when a second device exists), and that the caller's
+    device is unchanged after the call."""
+    import torch
+    ctx = mf.context()
+    dev = ctx.device()
+    assert dev == torch.cuda.current_device()
+    rng = np.random.default_rng(77)
+    n = 24
+    a = rng.standard_normal(n * n)
+    ref, rpiv = a.copy(), np.zeros(n, np.int32)
+    rsign = mf.Factorization.Lu(n, n, ref, n, rpiv)
+    other = (dev + 1) % torch.cuda.device_count()
+    prev = torch.cuda.current_device()
+    torch.cuda.set_device(other)
+    try:
+        got, gpiv = a.copy(), np.zeros(n, np.int32)
+        gsign = mf.Factorization.Lu(n, n, got, n, gpiv)
+        assert torch.cuda.current_device() == other
+    finally:
+        torch.cuda.set_device(prev)
+    assert_bits(got, ref)
+    np.testing.assert_array_equal(gpiv, rpiv)
+    assert gsign == rsign

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from matflat_gb300 import synth
+from workloads import synth
 
 pytestmark = pytest.mark.gpu
 

@@ -69,7 +69,7 @@ def test_host_pipeline_other_operations(mf):
     """Every batched operation's host-buffer form equals its device-buffer form bit for bit
     (batches above 8,192 matrices, so the pipeline has at least two chunks)."""
     import torch
-    from matflat_gb300 import synth
+    from workloads import synth
     count = 9000
     # Cholesky + solve
     d = synth.spd_batch(count, 24, nrhs=1, seed=5)

@@ -4,7 +4,7 @@ conditioning allows."""
 import numpy as np
 import pytest
 
-from matflat_gb300 import synth
+from workloads import synth
 
 pytestmark = pytest.mark.gpu
 

@@ -3,7 +3,7 @@ against the closed form K^-1 - alpha alpha^T and against central finite differen
 import numpy as np
 
 from oracle import oracle
-from matflat_gb300 import synth
+from workloads import synth
 
 
 def _loss_grad(K, y):

@@ -1,6 +1,6 @@
 """Seeded synthetic batches with the shapes of the reference's benchmark configurations.
 
-Host-side generation (libmatflat_synth.so, counter-based SplitMix64 + Box-Muller), so the GPU
+Host-side generation (libworkloads_synth.so, counter-based SplitMix64 + Box-Muller), so the GPU
 path and the CPU oracle see identical bytes.  Every batch is packed: matrix i is column-major with
 leading dimension equal to its row count, at element offset a_off[i].
 """
@@ -17,10 +17,7 @@ _lib = None
 def _synth():
     global _lib
     if _lib is None:
-        path = _build.SYNTH_LIB
-        if not os.path.exists(path):
-            path = _build.build_synth()
-        lib = ctypes.CDLL(path)
+        lib = ctypes.CDLL(_build.build())
         lib.mfs_normal.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
         lib.mfs_uniform.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64,
