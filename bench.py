@@ -439,7 +439,7 @@ def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, 
     solver = mf.MixedSolveBatch(count, n)
 
     def run():
-        solver.run(a, b, x, berr, iters, info, lowp=lowp, max_iter=10, tol=1e-12)
+        solver.run(a, b, x, berr, iters, info, lowp=lowp, max_iter=10, tol=1e-12, sync=False)
 
     with torch.cuda.stream(stream):
         for _ in range(warmup):
@@ -455,6 +455,7 @@ def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, 
         t1.record(stream)
         stream.synchronize()
         clocks.stop()
+    solver.status()
     ms = t0.elapsed_time(t1) / steps
 
     # End to end through the C ABI: A and b from pinned host memory, x, berr, iters and info
@@ -484,6 +485,7 @@ def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, 
                     th.copy_(t, non_blocking=True)
             q1.record(stream)
             stream.synchronize()
+        solver.status()
         e2e_ms = q0.elapsed_time(q1) / steps
         e2e = {"value": count / (e2e_ms / 1e3), "unit": "solves/s",
                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in ins)),

@@ -59,7 +59,8 @@ enum mfg_status {
   MFG_ERR_ALLOC = -1002,       /* device or pinned allocation failed */
   MFG_ERR_INPLACE = -1003,     /* MulMatMat: a == c or b == c ("In-place operation is not
                                   supported.", Blas.MulMatMat.cs:301-304) */
-  /* -1004 is not used: no kernel of this library waits on another (see mfg_plan_status) */
+  MFG_ERR_TIMEOUT = -1004,     /* a bounded device-side wait of the mixed solver's tensor-core
+                                  update gave up; reported by mfg_plan_status */
   MFG_ERR_UNSUPPORTED = -1005  /* size or option outside what the library supports */
 };
 
@@ -415,13 +416,16 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
  * A plan for `count` systems of one order n (a multiple of 32, at most 1024); matrices packed
  * column-major with lda = n at stride n*n, right-hand sides and solutions at stride n.
  * The solver factors FP32 copies of A with partial pivoting (trailing updates on the tensor cores
- * in TF32 or BF16 with FP32 accumulation, or on the FP32 cores), then refines in FP64:
+ * in TF32 or BF16 with FP32 accumulation, hand-written tcgen05 + TMA, or on the FP32 cores),
+ * then refines in FP64:
  * r = b - A x, d = (LU)^-1 r in FP32, x += d, until the normwise backward error
  * berr = |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) <= tol, stalls, or max_iter sweeps pass.
  * Systems that do not converge are solved again with the exact FP64 LU (Factorization.Lu's
  * arithmetic).  Outputs per system: x, berr, iters (refinement sweeps), info (0 refined to tol,
  * 1 solved by the FP64 fallback, 2 singular).  a, b, x, berr, iters and info are device
- * pointers; the call returns after the results are complete. */
+ * pointers.  The call is asynchronous on the context's stream and allocates nothing: the plan owns
+ * the FP32 factors, the operand copies and the fallback's buffers (about 12 n^2 count bytes +
+ * the FP64 fallback copy of A, 8 n^2 count bytes).  Check mfg_plan_status after it. */
 enum mfg_lowp { MFG_LOWP_FP32 = 0, MFG_LOWP_TF32 = 1, MFG_LOWP_BF16 = 2 };
 MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n);
 MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const double* b, double* x,
@@ -441,10 +445,12 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 
-/* Waits for the context's stream and reports an asynchronous CUDA failure of the work queued so
- * far (including the last execution of `plan`): MFG_OK or MFG_ERR_CUDA (text in mfg_last_error).
- * Numerical failures are not statuses: they are in the `info` arrays.  No kernel of this library
- * waits on another, so no call reports a timeout. */
+/* Waits for the context's stream and reports an asynchronous failure of the work queued so far
+ * (including the last execution of `plan`): MFG_OK, MFG_ERR_CUDA (text in mfg_last_error), or,
+ * for a mixed-precision plan, MFG_ERR_TIMEOUT when one of the tensor-core update's bounded waits
+ * (TMA tile arrival, tensor-core completion; 0.2 s each) gave up, in which case that execution's
+ * solutions are not valid (the status is cleared by reading it).  Numerical failures are not
+ * statuses: they are in the `info` arrays. */
 MFG_API int mfg_plan_status(mfg_plan* plan);
 
 /* Allocation-free batched LU + solve (no counterpart in the reference: MatFlat has no batched

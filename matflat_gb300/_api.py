@@ -816,8 +816,13 @@ class MixedSolveBatch(_Batch):
         self.count = count
         self.n = n
 
-    def run(self, a, b, x, berr, iters, info, lowp="tf32", max_iter=10, tol=1e-12):
+    def run(self, a, b, x, berr, iters, info, lowp="tf32", max_iter=10, tol=1e-12, sync=True):
+        """Solves on the context's stream.  With sync (the default) the call waits for the
+        results and raises if a bounded device-side wait of the tensor-core update gave up
+        (mfg_plan_status); with sync=False it returns at once and status() checks later."""
         rc = self.ctx.lib.mfg_dgesv_mixed_batched(self.h, _dptr(a), _dptr(b), _dptr(x),
                                                   LOWP[lowp], max_iter, tol, _dptr(berr),
                                                   _dptr(iters), _dptr(info))
         self.ctx.check(rc, "mfg_dgesv_mixed_batched")
+        if sync:
+            self.status()

@@ -60,7 +60,7 @@ def build(force=False, verbose=False, extra_flags=()):
                 if r.returncode != 0:
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcublas", "-lcudart_static",
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart_static",
                                                                         "-lrt", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -187,11 +187,12 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_batched_kernel(BatchArgs p) 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const long long gw = (long long)blockIdx.x * WARPS + warp;
+  const int count = p.dcount ? *p.dcount : p.count;
   for (;;) {
     int idx = 0;
     if (lane == 0) idx = atomicAdd(p.queue, 1);
     idx = __shfl_sync(FULL_MASK, idx, 0);
-    if (idx >= p.count) break;
+    if (idx >= count) break;
     const int mat = p.order[idx];
     const int n = p.n[mat];
     const long long lda = p.lda[mat];

@@ -42,6 +42,9 @@ struct BatchArgs {
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
   int split;                 // potrf: split every dot in two halves a step apart
                              // (potrf_group_split; 4n doubles of per-group scratch)
+  const int* dcount;         // getrf: when set, the number of matrices to take from `order` is
+                             // read from device memory (a list built on the device); count
+                             // stays the upper bound the grid was sized for
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and
@@ -178,12 +181,25 @@ cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long st
 int mx_panel_width();
 cudaError_t mx_panel_attr(int nmax);
 cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t s);
+// opfmt: 0 no operand copies (FP32 mode), 1 TF32 (FP32 storage), 2 BF16; R = mx_op_rows(n).
 cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
-                     cudaStream_t s);
+                     void* op_a, void* op_b, int opfmt, int R, cudaStream_t s);
 cudaError_t mx_update_fp32(float* a32, int n, int k, const int* active, int count,
                            cudaStream_t s);
-cudaError_t mx_bf16_operands(const float* a32, int n, int k, void* l21, void* u12,
-                             const int* active, int count, cudaStream_t s);
+int mx_op_rows(int n);
+}  // namespace mfg
+struct CUtensorMap_st;
+namespace mfg {
+// Tensor-core trailing update (tcgen05 + TMA); the maps describe the operand copies.  *status is
+// set when a bounded device-side wait gives up.
+cudaError_t mx_make_tensor_maps(void* op_a, void* op_b, int n, int count, bool tf32,
+                                CUtensorMap_st* tm_a, CUtensorMap_st* tm_b);
+cudaError_t mx_update_tc(const CUtensorMap_st* tm_a, const CUtensorMap_st* tm_b, float* a32,
+                         int n, int k, bool tf32, int count, int* status, cudaStream_t s);
+// The exact FP64 fallback of the systems that did not converge, on the device.
+cudaError_t mx_fb_gather(const double* a, const double* b, double* x, double* fa, const int* state,
+                         int n, int count, int* order, int* fb_count, cudaStream_t s);
+cudaError_t mx_fb_finish(int* state, int* info, const int* fb_info, int count, cudaStream_t s);
 cudaError_t mx_refine(const double* a, const double* b, double* x, const float* lu,
                       const int* ipiv, int n, int count, int iter, double tol, double* berr,
                       int* iters, int* state, double* anorm, int* active, cudaStream_t s);

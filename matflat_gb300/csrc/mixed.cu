@@ -4,20 +4,29 @@
 //   1. rounds A to FP32 and factors it with partial pivoting, blocked right-looking with panel
 //      width NB: a panel kernel (one CTA per matrix) factors the (n-k)-by-NB panel in shared
 //      memory, applies its row interchanges to the rest of the matrix and forms
-//      U12 = L11^-1 A12; the trailing update A22 -= L21 U12 is one strided-batched GEMM over the
-//      whole batch on the tensor cores (TF32 or BF16 inputs, FP32 accumulation) or, in the FP32
-//      mode, on the FP32 cores;
+//      U12 = L11^-1 A12, and writes K-major copies of L21 and U12 in the low precision; the
+//      trailing update A22 -= L21 U12 is one launch over the whole batch on the tensor cores
+//      (mx_update_tc_kernel: TMA tile loads, tcgen05.mma kind::tf32 or kind::f16 with BF16
+//      inputs, FP32 accumulators in Tensor Memory) or, in the FP32 mode, on the FP32 cores;
 //   2. solves with the FP32 factors, then refines in FP64: r = b - A x with A in FP64,
 //      d = (LU)^-1 r in FP32, x += d, until the normwise backward error
 //      berr = |r|_inf / (|A|_inf |x|_inf + |b|_inf) reaches tol or stops halving (stall);
-//   3. hands the systems that did not converge to the exact FP64 LU (MatFlat's arithmetic).
+//   3. hands the systems that did not converge to the exact FP64 LU (MatFlat's arithmetic), all on
+//      the device: the systems are gathered into a buffer the plan owns and factored by the
+//      batched FP64 kernel over a device-side list, so a solve allocates nothing and never waits
+//      on the host.
 // The low-precision factorization is not MatFlat's arithmetic and makes no bit-exactness claim;
 // the contract is the FP64 backward error, reported per system.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "mf_device.cuh"
 #include "mf_kernels.h"
+#include "mf_tc.cuh"
 
 namespace mfg {
 
@@ -35,8 +44,23 @@ __global__ void mx_round_kernel(const double* __restrict__ a, float* __restrict_
 // Panel step k for one matrix per CTA: factor rows [k, n) x columns [k, k+NB) with partial
 // pivoting in shared memory, write ipiv (LAPACK convention: row k+j was swapped with ipiv[k+j]),
 // apply the interchanges to the other columns, and overwrite A12 with U12 = L11^-1 A12.
+// Low-precision operand copies for the tensor-core update, K-major: row i of L21 (global row
+// k+NB+i) at op_a[(mat*R + i)*NB ...], column j of U12 (global column k+NB+j) at
+// op_b[(mat*R + j)*NB ...]; R rows per system.  opfmt 0: none (FP32 mode), 1: FP32 storage of
+// the TF32-rounded value, 2: BF16.
+__device__ __forceinline__ void mx_store_op(void* op, long long idx, float v, int opfmt) {
+  if (opfmt == 1) {
+    uint32_t t;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+    reinterpret_cast<uint32_t*>(op)[idx] = t;
+  } else {
+    reinterpret_cast<__nv_bfloat16*>(op)[idx] = __float2bfloat16_rn(v);
+  }
+}
+
 __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n, int k, int* ipiv,
-                                                              const int* active) {
+                                                              const int* active, void* op_a,
+                                                              void* op_b, int opfmt, int R) {
   extern __shared__ float sp[];  // panel: (n-k) rows x NB columns, leading dimension ldp
   __shared__ float red_v[MX_THREADS / 32];
   __shared__ int red_i[MX_THREADS / 32];
@@ -114,6 +138,14 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
     a[(long long)(k + c) * n + k + r] = sp[c * ldp + r];
   }
   for (int j = tid; j < MX_NB; j += MX_THREADS) ip[k + j] = k + piv_s[j];
+  if (opfmt != 0) {
+    // L21, K-major: consecutive threads write consecutive K values of a row.
+    const long long base = (long long)mat * R * MX_NB;
+    for (int e = tid; e < (rows - MX_NB) * MX_NB; e += MX_THREADS) {
+      const int i = e / MX_NB, c = e - i * MX_NB;
+      mx_store_op(op_a, base + e, sp[c * ldp + MX_NB + i], opfmt);
+    }
+  }
   __syncthreads();
   // Interchanges on the columns left and right of the panel, in order.
   for (int c = tid; c < n; c += MX_THREADS) {
@@ -145,24 +177,10 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
         us[i * MX_THREADS] = fmaf(-lt[i], ut, us[i * MX_THREADS]);
     }
     for (int i = 0; i < MX_NB; ++i) col[i] = us[i * MX_THREADS];
-  }
-}
-
-// BF16 copies of L21 (rows [k+NB, n) x NB) and U12 (NB x columns [k+NB, n)) for the BF16 GEMM.
-__global__ void mx_bf16_operands_kernel(const float* a32, int n, int k, __nv_bfloat16* l21,
-                                        __nv_bfloat16* u12, const int* active) {
-  const int mat = blockIdx.y;
-  if (active && !active[mat]) return;
-  const float* a = a32 + (long long)mat * n * n;
-  const int m2 = n - k - MX_NB;
-  __nv_bfloat16* l = l21 + (long long)mat * n * MX_NB;
-  __nv_bfloat16* u = u12 + (long long)mat * n * MX_NB;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m2 * MX_NB;
-       e += gridDim.x * blockDim.x) {
-    const int c = e / m2, r = e - c * m2;
-    l[(long long)c * m2 + r] = __float2bfloat16_rn(a[(long long)(k + c) * n + k + MX_NB + r]);
-    const int uc = e / MX_NB, ur = e - uc * MX_NB;
-    u[(long long)uc * MX_NB + ur] = __float2bfloat16_rn(a[(long long)(k + MX_NB + uc) * n + k + ur]);
+    if (opfmt != 0) {
+      const long long base = ((long long)mat * R + (c - k - MX_NB)) * MX_NB;
+      for (int i = 0; i < MX_NB; ++i) mx_store_op(op_b, base + i, us[i * MX_THREADS], opfmt);
+    }
   }
 }
 
@@ -395,9 +413,9 @@ cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t 
 }
 
 cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
-                     cudaStream_t s) {
+                     void* op_a, void* op_b, int opfmt, int R, cudaStream_t s) {
   const size_t smem = sizeof(float) * ((size_t)(n - k) * MX_NB + (size_t)MX_NB * MX_THREADS);
-  mx_panel_kernel<<<count, MX_THREADS, smem, s>>>(a32, n, k, ipiv, active);
+  mx_panel_kernel<<<count, MX_THREADS, smem, s>>>(a32, n, k, ipiv, active, op_a, op_b, opfmt, R);
   return cudaGetLastError();
 }
 
@@ -416,22 +434,215 @@ cudaError_t mx_update_fp32(float* a32, int n, int k, const int* active, int coun
   return cudaGetLastError();
 }
 
-cudaError_t mx_bf16_operands(const float* a32, int n, int k, void* l21, void* u12,
-                             const int* active, int count, cudaStream_t s) {
-  const int m2 = n - k - MX_NB;
-  if (m2 <= 0) return cudaSuccess;
-  const int blocks = (m2 * MX_NB + 255) / 256;
-  mx_bf16_operands_kernel<<<dim3(blocks, count), 256, 0, s>>>(
-      a32, n, k, (__nv_bfloat16*)l21, (__nv_bfloat16*)u12, active);
-  return cudaGetLastError();
-}
-
 cudaError_t mx_refine(const double* a, const double* b, double* x, const float* lu,
                       const int* ipiv, int n, int count, int iter, double tol, double* berr,
                       int* iters, int* state, double* anorm, int* active, cudaStream_t s) {
   const size_t smem = sizeof(double) * (size_t)n + sizeof(float) * (size_t)n;
   mx_refine_kernel<<<count, MX_RT, smem, s>>>(a, b, x, lu, ipiv, n, count, iter, tol, berr,
                                               iters, state, anorm, active);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Trailing update on the tensor cores: A22 -= L21 U12 for every system, one CTA of 4 warps per
+// 128 x 128 tile of A22 (grid: systems x tiles^2).  Thread 0 loads the tile's 128 rows of L21
+// and 128 columns of U12 (K = NB = 32 low-precision values each, K-major) with two TMA copies,
+// issues the tcgen05.mma steps (4 of K = 8 for TF32, 2 of K = 16 for BF16) into a 128-column FP32
+// accumulator in Tensor Memory and commits them to an mbarrier; then each warp reads its 32 lanes
+// (rows) of the accumulator with tcgen05.ld and subtracts them from A22 in global memory, one
+// coalesced column segment per load.  Waits are bounded; a wait that runs out sets *status.
+constexpr uint64_t MX_TC_WAIT_NS = 200000000ull;  // 0.2 s
+constexpr int MX_TC_TILE = 128;
+
+struct MxTcArgs {
+  float* a32;
+  int n, k, m2, tiles;
+  int* status;
+};
+
+template <bool TF32>
+__global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant__ CUtensorMap tm_a,
+                                                          const __grid_constant__ CUtensorMap tm_b,
+                                                          MxTcArgs p) {
+  constexpr int ROWB = TF32 ? 128 : 64;          // bytes of one operand row (32 values)
+  constexpr uint32_t SBO = 8 * ROWB;             // 8-row swizzle atom
+  constexpr uint32_t SWZ = TF32 ? 2 : 4;         // 128-byte / 64-byte swizzle
+  constexpr int KSTEPS = TF32 ? 4 : 2;           // 32 bytes of K per tcgen05.mma
+  constexpr uint32_t IDESC =
+      tc::instr_desc(TF32 ? tc::FMT_TF32 : tc::FMT_BF16, MX_TC_TILE, MX_TC_TILE);
+  extern __shared__ uint8_t mx_tc_smem[];
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(mx_tc_smem) + 1023) & ~(uintptr_t)1023);
+  uint8_t* sa = base;
+  uint8_t* sb = base + MX_TC_TILE * ROWB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sb + MX_TC_TILE * ROWB);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
+  int* issued = reinterpret_cast<int*>(slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int z = blockIdx.x;
+  const int ti = blockIdx.y % p.tiles, tj = blockIdx.y / p.tiles;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::mbar_fence_init();
+    *issued = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(slot, MX_TC_TILE);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *slot;
+  if (threadIdx.x == 0) {
+    tc::mbar_expect_tx(&bar[0], 2 * MX_TC_TILE * ROWB);
+    tc::tma_load_3d(sa, &tm_a, &bar[0], 0, ti * MX_TC_TILE, z);
+    tc::tma_load_3d(sb, &tm_b, &bar[0], 0, tj * MX_TC_TILE, z);
+    if (tc::mbar_wait(&bar[0], 0, MX_TC_WAIT_NS)) {
+      const uint64_t ad = tc::smem_desc(sa, SBO, SWZ);
+      const uint64_t bd = tc::smem_desc(sb, SBO, SWZ);
+#pragma unroll
+      for (int s = 0; s < KSTEPS; ++s)      // +32 bytes of K: +2 in the encoded start address
+        tc::mma<TF32>(tmem, ad + 2 * s, bd + 2 * s, IDESC, s > 0 ? 1u : 0u);
+      tc::mma_commit(&bar[1]);
+      *issued = 1;
+    } else {
+      tc::mbar_wait(&bar[0], 0, MX_TC_WAIT_NS);   // let the copies land before leaving
+      atomicExch(p.status, 1);
+    }
+  }
+  __syncthreads();
+  bool ready = false;
+  if (*issued) {
+    ready = tc::mbar_wait(&bar[1], 0, MX_TC_WAIT_NS);
+    if (!ready) atomicExch(p.status, 2);
+  }
+  ready = __syncthreads_and(ready ? 1 : 0) != 0;
+  tc::fence_after_sync();
+  if (ready) {
+    const int row = ti * MX_TC_TILE + warp * 32 + lane;
+    float* c0 = p.a32 + (long long)z * p.n * p.n + (long long)(p.k + 32) * p.n + (p.k + 32);
+#pragma unroll 1
+    for (int c = 0; c < MX_TC_TILE / 32; ++c) {
+      uint32_t r[32];
+      tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+      const int col0 = tj * MX_TC_TILE + c * 32;
+      if (row < p.m2) {
+        float* dst = c0 + (long long)col0 * p.n + row;
+        const int ncol = min(32, p.m2 - col0);
+#pragma unroll
+        for (int q = 0; q < 32; ++q)
+          if (q < ncol) dst[(long long)q * p.n] -= __uint_as_float(r[q]);
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, MX_TC_TILE);
+  }
+}
+
+// Shared memory of the update kernel: a 1024-byte alignment margin, the two operand tiles, two
+// mbarriers, the TMEM address slot and a flag.
+static size_t mx_tc_smem_bytes(bool tf32) {
+  return 1024 + 2 * MX_TC_TILE * (tf32 ? 128 : 64) + 64;
+}
+
+cudaError_t mx_update_tc(const CUtensorMap* tm_a, const CUtensorMap* tm_b, float* a32, int n,
+                         int k, bool tf32, int count, int* status, cudaStream_t s) {
+  const int m2 = n - k - MX_NB;
+  if (m2 <= 0 || count == 0) return cudaSuccess;
+  const int tiles = (m2 + MX_TC_TILE - 1) / MX_TC_TILE;
+  MxTcArgs p{a32, n, k, m2, tiles, status};
+  const dim3 grid((unsigned)count, (unsigned)(tiles * tiles));
+  if (tf32)
+    mx_update_tc_kernel<true><<<grid, 128, mx_tc_smem_bytes(true), s>>>(*tm_a, *tm_b, p);
+  else
+    mx_update_tc_kernel<false><<<grid, 128, mx_tc_smem_bytes(false), s>>>(*tm_a, *tm_b, p);
+  return cudaGetLastError();
+}
+
+// Rows per system of the operand copies: the tiles read 128-row boxes, so the copies are padded
+// to a multiple of 128 rows (rows past the system's trailing block are read but never stored).
+int mx_op_rows(int n) { return (n + MX_TC_TILE - 1) / MX_TC_TILE * MX_TC_TILE; }
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  });
+  return fn;
+}
+
+// TMA descriptors of the two operand copies: 3-D (K = 32 values, R rows, count systems), boxes of
+// 32 x 128 x 1, 128-byte (TF32) or 64-byte (BF16) swizzle.
+cudaError_t mx_make_tensor_maps(void* op_a, void* op_b, int n, int count, bool tf32,
+                                CUtensorMap* tm_a, CUtensorMap* tm_b) {
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return cudaErrorNotSupported;
+  const cuuint64_t es = tf32 ? 4 : 2;
+  const int R = mx_op_rows(n);
+  const cuuint64_t dims[3] = {(cuuint64_t)MX_NB, (cuuint64_t)R, (cuuint64_t)count};
+  const cuuint64_t strides[2] = {MX_NB * es, (cuuint64_t)R * MX_NB * es};
+  const cuuint32_t box[3] = {(cuuint32_t)MX_NB, (cuuint32_t)MX_TC_TILE, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt =
+      tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  const CUtensorMapSwizzle sw = tf32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  void* ops[2] = {op_a, op_b};
+  CUtensorMap* maps[2] = {tm_a, tm_b};
+  for (int i = 0; i < 2; ++i) {
+    const CUresult r = encode(maps[i], dt, 3, ops[i], dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------------------------
+// The exact FP64 fallback, on the device.  Systems whose refinement did not converge
+// (state != 1) are copied into the plan's fallback buffer (A) and into x (b, solved in place),
+// and listed in `order` (count in *fb_count); the batched FP64 LU then runs over that list.
+__global__ void mx_fb_gather_kernel(const double* a, const double* b, double* x, double* fa,
+                                    const int* state, int n, int* order, int* fb_count) {
+  const int i = blockIdx.x;
+  if (state[i] == 1) return;
+  if (threadIdx.x == 0) order[atomicAdd(fb_count, 1)] = i;
+  const long long nn = (long long)n * n;
+  const double* src = a + i * nn;
+  double* dst = fa + i * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) dst[e] = src[e];
+  for (int e = threadIdx.x; e < n; e += blockDim.x) x[(long long)i * n + e] = b[(long long)i * n + e];
+}
+
+// info / state per system: 0 refined to the tolerance, 1 solved by the FP64 fallback, 2 the
+// FP64 factor is singular.
+__global__ void mx_fb_finish_kernel(int* state, int* info, const int* fb_info, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int v = state[i] == 1 ? 0 : (fb_info[i] != 0 ? 2 : 1);
+  info[i] = v;
+  state[i] = v;
+}
+
+cudaError_t mx_fb_gather(const double* a, const double* b, double* x, double* fa, const int* state,
+                         int n, int count, int* order, int* fb_count, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  mx_fb_gather_kernel<<<count, 256, 0, s>>>(a, b, x, fa, state, n, order, fb_count);
+  return cudaGetLastError();
+}
+
+cudaError_t mx_fb_finish(int* state, int* info, const int* fb_info, int count, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  mx_fb_finish_kernel<<<(count + 255) / 256, 256, 0, s>>>(state, info, fb_info, count);
   return cudaGetLastError();
 }
 

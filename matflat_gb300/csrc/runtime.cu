@@ -3,7 +3,7 @@
 //
 // Argument validation mirrors MatFlat's checks, in MatFlat's order, and reports the 1-based
 // position of the offending argument as a negative status (the context is argument 1).
-#include <cublas_v2.h>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -78,7 +78,6 @@ cudaError_t g_attr_err[64];
 }  // namespace
 
 struct mfg_ctx {
-  cublasHandle_t cublas = nullptr;  // created on first use (mixed-precision trailing updates)
   int device = 0;
   int sm_count = 0;
   cudaStream_t own_stream = nullptr;
@@ -130,7 +129,9 @@ struct mfg_plan {
   int ctas_t = 0;    // GEVD: the grid of the float / Complex kernel
   long long dstride = 0;  // GETRF/POTRF: the double kernels' per-group scratch stride
   int mx_n = 0;      // MIXED: order of every matrix
-  DevBuf mx_work;    // MIXED: FP32 factors | ipiv | BF16 operands | per-system state
+  DevBuf mx_work;    // MIXED: FP32 factors | ipiv | operand copies | per-system state | fallback
+  mfg_plan* mx_fb = nullptr;  // MIXED: the exact FP64 LU plan of the fallback (all systems)
+  alignas(64) CUtensorMap mx_tm[4];  // MIXED: TMA maps of the operand copies (TF32 A, B; BF16)
   int ctas = 0;
   int warps = 0;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
@@ -838,6 +839,7 @@ struct Carve {
     return r;
   }
   static size_t bytes_for(size_t count, size_t elem) { return ((count * elem + 255) / 256) * 256; }
+  size_t used() const { return off; }
 };
 
 }  // namespace
@@ -876,7 +878,6 @@ MFG_API int mfg_destroy(mfg_ctx* ctx) {
   if (!ctx) return -1;
   DeviceScope device_scope_(ctx);
   cudaStreamSynchronize(ctx->stream);
-  if (ctx->cublas) cublasDestroy(ctx->cublas);
   ctx->work.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -2259,6 +2260,7 @@ MFG_API int mfg_plan_destroy(mfg_plan* plan) {
   plan->meta.release();
   plan->scratch.release();
   plan->gsolve.release();
+  if (plan->mx_fb) mfg_plan_destroy(plan->mx_fb);
   plan->mx_work.release();
   delete plan;
   return MFG_OK;
@@ -3143,6 +3145,83 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
 // ------------------------------------------------------------------------------------------
 // Mixed-precision LU solve with FP64 iterative refinement.
 
+}  // extern "C"
+
+namespace {
+// Workspace layout of a mixed plan (one allocation at plan creation; nothing is allocated by a
+// solve).
+struct MixedLayout {
+  float* a32;
+  int* ipiv;
+  void* op_a;
+  void* op_b;
+  double* anorm;
+  int* state;
+  int* active;
+  int* status;      // set by a bounded device-side wait that gave up
+  double* fb_a;     // fallback: copies of the systems that did not converge
+  int* fb_piv;
+  int* fb_sign;
+  int* fb_info;
+  int* fb_order;
+  int* fb_count;
+};
+
+MixedLayout mixed_layout(void* base, int count, int n, size_t* bytes) {
+  Carve cv(base);
+  const size_t nn = (size_t)n * n * count;
+  const size_t ops = (size_t)mfg::mx_op_rows(n) * mfg::mx_panel_width() * count;
+  MixedLayout L;
+  L.a32 = cv.take<float>(nn);
+  L.ipiv = cv.take<int>((size_t)n * count);
+  L.op_a = cv.take<float>(ops);
+  L.op_b = cv.take<float>(ops);
+  L.anorm = cv.take<double>(count);
+  L.state = cv.take<int>(count);
+  L.active = cv.take<int>(count);
+  L.status = cv.take<int>(64);
+  L.fb_a = cv.take<double>(nn);
+  L.fb_piv = cv.take<int>((size_t)n * count);
+  L.fb_sign = cv.take<int>(count);
+  L.fb_info = cv.take<int>(count);
+  L.fb_order = cv.take<int>(count);
+  L.fb_count = cv.take<int>(64);
+  if (bytes) *bytes = cv.used();
+  return L;
+}
+
+int mixed_plan_setup(mfg_ctx* ctx, mfg_plan* p) {
+  const int n = p->mx_n, count = p->count;
+  size_t bytes = 0;
+  mixed_layout(nullptr, count, n, &bytes);
+  MFG_CUDA(ctx, p->mx_work.reserve(bytes + 256));
+  MFG_CUDA(ctx, cudaMemset(p->mx_work.ptr, 0, bytes + 256));
+  MFG_CUDA(ctx, p->meta.reserve(256));
+  MFG_CUDA(ctx, mfg::mx_panel_attr(1024));
+  p->args.queue = (int*)p->meta.ptr;
+  const MixedLayout L = mixed_layout(p->mx_work.ptr, count, n, nullptr);
+  if (count > 0) {
+    MFG_CUDA(ctx, mfg::mx_make_tensor_maps(L.op_a, L.op_b, n, count, true, &p->mx_tm[0],
+                                           &p->mx_tm[1]));
+    MFG_CUDA(ctx, mfg::mx_make_tensor_maps(L.op_a, L.op_b, n, count, false, &p->mx_tm[2],
+                                           &p->mx_tm[3]));
+    // The fallback's exact FP64 LU over every system slot (only the listed ones run).
+    std::vector<int> nn(count, n);
+    std::vector<int64_t> aoff(count), poff(count);
+    for (int q = 0; q < count; q++) {
+      aoff[q] = (int64_t)q * n * n;
+      poff[q] = (int64_t)q * n;
+    }
+    const int rc = plan_create(ctx, &p->mx_fb, mfg_plan::GETRF, count, nn.data(), nullptr,
+                               aoff.data(), poff.data(), 1, poff.data());
+    if (rc != MFG_OK) return rc;
+  }
+  return MFG_OK;
+}
+}  // namespace
+
+extern "C" {
+
 MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n) {
   DeviceScope device_scope_(ctx);
   if (!ctx) return -1;
@@ -3159,22 +3238,11 @@ MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count
   p->nrhs = 1;
   p->mx_n = n;
   p->max_n = n;
-  const size_t nn = (size_t)n * n * count;
-  const size_t bytes = Carve::bytes_for(nn, 4) + Carve::bytes_for((size_t)n * count, 4) +
-                       2 * Carve::bytes_for((size_t)n * nb * count, 2) +
-                       Carve::bytes_for(count, 8) + 3 * Carve::bytes_for(count, 4) + 256;
-  cudaError_t e = p->mx_work.reserve(bytes);
-  if (e != cudaSuccess) {
-    delete p;
-    return cuda_fail(ctx, e, "cudaMalloc(mixed workspace)");
+  const int rc = mixed_plan_setup(ctx, p);
+  if (rc != MFG_OK) {
+    mfg_plan_destroy(p);
+    return rc;
   }
-  e = p->meta.reserve(256);
-  if (e == cudaSuccess) e = mfg::mx_panel_attr(1024);
-  if (e != cudaSuccess) {
-    delete p;
-    return cuda_fail(ctx, e, "mixed plan set-up");
-  }
-  p->args.queue = (int*)p->meta.ptr;
   *plan = p;
   return MFG_OK;
 }
@@ -3199,134 +3267,67 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
   if (!info) return fail(ctx, -10, "info is null");
   const int n = plan->mx_n, count = plan->count, nb = mfg::mx_panel_width();
   cudaStream_t s = ctx->stream;
-  Carve cv(plan->mx_work.ptr);
-  float* a32 = cv.take<float>((size_t)n * n * count);
-  int* ipiv = cv.take<int>((size_t)n * count);
-  void* l21 = cv.take<uint16_t>((size_t)n * nb * count);
-  void* u12 = cv.take<uint16_t>((size_t)n * nb * count);
-  double* anorm = cv.take<double>(count);
-  int* state = cv.take<int>(count);
-  int* active = cv.take<int>(count);
-  if (lowp != MFG_LOWP_FP32 && !ctx->cublas) {
-    if (cublasCreate(&ctx->cublas) != CUBLAS_STATUS_SUCCESS)
-      return fail(ctx, MFG_ERR_CUDA, "cublasCreate failed");
-  }
-  if (ctx->cublas) {
-    cublasSetStream(ctx->cublas, s);
-    cublasSetMathMode(ctx->cublas, lowp == MFG_LOWP_TF32 ? CUBLAS_TF32_TENSOR_OP_MATH
-                                                         : CUBLAS_DEFAULT_MATH);
-  }
-  MFG_CUDA(ctx, mfg::mx_round(a, a32, (long long)n * n * count, s));
-  const long long sa = (long long)n * n;
-  const float alpha = -1.0f, beta = 1.0f;
+  const MixedLayout L = mixed_layout(plan->mx_work.ptr, count, n, nullptr);
+  const int opfmt = lowp == MFG_LOWP_TF32 ? 1 : lowp == MFG_LOWP_BF16 ? 2 : 0;
+  const int R = mfg::mx_op_rows(n);
+  MFG_CUDA(ctx, mfg::mx_round(a, L.a32, (long long)n * n * count, s));
   for (int k = 0; k < n; k += nb) {
-    MFG_CUDA(ctx, mfg::mx_panel(a32, n, k, ipiv, nullptr, count, s));
-    const int m2 = n - k - nb;
-    if (m2 <= 0) continue;
-    float* L21 = a32 + (long long)k * n + k + nb;
-    float* U12 = a32 + (long long)(k + nb) * n + k;
-    float* A22 = a32 + (long long)(k + nb) * n + k + nb;
-    if (lowp == MFG_LOWP_FP32) {
-      MFG_CUDA(ctx, mfg::mx_update_fp32(a32, n, k, nullptr, count, s));
-    } else if (lowp == MFG_LOWP_TF32) {
-      cublasStatus_t st = cublasGemmStridedBatchedEx(
-          ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m2, m2, nb, &alpha, L21, CUDA_R_32F, n, sa, U12,
-          CUDA_R_32F, n, sa, &beta, A22, CUDA_R_32F, n, sa, count, CUBLAS_COMPUTE_32F_FAST_TF32,
-          CUBLAS_GEMM_DEFAULT);
-      if (st != CUBLAS_STATUS_SUCCESS)
-        return fail(ctx, MFG_ERR_CUDA, "TF32 trailing update failed (cuBLAS %d)", (int)st);
+    MFG_CUDA(ctx, mfg::mx_panel(L.a32, n, k, L.ipiv, nullptr, count, L.op_a, L.op_b, opfmt, R, s));
+    if (n - k - nb <= 0) continue;
+    if (opfmt == 0) {
+      MFG_CUDA(ctx, mfg::mx_update_fp32(L.a32, n, k, nullptr, count, s));
     } else {
-      MFG_CUDA(ctx, mfg::mx_bf16_operands(a32, n, k, l21, u12, nullptr, count, s));
-      cublasStatus_t st = cublasGemmStridedBatchedEx(
-          ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m2, m2, nb, &alpha, l21, CUDA_R_16BF, m2,
-          (long long)n * nb, u12, CUDA_R_16BF, nb, (long long)n * nb, &beta, A22, CUDA_R_32F, n,
-          sa, count, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-      if (st != CUBLAS_STATUS_SUCCESS)
-        return fail(ctx, MFG_ERR_CUDA, "BF16 trailing update failed (cuBLAS %d)", (int)st);
+      const int t = opfmt == 1 ? 0 : 2;
+      MFG_CUDA(ctx, mfg::mx_update_tc(&plan->mx_tm[t], &plan->mx_tm[t + 1], L.a32, n, k,
+                                      opfmt == 1, count, L.status, s));
     }
   }
-  MFG_CUDA(ctx, cudaMemsetAsync(active, 0xFF, sizeof(int) * count, s));
-  MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, -1, tol, berr, iters, state, anorm,
-                               active, s));
+  MFG_CUDA(ctx, cudaMemsetAsync(L.active, 0xFF, sizeof(int) * count, s));
+  MFG_CUDA(ctx, mfg::mx_refine(a, b, x, L.a32, L.ipiv, n, count, -1, tol, berr, iters, L.state,
+                               L.anorm, L.active, s));
   for (int it = 0; it <= max_iter; ++it)
-    MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, it, tol, berr, iters, state,
-                                 anorm, active, s));
-  // Systems that did not converge (stalled, diverged, out of iterations, singular FP32 factor)
-  // are solved again with the exact FP64 LU.
-  std::vector<int> hstate(count);
-  MFG_CUDA(ctx, cudaMemcpyAsync(hstate.data(), state, sizeof(int) * count, cudaMemcpyDeviceToHost,
-                                s));
-  MFG_CUDA(ctx, cudaStreamSynchronize(s));
-  std::vector<int> hinfo(count, 0), redo;
-  for (int i = 0; i < count; i++)
-    if (hstate[i] != 1) redo.push_back(i);
-  if (!redo.empty()) {
-    const int r = (int)redo.size();
-    DevBuf tmp;
-    const size_t need = Carve::bytes_for((size_t)r * n * n, 8) + Carve::bytes_for((size_t)r * n, 8) +
-                        Carve::bytes_for((size_t)r * n, 4) + 2 * Carve::bytes_for(r, 4);
-    MFG_CUDA(ctx, tmp.reserve(need));
-    Carve tv(tmp.ptr);
-    double* ta = tv.take<double>((size_t)r * n * n);
-    double* tb = tv.take<double>((size_t)r * n);
-    int* tpiv = tv.take<int>((size_t)r * n);
-    int* tsign = tv.take<int>(r);
-    int* tinfo = tv.take<int>(r);
-    for (int q = 0; q < r; q++) {
-      const int i = redo[q];
-      MFG_CUDA(ctx, cudaMemcpyAsync(ta + (size_t)q * n * n, a + (size_t)i * n * n,
-                                    sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s));
-      MFG_CUDA(ctx, cudaMemcpyAsync(tb + (size_t)q * n, b + (size_t)i * n, sizeof(double) * n,
-                                    cudaMemcpyDeviceToDevice, s));
-    }
-    std::vector<int> nn(r, n);
-    std::vector<int64_t> aoff(r), poff(r);
-    for (int q = 0; q < r; q++) {
-      aoff[q] = (int64_t)q * n * n;
-      poff[q] = (int64_t)q * n;
-    }
-    mfg_plan* fp = nullptr;
-    int rc = plan_create(ctx, &fp, mfg_plan::GETRF, r, nn.data(), nullptr, aoff.data(),
-                         poff.data(), 1, poff.data());
-    if (rc != MFG_OK) return rc;
-    fp->args.a = ta;
-    fp->args.piv = tpiv;
-    fp->args.b = tb;
-    fp->args.sign = tsign;
-    fp->args.info = tinfo;
-    rc = plan_launch(fp, s);
-    if (rc != MFG_OK) {
-      mfg_plan_destroy(fp);
-      return rc;
-    }
-    std::vector<int> finfo(r);
-    MFG_CUDA(ctx, cudaMemcpyAsync(finfo.data(), tinfo, sizeof(int) * r, cudaMemcpyDeviceToHost,
-                                  s));
-    for (int q = 0; q < r; q++) {
-      const int i = redo[q];
-      MFG_CUDA(ctx, cudaMemcpyAsync(x + (size_t)i * n, tb + (size_t)q * n, sizeof(double) * n,
-                                    cudaMemcpyDeviceToDevice, s));
-    }
-    MFG_CUDA(ctx, cudaStreamSynchronize(s));
-    mfg_plan_destroy(fp);
-    for (int q = 0; q < r; q++) hinfo[redo[q]] = finfo[q] != 0 ? 2 : 1;
-    // Backward error of the FP64 solutions: one measuring sweep (no correction) over them.
-    MFG_CUDA(ctx, cudaMemcpyAsync(state, hinfo.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
-                                  s));
-    MFG_CUDA(ctx, mfg::mx_refine(a, b, x, a32, ipiv, n, count, -2, tol, berr, iters, state,
-                                 anorm, active, s));
-  }
-  MFG_CUDA(ctx, cudaMemcpyAsync(info, hinfo.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
-                                s));
-  MFG_CUDA(ctx, cudaStreamSynchronize(s));
+    MFG_CUDA(ctx, mfg::mx_refine(a, b, x, L.a32, L.ipiv, n, count, it, tol, berr, iters, L.state,
+                                 L.anorm, L.active, s));
+  // Systems that did not converge (stalled, diverged, out of iterations, singular low-precision
+  // factor) are solved again with the exact FP64 LU, entirely on the device.
+  MFG_CUDA(ctx, cudaMemsetAsync(L.fb_count, 0, sizeof(int), s));
+  MFG_CUDA(ctx, mfg::mx_fb_gather(a, b, x, L.fb_a, L.state, n, count, L.fb_order, L.fb_count, s));
+  mfg_plan* fp = plan->mx_fb;
+  fp->args.a = L.fb_a;
+  fp->args.piv = L.fb_piv;
+  fp->args.b = x;
+  fp->args.sign = L.fb_sign;
+  fp->args.info = L.fb_info;
+  fp->args.solve_only = 0;
+  fp->args.order = L.fb_order;
+  fp->args.dcount = L.fb_count;
+  const int rc = plan_launch(fp, s);
+  if (rc != MFG_OK) return rc;
+  MFG_CUDA(ctx, mfg::mx_fb_finish(L.state, info, L.fb_info, count, s));
+  // Backward error of the FP64 solutions: one measuring sweep (no correction) over them.
+  MFG_CUDA(ctx, mfg::mx_refine(a, b, x, L.a32, L.ipiv, n, count, -2, tol, berr, iters, L.state,
+                               L.anorm, L.active, s));
   return MFG_OK;
 }
 
 MFG_API int mfg_plan_status(mfg_plan* plan) {
   DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
-  MFG_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
-  MFG_CUDA(plan->ctx, cudaGetLastError());
+  mfg_ctx* ctx = plan->ctx;
+  MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  MFG_CUDA(ctx, cudaGetLastError());
+  if (plan->kind == mfg_plan::MIXED && plan->count > 0) {
+    const MixedLayout L = mixed_layout(plan->mx_work.ptr, plan->count, plan->mx_n, nullptr);
+    int st = 0;
+    MFG_CUDA(ctx, cudaMemcpy(&st, L.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+      MFG_CUDA(ctx, cudaMemset(L.status, 0, sizeof(int)));
+      return fail(ctx, MFG_ERR_TIMEOUT,
+                  "a bounded device-side wait of the tensor-core update gave up (%s); the "
+                  "solutions of that execution are not valid",
+                  st == 1 ? "operand tiles" : "tensor-core result");
+    }
+  }
   return MFG_OK;
 }
 
