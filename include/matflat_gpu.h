@@ -412,6 +412,28 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
                                                 double* loss, double* grad, int* info,
                                                 int keep_factor);
 
+/* Reverse mode (vector-Jacobian product) of Factorization.Cholesky
+ * (MatFlat/Factorization.Cholesky.cs:114-168), its log-determinant and the solve A x = b done with
+ * the two Blas.SolveTriangular calls (MatFlat/Blas.SolveTriangular.cs:162-242), over a potrf plan
+ * (n <= 128).  Forward, per matrix: L = Cholesky(A), logdet = 2 sum log L_ii, x = A^-1 b.
+ * Given the cotangents lbar (dloss/dL, lower triangle, same layout as a; NULL = 0), logdet_bar
+ * (one per matrix; NULL = 0) and xbar (dloss/dx, laid out like b; NULL = 0, then x may be NULL),
+ * writes the symmetric gradient dloss/dA to abar (same layout as a; d loss = <abar, dA> for
+ * symmetric dA, so the derivative by an upper-triangle entry A_ij, i < j, that Cholesky reads is
+ * 2 abar_ij):
+ *   abar = sym(L^-T Phi(L^T lbar) L^-1) + logdet_bar A^-1 - sym(bbar x^T),  bbar = A^-1 xbar,
+ * Phi = lower triangle with the diagonal halved, sym(M) = (M + M^T)/2, and bbar (dloss/db) to
+ * bbar when not NULL (b layout; zero when xbar is NULL).  xbar needs a plan with nrhs >= 1.
+ * recompute = 1: a holds A and the factor is recomputed in place (a <- L, bit-identical to
+ * mfg_dpotrf_batched), so nothing is stored between the forward and the backward pass;
+ * recompute = 0: a holds L from mfg_dpotrf_batched.  info[i] = j+1 when the recomputed
+ * factorization fails at column j (abar then unspecified).  The backward pass uses fused
+ * multiply-adds (MatFlat defines no derivative order).  Device pointers; asynchronous. */
+MFG_API int mfg_dpotrf_backward_batched(mfg_plan* plan, double* a, const double* lbar,
+                                        const double* logdet_bar, const double* x,
+                                        const double* xbar, double* abar, double* bbar,
+                                        int* info, int recompute);
+
 /* Mixed-precision LU solve with FP64 iterative refinement (new; no MatFlat counterpart).
  * A plan for `count` systems of one order n (a multiple of 32, at most 1024); matrices packed
  * column-major with lda = n at stride n*n, right-hand sides and solutions at stride n.

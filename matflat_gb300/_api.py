@@ -23,6 +23,7 @@ _SIGS = {
     "mfg_synchronize": (_I, [_vp]),
     "mfg_last_error": (ctypes.c_char_p, [_vp]),
     "mfg_get_device": (_I, [_vp, _c_int_p]),
+    "mfg_dpotrf_backward_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _I]),
     "mfg_dgetrf": (_I, [_vp, _I, _I, _vp, _I, _vp, _c_int_p]),
     "mfg_dpotrf": (_I, [_vp, _I, _vp, _I, _c_int_p]),
     "mfg_dgeqrf": (_I, [_vp, _I, _I, _vp, _I, _vp]),
@@ -721,6 +722,16 @@ class CholeskyBatch(_Batch):
         name = "mfg_%spotrf_batched_host" % _elem(a, dtype)
         rc = getattr(self.ctx.lib, name)(self.h, _hptr(a), _hptr(b), _hptr(info))
         self.ctx.check(rc, name)
+
+    def backward(self, a, abar, info, lbar=None, logdet_bar=None, x=None, xbar=None, bbar=None,
+                 recompute=True):
+        """Vector-Jacobian product of (L = Cholesky(A), log det A, x = A^-1 b): writes the
+        symmetric gradient to abar (and A^-1 xbar to bbar).  recompute=True: a holds A and is
+        overwritten with L; False: a holds L already.  Device buffers; asynchronous."""
+        rc = self.ctx.lib.mfg_dpotrf_backward_batched(
+            self.h, _dptr(a), _dptr(lbar), _dptr(logdet_bar), _dptr(x), _dptr(xbar),
+            _dptr(abar), _dptr(bbar), _dptr(info), 1 if recompute else 0)
+        self.ctx.check(rc, "mfg_dpotrf_backward_batched")
 
     def loss_and_grad_host(self, k, y, loss, grad, info, keep_factor=True):
         """loss_and_grad on host arrays, copies pipelined with compute.  Synchronous."""

@@ -119,6 +119,27 @@ cudaError_t launch_chol_grad_batched(const BatchArgs& args, double* loss, double
                                      int keep_factor, int ctas, cudaStream_t s);
 cudaError_t init_grad_attributes();
 
+// Reverse mode of Cholesky / log-determinant / solve (chol_bwd.cu), one CTA per matrix, n <= 128.
+struct CholBwdArgs {
+  const int* order;
+  const int* n;
+  const int* lda;
+  const long long* a_off;
+  const long long* b_off;
+  const double* l;           // the factor L (lower triangle), a_off / lda layout
+  const double* lbar;        // cotangent of L (lower triangle), same layout; null: zero
+  const double* logdet_bar;  // one per matrix; null: zero
+  const double* x;           // forward solution (b_off layout); needed with xbar
+  const double* xbar;        // cotangent of x; null: zero
+  double* abar;              // output: symmetric gradient, a_off / lda layout
+  double* bbar;              // output (optional): A^-1 xbar
+  const int* info;           // matrices with info != 0 are skipped; null: none
+  int count;
+  int* queue;
+};
+int chol_backward_max_n();
+cudaError_t launch_chol_backward(const CholBwdArgs& args, int ctas, cudaStream_t s);
+
 // Batched GEVD front half (chol.cu): B -> L (Cholesky), C = L^-1 A L^-T (leading dimension n).
 struct GevdArgs {
   const int* order;

@@ -3142,6 +3142,62 @@ MFG_API int mfg_dpotrf_logdet_solve_grad_batched(mfg_plan* plan, double* k, doub
 }
 
 
+MFG_API int mfg_dpotrf_backward_batched(mfg_plan* plan, double* a, const double* lbar,
+                                        const double* logdet_bar, const double* x,
+                                        const double* xbar, double* abar, double* bbar,
+                                        int* info, int recompute) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF) return fail(ctx, -1, "plan is not a potrf plan");
+  if (plan->max_n > mfg::chol_backward_max_n())
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "matrix order %d > %d is not supported here",
+                plan->max_n, mfg::chol_backward_max_n());
+  if (plan->count == 0) return MFG_OK;
+  if (!a) return fail(ctx, -2, "a is null");
+  if (xbar && !x) return fail(ctx, -5, "x is null (needed with xbar)");
+  if (xbar && plan->nrhs < 1)
+    return fail(ctx, -6, "xbar needs a plan with right-hand-side offsets (nrhs >= 1)");
+  if (!abar) return fail(ctx, -7, "abar is null");
+  if ((const void*)abar == (const void*)a || (const void*)abar == (const void*)lbar)
+    return fail(ctx, -7, "abar must not alias a or lbar");
+  if (!info) return fail(ctx, -9, "info is null");
+  cudaStream_t s = ctx->stream;
+  if (recompute) {
+    // L = Cholesky(A) in place, MatFlat's arithmetic (the plan's forward kernel, no solve).
+    BatchArgs f = plan->args;
+    f.a = a;
+    f.b = nullptr;
+    f.nrhs = 0;
+    f.info = info;
+    f.solve_only = 0;
+    MFG_CUDA(ctx, cudaMemsetAsync(f.queue, 0, sizeof(int), s));
+    MFG_CUDA(ctx, mfg::launch_potrf_batched(f, plan->ctas, plan->warps, s));
+  } else {
+    MFG_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(int) * plan->count, s));
+  }
+  mfg::CholBwdArgs b{};
+  b.order = plan->args.order;
+  b.n = plan->args.n;
+  b.lda = plan->args.lda;
+  b.a_off = plan->args.a_off;
+  b.b_off = plan->args.b_off;
+  b.l = a;
+  b.lbar = lbar;
+  b.logdet_bar = logdet_bar;
+  b.x = xbar ? x : nullptr;
+  b.xbar = xbar;
+  b.abar = abar;
+  b.bbar = plan->nrhs > 0 ? bbar : nullptr;
+  b.info = info;
+  b.count = plan->count;
+  b.queue = plan->args.queue;
+  MFG_CUDA(ctx, cudaMemsetAsync(b.queue, 0, sizeof(int), s));
+  const int ctas = (int)std::min<long long>((long long)ctx->sm_count * 4, plan->count);
+  MFG_CUDA(ctx, mfg::launch_chol_backward(b, std::max(1, ctas), s));
+  return MFG_OK;
+}
+
 // ------------------------------------------------------------------------------------------
 // Mixed-precision LU solve with FP64 iterative refinement.
 

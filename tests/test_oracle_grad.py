@@ -66,3 +66,45 @@ def test_non_pd_reports_info():
     K = np.array([[1.0, 2.0], [2.0, 1.0]])
     info, loss, _, _ = _loss_grad(K, np.ones(2))
     assert info == 2 and np.isnan(loss)
+
+
+def test_reverse_mode_reference_matches_finite_differences():
+    """The FP64 reference VJP of (Cholesky factor, log det, solve) used by the GPU backward tests
+    agrees with central differences (h = 1e-6) along random symmetric directions."""
+    from tests.chol_vjp import oracle_factor, objective, vjp
+    rng = np.random.default_rng(21)
+    for n in (1, 3, 8, 24):
+        B = rng.standard_normal((n, n))
+        A = B @ B.T + n * np.eye(n)
+        b = rng.standard_normal(n)
+        lbar = np.tril(rng.standard_normal((n, n)))
+        ldb = rng.standard_normal()
+        xbar = rng.standard_normal(n)
+        info, L = oracle_factor(A)
+        assert info == 0
+        x = np.linalg.solve(A, b)
+        G, bbar = vjp(L, lbar, ldb, x, xbar)
+        np.testing.assert_allclose(bbar, np.linalg.solve(A, xbar), rtol=1e-10, atol=1e-12)
+        for _ in range(3):
+            E = rng.standard_normal((n, n))
+            E = E + E.T
+            h = 1e-6
+            fd = (objective(A + h * E, lbar, ldb, b, xbar) -
+                  objective(A - h * E, lbar, ldb, b, xbar)) / (2 * h)
+            an = np.sum(G * E)
+            assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (n, fd, an)
+
+
+def test_reverse_mode_reference_reduces_to_the_loss_gradient():
+    """With lbar = 0, logdet_bar = 1, xbar = y and x = alpha, the VJP is the loss gradient
+    K^-1 - alpha alpha^T of the oracle's composition."""
+    from tests.chol_vjp import oracle_factor, vjp
+    rng = np.random.default_rng(22)
+    n = 20
+    B = rng.standard_normal((n, n))
+    K = B @ B.T + n * np.eye(n)
+    y = rng.standard_normal(n)
+    info, loss, G, alpha = _loss_grad(K, y)
+    _, L = oracle_factor(K)
+    V, _ = vjp(L, np.zeros((n, n)), 1.0, alpha, y)
+    np.testing.assert_allclose(V, G, rtol=1e-10, atol=1e-13)
