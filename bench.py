@@ -57,6 +57,11 @@ CONFIGS = {
                           "its gradient K^-1 - alpha alpha^T, 4,096 RBF kernel matrices n=128 "
                           "(x~U[0,1]^3, length 0.3, jitter 1e-6), y~N(0,1), seed 0",
                  count=4096, n=128),
+    "bwd": dict(workload="reverse mode of Cholesky / log det / solve with random cotangents "
+                         "(Lbar lower N(0,1), logdet_bar 1, xbar N(0,1)), factor recomputed in "
+                         "MatFlat order, 4,096 RBF kernel matrices n=128 (x~U[0,1]^3, length 0.3, "
+                         "jitter 1e-6), seed 0",
+                count=4096, n=128),
     "mixed": dict(workload="mixed-precision LU solve + FP64 iterative refinement to 1e-12 "
                            "normwise backward error, 2,048 systems n=512, A=U diag(sigma) V^T "
                            "(U, V Q factors of N(0,1)), sigma log-spaced to cond, x_true~N(0,1), "
@@ -123,6 +128,19 @@ def grad_flops(n):
     """Cholesky forward (n^3/3) plus the adjoint (2n^3/3): n^3 per matrix."""
     n = n.astype(np.float64)
     return float(np.sum(n ** 3))
+
+
+def bwd_flops(n):
+    """Recomputed factor (n^3/3), X = L^T Lbar below the diagonal (n^3/3), S L^-1 (n^3) and the
+    lower triangle of L^-T Y (n^3/3): 2n^3 per matrix."""
+    n = n.astype(np.float64)
+    return float(np.sum(2.0 * n ** 3))
+
+
+def bwd_bytes(n):
+    """Read A, Lbar, x, xbar, logdet_bar; write L, abar, bbar."""
+    n = n.astype(np.float64)
+    return float(np.sum(32 * n ** 2 + 24 * n + 8))
 
 
 def grad_bytes(n):
@@ -263,7 +281,7 @@ def make_inputs(cfg_name, rank):
     if cfg_name == "chol100k":
         return synth.spd_batch_uneven(cfg["count"], cfg["nmin"], cfg["nmax"], cfg["nrhs"],
                                       seed=rank)
-    if cfg_name == "grad":
+    if cfg_name in ("grad", "bwd"):
         return synth.rbf_batch(cfg["count"], cfg["n"], seed=rank)
     if cfg_name.startswith("gevd"):
         return synth.gevd_batch(cfg["count"], cfg["n"], seed=rank, dtype=cfg.get("dtype", "f64"))
@@ -411,6 +429,7 @@ def metric_name(cfg_name):
             "chol": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "chol100k": "batched FP64 Cholesky+solve matrices/s (MatFlat-exact)",
             "grad": "batched FP64 Cholesky/log-det/solve loss+gradient matrices/s",
+            "bwd": "batched FP64 Cholesky/log-det/solve reverse mode (VJP) matrices/s",
             "qr": "batched FP64 QR least-squares matrices/s (MatFlat-exact factors)",
             "qr32": "batched FP32 QR least-squares matrices/s (MatFlat-exact factors)"}[cfg_name]
 
@@ -645,7 +664,7 @@ def main():
     ap.add_argument("--count", type=int, default=None,
                     help="override the batch size (small cases for profiling)")
     ap.add_argument("--cond", type=float, default=1e5, help="mixed: condition number")
-    ap.add_argument("--lowp", default="tf32", choices=["fp32", "tf32", "bf16"],
+    ap.add_argument("--lowp", default="tf32x3", choices=["fp32", "tf32", "bf16", "tf32x3"],
                     help="mixed: precision of the factorization")
     ap.add_argument("--n", type=int, default=None, help="mixed: order of the systems")
     ap.add_argument("--no-autotune", action="store_true",
@@ -783,6 +802,28 @@ def main():
             kernel_key = "potrf_batched_kernel"
             if cfg_name == "chol100k":
                 traffic_key = "potrf_batched_kernel_chol100k"
+        elif cfg_name == "bwd":
+            plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
+            g = torch.Generator(device="cuda")
+            g.manual_seed(rank)
+            lbar = torch.randn(a0.numel(), dtype=torch.float64, device="cuda", generator=g)
+            xbar = torch.randn(b0.numel(), dtype=torch.float64, device="cuda", generator=g)
+            ldb = torch.ones(count, dtype=torch.float64, device="cuda")
+            # x = A^-1 b from the forward pass (factor + solve), once, untimed
+            xs = b0.clone()
+            fa = a0.clone()
+            plan.run(fa, xs, info)
+            abar = torch.empty_like(a0)
+            bbar = torch.empty_like(b0)
+            del fa
+
+            def run():
+                plan.backward(a, abar, info, lbar=lbar, logdet_bar=ldb, x=xs, xbar=xbar,
+                              bbar=bbar, recompute=True)
+            outs = [abar, bbar, info]
+            flops = bwd_flops(d["n"])
+            byts = bwd_bytes(d["n"])
+            kernel_key = "chol_backward_kernel"
         else:
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
             loss = torch.zeros(count, dtype=torch.float64, device="cuda")
@@ -847,7 +888,7 @@ def main():
     # of the batch inside one synchronous call, timed by the host clock.  The calls work in
     # place, so the input arrays are restored from pristine pinned copies before each (untimed).
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and cfg_name != "bwd":
         def pinned_like(t, dtype=None):
             return torch.empty(t.shape, dtype=dtype or t.dtype).pin_memory()
 
@@ -943,7 +984,7 @@ def main():
 
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------------------------
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and cfg_name != "bwd":
         rate, sample_n, threads, t = cpu_sample_rate(cfg_name, d, budget_s=args.cpu_budget)
         cpu = {"value": rate, "unit": "matrices/s", "cores": threads, "kind": "port",
                "sample": "%d matrices (batch of %d, evenly strided, repeated if smaller than "
@@ -995,7 +1036,8 @@ def main():
                                         "batched factorization/solve (one graph replay)"},
             "kernel_ms_per_step": kmed,
             "launch_shape": None if tuned is None else dict(
-                zip(["warps_per_cta", "warps_per_sm", "lanes_per_matrix", "mul_mode",
+                zip(["warps_per_cta", "warps_per_sm",
+                     "lanes_table" if cfg_name == "lu" else "lanes_per_matrix", "mul_mode",
                      "dot_pairs_per_block"], tuned),
                 source="mfg_plan_autotune at plan creation (outside the timed region)"),
             "gpu_launches": args.steps,

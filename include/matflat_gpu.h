@@ -446,9 +446,14 @@ MFG_API int mfg_dpotrf_backward_batched(mfg_plan* plan, double* a, const double*
  * arithmetic).  Outputs per system: x, berr, iters (refinement sweeps), info (0 refined to tol,
  * 1 solved by the FP64 fallback, 2 singular).  a, b, x, berr, iters and info are device
  * pointers.  The call is asynchronous on the context's stream and allocates nothing: the plan owns
- * the FP32 factors, the operand copies and the fallback's buffers (about 12 n^2 count bytes +
- * the FP64 fallback copy of A, 8 n^2 count bytes).  Check mfg_plan_status after it. */
-enum mfg_lowp { MFG_LOWP_FP32 = 0, MFG_LOWP_TF32 = 1, MFG_LOWP_BF16 = 2 };
+ * the FP32 factors, the operand copies and the fallback's buffers (about 4 n^2 count bytes of
+ * factors, 4 copies of n x 32 values per system, and the FP64 fallback copy of A, 8 n^2 count
+ * bytes).  Check mfg_plan_status after it. */
+/* lowp: FP32 (trailing updates on the FP32 cores), TF32 or BF16 (tensor cores, FP32
+ * accumulation), TF32X3 (tensor cores, each operand split into a TF32 high and low part and the
+ * three leading products accumulated: about FP32's accuracy, so refinement converges where the
+ * FP32 mode does). */
+enum mfg_lowp { MFG_LOWP_FP32 = 0, MFG_LOWP_TF32 = 1, MFG_LOWP_BF16 = 2, MFG_LOWP_TF32X3 = 3 };
 MFG_API int mfg_plan_gesv_mixed_batched(mfg_ctx* ctx, mfg_plan** plan, int count, int n);
 MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const double* b, double* x,
                                     int lowp, int max_iter, double tol, double* berr, int* iters,

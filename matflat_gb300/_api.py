@@ -811,7 +811,7 @@ def selftest_dmul(a, b, out):
               "mfg_selftest_dmul")
 
 
-LOWP = {"fp32": 0, "tf32": 1, "bf16": 2}
+LOWP = {"fp32": 0, "tf32": 1, "bf16": 2, "tf32x3": 3}
 
 
 class MixedSolveBatch(_Batch):

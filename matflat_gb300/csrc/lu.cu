@@ -31,20 +31,23 @@ namespace mfg {
 //   mode 1: column 1 (sum = L(i,0) * U(0,1))
 //   mode 2: column c >= 2 (sum = scol[i] + (L(i,c-2)*U(c-2,c) + L(i,c-1)*U(c-1,c)))
 // Tr supplies the element type's arithmetic (double, float or Complex overload).
-template <class Tr>
+// G: lanes per matrix (8, 16 or 32): the matrix is worked on by a group of G consecutive lanes
+// of the warp, the other groups of the warp work on other matrices of the same order.
+template <class Tr, int G = 32>
 __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n, long long lda,
                                                  int c, int mode,
                                                  const typename Tr::Acc* scol, int* piv,
                                                  int& sign, int& info) {
   using T = typename Tr::T;
   using Acc = typename Tr::Acc;
-  const int lane = threadIdx.x & 31;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
   T* cc = a + (long long)c * lda;
   unsigned long long bkey = 0ull;
   int bidx = INT_MAX;
   bool first_nan = false;
   if (mode == 0) {
-    for (int i = c + lane; i < m; i += 32) {
+    for (int i = c + lane; i < m; i += G) {
       const T v = cc[i];
       const unsigned long long key = Tr::key(v);
       if (key > bkey) {
@@ -58,7 +61,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
     const T u1 = cc[c - 1];                       // U(c-1, c)
     const T* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
     const T u2 = (mode == 2) ? cc[c - 2] : u1;    // U(c-2, c)
-    for (int i = c + lane; i < m; i += 32) {
+    for (int i = c + lane; i < m; i += G) {
       Acc s;
       if (mode == 1) {
         s = Tr::prod(l1[i], u1);
@@ -75,12 +78,13 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
       if (i == c) first_nan = Tr::nan0(v);
     }
   }
-  int p = warp_argmax(bkey, bidx);
-  // Row c is handled by lane 0; a NaN there can never be displaced by the strict ">" scan.
-  if (__shfl_sync(FULL_MASK, first_nan ? 1 : 0, 0)) p = c;
-  __syncwarp();
+  int p = group_argmax<G>(bkey, bidx);
+  // Row c is handled by the group's lane 0; a NaN there can never be displaced by the strict ">"
+  // scan.
+  if (__shfl_sync(gm, first_nan ? 1 : 0, 0, G)) p = c;
+  __syncwarp(gm);
   if (p != c && p < m) {
-    for (int col = lane; col < n; col += 32) {
+    for (int col = lane; col < n; col += G) {
       T* base = a + (long long)col * lda;
       const T t = base[c];
       base[c] = base[p];
@@ -93,38 +97,39 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
     }
     sign = -sign;
   }
-  __syncwarp();
+  __syncwarp(gm);
   const T diag = cc[c];
   if (Tr::nz(diag)) {
-    for (int i = c + 1 + lane; i < m; i += 32) cc[i] = Tr::div(cc[i], diag);
+    for (int i = c + 1 + lane; i < m; i += G) cc[i] = Tr::div(cc[i], diag);
   } else if (info == 0) {
     info = c + 1;
   }
-  __syncwarp();
+  __syncwarp(gm);
 }
 
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
 // and in `info` the first zero pivot (k+1), or 0.
-template <class Tr, int IM, int DB = DOT_BLOCK>
+template <class Tr, int IM, int DB = DOT_BLOCK, int G = 32>
 __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
                         typename Tr::Acc* scol, int& sign, int& info) {
   using T = typename Tr::T;
   using Acc = typename Tr::Acc;
-  const int lane = threadIdx.x & 31;
-  for (int i = lane; i < m; i += 32) piv[i] = i;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  for (int i = lane; i < m; i += G) piv[i] = i;
   sign = 1;
   info = 0;
-  __syncwarp();
+  __syncwarp(gm);
   const int K = m < n ? m : n;
-  lu_finish_column<Tr>(a, m, n, lda, 0, 0, scol, piv, sign, info);
+  lu_finish_column<Tr, G>(a, m, n, lda, 0, 0, scol, piv, sign, info);
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
     const int C = (k1 < K && k >= 1) ? m - k1 : 0;  // prefixes of column k1 (rows [k1, m))
     const T* rowk = a + k;                    // L(k, t) = rowk[t*lda]
     const T* colk1 = a + (long long)k1 * lda;
-    for (int d = lane; d < R + C; d += 32) {
+    for (int d = lane; d < R + C; d += G) {
       const bool isrow = d < R;
       const int idx = isrow ? k1 + d : k1 + (d - R);
       const T* x = isrow ? rowk : a + idx;
@@ -138,8 +143,8 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
         scol[idx] = s;
       }
     }
-    __syncwarp();
-    if (k1 < K) lu_finish_column<Tr>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
+    __syncwarp(gm);
+    if (k1 < K) lu_finish_column<Tr, G>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
   }
   // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
 }
@@ -148,28 +153,29 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
 // b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
 // upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
 // S: the solve arithmetic of the element type (DSolve, SSolve or ZSolve<false>).
-template <class S = DSolve>
+template <class S = DSolve, int G = 32>
 __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const int* piv,
                            typename S::T* b, long long ldb, int nrhs, typename S::T* xs,
                            typename S::Acc* acc) {
-  const int lane = threadIdx.x & 31;
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
   const int ldx = n | 1;
   for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
     const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
-    for (int e = lane; e < nr * n; e += 32) {
+    for (int e = lane; e < nr * n; e += G) {
       const int r = e / n;
       const int i = e - r * n;
       xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + piv[i]];
     }
-    __syncwarp();
-    warp_solve_dot<32, S>(lu, n, 1, lda, true, xs, ldx, acc, nr);
-    warp_solve_sweep<32, S>(lu, n, lda, 1, xs, ldx, nr);
-    for (int e = lane; e < nr * n; e += 32) {
+    __syncwarp(gm);
+    warp_solve_dot<G, S>(lu, n, 1, lda, true, xs, ldx, acc, nr);
+    warp_solve_sweep<G, S>(lu, n, lda, 1, xs, ldx, nr);
+    for (int e = lane; e < nr * n; e += G) {
       const int r = e / n;
       const int i = e - r * n;
       b[(long long)(r0 + r) * ldb + i] = xs[r * ldx + i];
     }
-    __syncwarp();
+    __syncwarp(gm);
   }
 }
 
@@ -268,6 +274,112 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Size-bucketed work.  The plan cuts the batch into tasks of up to 32/G matrices of one order,
+// with G (lanes per matrix: 8, 16 or 32) chosen per size bucket, and queues the tasks; a warp takes
+// one task at a time and its groups of G lanes each factor (and solve) one matrix of it, in exactly
+// the schedule above.  Small G keeps the lanes busy when a step has few dots; groups of a task
+// share the order, so they follow the same control flow.
+constexpr int GROUP_SMEM_DOUBLES = SMEM_N + 2;   // per group: the column sums (n <= SMEM_N)
+
+template <int IM, int DB, int G>
+__device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cnt, double* ws,
+                                           long long gw) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G;
+  if (g >= cnt) return;
+  const int mat = p.order[first + g];
+  const int n = p.n[mat];
+  const long long lda = p.lda[mat];
+  double* a = p.a + p.a_off[mat];
+  int* piv = p.piv + p.piv_off[mat];
+  double* scr;
+  double* sol;
+  if (n <= SMEM_N) {
+    scr = ws + g * GROUP_SMEM_DOUBLES;
+    sol = p.gsolve ? p.gsolve + (gw * GETRF_GROUPS + g) * GSOLVE_STRIDE : nullptr;
+  } else {   // only 32-lane tasks hold orders above SMEM_N
+    scr = p.gscratch + gw * p.gscratch_stride;
+    sol = scr + n;
+  }
+  const int ldx = n | 1;
+  int sign = 1, info = 0;
+  if (!p.solve_only) lu_warp<DTraits, IM, DB, G>(a, n, n, lda, piv, scr, sign, info);
+  if (p.nrhs > 0)
+    getrs_warp<DSolveIM, G>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol,
+                            sol + RHS_CHUNK * ldx);
+  if ((lane & (G - 1)) == 0 && !p.solve_only) {
+    p.sign[mat] = sign;
+    p.info[mat] = info;
+  }
+}
+
+// One launch per lanes-per-matrix bucket: G is a template parameter, so each variant keeps the
+// register count of its own schedule.  args.task_first / task_gc / ntasks / queue describe the
+// bucket's tasks.
+template <int WARPS, int IM, int DB, int G>
+__global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
+  extern __shared__ double sm_dyn[];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  double* ws = sm_dyn + warp * GETRF_GROUPS * GROUP_SMEM_DOUBLES;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(p.queue, 1);
+    t = __shfl_sync(FULL_MASK, t, 0);
+    if (t >= p.ntasks) break;
+    getrf_task<IM, DB, G>(p, p.task_first[t], p.task_gc[t] >> 8, ws, gw);
+    __syncwarp();
+  }
+}
+
+template <int WARPS>
+static size_t getrf_task_smem_bytes() {
+  return sizeof(double) * GETRF_GROUPS * GROUP_SMEM_DOUBLES * WARPS;
+}
+
+template <int WARPS, int G>
+static cudaError_t launch_getrf_task_g(const BatchArgs& args, int ctas, cudaStream_t s) {
+  const size_t smem = getrf_task_smem_bytes<WARPS>();
+  if (args.hw_mul)
+    getrf_task_kernel<WARPS, 0, 4, G><<<ctas, WARPS * 32, smem, s>>>(args);
+  else if (args.dot_block == 2)
+    getrf_task_kernel<WARPS, 1, 2, G><<<ctas, WARPS * 32, smem, s>>>(args);
+  else
+    getrf_task_kernel<WARPS, 1, 4, G><<<ctas, WARPS * 32, smem, s>>>(args);
+  return cudaGetLastError();
+}
+
+template <int WARPS>
+static cudaError_t launch_getrf_task_w(const BatchArgs& args, int ctas, int g, cudaStream_t s) {
+  if (g == 8) return launch_getrf_task_g<WARPS, 8>(args, ctas, s);
+  if (g == 16) return launch_getrf_task_g<WARPS, 16>(args, ctas, s);
+  return launch_getrf_task_g<WARPS, 32>(args, ctas, s);
+}
+
+template <int WARPS, int G>
+static cudaError_t set_getrf_task_attr_g() {
+  const int smem = (int)getrf_task_smem_bytes<WARPS>();
+  cudaError_t e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 0, 4, G>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 1, 2, G>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 1, 4, G>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
+template <int WARPS>
+static cudaError_t set_getrf_task_attr() {
+  cudaError_t e = set_getrf_task_attr_g<WARPS, 8>();
+  if (e == cudaSuccess) e = set_getrf_task_attr_g<WARPS, 16>();
+  if (e == cudaSuccess) e = set_getrf_task_attr_g<WARPS, 32>();
+  return e;
+}
+
 template <int WARPS>
 static cudaError_t launch_getrf_w(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = getrf_smem_bytes(args, WARPS);
@@ -360,7 +472,23 @@ cudaError_t init_getrf_attributes() {
   if ((e = set_getrf_attr<2>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<4>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<8>()) != cudaSuccess) return e;
+  if ((e = set_getrf_task_attr<1>()) != cudaSuccess) return e;
+  if ((e = set_getrf_task_attr<2>()) != cudaSuccess) return e;
+  if ((e = set_getrf_task_attr<4>()) != cudaSuccess) return e;
+  if ((e = set_getrf_task_attr<8>()) != cudaSuccess) return e;
+  if ((e = set_getrf_task_attr<16>()) != cudaSuccess) return e;
   return set_getrf_attr<16>();
+}
+
+cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g, cudaStream_t s) {
+  switch (warps) {
+    case 1: return launch_getrf_task_w<1>(args, ctas, g, s);
+    case 2: return launch_getrf_task_w<2>(args, ctas, g, s);
+    case 4: return launch_getrf_task_w<4>(args, ctas, g, s);
+    case 8: return launch_getrf_task_w<8>(args, ctas, g, s);
+    case 16: return launch_getrf_task_w<16>(args, ctas, g, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s) {

@@ -98,6 +98,37 @@ __device__ __forceinline__ int warp_argmax(unsigned long long key, int idx) {
   return idx;
 }
 
+// Lanes of a group of G consecutive lanes (G = 32: the whole warp) and the group's sync mask.
+template <int G>
+__device__ __forceinline__ int group_lane() {
+  return threadIdx.x & (G - 1);
+}
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+  if constexpr (G == 32) {
+    return FULL_MASK;
+  } else {
+    return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
+  }
+}
+
+// The same argmax over the G consecutive lanes of a group (G = 8, 16 or 32); only the group's
+// lanes take part, so other groups of the warp may be elsewhere.
+template <int G>
+__device__ __forceinline__ int group_argmax(unsigned long long key, int idx) {
+  const unsigned gm = group_mask<G>();
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(gm, key, off);
+    const int oi = __shfl_xor_sync(gm, idx, off);
+    if (ok > key || (ok == key && oi < idx)) {
+      key = ok;
+      idx = oi;
+    }
+  }
+  return idx;
+}
+
 // Internals.Dot (MatFlat/Internals.cs:265-292): for an odd length the first product seeds the
 // sum, then every following pair is added as sum = sum + (x_a*y_a + x_b*y_b); an even length
 // starts from sum = 0.0.  x and y are strided.  Reproduced operation for operation.

@@ -42,6 +42,9 @@ struct BatchArgs {
   int solve_only;            // getrf/potrf: a holds the factors already; only solve the b blocks
   int split;                 // potrf: split every dot in two halves a step apart
                              // (potrf_group_split; 4n doubles of per-group scratch)
+  const int* task_first;     // getrf (double): size-bucketed tasks; task t covers order[first ..
+  const int* task_gc;        // first + cnt) worked on by groups of G lanes (gc = G | cnt << 8);
+  int ntasks;                // null task_first: one matrix per warp through `order`
   const int* dcount;         // getrf: when set, the number of matrices to take from `order` is
                              // read from device memory (a list built on the device); count
                              // stays the upper bound the grid was sized for
@@ -51,9 +54,11 @@ struct BatchArgs {
                              // leaves the rest of the SM's L1 to the matrices; null: the solves
                              // are staged in shared memory too
 };
-// Doubles per warp of BatchArgs::gsolve: getrf (one matrix per warp), and potrf (32/G groups of
-// G lanes, each with gsolve_group_doubles(G)).
+// Doubles per matrix group of BatchArgs::gsolve for getrf (a warp holds up to GETRF_GROUPS groups,
+// one matrix each), and per warp for potrf (32/G groups of G lanes, each with
+// gsolve_group_doubles(G)).
 constexpr long long GSOLVE_STRIDE = (2LL * RHS_CHUNK * (SMEM_N + 1) + 31) / 32 * 32;
+constexpr int GETRF_GROUPS = 4;   // 8 lanes per matrix at the smallest
 constexpr long long gsolve_group_doubles(int g) {
   return (2LL * RHS_CHUNK * (4 * g + 1) + 31) / 32 * 32;
 }
@@ -202,9 +207,11 @@ cudaError_t launch_getrf_strided_noalloc(double* a, int n, int lda, long long st
 int mx_panel_width();
 cudaError_t mx_panel_attr(int nmax);
 cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t s);
-// opfmt: 0 no operand copies (FP32 mode), 1 TF32 (FP32 storage), 2 BF16; R = mx_op_rows(n).
+// opfmt: 0 no operand copies (FP32 mode), 1 TF32 (FP32 storage), 2 BF16, 3 split TF32 (low
+// parts in op_a2 / op_b2); R = mx_op_rows(n).
 cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
-                     void* op_a, void* op_b, int opfmt, int R, cudaStream_t s);
+                     void* op_a, void* op_b, void* op_a2, void* op_b2, int opfmt, int R,
+                     cudaStream_t s);
 cudaError_t mx_update_fp32(float* a32, int n, int k, const int* active, int count,
                            cudaStream_t s);
 int mx_op_rows(int n);
@@ -215,8 +222,10 @@ namespace mfg {
 // set when a bounded device-side wait gives up.
 cudaError_t mx_make_tensor_maps(void* op_a, void* op_b, int n, int count, bool tf32,
                                 CUtensorMap_st* tm_a, CUtensorMap_st* tm_b);
-cudaError_t mx_update_tc(const CUtensorMap_st* tm_a, const CUtensorMap_st* tm_b, float* a32,
-                         int n, int k, bool tf32, int count, int* status, cudaStream_t s);
+// mode 0 TF32, 1 BF16, 2 split TF32; tm: the maps of op_a, op_b (and op_a2, op_b2 for mode 2).
+cudaError_t mx_update_tc(const CUtensorMap_st* tm, float* a32, int n, int k, int mode, int count,
+                         int* status, cudaStream_t s);
+cudaError_t mx_tc_attr();
 // The exact FP64 fallback of the systems that did not converge, on the device.
 cudaError_t mx_fb_gather(const double* a, const double* b, double* x, double* fa, const int* state,
                          int n, int count, int* order, int* fb_count, cudaStream_t s);
@@ -242,6 +251,9 @@ long long getri_t_scratch_bytes(int n, int elem);
 cudaError_t launch_getri_batched_t(const BatchArgs& args, int elem, int ctas, cudaStream_t s);
 
 // Batched LU (+ solve); launched persistent: grid = ctas, WARPS warps per CTA.
+// Size-bucketed batched LU (+ solve): one launch per lanes-per-matrix bucket g (8, 16 or 32) over
+// the bucket's tasks (args.task_first / task_gc / ntasks / queue).
+cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g, cudaStream_t s);
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 // Float and Complex overloads of the batched LU (+ solve): args.a / args.b point at float or
 // interleaved (re, im) double arrays, offsets count elements; per-warp global scratch (orders

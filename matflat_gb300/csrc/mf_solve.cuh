@@ -19,20 +19,6 @@
 
 namespace mfg {
 
-// Lanes of a group of G consecutive lanes (G = 32: the whole warp) and the group's sync mask.
-template <int G>
-__device__ __forceinline__ int group_lane() {
-  return threadIdx.x & (G - 1);
-}
-template <int G>
-__device__ __forceinline__ unsigned group_mask() {
-  if constexpr (G == 32) {
-    return FULL_MASK;
-  } else {
-    return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
-  }
-}
-
 // Element arithmetic of the solves (Blas.SolveTriangular's double, float and Complex overloads).
 //   prod/pair  the dot-form accumulation (Internals.Dot / DotConj tree, in the dot's type)
 //   fin        x[i] = (x[i] - dot) / diag      (float: computed in double, then rounded)
@@ -53,6 +39,16 @@ struct DSolve {
   static __device__ __forceinline__ T fin0(T x, T d, bool unit) { return unit ? x : __ddiv_rn(x, d); }
   static __device__ __forceinline__ T sdiv(T x, T d) { return __ddiv_rn(x, d); }
   static __device__ __forceinline__ T msub(T x, T a, T xi) { return __dsub_rn(x, __dmul_rn(a, xi)); }
+};
+
+// DSolve with the products on the integer pipes (imul_rn: the IEEE round-to-nearest product, bit
+// for bit), which leaves the FP64 pipe the additions, subtractions and divisions.
+struct DSolveIM : DSolve {
+  static __device__ __forceinline__ Acc prod(T a, T x) { return imul_rn(a, x); }
+  static __device__ __forceinline__ Acc pair(Acc s, T a0, T x0, T a1, T x1) {
+    return __dadd_rn(s, __dadd_rn(imul_rn(a0, x0), imul_rn(a1, x1)));
+  }
+  static __device__ __forceinline__ T msub(T x, T a, T xi) { return __dsub_rn(x, imul_rn(a, xi)); }
 };
 
 struct SSolve {

@@ -47,20 +47,31 @@ __global__ void mx_round_kernel(const double* __restrict__ a, float* __restrict_
 // Low-precision operand copies for the tensor-core update, K-major: row i of L21 (global row
 // k+NB+i) at op_a[(mat*R + i)*NB ...], column j of U12 (global column k+NB+j) at
 // op_b[(mat*R + j)*NB ...]; R rows per system.  opfmt 0: none (FP32 mode), 1: FP32 storage of
-// the TF32-rounded value, 2: BF16.
-__device__ __forceinline__ void mx_store_op(void* op, long long idx, float v, int opfmt) {
-  if (opfmt == 1) {
-    uint32_t t;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
-    reinterpret_cast<uint32_t*>(op)[idx] = t;
-  } else {
+// the TF32-rounded value, 2: BF16, 3: split TF32 (high parts in op_a / op_b, low parts in
+// op_a2 / op_b2).
+__device__ __forceinline__ uint32_t tf32_rna(float v) {
+  uint32_t t;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+  return t;
+}
+
+// opfmt 3 (split TF32): v = hi + lo with hi = tf32(v) in op and lo = tf32(v - hi) in op2, so that
+// hi*hi + hi*lo + lo*hi on the tensor cores carries about FP32's precision.
+__device__ __forceinline__ void mx_store_op(void* op, void* op2, long long idx, float v,
+                                            int opfmt) {
+  if (opfmt == 2) {
     reinterpret_cast<__nv_bfloat16*>(op)[idx] = __float2bfloat16_rn(v);
+    return;
   }
+  const uint32_t hi = tf32_rna(v);
+  reinterpret_cast<uint32_t*>(op)[idx] = hi;
+  if (opfmt == 3) reinterpret_cast<uint32_t*>(op2)[idx] = tf32_rna(v - __uint_as_float(hi));
 }
 
 __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n, int k, int* ipiv,
                                                               const int* active, void* op_a,
-                                                              void* op_b, int opfmt, int R) {
+                                                              void* op_b, void* op_a2, void* op_b2,
+                                                              int opfmt, int R) {
   extern __shared__ float sp[];  // panel: (n-k) rows x NB columns, leading dimension ldp
   __shared__ float red_v[MX_THREADS / 32];
   __shared__ int red_i[MX_THREADS / 32];
@@ -143,7 +154,7 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
     const long long base = (long long)mat * R * MX_NB;
     for (int e = tid; e < (rows - MX_NB) * MX_NB; e += MX_THREADS) {
       const int i = e / MX_NB, c = e - i * MX_NB;
-      mx_store_op(op_a, base + e, sp[c * ldp + MX_NB + i], opfmt);
+      mx_store_op(op_a, op_a2, base + e, sp[c * ldp + MX_NB + i], opfmt);
     }
   }
   __syncthreads();
@@ -179,7 +190,8 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
     for (int i = 0; i < MX_NB; ++i) col[i] = us[i * MX_THREADS];
     if (opfmt != 0) {
       const long long base = ((long long)mat * R + (c - k - MX_NB)) * MX_NB;
-      for (int i = 0; i < MX_NB; ++i) mx_store_op(op_b, base + i, us[i * MX_THREADS], opfmt);
+      for (int i = 0; i < MX_NB; ++i)
+        mx_store_op(op_b, op_b2, base + i, us[i * MX_THREADS], opfmt);
     }
   }
 }
@@ -413,9 +425,11 @@ cudaError_t mx_round(const double* a, float* a32, long long total, cudaStream_t 
 }
 
 cudaError_t mx_panel(float* a32, int n, int k, int* ipiv, const int* active, int count,
-                     void* op_a, void* op_b, int opfmt, int R, cudaStream_t s) {
+                     void* op_a, void* op_b, void* op_a2, void* op_b2, int opfmt, int R,
+                     cudaStream_t s) {
   const size_t smem = sizeof(float) * ((size_t)(n - k) * MX_NB + (size_t)MX_NB * MX_THREADS);
-  mx_panel_kernel<<<count, MX_THREADS, smem, s>>>(a32, n, k, ipiv, active, op_a, op_b, opfmt, R);
+  mx_panel_kernel<<<count, MX_THREADS, smem, s>>>(a32, n, k, ipiv, active, op_a, op_b, op_a2,
+                                                  op_b2, opfmt, R);
   return cudaGetLastError();
 }
 
@@ -460,11 +474,19 @@ struct MxTcArgs {
   int* status;
 };
 
-template <bool TF32>
+// MODE 0: TF32 (kind::tf32), 1: BF16 (kind::f16), 2: split TF32 (three kind::tf32 products per K
+// step: lo*hi, hi*lo, hi*hi, from the high and low parts of both operands; tm_a2 / tm_b2 describe
+// the low parts).
+template <int MODE>
 __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant__ CUtensorMap tm_a,
                                                           const __grid_constant__ CUtensorMap tm_b,
+                                                          const __grid_constant__ CUtensorMap tm_a2,
+                                                          const __grid_constant__ CUtensorMap tm_b2,
                                                           MxTcArgs p) {
+  constexpr bool TF32 = MODE != 1;
+  constexpr bool SPLIT = MODE == 2;
   constexpr int ROWB = TF32 ? 128 : 64;          // bytes of one operand row (32 values)
+  constexpr int TILEB = MX_TC_TILE * ROWB;       // bytes of one operand tile
   constexpr uint32_t SBO = 8 * ROWB;             // 8-row swizzle atom
   constexpr uint32_t SWZ = TF32 ? 2 : 4;         // 128-byte / 64-byte swizzle
   constexpr int KSTEPS = TF32 ? 4 : 2;           // 32 bytes of K per tcgen05.mma
@@ -474,8 +496,10 @@ __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(mx_tc_smem) + 1023) & ~(uintptr_t)1023);
   uint8_t* sa = base;
-  uint8_t* sb = base + MX_TC_TILE * ROWB;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sb + MX_TC_TILE * ROWB);
+  uint8_t* sb = base + TILEB;
+  uint8_t* sa2 = base + 2 * TILEB;               // split mode only
+  uint8_t* sb2 = base + 3 * TILEB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + (SPLIT ? 4 : 2) * TILEB);
   uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
   int* issued = reinterpret_cast<int*>(slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -493,15 +517,32 @@ __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant
   tc::fence_after_sync();
   const uint32_t tmem = *slot;
   if (threadIdx.x == 0) {
-    tc::mbar_expect_tx(&bar[0], 2 * MX_TC_TILE * ROWB);
+    tc::mbar_expect_tx(&bar[0], (SPLIT ? 4 : 2) * TILEB);
     tc::tma_load_3d(sa, &tm_a, &bar[0], 0, ti * MX_TC_TILE, z);
     tc::tma_load_3d(sb, &tm_b, &bar[0], 0, tj * MX_TC_TILE, z);
+    if (SPLIT) {
+      tc::tma_load_3d(sa2, &tm_a2, &bar[0], 0, ti * MX_TC_TILE, z);
+      tc::tma_load_3d(sb2, &tm_b2, &bar[0], 0, tj * MX_TC_TILE, z);
+    }
     if (tc::mbar_wait(&bar[0], 0, MX_TC_WAIT_NS)) {
       const uint64_t ad = tc::smem_desc(sa, SBO, SWZ);
       const uint64_t bd = tc::smem_desc(sb, SBO, SWZ);
+      uint32_t acc = 0u;
+      if (SPLIT) {
+        const uint64_t ad2 = tc::smem_desc(sa2, SBO, SWZ);
+        const uint64_t bd2 = tc::smem_desc(sb2, SBO, SWZ);
 #pragma unroll
-      for (int s = 0; s < KSTEPS; ++s)      // +32 bytes of K: +2 in the encoded start address
-        tc::mma<TF32>(tmem, ad + 2 * s, bd + 2 * s, IDESC, s > 0 ? 1u : 0u);
+        for (int s = 0; s < KSTEPS; ++s) {   // the small products first
+          tc::mma<true>(tmem, ad2 + 2 * s, bd + 2 * s, IDESC, acc);
+          acc = 1u;
+          tc::mma<true>(tmem, ad + 2 * s, bd2 + 2 * s, IDESC, acc);
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < KSTEPS; ++s) {     // +32 bytes of K: +2 in the encoded start address
+        tc::mma<TF32>(tmem, ad + 2 * s, bd + 2 * s, IDESC, acc);
+        acc = 1u;
+      }
       tc::mma_commit(&bar[1]);
       *issued = 1;
     } else {
@@ -544,21 +585,31 @@ __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant
 
 // Shared memory of the update kernel: a 1024-byte alignment margin, the two operand tiles, two
 // mbarriers, the TMEM address slot and a flag.
-static size_t mx_tc_smem_bytes(bool tf32) {
-  return 1024 + 2 * MX_TC_TILE * (tf32 ? 128 : 64) + 64;
+static size_t mx_tc_smem_bytes(int mode) {
+  return 1024 + (mode == 2 ? 4 : 2) * MX_TC_TILE * (mode == 1 ? 64 : 128) + 64;
 }
 
-cudaError_t mx_update_tc(const CUtensorMap* tm_a, const CUtensorMap* tm_b, float* a32, int n,
-                         int k, bool tf32, int count, int* status, cudaStream_t s) {
+// Raises the shared-memory limit of the split mode (four 16 KB tiles); once per device.
+cudaError_t mx_tc_attr() {
+  return cudaFuncSetAttribute(mx_update_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)mx_tc_smem_bytes(2));
+}
+
+// mode 0 TF32, 1 BF16, 2 split TF32 (tm[0..1] high parts, tm[2..3] low parts).
+cudaError_t mx_update_tc(const CUtensorMap* tm, float* a32, int n, int k, int mode, int count,
+                         int* status, cudaStream_t s) {
   const int m2 = n - k - MX_NB;
   if (m2 <= 0 || count == 0) return cudaSuccess;
   const int tiles = (m2 + MX_TC_TILE - 1) / MX_TC_TILE;
   MxTcArgs p{a32, n, k, m2, tiles, status};
   const dim3 grid((unsigned)count, (unsigned)(tiles * tiles));
-  if (tf32)
-    mx_update_tc_kernel<true><<<grid, 128, mx_tc_smem_bytes(true), s>>>(*tm_a, *tm_b, p);
+  const size_t smem = mx_tc_smem_bytes(mode);
+  if (mode == 0)
+    mx_update_tc_kernel<0><<<grid, 128, smem, s>>>(tm[0], tm[1], tm[0], tm[1], p);
+  else if (mode == 1)
+    mx_update_tc_kernel<1><<<grid, 128, smem, s>>>(tm[0], tm[1], tm[0], tm[1], p);
   else
-    mx_update_tc_kernel<false><<<grid, 128, mx_tc_smem_bytes(false), s>>>(*tm_a, *tm_b, p);
+    mx_update_tc_kernel<2><<<grid, 128, smem, s>>>(tm[0], tm[1], tm[2], tm[3], p);
   return cudaGetLastError();
 }
 

@@ -131,9 +131,17 @@ struct mfg_plan {
   int mx_n = 0;      // MIXED: order of every matrix
   DevBuf mx_work;    // MIXED: FP32 factors | ipiv | operand copies | per-system state | fallback
   mfg_plan* mx_fb = nullptr;  // MIXED: the exact FP64 LU plan of the fallback (all systems)
-  alignas(64) CUtensorMap mx_tm[4];  // MIXED: TMA maps of the operand copies (TF32 A, B; BF16)
+  // MIXED: TMA maps of the operand copies: TF32 A, B | BF16 A, B | split-TF32 low parts A, B
+  alignas(64) CUtensorMap mx_tm[6];
   int ctas = 0;
   int warps = 0;
+  // GETRF (double): size-bucketed tasks.  gsel picks the lanes-per-matrix table (-1: one matrix
+  // per warp, no tasks); segment s holds the tasks of G = 32 >> s lanes per matrix.
+  int gsel = -1;
+  int seg_off[3] = {0, 0, 0};
+  int seg_cnt[3] = {0, 0, 0};
+  int* d_task_first = nullptr;
+  int* d_task_gc = nullptr;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
   // Host copies of the layout (every batched kind), for the pipelined host-buffer calls: m (QR),
   // lda, ldb (GEVD), and the offsets of a, of the second array (piv / rdiag / B), of b and of C.
@@ -283,7 +291,77 @@ void choose_shape(mfg_plan* p, int fixed_warps = 0) {
 
 // Doubles per warp of the global solve staging of a getrf / potrf plan.
 long long gsolve_stride(int kind) {
-  return kind == mfg_plan::POTRF ? mfg::GSOLVE_STRIDE_C : mfg::GSOLVE_STRIDE;
+  return kind == mfg_plan::POTRF ? mfg::GSOLVE_STRIDE_C : mfg::GSOLVE_STRIDE * mfg::GETRF_GROUPS;
+}
+
+// Lanes per matrix of the LU's size buckets, by table: 0 all 32; 1 16 up to order 128; 2 8 up to
+// order 48, 16 up to 128; 3 8 up to 128; 4 8 up to 32, 16 up to 96.  Orders above 128 always
+// take 32 lanes (their vectors live in global scratch sized per warp).
+int lu_lanes(int gsel, int n) {
+  if (n > mfg::SMEM_N) return 32;
+  switch (gsel) {
+    case 1: return 16;
+    case 2: return n <= 48 ? 8 : 16;
+    case 3: return 8;
+    case 4: return n <= 32 ? 8 : n <= 96 ? 16 : 32;
+    default: return 32;
+  }
+}
+
+// Builds the tasks of a GETRF plan for table gsel: the matrices sorted by order, every run of one
+// order cut into tasks of 32/G matrices, the tasks grouped by G, and inside each group put in
+// "snake" order (largest, smallest, second largest, ...) so that the matrices in flight average
+// out.  Uploads order / task_first / task_gc.
+int getrf_build_tasks(mfg_plan* p, int gsel) {
+  mfg_ctx* ctx = p->ctx;
+  const int count = p->count;
+  std::vector<int> idx(count);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return p->hn[x] > p->hn[y]; });
+  struct Task { int first, cnt, g; };
+  std::vector<Task> segs[3];
+  for (int i = 0; i < count;) {
+    int j = i;
+    while (j < count && p->hn[idx[j]] == p->hn[idx[i]]) j++;
+    const int g = lu_lanes(gsel, p->hn[idx[i]]);
+    const int per = 32 / g;
+    const int sg = g == 32 ? 0 : g == 16 ? 1 : 2;
+    for (int k = i; k < j; k += per) segs[sg].push_back({k, std::min(per, j - k), g});
+    i = j;
+  }
+  std::vector<int> order, first, gc;
+  order.reserve(count);
+  for (int sg = 0; sg < 3; sg++) {
+    p->seg_off[sg] = (int)first.size();
+    p->seg_cnt[sg] = (int)segs[sg].size();
+    const auto& v = segs[sg];
+    int lo = 0, hi = (int)v.size() - 1;
+    while (lo <= hi) {
+      for (int side = 0; side < 2 && lo <= hi; side++) {
+        const Task& t = side == 0 ? v[lo++] : v[hi--];
+        first.push_back((int)order.size());
+        gc.push_back(t.g | (t.cnt << 8));
+        for (int q = 0; q < t.cnt; q++) order.push_back(idx[t.first + q]);
+      }
+    }
+  }
+  p->gsel = gsel;
+  if (count > 0) {
+    MFG_CUDA(ctx, cudaMemcpy((void*)p->args.order, order.data(), sizeof(int) * count,
+                             cudaMemcpyHostToDevice));
+    MFG_CUDA(ctx, cudaMemcpy(p->d_task_first, first.data(), sizeof(int) * first.size(),
+                             cudaMemcpyHostToDevice));
+    MFG_CUDA(ctx, cudaMemcpy(p->d_task_gc, gc.data(), sizeof(int) * gc.size(),
+                             cudaMemcpyHostToDevice));
+  }
+  p->args.task_first = p->d_task_first;
+  p->args.task_gc = p->d_task_gc;
+  p->args.ntasks = (int)first.size();
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return MFG_OK;
 }
 
 // Re-shapes a getrf/potrf plan: warps per CTA (1, 2, 4, 8 or 16), warps per SM, lanes per
@@ -295,6 +373,17 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
   const long long need = ((long long)p->count + warps - 1) / warps;
   if (ctas > need) ctas = need;
   if (ctas < 1) ctas = 1;
+  if (p->kind == mfg_plan::GETRF && group != p->gsel && group >= -1 && group <= 4) {
+    if (group >= 0) {
+      const int rc = getrf_build_tasks(p, group);
+      if (rc != MFG_OK) return rc;
+    } else {
+      p->gsel = -1;
+      p->args.task_first = nullptr;
+      p->args.task_gc = nullptr;
+      p->args.ntasks = 0;
+    }
+  }
   const int g = p->kind == mfg_plan::POTRF ? group : 32;
   const int smem_n = p->kind == mfg_plan::POTRF ? 4 * g : mfg::SMEM_N;
   long long stride = 0;
@@ -338,7 +427,8 @@ long long tune_key(int kind, int max_n, int count) {
 
 // A shape forced through the environment wins over the tuning table.
 bool tune_env_override() {
-  const char* names[] = {"MFG_WARPS_PER_CTA", "MFG_WARPS_PER_SM", "MFG_HW_MUL", "MFG_CHOL_GROUP"};
+  const char* names[] = {"MFG_WARPS_PER_CTA", "MFG_WARPS_PER_SM", "MFG_HW_MUL", "MFG_CHOL_GROUP",
+                         "MFG_LU_GROUPS"};
   for (const char* n : names) {
     const char* v = std::getenv(n);
     if (v && *v) return true;
@@ -351,9 +441,28 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   int* queue = p->kind == mfg_plan::GEQRF  ? p->qd.queue
                : p->kind == mfg_plan::GEVD ? p->gv.queue
                                            : p->args.queue;
-  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), s);
+  const bool tasks = p->kind == mfg_plan::GETRF && p->elem == 0 && p->gsel >= 0 &&
+                     !p->args.dcount;
+  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks ? 4 : 1) * sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
+  if (tasks) {
+    // One launch per lanes-per-matrix bucket (32, then 16, then 8 lanes), each persistent over
+    // its own task queue.
+    for (int sg = 0; sg < 3; sg++) {
+      if (p->seg_cnt[sg] == 0) continue;
+      BatchArgs a = p->args;
+      a.task_first = p->d_task_first + p->seg_off[sg];
+      a.task_gc = p->d_task_gc + p->seg_off[sg];
+      a.ntasks = p->seg_cnt[sg];
+      a.queue = p->args.queue + 1 + sg;
+      const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
+      const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
+      e = mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "batched LU launch");
+    }
+    return MFG_OK;
+  }
   if (p->kind == mfg_plan::GETRF && p->elem == 1)
     e = mfg::launch_sgetrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::GETRF && p->elem == 2)
@@ -471,7 +580,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   const size_t ints = (size_t)count;
   const size_t bytes_i = ((ints * sizeof(int) + 255) / 256) * 256;
   const size_t bytes_l = ((ints * sizeof(long long) + 255) / 256) * 256;
-  const size_t total = 3 * bytes_i + 3 * bytes_l + 256;
+  const size_t total = 5 * bytes_i + 3 * bytes_l + 256;
   cudaError_t e = p->meta.reserve(total);
   if (e != cudaSuccess) {
     delete p;
@@ -484,7 +593,9 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   long long* d_aoff = (long long*)(base + 3 * bytes_i);
   long long* d_pivoff = (long long*)(base + 3 * bytes_i + bytes_l);
   long long* d_boff = (long long*)(base + 3 * bytes_i + 2 * bytes_l);
-  int* d_queue = (int*)(base + 3 * bytes_i + 3 * bytes_l);
+  int* d_queue = (int*)(base + 3 * bytes_i + 3 * bytes_l);   // 4 counters (GETRF: per bucket)
+  p->d_task_first = (int*)(base + 3 * bytes_i + 3 * bytes_l + 256);
+  p->d_task_gc = (int*)(base + 4 * bytes_i + 3 * bytes_l + 256);
 
   std::vector<char> host(total, 0);
   std::memcpy(host.data(), order.data(), ints * sizeof(int));
@@ -575,6 +686,18 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     p->hlda[i] = lda ? lda[i] : n[i];
     if (kind == mfg_plan::GETRF || kind == mfg_plan::GETRI) p->hpivoff[i] = piv_off[i];
     if (nrhs > 0) p->hboff[i] = b_off[i];
+  }
+  if (kind == mfg_plan::GETRF) {
+    // Size-bucketed tasks (lanes per matrix by order); MFG_LU_GROUPS picks the table, -1 the
+    // one-matrix-per-warp queue.
+    const int gsel = env_int("MFG_LU_GROUPS", 2);
+    if (gsel >= 0) {
+      const int rc = getrf_build_tasks(p, gsel);
+      if (rc != MFG_OK) {
+        delete p;
+        return rc;
+      }
+    }
   }
   if (kind == mfg_plan::GETRF || kind == mfg_plan::POTRF) {
     if (!tune_env_override()) {
@@ -2191,11 +2314,14 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   tp->args.solve_only = 0;
   std::vector<std::array<int, 5>> cands;
   if (plan->kind == mfg_plan::GETRF) {
-    // Four-pair dot blocks need ~100 registers (up to 20 warps/SM), two-pair blocks ~80.
-    for (int w : {4, 8})
-      for (int wps : {8, 12, 16, 20})
-        for (int mul : {0, 2}) cands.push_back({w, wps, 32, mul, 4});
-    for (int wps : {20, 24}) cands.push_back({4, wps, 32, 0, 2});
+    // Slot 2 is the lanes-per-matrix table of the size buckets (lu_lanes; -1: one matrix per
+    // warp).  Two-pair dot blocks need ~72 registers (up to 28 warps/SM), four-pair ~100.  Tables
+    // with 16 or 8 lanes per matrix keep 2 or 4 matrices in flight per warp, so they are tried at
+    // fewer warps per SM.
+    for (int gsel : {0, 1, 2, 4})
+      for (int wps : {8, 12, 16, 24}) cands.push_back({4, wps, gsel, 0, 2});
+    cands.push_back({4, 24, -1, 0, 2});
+    cands.push_back({4, 20, -1, 0, 4});
   } else {
     // The integer-product variants need ~100 registers (up to 20 warps/SM), the FP64-pipe ones
     // ~128 (16 warps/SM).
@@ -3211,6 +3337,8 @@ struct MixedLayout {
   int* ipiv;
   void* op_a;
   void* op_b;
+  void* op_a2;      // split TF32: the low parts
+  void* op_b2;
   double* anorm;
   int* state;
   int* active;
@@ -3232,6 +3360,8 @@ MixedLayout mixed_layout(void* base, int count, int n, size_t* bytes) {
   L.ipiv = cv.take<int>((size_t)n * count);
   L.op_a = cv.take<float>(ops);
   L.op_b = cv.take<float>(ops);
+  L.op_a2 = cv.take<float>(ops);
+  L.op_b2 = cv.take<float>(ops);
   L.anorm = cv.take<double>(count);
   L.state = cv.take<int>(count);
   L.active = cv.take<int>(count);
@@ -3261,6 +3391,9 @@ int mixed_plan_setup(mfg_ctx* ctx, mfg_plan* p) {
                                            &p->mx_tm[1]));
     MFG_CUDA(ctx, mfg::mx_make_tensor_maps(L.op_a, L.op_b, n, count, false, &p->mx_tm[2],
                                            &p->mx_tm[3]));
+    MFG_CUDA(ctx, mfg::mx_make_tensor_maps(L.op_a2, L.op_b2, n, count, true, &p->mx_tm[4],
+                                           &p->mx_tm[5]));
+    MFG_CUDA(ctx, mfg::mx_tc_attr());
     // The fallback's exact FP64 LU over every system slot (only the listed ones run).
     std::vector<int> nn(count, n);
     std::vector<int64_t> aoff(count), poff(count);
@@ -3314,7 +3447,8 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
   if (!a) return fail(ctx, -2, "a is null");
   if (!b) return fail(ctx, -3, "b is null");
   if (!x) return fail(ctx, -4, "x is null");
-  if (lowp != MFG_LOWP_FP32 && lowp != MFG_LOWP_TF32 && lowp != MFG_LOWP_BF16)
+  if (lowp != MFG_LOWP_FP32 && lowp != MFG_LOWP_TF32 && lowp != MFG_LOWP_BF16 &&
+      lowp != MFG_LOWP_TF32X3)
     return fail(ctx, -5, "unknown low precision %d", lowp);
   if (max_iter < 0) return fail(ctx, -6, "max_iter must be >= 0");
   if (!(tol > 0)) return fail(ctx, -7, "tol must be > 0");
@@ -3324,18 +3458,22 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
   const int n = plan->mx_n, count = plan->count, nb = mfg::mx_panel_width();
   cudaStream_t s = ctx->stream;
   const MixedLayout L = mixed_layout(plan->mx_work.ptr, count, n, nullptr);
-  const int opfmt = lowp == MFG_LOWP_TF32 ? 1 : lowp == MFG_LOWP_BF16 ? 2 : 0;
+  const int opfmt = lowp == MFG_LOWP_TF32 ? 1 : lowp == MFG_LOWP_BF16 ? 2
+                  : lowp == MFG_LOWP_TF32X3 ? 3 : 0;
+  // TMA maps of the mode: high parts (or the only parts) first, then the split mode's low parts.
+  const CUtensorMap tm[4] = {plan->mx_tm[opfmt == 2 ? 2 : 0], plan->mx_tm[opfmt == 2 ? 3 : 1],
+                             plan->mx_tm[4], plan->mx_tm[5]};
   const int R = mfg::mx_op_rows(n);
   MFG_CUDA(ctx, mfg::mx_round(a, L.a32, (long long)n * n * count, s));
   for (int k = 0; k < n; k += nb) {
-    MFG_CUDA(ctx, mfg::mx_panel(L.a32, n, k, L.ipiv, nullptr, count, L.op_a, L.op_b, opfmt, R, s));
+    MFG_CUDA(ctx, mfg::mx_panel(L.a32, n, k, L.ipiv, nullptr, count, L.op_a, L.op_b, L.op_a2,
+                                L.op_b2, opfmt, R, s));
     if (n - k - nb <= 0) continue;
     if (opfmt == 0) {
       MFG_CUDA(ctx, mfg::mx_update_fp32(L.a32, n, k, nullptr, count, s));
     } else {
-      const int t = opfmt == 1 ? 0 : 2;
-      MFG_CUDA(ctx, mfg::mx_update_tc(&plan->mx_tm[t], &plan->mx_tm[t + 1], L.a32, n, k,
-                                      opfmt == 1, count, L.status, s));
+      MFG_CUDA(ctx, mfg::mx_update_tc(tm, L.a32, n, k, opfmt == 1 ? 0 : opfmt == 2 ? 1 : 2, count,
+                                      L.status, s));
     }
   }
   MFG_CUDA(ctx, cudaMemsetAsync(L.active, 0xFF, sizeof(int) * count, s));

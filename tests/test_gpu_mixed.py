@@ -32,7 +32,7 @@ def _solve(mf, a, b, count, n, lowp, max_iter):
             info.cpu().numpy())
 
 
-@pytest.mark.parametrize("lowp", ["fp32", "tf32", "bf16"])
+@pytest.mark.parametrize("lowp", ["fp32", "tf32", "bf16", "tf32x3"])
 @pytest.mark.parametrize("cond", [1e2, 1e5, 1e8])
 @pytest.mark.parametrize("n,count", [(96, 6), (512, 4)])
 def test_mixed_solve(mf, lowp, cond, n, count):
@@ -50,6 +50,9 @@ def test_mixed_solve(mf, lowp, cond, n, count):
         # refinement converges from the FP32 and TF32 factors
         assert (gi == 0).all(), (gi, it)
         assert it.max() <= 8, it
+    if cond <= 1e5 and lowp in ("fp32", "tf32x3"):
+        # FP32-level factors (FP32 cores, or split TF32 on the tensor cores) at cond 1e5
+        assert (gi == 0).all(), (gi, it)
     if cond <= 1e2 and lowp == "bf16":
         assert (gi == 0).any(), (gi, it)   # the BF16 tensor-core factor is usable
     if cond >= 1e8 and lowp != "fp32":
@@ -59,7 +62,7 @@ def test_mixed_solve(mf, lowp, cond, n, count):
 def test_mixed_solve_n1024(mf):
     count, n, cond = 2, 1024, 1e5
     a, b, xt = synth.conditioned_batch(count, n, cond, seed=11)
-    for lowp in ("tf32", "bf16"):
+    for lowp in ("tf32", "bf16", "tf32x3"):
         x, gb, it, gi = _solve(mf, a, b, count, n, lowp, 20)
         for i in range(count):
             A = a[i * n * n:(i + 1) * n * n].reshape(n, n).T

@@ -380,3 +380,40 @@ def test_qr_batched_least_squares(mf, dtype):
             res = np.linalg.norm(A.T @ (A @ x.astype(np.float64) - bi))
             assert res / scale <= tol, (i, res / scale)
         assert np.max(np.abs(xg - xo)) <= tol * 1e3 * max(1.0, np.max(np.abs(xo)))
+
+
+@pytest.mark.parametrize("table", [-1, 0, 1, 2, 3, 4])
+def test_lu_batched_every_lanes_table(mf, table, monkeypatch):
+    """Every lanes-per-matrix table of the size-bucketed LU (8, 16 or 32 lanes per matrix by
+    order; -1 the one-matrix-per-warp queue) gives the oracle's factors, pivots, signs and
+    solutions bit for bit, over orders 1..140 and uneven, ragged tasks."""
+    import torch
+    monkeypatch.setenv("MFG_LU_GROUPS", str(table))
+    rng = np.random.default_rng(40 + table)
+    n = rng.integers(1, 141, size=157).astype(np.int32)
+    n[:9] = [1, 2, 8, 9, 48, 49, 96, 128, 129]
+    nrhs = 4
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]])
+    a = rng.standard_normal(int(sz.sum()))
+    a[a_off[11]:a_off[11] + n[11] * n[11]] = 0.0
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]])
+    b_off = piv_off * nrhs
+    b = rng.standard_normal(int(n.sum()) * nrhs)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=nrhs, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(int(n.sum()), dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    oa, ob = a.copy(), b.copy()
+    opiv = np.zeros(int(n.sum()), np.int32)
+    osign = np.zeros(len(n), np.int32)
+    oracle.lu_solve_batched(n, a_off, oa, piv_off, opiv, b_off, ob, nrhs, osign, 4)
+    assert_bits(_host(da), oa)
+    np.testing.assert_array_equal(_host(dpiv), opiv)
+    np.testing.assert_array_equal(_host(dsign), osign)
+    assert_bits(_host(db), ob)
+    assert _host(dinfo)[11] == 1
