@@ -722,6 +722,8 @@ def main():
         a_host = torch.from_numpy(d["a"].astype(npdt)).pin_memory()
         b_host = torch.from_numpy(d["b"].astype(npdt)).pin_memory()
         plan = mf.QrBatch(d["m"], d["n"], d["a_off"], d["rdiag_off"], nrhs=1, b_off=d["b_off"])
+        if not args.no_autotune:
+            tuned = plan.autotune()
         a0 = a_host.to("cuda")
         b0 = b_host.to("cuda")
         a = torch.empty_like(a0)

@@ -459,15 +459,18 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
                                     int lowp, int max_iter, double tol, double* berr, int* iters,
                                     int* info);
 
-/* Launch-shape autotuner (no counterpart in the reference) for getrf and potrf plans.  Times
- * candidate shapes — warps per CTA and per SM, lanes per matrix (potrf) and which pipe does the
- * multiplies — on a synthetic batch of up to 20,000 matrices with the plan's size mix (sampled
- * evenly), installs the fastest in the plan and records it in the context's tuning table under the
- * plan's size bucket (kind, largest order, batch size), so later plans of that bucket on this
- * context start from it.  Synchronous; allocates and frees its own buffers; every shape gives the
- * same bits.  config (may be NULL) receives 5 ints: {warps per CTA, warps per SM, lanes per
- * matrix, multiply mode, dot-product pairs per pipelined block}.  Environment overrides of the shape (MFG_WARPS_PER_*, MFG_HW_MUL,
- * MFG_CHOL_GROUP) take precedence over the table for new plans. */
+/* Launch-shape autotuner (no counterpart in the reference) for getrf, potrf and geqrf plans.
+ * Times candidate shapes on a synthetic batch with the plan's size mix (sampled evenly: up to
+ * 20,000 matrices, 8,000 for QR), installs the fastest in the plan and records it in the
+ * context's tuning table under the plan's size bucket, so later plans of that bucket on this
+ * context start from it.  getrf: the lanes-per-matrix table of its size buckets (8, 16 or 32
+ * lanes per matrix by order; -1 one matrix per warp), warps per SM, dot-product block; potrf:
+ * lanes per matrix, warps per SM, multiply pipe; geqrf: lanes per matrix and warps per SM, keyed
+ * by the (largest m, largest n) bucket.  Synchronous; allocates and frees its own buffers; every
+ * shape gives the same bits.  config (may be NULL) receives 5 ints: {warps per CTA, warps per
+ * SM, lanes per matrix (getrf: the lanes table), multiply mode, dot-product pairs per pipelined
+ * block}.  Environment overrides of the shape (MFG_WARPS_PER_*, MFG_HW_MUL, MFG_CHOL_GROUP,
+ * MFG_LU_GROUPS, MFG_QR_GROUP) take precedence over the table for new plans. */
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan);

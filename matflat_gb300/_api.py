@@ -483,8 +483,9 @@ class _Batch:
 
     def autotune(self):
         """Times candidate launch shapes on a synthetic batch with this plan's size mix and keeps
-        the fastest (getrf and potrf plans); returns (warps per CTA, warps per SM, lanes per
-        matrix, multiply mode, dot pairs per block)."""
+        the fastest (getrf, potrf and geqrf plans); returns (warps per CTA, warps per SM, lanes
+        per matrix (getrf: the lanes table of its size buckets), multiply mode, dot pairs per
+        block)."""
         cfg = (ctypes.c_int * 5)()
         rc = self.ctx.lib.mfg_plan_autotune(self.h, cfg)
         self.ctx.check(rc, "mfg_plan_autotune")

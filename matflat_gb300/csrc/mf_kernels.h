@@ -193,6 +193,8 @@ cudaError_t launch_ger_strided_t(int elem, int m, int n, const void* x, int incx
                                  const void* y, int incy, long long sy, void* a, int lda,
                                  long long sa, int count, int conj, cudaStream_t s);
 
+// Fills a QR plan's matrices and right-hand sides with the autotuner's synthetic batch (tune.cu).
+cudaError_t launch_tune_fill_qr(const QrBatchArgs<double>& args, cudaStream_t s);
 // Fills args.a (and args.b when nrhs > 0) with the autotuner's synthetic batch (tune.cu).
 cudaError_t launch_tune_fill(const BatchArgs& args, int spd, cudaStream_t s);
 

@@ -123,6 +123,9 @@ struct mfg_plan {
   mfg::GevdArgs gv{};  // GEVD: the front half of the generalized eigenproblem
   mfg::QrBatchArgs<double> qz{};  // GEQRF: the Complex overload (interleaved doubles)
   int qr_max_cols = 0;             // GEQRF: max over the batch of n + nrhs
+  int qr_coef_need = 0;            // GEQRF: per-group coefficient count (fused: 2 (n + nrhs))
+  const int* qr_order_work = nullptr;     // GEQRF: queue order for 32 lanes (longest first)
+  const int* qr_order_grouped = nullptr;  // GEQRF: queue order for smaller groups (by n, then m)
   int qr_float = 0;  // GEQRF: which overload the next launch runs (0 double, 1 float, 2 Complex)
   int elem = 0;      // GETRF/POTRF/GETRI/GEVD: element type of the next launch (0 double, 1 float,
                      // 2 Complex)
@@ -810,6 +813,54 @@ int plan_create_gevd(mfg_ctx* ctx, mfg_plan** out, int count, const int* n, cons
   return MFG_OK;
 }
 
+int max_n_of(const int* n, int count) {
+  int mx = 0;
+  for (int i = 0; i < count; i++) mx = std::max(mx, n[i]);
+  return mx;
+}
+
+// Tuning-table key of a QR plan: the buckets of its largest n (16, 32, 64, more) and largest m
+// (128, 256, 512, more) and the batch size's power of two.
+long long qr_tune_key(int max_n, int max_m, int count) {
+  const int nb = max_n <= 16 ? 0 : max_n <= 32 ? 1 : max_n <= 64 ? 2 : 3;
+  const int mb = max_m <= 128 ? 0 : max_m <= 256 ? 1 : max_m <= 512 ? 2 : 3;
+  int cb = 0;
+  while (cb < 40 && (1LL << (cb + 1)) <= count) cb++;
+  return (long long)mfg_plan::GEQRF * 10000 + nb * 1000 + mb * 100 + cb;
+}
+
+// Re-shapes a QR plan: lanes per matrix (4, 8, 16 or 32, both real overloads) and warps per SM;
+// picks the matching queue order, grows the coefficient scratch, drops the cached graph.
+int qr_reshape(mfg_plan* p, int group, int wps) {
+  mfg_ctx* ctx = p->ctx;
+  if (group != 4 && group != 8 && group != 16 && group != 32) return MFG_OK;
+  const int warps = group == 32 ? env_int("MFG_WARPS_PER_CTA", 4) : 4;
+  long long ctas = (long long)ctx->sm_count * wps / warps;
+  const long long per = group == 32 ? 1 : 32 / group;
+  const long long need = ((long long)p->count + warps * per - 1) / (warps * per);
+  if (ctas > need) ctas = need;
+  if (ctas < 1) ctas = 1;
+  long long stride = 0;
+  if (p->qr_coef_need > mfg::qr_smem_coefs(group)) {
+    stride = (p->qr_coef_need + 31) / 32 * 32;
+    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // the scratch may be in use
+    MFG_CUDA(ctx, p->scratch.reserve((size_t)stride * sizeof(double) * (size_t)ctas * warps *
+                                     (size_t)(32 / group)));
+  }
+  p->warps = warps;
+  p->ctas = (int)ctas;
+  p->qd.group = p->qs.group = group;
+  p->qd.order = p->qs.order = group < 32 ? p->qr_order_grouped : p->qr_order_work;
+  p->qd.gscratch_stride = p->qs.gscratch_stride = stride;
+  p->qd.gscratch = (double*)p->scratch.ptr;
+  p->qs.gscratch = (float*)p->scratch.ptr;
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return MFG_OK;
+}
+
 int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const int* n,
                    const int* lda, const int64_t* a_off, const int64_t* rdiag_off, int nrhs,
                    const int64_t* b_off) {
@@ -932,6 +983,9 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   p->qz.gscratch_stride = 0;
   p->qr_max_cols = max_cols;
   const int* order_grouped = (const int*)(base + 4 * bi + 3 * bl + 256);
+  p->qr_order_work = (const int*)base;
+  p->qr_order_grouped = order_grouped;
+  p->qr_coef_need = coef_need;
   if (group_d < 32) p->qd.order = order_grouped;
   if (group_s < 32) p->qs.order = order_grouped;
   p->qd.gscratch = (double*)p->scratch.ptr;
@@ -945,6 +999,18 @@ int plan_create_qr(mfg_ctx* ctx, mfg_plan** out, int count, const int* m, const 
   for (int i = 0; i < count; i++) {
     p->hlda[i] = lda ? lda[i] : m[i];
     if (nrhs > 0) p->hboff[i] = b_off[i];
+  }
+  if (genv == 0 && !tune_env_override()) {
+    int max_m = 0;
+    for (int i = 0; i < count; i++) max_m = std::max(max_m, m[i]);
+    auto it = ctx->tune.find(qr_tune_key(max_n_of(n, count), max_m, count));
+    if (it != ctx->tune.end()) {
+      const int rc = qr_reshape(p, it->second[2], it->second[1]);
+      if (rc != MFG_OK) {
+        delete p;
+        return rc;
+      }
+    }
   }
   *out = p;
   return MFG_OK;
@@ -2261,12 +2327,125 @@ MFG_API int mfg_zgevd_front_batched(mfg_plan* plan, const double* a, double* b, 
   return gevd_front_any(plan, 2, a, b, c, info);
 }
 
+}  // extern "C"
+
+namespace {
+
+// QR plans: times lanes per matrix (4, 8, 16, 32) and warps per SM on a sample of up to 8,000
+// matrices spread evenly over the batch (so it keeps the plan's (m, n) mix), with the FP64
+// kernel, and installs the fastest for both real overloads; the tuning table keeps it under the
+// plan's (m, n) size bucket for later plans.
+int qr_autotune(mfg_plan* plan, int* config) {
+  mfg_ctx* ctx = plan->ctx;
+  cudaStream_t s = ctx->stream;
+  const int cap = 8000;
+  const int step = (plan->count + cap - 1) / cap;
+  std::vector<int> sm, sn;
+  for (int i = 0; i < plan->count; i += step) {
+    sm.push_back(plan->hm[i]);
+    sn.push_back(plan->hn[i]);
+  }
+  const int cnt = (int)sm.size();
+  const int nrhs = plan->nrhs;
+  std::vector<int64_t> aoff(cnt), roff(cnt), boff(cnt);
+  long long at = 0, rt = 0, bt = 0;
+  int max_m = 0, max_n = 0;
+  for (int i = 0; i < cnt; i++) {
+    aoff[i] = at;
+    at += (long long)sm[i] * sn[i];
+    roff[i] = rt;
+    rt += sn[i];
+    boff[i] = bt;
+    bt += (long long)sm[i] * nrhs;
+  }
+  for (int i = 0; i < plan->count; i++) {
+    max_m = std::max(max_m, plan->hm[i]);
+    max_n = std::max(max_n, plan->hn[i]);
+  }
+  mfg_plan* tp = nullptr;
+  int rc = plan_create_qr(ctx, &tp, cnt, sm.data(), sn.data(), nullptr, aoff.data(), roff.data(),
+                          nrhs, nrhs > 0 ? boff.data() : nullptr);
+  if (rc != MFG_OK) return rc;
+  DevBuf buf;
+  const size_t need = Carve::bytes_for(at, 8) * 2 + Carve::bytes_for(bt + 1, 8) * 2 +
+                      Carve::bytes_for(rt, 8);
+  cudaError_t ce = buf.reserve(need);
+  if (ce != cudaSuccess) {
+    mfg_plan_destroy(tp);
+    return cuda_fail(ctx, ce, "cudaMalloc(autotune batch)");
+  }
+  Carve cv(buf.ptr);
+  double* a = cv.take<double>(at);
+  double* a0 = cv.take<double>(at);
+  double* b = cv.take<double>(bt + 1);
+  double* b0 = cv.take<double>(bt + 1);
+  double* rd = cv.take<double>(rt);
+  tp->qd.a = a;
+  tp->qd.b = nrhs > 0 ? b : nullptr;
+  tp->qd.rdiag = rd;
+  tp->qd.solve_only = 0;
+  tp->qr_float = 0;
+  std::vector<std::array<int, 5>> cands;
+  for (int g : {4, 8, 16, 32})
+    for (int wps : {8, 12, 16, 24}) cands.push_back({4, wps, g, 0, 0});
+  std::array<int, 5> best = cands[0];
+  float best_ms = 3.0e38f;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ce = mfg::launch_tune_fill_qr(tp->qd, s);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(a0, a, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(b0, b, sizeof(double) * (bt + 1), cudaMemcpyDeviceToDevice, s);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  for (size_t c = 0; ce == cudaSuccess && rc == MFG_OK && c < cands.size(); c++) {
+    const auto& k = cands[c];
+    rc = qr_reshape(tp, k[2], k[1]);
+    float tmin = 3.0e38f;
+    for (int rep = 0; rc == MFG_OK && ce == cudaSuccess && rep < 2; rep++) {
+      ce = cudaMemcpyAsync(a, a0, sizeof(double) * at, cudaMemcpyDeviceToDevice, s);
+      if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(b, b0, sizeof(double) * (bt + 1), cudaMemcpyDeviceToDevice, s);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+      if (ce == cudaSuccess) rc = plan_launch(tp, s);
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (rc == MFG_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == MFG_OK && ce == cudaSuccess) tmin = std::min(tmin, ms);
+    }
+    if (tmin < best_ms) {
+      best_ms = tmin;
+      best = k;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(s);
+  buf.release();
+  mfg_plan_destroy(tp);
+  if (rc != MFG_OK) return rc;
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "autotune");
+  pipe_release(plan);
+  rc = qr_reshape(plan, best[2], best[1]);
+  if (rc != MFG_OK) return rc;
+  best[0] = plan->warps;
+  ctx->tune[qr_tune_key(max_n, max_m, plan->count)] = best;
+  if (config)
+    for (int i = 0; i < 5; i++) config[i] = best[i];
+  return MFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
+  if (plan->kind == mfg_plan::GEQRF) return plan->count > 0 ? qr_autotune(plan, config) : MFG_OK;
   if (plan->kind != mfg_plan::GETRF && plan->kind != mfg_plan::POTRF)
-    return fail(ctx, MFG_ERR_UNSUPPORTED, "autotune: getrf and potrf plans only");
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "autotune: getrf, potrf and geqrf plans only");
   if (plan->count == 0) return MFG_OK;
   cudaStream_t s = ctx->stream;
   // A sample of up to 20,000 matrices spread evenly over the batch keeps its size mix.

@@ -49,4 +49,35 @@ cudaError_t launch_tune_fill(const BatchArgs& args, int spd, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// QR plans: A (m-by-n, leading dimension lda) and the right-hand sides (m per column) uniform in
+// (-1, 1), one warp per matrix.
+__global__ void tune_fill_qr_kernel(QrBatchArgs<double> p, unsigned long long seed) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long mat = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       mat < p.count; mat += warps) {
+    const int m = p.m[mat], n = p.n[mat];
+    const long long lda = p.lda[mat];
+    double* a = p.a + p.a_off[mat];
+    for (long long e = lane; e < (long long)m * n; e += 32) {
+      const int j = (int)(e / m);
+      const int i = (int)(e - (long long)j * m);
+      a[(long long)j * lda + i] = tune_uniform(seed, mat, e);
+    }
+    if (p.nrhs > 0) {
+      double* b = p.b + p.b_off[mat];
+      for (long long e = lane; e < (long long)m * p.nrhs; e += 32)
+        b[e] = tune_uniform(seed ^ 0x5555555555555555ull, mat, e);
+    }
+  }
+}
+
+cudaError_t launch_tune_fill_qr(const QrBatchArgs<double>& args, cudaStream_t s) {
+  if (args.count <= 0) return cudaSuccess;
+  long long blocks = ((long long)args.count + 7) / 8;
+  if (blocks > 4096) blocks = 4096;
+  tune_fill_qr_kernel<<<(unsigned)blocks, 256, 0, s>>>(args, 0x13198A2E03707344ull);
+  return cudaGetLastError();
+}
+
 }  // namespace mfg

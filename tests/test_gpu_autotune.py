@@ -83,3 +83,45 @@ def test_autotune_rejects_other_plans(mf):
     batch = mf.LuInverseBatch(n, a_off, piv_off)
     with pytest.raises(RuntimeError):
         batch.autotune()
+
+
+def test_autotune_geqrf(mf):
+    """QR plans: the autotuner picks lanes per matrix and warps per SM for the plan's (m, n) mix;
+    the factors stay bit-identical to the oracle (double and float overloads), and a later plan
+    of the same size bucket, which starts from the recorded shape, too."""
+    import torch
+    rng = np.random.default_rng(43)
+    count = 600
+    m = rng.integers(64, 300, size=count).astype(np.int32)
+    n = np.minimum(rng.integers(16, 65, size=count), m).astype(np.int32)
+    a_off, atot = _packed(m, n)
+    r_off, rtot = _packed(n, np.ones_like(n))
+    b_off, btot = _packed(m, np.ones_like(m))
+    a = rng.standard_normal(atot)
+    b = rng.standard_normal(btot)
+    exp_a, exp_r = a.copy(), np.zeros(rtot)
+    for i in range(count):
+        ai = exp_a[a_off[i]:a_off[i] + m[i] * n[i]]
+        ri = exp_r[r_off[i]:r_off[i] + n[i]]
+        oracle.qr(int(m[i]), int(n[i]), ai, int(m[i]), ri)
+    for round_ in range(2):
+        batch = mf.QrBatch(m, n, a_off, r_off, nrhs=1, b_off=b_off)
+        if round_ == 0:
+            cfg = batch.autotune()
+            assert cfg[2] in (4, 8, 16, 32) and cfg[1] in (8, 12, 16, 24)
+        for dtype in (np.float64, np.float32):
+            da, db = _dev(a.astype(dtype)), _dev(b.astype(dtype))
+            dr = torch.zeros(rtot, dtype=da.dtype, device="cuda")
+            batch.run(da, dr, db, single=(dtype == np.float32))
+            mf.context().synchronize()
+            if dtype == np.float64:
+                assert_bits(_host(da), exp_a)
+                assert_bits(_host(dr), exp_r)
+            else:
+                ea, er = a.astype(np.float32), np.zeros(rtot, np.float32)
+                for i in range(0, count, 37):
+                    ai = ea[a_off[i]:a_off[i] + m[i] * n[i]]
+                    ri = er[r_off[i]:r_off[i] + n[i]]
+                    oracle.qr(int(m[i]), int(n[i]), ai, int(m[i]), ri)
+                    assert_bits(_host(da)[a_off[i]:a_off[i] + m[i] * n[i]], ai)
+        batch.close()
