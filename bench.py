@@ -76,6 +76,22 @@ CONFIGS = {
 }
 
 
+def lu_lanes(table, n):
+    """Lanes per matrix of the LU's size bucket for order n under a lanes table (the library's
+    lu_lanes, csrc/runtime.cu), to count the per-bucket launches of a step."""
+    if n > 128 or table <= 0:
+        return 32
+    if table == 1:
+        return 16
+    if table == 2:
+        return 8 if n <= 48 else 16
+    if table == 3:
+        return 8
+    if table == 4:
+        return 8 if n <= 32 else 16 if n <= 96 else 32
+    return 32
+
+
 def lu_flops(n, nrhs):
     """Algorithmic flops of LU (2n^3/3 - n^2/2 - n/6) plus nrhs two-triangle solves (2n^2)."""
     n = n.astype(np.float64)
@@ -843,6 +859,16 @@ def main():
         a.copy_(a0, non_blocking=True)
         b.copy_(b0, non_blocking=True)
 
+    # Launches of the library's kernels in one step: the LU runs one persistent launch per
+    # lanes-per-matrix bucket present in the batch, every other configuration one launch.
+    launches_per_step = 1
+    if cfg_name == "lu":
+        table = tuned[2] if tuned is not None else int(os.environ.get("MFG_LU_GROUPS", "2"))
+        launches_per_step = len({lu_lanes(table, int(v)) for v in np.unique(d["n"])}) \
+            if table >= 0 else 1
+    elif cfg_name == "bwd":
+        launches_per_step = 2     # the recomputed factor, then the backward pass
+
     # ---- device-resident throughput --------------------------------------------------------
     # Every step starts from a cold L2: a 256 MB buffer (twice the L2) is overwritten before the
     # step's timed interval (restore + run), so configurations whose inputs fit in L2 are
@@ -1042,7 +1068,7 @@ def main():
                      "lanes_table" if cfg_name == "lu" else "lanes_per_matrix", "mul_mode",
                      "dot_pairs_per_block"], tuned),
                 source="mfg_plan_autotune at plan creation (outside the timed region)"),
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * launches_per_step,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -141,8 +141,11 @@ struct mfg_plan {
   // GETRF (double): size-bucketed tasks.  gsel picks the lanes-per-matrix table (-1: one matrix
   // per warp, no tasks); segment s holds the tasks of G = 32 >> s lanes per matrix.
   int gsel = -1;
-  int seg_off[3] = {0, 0, 0};
-  int seg_cnt[3] = {0, 0, 0};
+  int seg_off[4] = {0, 0, 0, 0};
+  int seg_cnt[4] = {0, 0, 0, 0};
+  // POTRF (double): lanes-per-matrix table of the size buckets (0: one group size for the plan,
+  // args.group); segment s of `order` holds the matrices of G = 32 >> s lanes.
+  int csel = 0;
   int* d_task_first = nullptr;
   int* d_task_gc = nullptr;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
@@ -311,6 +314,44 @@ int lu_lanes(int gsel, int n) {
   }
 }
 
+// Lanes per matrix of the Cholesky's size buckets, by table: 1 4 up to order 16, 8 up to 32, 16
+// up to 64, 32 above; 2 8 up to 32, 16 up to 64, 32 above.  A group of G lanes keeps its vectors
+// in shared memory for orders up to 4G, which both tables respect.
+int chol_lanes(int csel, int n) {
+  if (csel == 1) return n <= 16 ? 4 : n <= 32 ? 8 : n <= 64 ? 16 : 32;
+  if (csel == 2) return n <= 32 ? 8 : n <= 64 ? 16 : 32;
+  return 32;
+}
+
+// Orders a POTRF plan's queue by size bucket for table csel: segments of 32, 16, 8 and 4 lanes
+// per matrix, each in decreasing order of n (the groups of a warp take consecutive entries, so
+// they get matrices of about the same order).  csel 0 restores the single queue.
+int potrf_build_segments(mfg_plan* p, int csel) {
+  mfg_ctx* ctx = p->ctx;
+  const int count = p->count;
+  std::vector<int> idx(count);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return p->hn[x] > p->hn[y]; });
+  std::vector<int> order;
+  order.reserve(count);
+  for (int sg = 0; sg < 4; sg++) {
+    p->seg_off[sg] = (int)order.size();
+    for (int i : idx)
+      if ((32 >> sg) == (csel > 0 ? chol_lanes(csel, p->hn[i]) : 32)) order.push_back(i);
+    p->seg_cnt[sg] = (int)order.size() - p->seg_off[sg];
+  }
+  if (csel == 0) order = snake_order(count, p->hn.data());
+  if (count > 0)
+    MFG_CUDA(ctx, cudaMemcpy((void*)p->args.order, order.data(), sizeof(int) * count,
+                             cudaMemcpyHostToDevice));
+  p->csel = csel;
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return MFG_OK;
+}
+
 // Builds the tasks of a GETRF plan for table gsel: the matrices sorted by order, every run of one
 // order cut into tasks of 32/G matrices, the tasks grouped by G, and inside each group put in
 // "snake" order (largest, smallest, second largest, ...) so that the matrices in flight average
@@ -387,6 +428,14 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
       p->args.ntasks = 0;
     }
   }
+  if (p->kind == mfg_plan::POTRF) {
+    const int csel = group < 0 ? -group : 0;
+    if (csel != p->csel) {
+      const int rc = potrf_build_segments(p, csel);
+      if (rc != MFG_OK) return rc;
+    }
+    if (group < 0) group = 32;
+  }
   const int g = p->kind == mfg_plan::POTRF ? group : 32;
   const int smem_n = p->kind == mfg_plan::POTRF ? 4 * g : mfg::SMEM_N;
   long long stride = 0;
@@ -431,7 +480,7 @@ long long tune_key(int kind, int max_n, int count) {
 // A shape forced through the environment wins over the tuning table.
 bool tune_env_override() {
   const char* names[] = {"MFG_WARPS_PER_CTA", "MFG_WARPS_PER_SM", "MFG_HW_MUL", "MFG_CHOL_GROUP",
-                         "MFG_LU_GROUPS"};
+                         "MFG_LU_GROUPS", "MFG_CHOL_TABLE"};
   for (const char* n : names) {
     const char* v = std::getenv(n);
     if (v && *v) return true;
@@ -446,7 +495,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
                                            : p->args.queue;
   const bool tasks = p->kind == mfg_plan::GETRF && p->elem == 0 && p->gsel >= 0 &&
                      !p->args.dcount;
-  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks ? 4 : 1) * sizeof(int), s);
+  const bool csegs = p->kind == mfg_plan::POTRF && p->elem == 0 && p->csel > 0;
+  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 5 : 1) * sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
   if (tasks) {
@@ -484,7 +534,21 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
     e = mfg::launch_spotrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->kind == mfg_plan::POTRF && p->elem == 2)
     e = mfg::launch_zpotrf_batched(p->args, p->ctas, p->warps, s);
-  else if (p->kind == mfg_plan::POTRF)
+  else if (csegs) {
+    // One launch per lanes-per-matrix bucket, each over its segment of the queue.
+    for (int sg = 0; sg < 4 && e == cudaSuccess; sg++) {
+      if (p->seg_cnt[sg] == 0) continue;
+      BatchArgs a = p->args;
+      a.order = p->args.order + p->seg_off[sg];
+      a.count = p->seg_cnt[sg];
+      a.group = 32 >> sg;
+      a.queue = p->args.queue + 1 + sg;
+      const long long per = (long long)p->warps * (32 / a.group);
+      const long long need = ((long long)a.count + per - 1) / per;
+      const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
+      e = mfg::launch_potrf_batched(a, ctas, p->warps, s);
+    }
+  } else if (p->kind == mfg_plan::POTRF)
     e = mfg::launch_potrf_batched(p->args, p->ctas, p->warps, s);
   else if (p->qr_float == 2)
     e = mfg::launch_zqr_batched(p->qz, p->ctas, p->warps, s);
@@ -596,7 +660,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
   long long* d_aoff = (long long*)(base + 3 * bytes_i);
   long long* d_pivoff = (long long*)(base + 3 * bytes_i + bytes_l);
   long long* d_boff = (long long*)(base + 3 * bytes_i + 2 * bytes_l);
-  int* d_queue = (int*)(base + 3 * bytes_i + 3 * bytes_l);   // 4 counters (GETRF: per bucket)
+  int* d_queue = (int*)(base + 3 * bytes_i + 3 * bytes_l);   // work counters (one per bucket)
   p->d_task_first = (int*)(base + 3 * bytes_i + 3 * bytes_l + 256);
   p->d_task_gc = (int*)(base + 4 * bytes_i + 3 * bytes_l + 256);
 
@@ -696,6 +760,16 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     const int gsel = env_int("MFG_LU_GROUPS", 2);
     if (gsel >= 0) {
       const int rc = getrf_build_tasks(p, gsel);
+      if (rc != MFG_OK) {
+        delete p;
+        return rc;
+      }
+    }
+  }
+  if (kind == mfg_plan::POTRF) {
+    const int csel = env_int("MFG_CHOL_TABLE", 0);
+    if (csel == 1 || csel == 2) {
+      const int rc = potrf_build_segments(p, csel);
       if (rc != MFG_OK) {
         delete p;
         return rc;
@@ -2509,6 +2583,9 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
         for (int mul : {0, 1}) cands.push_back({4, wps, g, mul, 4});
       cands.push_back({4, 20, g, 0, 4});
     }
+    // Lanes per matrix by size bucket (slot 2 = -table, chol_lanes).
+    for (int t : {1, 2})
+      for (int wps : {12, 16, 20}) cands.push_back({4, wps, -t, 0, 4});
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::array<int, 5> best = cands[0];

@@ -417,3 +417,43 @@ def test_lu_batched_every_lanes_table(mf, table, monkeypatch):
     np.testing.assert_array_equal(_host(dsign), osign)
     assert_bits(_host(db), ob)
     assert _host(dinfo)[11] == 1
+
+
+@pytest.mark.parametrize("table", [0, 1, 2])
+def test_cholesky_batched_every_lanes_table(mf, table, monkeypatch):
+    """The batched Cholesky + solve with lanes per matrix chosen per size bucket (4/8/16/32 lanes
+    by order; 0: one group size for the plan) gives the oracle's factors, solutions and info bit
+    for bit over orders 1..140."""
+    import torch
+    monkeypatch.setenv("MFG_CHOL_TABLE", str(table))
+    rng = np.random.default_rng(60 + table)
+    n = rng.integers(1, 141, size=150).astype(np.int32)
+    n[:8] = [1, 4, 16, 17, 32, 33, 64, 129]
+    mats = []
+    for k in n:
+        bm = rng.standard_normal((k, k))
+        mats.append((bm @ bm.T + k * np.eye(k)).reshape(-1, order="F"))
+    mats[9] = -mats[9]                                       # not positive definite
+    a = np.concatenate(mats)
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]])
+    b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]])
+    b = rng.standard_normal(int(n.sum()))
+    batch = mf.CholeskyBatch(n, a_off, nrhs=1, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, db, dinfo)
+    mf.context().synchronize()
+    oa, ob = a.copy(), b.copy()
+    oinfo = np.zeros(len(n), np.int32)
+    oracle.chol_solve_batched(n, a_off, oa, b_off, ob, oinfo, 4)
+    gi = _host(dinfo)
+    np.testing.assert_array_equal(gi, oinfo)
+    ga, gb = _host(da), _host(db)
+    for i in range(len(n)):
+        if oinfo[i] != 0:
+            continue
+        s0, s1 = a_off[i], a_off[i] + sz[i]
+        assert_bits(ga[s0:s1], oa[s0:s1])
+        assert_bits(gb[b_off[i]:b_off[i] + n[i]], ob[b_off[i]:b_off[i] + n[i]])
