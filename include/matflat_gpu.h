@@ -461,7 +461,7 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
 
 /* Launch-shape autotuner (no counterpart in the reference) for getrf, potrf and geqrf plans.
  * Times candidate shapes on a synthetic batch with the plan's size mix (sampled evenly: up to
- * 20,000 matrices, 8,000 for QR), installs the fastest in the plan and records it in the
+ * 100,000 matrices, 50,000 for QR), installs the fastest in the plan and records it in the
  * context's tuning table under the plan's size bucket, so later plans of that bucket on this
  * context start from it.  getrf: the lanes-per-matrix table of its size buckets (8, 16 or 32
  * lanes per matrix by order; -1 one matrix per warp), warps per SM, dot-product block; potrf:

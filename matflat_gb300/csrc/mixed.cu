@@ -561,6 +561,8 @@ __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant
   if (ready) {
     const int row = ti * MX_TC_TILE + warp * 32 + lane;
     float* c0 = p.a32 + (long long)z * p.n * p.n + (long long)(p.k + 32) * p.n + (p.k + 32);
+    // All 32 loads of a column chunk are issued before any store (the compiler cannot reorder
+    // loads above stores to the same array), so each thread keeps 32 reads in flight.
 #pragma unroll 1
     for (int c = 0; c < MX_TC_TILE / 32; ++c) {
       uint32_t r[32];
@@ -569,9 +571,12 @@ __global__ void __launch_bounds__(128) mx_update_tc_kernel(const __grid_constant
       if (row < p.m2) {
         float* dst = c0 + (long long)col0 * p.n + row;
         const int ncol = min(32, p.m2 - col0);
+        float old[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) old[q] = q < ncol ? dst[(long long)q * p.n] : 0.0f;
 #pragma unroll
         for (int q = 0; q < 32; ++q)
-          if (q < ncol) dst[(long long)q * p.n] -= __uint_as_float(r[q]);
+          if (q < ncol) dst[(long long)q * p.n] = old[q] - __uint_as_float(r[q]);
       }
     }
   }

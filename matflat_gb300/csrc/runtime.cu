@@ -2405,14 +2405,16 @@ MFG_API int mfg_zgevd_front_batched(mfg_plan* plan, const double* a, double* b, 
 
 namespace {
 
-// QR plans: times lanes per matrix (4, 8, 16, 32) and warps per SM on a sample of up to 8,000
+// QR plans: times lanes per matrix (4, 8, 16, 32) and warps per SM on a sample of up to 50,000
 // matrices spread evenly over the batch (so it keeps the plan's (m, n) mix), with the FP64
 // kernel, and installs the fastest for both real overloads; the tuning table keeps it under the
 // plan's (m, n) size bucket for later plans.
 int qr_autotune(mfg_plan* plan, int* config) {
   mfg_ctx* ctx = plan->ctx;
   cudaStream_t s = ctx->stream;
-  const int cap = 8000;
+  // Groups of fewer lanes hold 2-8 matrices per warp: the sample must keep every warp of the
+  // launch busy for many matrices, or the trial favours 32 lanes (it did with 8,000 matrices).
+  const int cap = 50000;
   const int step = (plan->count + cap - 1) / cap;
   std::vector<int> sm, sn;
   for (int i = 0; i < plan->count; i += step) {
@@ -2522,8 +2524,9 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
     return fail(ctx, MFG_ERR_UNSUPPORTED, "autotune: getrf, potrf and geqrf plans only");
   if (plan->count == 0) return MFG_OK;
   cudaStream_t s = ctx->stream;
-  // A sample of up to 20,000 matrices spread evenly over the batch keeps its size mix.
-  const int cap = 20000;
+  // A sample of up to 100,000 matrices spread evenly over the batch keeps its size mix, and
+  // keeps enough tasks per warp for the tables that put several matrices in a warp.
+  const int cap = 100000;
   const int step = (plan->count + cap - 1) / cap;
   std::vector<int> sn;
   for (int i = 0; i < plan->count; i += step) sn.push_back(plan->hn[i]);

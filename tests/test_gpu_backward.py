@@ -43,7 +43,8 @@ def test_backward_matches_reference_vjp(mf, recompute):
     a = torch.from_numpy(_flat(mats)).cuda()
     info = torch.zeros(len(ns), dtype=torch.int32, device="cuda")
     if not recompute:
-        plan.run(a, None, info)
+        scratch_b = torch.zeros(btotal, dtype=torch.float64, device="cuda")
+        plan.run(a, scratch_b, info)
     lbar = torch.from_numpy(_flat(lbars)).cuda()
     abar = torch.zeros(total, dtype=torch.float64, device="cuda")
     bbar = torch.zeros(btotal, dtype=torch.float64, device="cuda")
