@@ -149,6 +149,139 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
   // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
 }
 
+// ---------------------------------------------------------------------------------------------
+// The same schedule with a whole CTA of W warps on one matrix, for large orders when there are too
+// few matrices to give every SM several warps (and for the mixed solver's FP64 fallback): a step's
+// 2(n-k-1) dots are spread over the CTA's threads, the pivot search is a warp argmax followed by a
+// reduction over the W warps' candidates (larger key, then smaller row), and the swap and the
+// scaling are spread over the threads.  Per-entry arithmetic is unchanged, so the bits are the same.
+struct CtaRed {
+  unsigned long long key[32];
+  int idx[32];
+  int nan0;
+};
+
+template <int W>
+__device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int mode,
+                                     const double* scol, int* piv, int& sign, int& info,
+                                     CtaRed* red) {
+  using Tr = DTraits;
+  constexpr int T = W * 32;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  double* cc = a + (long long)c * lda;
+  unsigned long long bkey = 0ull;
+  int bidx = INT_MAX;
+  if (mode == 0) {
+    for (int i = c + tid; i < n; i += T) {
+      const double v = cc[i];
+      const unsigned long long key = Tr::key(v);
+      if (key > bkey) {
+        bkey = key;
+        bidx = i;
+      }
+      if (i == c) red->nan0 = Tr::nan0(v) ? 1 : 0;
+    }
+  } else {
+    const double* l1 = a + (long long)(c - 1) * lda;
+    const double u1 = cc[c - 1];
+    const double* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
+    const double u2 = (mode == 2) ? cc[c - 2] : u1;
+    for (int i = c + tid; i < n; i += T) {
+      const double s = mode == 1 ? Tr::prod(l1[i], u1) : Tr::pair(scol[i], l2[i], u2, l1[i], u1);
+      const double v = Tr::fin(cc[i], s);
+      cc[i] = v;
+      const unsigned long long key = Tr::key(v);
+      if (key > bkey) {
+        bkey = key;
+        bidx = i;
+      }
+      if (i == c) red->nan0 = Tr::nan0(v) ? 1 : 0;
+    }
+  }
+  const int wp = warp_argmax(bkey, bidx);
+  unsigned long long wk = bkey;   // the warp's largest key, which belongs to row wp
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(FULL_MASK, wk, off);
+    if (ok > wk) wk = ok;
+  }
+  if (lane == 0) {
+    red->key[warp] = wk;
+    red->idx[warp] = wp;
+  }
+  __syncthreads();
+  unsigned long long best = red->key[0];
+  int p = red->idx[0];
+  for (int w = 1; w < W; ++w) {
+    const unsigned long long k2 = red->key[w];
+    const int i2 = red->idx[w];
+    if (k2 > best || (k2 == best && i2 < p)) {
+      best = k2;
+      p = i2;
+    }
+  }
+  if (red->nan0) p = c;
+  if (p != c && p < n) {
+    for (int col = tid; col < n; col += T) {
+      double* base = a + (long long)col * lda;
+      const double t = base[c];
+      base[c] = base[p];
+      base[p] = t;
+    }
+    if (tid == 0) {
+      const int t = piv[c];
+      piv[c] = piv[p];
+      piv[p] = t;
+    }
+    sign = -sign;
+  }
+  __syncthreads();
+  const double diag = cc[c];
+  if (Tr::nz(diag)) {
+    for (int i = c + 1 + tid; i < n; i += T) cc[i] = Tr::div(cc[i], diag);
+  } else if (info == 0) {
+    info = c + 1;
+  }
+  __syncthreads();
+}
+
+template <int W, int IM, int DB>
+__device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, int& sign,
+                       int& info, CtaRed* red) {
+  using Tr = DTraits;
+  constexpr int T = W * 32;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n; i += T) piv[i] = i;
+  sign = 1;
+  info = 0;
+  __syncthreads();
+  lu_cta_finish_column<W>(a, n, lda, 0, 0, scol, piv, sign, info, red);
+  for (int k = 0; k < n; ++k) {
+    const int k1 = k + 1;
+    const int R = n - k1;
+    const int C = (k1 < n && k >= 1) ? n - k1 : 0;
+    const double* rowk = a + k;
+    const double* colk1 = a + (long long)k1 * lda;
+    for (int d = tid; d < R + C; d += T) {
+      const bool isrow = d < R;
+      const int idx = isrow ? k1 + d : k1 + (d - R);
+      const double* x = isrow ? rowk : a + idx;
+      const double* y = isrow ? a + (long long)idx * lda : colk1;
+      const int len = isrow ? k : k - 1;
+      const double s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
+      if (isrow) {
+        double* dst = a + (long long)idx * lda + k;
+        *dst = Tr::fin(*dst, s);
+      } else {
+        scol[idx] = s;
+      }
+    }
+    __syncthreads();
+    if (k1 < n)
+      lu_cta_finish_column<W>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info, red);
+  }
+}
+
 // Solves A x = b for nr right-hand sides from the factors of one square matrix:
 // b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
 // upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
@@ -334,6 +467,56 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
   }
 }
 
+// One matrix per CTA of CTA_WARPS warps, taken from `order` (count from p.count or *p.dcount;
+// with p.task_first, work item t is order position task_first[t]); the column sums in shared
+// memory (dynamic, nmax doubles), the solve by warp 0 staged in the CTA's slice of the global
+// scratch.
+constexpr int CTA_WARPS = 8;
+
+template <int IM, int DB>
+__global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p) {
+  extern __shared__ double sm_dyn[];
+  __shared__ CtaRed red;
+  __shared__ int next;
+  const int tid = threadIdx.x;
+  const int count = p.dcount ? *p.dcount : p.count;
+  for (;;) {
+    if (tid == 0) next = atomicAdd(p.queue, 1);
+    __syncthreads();
+    const int idx = next;
+    __syncthreads();
+    if (idx >= count) break;
+    const int mat = p.order[p.task_first ? p.task_first[idx] : idx];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    double* a = p.a + p.a_off[mat];
+    int* piv = p.piv + p.piv_off[mat];
+    int sign = 1, info = 0;
+    if (!p.solve_only) lu_cta<CTA_WARPS, IM, DB>(a, n, lda, piv, sm_dyn, sign, info, &red);
+    if (p.nrhs > 0 && tid < 32) {
+      double* sol = p.gscratch + (long long)blockIdx.x * p.gscratch_stride;
+      getrs_warp<DSolveIM, 32>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol,
+                               sol + RHS_CHUNK * (n | 1));
+    }
+    if (tid == 0 && !p.solve_only) {
+      p.sign[mat] = sign;
+      p.info[mat] = info;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s) {
+  const size_t smem = sizeof(double) * (size_t)nmax;
+  if (args.hw_mul)
+    getrf_cta_kernel<0, 4><<<ctas, CTA_WARPS * 32, smem, s>>>(args);
+  else
+    getrf_cta_kernel<1, 2><<<ctas, CTA_WARPS * 32, smem, s>>>(args);
+  return cudaGetLastError();
+}
+
+int getrf_cta_warps() { return CTA_WARPS; }
+
 template <int WARPS>
 static size_t getrf_task_smem_bytes() {
   return sizeof(double) * GETRF_GROUPS * GROUP_SMEM_DOUBLES * WARPS;
@@ -472,6 +655,13 @@ cudaError_t init_getrf_attributes() {
   if ((e = set_getrf_attr<2>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<4>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<8>()) != cudaSuccess) return e;
+  // The CTA-per-matrix kernel keeps the column sums of orders up to 25,600 in shared memory.
+  if ((e = cudaFuncSetAttribute(getrf_cta_kernel<0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(getrf_cta_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024)) != cudaSuccess)
+    return e;
   if ((e = set_getrf_task_attr<1>()) != cudaSuccess) return e;
   if ((e = set_getrf_task_attr<2>()) != cudaSuccess) return e;
   if ((e = set_getrf_task_attr<4>()) != cudaSuccess) return e;

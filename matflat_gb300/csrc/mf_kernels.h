@@ -256,6 +256,11 @@ cudaError_t launch_getri_batched_t(const BatchArgs& args, int elem, int ctas, cu
 // Size-bucketed batched LU (+ solve): one launch per lanes-per-matrix bucket g (8, 16 or 32) over
 // the bucket's tasks (args.task_first / task_gc / ntasks / queue).
 cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g, cudaStream_t s);
+// One CTA per matrix (getrf_cta_warps() warps) over `order` (or, with args.task_first, over the
+// listed order positions); nmax = the largest order (its column sums live in shared memory); the
+// solve's staging in args.gscratch, one slice of warp_scratch_doubles(nmax) per CTA.
+cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s);
+int getrf_cta_warps();
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 // Float and Complex overloads of the batched LU (+ solve): args.a / args.b point at float or
 // interleaved (re, im) double arrays, offsets count elements; per-warp global scratch (orders

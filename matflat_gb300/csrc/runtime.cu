@@ -146,6 +146,7 @@ struct mfg_plan {
   // POTRF (double): lanes-per-matrix table of the size buckets (0: one group size for the plan,
   // args.group); segment s of `order` holds the matrices of G = 32 >> s lanes.
   int csel = 0;
+  int cta_nmax = 0;  // GETRF: largest order of the CTA-per-matrix segment (segment 3)
   int* d_task_first = nullptr;
   int* d_task_gc = nullptr;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
@@ -363,19 +364,33 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return p->hn[x] > p->hn[y]; });
   struct Task { int first, cnt, g; };
-  std::vector<Task> segs[3];
+  std::vector<Task> segs[4];
+  // Orders above SMEM_N go to whole CTAs (segment 3) when there are too few of them to give every
+  // SM eight warps; MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
+  long long big = 0;
+  for (int i = 0; i < count; i++) big += p->hn[i] > mfg::SMEM_N ? 1 : 0;
+  const int cta_env = env_int("MFG_LU_CTA", -1);
+  const bool cta = cta_env >= 0 ? cta_env == 1 : big < 8LL * ctx->sm_count;
   for (int i = 0; i < count;) {
     int j = i;
     while (j < count && p->hn[idx[j]] == p->hn[idx[i]]) j++;
-    const int g = lu_lanes(gsel, p->hn[idx[i]]);
+    const int nn = p->hn[idx[i]];
+    if (cta && nn > mfg::SMEM_N) {
+      for (int k = i; k < j; k++) segs[3].push_back({k, 1, 0});
+      i = j;
+      continue;
+    }
+    const int g = lu_lanes(gsel, nn);
     const int per = 32 / g;
     const int sg = g == 32 ? 0 : g == 16 ? 1 : 2;
     for (int k = i; k < j; k += per) segs[sg].push_back({k, std::min(per, j - k), g});
     i = j;
   }
+  p->cta_nmax = 0;
+  for (const Task& t : segs[3]) p->cta_nmax = std::max(p->cta_nmax, p->hn[idx[t.first]]);
   std::vector<int> order, first, gc;
   order.reserve(count);
-  for (int sg = 0; sg < 3; sg++) {
+  for (int sg = 0; sg < 4; sg++) {
     p->seg_off[sg] = (int)first.size();
     p->seg_cnt[sg] = (int)segs[sg].size();
     const auto& v = segs[sg];
@@ -496,22 +511,31 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   const bool tasks = p->kind == mfg_plan::GETRF && p->elem == 0 && p->gsel >= 0 &&
                      !p->args.dcount;
   const bool csegs = p->kind == mfg_plan::POTRF && p->elem == 0 && p->csel > 0;
-  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 5 : 1) * sizeof(int), s);
+  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 6 : 1) * sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
   if (tasks) {
     // One launch per lanes-per-matrix bucket (32, then 16, then 8 lanes), each persistent over
     // its own task queue.
-    for (int sg = 0; sg < 3; sg++) {
+    for (int sg = 0; sg < 4; sg++) {
       if (p->seg_cnt[sg] == 0) continue;
       BatchArgs a = p->args;
       a.task_first = p->d_task_first + p->seg_off[sg];
       a.task_gc = p->d_task_gc + p->seg_off[sg];
       a.ntasks = p->seg_cnt[sg];
       a.queue = p->args.queue + 1 + sg;
-      const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
-      const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
-      e = mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
+      if (sg == 3) {
+        // One matrix per CTA: the CTA kernel counts its work items in `count`.
+        a.count = a.ntasks;
+        const long long slices = (long long)p->ctas * p->warps;   // scratch slices
+        const int ctas = (int)std::max<long long>(
+            1, std::min<long long>({(long long)a.ntasks, 2LL * ctx->sm_count, slices}));
+        e = mfg::launch_getrf_cta(a, ctas, p->cta_nmax, s);
+      } else {
+        const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
+        const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
+        e = mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
+      }
       if (e != cudaSuccess) return cuda_fail(ctx, e, "batched LU launch");
     }
     return MFG_OK;
@@ -3745,17 +3769,23 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
   // factor) are solved again with the exact FP64 LU, entirely on the device.
   MFG_CUDA(ctx, cudaMemsetAsync(L.fb_count, 0, sizeof(int), s));
   MFG_CUDA(ctx, mfg::mx_fb_gather(a, b, x, L.fb_a, L.state, n, count, L.fb_order, L.fb_count, s));
+  // The listed systems, one per CTA (a few systems would otherwise leave most SMs idle).
   mfg_plan* fp = plan->mx_fb;
-  fp->args.a = L.fb_a;
-  fp->args.piv = L.fb_piv;
-  fp->args.b = x;
-  fp->args.sign = L.fb_sign;
-  fp->args.info = L.fb_info;
-  fp->args.solve_only = 0;
-  fp->args.order = L.fb_order;
-  fp->args.dcount = L.fb_count;
-  const int rc = plan_launch(fp, s);
-  if (rc != MFG_OK) return rc;
+  BatchArgs fa = fp->args;
+  fa.a = L.fb_a;
+  fa.piv = L.fb_piv;
+  fa.b = x;
+  fa.sign = L.fb_sign;
+  fa.info = L.fb_info;
+  fa.solve_only = 0;
+  fa.order = L.fb_order;
+  fa.dcount = L.fb_count;
+  fa.task_first = nullptr;
+  MFG_CUDA(ctx, cudaMemsetAsync(fa.queue, 0, sizeof(int), s));
+  const long long slices = (long long)fp->ctas * fp->warps;
+  const int fctas = (int)std::max<long long>(
+      1, std::min<long long>({(long long)count, 2LL * ctx->sm_count, slices}));
+  MFG_CUDA(ctx, mfg::launch_getrf_cta(fa, fctas, n, s));
   MFG_CUDA(ctx, mfg::mx_fb_finish(L.state, info, L.fb_info, count, s));
   // Backward error of the FP64 solutions: one measuring sweep (no correction) over them.
   MFG_CUDA(ctx, mfg::mx_refine(a, b, x, L.a32, L.ipiv, n, count, -2, tol, berr, iters, L.state,

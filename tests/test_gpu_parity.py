@@ -457,3 +457,40 @@ def test_cholesky_batched_every_lanes_table(mf, table, monkeypatch):
         s0, s1 = a_off[i], a_off[i] + sz[i]
         assert_bits(ga[s0:s1], oa[s0:s1])
         assert_bits(gb[b_off[i]:b_off[i] + n[i]], ob[b_off[i]:b_off[i] + n[i]])
+
+
+@pytest.mark.parametrize("cta", ["0", "1"])
+def test_lu_batched_large_orders_cta(mf, cta, monkeypatch):
+    """Orders above 128 factored by a whole CTA per matrix (MFG_LU_CTA=1, the choice when few
+    such matrices cannot fill the GPU with warps) or one warp per matrix (0): the same bits as
+    the oracle, with small orders in the same batch."""
+    import torch
+    monkeypatch.setenv("MFG_LU_CTA", cta)
+    rng = np.random.default_rng(70)
+    n = np.concatenate([rng.integers(129, 301, size=14), rng.integers(1, 60, size=20),
+                        [129, 300, 256]]).astype(np.int32)
+    nrhs = 2
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]])
+    a = rng.standard_normal(int(sz.sum()))
+    a[a_off[3]:a_off[3] + sz[3]] = 0.0
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]])
+    b_off = piv_off * nrhs
+    b = rng.standard_normal(int(n.sum()) * nrhs)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=nrhs, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(int(n.sum()), dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    oa, ob = a.copy(), b.copy()
+    opiv = np.zeros(int(n.sum()), np.int32)
+    osign = np.zeros(len(n), np.int32)
+    oracle.lu_solve_batched(n, a_off, oa, piv_off, opiv, b_off, ob, nrhs, osign, 4)
+    assert_bits(_host(da), oa)
+    np.testing.assert_array_equal(_host(dpiv), opiv)
+    np.testing.assert_array_equal(_host(dsign), osign)
+    assert_bits(_host(db), ob)
+    assert _host(dinfo)[3] == 1
