@@ -468,13 +468,16 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
 }
 
 // One matrix per CTA of CTA_WARPS warps, taken from `order` (count from p.count or *p.dcount;
-// with p.task_first, work item t is order position task_first[t]); the column sums in shared
-// memory (dynamic, nmax doubles), the solve by warp 0 staged in the CTA's slice of the global
-// scratch.
+// with p.task_first, work item t is order position task_first[t]).  Dynamic shared memory holds
+// the column sums (nmax doubles) and, when it fits (smem_solve), the solve's staging
+// (2 RHS_CHUNK (nmax | 1) doubles after them); otherwise the solve is staged in the CTA's slice of
+// the global scratch, which plans holding orders above SMEM_N allocate.
 constexpr int CTA_WARPS = 8;
+constexpr size_t CTA_SMEM_MAX = 200 * 1024;
 
 template <int IM, int DB>
-__global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p) {
+__global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p, int nmax,
+                                                                   int smem_solve) {
   extern __shared__ double sm_dyn[];
   __shared__ CtaRed red;
   __shared__ int next;
@@ -494,7 +497,8 @@ __global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p) 
     int sign = 1, info = 0;
     if (!p.solve_only) lu_cta<CTA_WARPS, IM, DB>(a, n, lda, piv, sm_dyn, sign, info, &red);
     if (p.nrhs > 0 && tid < 32) {
-      double* sol = p.gscratch + (long long)blockIdx.x * p.gscratch_stride;
+      double* sol = smem_solve ? sm_dyn + nmax
+                               : p.gscratch + (long long)blockIdx.x * p.gscratch_stride;
       getrs_warp<DSolveIM, 32>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol,
                                sol + RHS_CHUNK * (n | 1));
     }
@@ -507,11 +511,17 @@ __global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p) 
 }
 
 cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s) {
-  const size_t smem = sizeof(double) * (size_t)nmax;
+  const size_t with_solve =
+      sizeof(double) * ((size_t)nmax + 2 * (size_t)RHS_CHUNK * (size_t)(nmax | 1));
+  const int smem_solve = with_solve <= CTA_SMEM_MAX ? 1 : 0;
+  // Without room for the solve in shared memory the staging needs the plan's global scratch.
+  if (!smem_solve && args.nrhs > 0 && !args.gscratch) return cudaErrorInvalidValue;
+  const size_t smem = smem_solve ? with_solve : sizeof(double) * (size_t)nmax;
+  if (smem > CTA_SMEM_MAX) return cudaErrorInvalidValue;
   if (args.hw_mul)
-    getrf_cta_kernel<0, 4><<<ctas, CTA_WARPS * 32, smem, s>>>(args);
+    getrf_cta_kernel<0, 4><<<ctas, CTA_WARPS * 32, smem, s>>>(args, nmax, smem_solve);
   else
-    getrf_cta_kernel<1, 2><<<ctas, CTA_WARPS * 32, smem, s>>>(args);
+    getrf_cta_kernel<1, 2><<<ctas, CTA_WARPS * 32, smem, s>>>(args, nmax, smem_solve);
   return cudaGetLastError();
 }
 
@@ -655,12 +665,13 @@ cudaError_t init_getrf_attributes() {
   if ((e = set_getrf_attr<2>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<4>()) != cudaSuccess) return e;
   if ((e = set_getrf_attr<8>()) != cudaSuccess) return e;
-  // The CTA-per-matrix kernel keeps the column sums of orders up to 25,600 in shared memory.
+  // The CTA-per-matrix kernel keeps the column sums (and, up to order ~2,800, the solve's
+  // staging) in up to CTA_SMEM_MAX bytes of shared memory.
   if ((e = cudaFuncSetAttribute(getrf_cta_kernel<0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                200 * 1024)) != cudaSuccess)
+                                (int)CTA_SMEM_MAX)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(getrf_cta_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                200 * 1024)) != cudaSuccess)
+                                (int)CTA_SMEM_MAX)) != cudaSuccess)
     return e;
   if ((e = set_getrf_task_attr<1>()) != cudaSuccess) return e;
   if ((e = set_getrf_task_attr<2>()) != cudaSuccess) return e;

@@ -257,8 +257,9 @@ cudaError_t launch_getri_batched_t(const BatchArgs& args, int elem, int ctas, cu
 // the bucket's tasks (args.task_first / task_gc / ntasks / queue).
 cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g, cudaStream_t s);
 // One CTA per matrix (getrf_cta_warps() warps) over `order` (or, with args.task_first, over the
-// listed order positions); nmax = the largest order (its column sums live in shared memory); the
-// solve's staging in args.gscratch, one slice of warp_scratch_doubles(nmax) per CTA.
+// listed order positions); nmax = the largest order.  Its column sums and, up to order ~2,800,
+// the solve's staging live in shared memory; above that the solve is staged in args.gscratch, one
+// slice of warp_scratch_doubles(nmax) per CTA (cudaErrorInvalidValue if it is missing).
 cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s);
 int getrf_cta_warps();
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);

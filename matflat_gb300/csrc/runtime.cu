@@ -286,7 +286,8 @@ void choose_shape(mfg_plan* p, int fixed_warps = 0) {
   if (inv) {
     ctas = (long long)p->ctx->sm_count * mfg::getri_ctas_per_sm();
   } else {
-    const int wps = env_int("MFG_WARPS_PER_SM", 16);
+    // 24 warps per SM for the LU (its measured best on the 100,000-matrix batch), 16 otherwise.
+    const int wps = env_int("MFG_WARPS_PER_SM", p->kind == mfg_plan::GETRF ? 24 : 16);
     ctas = (long long)p->ctx->sm_count * wps / warps;
   }
   // Never more warps than matrices.
@@ -508,8 +509,10 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   int* queue = p->kind == mfg_plan::GEQRF  ? p->qd.queue
                : p->kind == mfg_plan::GEVD ? p->gv.queue
                                            : p->args.queue;
+  // The task kernels stage their solves in the plan's gsolve slices (MFG_GSOLVE=0 plans have none
+  // and keep the one-matrix-per-warp kernel).
   const bool tasks = p->kind == mfg_plan::GETRF && p->elem == 0 && p->gsel >= 0 &&
-                     !p->args.dcount;
+                     !p->args.dcount && (p->nrhs == 0 || p->args.gsolve != nullptr);
   const bool csegs = p->kind == mfg_plan::POTRF && p->elem == 0 && p->csel > 0;
   cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 6 : 1) * sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
@@ -2598,8 +2601,12 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
     // warp).  Two-pair dot blocks need ~72 registers (up to 28 warps/SM), four-pair ~100.  Tables
     // with 16 or 8 lanes per matrix keep 2 or 4 matrices in flight per warp, so they are tried at
     // fewer warps per SM.
-    for (int gsel : {0, 1, 2, 4})
-      for (int wps : {8, 12, 16, 24}) cands.push_back({4, wps, gsel, 0, 2});
+    // Measured on the 100,000-matrix batch (n 8..128): 16 lanes per matrix at n = 128 is slower
+    // than 32 (two matrices per warp double the footprint in flight), 8 lanes pays off at small
+    // orders; the tables are tried at 20-28 warps per SM, where they are fastest.
+    for (int gsel : {0, 2, 4})
+      for (int wps : {20, 24, 28}) cands.push_back({4, wps, gsel, 0, 2});
+    cands.push_back({4, 24, 1, 0, 2});
     cands.push_back({4, 24, -1, 0, 2});
     cands.push_back({4, 20, -1, 0, 4});
   } else {

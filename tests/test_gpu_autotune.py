@@ -35,7 +35,8 @@ def test_autotune_getrf(mf):
         batch = mf.LuBatch(n, a_off, piv_off, nrhs=2, b_off=b_off)
         if round_ == 0:
             cfg = batch.autotune()
-            assert len(cfg) == 5 and cfg[0] in (4, 8) and cfg[1] in (8, 12, 16, 20, 24)
+            assert len(cfg) == 5 and cfg[0] in (4, 8) and cfg[1] in (20, 24, 28)
+            assert cfg[2] in (-1, 0, 1, 2, 4)          # the lanes table of the size buckets
             assert cfg[3] in (0, 2) and cfg[4] in (2, 4)
         da, db = _dev(a), _dev(b)
         dpiv = torch.zeros(ptot, dtype=torch.int32, device="cuda")
@@ -66,7 +67,7 @@ def test_autotune_potrf(mf):
     oracle.chol_solve_batched(n, a_off, oa, b_off, ob, oinfo, 4)
     batch = mf.CholeskyBatch(n, a_off, nrhs=1, b_off=b_off)
     cfg = batch.autotune()
-    assert cfg[2] in (4, 8, 16, 32) and cfg[3] in (0, 1)
+    assert cfg[2] in (4, 8, 16, 32, -1, -2) and cfg[3] in (0, 1)   # -t: lanes by size bucket
     da, db = _dev(a), _dev(b)
     dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
     batch.run(da, db, dinfo)
