@@ -92,6 +92,15 @@ def lu_lanes(table, n):
     return 32
 
 
+def chol_lanes(table, n):
+    """Lanes per matrix of the Cholesky's size bucket (the library's chol_lanes)."""
+    if table == 1:
+        return 4 if n <= 16 else 8 if n <= 32 else 16 if n <= 64 else 32
+    if table == 2:
+        return 8 if n <= 32 else 16 if n <= 64 else 32
+    return 32
+
+
 def lu_flops(n, nrhs):
     """Algorithmic flops of LU (2n^3/3 - n^2/2 - n/6) plus nrhs two-triangle solves (2n^2)."""
     n = n.astype(np.float64)
@@ -806,7 +815,8 @@ def main():
             outs = [a, b, piv, sign, info]
             flops = lu_flops(d["n"], d["nrhs"])
             byts = lu_bytes(d["n"], d["nrhs"])
-            kernel_key = "getrf_batched_kernel"
+            table = tuned[2] if tuned is not None else int(os.environ.get("MFG_LU_GROUPS", "2"))
+            kernel_key = "getrf_task_kernel" if table >= 0 else "getrf_batched_kernel"
         elif cfg_name in ("chol", "chol100k"):
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
             if not args.no_autotune:
@@ -868,6 +878,8 @@ def main():
             if table >= 0 else 1
     elif cfg_name == "bwd":
         launches_per_step = 2     # the recomputed factor, then the backward pass
+    elif cfg_name in ("chol", "chol100k") and tuned is not None and tuned[2] < 0:
+        launches_per_step = len({chol_lanes(-tuned[2], int(v)) for v in np.unique(d["n"])})
 
     # ---- device-resident throughput --------------------------------------------------------
     # Every step starts from a cold L2: a 256 MB buffer (twice the L2) is overwritten before the
