@@ -245,11 +245,19 @@ __global__ void __launch_bounds__(256) mx_update_fp32_kernel(float* a32, int n, 
   }
 }
 
-// Solves (LU) y = v in FP32 for one matrix per warp: the interchanges, unit-lower forward sweep,
-// upper backward sweep.  v: FP32 vector of n in shared memory of the warp.
-__device__ void mx_lu_solve_warp(const float* lu, const int* ip, int n, float* v) {
-  const int lane = threadIdx.x & 31;
-  if (lane == 0)
+// Solves (LU) y = v in FP32 for one matrix: the interchanges, unit-lower forward sweep, upper
+// backward sweep.  v: FP32 vector of n in shared memory.
+// The whole CTA works (nt threads; n a multiple of 32), in blocks of 32 columns: warp 0 solves the
+// block's 32 x 32 diagonal part with each lane holding one row in a register (the block's
+// columns loaded up front), then every thread applies the block's 32 columns to its rows outside
+// the block, column after column, with coalesced column loads.  Each entry of v receives its
+// fused multiply-adds in column-sweep order (t ascending forward, descending backward), and the
+// column loads are independent of one another: a solve is not one dependent global load per
+// column, as a single warp sweeping the columns was (measured as half of a solve's time).
+__device__ void mx_lu_solve_cta(const float* lu, const int* ip, int n, float* v) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nt = blockDim.x;
+  if (tid == 0)
     for (int i = 0; i < n; ++i) {
       const int p = ip[i];
       if (p != i) {
@@ -258,20 +266,55 @@ __device__ void mx_lu_solve_warp(const float* lu, const int* ip, int n, float* v
         v[p] = t;
       }
     }
-  __syncwarp();
-  for (int t = 0; t < n; ++t) {
-    const float yt = v[t];
-    const float* col = lu + (long long)t * n;
-    for (int i = t + 1 + lane; i < n; i += 32) v[i] = fmaf(-col[i], yt, v[i]);
-    __syncwarp();
+  __syncthreads();
+  // Forward, unit lower: v[i] -= L(i,t) v[t] for t < i, t ascending.
+  for (int b0 = 0; b0 < n; b0 += 32) {
+    if (warp == 0) {
+      const int r = b0 + lane;
+      float lr[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) lr[t] = lu[(long long)(b0 + t) * n + r];
+      float vr = v[r];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) {
+        const float yt = __shfl_sync(FULL_MASK, vr, t);
+        if (lane > t) vr = fmaf(-lr[t], yt, vr);
+      }
+      v[r] = vr;
+    }
+    __syncthreads();
+    for (int i = b0 + 32 + tid; i < n; i += nt) {
+      float vi = v[i];
+#pragma unroll 8
+      for (int t = 0; t < 32; ++t) vi = fmaf(-lu[(long long)(b0 + t) * n + i], v[b0 + t], vi);
+      v[i] = vi;
+    }
+    __syncthreads();
   }
-  for (int t = n - 1; t >= 0; --t) {
-    const float* col = lu + (long long)t * n;
-    if (lane == 0) v[t] = v[t] / col[t];
-    __syncwarp();
-    const float xt = v[t];
-    for (int i = lane; i < t; i += 32) v[i] = fmaf(-col[i], xt, v[i]);
-    __syncwarp();
+  // Backward, upper: v[t] /= U(t,t); v[i] -= U(i,t) v[t] for i < t, t descending.
+  for (int b0 = n - 32; b0 >= 0; b0 -= 32) {
+    if (warp == 0) {
+      const int r = b0 + lane;
+      float ur[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) ur[t] = lu[(long long)(b0 + t) * n + r];
+      float vr = v[r];
+#pragma unroll
+      for (int t = 31; t >= 0; --t) {
+        if (lane == t) vr = vr / ur[t];
+        const float xt = __shfl_sync(FULL_MASK, vr, t);
+        if (lane < t) vr = fmaf(-ur[t], xt, vr);
+      }
+      v[r] = vr;
+    }
+    __syncthreads();
+    for (int i = tid; i < b0; i += nt) {
+      float vi = v[i];
+#pragma unroll 8
+      for (int t = 31; t >= 0; --t) vi = fmaf(-lu[(long long)(b0 + t) * n + i], v[b0 + t], vi);
+      v[i] = vi;
+    }
+    __syncthreads();
   }
 }
 
@@ -318,8 +361,7 @@ __global__ void __launch_bounds__(MX_RT) mx_refine_kernel(
       }
       return;
     }
-    if (warp == 0) mx_lu_solve_warp(LU, IP, n, v);
-    __syncthreads();
+    mx_lu_solve_cta(LU, IP, n, v);
     for (int i = tid; i < n; i += MX_RT) X[i] = (double)v[i];
     if (tid == 0) {
       state[mat] = 0;
@@ -414,8 +456,7 @@ __global__ void __launch_bounds__(MX_RT) mx_refine_kernel(
     if (i < n) v[i] = (float)r[q];
   }
   __syncthreads();
-  if (warp == 0) mx_lu_solve_warp(LU, IP, n, v);
-  __syncthreads();
+  mx_lu_solve_cta(LU, IP, n, v);
   for (int i = tid; i < n; i += MX_RT) X[i] = sx[i] + (double)v[i];
 }
 
