@@ -157,18 +157,61 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
       mx_store_op(op_a, op_a2, base + e, sp[c * ldp + MX_NB + i], opfmt);
     }
   }
-  __syncthreads();
-  // Interchanges on the columns left and right of the panel, in order.
-  for (int c = tid; c < n; c += MX_THREADS) {
-    if (c >= k && c < k + MX_NB) continue;
-    float* col = a + (long long)c * n;
+  // Interchanges on the columns left and right of the panel.  The panel's 32 swaps (row j with
+  // row piv_s[j], in order) touch at most 64 rows; thread 0 composes them into one permutation of
+  // those rows (new row dst[q] = old row src[q]), and each warp applies it to a column at a
+  // time: all lanes gather their rows first, then scatter, so a column costs two rounds of
+  // independent accesses instead of 32 dependent swaps.
+  __shared__ int pm_src[2 * MX_NB], pm_dst[2 * MX_NB];
+  __shared__ int pm_cnt;
+  if (tid == 0) {
+    int rows_t[2 * MX_NB], cur[2 * MX_NB];
+    int nt = 0;
     for (int j = 0; j < MX_NB; ++j) {
       const int p = piv_s[j];
-      if (p != j) {
-        const float t = col[k + j];
-        col[k + j] = col[k + p];
-        col[k + p] = t;
+      if (p == j) continue;
+      int qa = -1, qb = -1;
+      for (int q = 0; q < nt; ++q) {
+        if (rows_t[q] == j) qa = q;
+        if (rows_t[q] == p) qb = q;
       }
+      if (qa < 0) {
+        rows_t[nt] = j;
+        cur[nt] = j;
+        qa = nt++;
+      }
+      if (qb < 0) {
+        rows_t[nt] = p;
+        cur[nt] = p;
+        qb = nt++;
+      }
+      const int t = cur[qa];
+      cur[qa] = cur[qb];
+      cur[qb] = t;
+    }
+    int cnt = 0;
+    for (int q = 0; q < nt; ++q)
+      if (cur[q] != rows_t[q]) {
+        pm_dst[cnt] = rows_t[q];
+        pm_src[cnt] = cur[q];
+        ++cnt;
+      }
+    pm_cnt = cnt;
+  }
+  __syncthreads();
+  {
+    const int lane = tid & 31, warp = tid >> 5, cnt = pm_cnt;
+    const int s0 = lane < cnt ? pm_src[lane] : 0, d0 = lane < cnt ? pm_dst[lane] : 0;
+    const int s1 = lane + 32 < cnt ? pm_src[lane + 32] : 0;
+    const int d1 = lane + 32 < cnt ? pm_dst[lane + 32] : 0;
+    for (int c = warp; c < n && cnt > 0; c += MX_THREADS / 32) {
+      if (c >= k && c < k + MX_NB) continue;
+      float* col = a + (long long)c * n + k;
+      const float v0 = lane < cnt ? col[s0] : 0.0f;
+      const float v1 = lane + 32 < cnt ? col[s1] : 0.0f;
+      __syncwarp();
+      if (lane < cnt) col[d0] = v0;
+      if (lane + 32 < cnt) col[d1] = v1;
     }
   }
   __syncthreads();
