@@ -131,16 +131,16 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
         sp[c * ldp + p] = t;
       }
     __syncthreads();
+    // Scale the column and apply the rank-1 update to the panel's remaining columns, a whole row
+    // per thread: the row's multiplier stays in a register, and row j (the U entries it reads)
+    // is not changed by this step, so no barrier separates the two.
     const float d = sp[j * ldp + j];
-    if (d != 0.0f)
-      for (int i = j + 1 + tid; i < rows; i += MX_THREADS) sp[j * ldp + i] /= d;
-    __syncthreads();
-    // Rank-1 update of the panel's remaining columns.
-    const int w = MX_NB - j - 1;
-    for (int e = tid; e < (rows - j - 1) * w; e += MX_THREADS) {
-      const int c = j + 1 + e / (rows - j - 1);
-      const int i = j + 1 + e % (rows - j - 1);
-      sp[c * ldp + i] = fmaf(-sp[j * ldp + i], sp[c * ldp + j], sp[c * ldp + i]);
+    for (int i = j + 1 + tid; i < rows; i += MX_THREADS) {
+      float l = sp[j * ldp + i];
+      if (d != 0.0f) l /= d;
+      sp[j * ldp + i] = l;
+      for (int c = j + 1; c < MX_NB; ++c)
+        sp[c * ldp + i] = fmaf(-l, sp[c * ldp + j], sp[c * ldp + i]);
     }
     __syncthreads();
   }
