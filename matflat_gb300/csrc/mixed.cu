@@ -204,14 +204,27 @@ __global__ void __launch_bounds__(MX_THREADS) mx_panel_kernel(float* a32, int n,
     const int s0 = lane < cnt ? pm_src[lane] : 0, d0 = lane < cnt ? pm_dst[lane] : 0;
     const int s1 = lane + 32 < cnt ? pm_src[lane + 32] : 0;
     const int d1 = lane + 32 < cnt ? pm_dst[lane + 32] : 0;
-    for (int c = warp; c < n && cnt > 0; c += MX_THREADS / 32) {
-      if (c >= k && c < k + MX_NB) continue;
-      float* col = a + (long long)c * n + k;
-      const float v0 = lane < cnt ? col[s0] : 0.0f;
-      const float v1 = lane + 32 < cnt ? col[s1] : 0.0f;
+    // Eight columns per warp and round, so eight gathers are in flight at once (k is a multiple
+    // of 32: a group of eight columns lies entirely inside or outside the panel).
+    constexpr int CG = 8;
+    for (int c0 = warp * CG; c0 < n && cnt > 0; c0 += (MX_THREADS / 32) * CG) {
+      if (c0 >= k && c0 < k + MX_NB) continue;
+      float v0[CG], v1[CG];
+#pragma unroll
+      for (int u = 0; u < CG; ++u) {
+        const float* col = a + (long long)(c0 + u) * n + k;
+        const bool ok = c0 + u < n;
+        v0[u] = ok && lane < cnt ? col[s0] : 0.0f;
+        v1[u] = ok && lane + 32 < cnt ? col[s1] : 0.0f;
+      }
       __syncwarp();
-      if (lane < cnt) col[d0] = v0;
-      if (lane + 32 < cnt) col[d1] = v1;
+#pragma unroll
+      for (int u = 0; u < CG; ++u) {
+        float* col = a + (long long)(c0 + u) * n + k;
+        if (c0 + u >= n) continue;
+        if (lane < cnt) col[d0] = v0[u];
+        if (lane + 32 < cnt) col[d1] = v1[u];
+      }
     }
   }
   __syncthreads();
