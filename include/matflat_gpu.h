@@ -512,6 +512,13 @@ MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, d
 MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, double* out,
                               int64_t n);
 
+/* Diagnostics (no MatFlat counterpart): out[i] = a[i] / b[i] computed by the integer-pipe
+ * quotient the LU and Cholesky column scalings use (with the reciprocal of b[i] as its per-divisor
+ * input), for n elements (device pointers, asynchronous on the context's stream).  It must equal
+ * the IEEE round-to-nearest quotient bit for bit. */
+MFG_API int mfg_selftest_ddiv(mfg_ctx* ctx, const double* a, const double* b, double* out,
+                              int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

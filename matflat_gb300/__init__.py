@@ -34,6 +34,7 @@ from ._api import (  # noqa: F401
     library,
     library_path,
     selftest_dmul,
+    selftest_ddiv,
 )
 
 __version__ = "0.1.0"

@@ -116,6 +116,7 @@ _SIGS = {
     "mfg_plan_getri_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _vp, _vp, _vp, _vp]),
     "mfg_dgetri_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_selftest_dmul": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
+    "mfg_selftest_ddiv": (_I, [_vp, _vp, _vp, _vp, ctypes.c_int64]),
     "mfg_plan_gesv_mixed_batched": (_I, [_vp, ctypes.POINTER(_vp), _I, _I]),
     "mfg_dgesv_mixed_batched": (_I, [_vp, _vp, _vp, _vp, _I, _I, ctypes.c_double, _vp, _vp,
                                      _vp]),
@@ -810,6 +811,13 @@ def selftest_dmul(a, b, out):
     ctx = context()
     ctx.check(ctx.lib.mfg_selftest_dmul(ctx.h, _dptr(a), _dptr(b), _dptr(out), a.numel()),
               "mfg_selftest_dmul")
+
+
+def selftest_ddiv(a, b, out):
+    """out = a / b through the integer-pipe quotient (device tensors of float64)."""
+    ctx = context()
+    ctx.check(ctx.lib.mfg_selftest_ddiv(ctx.h, _dptr(a), _dptr(b), _dptr(out), a.numel()),
+              "mfg_selftest_ddiv")
 
 
 LOWP = {"fp32": 0, "tf32": 1, "bf16": 2, "tf32x3": 3}

@@ -149,6 +149,24 @@ cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, l
   return cudaGetLastError();
 }
 
+// The integer-pipe quotient with its per-divisor reciprocal, as the factorizations use it.
+__global__ void selftest_div_kernel(const double* a, const double* b, double* out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double d = b[i];
+    out[i] = idiv_rn(a[i], d, __drcp_rn(d));
+  }
+}
+
+cudaError_t launch_selftest_div(const double* a, const double* b, double* out, long long n,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  selftest_div_kernel<<<(unsigned)blocks, 256, 0, s>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
 // Float and Complex overloads of SolveTriangular (Blas.SolveTriangular.cs:44-124, :280-395).
 // TrP: plain element arithmetic, TrC: the Conj modes (Complex only; float uses TrP for both).
 template <class TrP, class TrC>

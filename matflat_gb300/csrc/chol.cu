@@ -26,6 +26,14 @@ namespace mfg {
 // one warp per matrix; G < 32: 32/G matrices per warp, which amortises the per-column square root
 // and the serial solve steps over several matrices).  dsum: n doubles of per-group scratch.
 // Returns 0, or k+1 when A is not positive definite at column k.
+// x / lkk, the column's divisor; with IM on the integer pipes (ykk = the reciprocal of lkk, formed
+// once per column), bit-identical to the FP64 division.
+template <bool IM>
+__device__ __forceinline__ double chol_quot(double x, double lkk, double ykk) {
+  if constexpr (IM) return idiv_rn(x, lkk, ykk);
+  else return __ddiv_rn(x, lkk);
+}
+
 template <int G, bool IM>
 __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
   const int lane = group_lane<G>();
@@ -37,14 +45,15 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
     const double s = __dsub_rn(colk[k], dsum[k]);
     if (!positive(s)) return k + 1;  // uniform across the group
     const double lkk = __dsqrt_rn(s);
+    const double ykk = IM ? __drcp_rn(lkk) : 0.0;
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += G) {
       // Dot(k, a + j, lda, a + k, lda): row j of L against row k of L.
       const double d = exact_dot<IM>(k, a + j, lda, a + k, lda);
-      const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], d), lkk);
+      const double t = chol_quot<IM>(__dsub_rn(a[(long long)j * lda + k], d), lkk, ykk);
       colk[j] = t;
-      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
+      dsum[j] = __dadd_rn(dsum[j], xmul<IM>(t, t));
     }
     __syncwarp(gm);
   }
@@ -86,12 +95,13 @@ __device__ int potrf_group_split(double* a, int n, long long lda, double* dsum) 
     const double s = __dsub_rn(colk[k], dsum[k]);
     if (!positive(s)) return k + 1;  // uniform across the group
     const double lkk = __dsqrt_rn(s);
+    const double ykk = IM ? __drcp_rn(lkk) : 0.0;
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += G) {
-      const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], full[j]), lkk);
+      const double t = chol_quot<IM>(__dsub_rn(a[(long long)j * lda + k], full[j]), lkk, ykk);
       colk[j] = t;
-      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
+      dsum[j] = __dadd_rn(dsum[j], xmul<IM>(t, t));
     }
     __syncwarp(gm);
     // Second halves of column c1 = k+1 (rows j > c1) and first halves of c2 = k+2 (rows j > c2).

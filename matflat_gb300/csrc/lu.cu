@@ -19,6 +19,8 @@
 // being factored): on GB300 the FP64 pipe, not memory, bounds this kernel.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
@@ -33,7 +35,7 @@ namespace mfg {
 // Tr supplies the element type's arithmetic (double, float or Complex overload).
 // G: lanes per matrix (8, 16 or 32): the matrix is worked on by a group of G consecutive lanes
 // of the warp, the other groups of the warp work on other matrices of the same order.
-template <class Tr, int G = 32>
+template <class Tr, int G = 32, bool IDIV = false>
 __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n, long long lda,
                                                  int c, int mode,
                                                  const typename Tr::Acc* scol, int* piv,
@@ -100,7 +102,13 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
   __syncwarp(gm);
   const T diag = cc[c];
   if (Tr::nz(diag)) {
-    for (int i = c + 1 + lane; i < m; i += G) cc[i] = Tr::div(cc[i], diag);
+    if constexpr (IDIV) {
+      // Quotients on the integer pipes (the same bits as the FP64 division): the reciprocal is
+      // formed once per column.
+      idiv_column(cc, c + 1 + lane, m, G, diag);
+    } else {
+      for (int i = c + 1 + lane; i < m; i += G) cc[i] = Tr::div(cc[i], diag);
+    }
   } else if (info == 0) {
     info = c + 1;
   }
@@ -122,7 +130,8 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
   info = 0;
   __syncwarp(gm);
   const int K = m < n ? m : n;
-  lu_finish_column<Tr, G>(a, m, n, lda, 0, 0, scol, piv, sign, info);
+  constexpr bool IDIV = IM != 0 && std::is_same<Tr, DTraits>::value;
+  lu_finish_column<Tr, G, IDIV>(a, m, n, lda, 0, 0, scol, piv, sign, info);
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
@@ -144,7 +153,8 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
       }
     }
     __syncwarp(gm);
-    if (k1 < K) lu_finish_column<Tr, G>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
+    if (k1 < K)
+      lu_finish_column<Tr, G, IDIV>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
   }
   // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
 }
@@ -161,7 +171,7 @@ struct CtaRed {
   int nan0;
 };
 
-template <int W>
+template <int W, bool IDIV = false>
 __device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int mode,
                                      const double* scol, int* piv, int& sign, int& info,
                                      CtaRed* red) {
@@ -238,7 +248,11 @@ __device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int
   __syncthreads();
   const double diag = cc[c];
   if (Tr::nz(diag)) {
-    for (int i = c + 1 + tid; i < n; i += T) cc[i] = Tr::div(cc[i], diag);
+    if constexpr (IDIV) {
+      idiv_column(cc, c + 1 + tid, n, T, diag);
+    } else {
+      for (int i = c + 1 + tid; i < n; i += T) cc[i] = Tr::div(cc[i], diag);
+    }
   } else if (info == 0) {
     info = c + 1;
   }
@@ -255,7 +269,7 @@ __device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, 
   sign = 1;
   info = 0;
   __syncthreads();
-  lu_cta_finish_column<W>(a, n, lda, 0, 0, scol, piv, sign, info, red);
+  lu_cta_finish_column<W, IM != 0>(a, n, lda, 0, 0, scol, piv, sign, info, red);
   for (int k = 0; k < n; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;
@@ -278,7 +292,7 @@ __device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, 
     }
     __syncthreads();
     if (k1 < n)
-      lu_cta_finish_column<W>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info, red);
+      lu_cta_finish_column<W, IM != 0>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info, red);
   }
 }
 

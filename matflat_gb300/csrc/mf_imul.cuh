@@ -123,6 +123,113 @@ __device__ __forceinline__ void mul_block_s(const double* a, double b, double* p
   mul_block<IM, R, ZEROS>(a, bb, p);
 }
 
+// Correctly rounded quotient a / b on the integer pipes, from the definition of IEEE division and
+// an exact integer remainder (no FP64 instruction).  y must be the correctly rounded reciprocal of
+// b (one __drcp_rn per divisor, shared by all the quotients of a column).
+//
+// For normal a, b with significands Ma, Mb in [2^52, 2^53): the result significand is
+// q = RN(N / Mb), N = Ma * 2^s, s = 52 when Ma >= Mb (N / Mb in [2^52, 2^53)) and 53 otherwise,
+// exponent ea - eb + 1023 - (s - 52).  With Y the significand of y (1/Mb = Y' * 2^-(104 + db),
+// db = 0 when b is a power of two, else 1, and |Y - Y'| <= 1/2), Q0 = floor(Ma * Y / 2^(104 + db
+// - s)) lies within 1 of N / Mb (relative error of Y at most 2^-53, N / Mb < 2^53), so after one
+// correction step against the exact remainder R = N - Q0 * Mb (|R| < 2^55: computed modulo 2^64)
+// Q0 = floor(N / Mb) and 0 <= R < Mb; the quotient rounds up when 2R > Mb (2R == Mb cannot occur
+// for binary significands, and would round to even).  A carry to 2^53 is absorbed by adding the
+// significand onto (exponent - 1) << 52.  Zeros, subnormals, infinities, NaN and out-of-range
+// quotients take __ddiv_rn, so the function returns exactly __ddiv_rn(a, b) for every input; a zero
+// dividend over a normal divisor gives the signed zero directly.
+// The divisor's part of the quotient, formed once per divisor (column).
+struct IDivisor {
+  unsigned long long mb;   // significand of b, implicit bit included
+  unsigned long long sgn;  // sign bit of b
+  unsigned y1, y0;         // significand of y = 1/b in 32 + 21 bit limbs
+  int eb;                  // biased exponent of b
+  int sh;                  // 105 - db (db: 0 when b is a power of two): shift = sh - s
+  bool ok;                 // b and y normal: the integer path applies
+};
+
+__device__ __forceinline__ IDivisor idiv_prepare(double b, double y) {
+  const unsigned long long B = dbits(b), Yb = dbits(y);
+  const unsigned long long M52 = (1ull << 52) - 1ull;
+  IDivisor d;
+  d.eb = (int)((B >> 52) & 0x7FF);
+  const int ey = (int)((Yb >> 52) & 0x7FF);
+  d.ok = (unsigned)(d.eb - 1) < 2046u && (unsigned)(ey - 1) < 2046u;
+  d.mb = (B & M52) | (1ull << 52);
+  d.sgn = B & 0x8000000000000000ull;
+  const unsigned long long Y = (Yb & M52) | (1ull << 52);
+  d.y1 = (unsigned)(Y >> 21);
+  d.y0 = (unsigned)Y & 0x1FFFFFu;
+  d.sh = (B & M52) != 0ull ? 105 : 104;
+  return d;
+}
+
+// Branch-free form: the integer-path quotient, with ok = false where it does not apply (the caller
+// then divides on the FP64 pipe).
+__device__ __forceinline__ double idiv_nb(double a, const IDivisor& d, bool& ok) {
+  const unsigned long long A = dbits(a);
+  const unsigned long long M52 = (1ull << 52) - 1ull;
+  const int ea = (int)((A >> 52) & 0x7FF);
+  const unsigned long long Ma = (A & M52) | (1ull << 52);
+  const unsigned long long Mb = d.mb;
+  const bool ge = Ma >= Mb;
+  const int eq = ea - d.eb + (ge ? 1023 : 1022);
+  const bool zero = (A << 1) == 0ull;
+  ok = d.ok && (zero || ((unsigned)(ea - 1) < 2046u && (unsigned)(eq - 1) < 2045u));
+  const int s = ge ? 52 : 53;
+  // floor(Ma * Y / 2^42) from 32/21-bit limbs (as in imul_bits), then the remaining shift.
+  const unsigned a1 = (unsigned)(Ma >> 21), a0 = (unsigned)Ma & 0x1FFFFFu;
+  const unsigned long long hh = (unsigned long long)a1 * d.y1;
+  const unsigned long long c = (unsigned long long)a1 * d.y0 + (unsigned long long)a0 * d.y1;
+  const unsigned long long ll = (unsigned long long)a0 * d.y0;
+  const unsigned long long t = hh + ((c + (ll >> 21)) >> 21);
+  unsigned long long q = t >> (d.sh - s - 42);
+  long long r = (long long)((Ma << s) - q * Mb);
+  if (r < 0) {
+    q -= 1ull;
+    r += (long long)Mb;
+  } else if (r >= (long long)Mb) {
+    q += 1ull;
+    r -= (long long)Mb;
+  }
+  const unsigned long long r2 = (unsigned long long)r << 1;
+  q += (r2 > Mb || (r2 == Mb && (q & 1ull))) ? 1ull : 0ull;
+  const unsigned long long sg = (A & 0x8000000000000000ull) ^ d.sgn;
+  return __longlong_as_double(
+      (long long)(zero ? sg : (sg | ((((unsigned long long)(eq - 1)) << 52) + q))));
+}
+
+__device__ __forceinline__ double idiv_rn(double a, double b, const IDivisor& d) {
+  bool ok;
+  const double q = idiv_nb(a, d, ok);
+  return ok ? q : __ddiv_rn(a, b);
+}
+
+__device__ __forceinline__ double idiv_rn(double a, double b, double y) {
+  return idiv_rn(a, b, idiv_prepare(b, y));
+}
+
+// x[i] = x[i] / b for i = first, first + step, ... < end, the quotients on the integer pipes; the
+// (rare) elements outside its range are divided on the FP64 pipe in a second pass, so the loop body
+// stays one basic block.
+__device__ __forceinline__ void idiv_column(double* x, int first, int end, int step, double b) {
+  const IDivisor d = idiv_prepare(b, __drcp_rn(b));
+  unsigned long long bad = 0ull;
+  int it = 0;
+  for (int i = first; i < end; i += step, ++it) {
+    bool ok;
+    const double q = idiv_nb(x[i], d, ok);
+    if (ok) x[i] = q;
+    else bad |= it < 64 ? 1ull << it : 0ull;
+    if (!ok && it >= 64) x[i] = __ddiv_rn(x[i], b);
+  }
+  if (bad) {
+    it = 0;
+    for (int i = first; i < end && it < 64; i += step, ++it)
+      if ((bad >> it) & 1ull) x[i] = __ddiv_rn(x[i], b);
+  }
+}
+
 template <>
 __device__ __forceinline__ double xmul<false>(double a, double b) {
   return __dmul_rn(a, b);

@@ -117,6 +117,8 @@ cudaError_t launch_qr_r_single(const T* a, int n, int lda, T* r, int ldr, const 
 // Diagnostics: out[i] = the integer-pipe product of a[i] and b[i] (device pointers).
 cudaError_t launch_selftest_mul(const double* a, const double* b, double* out, long long n,
                                 cudaStream_t s);
+cudaError_t launch_selftest_div(const double* a, const double* b, double* out, long long n,
+                                cudaStream_t s);
 
 // Batched loss = y^T K^-1 y + log det K and its gradient K^-1 - alpha alpha^T (n <= 128; see
 // chol.cu).  Uses args.a (K), args.b (y -> alpha), args.info.

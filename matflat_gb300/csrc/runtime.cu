@@ -3494,6 +3494,16 @@ MFG_API int mfg_selftest_dmul(mfg_ctx* ctx, const double* a, const double* b, do
   return MFG_OK;
 }
 
+MFG_API int mfg_selftest_ddiv(mfg_ctx* ctx, const double* a, const double* b, double* out,
+                              int64_t n) {
+  DeviceScope device_scope_(ctx);
+  if (!ctx) return -1;
+  if (n < 0) return fail(ctx, -5, "n must be >= 0");
+  if (n > 0 && (!a || !b || !out)) return fail(ctx, !a ? -2 : (!b ? -3 : -4), "null pointer");
+  MFG_CUDA(ctx, mfg::launch_selftest_div(a, b, out, n, ctx->stream));
+  return MFG_OK;
+}
+
 MFG_API int mfg_dgetrf_strided_batched_noalloc(mfg_ctx* ctx, int n, int count, double* a,
                                               int lda, int64_t stride_a, int* piv,
                                               int64_t stride_piv, int nrhs, double* b,
