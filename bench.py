@@ -641,6 +641,54 @@ def run_mixed(args, torch, mf, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def chol_fma_check(torch, d, a_in, a_out, b_in, b_out, info):
+    """The FMA form's promise on the whole timed batch (device tensors, after timing): normwise
+    backward error of the factor, ||A - L L^T||_1 / ||A||_1, and of the solution,
+    ||b - A x||_1 / (||A||_1 ||x||_1 + ||b||_1), both within 1e-13 n; info equal to the oracle's
+    (MatFlat's arithmetic) for every matrix; and how many factors happen to equal MatFlat's bits."""
+    from oracle import oracle
+    n = d["n"]
+    info_h = info.cpu().numpy()
+    oa = d["a"].copy()
+    ob = d["b"].copy()
+    oinfo = np.zeros(len(n), np.int32)
+    t0 = time.perf_counter()
+    oracle.chol_solve_batched(n, d["a_off"], oa, d["b_off"], ob, oinfo, os.cpu_count() or 1,
+                              nrhs=d["nrhs"])
+    t_or = time.perf_counter() - t0
+    a_off = torch.from_numpy(d["a_off"]).cuda()
+    b_off = torch.from_numpy(d["b_off"]).cuda()
+    oa_d = torch.from_numpy(oa).cuda()
+    worst_f = worst_x = 0.0
+    same_bits = 0
+    for nv in np.unique(n):
+        nn = int(nv)
+        idx = torch.from_numpy(np.nonzero((n == nv) & (info_h == 0))[0]).cuda()
+        if idx.numel() == 0:
+            continue
+        ca = a_off[idx][:, None] + torch.arange(nn * nn, device="cuda")[None, :]
+        A = a_in[ca].view(-1, nn, nn).transpose(1, 2)
+        L = a_out[ca].view(-1, nn, nn).transpose(1, 2)
+        same_bits += int((a_out[ca] == oa_d[ca]).all(1).sum().item())
+        na = A.abs().sum(1).amax(1)
+        ef = (A - L @ L.transpose(1, 2)).abs().sum(1).amax(1) / na
+        worst_f = max(worst_f, float((ef / nn).max().item()))
+        for r in range(d["nrhs"]):
+            cb = b_off[idx][:, None] + r * nn + torch.arange(nn, device="cuda")[None, :]
+            x = b_out[cb]
+            bb = b_in[cb]
+            res = (bb - (A @ x[:, :, None])[:, :, 0]).abs().sum(1)
+            ex = res / (na * x.abs().sum(1) + bb.abs().sum(1))
+            worst_x = max(worst_x, float((ex / nn).max().item()))
+    return {"factor_berr_over_n_max": worst_f, "solve_berr_over_n_max": worst_x,
+            "bound_over_n": 1e-13, "within_bound": worst_f <= 1e-13 and worst_x <= 1e-13,
+            "info_identical_to_oracle": bool((info_h == oinfo).all()),
+            "not_positive_definite": int((oinfo != 0).sum()),
+            "factors_equal_to_matflat_bits": same_bits, "checked": int(len(n)),
+            "checker": "torch FP64 batched products on the device; oracle (MatFlat Cholesky, "
+                       "C++) for info, %.1f s" % t_or}
+
+
 def lu_parity(d, a_out, b_out, piv_out, sign_out, info_out):
     """The oracle (MatFlat's LuCore + solve restated in C++) over the WHOLE timed batch, after
     the timed region, compared with the GPU's outputs of the last timed step bit for bit."""
@@ -700,6 +748,9 @@ def main():
                     help="lu: skip the oracle check of the whole timed batch")
     ap.add_argument("--no-mixed", action="store_true",
                     help="lu: skip the mixed-precision sub-measurement")
+    ap.add_argument("--form", default="exact", choices=["exact", "fma"],
+                    help="chol/chol100k: arithmetic form of the factorization (exact: MatFlat's "
+                         "bits; fma: fused multiply-adds, checked by backward error)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: warmup raised to 3", file=sys.stderr)
@@ -819,6 +870,7 @@ def main():
             kernel_key = "getrf_task_kernel" if table >= 0 else "getrf_batched_kernel"
         elif cfg_name in ("chol", "chol100k"):
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+            plan.set_form(args.form)
             if not args.no_autotune:
                 tuned = plan.autotune()
 
@@ -916,6 +968,9 @@ def main():
     parity_outs = None
     if cfg_name == "lu" and rank == 0 and not args.no_parity:
         parity_outs = [t.cpu().numpy() for t in (a, b, piv, sign, info)]
+    form_check = None
+    if cfg_name in ("chol", "chol100k") and args.form == "fma" and rank == 0:
+        form_check = chol_fma_check(torch, d, a0, a, b0, b, info)
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -1088,6 +1143,11 @@ def main():
         }
         if parity is not None:
             line["parity"] = parity
+        if form_check is not None:
+            line["config"]["form"] = ("fma: fused multiply-adds in any order, reciprocal column "
+                                      "scaling (mfg_plan_set_form); not MatFlat's bits, checked "
+                                      "by backward error")
+            line["form_check"] = form_check
         if mixed is not None:
             line["mixed"] = mixed
         print(json.dumps(line), flush=True)

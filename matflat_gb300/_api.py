@@ -63,6 +63,7 @@ _SIGS = {
     "mfg_dgetrf_batched": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
+    "mfg_plan_set_form": (_I, [_vp, ctypes.c_int]),
     **{"mfg_%sgemv_strided_batched" % _p: (_I, [_vp, _I, _I, _I, _vp, _I, ctypes.c_int64, _vp,
                                                  _I, ctypes.c_int64, _vp, _I, ctypes.c_int64, _I])
        for _p in "sz"},
@@ -710,6 +711,12 @@ class CholeskyBatch(_Batch):
         self.count = len(self._n)
         self.nrhs = nrhs
 
+    def set_form(self, form):
+        """Arithmetic form of the double factorization: "exact" (MatFlat's bits, the default) or
+        "fma" (fused multiply-adds in any order: backward-stable factors, not MatFlat's bits)."""
+        code = FORMS[form]
+        self.ctx.check(self.ctx.lib.mfg_plan_set_form(self.h, code), "mfg_plan_set_form")
+
     def run(self, a, b, info, dtype=None):
         """Factor (+ solve) device buffers; the element type follows a's dtype (float64,
         float32, complex128; dtype="z" for Complex held as interleaved float64).  Complex
@@ -821,6 +828,7 @@ def selftest_ddiv(a, b, out):
 
 
 LOWP = {"fp32": 0, "tf32": 1, "bf16": 2, "tf32x3": 3}
+FORMS = {"exact": 0, "fma": 1}
 
 
 class MixedSolveBatch(_Batch):

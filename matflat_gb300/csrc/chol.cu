@@ -26,14 +26,6 @@ namespace mfg {
 // one warp per matrix; G < 32: 32/G matrices per warp, which amortises the per-column square root
 // and the serial solve steps over several matrices).  dsum: n doubles of per-group scratch.
 // Returns 0, or k+1 when A is not positive definite at column k.
-// x / lkk, the column's divisor; with IM on the integer pipes (ykk = the reciprocal of lkk, formed
-// once per column), bit-identical to the FP64 division.
-template <bool IM>
-__device__ __forceinline__ double chol_quot(double x, double lkk, double ykk) {
-  if constexpr (IM) return idiv_rn(x, lkk, ykk);
-  else return __ddiv_rn(x, lkk);
-}
-
 template <int G, bool IM>
 __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
   const int lane = group_lane<G>();
@@ -45,15 +37,14 @@ __device__ int potrf_group(double* a, int n, long long lda, double* dsum) {
     const double s = __dsub_rn(colk[k], dsum[k]);
     if (!positive(s)) return k + 1;  // uniform across the group
     const double lkk = __dsqrt_rn(s);
-    const double ykk = IM ? __drcp_rn(lkk) : 0.0;
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += G) {
       // Dot(k, a + j, lda, a + k, lda): row j of L against row k of L.
       const double d = exact_dot<IM>(k, a + j, lda, a + k, lda);
-      const double t = chol_quot<IM>(__dsub_rn(a[(long long)j * lda + k], d), lkk, ykk);
+      const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], d), lkk);
       colk[j] = t;
-      dsum[j] = __dadd_rn(dsum[j], xmul<IM>(t, t));
+      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
     }
     __syncwarp(gm);
   }
@@ -95,13 +86,12 @@ __device__ int potrf_group_split(double* a, int n, long long lda, double* dsum) 
     const double s = __dsub_rn(colk[k], dsum[k]);
     if (!positive(s)) return k + 1;  // uniform across the group
     const double lkk = __dsqrt_rn(s);
-    const double ykk = IM ? __drcp_rn(lkk) : 0.0;
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
     for (int j = k + 1 + lane; j < n; j += G) {
-      const double t = chol_quot<IM>(__dsub_rn(a[(long long)j * lda + k], full[j]), lkk, ykk);
+      const double t = __ddiv_rn(__dsub_rn(a[(long long)j * lda + k], full[j]), lkk);
       colk[j] = t;
-      dsum[j] = __dadd_rn(dsum[j], xmul<IM>(t, t));
+      dsum[j] = __dadd_rn(dsum[j], __dmul_rn(t, t));
     }
     __syncwarp(gm);
     // Second halves of column c1 = k+1 (rows j > c1) and first halves of c2 = k+2 (rows j > c2).
@@ -171,6 +161,88 @@ __device__ void potrs_group(const double* l, int n, long long lda, double* b, lo
   }
 }
 
+// Dot product with fused multiply-adds in four independent chains (the FMA form: any order is
+// allowed, so the chains give the loop instruction-level parallelism); the next block's operands
+// are loaded before the current block's multiply-adds.
+__device__ __forceinline__ double fma_dot(int len, const double* x, long long incx, const double* y,
+                                          long long incy) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const int blocks = len >> 2;
+  if (blocks > 0) {
+    double xa[4], ya[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      xa[u] = x[u * incx];
+      ya[u] = y[u * incy];
+    }
+    for (int blk = 0; blk < blocks; ++blk) {
+      double xb[4], yb[4];
+      const bool more = blk + 1 < blocks;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          xb[u] = x[(4 + u) * incx];
+          yb[u] = y[(4 + u) * incy];
+        }
+      }
+      s0 = __fma_rn(xa[0], ya[0], s0);
+      s1 = __fma_rn(xa[1], ya[1], s1);
+      s2 = __fma_rn(xa[2], ya[2], s2);
+      s3 = __fma_rn(xa[3], ya[3], s3);
+      x += 4 * incx;
+      y += 4 * incy;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          xa[u] = xb[u];
+          ya[u] = yb[u];
+        }
+      }
+    }
+  }
+  for (int t = blocks * 4; t < len; ++t) {
+    s0 = __fma_rn(x[0], y[0], s0);
+    x += incx;
+    y += incy;
+  }
+  return __dadd_rn(__dadd_rn(s0, s1), __dadd_rn(s2, s3));
+}
+
+// The FMA form of the factorization (selected per plan; not MatFlat's bits): the same column
+// order and the same failure test (A(k,k) - sum of squares <= 0 -> k+1) as potrf_group, but every
+// dot runs as fused multiply-adds in four chains, the column is scaled by the reciprocal of its
+// diagonal and the sums of squares accumulate with fused multiply-adds.  The result satisfies the
+// usual Cholesky backward-error bound |A - L L^T| <= gamma_(n+2) |L| |L^T|.
+template <int G>
+__device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum) {
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  for (int j = lane; j < n; j += G) dsum[j] = 0.0;
+  __syncwarp(gm);
+  for (int k = 0; k < n; ++k) {
+    double* colk = a + (long long)k * lda;
+    const double s = __dsub_rn(colk[k], dsum[k]);
+    if (!positive(s)) return k + 1;  // uniform across the group
+    const double lkk = __dsqrt_rn(s);
+    const double rk = __drcp_rn(lkk);
+    __syncwarp(gm);
+    if (lane == 0) colk[k] = lkk;
+    for (int j = k + 1 + lane; j < n; j += G) {
+      const double d = fma_dot(k, a + j, lda, a + k, lda);
+      const double t = __dmul_rn(__dsub_rn(a[(long long)j * lda + k], d), rk);
+      colk[j] = t;
+      dsum[j] = __fma_rn(t, t, dsum[j]);
+    }
+    __syncwarp(gm);
+  }
+  for (int c = 1; c < n; ++c) {
+    double* col = a + (long long)c * lda;
+    for (int r = lane; r < c; r += G) col[r] = 0.0;
+  }
+  __syncwarp(gm);
+  return 0;
+}
+
 // Per-warp shared memory: every group keeps its column sums and staged right-hand sides there
 // for n <= 4G (G = 32: n <= 128); larger matrices use the group's slice of global scratch.
 template <int G>
@@ -190,7 +262,9 @@ static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
 }
 
-template <int WARPS, bool IM, int G, bool SPLIT = false>
+// FMA = true: the FMA form of the factorization (potrf_group_fma); the solves keep MatFlat's
+// arithmetic on the factor they are given.
+template <int WARPS, bool IM, int G, bool SPLIT = false, bool FMA = false>
 __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   constexpr int GPW = 32 / G;  // groups (matrices in flight) per warp
@@ -220,7 +294,9 @@ __global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) 
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
       int info = 0;
       if (!p.solve_only) {
-        if constexpr (SPLIT)
+        if constexpr (FMA)
+          info = potrf_group_fma<G>(a, n, lda, scr);
+        else if constexpr (SPLIT)
           info = potrf_group_split<G, IM>(a, n, lda, scr);
         else
           info = potrf_group<G, IM>(a, n, lda, scr);
@@ -242,6 +318,10 @@ __global__ void __launch_bounds__(32) potrf_single_kernel(double* a, int n, int 
 template <int WARPS, int G>
 static cudaError_t launch_potrf_wg(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = potrf_smem_bytes(args, WARPS);
+  if (args.fma) {
+    potrf_batched_kernel<WARPS, true, G, false, true><<<ctas, WARPS * 32, smem, s>>>(args);
+    return cudaGetLastError();
+  }
   if constexpr (G == 32) {
     if (args.split && !args.hw_mul) {
       potrf_batched_kernel<WARPS, true, G, true><<<ctas, WARPS * 32, smem, s>>>(args);
@@ -271,6 +351,9 @@ static cudaError_t set_potrf_attr_g() {
   const size_t smem = sizeof(double) * SMEM_WARP_DOUBLES_C * WARPS;
   cudaError_t e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G, false, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if constexpr (G == 32) {
     e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G, true>,

@@ -130,7 +130,7 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
   info = 0;
   __syncwarp(gm);
   const int K = m < n ? m : n;
-  constexpr bool IDIV = IM != 0 && std::is_same<Tr, DTraits>::value;
+  constexpr bool IDIV = MFG_IDIV && IM != 0 && std::is_same<Tr, DTraits>::value;
   lu_finish_column<Tr, G, IDIV>(a, m, n, lda, 0, 0, scol, piv, sign, info);
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
@@ -269,7 +269,7 @@ __device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, 
   sign = 1;
   info = 0;
   __syncthreads();
-  lu_cta_finish_column<W, IM != 0>(a, n, lda, 0, 0, scol, piv, sign, info, red);
+  lu_cta_finish_column<W, MFG_IDIV && IM != 0>(a, n, lda, 0, 0, scol, piv, sign, info, red);
   for (int k = 0; k < n; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;
@@ -292,7 +292,8 @@ __device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, 
     }
     __syncthreads();
     if (k1 < n)
-      lu_cta_finish_column<W, IM != 0>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info, red);
+      lu_cta_finish_column<W, MFG_IDIV && IM != 0>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign,
+                                                   info, red);
   }
 }
 

@@ -48,6 +48,8 @@ struct BatchArgs {
   const int* dcount;         // getrf: when set, the number of matrices to take from `order` is
                              // read from device memory (a list built on the device); count
                              // stays the upper bound the grid was sized for
+  int fma;                   // potrf: the FMA form (fused multiply-adds in any order, reciprocal
+                             // scaling): backward-stable factors, not MatFlat's bits
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and

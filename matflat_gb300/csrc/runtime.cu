@@ -2542,6 +2542,23 @@ int qr_autotune(mfg_plan* plan, int* config) {
 
 extern "C" {
 
+MFG_API int mfg_plan_set_form(mfg_plan* plan, int form) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (plan->kind != mfg_plan::POTRF)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "set_form: potrf plans only");
+  if (form != MFG_FORM_EXACT && form != MFG_FORM_FMA)
+    return fail(ctx, -2, "form must be MFG_FORM_EXACT or MFG_FORM_FMA");
+  plan->args.fma = form == MFG_FORM_FMA ? 1 : 0;
+  pipe_release(plan);  // host-buffer chunk plans are rebuilt with the form on next use
+  if (plan->exec) {
+    cudaGraphExecDestroy(plan->exec);
+    plan->exec = nullptr;
+  }
+  return MFG_OK;
+}
+
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
@@ -2595,6 +2612,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   tp->args.sign = plan->kind == mfg_plan::GETRF ? sign : nullptr;
   tp->args.info = info;
   tp->args.solve_only = 0;
+  tp->args.fma = plan->args.fma;
   std::vector<std::array<int, 5>> cands;
   if (plan->kind == mfg_plan::GETRF) {
     // Slot 2 is the lanes-per-matrix table of the size buckets (lu_lanes; -1: one matrix per
@@ -2612,10 +2630,13 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   } else {
     // The integer-product variants need ~100 registers (up to 20 warps/SM), the FP64-pipe ones
     // ~128 (16 warps/SM).
+    // The FMA form has no multiply pipe to choose.
     for (int g : {4, 8, 16, 32}) {
       for (int wps : {8, 16})
-        for (int mul : {0, 1}) cands.push_back({4, wps, g, mul, 4});
+        for (int mul : {0, 1})
+          if (mul == 0 || !plan->args.fma) cands.push_back({4, wps, g, mul, 4});
       cands.push_back({4, 20, g, 0, 4});
+      if (plan->args.fma) cands.push_back({4, 24, g, 0, 4});
     }
     // Lanes per matrix by size bucket (slot 2 = -table, chol_lanes).
     for (int t : {1, 2})
@@ -2661,7 +2682,9 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   pipe_release(plan);  // host-buffer chunk plans are rebuilt with the new shape on next use
   rc = plan_reshape(plan, best[0], best[1], best[2], best[3], best[4]);
   if (rc != MFG_OK) return rc;
-  ctx->tune[tune_key((int)plan->kind, plan->max_n, plan->count)] = best;
+  // Plans in the FMA form record their shape under a key of their own.
+  ctx->tune[tune_key((int)plan->kind + (plan->args.fma ? 100 : 0), plan->max_n, plan->count)] =
+      best;
   if (config)
     for (int i = 0; i < 5; i++) config[i] = best[i];
   return MFG_OK;
@@ -3045,6 +3068,7 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
                         p->args.group, p->args.hw_mul, p->args.dot_block);
       if (rc == MFG_OK) rc = plan_set_elem(sub, pipe_elem(op));
       if (rc != MFG_OK) return rc;
+      sub->args.fma = p->args.fma;
     }
     if (p->kind == mfg_plan::GEVD) {
       rc = plan_set_elem(sub, pipe_elem(op));
