@@ -227,11 +227,31 @@ __device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum) {
     const double rk = __drcp_rn(lkk);
     __syncwarp(gm);
     if (lane == 0) colk[k] = lkk;
-    for (int j = k + 1 + lane; j < n; j += G) {
-      const double d = fma_dot(k, a + j, lda, a + k, lda);
-      const double t = __dmul_rn(__dsub_rn(a[(long long)j * lda + k], d), rk);
-      colk[j] = t;
-      dsum[j] = __fma_rn(t, t, dsum[j]);
+    // S lanes per row: 1 while the step has at least half as many rows as the group has lanes,
+    // else 2 or 4 lanes share each row's dot (a contiguous part of it each), combined with
+    // shuffles within the S lanes.  Every lane runs the same number of rounds (convergent
+    // shuffles); lanes past the last row contribute zero.
+    const int rows = n - k - 1;
+    const int S = (rows * 2 > G || k < 8) ? 1 : (rows * 4 <= G ? 4 : 2);
+    const int len = (k + S - 1) / S;
+    const int part = lane & (S - 1);
+    const int t0 = part * len;
+    const int cnt = max(0, min(len, k - t0));
+    for (int j0 = k + 1; j0 < n; j0 += G / S) {
+      const int j = j0 + lane / S;
+      const bool live = j < n;
+      double d = live && cnt > 0 ? fma_dot(cnt, a + j + (long long)t0 * lda, lda,
+                                           a + k + (long long)t0 * lda, lda)
+                                 : 0.0;
+      if (S > 1) {
+        d = __dadd_rn(d, __shfl_xor_sync(gm, d, 1, G));
+        if (S > 2) d = __dadd_rn(d, __shfl_xor_sync(gm, d, 2, G));
+      }
+      if (live && part == 0) {
+        const double t = __dmul_rn(__dsub_rn(a[(long long)j * lda + k], d), rk);
+        colk[j] = t;
+        dsum[j] = __fma_rn(t, t, dsum[j]);
+      }
     }
     __syncwarp(gm);
   }
@@ -262,10 +282,17 @@ static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
 }
 
+// Resident warps per SM the FMA variant is compiled for (caps its registers at 65536 / (32 x
+// this)).
+#ifndef MFG_CHOL_FMA_WARPS
+#define MFG_CHOL_FMA_WARPS 24
+#endif
+
 // FMA = true: the FMA form of the factorization (potrf_group_fma); the solves keep MatFlat's
 // arithmetic on the factor they are given.
 template <int WARPS, bool IM, int G, bool SPLIT = false, bool FMA = false>
-__global__ void __launch_bounds__(WARPS * 32) potrf_batched_kernel(BatchArgs p) {
+__global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS : 1)
+    potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   constexpr int GPW = 32 / G;  // groups (matrices in flight) per warp
   const int warp = threadIdx.x >> 5;

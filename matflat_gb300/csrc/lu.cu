@@ -39,7 +39,7 @@ template <class Tr, int G = 32, bool IDIV = false>
 __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n, long long lda,
                                                  int c, int mode,
                                                  const typename Tr::Acc* scol, int* piv,
-                                                 int& sign, int& info) {
+                                                 int& sign, int& info, int* pivot = nullptr) {
   using T = typename Tr::T;
   using Acc = typename Tr::Acc;
   const int lane = group_lane<G>();
@@ -84,6 +84,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
   // Row c is handled by the group's lane 0; a NaN there can never be displaced by the strict ">"
   // scan.
   if (__shfl_sync(gm, first_nan ? 1 : 0, 0, G)) p = c;
+  if (pivot) *pivot = p;
   __syncwarp(gm);
   if (p != c && p < m) {
     for (int col = lane; col < n; col += G) {
@@ -118,9 +119,19 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
 // Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
 // vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
 // and in `info` the first zero pivot (k+1), or 0.
-template <class Tr, int IM, int DB = DOT_BLOCK, int G = 32>
+//
+// EARLY (square matrices; scol2: m more values): the lanes left idle in the last round of a step
+// compute prefixes of the column after next.  Column c's prefix Dot(c-2, L(i,:), U(:,c)) reads
+// U rows 0..c-3 only, which are final after step c-3, so it may run at step c-2 instead of c-1;
+// the values are the same (the same dot, evaluated once).  At step k the rows [m - e, m) (e <= the
+// idle lanes of the step's last round, rows >= k+2) get column k+2's prefix early; at step k+1
+// column k+2's regular items cover the other rows, plus the row swapped into the early range by
+// column k+1's pivot (its early value belonged to the row that moved out).  Columns alternate
+// between the two prefix arrays (scol: even columns, scol2: odd).
+template <class Tr, int IM, int DB = DOT_BLOCK, int G = 32, bool EARLY = false>
 __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
-                        typename Tr::Acc* scol, int& sign, int& info) {
+                        typename Tr::Acc* scol, int& sign, int& info,
+                        typename Tr::Acc* scol2 = nullptr) {
   using T = typename Tr::T;
   using Acc = typename Tr::Acc;
   const int lane = group_lane<G>();
@@ -132,29 +143,51 @@ __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv
   const int K = m < n ? m : n;
   constexpr bool IDIV = MFG_IDIV && IM != 0 && std::is_same<Tr, DTraits>::value;
   lu_finish_column<Tr, G, IDIV>(a, m, n, lda, 0, 0, scol, piv, sign, info);
+  int e_prev = 0;        // rows [m - e_prev, m) got column k1's prefix at the previous step
+  int p_prev = INT_MAX;  // the pivot row of column k (chosen at the end of the previous step)
   for (int k = 0; k < K; ++k) {
     const int k1 = k + 1;
     const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
-    const int C = (k1 < K && k >= 1) ? m - k1 : 0;  // prefixes of column k1 (rows [k1, m))
     const T* rowk = a + k;                    // L(k, t) = rowk[t*lda]
     const T* colk1 = a + (long long)k1 * lda;
-    for (int d = lane; d < R + C; d += G) {
+    Acc* pre1 = (EARLY && (k1 & 1)) ? scol2 : scol;   // column k1's prefixes
+    // Regular prefix items of column k1: rows [k1, m - e_prev), plus the displaced row.
+    const bool has_col = k1 < K && k >= 1;
+    const int nreg0 = has_col ? max(0, m - e_prev - k1) : 0;
+    const int disp = (has_col && EARLY && e_prev > 0 && p_prev >= m - e_prev && p_prev < m) ? 1
+                                                                                            : 0;
+    const int C = nreg0 + disp;
+    int E = 0;
+    if constexpr (EARLY) {
+      if (k >= 2 && k + 2 < K) E = min(m - (k + 2), (G - (R + C) % G) % G);
+    }
+    Acc* pre2 = (k & 1) ? scol2 : scol;               // column k+2's prefixes (EARLY)
+    const T* colk2 = a + (long long)(k + 2) * lda;
+    for (int d = lane; d < R + C + E; d += G) {
+      // One dot per item (a single call site keeps the register count of one dot loop): row
+      // items U(k, idx) (length k), column k1's prefixes (k-1), column k+2's early prefixes (k).
       const bool isrow = d < R;
-      const int idx = isrow ? k1 + d : k1 + (d - R);
+      const bool isreg = !isrow && d < R + C;
+      const int c = d - R;
+      const int idx = isrow ? k1 + d : isreg ? (c < nreg0 ? k1 + c : p_prev) : m - E + (c - C);
       const T* x = isrow ? rowk : a + idx;
-      const T* y = isrow ? a + (long long)idx * lda : colk1;
-      const int len = isrow ? k : k - 1;
+      const T* y = isrow ? a + (long long)idx * lda : isreg ? colk1 : colk2;
+      const int len = isreg ? k - 1 : k;
       const Acc s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
       if (isrow) {
         T* dst = a + (long long)idx * lda + k;
         *dst = Tr::fin(*dst, s);
       } else {
-        scol[idx] = s;
+        (isreg ? pre1 : pre2)[idx] = s;
       }
     }
     __syncwarp(gm);
+    int pk = INT_MAX;
     if (k1 < K)
-      lu_finish_column<Tr, G, IDIV>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign, info);
+      lu_finish_column<Tr, G, IDIV>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, pre1, piv, sign, info,
+                                    &pk);
+    e_prev = E;
+    p_prev = pk;
   }
   // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
 }
@@ -428,7 +461,8 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
 // one task at a time and its groups of G lanes each factor (and solve) one matrix of it, in exactly
 // the schedule above.  Small G keeps the lanes busy when a step has few dots; groups of a task
 // share the order, so they follow the same control flow.
-constexpr int GROUP_SMEM_DOUBLES = SMEM_N + 2;   // per group: the column sums (n <= SMEM_N)
+// Per group: the column sums of even and of odd columns (n <= SMEM_N), SMEM_N + 1 apart.
+constexpr int GROUP_SMEM_DOUBLES = 2 * SMEM_N + 2;
 
 template <int IM, int DB, int G>
 __device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cnt, double* ws,
@@ -442,17 +476,20 @@ __device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cn
   double* a = p.a + p.a_off[mat];
   int* piv = p.piv + p.piv_off[mat];
   double* scr;
+  double* scr2;
   double* sol;
   if (n <= SMEM_N) {
     scr = ws + g * GROUP_SMEM_DOUBLES;
+    scr2 = scr + SMEM_N + 1;
     sol = p.gsolve ? p.gsolve + (gw * GETRF_GROUPS + g) * GSOLVE_STRIDE : nullptr;
   } else {   // only 32-lane tasks hold orders above SMEM_N
     scr = p.gscratch + gw * p.gscratch_stride;
-    sol = scr + n;
+    scr2 = scr + n;
+    sol = scr + 2 * n;
   }
   const int ldx = n | 1;
   int sign = 1, info = 0;
-  if (!p.solve_only) lu_warp<DTraits, IM, DB, G>(a, n, n, lda, piv, scr, sign, info);
+  if (!p.solve_only) lu_warp<DTraits, IM, DB, G, true>(a, n, n, lda, piv, scr, sign, info, scr2);
   if (p.nrhs > 0)
     getrs_warp<DSolveIM, G>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol,
                             sol + RHS_CHUNK * ldx);
@@ -471,7 +508,7 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const long long gw = (long long)blockIdx.x * WARPS + warp;
-  double* ws = sm_dyn + warp * GETRF_GROUPS * GROUP_SMEM_DOUBLES;
+  double* ws = sm_dyn + warp * (32 / G) * GROUP_SMEM_DOUBLES;
   for (;;) {
     int t = 0;
     if (lane == 0) t = atomicAdd(p.queue, 1);
@@ -543,13 +580,13 @@ cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStre
 int getrf_cta_warps() { return CTA_WARPS; }
 
 template <int WARPS>
-static size_t getrf_task_smem_bytes() {
-  return sizeof(double) * GETRF_GROUPS * GROUP_SMEM_DOUBLES * WARPS;
+static size_t getrf_task_smem_bytes(int g) {
+  return sizeof(double) * (32 / g) * GROUP_SMEM_DOUBLES * WARPS;
 }
 
 template <int WARPS, int G>
 static cudaError_t launch_getrf_task_g(const BatchArgs& args, int ctas, cudaStream_t s) {
-  const size_t smem = getrf_task_smem_bytes<WARPS>();
+  const size_t smem = getrf_task_smem_bytes<WARPS>(G);
   if (args.hw_mul)
     getrf_task_kernel<WARPS, 0, 4, G><<<ctas, WARPS * 32, smem, s>>>(args);
   else if (args.dot_block == 2)
@@ -568,7 +605,7 @@ static cudaError_t launch_getrf_task_w(const BatchArgs& args, int ctas, int g, c
 
 template <int WARPS, int G>
 static cudaError_t set_getrf_task_attr_g() {
-  const int smem = (int)getrf_task_smem_bytes<WARPS>();
+  const int smem = (int)getrf_task_smem_bytes<WARPS>(G);
   cudaError_t e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 0, 4, G>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)

@@ -11,11 +11,11 @@ namespace mfg {
 constexpr int SMEM_N = 128;
 // Right-hand sides solved together per pass of the warp solvers.
 constexpr int RHS_CHUNK = 4;
-// Doubles of per-warp scratch needed for a matrix of order n (column sums, staged right-hand
-// sides and their accumulators).
+// Doubles of per-warp scratch needed for a matrix of order n (column sums (two arrays: the LU
+// task kernel keeps even and odd columns apart), staged right-hand sides and their accumulators).
 inline long long warp_scratch_doubles(int n) {
   const long long ld = (long long)(n | 1);
-  return (long long)n + 2LL * RHS_CHUNK * ld + 2;
+  return 2LL * n + 2LL * RHS_CHUNK * ld + 2;
 }
 
 struct BatchArgs {
