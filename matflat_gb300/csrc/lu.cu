@@ -65,7 +65,11 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
     const T u2 = (mode == 2) ? cc[c - 2] : u1;    // U(c-2, c)
     for (int i = c + lane; i < m; i += G) {
       Acc s;
-      if (mode == 1) {
+      if constexpr (IDIV) {
+        // Double with integer-pipe arithmetic: the products on the integer pipes too.
+        s = mode == 1 ? imul_rn(l1[i], u1)
+                      : __dadd_rn(scol[i], __dadd_rn(imul_rn(l2[i], u2), imul_rn(l1[i], u1)));
+      } else if (mode == 1) {
         s = Tr::prod(l1[i], u1);
       } else {
         s = Tr::pair(scol[i], l2[i], u2, l1[i], u1);
@@ -128,6 +132,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
 // column k+2's regular items cover the other rows, plus the row swapped into the early range by
 // column k+1's pivot (its early value belonged to the row that moved out).  Columns alternate
 // between the two prefix arrays (scol: even columns, scol2: odd).
+
 template <class Tr, int IM, int DB = DOT_BLOCK, int G = 32, bool EARLY = false>
 __device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
                         typename Tr::Acc* scol, int& sign, int& info,
@@ -207,7 +212,7 @@ struct CtaRed {
 template <int W, bool IDIV = false>
 __device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int mode,
                                      const double* scol, int* piv, int& sign, int& info,
-                                     CtaRed* red) {
+                                     CtaRed* red, int* pivot = nullptr) {
   using Tr = DTraits;
   constexpr int T = W * 32;
   const int tid = threadIdx.x;
@@ -231,7 +236,10 @@ __device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int
     const double* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
     const double u2 = (mode == 2) ? cc[c - 2] : u1;
     for (int i = c + tid; i < n; i += T) {
-      const double s = mode == 1 ? Tr::prod(l1[i], u1) : Tr::pair(scol[i], l2[i], u2, l1[i], u1);
+      const double s =
+          IDIV ? (mode == 1 ? imul_rn(l1[i], u1)
+                            : __dadd_rn(scol[i], __dadd_rn(imul_rn(l2[i], u2), imul_rn(l1[i], u1))))
+               : (mode == 1 ? Tr::prod(l1[i], u1) : Tr::pair(scol[i], l2[i], u2, l1[i], u1));
       const double v = Tr::fin(cc[i], s);
       cc[i] = v;
       const unsigned long long key = Tr::key(v);
@@ -264,6 +272,7 @@ __device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int
     }
   }
   if (red->nan0) p = c;
+  if (pivot) *pivot = p;
   if (p != c && p < n) {
     for (int col = tid; col < n; col += T) {
       double* base = a + (long long)col * lda;
@@ -327,6 +336,64 @@ __device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, 
     if (k1 < n)
       lu_cta_finish_column<W, MFG_IDIV && IM != 0>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign,
                                                    info, red);
+  }
+}
+
+// lu_cta with the early prefixes of lu_warp<..., EARLY = true>: threads left idle in the last round
+// of step k compute column k+2's prefixes for the bottom rows (the same dots, evaluated once, in the
+// same tree), and the row swapped into that range by column k+1's pivot gets its prefix again at
+// step k+1.  Column sums alternate between scol (even columns) and scol2 (odd columns).
+template <int W, int IM, int DB>
+__device__ void lu_cta_early(double* a, int n, long long lda, int* piv, double* scol,
+                             double* scol2, int& sign, int& info, CtaRed* red) {
+  using Tr = DTraits;
+  constexpr int T = W * 32;
+  constexpr bool IDIV = MFG_IDIV && IM != 0;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n; i += T) piv[i] = i;
+  sign = 1;
+  info = 0;
+  __syncthreads();
+  lu_cta_finish_column<W, IDIV>(a, n, lda, 0, 0, scol, piv, sign, info, red);
+  int e_prev = 0;
+  int p_prev = INT_MAX;
+  for (int k = 0; k < n; ++k) {
+    const int k1 = k + 1;
+    const int R = n - k1;
+    const double* rowk = a + k;
+    const double* colk1 = a + (long long)k1 * lda;
+    double* pre1 = (k1 & 1) ? scol2 : scol;
+    const bool has_col = k1 < n && k >= 1;
+    const int nreg0 = has_col ? max(0, n - e_prev - k1) : 0;
+    const int disp = (has_col && e_prev > 0 && p_prev >= n - e_prev && p_prev < n) ? 1 : 0;
+    const int C = nreg0 + disp;
+    int E = 0;
+    if (k >= 2 && k + 2 < n) E = min(n - (k + 2), (T - (R + C) % T) % T);
+    double* pre2 = (k & 1) ? scol2 : scol;
+    const double* colk2 = a + (long long)(k + 2) * lda;
+    for (int d = tid; d < R + C + E; d += T) {
+      const bool isrow = d < R;
+      const bool isreg = !isrow && d < R + C;
+      const int c = d - R;
+      const int idx = isrow ? k1 + d : isreg ? (c < nreg0 ? k1 + c : p_prev) : n - E + (c - C);
+      const double* x = isrow ? rowk : a + idx;
+      const double* y = isrow ? a + (long long)idx * lda : isreg ? colk1 : colk2;
+      const int len = isreg ? k - 1 : k;
+      const double s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
+      if (isrow) {
+        double* dst = a + (long long)idx * lda + k;
+        *dst = Tr::fin(*dst, s);
+      } else {
+        (isreg ? pre1 : pre2)[idx] = s;
+      }
+    }
+    __syncthreads();
+    int pk = INT_MAX;
+    if (k1 < n)
+      lu_cta_finish_column<W, IDIV>(a, n, lda, k1, k1 == 1 ? 1 : 2, pre1, piv, sign, info, red,
+                                    &pk);
+    e_prev = E;
+    p_prev = pk;
   }
 }
 
@@ -489,7 +556,8 @@ __device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cn
   }
   const int ldx = n | 1;
   int sign = 1, info = 0;
-  if (!p.solve_only) lu_warp<DTraits, IM, DB, G, true>(a, n, n, lda, piv, scr, sign, info, scr2);
+  if (!p.solve_only)
+    lu_warp<DTraits, IM, DB, G, true>(a, n, n, lda, piv, scr, sign, info, scr2);
   if (p.nrhs > 0)
     getrs_warp<DSolveIM, G>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, sol,
                             sol + RHS_CHUNK * ldx);
@@ -503,7 +571,7 @@ __device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cn
 // register count of its own schedule.  args.task_first / task_gc / ntasks / queue describe the
 // bucket's tasks.
 template <int WARPS, int IM, int DB, int G>
-__global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
+__device__ __forceinline__ void getrf_task_loop(const BatchArgs& p) {
   extern __shared__ double sm_dyn[];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -517,6 +585,18 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
     getrf_task<IM, DB, G>(p, p.task_first[t], p.task_gc[t] >> 8, ws, gw);
     __syncwarp();
   }
+}
+
+template <int WARPS, int IM, int DB, int G>
+__global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
+  getrf_task_loop<WARPS, IM, DB, G>(p);
+}
+
+// The same with the register allocation bounded for MINB resident CTAs of 4 warps per SM (28 or
+// 32 warps): the plan launches it when its shape asks for that many.
+template <int IM, int DB, int G, int MINB>
+__global__ void __launch_bounds__(128, MINB) getrf_task_kernel_occ(BatchArgs p) {
+  getrf_task_loop<4, IM, DB, G>(p);
 }
 
 // One matrix per CTA of CTA_WARPS warps, taken from `order` (count from p.count or *p.dcount;
@@ -562,6 +642,140 @@ __global__ void __launch_bounds__(CTA_WARPS * 32) getrf_cta_kernel(BatchArgs p, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Resident form: one matrix per CTA of W warps, held in shared memory for the whole factorization
+// and solve.  The CTA copies the matrix in (asynchronous 8-byte copies, column by column into a
+// leading dimension n | 1, odd, so that the row-k dots, whose lanes walk different columns, hit
+// different banks), runs lu_cta_early on the copy, writes the factors back with coalesced stores
+// and solves from the shared copy, the right-hand sides split over the warps.  Several CTAs share
+// an SM, so the warps a step leaves idle are covered by the other CTAs' work, and every operand of
+// the Crout dots comes from shared memory instead of L1/L2.  A matrix whose copy does not fit the
+// CTA's shared memory (smem_doubles) is factored in place in global memory, as getrf_cta_kernel
+// does.  Work items are the plan's tasks (one matrix each), `ntasks` of them.
+//
+// Shared memory per CTA: the copy (n (n|1) doubles), two column-sum vectors (2n), and per warp
+// the staging of its right-hand sides (2 nrc (n|1), nrc = min(ceil(nrhs / W), RHS_CHUNK)).
+__host__ __device__ inline long long blk_smem_doubles(int n, int nrhs, int w, bool resident) {
+  const long long ld = n | 1;
+  int nrc = (nrhs + w - 1) / w;
+  if (nrc > RHS_CHUNK) nrc = RHS_CHUNK;
+  return (resident ? (long long)n * ld : 0) + 2LL * n + (long long)w * 2 * nrc * ld;
+}
+
+template <int W, int IM, int DB>
+__global__ void __launch_bounds__(W * 32) getrf_blk_kernel(BatchArgs p, int smem_doubles) {
+  extern __shared__ double sm_dyn[];
+  __shared__ CtaRed red;
+  __shared__ int next;
+  constexpr int T = W * 32;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  for (;;) {
+    if (tid == 0) next = atomicAdd(p.queue, 1);
+    __syncthreads();
+    const int t = next;
+    __syncthreads();
+    if (t >= p.ntasks) break;
+    const int mat = p.order[p.task_first[t]];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    double* a = p.a + p.a_off[mat];
+    int* piv = p.piv + p.piv_off[mat];
+    const int lds = n | 1;
+    // Solve-only calls read the factors where they are.
+    const bool res = !p.solve_only && blk_smem_doubles(n, p.nrhs, W, true) <= smem_doubles;
+    double* m = res ? sm_dyn : a;
+    const long long ldm = res ? (long long)lds : lda;
+    double* scol = sm_dyn + (res ? (long long)n * lds : 0);
+    double* scol2 = scol + n;
+    double* stage = scol2 + n;
+    const int ne = n * n;
+    if (res) {
+      for (int e = tid; e < ne; e += T) {
+        const int j = e / n;
+        const int i = e - j * n;
+        const unsigned d = (unsigned)__cvta_generic_to_shared(m + (long long)j * lds + i);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d),
+                     "l"(a + (long long)j * lda + i)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncthreads();
+    }
+    int sign = 1, info = 0;
+    if (!p.solve_only) lu_cta_early<W, IM, DB>(m, n, ldm, piv, scol, scol2, sign, info, &red);
+    if (res) {
+      for (int e = tid; e < ne; e += T) {
+        const int j = e / n;
+        const int i = e - j * n;
+        a[(long long)j * lda + i] = m[(long long)j * lds + i];
+      }
+    }
+    if (p.nrhs > 0) {
+      // Warp w solves right-hand sides [w q, min(nrhs, (w + 1) q)), q = ceil(nrhs / W).
+      const int q = (p.nrhs + W - 1) / W;
+      const int r0 = warp * q;
+      const int nr = min(p.nrhs, r0 + q) - r0;
+      int nrc = q < RHS_CHUNK ? q : RHS_CHUNK;
+      double* xs = stage + (long long)warp * 2 * nrc * lds;
+      if (nr > 0)
+        getrs_warp<DSolveIM, 32>(m, n, ldm, piv, p.b + p.b_off[mat] + (long long)r0 * n, n, nr,
+                                 xs, xs + (long long)nrc * lds);
+    }
+    if (tid == 0 && !p.solve_only) {
+      p.sign[mat] = sign;
+      p.info[mat] = info;
+    }
+    __syncthreads();
+  }
+}
+
+constexpr int BLK_SMEM_MAX = 227 * 1024 - 1024;  // dynamic bytes, leaving room for the static part
+
+template <int W>
+static cudaError_t launch_getrf_blk_w(const BatchArgs& args, int ctas, int smem_bytes,
+                                      cudaStream_t s) {
+  const int sd = smem_bytes / (int)sizeof(double);
+  if (args.hw_mul)
+    getrf_blk_kernel<W, 0, 4><<<ctas, W * 32, smem_bytes, s>>>(args, sd);
+  else if (args.dot_block == 2)
+    getrf_blk_kernel<W, 1, 2><<<ctas, W * 32, smem_bytes, s>>>(args, sd);
+  else
+    getrf_blk_kernel<W, 1, 4><<<ctas, W * 32, smem_bytes, s>>>(args, sd);
+  return cudaGetLastError();
+}
+
+template <int W>
+static cudaError_t set_getrf_blk_attr() {
+  cudaError_t e = cudaFuncSetAttribute(getrf_blk_kernel<W, 0, 4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, BLK_SMEM_MAX);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_blk_kernel<W, 1, 2>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, BLK_SMEM_MAX);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_blk_kernel<W, 1, 4>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, BLK_SMEM_MAX);
+  return e;
+}
+
+long long getrf_blk_smem_doubles(int n, int nrhs, int w, bool resident) {
+  return blk_smem_doubles(n, nrhs, w, resident);
+}
+
+int getrf_blk_smem_max() { return BLK_SMEM_MAX; }
+
+cudaError_t launch_getrf_blk(const BatchArgs& args, int ctas, int w, int smem_bytes,
+                             cudaStream_t s) {
+  if (smem_bytes > BLK_SMEM_MAX || smem_bytes < 0) return cudaErrorInvalidValue;
+  switch (w) {
+    case 2: return launch_getrf_blk_w<2>(args, ctas, smem_bytes, s);
+    case 4: return launch_getrf_blk_w<4>(args, ctas, smem_bytes, s);
+    case 8: return launch_getrf_blk_w<8>(args, ctas, smem_bytes, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s) {
   const size_t with_solve =
       sizeof(double) * ((size_t)nmax + 2 * (size_t)RHS_CHUNK * (size_t)(nmax | 1));
@@ -589,6 +803,10 @@ static cudaError_t launch_getrf_task_g(const BatchArgs& args, int ctas, cudaStre
   const size_t smem = getrf_task_smem_bytes<WARPS>(G);
   if (args.hw_mul)
     getrf_task_kernel<WARPS, 0, 4, G><<<ctas, WARPS * 32, smem, s>>>(args);
+  else if (WARPS == 4 && args.dot_block == 2 && args.minb >= 8)
+    getrf_task_kernel_occ<1, 2, G, 8><<<ctas, 128, smem, s>>>(args);
+  else if (WARPS == 4 && args.dot_block == 2 && args.minb == 7)
+    getrf_task_kernel_occ<1, 2, G, 7><<<ctas, 128, smem, s>>>(args);
   else if (args.dot_block == 2)
     getrf_task_kernel<WARPS, 1, 2, G><<<ctas, WARPS * 32, smem, s>>>(args);
   else
@@ -613,6 +831,12 @@ static cudaError_t set_getrf_task_attr_g() {
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 1, 4, G>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (WARPS == 4 && e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_task_kernel_occ<1, 2, G, 8>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (WARPS == 4 && e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_task_kernel_occ<1, 2, G, 7>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;
 }
@@ -730,6 +954,9 @@ cudaError_t init_getrf_attributes() {
   if ((e = set_getrf_task_attr<4>()) != cudaSuccess) return e;
   if ((e = set_getrf_task_attr<8>()) != cudaSuccess) return e;
   if ((e = set_getrf_task_attr<16>()) != cudaSuccess) return e;
+  if ((e = set_getrf_blk_attr<2>()) != cudaSuccess) return e;
+  if ((e = set_getrf_blk_attr<4>()) != cudaSuccess) return e;
+  if ((e = set_getrf_blk_attr<8>()) != cudaSuccess) return e;
   return set_getrf_attr<16>();
 }
 

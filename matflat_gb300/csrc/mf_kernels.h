@@ -48,6 +48,8 @@ struct BatchArgs {
   const int* dcount;         // getrf: when set, the number of matrices to take from `order` is
                              // read from device memory (a list built on the device); count
                              // stays the upper bound the grid was sized for
+  int minb;                  // getrf (double, size-bucketed tasks): CTAs per SM of the launch
+                             // shape (7 or 8 select variants compiled for that occupancy)
   int fma;                   // potrf: the FMA form (fused multiply-adds in any order, reciprocal
                              // scaling): backward-stable factors, not MatFlat's bits
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
@@ -266,6 +268,14 @@ cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g
 // slice of warp_scratch_doubles(nmax) per CTA (cudaErrorInvalidValue if it is missing).
 cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s);
 int getrf_cta_warps();
+// Resident form: one matrix per CTA of w warps (2, 4 or 8) over the task list (one matrix per
+// task), the matrix held in smem_bytes of dynamic shared memory when it fits.
+cudaError_t launch_getrf_blk(const BatchArgs& args, int ctas, int w, int smem_bytes,
+                             cudaStream_t s);
+// Shared memory (doubles) the resident form needs for one matrix of order n (resident: with the
+// copy of the matrix), and the largest dynamic shared memory it may be given (bytes).
+long long getrf_blk_smem_doubles(int n, int nrhs, int w, bool resident);
+int getrf_blk_smem_max();
 cudaError_t launch_getrf_batched(const BatchArgs& args, int ctas, int warps, cudaStream_t s);
 // Float and Complex overloads of the batched LU (+ solve): args.a / args.b point at float or
 // interleaved (re, im) double arrays, offsets count elements; per-warp global scratch (orders

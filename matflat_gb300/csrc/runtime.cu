@@ -80,6 +80,7 @@ cudaError_t g_attr_err[64];
 struct mfg_ctx {
   int device = 0;
   int sm_count = 0;
+  int smem_per_sm = 0;   // shared memory per SM (bytes)
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   DevBuf work;
@@ -141,12 +142,18 @@ struct mfg_plan {
   // GETRF (double): size-bucketed tasks.  gsel picks the lanes-per-matrix table (-1: one matrix
   // per warp, no tasks); segment s holds the tasks of G = 32 >> s lanes per matrix.
   int gsel = -1;
-  int seg_off[4] = {0, 0, 0, 0};
-  int seg_cnt[4] = {0, 0, 0, 0};
+  int seg_off[5] = {0, 0, 0, 0, 0};
+  int seg_cnt[5] = {0, 0, 0, 0, 0};
   // POTRF (double): lanes-per-matrix table of the size buckets (0: one group size for the plan,
   // args.group); segment s of `order` holds the matrices of G = 32 >> s lanes.
   int csel = 0;
   int cta_nmax = 0;  // GETRF: largest order of the CTA-per-matrix segment (segment 3)
+  // GETRF (double): resident form (segment 4): orders in [blk_lo, SMEM_N] go to one CTA of blk_w
+  // warps each, blk_cps CTAs per SM, the matrix in shared memory; blk_lo = 0: off.
+  int blk_lo = 0;
+  int blk_w = 4;
+  int blk_cps = 2;
+  int blk_nmax = 0;
   int* d_task_first = nullptr;
   int* d_task_gc = nullptr;
   std::vector<int> hn;  // GETRF/POTRF: the order of every matrix (host copy, for the autotuner)
@@ -365,7 +372,7 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return p->hn[x] > p->hn[y]; });
   struct Task { int first, cnt, g; };
-  std::vector<Task> segs[4];
+  std::vector<Task> segs[5];
   // Orders above SMEM_N go to whole CTAs (segment 3) when there are too few of them to give every
   // SM eight warps; MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
   long long big = 0;
@@ -381,6 +388,11 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
       i = j;
       continue;
     }
+    if (p->blk_lo > 0 && nn >= p->blk_lo && nn <= mfg::SMEM_N) {
+      for (int k = i; k < j; k++) segs[4].push_back({k, 1, 0});
+      i = j;
+      continue;
+    }
     const int g = lu_lanes(gsel, nn);
     const int per = 32 / g;
     const int sg = g == 32 ? 0 : g == 16 ? 1 : 2;
@@ -389,9 +401,11 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   }
   p->cta_nmax = 0;
   for (const Task& t : segs[3]) p->cta_nmax = std::max(p->cta_nmax, p->hn[idx[t.first]]);
+  p->blk_nmax = 0;
+  for (const Task& t : segs[4]) p->blk_nmax = std::max(p->blk_nmax, p->hn[idx[t.first]]);
   std::vector<int> order, first, gc;
   order.reserve(count);
-  for (int sg = 0; sg < 4; sg++) {
+  for (int sg = 0; sg < 5; sg++) {
     p->seg_off[sg] = (int)first.size();
     p->seg_cnt[sg] = (int)segs[sg].size();
     const auto& v = segs[sg];
@@ -504,6 +518,20 @@ bool tune_env_override() {
   return false;
 }
 
+// Dynamic shared memory of one resident-form CTA: an equal share of the SM's shared memory for
+// blk_cps CTAs (less 2 KB each for the CTA's reservation and static variables), at least what the
+// segment's largest order needs without its copy, at most what the kernel may be given.
+int blk_smem_bytes(const mfg_plan* p) {
+  const int cps = std::max(1, p->blk_cps);
+  long long b = (long long)p->ctx->smem_per_sm / cps - 2048;
+  b = b / 128 * 128;
+  const long long floor_b =
+      (long long)sizeof(double) * mfg::getrf_blk_smem_doubles(p->blk_nmax, p->nrhs, p->blk_w, false);
+  if (b < floor_b) b = floor_b;
+  if (b > mfg::getrf_blk_smem_max()) b = mfg::getrf_blk_smem_max();
+  return (int)b;
+}
+
 int plan_launch(mfg_plan* p, cudaStream_t s) {
   mfg_ctx* ctx = p->ctx;
   int* queue = p->kind == mfg_plan::GEQRF  ? p->qd.queue
@@ -520,14 +548,20 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   if (tasks) {
     // One launch per lanes-per-matrix bucket (32, then 16, then 8 lanes), each persistent over
     // its own task queue.
-    for (int sg = 0; sg < 4; sg++) {
+    for (int sg = 0; sg < 5; sg++) {
       if (p->seg_cnt[sg] == 0) continue;
       BatchArgs a = p->args;
       a.task_first = p->d_task_first + p->seg_off[sg];
       a.task_gc = p->d_task_gc + p->seg_off[sg];
       a.ntasks = p->seg_cnt[sg];
       a.queue = p->args.queue + 1 + sg;
-      if (sg == 3) {
+      if (sg == 4) {
+        // Resident form: blk_cps CTAs of blk_w warps per SM, each with an equal share of the
+        // SM's shared memory (at least what a matrix of the segment needs without its copy).
+        int ctas = (int)std::min<long long>(a.ntasks, (long long)ctx->sm_count * p->blk_cps);
+        if (ctas < 1) ctas = 1;
+        e = mfg::launch_getrf_blk(a, ctas, p->blk_w, blk_smem_bytes(p), s);
+      } else if (sg == 3) {
         // One matrix per CTA: the CTA kernel counts its work items in `count`.
         a.count = a.ntasks;
         const long long slices = (long long)p->ctas * p->warps;   // scratch slices
@@ -537,6 +571,7 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
       } else {
         const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
         const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
+        a.minb = p->ctas / std::max(1, ctx->sm_count);
         e = mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
       }
       if (e != cudaSuccess) return cuda_fail(ctx, e, "batched LU launch");
@@ -785,6 +820,15 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     // Size-bucketed tasks (lanes per matrix by order); MFG_LU_GROUPS picks the table, -1 the
     // one-matrix-per-warp queue.
     const int gsel = env_int("MFG_LU_GROUPS", 2);
+    // Resident form: MFG_LU_BLK = "lo,w,cps" (smallest order, warps per CTA, CTAs per SM).
+    if (const char* v = std::getenv("MFG_LU_BLK")) {
+      int lo = 0, w = 4, cps = 2;
+      if (std::sscanf(v, "%d,%d,%d", &lo, &w, &cps) >= 1) {
+        p->blk_lo = lo;
+        p->blk_w = (w == 2 || w == 4 || w == 8) ? w : 4;
+        p->blk_cps = std::max(1, std::min(cps, 16));
+      }
+    }
     if (gsel >= 0) {
       const int rc = getrf_build_tasks(p, gsel);
       if (rc != MFG_OK) {
@@ -1147,6 +1191,7 @@ MFG_API int mfg_create(mfg_ctx** ctx) {
   mfg_ctx* c = new mfg_ctx();
   cudaGetDevice(&c->device);
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
   e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -2623,7 +2668,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
     // than 32 (two matrices per warp double the footprint in flight), 8 lanes pays off at small
     // orders; the tables are tried at 20-28 warps per SM, where they are fastest.
     for (int gsel : {0, 2, 4})
-      for (int wps : {20, 24, 28}) cands.push_back({4, wps, gsel, 0, 2});
+      for (int wps : {20, 24, 28, 32}) cands.push_back({4, wps, gsel, 0, 2});
     cands.push_back({4, 24, 1, 0, 2});
     cands.push_back({4, 24, -1, 0, 2});
     cands.push_back({4, 20, -1, 0, 4});

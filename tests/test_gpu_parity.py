@@ -419,6 +419,63 @@ def test_lu_batched_every_lanes_table(mf, table, monkeypatch):
     assert _host(dinfo)[11] == 1
 
 
+@pytest.mark.parametrize("env", [
+    {"MFG_LU_GROUPS": "0", "MFG_WARPS_PER_SM": "28"},
+    {"MFG_LU_GROUPS": "2", "MFG_WARPS_PER_SM": "32"},
+    {"MFG_LU_BLK": "1,4,2"},
+    {"MFG_LU_BLK": "60,2,5"},
+    {"MFG_LU_BLK": "100,4,1"},
+    {"MFG_LU_BLK": "1,8,3"},
+], ids=["occ28", "occ32", "res-4x2", "res-2x5", "res-4x1", "res-8x3"])
+def test_lu_batched_launch_forms(mf, env, monkeypatch):
+    """The register-bounded variants of the task kernel (28 and 32 warps per SM) and the resident
+    form (one matrix per CTA of 2, 4 or 8 warps, the matrix in shared memory when it fits, in
+    global memory otherwise) give the oracle's factors, pivots, signs and solutions bit for bit,
+    over orders 1..140 including a zero matrix, NaN and infinite entries and tied pivots."""
+    import torch
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    rng = np.random.default_rng(77)
+    n = rng.integers(1, 141, size=160).astype(np.int32)
+    n[:10] = [1, 2, 8, 9, 48, 60, 96, 100, 128, 129]
+    nrhs = 4
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]])
+    a = rng.standard_normal(int(sz.sum()))
+    a[a_off[11]:a_off[11] + n[11] * n[11]] = 0.0
+    a[a_off[12] + 5] = np.nan
+    a[a_off[13] + 3] = np.inf
+    m14 = a[a_off[14]:a_off[14] + n[14] * n[14]].reshape(n[14], n[14], order="F")
+    m14[:, 0] = 1.0                       # every first-column candidate ties
+    a[a_off[14]:a_off[14] + n[14] * n[14]] = m14.reshape(-1, order="F")
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]])
+    b_off = piv_off * nrhs
+    b = rng.standard_normal(int(n.sum()) * nrhs)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=nrhs, b_off=b_off)
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(int(n.sum()), dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(len(n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    oa, ob = a.copy(), b.copy()
+    opiv = np.zeros(int(n.sum()), np.int32)
+    osign = np.zeros(len(n), np.int32)
+    oracle.lu_solve_batched(n, a_off, oa, piv_off, opiv, b_off, ob, nrhs, osign, 4)
+    assert_bits(_host(da), oa)
+    np.testing.assert_array_equal(_host(dpiv), opiv)
+    np.testing.assert_array_equal(_host(dsign), osign)
+    assert_bits(_host(db), ob)
+    assert _host(dinfo)[11] == 1
+    # Solve-only calls on the factors give the fused call's solutions.
+    db2 = _dev(b)
+    torch.cuda.synchronize()
+    batch.solve(da, dpiv, db2)
+    mf.context().synchronize()
+    assert_bits(_host(db2), ob)
+
+
 @pytest.mark.parametrize("table", [0, 1, 2])
 def test_cholesky_batched_every_lanes_table(mf, table, monkeypatch):
     """The batched Cholesky + solve with lanes per matrix chosen per size bucket (4/8/16/32 lanes
