@@ -214,7 +214,7 @@ __device__ __forceinline__ double fma_dot(int len, const double* x, long long in
 // diagonal and the sums of squares accumulate with fused multiply-adds.  The result satisfies the
 // usual Cholesky backward-error bound |A - L L^T| <= gamma_(n+2) |L| |L^T|.
 template <int G>
-__device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum) {
+__device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum, double* rcp) {
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int j = lane; j < n; j += G) dsum[j] = 0.0;
@@ -226,7 +226,10 @@ __device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum) {
     const double lkk = __dsqrt_rn(s);
     const double rk = __drcp_rn(lkk);
     __syncwarp(gm);
-    if (lane == 0) colk[k] = lkk;
+    if (lane == 0) {
+      colk[k] = lkk;
+      rcp[k] = rk;
+    }
     // S lanes per row: 1 while the step has at least half as many rows as the group has lanes,
     // else 2 or 4 lanes share each row's dot (a contiguous part of it each), combined with
     // shuffles within the S lanes.  Every lane runs the same number of rounds (convergent
@@ -263,6 +266,68 @@ __device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum) {
   return 0;
 }
 
+// The FMA form's solves, L y = b then L^T x = y, on the factor potrf_group_fma left (rcp[k] =
+// 1 / L(k,k) rounded, from the factorization): column sweeps with fused multiply-adds and
+// multiplications by the reciprocal diagonal, backward stable like the factorization (not
+// MatFlat's bits).  Right-hand sides are staged in xs (leading dimension n | 1).
+template <int G>
+__device__ void potrs_group_fma(const double* l, int n, long long lda, const double* rcp,
+                                double* b, long long ldb, int nrhs, double* xs) {
+  const int lane = group_lane<G>();
+  const unsigned gm = group_mask<G>();
+  const int ldx = n | 1;
+  for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
+    const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
+    for (int e = lane; e < nr * n; e += G) {
+      const int r = e / n;
+      const int i = e - r * n;
+      xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + i];
+    }
+    __syncwarp(gm);
+    // Forward: x_t = x_t / L(t,t), then x_i -= L(i,t) x_t below it (column t of L, contiguous).
+    for (int t = 0; t < n; ++t) {
+      const double rt = rcp[t];
+      const double* colt = l + (long long)t * lda;
+      double xt[RHS_CHUNK];
+#pragma unroll
+      for (int r = 0; r < RHS_CHUNK; ++r) xt[r] = r < nr ? __dmul_rn(xs[r * ldx + t], rt) : 0.0;
+      __syncwarp(gm);
+      if (lane == 0)
+        for (int r = 0; r < nr; ++r) xs[r * ldx + t] = xt[r];
+      for (int i = t + 1 + lane; i < n; i += G) {
+        const double lit = colt[i];
+#pragma unroll
+        for (int r = 0; r < RHS_CHUNK; ++r)
+          if (r < nr) xs[r * ldx + i] = __fma_rn(-lit, xt[r], xs[r * ldx + i]);
+      }
+      __syncwarp(gm);
+    }
+    // Backward: x_t = x_t / L(t,t), then x_i -= L(t,i) x_t above it (row t of L).
+    for (int t = n - 1; t >= 0; --t) {
+      const double rt = rcp[t];
+      double xt[RHS_CHUNK];
+#pragma unroll
+      for (int r = 0; r < RHS_CHUNK; ++r) xt[r] = r < nr ? __dmul_rn(xs[r * ldx + t], rt) : 0.0;
+      __syncwarp(gm);
+      if (lane == 0)
+        for (int r = 0; r < nr; ++r) xs[r * ldx + t] = xt[r];
+      for (int i = lane; i < t; i += G) {
+        const double lti = l[(long long)i * lda + t];
+#pragma unroll
+        for (int r = 0; r < RHS_CHUNK; ++r)
+          if (r < nr) xs[r * ldx + i] = __fma_rn(-lti, xt[r], xs[r * ldx + i]);
+      }
+      __syncwarp(gm);
+    }
+    for (int e = lane; e < nr * n; e += G) {
+      const int r = e / n;
+      const int i = e - r * n;
+      b[(long long)(r0 + r) * ldb + i] = xs[r * ldx + i];
+    }
+    __syncwarp(gm);
+  }
+}
+
 // Per-warp shared memory: every group keeps its column sums and staged right-hand sides there
 // for n <= 4G (G = 32: n <= 128); larger matrices use the group's slice of global scratch.
 template <int G>
@@ -288,8 +353,8 @@ static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
 #define MFG_CHOL_FMA_WARPS 24
 #endif
 
-// FMA = true: the FMA form of the factorization (potrf_group_fma); the solves keep MatFlat's
-// arithmetic on the factor they are given.
+// FMA = true: the FMA form of the factorization (potrf_group_fma) and of the solves
+// (potrs_group_fma).
 template <int WARPS, bool IM, int G, bool SPLIT = false, bool FMA = false>
 __global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS : 1)
     potrf_batched_kernel(BatchArgs p) {
@@ -319,17 +384,31 @@ __global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS :
       double* scr = (n <= 4 * G) ? smem_group : p.gscratch + gg * p.gscratch_stride;
       const int ldx = n | 1;
       double* sol = (n <= 4 * G && gs) ? gsol : scr + n;
+      // FMA form: the reciprocal diagonal for its solves (after the column sums in the group's
+      // shared area, or in the solve accumulator the FMA solves do not use).
+      double* rcp = (n <= 4 * G && gs) ? scr + n : sol + RHS_CHUNK * ldx;
       int info = 0;
       if (!p.solve_only) {
         if constexpr (FMA)
-          info = potrf_group_fma<G>(a, n, lda, scr);
+          info = potrf_group_fma<G>(a, n, lda, scr, rcp);
         else if constexpr (SPLIT)
           info = potrf_group_split<G, IM>(a, n, lda, scr);
         else
           info = potrf_group<G, IM>(a, n, lda, scr);
       }
-      if (info == 0 && p.nrhs > 0)
+      if constexpr (FMA) {
+        if (info == 0 && p.nrhs > 0) {
+          // Solve-only calls form the reciprocals from the stored diagonal: the same values
+          // as the factorization's.
+          if (p.solve_only) {
+            for (int t = lane & (G - 1); t < n; t += G) rcp[t] = __drcp_rn(a[(long long)t * lda + t]);
+            __syncwarp(group_mask<G>());
+          }
+          potrs_group_fma<G>(a, n, lda, rcp, p.b + p.b_off[mat], n, p.nrhs, sol);
+        }
+      } else if (info == 0 && p.nrhs > 0) {
         potrs_group<G>(a, n, lda, p.b + p.b_off[mat], n, p.nrhs, sol, sol + RHS_CHUNK * ldx);
+      }
       if ((lane & (G - 1)) == 0 && !p.solve_only) p.info[mat] = info;
     }
     __syncwarp();

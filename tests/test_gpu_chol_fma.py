@@ -66,6 +66,15 @@ def test_cholesky_fma_backward_error(mf, table, monkeypatch):
         differs += int(not np.array_equal(ga[sl], oa[sl]))
     # the form is a different arithmetic: most factors differ from MatFlat's in the last bits
     assert differs > 0
+    # a solve-only call on the FMA factors gives the fused call's solutions bit for bit
+    db2 = _dev(b)
+    torch.cuda.synchronize()
+    batch.solve(da, db2)
+    mf.context().synchronize()
+    ok = oinfo == 0
+    for i in np.nonzero(ok)[0][::5]:
+        sl = slice(b_off[i], b_off[i] + int(n[i]))
+        assert_bits(_host(db2)[sl], gb[sl], "solve-only, matrix %d" % i)
     # switching the plan back gives MatFlat's bits again
     batch.set_form("exact")
     da, db = _dev(a), _dev(b)
