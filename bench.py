@@ -689,6 +689,63 @@ def chol_fma_check(torch, d, a_in, a_out, b_in, b_out, info):
                        "C++) for info, %.1f s" % t_or}
 
 
+def measure_cholesky(torch, mf, rank, steps, warmup, fp64_peak):
+    """The Cholesky half of the metric on the default line: 100,000 SPD matrices n~U{8..128}
+    (the chol100k configuration) + 1-RHS solve, the FMA form (backward-error checked over the
+    whole batch) and MatFlat's exact form, each autotuned at plan creation, timed like the main
+    step (L2 flushed, device-to-device restore of the inputs, one plan execution) with CUDA
+    events on the plan's stream."""
+    ctx = mf.context()
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    d = make_inputs("chol100k", rank)
+    count = len(d["n"])
+    a0 = torch.from_numpy(d["a"]).cuda()
+    b0 = torch.from_numpy(d["b"]).cuda()
+    a = torch.empty_like(a0)
+    b = torch.empty_like(b0)
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flops = chol_flops(d["n"], d["nrhs"])
+    out = {"workload": CONFIGS["chol100k"]["workload"], "count": count}
+    for form in ("fma", "exact"):
+        plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+        plan.set_form(form)
+        tuned = plan.autotune()
+        ks, ke = [], []
+        with torch.cuda.stream(stream):
+            for it in range(warmup + steps):
+                flush.zero_()
+                a.copy_(a0)
+                b.copy_(b0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                plan.run(a, b, info)
+                e1.record(stream)
+                if it >= warmup:
+                    ks.append(e0)
+                    ke.append(e1)
+            stream.synchronize()
+        kms = statistics.median(s0.elapsed_time(s1) for s0, s1 in zip(ks, ke))
+        tf = flops / (kms / 1e3) / 1e12
+        rec = {"value": count / (kms / 1e3), "unit": "matrices/s", "kernel_ms": kms,
+               "roofline": {"bound": "fp64", "achieved": tf, "peak": fp64_peak,
+                            "unit": "TFLOP/s", "frac": tf / fp64_peak},
+               "launch_shape": dict(zip(["warps_per_cta", "warps_per_sm", "lanes_per_matrix",
+                                         "mul_mode", "dot_pairs_per_block"], tuned))}
+        if form == "fma":
+            rec["form"] = ("fused multiply-adds in any order, reciprocal column scaling, FMA "
+                           "solves (mfg_plan_set_form); not MatFlat's bits, checked by backward "
+                           "error over the whole batch")
+            rec["form_check"] = chol_fma_check(torch, d, a0, a, b0, b, info)
+        else:
+            rec["form"] = "MatFlat's arithmetic, bit for bit"
+        out[form] = rec
+        del plan
+    return out
+
+
 def lu_parity(d, a_out, b_out, piv_out, sign_out, info_out):
     """The oracle (MatFlat's LuCore + solve restated in C++) over the WHOLE timed batch, after
     the timed region, compared with the GPU's outputs of the last timed step bit for bit."""
@@ -748,6 +805,9 @@ def main():
                     help="lu: skip the oracle check of the whole timed batch")
     ap.add_argument("--no-mixed", action="store_true",
                     help="lu: skip the mixed-precision sub-measurement")
+    ap.add_argument("--no-cholesky", action="store_true",
+                    help="lu: skip the Cholesky record (100,000 SPD matrices, FMA and exact "
+                         "forms) of the default line")
     ap.add_argument("--form", default="exact", choices=["exact", "fma"],
                     help="chol/chol100k: arithmetic form of the factorization (exact: MatFlat's "
                          "bits; fma: fused multiply-adds, checked by backward error)")
@@ -1116,6 +1176,11 @@ def main():
                  "timing": "CUDA events on the solver's stream, 3 warm-up + 3 timed solves; "
                            "plain rate: one timed exact FP64 LU + solve of the same systems"}
 
+    # ---- the Cholesky half of the metric (100,000 SPD matrices n~U{8..128}) -------------------
+    cholesky = None
+    if cfg_name == "lu" and not args.no_cholesky:
+        cholesky = measure_cholesky(torch, mf, rank, 5, 3, fp64_peak)
+
     if rank == 0:
         line = {
             "metric": metric_name(cfg_name), "value": value, "unit": "matrices/s",
@@ -1150,6 +1215,8 @@ def main():
             line["form_check"] = form_check
         if mixed is not None:
             line["mixed"] = mixed
+        if cholesky is not None:
+            line["cholesky"] = cholesky
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -593,7 +593,8 @@ __global__ void __launch_bounds__(WARPS * 32) getrf_task_kernel(BatchArgs p) {
 }
 
 // The same with the register allocation bounded for MINB resident CTAs of 4 warps per SM (28 or
-// 32 warps): the plan launches it when its shape asks for that many.
+// 32 warps): the plan launches it when its shape asks for that many, for 32 lanes per matrix (the
+// 16- and 8-lane schedules spill under that bound and run slower).
 template <int IM, int DB, int G, int MINB>
 __global__ void __launch_bounds__(128, MINB) getrf_task_kernel_occ(BatchArgs p) {
   getrf_task_loop<4, IM, DB, G>(p);
@@ -803,9 +804,9 @@ static cudaError_t launch_getrf_task_g(const BatchArgs& args, int ctas, cudaStre
   const size_t smem = getrf_task_smem_bytes<WARPS>(G);
   if (args.hw_mul)
     getrf_task_kernel<WARPS, 0, 4, G><<<ctas, WARPS * 32, smem, s>>>(args);
-  else if (WARPS == 4 && args.dot_block == 2 && args.minb >= 8)
+  else if (WARPS == 4 && G == 32 && args.dot_block == 2 && args.minb >= 8)
     getrf_task_kernel_occ<1, 2, G, 8><<<ctas, 128, smem, s>>>(args);
-  else if (WARPS == 4 && args.dot_block == 2 && args.minb == 7)
+  else if (WARPS == 4 && G == 32 && args.dot_block == 2 && args.minb == 7)
     getrf_task_kernel_occ<1, 2, G, 7><<<ctas, 128, smem, s>>>(args);
   else if (args.dot_block == 2)
     getrf_task_kernel<WARPS, 1, 2, G><<<ctas, WARPS * 32, smem, s>>>(args);
@@ -832,10 +833,10 @@ static cudaError_t set_getrf_task_attr_g() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(getrf_task_kernel<WARPS, 1, 4, G>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (WARPS == 4 && e == cudaSuccess)
+  if (WARPS == 4 && G == 32 && e == cudaSuccess)
     e = cudaFuncSetAttribute(getrf_task_kernel_occ<1, 2, G, 8>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (WARPS == 4 && e == cudaSuccess)
+  if (WARPS == 4 && G == 32 && e == cudaSuccess)
     e = cudaFuncSetAttribute(getrf_task_kernel_occ<1, 2, G, 7>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;

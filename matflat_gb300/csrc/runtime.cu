@@ -3109,8 +3109,13 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     if (p->kind == mfg_plan::GETRF || p->kind == mfg_plan::POTRF) {
       // Same launch shape as the parent plan (which the autotuner may have chosen), then the
       // element type's scratch.
-      rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count),
-                        p->args.group, p->args.hw_mul, p->args.dot_block);
+      // The lanes table (GETRF) or the Cholesky's size-bucket table travel in plan_reshape's
+      // group argument, as the autotuner passes them.
+      const int group = p->kind == mfg_plan::GETRF ? p->gsel
+                        : p->csel > 0               ? -p->csel
+                                                    : p->args.group;
+      rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count), group,
+                        p->args.hw_mul, p->args.dot_block);
       if (rc == MFG_OK) rc = plan_set_elem(sub, pipe_elem(op));
       if (rc != MFG_OK) return rc;
       sub->args.fma = p->args.fma;
