@@ -689,6 +689,42 @@ def chol_fma_check(torch, d, a_in, a_out, b_in, b_out, info):
                        "C++) for info, %.1f s" % t_or}
 
 
+def qr_fma_check(d, a_out, rd_out, b_out, every=25):
+    """The FMA-form QR's promise on a strided sample of the timed batch (host copies, after
+    timing): the reflectors and R reproduce A to a normwise backward error within 1e-13 m
+    (A = H_0 ... H_{n-1} [R; 0], H_k = I - v_k v_k^T / v_k[0], MatFlat's storage), and the
+    least-squares solution's normal-equation residual ||A^T (A x - b)|| / (||A|| ||b||) against
+    the exact form's bound used by the tests (1e-9)."""
+    t0 = time.perf_counter()
+    worst_f = worst_ls = 0.0
+    checked = 0
+    for i in range(0, len(d["m"]), every):
+        mi, ni = int(d["m"][i]), int(d["n"][i])
+        ao, bo, ro = int(d["a_off"][i]), int(d["b_off"][i]), int(d["rdiag_off"][i])
+        A = d["a"][ao:ao + mi * ni].reshape(ni, mi).T
+        F = a_out[ao:ao + mi * ni].reshape(ni, mi).T
+        rd = rd_out[ro:ro + ni]
+        r = np.zeros((mi, ni))
+        r[:ni, :] = np.triu(F[:ni, :], 1)
+        r[np.arange(ni), np.arange(ni)] = rd
+        for k in range(ni - 1, -1, -1):
+            v = F[k:, k]
+            if rd[k] != 0 and v[0] != 0:
+                r[k:, :] -= np.outer(v, v @ r[k:, :]) / v[0]
+        na = np.linalg.norm(A)
+        worst_f = max(worst_f, np.linalg.norm(A - r) / na / mi)
+        bi = d["b"][bo:bo + mi]
+        x = b_out[bo:bo + ni]
+        worst_ls = max(worst_ls, np.linalg.norm(A.T @ (A @ x - bi)) / (na * np.linalg.norm(bi)))
+        checked += 1
+    return {"factor_berr_over_m_max": float(worst_f), "bound_over_m": 1e-13,
+            "ls_normal_residual_max": float(worst_ls), "ls_bound": 1e-9,
+            "within_bound": bool(worst_f <= 1e-13 and worst_ls <= 1e-9), "checked": checked,
+            "sample": "every %dth matrix of the timed batch" % every,
+            "checker": "numpy FP64 reconstruction from the stored reflectors, %.1f s"
+                       % (time.perf_counter() - t0)}
+
+
 def measure_cholesky(torch, mf, rank, steps, warmup, fp64_peak):
     """The Cholesky half of the metric on the default line: 100,000 SPD matrices n~U{8..128}
     (the chol100k configuration) + 1-RHS solve, the FMA form (backward-error checked over the
@@ -858,6 +894,8 @@ def main():
         a_host = torch.from_numpy(d["a"].astype(npdt)).pin_memory()
         b_host = torch.from_numpy(d["b"].astype(npdt)).pin_memory()
         plan = mf.QrBatch(d["m"], d["n"], d["a_off"], d["rdiag_off"], nrhs=1, b_off=d["b_off"])
+        if cfg_name == "qr":
+            plan.set_form(args.form)
         if not args.no_autotune:
             tuned = plan.autotune()
         a0 = a_host.to("cuda")
@@ -1031,6 +1069,8 @@ def main():
     form_check = None
     if cfg_name in ("chol", "chol100k") and args.form == "fma" and rank == 0:
         form_check = chol_fma_check(torch, d, a0, a, b0, b, info)
+    if cfg_name == "qr" and args.form == "fma" and rank == 0:
+        form_check = qr_fma_check(d, a.cpu().numpy(), rdiag.cpu().numpy(), b.cpu().numpy())
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -1209,9 +1249,9 @@ def main():
         if parity is not None:
             line["parity"] = parity
         if form_check is not None:
-            line["config"]["form"] = ("fma: fused multiply-adds in any order, reciprocal column "
-                                      "scaling (mfg_plan_set_form); not MatFlat's bits, checked "
-                                      "by backward error")
+            line["config"]["form"] = ("fma: fused multiply-adds, reciprocal column scaling "
+                                      "(mfg_plan_set_form); not MatFlat's bits, checked by "
+                                      "backward error")
             line["form_check"] = form_check
         if mixed is not None:
             line["mixed"] = mixed

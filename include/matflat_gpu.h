@@ -473,15 +473,20 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
  * MFG_LU_GROUPS, MFG_QR_GROUP) take precedence over the table for new plans. */
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 
-/* Arithmetic form of a batched Cholesky plan (no counterpart in the reference; MatFlat has one
- * form).  MFG_FORM_EXACT (default): MatFlat's arithmetic, bit-identical factors, info and
- * solutions.  MFG_FORM_FMA: the same column order and failure test, with fused multiply-adds in
- * any order and the column scaled by the reciprocal of its diagonal: the factor satisfies the
- * Cholesky backward-error bound |A - L L^T| <= gamma_(n+2) |L| |L^T| instead of MatFlat's bits
- * (solutions then use MatFlat's triangular solves on that factor), and info reports a column
- * whose computed pivot is not positive, which differs from MatFlat only for matrices within
- * rounding of the positive-definite boundary.  Applies to the double overload of potrf plans;
- * MFG_ERR_UNSUPPORTED for other plans.  Drops the plan's cached graph. */
+/* Arithmetic form of a batched Cholesky or QR plan (no counterpart in the reference; MatFlat has
+ * one form).  MFG_FORM_EXACT (default): MatFlat's arithmetic, bit-identical factors, info and
+ * solutions.  MFG_FORM_FMA, Cholesky (double overload): the same column order and failure test,
+ * with fused multiply-adds in any order and the column scaled by the reciprocal of its
+ * diagonal: the factor satisfies the Cholesky backward-error bound
+ * |A - L L^T| <= gamma_(n+2) |L| |L^T| instead of MatFlat's bits, the solves are fused
+ * multiply-add column sweeps with that reciprocal diagonal (solve-only calls give the same
+ * bits), and info reports a column whose computed pivot is not positive, which differs from
+ * MatFlat only for matrices within rounding of the positive-definite boundary.  MFG_FORM_FMA, QR
+ * (double overload): MatFlat's Householder algorithm and storage (no sign choice,
+ * rdiag = -norm, the same degenerate-reflector rules) with fused multiply-add dots, norms and
+ * updates and the column scaled by the reciprocal of its norm: backward-stable factors and
+ * least-squares solutions instead of MatFlat's bits.  MFG_ERR_UNSUPPORTED for other plans.
+ * Drops the plan's cached graph. */
 enum mfg_form { MFG_FORM_EXACT = 0, MFG_FORM_FMA = 1 };
 MFG_API int mfg_plan_set_form(mfg_plan* plan, int form);
 

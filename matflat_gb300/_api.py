@@ -790,6 +790,12 @@ class QrBatch(_Batch):
         self.count = len(self._m)
         self.nrhs = nrhs
 
+    def set_form(self, form):
+        """Arithmetic form of the double factorization: "exact" (MatFlat's bits, the default) or
+        "fma" (fused multiply-adds, backward-stable factors, not MatFlat's bits)."""
+        code = FORMS[form]
+        self.ctx.check(self.ctx.lib.mfg_plan_set_form(self.h, code), "mfg_plan_set_form")
+
     def run(self, a, rdiag, b=None, single=False, dtype=None):
         """QR (+ least squares) of device buffers: float64 (default), float32 (single=True or a
         float32 tensor) or Complex (a complex128 tensor, or dtype="z" for interleaved float64;

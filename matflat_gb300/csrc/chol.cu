@@ -161,53 +161,6 @@ __device__ void potrs_group(const double* l, int n, long long lda, double* b, lo
   }
 }
 
-// Dot product with fused multiply-adds in four independent chains (the FMA form: any order is
-// allowed, so the chains give the loop instruction-level parallelism); the next block's operands
-// are loaded before the current block's multiply-adds.
-__device__ __forceinline__ double fma_dot(int len, const double* x, long long incx, const double* y,
-                                          long long incy) {
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-  const int blocks = len >> 2;
-  if (blocks > 0) {
-    double xa[4], ya[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      xa[u] = x[u * incx];
-      ya[u] = y[u * incy];
-    }
-    for (int blk = 0; blk < blocks; ++blk) {
-      double xb[4], yb[4];
-      const bool more = blk + 1 < blocks;
-      if (more) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          xb[u] = x[(4 + u) * incx];
-          yb[u] = y[(4 + u) * incy];
-        }
-      }
-      s0 = __fma_rn(xa[0], ya[0], s0);
-      s1 = __fma_rn(xa[1], ya[1], s1);
-      s2 = __fma_rn(xa[2], ya[2], s2);
-      s3 = __fma_rn(xa[3], ya[3], s3);
-      x += 4 * incx;
-      y += 4 * incy;
-      if (more) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          xa[u] = xb[u];
-          ya[u] = yb[u];
-        }
-      }
-    }
-  }
-  for (int t = blocks * 4; t < len; ++t) {
-    s0 = __fma_rn(x[0], y[0], s0);
-    x += incx;
-    y += incy;
-  }
-  return __dadd_rn(__dadd_rn(s0, s1), __dadd_rn(s2, s3));
-}
-
 // The FMA form of the factorization (selected per plan; not MatFlat's bits): the same column
 // order and the same failure test (A(k,k) - sum of squares <= 0 -> k+1) as potrf_group, but every
 // dot runs as fused multiply-adds in four chains, the column is scaled by the reciprocal of its

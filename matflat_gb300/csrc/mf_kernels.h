@@ -95,6 +95,8 @@ struct QrBatchArgs {
   int solve_only;            // a and rdiag hold the factorization; only solve the b blocks
   int fused;                 // one pass per trailing column and step (qr_warp_fused); the
                              // coefficient scratch then holds 2 (n + nrhs) values
+  int fma;                   // double: the FMA form (fused multiply-adds, reciprocal column
+                             // scaling): backward-stable factors, not MatFlat's bits
 };
 // Shared-memory coefficients per matrix of the batched QR for a group size.
 int qr_smem_coefs(int group);

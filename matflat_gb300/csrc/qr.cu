@@ -18,6 +18,8 @@
 // a, diagonal rdiag).  On exit b[0:n] = x and b[n:m] holds the residual components.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "mf_device.cuh"
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
@@ -69,6 +71,12 @@ struct QrArith<double> {
   static __device__ __forceinline__ bool nz(double v) { return nonzero(v); }
   static __device__ __forceinline__ bool nzr(double v) { return nonzero(v); }
   static __device__ __forceinline__ double divn(double x, double norm) { return __ddiv_rn(x, norm); }
+  // x[i] = x[i] / norm for i = first, first + step, ... < end: the quotients on the integer pipes
+  // (idiv_column: the same bits as the FP64 division).
+  static __device__ __forceinline__ void divcol(double* x, int first, int end, int step,
+                                                double norm) {
+    idiv_column(x, first, end, step, norm);
+  }
   static __device__ __forceinline__ double neg_r(double norm) { return -norm; }
   // QrOrthogonalFactor's dot and update (Qr.cs:408-409)
   static __device__ __forceinline__ double qdot(int len, const double* a, const double* q) {
@@ -111,6 +119,10 @@ struct QrArith<float> {
   static __device__ __forceinline__ bool nz(float v) { return (__float_as_uint(v) << 1) != 0u; }
   static __device__ __forceinline__ bool nzr(float v) { return nz(v); }
   static __device__ __forceinline__ float divn(float x, float norm) { return __fdiv_rn(x, norm); }
+  static __device__ __forceinline__ void divcol(float* x, int first, int end, int step,
+                                                float norm) {
+    for (int i = first; i < end; i += step) x[i] = __fdiv_rn(x[i], norm);
+  }
   static __device__ __forceinline__ float neg_r(float norm) { return -norm; }
   static __device__ __forceinline__ double qdot(int len, const float* a, const float* q) {
     return exact_dot_f(len, a, 1, q, 1);
@@ -157,6 +169,10 @@ struct QrArith<zdouble> {
   static __device__ __forceinline__ zdouble divn(zdouble x, double norm) {
     return zdiv(x, zmake(norm, 0.0));
   }
+  static __device__ __forceinline__ void divcol(zdouble* x, int first, int end, int step,
+                                                double norm) {
+    for (int i = first; i < end; i += step) x[i] = zdiv(x[i], zmake(norm, 0.0));
+  }
   static __device__ __forceinline__ zdouble add1(zdouble x) { return zadd(x, zmake(1.0, 0.0)); }
   static __device__ __forceinline__ zdouble coef(zdouble d, zdouble v0) { return zdiv(zneg(d), v0); }
   static __device__ __forceinline__ zdouble muladd(zdouble dst, zdouble x, zdouble s) {
@@ -174,6 +190,56 @@ struct QrArith<zdouble> {
   static __device__ __forceinline__ zdouble rdiag_elem(double r) { return zmake(r, 0.0); }
 };
 
+// The FMA form of the double QR (selected per plan, not MatFlat's bits): the same Householder
+// algorithm and storage (no reflector sign choice, rdiag = -norm, the degenerate-reflector rules),
+// with every dot and norm as fused multiply-adds in four chains, the updates as fused
+// multiply-adds and the column scaled by the reciprocal of its norm.  Householder QR in any
+// such arithmetic is backward stable: the computed R is the exact R of A + dA with
+// ||dA|| <= c m n u ||A||.
+struct QrArithFma {
+  using R = double;
+  static __device__ __forceinline__ double norm(int len, const double* x) {
+    return __dsqrt_rn(fma_dot(len, x, 1, x, 1));
+  }
+  // The column dots in the order the fused column pass accumulates them (prod, then pair after
+  // pair), so that solve-only calls apply the reflectors to right-hand sides with the fused
+  // call's bits.
+  static __device__ __forceinline__ double dot(int len, const double* x, const double* y) {
+    double d = 0.0;
+    int r = 0;
+    if (len & 1) {
+      d = __dmul_rn(x[0], y[0]);
+      r = 1;
+    }
+#pragma unroll 4
+    for (; r < len; r += 2) d = __fma_rn(x[r + 1], y[r + 1], __fma_rn(x[r], y[r], d));
+    return d;
+  }
+  static __device__ __forceinline__ double div(double x, double y) { return __ddiv_rn(x, y); }
+  static __device__ __forceinline__ double add1(double x) { return __dadd_rn(x, 1.0); }
+  static __device__ __forceinline__ double coef(double d, double v0) { return __ddiv_rn(-d, v0); }
+  static __device__ __forceinline__ double muladd(double dst, double x, double s) {
+    return __fma_rn(x, s, dst);
+  }
+  static __device__ __forceinline__ double mulsub(double dst, double x, double s) {
+    return __fma_rn(-x, s, dst);
+  }
+  static __device__ __forceinline__ bool nz(double v) { return nonzero(v); }
+  static __device__ __forceinline__ bool nzr(double v) { return nonzero(v); }
+  static __device__ __forceinline__ double divn(double x, double norm) { return __ddiv_rn(x, norm); }
+  static __device__ __forceinline__ void divcol(double* x, int first, int end, int step,
+                                                double norm) {
+    const double r = __drcp_rn(norm);
+    for (int i = first; i < end; i += step) x[i] = __dmul_rn(x[i], r);
+  }
+  static __device__ __forceinline__ double neg_r(double norm) { return -norm; }
+  static __device__ __forceinline__ double prod(double x, double y) { return __dmul_rn(x, y); }
+  static __device__ __forceinline__ double pair(double s, double x0, double y0, double x1,
+                                                double y1) {
+    return __fma_rn(x1, y1, __fma_rn(x0, y0, s));
+  }
+};
+
 // Column j of the factored matrix, or right-hand side j - n when j >= n.
 template <typename T>
 __device__ __forceinline__ T* qr_col(T* a, long long lda, int n, T* b, long long ldb, int j) {
@@ -185,10 +251,9 @@ __device__ __forceinline__ T* qr_col(T* a, long long lda, int n, T* b, long long
 // (a whole warp for G = 32; 32/G matrices per warp otherwise): the norm is one sequential dot
 // (every lane of the group evaluates it), the trailing-column dots are spread one per lane, and
 // the rank-1 update over (row, column) pairs.
-template <typename T, int G = 32>
-__device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag, T* b,
+template <typename T, int G = 32, class A = QrArith<T>>
+__device__ void qr_warp(T* a, int m, int n, long long lda, typename A::R* rdiag, T* b,
                         long long ldb, int nb, T* coefs) {
-  using A = QrArith<T>;
   using R = typename A::R;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
@@ -197,7 +262,7 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::
     const int len = m - k;
     const R norm = A::norm(len, ck + k);  // every lane of the group, same value
     if (A::nzr(norm)) {
-      for (int r = k + lane; r < m; r += G) ck[r] = A::divn(ck[r], norm);
+      A::divcol(ck, k + lane, m, G, norm);
       __syncwarp(gm);
       if (lane == 0) ck[k] = A::add1(ck[k]);
       __syncwarp(gm);
@@ -233,10 +298,9 @@ __device__ void qr_warp(T* a, int m, int n, long long lda, typename QrArith<T>::
 // operations in the same order as in qr_warp (every update of a column precedes the next dot on
 // it, and the dot's pairwise tree is unchanged), so the factors and rdiag are bit-identical.
 // coefs: 2 (n + nb) values (the previous step's coefficients and the current ones).
-template <typename T, int G = 32>
-__device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArith<T>::R* rdiag,
+template <typename T, int G = 32, class A = QrArith<T>>
+__device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename A::R* rdiag,
                               T* b, long long ldb, int nb, T* coefs) {
-  using A = QrArith<T>;
   using R = typename A::R;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
@@ -256,7 +320,7 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
     const bool has = A::nzr(norm);
     T v0{};
     if (has) {
-      for (int r = k + lane; r < m; r += G) ck[r] = A::divn(ck[r], norm);
+      A::divcol(ck, k + lane, m, G, norm);
       __syncwarp(gm);
       if (lane == 0) ck[k] = A::add1(ck[k]);
       __syncwarp(gm);
@@ -362,11 +426,10 @@ __device__ void qr_warp_fused(T* a, int m, int n, long long lda, typename QrArit
 // Applies the stored reflectors of a factored matrix to the nb columns of b, in the order and
 // arithmetic the factorization applies them (the right-hand-side branch of qr_warp): reflector k
 // exists when rdiag[k] != 0 (the column norm was nonzero) and acts when v[0] != 0.
-template <typename T, int G = 32>
+template <typename T, int G = 32, class A = QrArith<T>>
 __device__ void qr_apply_warp(const T* a, int m, int n, long long lda,
-                              const typename QrArith<T>::R* rdiag, T* b, long long ldb, int nb,
+                              const typename A::R* rdiag, T* b, long long ldb, int nb,
                               T* coefs) {
-  using A = QrArith<T>;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int k = 0; k < n; ++k) {
@@ -393,10 +456,9 @@ __device__ void qr_apply_warp(const T* a, int m, int n, long long lda,
 
 // R x = y for the first n entries of every right-hand side (Blas.SolveTriangular Upper/NoTrans,
 // MatFlat/Blas.SolveTriangular.cs:191-199, against QrUpperTriangularFactor's R).
-template <typename T, int G = 32>
+template <typename T, int G = 32, class A = QrArith<T>>
 __device__ void qr_rsolve_warp(const T* a, int n, long long lda, const T* rdiag, T* b,
                                long long ldb, int nb) {
-  using A = QrArith<T>;
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   for (int i = n - 1; i >= 0; --i) {
@@ -458,9 +520,12 @@ int qr_smem_coefs(int group) { return group == 32 ? QR_SMEM_COEFS : QR_GROUP_COE
 // queue (a warp takes 32/G consecutive ones, which the plan orders to have equal n).
 // Sixteen warps per SM are needed to hide the latency of the trailing-matrix streams: the
 // register budget is capped accordingly (128 per thread).
-template <typename T, int WARPS, int G, bool SOLVE = false>
+// FMA (double only): the FMA form's arithmetic (QrArithFma) for the factorization, the
+// reflector applications of solve-only calls and the triangular solve.
+template <typename T, int WARPS, int G, bool SOLVE = false, bool FMA = false>
 __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
     qr_batched_kernel(QrBatchArgs<T> p) {
+  using A = std::conditional_t<FMA, QrArithFma, QrArith<T>>;
   constexpr int GPW = 32 / G;
   constexpr int CO = G == 32 ? QR_SMEM_COEFS : QR_GROUP_COEFS;
   __shared__ T sm[WARPS][GPW][CO];
@@ -486,12 +551,12 @@ __global__ void __launch_bounds__(WARPS * 32, (16 / WARPS) > 0 ? 16 / WARPS : 1)
       T* coefs = (need <= CO) ? &sm[warp][g][0]
                               : p.gscratch + (gw * GPW + g) * p.gscratch_stride;
       if constexpr (SOLVE)
-        qr_apply_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+        qr_apply_warp<T, G, A>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       else if (p.fused)
-        qr_warp_fused<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+        qr_warp_fused<T, G, A>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
       else
-        qr_warp<T, G>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
-      if (p.nrhs > 0) qr_rsolve_warp<T, G>(a, n, lda, rd, b, m, p.nrhs);
+        qr_warp<T, G, A>(a, m, n, lda, rd, b, m, p.nrhs, coefs);
+      if (p.nrhs > 0) qr_rsolve_warp<T, G, A>(a, n, lda, rd, b, m, p.nrhs);
     }
     __syncwarp();
   }
@@ -611,22 +676,22 @@ __global__ void qr_r_single_kernel(const T* a, int n, int lda, T* r, int ldr,
   r[(long long)i * ldr + row] = v;
 }
 
-template <typename T, bool SOLVE>
+template <typename T, bool SOLVE, bool FMA>
 static cudaError_t launch_qr_batched_s(const QrBatchArgs<T>& args, int ctas, int warps,
                                        cudaStream_t s) {
   if (args.group == 16) {
-    qr_batched_kernel<T, 4, 16, SOLVE><<<ctas, 128, 0, s>>>(args);
+    qr_batched_kernel<T, 4, 16, SOLVE, FMA><<<ctas, 128, 0, s>>>(args);
   } else if (args.group == 8) {
-    qr_batched_kernel<T, 4, 8, SOLVE><<<ctas, 128, 0, s>>>(args);
+    qr_batched_kernel<T, 4, 8, SOLVE, FMA><<<ctas, 128, 0, s>>>(args);
   } else if (args.group == 4) {
-    qr_batched_kernel<T, 4, 4, SOLVE><<<ctas, 128, 0, s>>>(args);
+    qr_batched_kernel<T, 4, 4, SOLVE, FMA><<<ctas, 128, 0, s>>>(args);
   } else {
     switch (warps) {
-      case 1: qr_batched_kernel<T, 1, 32, SOLVE><<<ctas, 32, 0, s>>>(args); break;
-      case 2: qr_batched_kernel<T, 2, 32, SOLVE><<<ctas, 64, 0, s>>>(args); break;
-      case 4: qr_batched_kernel<T, 4, 32, SOLVE><<<ctas, 128, 0, s>>>(args); break;
-      case 8: qr_batched_kernel<T, 8, 32, SOLVE><<<ctas, 256, 0, s>>>(args); break;
-      case 16: qr_batched_kernel<T, 16, 32, SOLVE><<<ctas, 512, 0, s>>>(args); break;
+      case 1: qr_batched_kernel<T, 1, 32, SOLVE, FMA><<<ctas, 32, 0, s>>>(args); break;
+      case 2: qr_batched_kernel<T, 2, 32, SOLVE, FMA><<<ctas, 64, 0, s>>>(args); break;
+      case 4: qr_batched_kernel<T, 4, 32, SOLVE, FMA><<<ctas, 128, 0, s>>>(args); break;
+      case 8: qr_batched_kernel<T, 8, 32, SOLVE, FMA><<<ctas, 256, 0, s>>>(args); break;
+      case 16: qr_batched_kernel<T, 16, 32, SOLVE, FMA><<<ctas, 512, 0, s>>>(args); break;
       default: return cudaErrorInvalidValue;
     }
   }
@@ -635,8 +700,13 @@ static cudaError_t launch_qr_batched_s(const QrBatchArgs<T>& args, int ctas, int
 
 template <typename T>
 cudaError_t launch_qr_batched(const QrBatchArgs<T>& args, int ctas, int warps, cudaStream_t s) {
-  return args.solve_only ? launch_qr_batched_s<T, true>(args, ctas, warps, s)
-                         : launch_qr_batched_s<T, false>(args, ctas, warps, s);
+  if constexpr (std::is_same<T, double>::value) {
+    if (args.fma)
+      return args.solve_only ? launch_qr_batched_s<T, true, true>(args, ctas, warps, s)
+                             : launch_qr_batched_s<T, false, true>(args, ctas, warps, s);
+  }
+  return args.solve_only ? launch_qr_batched_s<T, true, false>(args, ctas, warps, s)
+                         : launch_qr_batched_s<T, false, false>(args, ctas, warps, s);
 }
 
 template <typename T>

@@ -2533,6 +2533,7 @@ int qr_autotune(mfg_plan* plan, int* config) {
   tp->qd.rdiag = rd;
   tp->qd.solve_only = 0;
   tp->qr_float = 0;
+  tp->qd.fma = plan->qd.fma;
   std::vector<std::array<int, 5>> cands;
   for (int g : {4, 8, 16, 32})
     for (int wps : {8, 12, 16, 24}) cands.push_back({4, wps, g, 0, 0});
@@ -2591,11 +2592,13 @@ MFG_API int mfg_plan_set_form(mfg_plan* plan, int form) {
   DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
-  if (plan->kind != mfg_plan::POTRF)
-    return fail(ctx, MFG_ERR_UNSUPPORTED, "set_form: potrf plans only");
+  if (plan->kind != mfg_plan::POTRF && plan->kind != mfg_plan::GEQRF)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "set_form: potrf and geqrf plans only");
   if (form != MFG_FORM_EXACT && form != MFG_FORM_FMA)
     return fail(ctx, -2, "form must be MFG_FORM_EXACT or MFG_FORM_FMA");
+  // Cholesky: every overload's factorization and solves; QR: the double overload.
   plan->args.fma = form == MFG_FORM_FMA ? 1 : 0;
+  plan->qd.fma = plan->args.fma;
   pipe_release(plan);  // host-buffer chunk plans are rebuilt with the form on next use
   if (plan->exec) {
     cudaGraphExecDestroy(plan->exec);
@@ -3123,6 +3126,12 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
     if (p->kind == mfg_plan::GEVD) {
       rc = plan_set_elem(sub, pipe_elem(op));
       if (rc != MFG_OK) return rc;
+    }
+    if (op == OP_GEQRF_D || op == OP_GEQRF_S) {
+      // The parent's (possibly autotuned) lanes per matrix and warps per SM, and its form.
+      rc = qr_reshape(sub, p->qd.group, std::max(1, p->ctas * p->warps / ctx->sm_count));
+      if (rc != MFG_OK) return rc;
+      sub->qd.fma = p->qd.fma;
     }
     if (op == OP_GEQRF_Z) {
       rc = zqr_prepare(sub);
