@@ -816,6 +816,99 @@ def lu_parity(d, a_out, b_out, piv_out, sign_out, info_out):
             "zero_pivot_matrices": int((info_out != 0).sum())}
 
 
+def lu_berr(torch, d, a_in, a_out, piv_out, b_in, b_out):
+    """Normwise backward errors of a batch of LU factors and solutions on the device (torch
+    FP64, one batched product per order): max over the matrices with finite factors of
+    ||PA - LU||_1 / (||A||_1 n) and of ||b - Ax||_1 / ((||A||_1 ||x||_1 + ||b||_1) n), with
+    MatFlat's permutation vector (row i of PA is row piv[i] of A)."""
+    n = d["n"]
+    a_off = torch.from_numpy(d["a_off"]).cuda()
+    p_off = torch.from_numpy(d["piv_off"]).cuda()
+    b_off = torch.from_numpy(d["b_off"]).cuda()
+    worst_f = worst_x = 0.0
+    for nv in np.unique(n):
+        nn = int(nv)
+        idx = torch.from_numpy(np.nonzero(n == nv)[0]).cuda()
+        ca = a_off[idx][:, None] + torch.arange(nn * nn, device="cuda")[None, :]
+        A = a_in[ca].view(-1, nn, nn).transpose(1, 2)
+        F = a_out[ca].view(-1, nn, nn).transpose(1, 2)
+        P = piv_out[p_off[idx][:, None] + torch.arange(nn, device="cuda")[None, :]].long()
+        L = torch.tril(F, -1) + torch.eye(nn, dtype=F.dtype, device="cuda")
+        U = torch.triu(F)
+        PA = torch.gather(A, 1, P[:, :, None].expand(-1, -1, nn))
+        na = A.abs().sum(1).amax(1)
+        ok = torch.isfinite(F).all(2).all(1)
+        ef = (PA - L @ U).abs().sum(1).amax(1) / na
+        worst_f = max(worst_f, float((ef[ok] / nn).max().item()) if ok.any() else 0.0)
+        for r in range(d["nrhs"]):
+            cb = b_off[idx][:, None] + r * nn + torch.arange(nn, device="cuda")[None, :]
+            x, bb = b_out[cb], b_in[cb]
+            res = (bb - (A @ x[:, :, None])[:, :, 0]).abs().sum(1)
+            ex = res / (na * x.abs().sum(1) + bb.abs().sum(1))
+            worst_x = max(worst_x, float((ex[ok] / nn).max().item()) if ok.any() else 0.0)
+    return worst_f, worst_x
+
+
+def measure_lu_fma(torch, mf, d, rank, steps, warmup, fp64_peak, flops):
+    """The LU's FMA form on the headline batch (mfg_plan_set_form): fused multiply-adds with
+    MatFlat's pivots kept by a screen and an exact redo of the matrices it rejects.  Timed like the
+    main step (L2 flushed, device-to-device restore, one plan execution, CUDA events on the plan's
+    stream); then the pivots and signs of the last timed step against the oracle over the whole
+    batch, and the backward errors of the factors and solutions."""
+    ctx = mf.context()
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    count = len(d["n"])
+    a0 = torch.from_numpy(d["a"]).cuda()
+    b0 = torch.from_numpy(d["b"]).cuda()
+    a = torch.empty_like(a0)
+    b = torch.empty_like(b0)
+    piv = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
+    sign = torch.zeros(count, dtype=torch.int32, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    plan = mf.LuBatch(d["n"], d["a_off"], d["piv_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+    plan.set_form("fma")
+    tuned = plan.autotune()
+    ks, ke = [], []
+    with torch.cuda.stream(stream):
+        for it in range(warmup + steps):
+            flush.zero_()
+            a.copy_(a0)
+            b.copy_(b0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(a, piv, b, sign, info)
+            e1.record(stream)
+            if it >= warmup:
+                ks.append(e0)
+                ke.append(e1)
+        stream.synchronize()
+    kms = statistics.median(s0.elapsed_time(s1) for s0, s1 in zip(ks, ke))
+    fallbacks = plan.form_fallbacks()
+    par = lu_parity(d, a.cpu().numpy(), b.cpu().numpy(), piv.cpu().numpy(), sign.cpu().numpy(),
+                    info.cpu().numpy())
+    bf, bx = lu_berr(torch, d, a0, a, piv, b0, b)
+    tf = flops / (kms / 1e3) / 1e12
+    return {"value": count / (kms / 1e3), "unit": "matrices/s", "kernel_ms": kms,
+            "roofline": {"bound": "fp64", "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": tf / fp64_peak},
+            "launch_shape": dict(zip(["warps_per_cta", "warps_per_sm", "lanes_table",
+                                      "mul_mode", "dot_pairs_per_block"], tuned)),
+            "form": "fused multiply-add dots, reciprocal column scaling, MatFlat's pivot rule "
+                    "with a screen (runner-up within ~1.5e-8 of the pivot, ties, zero or "
+                    "non-finite candidates) that redoes rejected matrices in MatFlat's arithmetic; "
+                    "not MatFlat's bits",
+            "fallbacks": fallbacks,
+            "pivots_identical_to_oracle": par["pivots_identical"],
+            "signs_identical_to_oracle": par["signs_identical"],
+            "pivot_mismatches": par["mismatches"]["pivots"],
+            "factor_berr_over_n_max": bf, "solve_berr_over_n_max": bx, "bound_over_n": 1e-13,
+            "within_bound": bf <= 1e-13 and bx <= 1e-13,
+            "checker": par["checker"] + "; torch FP64 batched products for the backward errors"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -841,6 +934,10 @@ def main():
                     help="lu: skip the oracle check of the whole timed batch")
     ap.add_argument("--no-mixed", action="store_true",
                     help="lu: skip the mixed-precision sub-measurement")
+    ap.add_argument("--no-lu-fma", action="store_true",
+                    help="lu: skip the record of the LU's FMA form in the default line")
+    ap.add_argument("--fixed-n", type=int, default=None,
+                    help="lu, inv, chol100k: every matrix of this order (profiling aid)")
     ap.add_argument("--no-cholesky", action="store_true",
                     help="lu: skip the Cholesky record (100,000 SPD matrices, FMA and exact "
                          "forms) of the default line")
@@ -854,6 +951,10 @@ def main():
     cfg_name = args.config
     if args.count:
         CONFIGS[cfg_name]["count"] = args.count
+    if args.fixed_n:
+        # Profiling aid: every matrix of the LU / LuInverse batch has this order.
+        CONFIGS[cfg_name]["nmin"] = CONFIGS[cfg_name]["nmax"] = args.fixed_n
+        CONFIGS[cfg_name]["workload"] += " [all n = %d]" % args.fixed_n
     if args.impl == "reference":
         run_reference(args, cfg_name)
         return
@@ -954,6 +1055,7 @@ def main():
             kernel_key = "getri_batched_kernel"
         elif cfg_name == "lu":
             plan = mf.LuBatch(d["n"], d["a_off"], d["piv_off"], nrhs=d["nrhs"], b_off=d["b_off"])
+            plan.set_form(args.form)
             if not args.no_autotune:
                 tuned = plan.autotune()
             piv = torch.zeros(d["piv_total"], dtype=torch.int32, device="cuda")
@@ -1220,6 +1322,9 @@ def main():
     cholesky = None
     if cfg_name == "lu" and not args.no_cholesky:
         cholesky = measure_cholesky(torch, mf, rank, 5, 3, fp64_peak)
+    lu_fma = None
+    if cfg_name == "lu" and args.form == "exact" and not args.no_lu_fma:
+        lu_fma = measure_lu_fma(torch, mf, d, rank, 5, 3, fp64_peak, flops)
 
     if rank == 0:
         line = {
@@ -1257,6 +1362,8 @@ def main():
             line["mixed"] = mixed
         if cholesky is not None:
             line["cholesky"] = cholesky
+        if lu_fma is not None:
+            line["lu_fma"] = lu_fma
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

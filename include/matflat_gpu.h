@@ -485,10 +485,24 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
  * (double overload): MatFlat's Householder algorithm and storage (no sign choice,
  * rdiag = -norm, the same degenerate-reflector rules) with fused multiply-add dots, norms and
  * updates and the column scaled by the reciprocal of its norm: backward-stable factors and
- * least-squares solutions instead of MatFlat's bits.  MFG_ERR_UNSUPPORTED for other plans.
+ * least-squares solutions instead of MatFlat's bits.  MFG_FORM_FMA, LU (double overload, the
+ * size-bucketed schedule; orders above 128 in CTA-per-matrix batches stay exact): MatFlat's pivot
+ * rule and Crout schedule with fused multiply-add dots and reciprocal column scaling, and a
+ * screen at every column that keeps MatFlat's pivots: a matrix whose pivot could depend on
+ * rounding (the runner-up within about 1.5e-8 of the pivot, ties, a zero pivot, NaN or infinite
+ * candidates) is redone in MatFlat's arithmetic (mfg_plan_form_fallbacks counts them); factors
+ * satisfy |PA - LU| <= gamma_n |L| |U|, solutions come from fused multiply-add column sweeps.
+ * The screen is not a proof that every pivot is MatFlat's.  MFG_ERR_UNSUPPORTED for other
+ * plans.
  * Drops the plan's cached graph. */
 enum mfg_form { MFG_FORM_EXACT = 0, MFG_FORM_FMA = 1 };
 MFG_API int mfg_plan_set_form(mfg_plan* plan, int form);
+
+/* Matrices of a getrf plan's last execution (device or host-buffer call) that the FMA form
+ * redid in MatFlat's arithmetic because their pivot choice did not pass its screen (no
+ * counterpart in the reference).  Synchronizes with the plan's work; 0 for the exact form and
+ * for other plans. */
+MFG_API int mfg_plan_form_fallbacks(mfg_plan* plan, long long* count);
 
 MFG_API int mfg_plan_destroy(mfg_plan* plan);
 

@@ -64,6 +64,7 @@ _SIGS = {
     "mfg_dpotrf_batched": (_I, [_vp, _vp, _vp, _vp]),
     "mfg_plan_autotune": (_I, [_vp, _c_int_p]),
     "mfg_plan_set_form": (_I, [_vp, ctypes.c_int]),
+    "mfg_plan_form_fallbacks": (_I, [_vp, _vp]),
     **{"mfg_%sgemv_strided_batched" % _p: (_I, [_vp, _I, _I, _I, _vp, _I, ctypes.c_int64, _vp,
                                                  _I, ctypes.c_int64, _vp, _I, ctypes.c_int64, _I])
        for _p in "sz"},
@@ -525,6 +526,20 @@ class LuBatch(_Batch):
         super().__init__(ctx, h)
         self.count = len(self._n)
         self.nrhs = nrhs
+
+    def set_form(self, form):
+        """Arithmetic form of the double factorization: "exact" (MatFlat's bits, the default) or
+        "fma" (fused multiply-adds with MatFlat's pivots kept by a screen and an exact redo of
+        the matrices it rejects; backward-stable factors, not MatFlat's bits)."""
+        code = FORMS[form]
+        self.ctx.check(self.ctx.lib.mfg_plan_set_form(self.h, code), "mfg_plan_set_form")
+
+    def form_fallbacks(self):
+        """Matrices of the last execution that the FMA form redid in MatFlat's arithmetic."""
+        v = ctypes.c_longlong(0)
+        self.ctx.check(self.ctx.lib.mfg_plan_form_fallbacks(self.h, ctypes.byref(v)),
+                       "mfg_plan_form_fallbacks")
+        return v.value
 
     def run(self, a, piv, b, sign, info, dtype=None):
         """Factor (+ solve) device buffers.  The element type follows a's dtype (float64,

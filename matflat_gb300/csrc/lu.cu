@@ -1,22 +1,9 @@
-// LU with partial pivoting in MatFlat's arithmetic (Factorization.LuCore,
-// MatFlat/Factorization.Lu.cs:296-350), plus the fused solve used by the batched solver.
-//
-// MatFlat is a left-looking "dot product" LU: for column j it computes every entry as
-//     v(i,j) = A'(i,j) - Dot(min(i,j), L(i,0:), U(0:,j))         (Lu.cs:315-320)
-// with Internals.Dot's pairwise tree, picks the pivot by a strict ">" scan over |v|
-// (Lu.cs:323-330), swaps whole rows (Lu.cs:332-337) and divides the sub-diagonal by the pivot
-// (Lu.cs:340-344).  Every entry's value depends only on its own dot, so the entries can be
-// computed in any order that respects data dependencies.  This kernel uses the Crout order:
-// step k finishes row k of U (U(k,j), j > k: dots of length k) and column k+1 of L (dots of
-// length k+1), each dot evaluated with exactly MatFlat's tree, so factors and pivots are
-// bit-identical.  To keep the 32 lanes busy, the long prefix of every column-(k+1) dot (all pairs
-// but the last) runs in the same round as the row-k dots; the last pair, which needs L(:,k) and
-// U(k,k+1), is added afterwards:
-//     Dot(k+1, x, y) = Dot(k-1, x, y) + (x[k-1]*y[k-1] + x[k]*y[k])      (k >= 1)
-//     Dot(1, x, y)   = x[0]*y[0]
-//
-// One warp owns one matrix; the matrix stays in its global buffer (L1/L2 resident while it is
-// being factored): on GB300 the FP64 pipe, not memory, bounds this kernel.
+// Batched LU + solve kernels in MatFlat's arithmetic (Factorization.LuCore,
+// MatFlat/Factorization.Lu.cs:296-350; the warp-level routines are in mf_lu.cuh): the
+// size-bucketed task kernels (G lanes per matrix, persistent, one launch per bucket), the
+// one-matrix-per-warp and float / Complex kernels, the CTA-per-matrix kernel for large orders,
+// the resident form (one matrix per CTA in shared memory), the single-matrix drop-ins and the
+// allocation-free entry point.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -25,177 +12,9 @@
 #include "mf_kernels.h"
 #include "mf_scalar.cuh"
 #include "mf_solve.cuh"
+#include "mf_lu.cuh"
 
 namespace mfg {
-
-// Finishes column c (rows [c, m)) once its dot sums are final, then pivots and scales it.
-//   mode 0: column 0 (no dot: v = A - 0.0 = A, left as is)
-//   mode 1: column 1 (sum = L(i,0) * U(0,1))
-//   mode 2: column c >= 2 (sum = scol[i] + (L(i,c-2)*U(c-2,c) + L(i,c-1)*U(c-1,c)))
-// Tr supplies the element type's arithmetic (double, float or Complex overload).
-// G: lanes per matrix (8, 16 or 32): the matrix is worked on by a group of G consecutive lanes
-// of the warp, the other groups of the warp work on other matrices of the same order.
-template <class Tr, int G = 32, bool IDIV = false>
-__device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n, long long lda,
-                                                 int c, int mode,
-                                                 const typename Tr::Acc* scol, int* piv,
-                                                 int& sign, int& info, int* pivot = nullptr) {
-  using T = typename Tr::T;
-  using Acc = typename Tr::Acc;
-  const int lane = group_lane<G>();
-  const unsigned gm = group_mask<G>();
-  T* cc = a + (long long)c * lda;
-  unsigned long long bkey = 0ull;
-  int bidx = INT_MAX;
-  bool first_nan = false;
-  if (mode == 0) {
-    for (int i = c + lane; i < m; i += G) {
-      const T v = cc[i];
-      const unsigned long long key = Tr::key(v);
-      if (key > bkey) {
-        bkey = key;
-        bidx = i;
-      }
-      if (i == c) first_nan = Tr::nan0(v);
-    }
-  } else {
-    const T* l1 = a + (long long)(c - 1) * lda;  // L(:, c-1)
-    const T u1 = cc[c - 1];                       // U(c-1, c)
-    const T* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
-    const T u2 = (mode == 2) ? cc[c - 2] : u1;    // U(c-2, c)
-    for (int i = c + lane; i < m; i += G) {
-      Acc s;
-      if constexpr (IDIV) {
-        // Double with integer-pipe arithmetic: the products on the integer pipes too.
-        s = mode == 1 ? imul_rn(l1[i], u1)
-                      : __dadd_rn(scol[i], __dadd_rn(imul_rn(l2[i], u2), imul_rn(l1[i], u1)));
-      } else if (mode == 1) {
-        s = Tr::prod(l1[i], u1);
-      } else {
-        s = Tr::pair(scol[i], l2[i], u2, l1[i], u1);
-      }
-      const T v = Tr::fin(cc[i], s);
-      cc[i] = v;
-      const unsigned long long key = Tr::key(v);
-      if (key > bkey) {
-        bkey = key;
-        bidx = i;
-      }
-      if (i == c) first_nan = Tr::nan0(v);
-    }
-  }
-  int p = group_argmax<G>(bkey, bidx);
-  // Row c is handled by the group's lane 0; a NaN there can never be displaced by the strict ">"
-  // scan.
-  if (__shfl_sync(gm, first_nan ? 1 : 0, 0, G)) p = c;
-  if (pivot) *pivot = p;
-  __syncwarp(gm);
-  if (p != c && p < m) {
-    for (int col = lane; col < n; col += G) {
-      T* base = a + (long long)col * lda;
-      const T t = base[c];
-      base[c] = base[p];
-      base[p] = t;
-    }
-    if (lane == 0) {
-      const int t = piv[c];
-      piv[c] = piv[p];
-      piv[p] = t;
-    }
-    sign = -sign;
-  }
-  __syncwarp(gm);
-  const T diag = cc[c];
-  if (Tr::nz(diag)) {
-    if constexpr (IDIV) {
-      // Quotients on the integer pipes (the same bits as the FP64 division): the reciprocal is
-      // formed once per column.
-      idiv_column(cc, c + 1 + lane, m, G, diag);
-    } else {
-      for (int i = c + 1 + lane; i < m; i += G) cc[i] = Tr::div(cc[i], diag);
-    }
-  } else if (info == 0) {
-    info = c + 1;
-  }
-  __syncwarp(gm);
-}
-
-// Factors the m-by-n matrix a (leading dimension lda) in place; piv receives the permutation
-// vector (m entries).  scol: m values of per-warp scratch (Tr::Acc).  Returns Lu's sign in `sign`
-// and in `info` the first zero pivot (k+1), or 0.
-//
-// EARLY (square matrices; scol2: m more values): the lanes left idle in the last round of a step
-// compute prefixes of the column after next.  Column c's prefix Dot(c-2, L(i,:), U(:,c)) reads
-// U rows 0..c-3 only, which are final after step c-3, so it may run at step c-2 instead of c-1;
-// the values are the same (the same dot, evaluated once).  At step k the rows [m - e, m) (e <= the
-// idle lanes of the step's last round, rows >= k+2) get column k+2's prefix early; at step k+1
-// column k+2's regular items cover the other rows, plus the row swapped into the early range by
-// column k+1's pivot (its early value belonged to the row that moved out).  Columns alternate
-// between the two prefix arrays (scol: even columns, scol2: odd).
-
-template <class Tr, int IM, int DB = DOT_BLOCK, int G = 32, bool EARLY = false>
-__device__ void lu_warp(typename Tr::T* a, int m, int n, long long lda, int* piv,
-                        typename Tr::Acc* scol, int& sign, int& info,
-                        typename Tr::Acc* scol2 = nullptr) {
-  using T = typename Tr::T;
-  using Acc = typename Tr::Acc;
-  const int lane = group_lane<G>();
-  const unsigned gm = group_mask<G>();
-  for (int i = lane; i < m; i += G) piv[i] = i;
-  sign = 1;
-  info = 0;
-  __syncwarp(gm);
-  const int K = m < n ? m : n;
-  constexpr bool IDIV = MFG_IDIV && IM != 0 && std::is_same<Tr, DTraits>::value;
-  lu_finish_column<Tr, G, IDIV>(a, m, n, lda, 0, 0, scol, piv, sign, info);
-  int e_prev = 0;        // rows [m - e_prev, m) got column k1's prefix at the previous step
-  int p_prev = INT_MAX;  // the pivot row of column k (chosen at the end of the previous step)
-  for (int k = 0; k < K; ++k) {
-    const int k1 = k + 1;
-    const int R = n - k1;                     // row-k dots: U(k, j), j in [k1, n)
-    const T* rowk = a + k;                    // L(k, t) = rowk[t*lda]
-    const T* colk1 = a + (long long)k1 * lda;
-    Acc* pre1 = (EARLY && (k1 & 1)) ? scol2 : scol;   // column k1's prefixes
-    // Regular prefix items of column k1: rows [k1, m - e_prev), plus the displaced row.
-    const bool has_col = k1 < K && k >= 1;
-    const int nreg0 = has_col ? max(0, m - e_prev - k1) : 0;
-    const int disp = (has_col && EARLY && e_prev > 0 && p_prev >= m - e_prev && p_prev < m) ? 1
-                                                                                            : 0;
-    const int C = nreg0 + disp;
-    int E = 0;
-    if constexpr (EARLY) {
-      if (k >= 2 && k + 2 < K) E = min(m - (k + 2), (G - (R + C) % G) % G);
-    }
-    Acc* pre2 = (k & 1) ? scol2 : scol;               // column k+2's prefixes (EARLY)
-    const T* colk2 = a + (long long)(k + 2) * lda;
-    for (int d = lane; d < R + C + E; d += G) {
-      // One dot per item (a single call site keeps the register count of one dot loop): row
-      // items U(k, idx) (length k), column k1's prefixes (k-1), column k+2's early prefixes (k).
-      const bool isrow = d < R;
-      const bool isreg = !isrow && d < R + C;
-      const int c = d - R;
-      const int idx = isrow ? k1 + d : isreg ? (c < nreg0 ? k1 + c : p_prev) : m - E + (c - C);
-      const T* x = isrow ? rowk : a + idx;
-      const T* y = isrow ? a + (long long)idx * lda : isreg ? colk1 : colk2;
-      const int len = isreg ? k - 1 : k;
-      const Acc s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
-      if (isrow) {
-        T* dst = a + (long long)idx * lda + k;
-        *dst = Tr::fin(*dst, s);
-      } else {
-        (isreg ? pre1 : pre2)[idx] = s;
-      }
-    }
-    __syncwarp(gm);
-    int pk = INT_MAX;
-    if (k1 < K)
-      lu_finish_column<Tr, G, IDIV>(a, m, n, lda, k1, k1 == 1 ? 1 : 2, pre1, piv, sign, info,
-                                    &pk);
-    e_prev = E;
-    p_prev = pk;
-  }
-  // MatFlat also visits columns j >= m when n > m, but nothing changes there (no pivot rows).
-}
 
 // ---------------------------------------------------------------------------------------------
 // The same schedule with a whole CTA of W warps on one matrix, for large orders when there are too
@@ -397,36 +216,6 @@ __device__ void lu_cta_early(double* a, int n, long long lda, int* piv, double* 
   }
 }
 
-// Solves A x = b for nr right-hand sides from the factors of one square matrix:
-// b' = P b (b'[i] = b[piv[i]]), then the unit-lower solve (dot form, LuInverse idiom), then the
-// upper solve (column sweep).  b: column-major, leading dimension ldb, overwritten with x.
-// S: the solve arithmetic of the element type (DSolve, SSolve or ZSolve<false>).
-template <class S = DSolve, int G = 32>
-__device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const int* piv,
-                           typename S::T* b, long long ldb, int nrhs, typename S::T* xs,
-                           typename S::Acc* acc) {
-  const int lane = group_lane<G>();
-  const unsigned gm = group_mask<G>();
-  const int ldx = n | 1;
-  for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
-    const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
-    for (int e = lane; e < nr * n; e += G) {
-      const int r = e / n;
-      const int i = e - r * n;
-      xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + piv[i]];
-    }
-    __syncwarp(gm);
-    warp_solve_dot<G, S>(lu, n, 1, lda, true, xs, ldx, acc, nr);
-    warp_solve_sweep<G, S>(lu, n, lda, 1, xs, ldx, nr);
-    for (int e = lane; e < nr * n; e += G) {
-      const int r = e / n;
-      const int i = e - r * n;
-      b[(long long)(r0 + r) * ldb + i] = xs[r * ldx + i];
-    }
-    __syncwarp(gm);
-  }
-}
-
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 // Per-warp shared memory when the solve is staged in global memory (BatchArgs::gsolve).
 constexpr int SMEM_WARP_DOUBLES_G = SMEM_N + 2;
@@ -528,8 +317,6 @@ __global__ void __launch_bounds__(32) getrf_single_kernel(typename Tr::T* a, int
 // one task at a time and its groups of G lanes each factor (and solve) one matrix of it, in exactly
 // the schedule above.  Small G keeps the lanes busy when a step has few dots; groups of a task
 // share the order, so they follow the same control flow.
-// Per group: the column sums of even and of odd columns (n <= SMEM_N), SMEM_N + 1 apart.
-constexpr int GROUP_SMEM_DOUBLES = 2 * SMEM_N + 2;
 
 template <int IM, int DB, int G>
 __device__ __forceinline__ void getrf_task(const BatchArgs& p, int first, int cnt, double* ws,

@@ -258,6 +258,37 @@ __device__ __forceinline__ double fma_dot(int len, const double* x, long long in
   return __dadd_rn(__dadd_rn(s0, s1), __dadd_rn(s2, s3));
 }
 
+// The same with two chains and blocks of two (fewer registers: for kernels that want warps more
+// than instruction-level parallelism).
+__device__ __forceinline__ double fma_dot2(int len, const double* x, long long incx,
+                                           const double* y, long long incy) {
+  double s0 = 0.0, s1 = 0.0;
+  const int blocks = len >> 1;
+  if (blocks > 0) {
+    double x0 = x[0], x1 = x[incx], y0 = y[0], y1 = y[incy];
+    for (int blk = 0; blk < blocks; ++blk) {
+      const bool more = blk + 1 < blocks;
+      double nx0 = 0.0, nx1 = 0.0, ny0 = 0.0, ny1 = 0.0;
+      if (more) {
+        nx0 = x[2 * incx];
+        nx1 = x[3 * incx];
+        ny0 = y[2 * incy];
+        ny1 = y[3 * incy];
+      }
+      s0 = __fma_rn(x0, y0, s0);
+      s1 = __fma_rn(x1, y1, s1);
+      x += 2 * incx;
+      y += 2 * incy;
+      x0 = nx0;
+      x1 = nx1;
+      y0 = ny0;
+      y1 = ny1;
+    }
+  }
+  if (len & 1) s0 = __fma_rn(x[0], y[0], s0);
+  return __dadd_rn(s0, s1);
+}
+
 // Copies src[k*stride] to dst[k] (shared memory) for k in [k0, k1) with asynchronous 8-byte
 // copies, one element per lane per round (cp.async, completed by stage_wait): a warp stages the
 // next row or column of a factor while it computes with the current one.

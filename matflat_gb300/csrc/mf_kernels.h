@@ -50,8 +50,12 @@ struct BatchArgs {
                              // stays the upper bound the grid was sized for
   int minb;                  // getrf (double, size-bucketed tasks): CTAs per SM of the launch
                              // shape (7 or 8 select variants compiled for that occupancy)
-  int fma;                   // potrf: the FMA form (fused multiply-adds in any order, reciprocal
-                             // scaling): backward-stable factors, not MatFlat's bits
+  int fma;                   // potrf, getrf (double): the FMA form (fused multiply-adds in any
+                             // order, reciprocal scaling): backward-stable factors, not MatFlat's
+                             // bits (getrf keeps MatFlat's pivots, see lu_fma.cu)
+  double* fbackup;           // getrf FMA form: per-warp copies of the matrices being factored,
+  long long fbackup_stride;  // fbackup_stride doubles per warp (32/G groups share it evenly)
+  int* fcount;               // getrf FMA form: matrices redone in MatFlat's arithmetic
   double* gsolve;            // getrf/potrf: per-warp global staging of the solves (GSOLVE_STRIDE
                              // / GSOLVE_STRIDE_C doubles per warp) for the orders whose column
                              // sums fit in shared memory, which then holds only those sums and
@@ -270,6 +274,12 @@ cudaError_t launch_getrf_tasks(const BatchArgs& args, int ctas, int warps, int g
 // slice of warp_scratch_doubles(nmax) per CTA (cudaErrorInvalidValue if it is missing).
 cudaError_t launch_getrf_cta(const BatchArgs& args, int ctas, int nmax, cudaStream_t s);
 int getrf_cta_warps();
+// FMA form of the size-bucketed LU (+ solve) (lu_fma.cu): the same tasks and queue as
+// launch_getrf_tasks; needs args.fbackup (args.fbackup_stride doubles per launched warp, at least
+// (32/g) n^2 for the bucket's largest n) and args.fcount.
+cudaError_t launch_getrf_tasks_fma(const BatchArgs& args, int ctas, int warps, int g,
+                                   cudaStream_t s);
+cudaError_t init_getrf_fma_attributes();
 // Resident form: one matrix per CTA of w warps (2, 4 or 8) over the task list (one matrix per
 // task), the matrix held in smem_bytes of dynamic shared memory when it fits.
 cudaError_t launch_getrf_blk(const BatchArgs& args, int ctas, int w, int smem_bytes,

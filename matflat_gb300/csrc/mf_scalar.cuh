@@ -119,6 +119,30 @@ struct DTraits {
   static __device__ __forceinline__ T div(T a, T d) { return __ddiv_rn(a, d); }
 };
 
+// The FMA form of the double LU (not MatFlat's bits): the same Crout schedule and pivot rule, with
+// every dot as fused multiply-adds (any order; fma_dot's four chains, the last pair fused onto
+// the prefix) and the column scaled by the reciprocal of the pivot.
+struct DTraitsFma {
+  using T = double;
+  using Acc = double;
+  // DB = 1: two chains (fma_dot2), else four (fma_dot).
+  template <int IM, int DB>
+  static __device__ __forceinline__ Acc dot(int len, const T* x, long long incx, const T* y,
+                                            long long incy) {
+    if constexpr (DB == 1) return fma_dot2(len, x, incx, y, incy);
+    return fma_dot(len, x, incx, y, incy);
+  }
+  static __device__ __forceinline__ Acc prod(T x, T y) { return __dmul_rn(x, y); }
+  static __device__ __forceinline__ Acc pair(Acc s, T x0, T y0, T x1, T y1) {
+    return __fma_rn(x1, y1, __fma_rn(x0, y0, s));
+  }
+  static __device__ __forceinline__ T fin(T a, Acc s) { return __dsub_rn(a, s); }
+  static __device__ __forceinline__ unsigned long long key(T v) { return pivot_key(v); }
+  static __device__ __forceinline__ bool nan0(T v) { return is_nan(v); }
+  static __device__ __forceinline__ bool nz(T v) { return nonzero(v); }
+  static __device__ __forceinline__ T div(T a, T d) { return __ddiv_rn(a, d); }
+};
+
 struct STraits {
   using T = float;
   using Acc = double;

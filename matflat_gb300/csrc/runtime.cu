@@ -118,6 +118,9 @@ struct mfg_plan {
   DevBuf meta;      // order | n | lda | a_off | piv_off | b_off | queue
   DevBuf scratch;   // per-warp scratch for n > SMEM_N
   DevBuf gsolve;    // GETRF: per-warp global staging of the solve (BatchArgs::gsolve)
+  DevBuf fbackup;   // GETRF FMA form: per-warp copies of the matrices being factored
+  long long fma_stride = 0;   // GETRF: doubles per warp the FMA form's copies need
+  bool last_host = false;     // the last execution went through the host-buffer pipeline
   BatchArgs args{};
   mfg::QrBatchArgs<double> qd{};
   mfg::QrBatchArgs<float> qs{};
@@ -218,6 +221,7 @@ cudaError_t init_device_attributes(int device) {
   const int slot = device & 63;
   std::call_once(g_attr_once[slot], [slot]() {
     cudaError_t e = mfg::init_getrf_attributes();
+    if (e == cudaSuccess) e = mfg::init_getrf_fma_attributes();
     if (e == cudaSuccess) e = mfg::init_potrf_attributes();
     if (e == cudaSuccess) e = mfg::init_potrf_t_attributes();
     if (e == cudaSuccess) e = mfg::init_getri_attributes();
@@ -361,6 +365,29 @@ int potrf_build_segments(mfg_plan* p, int csel) {
   return MFG_OK;
 }
 
+// The FMA form's per-warp copies of a GETRF plan: fma_stride doubles for every warp its launches
+// can run (waits for the stream when the buffer grows: it may be in use).  The fallback counter
+// is the plan's work-counter slot 8, zeroed with the queues before every launch.
+int fma_backup_reserve(mfg_plan* p) {
+  if (p->kind != mfg_plan::GETRF || !p->args.fma) return MFG_OK;
+  mfg_ctx* ctx = p->ctx;
+  const long long stride = std::max<long long>(p->fma_stride, 32);
+  const size_t bytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+  if (bytes > p->fbackup.bytes) {
+    MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MFG_CUDA(ctx, p->fbackup.reserve(bytes));
+  }
+  p->args.fbackup = (double*)p->fbackup.ptr;
+  p->args.fbackup_stride = stride;
+  p->args.fcount = p->args.queue + 8;
+  return MFG_OK;
+}
+
+// Sets a plan's arithmetic form: Cholesky (every overload's kernel that has one) and QR (double)
+// take the flag; a GETRF plan in the FMA form also needs size-bucketed tasks (the one-matrix-per-
+// warp queue has no FMA kernel) and its copies.
+int plan_set_fma(mfg_plan* p, int on);
+
 // Builds the tasks of a GETRF plan for table gsel: the matrices sorted by order, every run of one
 // order cut into tasks of 32/G matrices, the tasks grouped by G, and inside each group put in
 // "snake" order (largest, smallest, second largest, ...) so that the matrices in flight average
@@ -403,6 +430,18 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   for (const Task& t : segs[3]) p->cta_nmax = std::max(p->cta_nmax, p->hn[idx[t.first]]);
   p->blk_nmax = 0;
   for (const Task& t : segs[4]) p->blk_nmax = std::max(p->blk_nmax, p->hn[idx[t.first]]);
+  // The FMA form's copies: per warp, 32/G matrices of the bucket's largest order.
+  p->fma_stride = 0;
+  for (int sg = 0; sg < 3; sg++) {
+    long long nm = 0;
+    for (const Task& t : segs[sg]) nm = std::max<long long>(nm, p->hn[idx[t.first]]);
+    p->fma_stride = std::max(p->fma_stride, (1LL << sg) * nm * nm);   // segment sg: 32 >> sg lanes
+  }
+  p->fma_stride = (p->fma_stride + 31) / 32 * 32;
+  if (p->args.fma) {
+    const int rc = fma_backup_reserve(p);
+    if (rc != MFG_OK) return rc;
+  }
   std::vector<int> order, first, gc;
   order.reserve(count);
   for (int sg = 0; sg < 5; sg++) {
@@ -494,6 +533,24 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
     cudaGraphExecDestroy(p->exec);
     p->exec = nullptr;
   }
+  return fma_backup_reserve(p);
+}
+
+int plan_set_fma(mfg_plan* p, int on) {
+  p->args.fma = on ? 1 : 0;
+  p->qd.fma = p->args.fma;
+  if (p->kind == mfg_plan::GETRF && on) {
+    if (p->gsel < 0) {
+      const int rc = getrf_build_tasks(p, 0);
+      if (rc != MFG_OK) return rc;
+    }
+    const int rc = fma_backup_reserve(p);
+    if (rc != MFG_OK) return rc;
+  }
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
   return MFG_OK;
 }
 
@@ -542,7 +599,7 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
   const bool tasks = p->kind == mfg_plan::GETRF && p->elem == 0 && p->gsel >= 0 &&
                      !p->args.dcount && (p->nrhs == 0 || p->args.gsolve != nullptr);
   const bool csegs = p->kind == mfg_plan::POTRF && p->elem == 0 && p->csel > 0;
-  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 6 : 1) * sizeof(int), s);
+  cudaError_t e = cudaMemsetAsync(queue, 0, (tasks || csegs ? 9 : 1) * sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(queue)");
   if (p->count == 0) return MFG_OK;
   if (tasks) {
@@ -572,7 +629,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
         const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
         const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));
         a.minb = p->ctas / std::max(1, ctx->sm_count);
-        e = mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
+        e = p->args.fma ? mfg::launch_getrf_tasks_fma(a, ctas, p->warps, 32 >> sg, s)
+                        : mfg::launch_getrf_tasks(a, ctas, p->warps, 32 >> sg, s);
       }
       if (e != cudaSuccess) return cuda_fail(ctx, e, "batched LU launch");
     }
@@ -2592,17 +2650,33 @@ MFG_API int mfg_plan_set_form(mfg_plan* plan, int form) {
   DeviceScope device_scope_(plan ? plan->ctx : nullptr);
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
-  if (plan->kind != mfg_plan::POTRF && plan->kind != mfg_plan::GEQRF)
-    return fail(ctx, MFG_ERR_UNSUPPORTED, "set_form: potrf and geqrf plans only");
+  if (plan->kind != mfg_plan::POTRF && plan->kind != mfg_plan::GEQRF &&
+      plan->kind != mfg_plan::GETRF)
+    return fail(ctx, MFG_ERR_UNSUPPORTED, "set_form: getrf, potrf and geqrf plans only");
   if (form != MFG_FORM_EXACT && form != MFG_FORM_FMA)
     return fail(ctx, -2, "form must be MFG_FORM_EXACT or MFG_FORM_FMA");
-  // Cholesky: every overload's factorization and solves; QR: the double overload.
-  plan->args.fma = form == MFG_FORM_FMA ? 1 : 0;
-  plan->qd.fma = plan->args.fma;
   pipe_release(plan);  // host-buffer chunk plans are rebuilt with the form on next use
-  if (plan->exec) {
-    cudaGraphExecDestroy(plan->exec);
-    plan->exec = nullptr;
+  return plan_set_fma(plan, form == MFG_FORM_FMA ? 1 : 0);
+}
+
+MFG_API int mfg_plan_form_fallbacks(mfg_plan* plan, long long* count) {
+  DeviceScope device_scope_(plan ? plan->ctx : nullptr);
+  if (!plan) return -1;
+  mfg_ctx* ctx = plan->ctx;
+  if (!count) return fail(ctx, -2, "count is null");
+  *count = 0;
+  if (plan->kind != mfg_plan::GETRF || plan->count == 0) return MFG_OK;
+  // Host-buffer calls return when their streams are done; device calls run on the context's.
+  MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<mfg_plan*> plans;
+  if (plan->last_host)
+    plans = plan->pipe.chunk;
+  else
+    plans.push_back(plan);
+  for (mfg_plan* q : plans) {
+    int v = 0;
+    MFG_CUDA(ctx, cudaMemcpy(&v, q->args.queue + 8, sizeof(int), cudaMemcpyDeviceToHost));
+    *count += v;
   }
   return MFG_OK;
 }
@@ -2660,7 +2734,13 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   tp->args.sign = plan->kind == mfg_plan::GETRF ? sign : nullptr;
   tp->args.info = info;
   tp->args.solve_only = 0;
-  tp->args.fma = plan->args.fma;
+  if (plan->args.fma) {
+    rc = plan_set_fma(tp, 1);
+    if (rc != MFG_OK) {
+      mfg_plan_destroy(tp);
+      return rc;
+    }
+  }
   std::vector<std::array<int, 5>> cands;
   if (plan->kind == mfg_plan::GETRF) {
     // Slot 2 is the lanes-per-matrix table of the size buckets (lu_lanes; -1: one matrix per
@@ -2670,11 +2750,20 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
     // Measured on the 100,000-matrix batch (n 8..128): 16 lanes per matrix at n = 128 is slower
     // than 32 (two matrices per warp double the footprint in flight), 8 lanes pays off at small
     // orders; the tables are tried at 20-28 warps per SM, where they are fastest.
-    for (int gsel : {0, 2, 4})
-      for (int wps : {20, 24, 28, 32}) cands.push_back({4, wps, gsel, 0, 2});
-    cands.push_back({4, 24, 1, 0, 2});
-    cands.push_back({4, 24, -1, 0, 2});
-    cands.push_back({4, 20, -1, 0, 4});
+    if (plan->args.fma) {
+      // The FMA form (no integer-pipe products) is fastest with fewer warps in flight and
+      // two-chain dots (slot 4 = 1): 65.5 ms at 16 warps/SM against 70.7 with four chains and
+      // 82.5 at 28 warps/SM on the 100,000-matrix batch.
+      for (int gsel : {0, 4})
+        for (int wps : {8, 12, 16, 20})
+          for (int db : {1, 2}) cands.push_back({4, wps, gsel, 0, db});
+    } else {
+      for (int gsel : {0, 2, 4})
+        for (int wps : {20, 24, 28, 32}) cands.push_back({4, wps, gsel, 0, 2});
+      cands.push_back({4, 24, 1, 0, 2});
+      cands.push_back({4, 24, -1, 0, 2});
+      cands.push_back({4, 20, -1, 0, 4});
+    }
   } else {
     // The integer-product variants need ~100 registers (up to 20 warps/SM), the FP64-pipe ones
     // ~128 (16 warps/SM).
@@ -2701,6 +2790,8 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
   for (size_t c = 0; ce == cudaSuccess && rc == MFG_OK && c < cands.size(); c++) {
     const auto& k = cands[c];
+    // The LU's FMA form runs on the size-bucketed tasks only.
+    if (plan->kind == mfg_plan::GETRF && plan->args.fma && k[2] < 0) continue;
     rc = plan_reshape(tp, k[0], k[1], k[2], k[3], k[4]);
     float tmin = 3.0e38f;
     for (int rep = 0; rc == MFG_OK && ce == cudaSuccess && rep < 2; rep++) {
@@ -2813,6 +2904,7 @@ int getrf_batched_any(mfg_plan* plan, int elem, void* a, int* piv, void* b, int*
   if (!plan) return -1;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
+  plan->last_host = false;
   if (plan->count > 0) {
     if (!a) return fail(ctx, -2, "a is null");
     if (!piv) return fail(ctx, -3, "piv is null");
@@ -2833,6 +2925,7 @@ int getrf_batched_any(mfg_plan* plan, int elem, void* a, int* piv, void* b, int*
 
 int getrs_batched_any(mfg_plan* plan, int elem, const void* a, const int* piv, void* b) {
   if (!plan) return -1;
+  plan->last_host = false;
   mfg_ctx* ctx = plan->ctx;
   if (plan->kind != mfg_plan::GETRF) return fail(ctx, -1, "plan is not a getrf plan");
   if (plan->nrhs < 1) return fail(ctx, -1, "the plan has no right-hand sides (nrhs = 0)");
@@ -3120,8 +3213,8 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
       rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count), group,
                         p->args.hw_mul, p->args.dot_block);
       if (rc == MFG_OK) rc = plan_set_elem(sub, pipe_elem(op));
+      if (rc == MFG_OK && p->args.fma) rc = plan_set_fma(sub, 1);
       if (rc != MFG_OK) return rc;
-      sub->args.fma = p->args.fma;
     }
     if (p->kind == mfg_plan::GEVD) {
       rc = plan_set_elem(sub, pipe_elem(op));
@@ -3273,6 +3366,7 @@ int pipe_run_body(mfg_plan* p, int op, int keep_factor, std::initializer_list<vo
 // on a failure part-way through, the copies and kernels queued for earlier chunks are drained
 // first (their own errors are ignored; the first failure is the one reported).
 int pipe_run(mfg_plan* p, int op, int keep_factor, std::initializer_list<void*> host) {
+  p->last_host = true;
   const int rc = pipe_run_body(p, op, keep_factor, host);
   if (rc != MFG_OK) {
     auto& pp = p->pipe;
