@@ -166,7 +166,8 @@ __device__ void potrs_group(const double* l, int n, long long lda, double* b, lo
 // dot runs as fused multiply-adds in four chains, the column is scaled by the reciprocal of its
 // diagonal and the sums of squares accumulate with fused multiply-adds.  The result satisfies the
 // usual Cholesky backward-error bound |A - L L^T| <= gamma_(n+2) |L| |L^T|.
-template <int G>
+// C4: four-chain dots (fma_dot), else two chains (fma_dot2: fewer registers).
+template <int G, bool C4 = true>
 __device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum, double* rcp) {
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
@@ -196,9 +197,11 @@ __device__ int potrf_group_fma(double* a, int n, long long lda, double* dsum, do
     for (int j0 = k + 1; j0 < n; j0 += G / S) {
       const int j = j0 + lane / S;
       const bool live = j < n;
-      double d = live && cnt > 0 ? fma_dot(cnt, a + j + (long long)t0 * lda, lda,
-                                           a + k + (long long)t0 * lda, lda)
-                                 : 0.0;
+      double d = 0.0;
+      if (live && cnt > 0)
+        d = C4 ? fma_dot(cnt, a + j + (long long)t0 * lda, lda, a + k + (long long)t0 * lda, lda)
+               : fma_dot2(cnt, a + j + (long long)t0 * lda, lda, a + k + (long long)t0 * lda,
+                          lda);
       if (S > 1) {
         d = __dadd_rn(d, __shfl_xor_sync(gm, d, 1, G));
         if (S > 2) d = __dadd_rn(d, __shfl_xor_sync(gm, d, 2, G));
@@ -307,7 +310,7 @@ static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
 #endif
 
 // FMA = true: the FMA form of the factorization (potrf_group_fma) and of the solves
-// (potrs_group_fma).
+// (potrs_group_fma); IM then selects four-chain (true) or two-chain (false) dots.
 template <int WARPS, bool IM, int G, bool SPLIT = false, bool FMA = false>
 __global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS : 1)
     potrf_batched_kernel(BatchArgs p) {
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS :
       int info = 0;
       if (!p.solve_only) {
         if constexpr (FMA)
-          info = potrf_group_fma<G>(a, n, lda, scr, rcp);
+          info = potrf_group_fma<G, IM>(a, n, lda, scr, rcp);
         else if constexpr (SPLIT)
           info = potrf_group_split<G, IM>(a, n, lda, scr);
         else
@@ -378,7 +381,11 @@ template <int WARPS, int G>
 static cudaError_t launch_potrf_wg(const BatchArgs& args, int ctas, cudaStream_t s) {
   const size_t smem = potrf_smem_bytes(args, WARPS);
   if (args.fma) {
-    potrf_batched_kernel<WARPS, true, G, false, true><<<ctas, WARPS * 32, smem, s>>>(args);
+    // dot_block 1: two-chain dots.
+    if (args.dot_block == 1)
+      potrf_batched_kernel<WARPS, false, G, false, true><<<ctas, WARPS * 32, smem, s>>>(args);
+    else
+      potrf_batched_kernel<WARPS, true, G, false, true><<<ctas, WARPS * 32, smem, s>>>(args);
     return cudaGetLastError();
   }
   if constexpr (G == 32) {
@@ -412,6 +419,9 @@ static cudaError_t set_potrf_attr_g() {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, true, G, false, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(potrf_batched_kernel<WARPS, false, G, false, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if constexpr (G == 32) {

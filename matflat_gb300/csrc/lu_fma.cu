@@ -160,8 +160,8 @@ __device__ __forceinline__ void getrf_task_fma_loop(const BatchArgs& p, int warp
   }
 }
 
-// Any number of warps per CTA (blockDim.x / 32); MINB: CTAs of 4 warps per SM the register
-// allocation must allow (1: no bound).
+// Any number of warps per CTA (blockDim.x / 32), or 4 warps with the register allocation bounded
+// for MINB resident CTAs per SM (5: 96 registers, 20 warps, no spills with two-chain dots).
 template <int G, int FDB>
 __global__ void __launch_bounds__(512, 1) getrf_task_fma_kernel(BatchArgs p) {
   getrf_task_fma_loop<G, FDB>(p, blockDim.x >> 5);
@@ -182,6 +182,8 @@ static void launch_fma_gd(const BatchArgs& args, int ctas, int warps, size_t sme
     getrf_task_fma_kernel_occ<G, FDB, 7><<<ctas, 128, smem, s>>>(args);
   else if (warps == 4 && args.minb == 6)
     getrf_task_fma_kernel_occ<G, FDB, 6><<<ctas, 128, smem, s>>>(args);
+  else if (warps == 4 && args.minb == 5)
+    getrf_task_fma_kernel_occ<G, FDB, 5><<<ctas, 128, smem, s>>>(args);
   else
     getrf_task_fma_kernel<G, FDB><<<ctas, warps * 32, smem, s>>>(args);
 }
@@ -214,6 +216,9 @@ static cudaError_t set_fma_attr_gd() {
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(getrf_task_fma_kernel_occ<G, FDB, 6>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(getrf_task_fma_kernel_occ<G, FDB, 5>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;
 }

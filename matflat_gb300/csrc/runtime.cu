@@ -2775,9 +2775,13 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
       cands.push_back({4, 20, g, 0, 4});
       if (plan->args.fma) cands.push_back({4, 24, g, 0, 4});
     }
-    // Lanes per matrix by size bucket (slot 2 = -table, chol_lanes).
+    // Lanes per matrix by size bucket (slot 2 = -table, chol_lanes); the FMA form also with
+    // two-chain dots (slot 4 = 1).
     for (int t : {1, 2})
-      for (int wps : {12, 16, 20}) cands.push_back({4, wps, -t, 0, 4});
+      for (int wps : {12, 16, 20}) {
+        cands.push_back({4, wps, -t, 0, 4});
+        if (plan->args.fma) cands.push_back({4, wps, -t, 0, 1});
+      }
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::array<int, 5> best = cands[0];
