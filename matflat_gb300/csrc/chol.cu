@@ -303,16 +303,19 @@ static size_t potrf_smem_bytes(const BatchArgs& args, int warps) {
   return sizeof(double) * (args.gsolve ? SMEM_WARP_DOUBLES_CG : SMEM_WARP_DOUBLES_C) * warps;
 }
 
-// Resident warps per SM the FMA variant is compiled for (caps its registers at 65536 / (32 x
-// this)).
+// Resident warps per SM the FMA and the exact variants are compiled for (caps their registers at
+// 65536 / (32 x this)).  Without a bound the exact variants took 130-159 registers, 12 warps/SM.
 #ifndef MFG_CHOL_FMA_WARPS
 #define MFG_CHOL_FMA_WARPS 24
+#endif
+#ifndef MFG_CHOL_WARPS
+#define MFG_CHOL_WARPS 20
 #endif
 
 // FMA = true: the FMA form of the factorization (potrf_group_fma) and of the solves
 // (potrs_group_fma); IM then selects four-chain (true) or two-chain (false) dots.
 template <int WARPS, bool IM, int G, bool SPLIT = false, bool FMA = false>
-__global__ void __launch_bounds__(WARPS * 32, FMA ? MFG_CHOL_FMA_WARPS / WARPS : 1)
+__global__ void __launch_bounds__(WARPS * 32, (FMA ? MFG_CHOL_FMA_WARPS : MFG_CHOL_WARPS) / WARPS > 0 ? (FMA ? MFG_CHOL_FMA_WARPS : MFG_CHOL_WARPS) / WARPS : 1)
     potrf_batched_kernel(BatchArgs p) {
   extern __shared__ double sm_dyn[];
   constexpr int GPW = 32 / G;  // groups (matrices in flight) per warp
