@@ -1105,6 +1105,7 @@ def main():
                 traffic_key = "potrf_batched_kernel_chol100k"
         elif cfg_name == "bwd":
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=1, b_off=d["b_off"])
+            plan.set_form(args.form)     # fma: the recomputed factor in the FMA form
             g = torch.Generator(device="cuda")
             g.manual_seed(rank)
             lbar = torch.randn(a0.numel(), dtype=torch.float64, device="cuda", generator=g)
