@@ -911,7 +911,8 @@ def measure_lu_fma(torch, mf, d, rank, steps, warmup, fp64_peak, flops):
     tf = flops / (kms / 1e3) / 1e12
     return {"value": count / (kms / 1e3), "unit": "matrices/s", "kernel_ms": kms,
             "roofline": {"bound": "fp64", "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": tf / fp64_peak},
+                         "frac": tf / fp64_peak, "kernel": "getrf_task_fma_kernel",
+                         "traffic": read_traffic("getrf_task_fma_kernel")},
             "launch_shape": dict(zip(["warps_per_cta", "warps_per_sm", "lanes_table",
                                       "mul_mode", "dot_pairs_per_block"], tuned)),
             "form": "fused multiply-add dots, reciprocal column scaling, MatFlat's pivot rule "
