@@ -127,7 +127,7 @@ __device__ __forceinline__ void lu_finish_column(typename Tr::T* a, int m, int n
       q = oq > q ? oq : q;
     }
     if (__any_sync(gm, bad || first_nan) || pk <= 1ull || pk - q < LU_FMA_MARGIN_ULPS) {
-      *fail = true;   // the same verdict on every lane of the group
+      *fail = true;   // the same outcome on every lane of the group
       return;
     }
   }
