@@ -89,6 +89,10 @@ def lu_lanes(table, n):
         return 8
     if table == 4:
         return 8 if n <= 32 else 16 if n <= 96 else 32
+    if table == 5:
+        return 8 if n <= 24 else 16 if n <= 64 else 32
+    if table == 6:
+        return 16 if n <= 48 else 32
     return 32
 
 

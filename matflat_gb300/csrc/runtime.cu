@@ -314,8 +314,9 @@ long long gsolve_stride(int kind) {
 }
 
 // Lanes per matrix of the LU's size buckets, by table: 0 all 32; 1 16 up to order 128; 2 8 up to
-// order 48, 16 up to 128; 3 8 up to 128; 4 8 up to 32, 16 up to 96.  Orders above 128 always
-// take 32 lanes (their vectors live in global scratch sized per warp).
+// order 48, 16 up to 128; 3 8 up to 128; 4 8 up to 32, 16 up to 96; 5 8 up to 24, 16 up to 64;
+// 6 16 up to 48.  Orders above 128 always take 32 lanes (their vectors live in global scratch
+// sized per warp).
 int lu_lanes(int gsel, int n) {
   if (n > mfg::SMEM_N) return 32;
   switch (gsel) {
@@ -323,6 +324,8 @@ int lu_lanes(int gsel, int n) {
     case 2: return n <= 48 ? 8 : 16;
     case 3: return 8;
     case 4: return n <= 32 ? 8 : n <= 96 ? 16 : 32;
+    case 5: return n <= 24 ? 8 : n <= 64 ? 16 : 32;
+    case 6: return n <= 48 ? 16 : 32;
     default: return 32;
   }
 }
@@ -486,7 +489,7 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
   const long long need = ((long long)p->count + warps - 1) / warps;
   if (ctas > need) ctas = need;
   if (ctas < 1) ctas = 1;
-  if (p->kind == mfg_plan::GETRF && group != p->gsel && group >= -1 && group <= 4) {
+  if (p->kind == mfg_plan::GETRF && group != p->gsel && group >= -1 && group <= 6) {
     if (group >= 0) {
       const int rc = getrf_build_tasks(p, group);
       if (rc != MFG_OK) return rc;
@@ -2754,13 +2757,15 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config) {
       // The FMA form (no integer-pipe products) is fastest with fewer warps in flight and
       // two-chain dots (slot 4 = 1): 65.5 ms at 16 warps/SM against 70.7 with four chains and
       // 82.5 at 28 warps/SM on the 100,000-matrix batch.
-      for (int gsel : {0, 4})
+      // Tables 5 and 6 (16 lanes for the small orders): 62.1 / 61.6 ms at 16 warps/SM.
+      for (int gsel : {0, 4, 5, 6})
         for (int wps : {8, 12, 16, 20})
           for (int db : {1, 2}) cands.push_back({4, wps, gsel, 0, db});
     } else {
       // Measured on the 100,000-matrix batch: table 0 at 28 warps/SM 81.4 ms, 24: 83.6, 32:
-      // 82.6; table 4 at 28: 85.4; table 2 at 24: 90.9; one matrix per warp (-1) at 24: 90.4.
-      for (int gsel : {0, 2, 4})
+      // 82.6; table 6 at 28: 80.6, table 5: 81.2; table 4 at 28: 85.4; table 2 at 24: 90.9; one
+      // matrix per warp (-1) at 24: 90.4.
+      for (int gsel : {0, 2, 4, 5, 6})
         for (int wps : {24, 28, 32}) cands.push_back({4, wps, gsel, 0, 2});
     }
   } else {
@@ -3211,8 +3216,11 @@ int pipe_build(mfg_plan* p, int op, int keep_factor) {
       // Same launch shape as the parent plan (which the autotuner may have chosen), then the
       // element type's scratch.
       // The lanes table (GETRF) or the Cholesky's size-bucket table travel in plan_reshape's
-      // group argument, as the autotuner passes them.
-      const int group = p->kind == mfg_plan::GETRF ? p->gsel
+      // group argument, as the autotuner passes them.  LU chunks take 32 lanes for every order
+      // (table 0, one launch per chunk): with a two-bucket table each chunk's second launch
+      // lengthens the pipeline (e2e 1.10 against 1.13 M matrices/s on the 100,000-matrix batch,
+      // 1.37 against 1.46 M in the FMA form).
+      const int group = p->kind == mfg_plan::GETRF ? (p->gsel >= 0 ? 0 : -1)
                         : p->csel > 0               ? -p->csel
                                                     : p->args.group;
       rc = plan_reshape(sub, p->warps, std::max(1, p->ctas * p->warps / ctx->sm_count), group,

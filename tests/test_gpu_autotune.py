@@ -36,7 +36,7 @@ def test_autotune_getrf(mf):
         if round_ == 0:
             cfg = batch.autotune()
             assert len(cfg) == 5 and cfg[0] in (4, 8) and cfg[1] in (24, 28, 32)
-            assert cfg[2] in (0, 2, 4)                 # the lanes table of the size buckets
+            assert cfg[2] in (0, 2, 4, 5, 6)           # the lanes table of the size buckets
             assert cfg[3] in (0, 2) and cfg[4] in (2, 4)
         da, db = _dev(a), _dev(b)
         dpiv = torch.zeros(ptot, dtype=torch.int32, device="cuda")

@@ -382,7 +382,7 @@ def test_qr_batched_least_squares(mf, dtype):
         assert np.max(np.abs(xg - xo)) <= tol * 1e3 * max(1.0, np.max(np.abs(xo)))
 
 
-@pytest.mark.parametrize("table", [-1, 0, 1, 2, 3, 4])
+@pytest.mark.parametrize("table", [-1, 0, 1, 2, 3, 4, 5, 6])
 def test_lu_batched_every_lanes_table(mf, table, monkeypatch):
     """Every lanes-per-matrix table of the size-bucketed LU (8, 16 or 32 lanes per matrix by
     order; -1 the one-matrix-per-warp queue) gives the oracle's factors, pivots, signs and
