@@ -117,3 +117,41 @@ def test_set_form_rejects_other_plans(mf):
     batch = mf.LuInverseBatch(n, a_off, piv_off)
     with pytest.raises(RuntimeError):      # the C call refuses a plan that is not a Cholesky
         mf.CholeskyBatch.set_form(batch, "fma")
+
+
+def test_cholesky_fma_padded(mf):
+    """lda > n in the FMA form: the factor is backward stable, the padding rows are untouched."""
+    import torch
+    rng = np.random.default_rng(79)
+    count = 150
+    n = rng.integers(1, 129, size=count).astype(np.int32)
+    lda = (n + rng.integers(1, 5, size=count)).astype(np.int32)
+    mats = []
+    for i, ni in enumerate(n):
+        bm = rng.standard_normal((ni, ni))
+        full = np.full((int(lda[i]), ni), 7.0)
+        full[:ni, :] = bm @ bm.T + ni * np.eye(ni)
+        mats.append(full.reshape(-1, order="F"))
+    sz = lda.astype(np.int64) * n
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    a = np.concatenate(mats)
+    b = rng.standard_normal(int(n.sum()))
+    batch = mf.CholeskyBatch(n, a_off, nrhs=1, b_off=b_off, lda=lda)
+    batch.set_form("fma")
+    da, db = _dev(a), _dev(b)
+    dinfo = torch.zeros(count, dtype=torch.int32, device="cuda")
+    batch.run(da, db, dinfo)
+    mf.context().synchronize()
+    assert not _host(dinfo).any()
+    ga, gb = _host(da), _host(db)
+    for i in range(count):
+        ni, li = int(n[i]), int(lda[i])
+        F = ga[a_off[i]:a_off[i] + li * ni].reshape(ni, li).T
+        assert (F[ni:, :] == 7.0).all()
+        A = a[a_off[i]:a_off[i] + li * ni].reshape(ni, li).T[:ni, :]
+        L = np.tril(F[:ni, :])
+        assert np.linalg.norm(A - L @ L.T, 1) / np.linalg.norm(A, 1) <= 1e-13 * ni, i
+        x, bi = gb[b_off[i]:b_off[i] + ni], b[b_off[i]:b_off[i] + ni]
+        assert np.linalg.norm(bi - A @ x, 1) / (np.linalg.norm(A, 1) * np.linalg.norm(x, 1) +
+                                                np.linalg.norm(bi, 1)) <= 1e-13 * ni, i

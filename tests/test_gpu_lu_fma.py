@@ -132,3 +132,48 @@ def test_lu_fma_host_buffers_and_autotune(mf):
     oracle.lu_solve_batched(n, a_off, a.copy(), piv_off, opiv, b_off, b.copy(), 4, osign, 8)
     np.testing.assert_array_equal(hpiv, opiv)
     np.testing.assert_array_equal(hsign, osign)
+
+
+@pytest.mark.parametrize("big", [False, True], ids=["cta-bucket", "task-bucket"])
+def test_lu_fma_padded_and_large_orders(mf, big):
+    """lda > n, and orders above 128: few of them run in the exact CTA-per-matrix kernel, many of
+    them in the FMA form's 32-lane tasks (scratch in global memory).  Pivots identical to the
+    oracle's, factors backward stable."""
+    import torch
+    rng = np.random.default_rng(320 + big)
+    count = 1400 if big else 120
+    n = rng.integers(1, 141, size=count).astype(np.int32)
+    if big:
+        n[:1300] = rng.integers(129, 141, size=1300)
+    lda = (n + rng.integers(0, 4, size=count)).astype(np.int32)
+    sz = lda.astype(np.int64) * n
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    a = rng.standard_normal(int(sz.sum()))
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    b_off = piv_off * 2
+    b = rng.standard_normal(int(n.sum()) * 2)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=2, b_off=b_off, lda=lda)
+    batch.set_form("fma")
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(int(n.sum()), dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(count, dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(count, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    ga, gpiv = _host(da), _host(dpiv)
+    for i in range(0, count, 7 if big else 1):
+        ni, li = int(n[i]), int(lda[i])
+        A = a[a_off[i]:a_off[i] + li * ni].reshape(ni, li).T
+        oa = a[a_off[i]:a_off[i] + li * ni].copy()
+        opiv = np.zeros(ni, np.int32)
+        oracle.lu(ni, ni, oa, li, opiv)
+        p = gpiv[piv_off[i]:piv_off[i] + ni]
+        np.testing.assert_array_equal(p, opiv, err_msg="matrix %d" % i)
+        F = ga[a_off[i]:a_off[i] + li * ni].reshape(ni, li).T
+        np.testing.assert_array_equal(F[ni:li, :], A[ni:li, :])     # padding untouched
+        F = F[:ni, :]
+        L = np.tril(F, -1) + np.eye(ni)
+        U = np.triu(F)
+        An = A[:ni, :]
+        assert np.linalg.norm(An[p, :] - L @ U, 1) / np.linalg.norm(An, 1) <= 1e-13 * ni, i
