@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libmatflat_gpu.so")
-SOURCES = ["lu.cu", "lu_fma.cu", "chol.cu", "getri.cu", "blas.cu", "qr.cu", "mixed.cu", "chol_bwd.cu", "tune.cu", "vec.cu", "runtime.cu"]
+SOURCES = ["lu.cu", "lu_fma.cu", "lu_big.cu", "chol.cu", "getri.cu", "blas.cu", "qr.cu", "mixed.cu", "chol_bwd.cu", "tune.cu", "vec.cu", "runtime.cu"]
 HEADERS = ["mf_device.cuh", "mf_imul.cuh", "mf_scalar.cuh", "mf_solve.cuh", "mf_tc.cuh", "mf_lu.cuh",
            "mf_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

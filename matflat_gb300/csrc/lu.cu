@@ -16,206 +16,6 @@
 
 namespace mfg {
 
-// ---------------------------------------------------------------------------------------------
-// The same schedule with a whole CTA of W warps on one matrix, for large orders when there are too
-// few matrices to give every SM several warps (and for the mixed solver's FP64 fallback): a step's
-// 2(n-k-1) dots are spread over the CTA's threads, the pivot search is a warp argmax followed by a
-// reduction over the W warps' candidates (larger key, then smaller row), and the swap and the
-// scaling are spread over the threads.  Per-entry arithmetic is unchanged, so the bits are the same.
-struct CtaRed {
-  unsigned long long key[32];
-  int idx[32];
-  int nan0;
-};
-
-template <int W, bool IDIV = false>
-__device__ void lu_cta_finish_column(double* a, int n, long long lda, int c, int mode,
-                                     const double* scol, int* piv, int& sign, int& info,
-                                     CtaRed* red, int* pivot = nullptr) {
-  using Tr = DTraits;
-  constexpr int T = W * 32;
-  const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  double* cc = a + (long long)c * lda;
-  unsigned long long bkey = 0ull;
-  int bidx = INT_MAX;
-  if (mode == 0) {
-    for (int i = c + tid; i < n; i += T) {
-      const double v = cc[i];
-      const unsigned long long key = Tr::key(v);
-      if (key > bkey) {
-        bkey = key;
-        bidx = i;
-      }
-      if (i == c) red->nan0 = Tr::nan0(v) ? 1 : 0;
-    }
-  } else {
-    const double* l1 = a + (long long)(c - 1) * lda;
-    const double u1 = cc[c - 1];
-    const double* l2 = (mode == 2) ? a + (long long)(c - 2) * lda : l1;
-    const double u2 = (mode == 2) ? cc[c - 2] : u1;
-    for (int i = c + tid; i < n; i += T) {
-      const double s =
-          IDIV ? (mode == 1 ? imul_rn(l1[i], u1)
-                            : __dadd_rn(scol[i], __dadd_rn(imul_rn(l2[i], u2), imul_rn(l1[i], u1))))
-               : (mode == 1 ? Tr::prod(l1[i], u1) : Tr::pair(scol[i], l2[i], u2, l1[i], u1));
-      const double v = Tr::fin(cc[i], s);
-      cc[i] = v;
-      const unsigned long long key = Tr::key(v);
-      if (key > bkey) {
-        bkey = key;
-        bidx = i;
-      }
-      if (i == c) red->nan0 = Tr::nan0(v) ? 1 : 0;
-    }
-  }
-  const int wp = warp_argmax(bkey, bidx);
-  unsigned long long wk = bkey;   // the warp's largest key, which belongs to row wp
-  for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long ok = __shfl_xor_sync(FULL_MASK, wk, off);
-    if (ok > wk) wk = ok;
-  }
-  if (lane == 0) {
-    red->key[warp] = wk;
-    red->idx[warp] = wp;
-  }
-  __syncthreads();
-  unsigned long long best = red->key[0];
-  int p = red->idx[0];
-  for (int w = 1; w < W; ++w) {
-    const unsigned long long k2 = red->key[w];
-    const int i2 = red->idx[w];
-    if (k2 > best || (k2 == best && i2 < p)) {
-      best = k2;
-      p = i2;
-    }
-  }
-  if (red->nan0) p = c;
-  if (pivot) *pivot = p;
-  if (p != c && p < n) {
-    for (int col = tid; col < n; col += T) {
-      double* base = a + (long long)col * lda;
-      const double t = base[c];
-      base[c] = base[p];
-      base[p] = t;
-    }
-    if (tid == 0) {
-      const int t = piv[c];
-      piv[c] = piv[p];
-      piv[p] = t;
-    }
-    sign = -sign;
-  }
-  __syncthreads();
-  const double diag = cc[c];
-  if (Tr::nz(diag)) {
-    if constexpr (IDIV) {
-      idiv_column(cc, c + 1 + tid, n, T, diag);
-    } else {
-      for (int i = c + 1 + tid; i < n; i += T) cc[i] = Tr::div(cc[i], diag);
-    }
-  } else if (info == 0) {
-    info = c + 1;
-  }
-  __syncthreads();
-}
-
-template <int W, int IM, int DB>
-__device__ void lu_cta(double* a, int n, long long lda, int* piv, double* scol, int& sign,
-                       int& info, CtaRed* red) {
-  using Tr = DTraits;
-  constexpr int T = W * 32;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < n; i += T) piv[i] = i;
-  sign = 1;
-  info = 0;
-  __syncthreads();
-  lu_cta_finish_column<W, MFG_IDIV && IM != 0>(a, n, lda, 0, 0, scol, piv, sign, info, red);
-  for (int k = 0; k < n; ++k) {
-    const int k1 = k + 1;
-    const int R = n - k1;
-    const int C = (k1 < n && k >= 1) ? n - k1 : 0;
-    const double* rowk = a + k;
-    const double* colk1 = a + (long long)k1 * lda;
-    for (int d = tid; d < R + C; d += T) {
-      const bool isrow = d < R;
-      const int idx = isrow ? k1 + d : k1 + (d - R);
-      const double* x = isrow ? rowk : a + idx;
-      const double* y = isrow ? a + (long long)idx * lda : colk1;
-      const int len = isrow ? k : k - 1;
-      const double s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
-      if (isrow) {
-        double* dst = a + (long long)idx * lda + k;
-        *dst = Tr::fin(*dst, s);
-      } else {
-        scol[idx] = s;
-      }
-    }
-    __syncthreads();
-    if (k1 < n)
-      lu_cta_finish_column<W, MFG_IDIV && IM != 0>(a, n, lda, k1, k1 == 1 ? 1 : 2, scol, piv, sign,
-                                                   info, red);
-  }
-}
-
-// lu_cta with the early prefixes of lu_warp<..., EARLY = true>: threads left idle in the last round
-// of step k compute column k+2's prefixes for the bottom rows (the same dots, evaluated once, in the
-// same tree), and the row swapped into that range by column k+1's pivot gets its prefix again at
-// step k+1.  Column sums alternate between scol (even columns) and scol2 (odd columns).
-template <int W, int IM, int DB>
-__device__ void lu_cta_early(double* a, int n, long long lda, int* piv, double* scol,
-                             double* scol2, int& sign, int& info, CtaRed* red) {
-  using Tr = DTraits;
-  constexpr int T = W * 32;
-  constexpr bool IDIV = MFG_IDIV && IM != 0;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < n; i += T) piv[i] = i;
-  sign = 1;
-  info = 0;
-  __syncthreads();
-  lu_cta_finish_column<W, IDIV>(a, n, lda, 0, 0, scol, piv, sign, info, red);
-  int e_prev = 0;
-  int p_prev = INT_MAX;
-  for (int k = 0; k < n; ++k) {
-    const int k1 = k + 1;
-    const int R = n - k1;
-    const double* rowk = a + k;
-    const double* colk1 = a + (long long)k1 * lda;
-    double* pre1 = (k1 & 1) ? scol2 : scol;
-    const bool has_col = k1 < n && k >= 1;
-    const int nreg0 = has_col ? max(0, n - e_prev - k1) : 0;
-    const int disp = (has_col && e_prev > 0 && p_prev >= n - e_prev && p_prev < n) ? 1 : 0;
-    const int C = nreg0 + disp;
-    int E = 0;
-    if (k >= 2 && k + 2 < n) E = min(n - (k + 2), (T - (R + C) % T) % T);
-    double* pre2 = (k & 1) ? scol2 : scol;
-    const double* colk2 = a + (long long)(k + 2) * lda;
-    for (int d = tid; d < R + C + E; d += T) {
-      const bool isrow = d < R;
-      const bool isreg = !isrow && d < R + C;
-      const int c = d - R;
-      const int idx = isrow ? k1 + d : isreg ? (c < nreg0 ? k1 + c : p_prev) : n - E + (c - C);
-      const double* x = isrow ? rowk : a + idx;
-      const double* y = isrow ? a + (long long)idx * lda : isreg ? colk1 : colk2;
-      const int len = isreg ? k - 1 : k;
-      const double s = Tr::template dot<IM, DB>(len, x, lda, y, 1);
-      if (isrow) {
-        double* dst = a + (long long)idx * lda + k;
-        *dst = Tr::fin(*dst, s);
-      } else {
-        (isreg ? pre1 : pre2)[idx] = s;
-      }
-    }
-    __syncthreads();
-    int pk = INT_MAX;
-    if (k1 < n)
-      lu_cta_finish_column<W, IDIV>(a, n, lda, k1, k1 == 1 ? 1 : 2, pre1, piv, sign, info, red,
-                                    &pk);
-    e_prev = E;
-    p_prev = pk;
-  }
-}
-
 constexpr int SMEM_WARP_DOUBLES = SMEM_N + 2 * RHS_CHUNK * (SMEM_N + 1) + 2;
 // Per-warp shared memory when the solve is staged in global memory (BatchArgs::gsolve).
 constexpr int SMEM_WARP_DOUBLES_G = SMEM_N + 2;

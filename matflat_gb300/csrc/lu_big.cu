@@ -1,0 +1,338 @@
+// The FMA form of the batched double LU + solve for orders above 128 (mfg_plan_set_form(
+// MFG_FORM_FMA) on a getrf plan): one matrix per CTA, blocked right-looking, so that the bulk of
+// the flops runs from shared-memory tiles instead of re-reading the matrix from L2/DRAM at every
+// Crout step (the warp and CTA schedules of mf_lu.cuh / lu.cu are memory-bound at these orders).
+// No counterpart in the reference, whose LU has one arithmetic; the pivots are MatFlat's
+// (Factorization.LuCore, MatFlat/Factorization.Lu.cs:296-350).
+//
+// Per panel of BIG_NB columns [j0, j1):
+//   1. the panel's columns one by one: pivot search with the FMA form's screen (the pivot's key
+//      must beat the runner-up's by LU_FMA_MARGIN_ULPS, every candidate finite, the pivot not
+//      zero), whole-row swap (MatFlat swaps whole rows, Lu.cs:332-337), scaling by the pivot's
+//      reciprocal, rank-1 update of the panel's later columns;
+//   2. U12 = L11^-1 A12 for the trailing columns (unit lower 32 x 32 from shared memory, one column
+//      per thread in registers);
+//   3. A22 -= L21 U12 in 64 x 64 tiles, both operands staged in shared memory, 4 x 4 fused
+//      multiply-adds per thread and k.
+// A matrix whose screen fails at any column is restored from the copy the CTA took before
+// factoring it and redone in MatFlat's arithmetic (lu_cta_early: the exact CTA schedule, MatFlat's
+// bits).  The solves are getrs_fma's column sweeps for every matrix, so solve-only calls reproduce
+// the fused call's bits.  The factors are backward stable, not MatFlat's bits.
+#include <cuda_runtime.h>
+
+#include "mf_lu.cuh"
+
+namespace mfg {
+
+constexpr int BIG_W = 8;               // warps per CTA
+constexpr int BIG_T = BIG_W * 32;
+constexpr int BIG_NB = 32;             // panel width
+constexpr int BIG_TM = 64;             // trailing-update tile: BIG_TM x BIG_TM, 4 x 4 per thread
+
+struct BigSmem {
+  double as[BIG_NB][BIG_TM];           // L21 tile, k-major (L11 during the U12 solve)
+  double bs[BIG_NB][BIG_TM + 1];       // U12 tile, k-major (odd row length: fewer bank conflicts)
+  double uj[BIG_NB];                   // row j of the panel after the swap
+  unsigned long long pk[BIG_W];        // per warp: largest key, runner-up, its row, non-finite
+  unsigned long long q[BIG_W];
+  int pi[BIG_W];
+  int bad[BIG_W];
+  CtaRed red;
+  int next;
+};
+
+// The thread's candidate (key, row) pairs of one column: largest key, runner-up, non-finite seen.
+struct Cand {
+  unsigned long long bk, sk;
+  int bi;
+  bool bad;
+  __device__ __forceinline__ void reset() {
+    bk = sk = 0ull;
+    bi = INT_MAX;
+    bad = false;
+  }
+  __device__ __forceinline__ void add(double v, int i) {
+    const unsigned long long key = pivot_key(v);
+    bad |= !finite_bits(v);
+    if (key > bk) {
+      sk = bk;
+      bk = key;
+      bi = i;
+    } else if (key > sk) {
+      sk = key;
+    }
+  }
+};
+
+// The CTA's pivot from every thread's candidates, with the screen: returns the pivot row, or -1
+// when the column fails (the same answer on every thread).  Ties between rows fail the screen, so
+// the tie rule of MatFlat's scan (the first row) never has to be reproduced.
+__device__ __forceinline__ int big_pivot(const Cand& c, BigSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wp = warp_argmax(c.bk, c.bi);
+  unsigned long long wk = c.bk;
+  unsigned long long wq = c.bi == wp ? c.sk : c.bk;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(FULL_MASK, wk, off);
+    const unsigned long long oq = __shfl_xor_sync(FULL_MASK, wq, off);
+    wk = ok > wk ? ok : wk;
+    wq = oq > wq ? oq : wq;
+  }
+  const bool wbad = __any_sync(FULL_MASK, c.bad);
+  if (lane == 0) {
+    sm.pk[warp] = wk;
+    sm.q[warp] = wq;
+    sm.pi[warp] = wp;
+    sm.bad[warp] = wbad ? 1 : 0;
+  }
+  __syncthreads();
+  unsigned long long pk = sm.pk[0];
+  int p = sm.pi[0];
+  int w0 = 0;
+  int bad = sm.bad[0];
+#pragma unroll
+  for (int w = 1; w < BIG_W; ++w) {
+    const unsigned long long k2 = sm.pk[w];
+    const int i2 = sm.pi[w];
+    bad |= sm.bad[w];
+    if (k2 > pk || (k2 == pk && i2 < p)) {
+      pk = k2;
+      p = i2;
+      w0 = w;
+    }
+  }
+  unsigned long long q = 0ull;
+#pragma unroll
+  for (int w = 0; w < BIG_W; ++w) {
+    const unsigned long long k2 = w == w0 ? sm.q[w] : sm.pk[w];
+    q = k2 > q ? k2 : q;
+  }
+  if (bad || pk <= 1ull || pk - q < LU_FMA_MARGIN_ULPS) return -1;
+  return p;
+}
+
+// Panel [j0, j1) of the n x n matrix a: returns false when a column fails the screen.
+__device__ bool big_panel(double* a, int n, long long lda, int j0, int j1, int* piv, int& sign,
+                          BigSmem& sm) {
+  const int tid = threadIdx.x;
+  Cand c;
+  c.reset();
+  {
+    const double* cj = a + (long long)j0 * lda;
+    for (int i = j0 + tid; i < n; i += BIG_T) c.add(cj[i], i);
+  }
+  for (int j = j0; j < j1; ++j) {
+    const int p = big_pivot(c, sm);
+    if (p < 0) return false;
+    // Whole-row swap; the threads holding the panel's columns keep row j's new values.
+    for (int col = tid; col < n; col += BIG_T) {
+      double* base = a + (long long)col * lda;
+      double v = base[j];
+      if (p != j) {
+        const double w = base[p];
+        base[p] = v;
+        base[j] = w;
+        v = w;
+      }
+      if (col >= j && col < j1) sm.uj[col - j0] = v;
+    }
+    if (p != j) {
+      if (tid == 0) {
+        const int t = piv[j];
+        piv[j] = piv[p];
+        piv[p] = t;
+      }
+      sign = -sign;
+    }
+    __syncthreads();
+    // Scaling, rank-1 update of the panel's later columns, candidates of column j + 1.
+    const double r = __drcp_rn(sm.uj[j - j0]);
+    double* cj = a + (long long)j * lda;
+    c.reset();
+    for (int i = j + 1 + tid; i < n; i += BIG_T) {
+      const double l = __dmul_rn(cj[i], r);
+      cj[i] = l;
+      if (j + 1 < j1) {
+        double* cc = cj + lda + i;
+        const double v = __fma_rn(-l, sm.uj[j + 1 - j0], *cc);
+        *cc = v;
+        c.add(v, i);
+      }
+#pragma unroll 8
+      for (int col = j + 2; col < j1; ++col) {
+        double* cc = a + (long long)col * lda + i;
+        *cc = __fma_rn(-l, sm.uj[col - j0], *cc);
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// U12 = L11^-1 A12: rows [j0, j0 + BIG_NB) of the columns [j0 + BIG_NB, n).
+__device__ void big_u12(double* a, int n, long long lda, int j0, BigSmem& sm) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < BIG_NB * BIG_NB; e += BIG_T) {
+    const int k = e / BIG_NB;
+    const int r = e - k * BIG_NB;
+    sm.as[k][r] = a[(long long)(j0 + k) * lda + j0 + r];
+  }
+  __syncthreads();
+  // One column per thread, row by row from the thread's own 32 values (L1-resident): a column
+  // held in registers (64 of them) with the solve unrolled spills under the two-CTA register bound.
+  for (int col = j0 + BIG_NB + tid; col < n; col += BIG_T) {
+    double* cp = a + (long long)col * lda + j0;
+    for (int r = 1; r < BIG_NB; ++r) {
+      double v = cp[r];
+#pragma unroll 8
+      for (int k = 0; k < r; ++k) v = __fma_rn(-sm.as[k][r], cp[k], v);
+      cp[r] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// A22 -= L21 U12 for the rows and columns [j1, n), j1 = j0 + BIG_NB.
+__device__ void big_update(double* a, int n, long long lda, int j0, BigSmem& sm) {
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int j1 = j0 + BIG_NB;
+  const int mt = (n - j1 + BIG_TM - 1) / BIG_TM;
+  for (int tile = 0; tile < mt * mt; ++tile) {
+    const int r0 = j1 + (tile % mt) * BIG_TM;
+    const int c0 = j1 + (tile / mt) * BIG_TM;
+    double acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+        acc[u][v] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
+      }
+    }
+    for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
+      const int k = e / BIG_TM;
+      const int rr = e - k * BIG_TM;
+      const int i = r0 + rr;
+      sm.as[k][rr] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
+    }
+    for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
+      const int cc = e / BIG_NB;
+      const int k = e - cc * BIG_NB;
+      const int jj = c0 + cc;
+      sm.bs[k][cc] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < BIG_NB; ++k) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) av[u] = sm.as[k][tx + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) bv[v] = sm.bs[k][ty + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = __fma_rn(-av[u], bv[v], acc[u][v]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+        if (i < n && jj < n) a[(long long)jj * lda + i] = acc[u][v];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The whole factorization in the FMA form; false when a column failed the screen (the matrix is
+// then partly factored and must be restored).
+__device__ bool big_lu_fma(double* a, int n, long long lda, int* piv, int& sign, BigSmem& sm) {
+  for (int i = threadIdx.x; i < n; i += BIG_T) piv[i] = i;
+  sign = 1;
+  __syncthreads();
+  for (int j0 = 0; j0 < n; j0 += BIG_NB) {
+    const int j1 = min(n, j0 + BIG_NB);
+    if (!big_panel(a, n, lda, j0, j1, piv, sign, sm)) return false;
+    if (j1 < n) {
+      big_u12(a, n, lda, j0, sm);
+      big_update(a, n, lda, j0, sm);
+    }
+  }
+  return true;
+}
+
+// The redo of a matrix the screen rejected: restore it from the CTA's copy, factor it in MatFlat's
+// arithmetic.  Out of line: rare, and inlined it would raise the main path's register count.
+__device__ __noinline__ void big_fallback(double* a, int n, long long lda, const double* bk,
+                                          int* piv, double* scol, int* sign, int* info,
+                                          CtaRed* red) {
+  __syncthreads();
+  for (int j = 0; j < n; ++j)
+    for (int i = threadIdx.x; i < n; i += BIG_T)
+      a[(long long)j * lda + i] = __ldcs(bk + (long long)j * n + i);
+  __syncthreads();
+  int sg = 1, inf = 0;
+  lu_cta_early<BIG_W, 1, 2>(a, n, lda, piv, scol, scol + n, sg, inf, red);
+  *sign = sg;
+  *info = inf;
+}
+
+// Work items: the plan's tasks (one matrix each, p.ntasks of them, taken from p.queue).  Per CTA:
+// a copy of up to bstride doubles in p.fbackup and a slice of p.gscratch (the solve's staging and
+// the fallback's column sums).
+__global__ void __launch_bounds__(BIG_T, 2) getrf_big_fma_kernel(BatchArgs p, long long bstride) {
+  __shared__ BigSmem sm;
+  const int tid = threadIdx.x;
+  double* slice = p.gscratch + (long long)blockIdx.x * p.gscratch_stride;
+  double* bk = p.fbackup + (long long)blockIdx.x * bstride;
+  for (;;) {
+    if (tid == 0) sm.next = atomicAdd(p.queue, 1);
+    __syncthreads();
+    const int t = sm.next;
+    __syncthreads();
+    if (t >= p.ntasks) break;
+    const int mat = p.order[p.task_first[t]];
+    const int n = p.n[mat];
+    const long long lda = p.lda[mat];
+    double* a = p.a + p.a_off[mat];
+    int* piv = p.piv + p.piv_off[mat];
+    int sign = 1, info = 0;
+    if (!p.solve_only) {
+      for (int j = 0; j < n; ++j)
+        for (int i = tid; i < n; i += BIG_T)
+          __stcs(bk + (long long)j * n + i, a[(long long)j * lda + i]);
+      __syncthreads();
+      if (!big_lu_fma(a, n, lda, piv, sign, sm)) {
+        big_fallback(a, n, lda, bk, piv, slice, &sign, &info, &sm.red);
+        if (tid == 0) atomicAdd(p.fcount, 1);
+      }
+      __syncthreads();
+    }
+    if (p.nrhs > 0 && tid < 32)
+      getrs_fma<32>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, slice + n, slice);
+    if (tid == 0 && !p.solve_only) {
+      p.sign[mat] = sign;
+      p.info[mat] = info;
+    }
+    __syncthreads();
+  }
+}
+
+long long getrf_big_backup_doubles(int nmax) {
+  return ((long long)nmax * nmax + 31) / 32 * 32;
+}
+
+cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, cudaStream_t s) {
+  if (ctas < 1 || nmax < 1 || !args.fbackup || !args.fcount || !args.gscratch ||
+      args.gscratch_stride < warp_scratch_doubles(nmax))
+    return cudaErrorInvalidValue;
+  getrf_big_fma_kernel<<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
+  return cudaGetLastError();
+}
+
+}  // namespace mfg

@@ -16,65 +16,6 @@
 
 namespace mfg {
 
-// A x = b for nr right-hand sides from the factors of one square matrix: b' = P b (b'[i] =
-// b[piv[i]]), then L y = b' (unit lower) and U x = y, both as column sweeps with fused
-// multiply-adds (column t of the factor is contiguous), U's diagonal applied as its reciprocal.
-// rcp: n doubles of the group's scratch.  b: column-major, leading dimension ldb, overwritten.
-template <int G>
-__device__ void getrs_fma(const double* lu, int n, long long lda, const int* piv, double* b,
-                          long long ldb, int nrhs, double* xs, double* rcp) {
-  const int lane = group_lane<G>();
-  const unsigned gm = group_mask<G>();
-  const int ldx = n | 1;
-  for (int t = lane; t < n; t += G) rcp[t] = __drcp_rn(lu[(long long)t * lda + t]);
-  __syncwarp(gm);
-  for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
-    const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
-    for (int e = lane; e < nr * n; e += G) {
-      const int r = e / n;
-      const int i = e - r * n;
-      xs[r * ldx + i] = b[(long long)(r0 + r) * ldb + piv[i]];
-    }
-    __syncwarp(gm);
-    for (int t = 0; t + 1 < n; ++t) {
-      const double* colt = lu + (long long)t * lda;
-      double xt[RHS_CHUNK];
-#pragma unroll
-      for (int r = 0; r < RHS_CHUNK; ++r) xt[r] = r < nr ? xs[r * ldx + t] : 0.0;
-      for (int i = t + 1 + lane; i < n; i += G) {
-        const double l = colt[i];
-#pragma unroll
-        for (int r = 0; r < RHS_CHUNK; ++r)
-          if (r < nr) xs[r * ldx + i] = __fma_rn(-l, xt[r], xs[r * ldx + i]);
-      }
-      __syncwarp(gm);
-    }
-    for (int t = n - 1; t >= 0; --t) {
-      const double* colt = lu + (long long)t * lda;
-      const double rt = rcp[t];
-      double xt[RHS_CHUNK];
-#pragma unroll
-      for (int r = 0; r < RHS_CHUNK; ++r) xt[r] = r < nr ? __dmul_rn(xs[r * ldx + t], rt) : 0.0;
-      __syncwarp(gm);
-      if (lane == 0)
-        for (int r = 0; r < nr; ++r) xs[r * ldx + t] = xt[r];
-      for (int i = lane; i < t; i += G) {
-        const double u = colt[i];
-#pragma unroll
-        for (int r = 0; r < RHS_CHUNK; ++r)
-          if (r < nr) xs[r * ldx + i] = __fma_rn(-u, xt[r], xs[r * ldx + i]);
-      }
-      __syncwarp(gm);
-    }
-    for (int e = lane; e < nr * n; e += G) {
-      const int r = e / n;
-      const int i = e - r * n;
-      b[(long long)(r0 + r) * ldb + i] = xs[r * ldx + i];
-    }
-    __syncwarp(gm);
-  }
-}
-
 // The fallback of a matrix the screen rejected: restore it from its copy and factor it in
 // MatFlat's arithmetic (products on the FP64 pipe: the same bits as the integer-pipe form).  Kept
 // out of line: it is rare, and inlined it would raise the register count of the FMA path.

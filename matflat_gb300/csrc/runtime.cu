@@ -368,6 +368,14 @@ int potrf_build_segments(mfg_plan* p, int csel) {
   return MFG_OK;
 }
 
+// CTAs of a GETRF plan's CTA-per-matrix launch (segment 3): at most two per SM and one per
+// scratch slice.
+long long getrf_cta_ctas(const mfg_plan* p) {
+  const long long slices = (long long)p->ctas * p->warps;
+  return std::max<long long>(
+      1, std::min<long long>({(long long)p->seg_cnt[3], 2LL * p->ctx->sm_count, slices}));
+}
+
 // The FMA form's per-warp copies of a GETRF plan: fma_stride doubles for every warp its launches
 // can run (waits for the stream when the buffer grows: it may be in use).  The fallback counter
 // is the plan's work-counter slot 8, zeroed with the queues before every launch.
@@ -375,7 +383,10 @@ int fma_backup_reserve(mfg_plan* p) {
   if (p->kind != mfg_plan::GETRF || !p->args.fma) return MFG_OK;
   mfg_ctx* ctx = p->ctx;
   const long long stride = std::max<long long>(p->fma_stride, 32);
-  const size_t bytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+  size_t bytes = (size_t)stride * sizeof(double) * (size_t)p->ctas * (size_t)p->warps;
+  if (p->seg_cnt[3] > 0)   // the blocked CTA kernel: one copy of the largest order per CTA
+    bytes = std::max(bytes, (size_t)getrf_cta_ctas(p) * sizeof(double) *
+                                (size_t)mfg::getrf_big_backup_doubles(p->cta_nmax));
   if (bytes > p->fbackup.bytes) {
     MFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     MFG_CUDA(ctx, p->fbackup.reserve(bytes));
@@ -404,11 +415,12 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   struct Task { int first, cnt, g; };
   std::vector<Task> segs[5];
   // Orders above SMEM_N go to whole CTAs (segment 3) when there are too few of them to give every
-  // SM eight warps; MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
+  // SM eight warps, and always in the FMA form (its blocked CTA kernel); MFG_LU_CTA = 0 / 1 forces
+  // the warp / CTA form.
   long long big = 0;
   for (int i = 0; i < count; i++) big += p->hn[i] > mfg::SMEM_N ? 1 : 0;
   const int cta_env = env_int("MFG_LU_CTA", -1);
-  const bool cta = cta_env >= 0 ? cta_env == 1 : big < 8LL * ctx->sm_count;
+  const bool cta = cta_env >= 0 ? cta_env == 1 : (p->args.fma || big < 8LL * ctx->sm_count);
   for (int i = 0; i < count;) {
     int j = i;
     while (j < count && p->hn[idx[j]] == p->hn[idx[i]]) j++;
@@ -441,10 +453,6 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
     p->fma_stride = std::max(p->fma_stride, (1LL << sg) * nm * nm);   // segment sg: 32 >> sg lanes
   }
   p->fma_stride = (p->fma_stride + 31) / 32 * 32;
-  if (p->args.fma) {
-    const int rc = fma_backup_reserve(p);
-    if (rc != MFG_OK) return rc;
-  }
   std::vector<int> order, first, gc;
   order.reserve(count);
   for (int sg = 0; sg < 5; sg++) {
@@ -462,6 +470,10 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
     }
   }
   p->gsel = gsel;
+  if (p->args.fma) {
+    const int rc = fma_backup_reserve(p);
+    if (rc != MFG_OK) return rc;
+  }
   if (count > 0) {
     MFG_CUDA(ctx, cudaMemcpy((void*)p->args.order, order.data(), sizeof(int) * count,
                              cudaMemcpyHostToDevice));
@@ -540,11 +552,13 @@ int plan_reshape(mfg_plan* p, int warps, int wps, int group, int mul, int dot_bl
 }
 
 int plan_set_fma(mfg_plan* p, int on) {
+  const bool changed = p->args.fma != (on ? 1 : 0);
   p->args.fma = on ? 1 : 0;
   p->qd.fma = p->args.fma;
-  if (p->kind == mfg_plan::GETRF && on) {
-    if (p->gsel < 0) {
-      const int rc = getrf_build_tasks(p, 0);
+  if (p->kind == mfg_plan::GETRF && (on || changed)) {
+    // Tasks are needed in the FMA form, and the segment of orders above SMEM_N depends on the form.
+    if (p->gsel < 0 || (changed && p->max_n > mfg::SMEM_N)) {
+      const int rc = getrf_build_tasks(p, p->gsel < 0 ? 0 : p->gsel);
       if (rc != MFG_OK) return rc;
     }
     const int rc = fma_backup_reserve(p);
@@ -622,12 +636,12 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
         if (ctas < 1) ctas = 1;
         e = mfg::launch_getrf_blk(a, ctas, p->blk_w, blk_smem_bytes(p), s);
       } else if (sg == 3) {
-        // One matrix per CTA: the CTA kernel counts its work items in `count`.
+        // One matrix per CTA: the CTA kernel counts its work items in `count`; the FMA form
+        // runs the blocked kernel.
         a.count = a.ntasks;
-        const long long slices = (long long)p->ctas * p->warps;   // scratch slices
-        const int ctas = (int)std::max<long long>(
-            1, std::min<long long>({(long long)a.ntasks, 2LL * ctx->sm_count, slices}));
-        e = mfg::launch_getrf_cta(a, ctas, p->cta_nmax, s);
+        const int ctas = (int)getrf_cta_ctas(p);
+        e = p->args.fma ? mfg::launch_getrf_big_fma(a, ctas, p->cta_nmax, s)
+                        : mfg::launch_getrf_cta(a, ctas, p->cta_nmax, s);
       } else {
         const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
         const int ctas = (int)std::max<long long>(1, std::min<long long>(p->ctas, need));

@@ -177,3 +177,88 @@ def test_lu_fma_padded_and_large_orders(mf, big):
         U = np.triu(F)
         An = A[:ni, :]
         assert np.linalg.norm(An[p, :] - L @ U, 1) / np.linalg.norm(An, 1) <= 1e-13 * ni, i
+
+
+def test_lu_fma_blocked_large_orders(mf):
+    """Orders above 128 in the FMA form run the blocked CTA kernel (panels of 32 columns, U12
+    solve, 64 x 64 trailing-update tiles): pivots and signs identical to the oracle's, factors and
+    solutions backward stable, padding rows untouched; a near-tie and a NaN at large orders are
+    redone in MatFlat's arithmetic (the oracle's bits); solve-only calls give the fused call's
+    bits; the exact form afterwards gives MatFlat's bits."""
+    import torch
+    rng = np.random.default_rng(330)
+    n = np.array([129, 160, 191, 200, 256, 257, 300, 333, 384, 512, 97, 64, 450, 130],
+                 np.int32)
+    count = len(n)
+    lda = (n + rng.integers(0, 4, size=count)).astype(np.int32)
+    sz = lda.astype(np.int64) * n
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    a = rng.standard_normal(int(sz.sum()))
+
+    def mat(i):
+        return a[a_off[i]:a_off[i] + sz[i]].reshape(n[i], lda[i]).T
+
+    mat(5)[7, 0] = 50.0
+    mat(5)[90, 0] = -50.0 * (1.0 + 2.0 ** -45)        # near-tie in column 0: redone exactly
+    mat(7)[200, 150] = np.nan                          # NaN: redone exactly
+    special = [5, 7]
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    nrhs = 2
+    b_off = piv_off * nrhs
+    b = rng.standard_normal(int(n.sum()) * nrhs)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=nrhs, b_off=b_off, lda=lda)
+    batch.set_form("fma")
+    da, db = _dev(a), _dev(b)
+    dpiv = torch.zeros(int(n.sum()), dtype=torch.int32, device="cuda")
+    dsign = torch.zeros(count, dtype=torch.int32, device="cuda")
+    dinfo = torch.zeros(count, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, db, dsign, dinfo)
+    mf.context().synchronize()
+    assert batch.form_fallbacks() == len(special)
+    ga, gb, gpiv, gsign = _host(da), _host(db), _host(dpiv), _host(dsign)
+    assert not _host(dinfo)[[i for i in range(count) if i not in special]].any()
+    for i in range(count):
+        ni, li = int(n[i]), int(lda[i])
+        A = mat(i)
+        oa = a[a_off[i]:a_off[i] + sz[i]].copy()
+        opiv = np.zeros(ni, np.int32)
+        osign = oracle.lu(ni, ni, oa, li, opiv)
+        p = gpiv[piv_off[i]:piv_off[i] + ni]
+        np.testing.assert_array_equal(p, opiv, err_msg="matrix %d" % i)
+        assert gsign[i] == osign, i
+        F = ga[a_off[i]:a_off[i] + sz[i]].reshape(ni, li).T
+        np.testing.assert_array_equal(F[ni:li, :], A[ni:li, :])     # padding untouched
+        if i in special:
+            assert_bits(ga[a_off[i]:a_off[i] + sz[i]], oa, "fallback matrix %d" % i)
+            continue
+        F = F[:ni, :]
+        L = np.tril(F, -1) + np.eye(ni)
+        U = np.triu(F)
+        An = A[:ni, :]
+        assert np.linalg.norm(An[p, :] - L @ U, 1) / np.linalg.norm(An, 1) <= 1e-13 * ni, i
+        for r in range(nrhs):
+            bs = slice(b_off[i] + r * ni, b_off[i] + (r + 1) * ni)
+            x, bi = gb[bs], b[bs]
+            ex = np.linalg.norm(bi - An @ x, 1) / (np.linalg.norm(An, 1) * np.linalg.norm(x, 1) +
+                                                   np.linalg.norm(bi, 1))
+            assert ex <= 1e-13 * ni, (i, r, ex)
+    # solve-only on the factors: the fused call's solutions bit for bit
+    db2 = _dev(b)
+    torch.cuda.synchronize()
+    batch.solve(da, dpiv, db2)
+    mf.context().synchronize()
+    assert_bits(_host(db2), gb)
+    # back to the exact form: MatFlat's bits on every matrix
+    batch.set_form("exact")
+    da = _dev(a)
+    torch.cuda.synchronize()
+    batch.run(da, dpiv, _dev(b), dsign, dinfo)
+    mf.context().synchronize()
+    ga = _host(da)
+    for i in (0, 4, 9):
+        ni, li = int(n[i]), int(lda[i])
+        oa = a[a_off[i]:a_off[i] + sz[i]].copy()
+        oracle.lu(ni, ni, oa, li, np.zeros(ni, np.int32))
+        assert_bits(ga[a_off[i]:a_off[i] + sz[i]], oa, "exact matrix %d" % i)
+    assert batch.form_fallbacks() == 0
