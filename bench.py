@@ -570,6 +570,27 @@ def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, 
     plain_ms = p0.elapsed_time(p1)
     plain_x = b2.reshape(count, n)
     pfe = ((plain_x - xt).abs().amax(1) / xt.abs().amax(1)).cpu().numpy()
+    exact_piv = piv.clone()
+    # The same plan in the FMA form (the plain form of the metric: MatFlat's pivots, backward-
+    # stable factors; orders above 128 run the blocked CTA kernel).
+    plain.set_form("fma")
+    with torch.cuda.stream(stream):
+        a2.copy_(a)
+        b2.copy_(b)
+        plain.run(a2, piv, b2, sign, pinfo)      # warm-up
+        a2.copy_(a)
+        b2.copy_(b)
+        p0.record(stream)
+        plain.run(a2, piv, b2, sign, pinfo)
+        p1.record(stream)
+        stream.synchronize()
+    fma_ms = p0.elapsed_time(p1)
+    fma_fe = ((b2.reshape(count, n) - xt).abs().amax(1) / xt.abs().amax(1)).cpu().numpy()
+    fma_plain = {"value": count / (fma_ms / 1e3), "unit": "solves/s", "ms": fma_ms,
+                 "fwd_err_max": float(np.max(fma_fe)),
+                 "pivots_identical_to_exact": bool(torch.equal(piv, exact_piv)),
+                 "redone_exact": plain.form_fallbacks()}
+    del exact_piv
     hist = {int(k): int(v) for k, v in zip(*np.unique(it, return_counts=True))}
 
     cpu = None
@@ -607,7 +628,9 @@ def measure_mixed(torch, mf, stream, count, n, cond, lowp, steps, warmup, seed, 
         "singular": int((inf == 2).sum()),
         "fp64_plain": {"value": count / (plain_ms / 1e3), "unit": "solves/s", "ms": plain_ms,
                        "fwd_err_max": float(np.max(pfe))},
+        "fp64_plain_fma": fma_plain,
         "speedup_vs_fp64_plain": plain_ms / ms,
+        "speedup_vs_fp64_plain_fma": fma_ms / ms,
         "flops": count * (2.0 * n ** 3 / 3),
         "e2e": e2e, "cpu": cpu, "clocks": clocks.summary(),
     }
@@ -640,7 +663,8 @@ def run_mixed(args, torch, mf, world, rank, local):
             "cpu_baseline": r["cpu"], "e2e": r["e2e"], "clocks": r["clocks"],
         }
         for k in ("berr_max", "berr_median", "fwd_err_max", "fwd_err_median", "iters_histogram",
-                  "fallback_fp64", "singular", "fp64_plain", "speedup_vs_fp64_plain"):
+                  "fallback_fp64", "singular", "fp64_plain", "speedup_vs_fp64_plain",
+                  "fp64_plain_fma", "speedup_vs_fp64_plain_fma"):
             line[k] = r[k]
         print(json.dumps(line), flush=True)
 
@@ -1339,11 +1363,14 @@ def main():
                  "fp64_plain_value": world * mcfg["count"] / (r["fp64_plain"]["ms"] / 1e3),
                  "fp64_plain_ms": r["fp64_plain"]["ms"],
                  "speedup_vs_fp64_plain": r["fp64_plain"]["ms"] / r["ms"],
+                 "fp64_plain_fma": r["fp64_plain_fma"],
+                 "speedup_vs_fp64_plain_fma": r["fp64_plain_fma"]["ms"] / r["ms"],
                  "berr_max": r["berr_max"], "berr_median": r["berr_median"],
                  "fwd_err_max": r["fwd_err_max"], "fp64_plain_fwd_err_max": r["fp64_plain"]["fwd_err_max"],
                  "iters_histogram": r["iters_histogram"], "fallback_fp64": r["fallback_fp64"],
                  "timing": "CUDA events on the solver's stream, 3 warm-up + 3 timed solves; "
-                           "plain rate: one timed exact FP64 LU + solve of the same systems"}
+                           "plain rates: one timed FP64 LU + solve of the same systems in the "
+                           "exact form and one in the FMA form"}
 
     # ---- the Cholesky half of the metric (100,000 SPD matrices n~U{8..128}) -------------------
     cholesky = None

@@ -30,8 +30,11 @@ constexpr int BIG_NB = 32;             // panel width
 constexpr int BIG_TM = 64;             // trailing-update tile: BIG_TM x BIG_TM, 4 x 4 per thread
 
 struct BigSmem {
-  double as[BIG_NB][BIG_TM];           // L21 tile, k-major (L11 during the U12 solve)
-  double bs[BIG_NB][BIG_TM + 1];       // U12 tile, k-major (odd row length: fewer bank conflicts)
+  // L21 and U12 tiles, k-major, each row permuted so that the 4 rows (columns) a thread works on
+  // are adjacent: tile row (column) rr = t + 16 u sits at 4 t + u, read as two 16-byte loads.
+  // as also holds L11 (unpermuted) during the U12 solve.
+  double as[BIG_NB][BIG_TM];
+  double bs[BIG_NB][BIG_TM + 2];
   double uj[BIG_NB];                   // row j of the panel after the swap
   unsigned long long pk[BIG_W];        // per warp: largest key, runner-up, its row, non-finite
   unsigned long long q[BIG_W];
@@ -215,22 +218,24 @@ __device__ void big_update(double* a, int n, long long lda, int j0, BigSmem& sm)
       const int k = e / BIG_TM;
       const int rr = e - k * BIG_TM;
       const int i = r0 + rr;
-      sm.as[k][rr] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
+      sm.as[k][4 * (rr & 15) + (rr >> 4)] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
     }
     for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
       const int cc = e / BIG_NB;
       const int k = e - cc * BIG_NB;
       const int jj = c0 + cc;
-      sm.bs[k][cc] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
+      sm.bs[k][4 * (cc & 15) + (cc >> 4)] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
     }
     __syncthreads();
 #pragma unroll 4
     for (int k = 0; k < BIG_NB; ++k) {
       double av[4], bv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) av[u] = sm.as[k][tx + 16 * u];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) bv[v] = sm.bs[k][ty + 16 * v];
+      const double2 a01 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx]);
+      const double2 a23 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx + 2]);
+      const double2 b01 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty]);
+      const double2 b23 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty + 2]);
+      av[0] = a01.x, av[1] = a01.y, av[2] = a23.x, av[3] = a23.y;
+      bv[0] = b01.x, bv[1] = b01.y, bv[2] = b23.x, bv[3] = b23.y;
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
 #pragma unroll
@@ -285,7 +290,10 @@ __device__ __noinline__ void big_fallback(double* a, int n, long long lda, const
 // Work items: the plan's tasks (one matrix each, p.ntasks of them, taken from p.queue).  Per CTA:
 // a copy of up to bstride doubles in p.fbackup and a slice of p.gscratch (the solve's staging and
 // the fallback's column sums).
-__global__ void __launch_bounds__(BIG_T, 2) getrf_big_fma_kernel(BatchArgs p, long long bstride) {
+// MINB: resident CTAs per SM the register allocation is bounded for (2: 128 registers, 3: 80).
+template <int MINB>
+__global__ void __launch_bounds__(BIG_T, MINB) getrf_big_fma_kernel(BatchArgs p,
+                                                                   long long bstride) {
   __shared__ BigSmem sm;
   const int tid = threadIdx.x;
   double* slice = p.gscratch + (long long)blockIdx.x * p.gscratch_stride;
@@ -327,11 +335,15 @@ long long getrf_big_backup_doubles(int nmax) {
   return ((long long)nmax * nmax + 31) / 32 * 32;
 }
 
-cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, cudaStream_t s) {
+cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps,
+                                 cudaStream_t s) {
   if (ctas < 1 || nmax < 1 || !args.fbackup || !args.fcount || !args.gscratch ||
       args.gscratch_stride < warp_scratch_doubles(nmax))
     return cudaErrorInvalidValue;
-  getrf_big_fma_kernel<<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
+  if (cps >= 3)
+    getrf_big_fma_kernel<3><<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
+  else
+    getrf_big_fma_kernel<2><<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
   return cudaGetLastError();
 }
 

@@ -283,7 +283,9 @@ cudaError_t init_getrf_fma_attributes();
 // FMA form for orders above SMEM_N (lu_big.cu): one matrix per CTA, blocked right-looking, over
 // the task list (one matrix per task).  Needs args.fbackup (getrf_big_backup_doubles(nmax) per
 // launched CTA), args.fcount and args.gscratch (a slice of warp_scratch_doubles(nmax) per CTA).
-cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, cudaStream_t s);
+// cps: CTAs per SM the launch is sized for (2 or 3: selects the register bound).
+cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps,
+                                 cudaStream_t s);
 long long getrf_big_backup_doubles(int nmax);
 // Resident form: one matrix per CTA of w warps (2, 4 or 8) over the task list (one matrix per
 // task), the matrix held in smem_bytes of dynamic shared memory when it fits.

@@ -151,6 +151,7 @@ struct mfg_plan {
   // args.group); segment s of `order` holds the matrices of G = 32 >> s lanes.
   int csel = 0;
   int cta_nmax = 0;  // GETRF: largest order of the CTA-per-matrix segment (segment 3)
+  int big_cps = 3;   // GETRF FMA form: CTAs per SM of the blocked kernel (2 or 3; MFG_LU_BIG_CPS)
   // GETRF (double): resident form (segment 4): orders in [blk_lo, SMEM_N] go to one CTA of blk_w
   // warps each, blk_cps CTAs per SM, the matrix in shared memory; blk_lo = 0: off.
   int blk_lo = 0;
@@ -368,12 +369,13 @@ int potrf_build_segments(mfg_plan* p, int csel) {
   return MFG_OK;
 }
 
-// CTAs of a GETRF plan's CTA-per-matrix launch (segment 3): at most two per SM and one per
-// scratch slice.
+// CTAs of a GETRF plan's CTA-per-matrix launch (segment 3): at most two per SM (the FMA form's
+// blocked kernel: big_cps) and one per scratch slice.
 long long getrf_cta_ctas(const mfg_plan* p) {
   const long long slices = (long long)p->ctas * p->warps;
+  const long long cps = p->args.fma ? p->big_cps : 2;
   return std::max<long long>(
-      1, std::min<long long>({(long long)p->seg_cnt[3], 2LL * p->ctx->sm_count, slices}));
+      1, std::min<long long>({(long long)p->seg_cnt[3], cps * p->ctx->sm_count, slices}));
 }
 
 // The FMA form's per-warp copies of a GETRF plan: fma_stride doubles for every warp its launches
@@ -640,7 +642,7 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
         // runs the blocked kernel.
         a.count = a.ntasks;
         const int ctas = (int)getrf_cta_ctas(p);
-        e = p->args.fma ? mfg::launch_getrf_big_fma(a, ctas, p->cta_nmax, s)
+        e = p->args.fma ? mfg::launch_getrf_big_fma(a, ctas, p->cta_nmax, p->big_cps, s)
                         : mfg::launch_getrf_cta(a, ctas, p->cta_nmax, s);
       } else {
         const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
@@ -904,6 +906,8 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
         p->blk_cps = std::max(1, std::min(cps, 16));
       }
     }
+    // The FMA form's blocked kernel for orders above SMEM_N: CTAs per SM (2 or 3).
+    p->big_cps = env_int("MFG_LU_BIG_CPS", 3) == 2 ? 2 : 3;
     if (gsel >= 0) {
       const int rc = getrf_build_tasks(p, gsel);
       if (rc != MFG_OK) {
