@@ -10,10 +10,10 @@
 //      must beat the runner-up's by LU_FMA_MARGIN_ULPS, every candidate finite, the pivot not
 //      zero), whole-row swap (MatFlat swaps whole rows, Lu.cs:332-337), scaling by the pivot's
 //      reciprocal, rank-1 update of the panel's later columns;
-//   2. U12 = L11^-1 A12 for the trailing columns (unit lower 32 x 32 from shared memory, one column
-//      per thread in registers);
-//   3. A22 -= L21 U12 in 64 x 64 tiles, both operands staged in shared memory, 4 x 4 fused
-//      multiply-adds per thread and k.
+//   2. per block of 64 trailing columns: U12 = L11^-1 A12 solved in shared memory (unit lower
+//      32 x 32 L11 from shared memory), written back and kept on chip for
+//   3. A22 -= L21 U12 in 64 x 64 tiles down the trailing rows, L21 staged in shared memory too,
+//      4 x 4 fused multiply-adds per thread and k.
 // A matrix whose screen fails at any column is restored from the copy the CTA took before
 // factoring it and redone in MatFlat's arithmetic (lu_cta_early: the exact CTA schedule, MatFlat's
 // bits).  The solves are getrs_fma's column sweeps for every matrix, so solve-only calls reproduce
@@ -31,10 +31,11 @@ constexpr int BIG_TM = 64;             // trailing-update tile: BIG_TM x BIG_TM,
 
 struct BigSmem {
   // L21 and U12 tiles, k-major, each row permuted so that the 4 rows (columns) a thread works on
-  // are adjacent: tile row (column) rr = t + 16 u sits at 4 t + u, read as two 16-byte loads.
-  // as also holds L11 (unpermuted) during the U12 solve.
+  // are adjacent: tile row (column) rr = t + 16 u sits at 4 t + u (big_pos), read as two 16-byte
+  // loads.
   double as[BIG_NB][BIG_TM];
   double bs[BIG_NB][BIG_TM + 2];
+  double l11[BIG_NB][BIG_NB + 1];      // L11 of the panel, row-major
   double uj[BIG_NB];                   // row j of the panel after the swap
   unsigned long long pk[BIG_W];        // per warp: largest key, runner-up, its row, non-finite
   unsigned long long q[BIG_W];
@@ -173,84 +174,90 @@ __device__ bool big_panel(double* a, int n, long long lda, int j0, int j1, int* 
   return true;
 }
 
-// U12 = L11^-1 A12: rows [j0, j0 + BIG_NB) of the columns [j0 + BIG_NB, n).
-__device__ void big_u12(double* a, int n, long long lda, int j0, BigSmem& sm) {
-  const int tid = threadIdx.x;
-  for (int e = tid; e < BIG_NB * BIG_NB; e += BIG_T) {
-    const int k = e / BIG_NB;
-    const int r = e - k * BIG_NB;
-    sm.as[k][r] = a[(long long)(j0 + k) * lda + j0 + r];
-  }
-  __syncthreads();
-  // One column per thread, row by row from the thread's own 32 values (L1-resident): a column
-  // held in registers (64 of them) with the solve unrolled spills under the two-CTA register bound.
-  for (int col = j0 + BIG_NB + tid; col < n; col += BIG_T) {
-    double* cp = a + (long long)col * lda + j0;
-    for (int r = 1; r < BIG_NB; ++r) {
-      double v = cp[r];
-#pragma unroll 8
-      for (int k = 0; k < r; ++k) v = __fma_rn(-sm.as[k][r], cp[k], v);
-      cp[r] = v;
-    }
-  }
-  __syncthreads();
-}
+// Position of tile column (row) cc in a permuted shared row: 4 (cc mod 16) + cc / 16.
+__device__ __forceinline__ int big_pos(int cc) { return 4 * (cc & 15) + (cc >> 4); }
 
-// A22 -= L21 U12 for the rows and columns [j1, n), j1 = j0 + BIG_NB.
-__device__ void big_update(double* a, int n, long long lda, int j0, BigSmem& sm) {
+// U12 = L11^-1 A12 and A22 -= L21 U12 for the rows and columns [j1, n), j1 = j0 + BIG_NB, one
+// block of BIG_TM trailing columns at a time: the block's U12 rows are solved in shared memory
+// (one column per thread of the first BIG_TM, from L11 in shared memory), written back, and kept
+// in shared memory for the block's BIG_TM x BIG_TM update tiles down the trailing rows.
+__device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem& sm) {
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int j1 = j0 + BIG_NB;
   const int mt = (n - j1 + BIG_TM - 1) / BIG_TM;
-  for (int tile = 0; tile < mt * mt; ++tile) {
-    const int r0 = j1 + (tile % mt) * BIG_TM;
-    const int c0 = j1 + (tile / mt) * BIG_TM;
-    double acc[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
-        acc[u][v] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
-      }
-    }
-    for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
-      const int k = e / BIG_TM;
-      const int rr = e - k * BIG_TM;
-      const int i = r0 + rr;
-      sm.as[k][4 * (rr & 15) + (rr >> 4)] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
-    }
+  for (int e = tid; e < BIG_NB * BIG_NB; e += BIG_T) {
+    const int k = e / BIG_NB;
+    const int r = e - k * BIG_NB;
+    sm.l11[r][k] = a[(long long)(j0 + k) * lda + j0 + r];
+  }
+  for (int cb = 0; cb < mt; ++cb) {
+    const int c0 = j1 + cb * BIG_TM;
     for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
       const int cc = e / BIG_NB;
       const int k = e - cc * BIG_NB;
       const int jj = c0 + cc;
-      sm.bs[k][4 * (cc & 15) + (cc >> 4)] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
+      sm.bs[k][big_pos(cc)] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
     }
     __syncthreads();
-#pragma unroll 4
-    for (int k = 0; k < BIG_NB; ++k) {
-      double av[4], bv[4];
-      const double2 a01 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx]);
-      const double2 a23 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx + 2]);
-      const double2 b01 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty]);
-      const double2 b23 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty + 2]);
-      av[0] = a01.x, av[1] = a01.y, av[2] = a23.x, av[3] = a23.y;
-      bv[0] = b01.x, bv[1] = b01.y, bv[2] = b23.x, bv[3] = b23.y;
+    if (tid < BIG_TM) {
+      for (int r = 1; r < BIG_NB; ++r) {
+        double v = sm.bs[r][tid];
+#pragma unroll 8
+        for (int k = 0; k < r; ++k) v = __fma_rn(-sm.l11[r][k], sm.bs[k][tid], v);
+        sm.bs[r][tid] = v;
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
+      const int cc = e / BIG_NB;
+      const int k = e - cc * BIG_NB;
+      const int jj = c0 + cc;
+      if (jj < n) a[(long long)jj * lda + j0 + k] = sm.bs[k][big_pos(cc)];
+    }
+    for (int rb = 0; rb < mt; ++rb) {
+      const int r0 = j1 + rb * BIG_TM;
+      double acc[4][4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = __fma_rn(-av[u], bv[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) {
+          const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+          acc[u][v] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
+        }
       }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
-        if (i < n && jj < n) a[(long long)jj * lda + i] = acc[u][v];
+      for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
+        const int k = e / BIG_TM;
+        const int rr = e - k * BIG_TM;
+        const int i = r0 + rr;
+        sm.as[k][big_pos(rr)] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
       }
+      __syncthreads();
+#pragma unroll 4
+      for (int k = 0; k < BIG_NB; ++k) {
+        double av[4], bv[4];
+        const double2 a01 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx]);
+        const double2 a23 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx + 2]);
+        const double2 b01 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty]);
+        const double2 b23 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty + 2]);
+        av[0] = a01.x, av[1] = a01.y, av[2] = a23.x, av[3] = a23.y;
+        bv[0] = b01.x, bv[1] = b01.y, bv[2] = b23.x, bv[3] = b23.y;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = __fma_rn(-av[u], bv[v], acc[u][v]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+          if (i < n && jj < n) a[(long long)jj * lda + i] = acc[u][v];
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -263,10 +270,7 @@ __device__ bool big_lu_fma(double* a, int n, long long lda, int* piv, int& sign,
   for (int j0 = 0; j0 < n; j0 += BIG_NB) {
     const int j1 = min(n, j0 + BIG_NB);
     if (!big_panel(a, n, lda, j0, j1, piv, sign, sm)) return false;
-    if (j1 < n) {
-      big_u12(a, n, lda, j0, sm);
-      big_update(a, n, lda, j0, sm);
-    }
+    if (j1 < n) big_u12_update(a, n, lda, j0, sm);
   }
   return true;
 }

@@ -136,15 +136,16 @@ def test_lu_fma_host_buffers_and_autotune(mf):
 
 @pytest.mark.parametrize("big", [False, True], ids=["cta-bucket", "task-bucket"])
 def test_lu_fma_padded_and_large_orders(mf, big):
-    """lda > n, and orders above 128: few of them run in the exact CTA-per-matrix kernel, many of
-    them in the FMA form's 32-lane tasks (scratch in global memory).  Pivots identical to the
-    oracle's, factors backward stable."""
+    """lda > n, and orders above 128: few of them run in the FMA form's blocked CTA kernel;
+    many of them in 32-lane tasks (scratch in global memory) up to order 176 and in the blocked
+    kernel above.  Pivots identical to the oracle's, factors backward stable."""
     import torch
     rng = np.random.default_rng(320 + big)
     count = 1400 if big else 120
     n = rng.integers(1, 141, size=count).astype(np.int32)
     if big:
         n[:1300] = rng.integers(129, 141, size=1300)
+        n[1300:1350] = rng.integers(177, 201, size=50)     # the blocked CTA kernel beside them
     lda = (n + rng.integers(0, 4, size=count)).astype(np.int32)
     sz = lda.astype(np.int64) * n
     a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
