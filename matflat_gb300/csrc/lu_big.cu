@@ -177,13 +177,96 @@ __device__ bool big_panel(double* a, int n, long long lda, int j0, int j1, int* 
 // Position of tile column (row) cc in a permuted shared row: 4 (cc mod 16) + cc / 16.
 __device__ __forceinline__ int big_pos(int cc) { return 4 * (cc & 15) + (cc >> 4); }
 
+// d = a b + d for one 8 x 8 x 4 double tile on the FP64 tensor pipe (mma.sync m8n8k4 f64): a is
+// the lane's element A(lane / 4, lane % 4) of the 8 x 4 operand, b its element B(lane % 4,
+// lane / 4) of the 4 x 8 operand, d its elements D(lane / 4, 2 (lane % 4) + {0, 1}).
+__device__ __forceinline__ void dmma_8x8x4(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+// Fragment order of a k-major 32 x 64 tile for the tensor-pipe update: element (k, rr) (rr the
+// tile row of L21, or the tile column of U12) sits where lane (rr mod 8) 4 + (k mod 4) of the
+// warp reads it for k-step k / 4 and 8-wide block rr / 8, so a fragment is 32 consecutive doubles.
+__device__ __forceinline__ int big_frag(int k, int rr) {
+  return (((k >> 2) * 8 + (rr >> 3)) << 5) + ((rr & 7) << 2) + (k & 3);
+}
+
+// A22 -= L21 U12 on the FP64 tensor pipe for the BIG_TM columns from c0, down the trailing rows
+// from j1 (mt tiles); bsf holds U12's block in fragment order.  Warp w computes tile rows
+// 16 (w mod 4) + [0, 16) and columns 32 (w / 4) + [0, 32).
+__device__ __forceinline__ void big_tiles_mma(double* a, int n, long long lda, int j0, int j1,
+                                              int c0, int mt, double* asf, const double* bsf) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 3) * 2;      // the warp's first 8-row block of the tile
+  const int wn = (warp >> 2) * 4;     // its first 8-column block
+  const int fr = lane >> 2;           // the lane's row of an accumulator tile
+  const int fc = (lane & 3) * 2;      // its first column
+  for (int rb = 0; rb < mt; ++rb) {
+    const int r0 = j1 + rb * BIG_TM;
+    double acc[2][4][2];
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi) {
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int i = r0 + (wm + mi) * 8 + fr, jj = c0 + (wn + ni) * 8 + fc + h;
+          acc[mi][ni][h] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
+        }
+      }
+    }
+    for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
+      const int k = e / BIG_TM;
+      const int rr = e - k * BIG_TM;
+      const int i = r0 + rr;
+      asf[big_frag(k, rr)] = i < n ? -a[(long long)(j0 + k) * lda + i] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int ks = 0; ks < BIG_NB / 4; ++ks) {
+      double af[2], bf[4];
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi) af[mi] = asf[((ks * 8 + wm + mi) << 5) + lane];
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) bf[ni] = bsf[((ks * 8 + wn + ni) << 5) + lane];
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi) {
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+          dmma_8x8x4(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+      }
+    }
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi) {
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int i = r0 + (wm + mi) * 8 + fr, jj = c0 + (wn + ni) * 8 + fc + h;
+          if (i < n && jj < n) a[(long long)jj * lda + i] = acc[mi][ni][h];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // U12 = L11^-1 A12 and A22 -= L21 U12 for the rows and columns [j1, n), j1 = j0 + BIG_NB, one
 // block of BIG_TM trailing columns at a time: the block's U12 rows are solved in shared memory
 // (one column per thread of the first BIG_TM, from L11 in shared memory), written back, and kept
 // in shared memory for the block's BIG_TM x BIG_TM update tiles down the trailing rows.
+// MMA: the tiles on the FP64 tensor pipe (each warp 16 x 32 of the tile as 2 x 4 mma tiles of
+// 8 x 8, operands in fragment order, big_frag); otherwise 4 x 4 fused multiply-adds per thread
+// (operands in big_pos order).
+template <bool MMA>
 __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem& sm) {
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
+  double* asf = &sm.as[0][0];
+  double* bsf = &sm.bs[0][0];
   const int j1 = j0 + BIG_NB;
   const int mt = (n - j1 + BIG_TM - 1) / BIG_TM;
   for (int e = tid; e < BIG_NB * BIG_NB; e += BIG_T) {
@@ -197,15 +280,20 @@ __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem&
       const int cc = e / BIG_NB;
       const int k = e - cc * BIG_NB;
       const int jj = c0 + cc;
-      sm.bs[k][big_pos(cc)] = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
+      const double v = jj < n ? a[(long long)jj * lda + j0 + k] : 0.0;
+      if constexpr (MMA) bsf[big_frag(k, cc)] = v;
+      else sm.bs[k][big_pos(cc)] = v;
     }
     __syncthreads();
     if (tid < BIG_TM) {
+      // Thread tid solves the column stored at position tid (MMA: tile column tid).
       for (int r = 1; r < BIG_NB; ++r) {
-        double v = sm.bs[r][tid];
+        double* vr = MMA ? bsf + big_frag(r, tid) : &sm.bs[r][tid];
+        double v = *vr;
 #pragma unroll 8
-        for (int k = 0; k < r; ++k) v = __fma_rn(-sm.l11[r][k], sm.bs[k][tid], v);
-        sm.bs[r][tid] = v;
+        for (int k = 0; k < r; ++k)
+          v = __fma_rn(-sm.l11[r][k], MMA ? bsf[big_frag(k, tid)] : sm.bs[k][tid], v);
+        *vr = v;
       }
     }
     __syncthreads();
@@ -213,7 +301,11 @@ __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem&
       const int cc = e / BIG_NB;
       const int k = e - cc * BIG_NB;
       const int jj = c0 + cc;
-      if (jj < n) a[(long long)jj * lda + j0 + k] = sm.bs[k][big_pos(cc)];
+      if (jj < n) a[(long long)jj * lda + j0 + k] = MMA ? bsf[big_frag(k, cc)] : sm.bs[k][big_pos(cc)];
+    }
+    if constexpr (MMA) {
+      big_tiles_mma(a, n, lda, j0, j1, c0, mt, asf, bsf);
+      continue;
     }
     for (int rb = 0; rb < mt; ++rb) {
       const int r0 = j1 + rb * BIG_TM;
@@ -263,6 +355,7 @@ __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem&
 
 // The whole factorization in the FMA form; false when a column failed the screen (the matrix is
 // then partly factored and must be restored).
+template <bool MMA>
 __device__ bool big_lu_fma(double* a, int n, long long lda, int* piv, int& sign, BigSmem& sm) {
   for (int i = threadIdx.x; i < n; i += BIG_T) piv[i] = i;
   sign = 1;
@@ -270,7 +363,7 @@ __device__ bool big_lu_fma(double* a, int n, long long lda, int* piv, int& sign,
   for (int j0 = 0; j0 < n; j0 += BIG_NB) {
     const int j1 = min(n, j0 + BIG_NB);
     if (!big_panel(a, n, lda, j0, j1, piv, sign, sm)) return false;
-    if (j1 < n) big_u12_update(a, n, lda, j0, sm);
+    if (j1 < n) big_u12_update<MMA>(a, n, lda, j0, sm);
   }
   return true;
 }
@@ -295,7 +388,7 @@ __device__ __noinline__ void big_fallback(double* a, int n, long long lda, const
 // a copy of up to bstride doubles in p.fbackup and a slice of p.gscratch (the solve's staging and
 // the fallback's column sums).
 // MINB: resident CTAs per SM the register allocation is bounded for (2: 128 registers, 3: 80).
-template <int MINB>
+template <int MINB, bool MMA>
 __global__ void __launch_bounds__(BIG_T, MINB) getrf_big_fma_kernel(BatchArgs p,
                                                                    long long bstride) {
   __shared__ BigSmem sm;
@@ -319,7 +412,7 @@ __global__ void __launch_bounds__(BIG_T, MINB) getrf_big_fma_kernel(BatchArgs p,
         for (int i = tid; i < n; i += BIG_T)
           __stcs(bk + (long long)j * n + i, a[(long long)j * lda + i]);
       __syncthreads();
-      if (!big_lu_fma(a, n, lda, piv, sign, sm)) {
+      if (!big_lu_fma<MMA>(a, n, lda, piv, sign, sm)) {
         big_fallback(a, n, lda, bk, piv, slice, &sign, &info, &sm.red);
         if (tid == 0) atomicAdd(p.fcount, 1);
       }
@@ -339,15 +432,20 @@ long long getrf_big_backup_doubles(int nmax) {
   return ((long long)nmax * nmax + 31) / 32 * 32;
 }
 
-cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps,
+cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps, bool mma,
                                  cudaStream_t s) {
   if (ctas < 1 || nmax < 1 || !args.fbackup || !args.fcount || !args.gscratch ||
       args.gscratch_stride < warp_scratch_doubles(nmax))
     return cudaErrorInvalidValue;
-  if (cps >= 3)
-    getrf_big_fma_kernel<3><<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
+  const long long bs = getrf_big_backup_doubles(nmax);
+  if (cps >= 3 && mma)
+    getrf_big_fma_kernel<3, true><<<ctas, BIG_T, 0, s>>>(args, bs);
+  else if (cps >= 3)
+    getrf_big_fma_kernel<3, false><<<ctas, BIG_T, 0, s>>>(args, bs);
+  else if (mma)
+    getrf_big_fma_kernel<2, true><<<ctas, BIG_T, 0, s>>>(args, bs);
   else
-    getrf_big_fma_kernel<2><<<ctas, BIG_T, 0, s>>>(args, getrf_big_backup_doubles(nmax));
+    getrf_big_fma_kernel<2, false><<<ctas, BIG_T, 0, s>>>(args, bs);
   return cudaGetLastError();
 }
 

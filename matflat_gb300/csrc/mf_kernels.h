@@ -283,8 +283,9 @@ cudaError_t init_getrf_fma_attributes();
 // FMA form for orders above SMEM_N (lu_big.cu): one matrix per CTA, blocked right-looking, over
 // the task list (one matrix per task).  Needs args.fbackup (getrf_big_backup_doubles(nmax) per
 // launched CTA), args.fcount and args.gscratch (a slice of warp_scratch_doubles(nmax) per CTA).
-// cps: CTAs per SM the launch is sized for (2 or 3: selects the register bound).
-cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps,
+// cps: CTAs per SM the launch is sized for (2 or 3: selects the register bound); mma: trailing
+// updates on the FP64 tensor pipe (mma.sync m8n8k4) instead of fused multiply-adds.
+cudaError_t launch_getrf_big_fma(const BatchArgs& args, int ctas, int nmax, int cps, bool mma,
                                  cudaStream_t s);
 long long getrf_big_backup_doubles(int nmax);
 // Resident form: one matrix per CTA of w warps (2, 4 or 8) over the task list (one matrix per

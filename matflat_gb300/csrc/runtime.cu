@@ -152,6 +152,7 @@ struct mfg_plan {
   int csel = 0;
   int cta_nmax = 0;  // GETRF: largest order of the CTA-per-matrix segment (segment 3)
   int big_cps = 3;   // GETRF FMA form: CTAs per SM of the blocked kernel (2 or 3; MFG_LU_BIG_CPS)
+  bool big_mma = false;  // ... and its trailing updates on the FP64 tensor pipe (MFG_LU_BIG_MMA)
   // GETRF (double): resident form (segment 4): orders in [blk_lo, SMEM_N] go to one CTA of blk_w
   // warps each, blk_cps CTAs per SM, the matrix in shared memory; blk_lo = 0: off.
   int blk_lo = 0;
@@ -646,7 +647,8 @@ int plan_launch(mfg_plan* p, cudaStream_t s) {
         // runs the blocked kernel.
         a.count = a.ntasks;
         const int ctas = (int)getrf_cta_ctas(p);
-        e = p->args.fma ? mfg::launch_getrf_big_fma(a, ctas, p->cta_nmax, p->big_cps, s)
+        e = p->args.fma ? mfg::launch_getrf_big_fma(a, ctas, p->cta_nmax, p->big_cps,
+                                                    p->big_mma, s)
                         : mfg::launch_getrf_cta(a, ctas, p->cta_nmax, s);
       } else {
         const long long need = ((long long)a.ntasks + p->warps - 1) / p->warps;
@@ -912,6 +914,7 @@ int plan_create(mfg_ctx* ctx, mfg_plan** out, mfg_plan::Kind kind, int count, co
     }
     // The FMA form's blocked kernel for orders above SMEM_N: CTAs per SM (2 or 3).
     p->big_cps = env_int("MFG_LU_BIG_CPS", 3) == 2 ? 2 : 3;
+    p->big_mma = env_int("MFG_LU_BIG_MMA", 0) != 0;
     if (gsel >= 0) {
       const int rc = getrf_build_tasks(p, gsel);
       if (rc != MFG_OK) {

@@ -180,13 +180,16 @@ def test_lu_fma_padded_and_large_orders(mf, big):
         assert np.linalg.norm(An[p, :] - L @ U, 1) / np.linalg.norm(An, 1) <= 1e-13 * ni, i
 
 
-def test_lu_fma_blocked_large_orders(mf):
+@pytest.mark.parametrize("mma", [0, 1], ids=["fma-tiles", "dmma-tiles"])
+def test_lu_fma_blocked_large_orders(mf, mma, monkeypatch):
     """Orders above 128 in the FMA form run the blocked CTA kernel (panels of 32 columns, U12
-    solve, 64 x 64 trailing-update tiles): pivots and signs identical to the oracle's, factors and
-    solutions backward stable, padding rows untouched; a near-tie and a NaN at large orders are
-    redone in MatFlat's arithmetic (the oracle's bits); solve-only calls give the fused call's
-    bits; the exact form afterwards gives MatFlat's bits."""
+    solve, 64 x 64 trailing-update tiles of fused multiply-adds, or of FP64 tensor-pipe mma with
+    MFG_LU_BIG_MMA=1): pivots and signs identical to the oracle's, factors and solutions backward
+    stable, padding rows untouched; a near-tie and a NaN at large orders are redone in MatFlat's
+    arithmetic (the oracle's bits); solve-only calls give the fused call's bits; the exact form
+    afterwards gives MatFlat's bits."""
     import torch
+    monkeypatch.setenv("MFG_LU_BIG_MMA", str(mma))
     rng = np.random.default_rng(330)
     n = np.array([129, 160, 191, 200, 256, 257, 300, 333, 384, 512, 97, 64, 450, 130],
                  np.int32)
