@@ -24,7 +24,9 @@
 
 namespace mfg {
 
+
 constexpr int BIG_W = 8;               // warps per CTA
+static_assert(2 * RHS_CHUNK >= BIG_W, "solve staging: BIG_W warps of n | 1 doubles per slice");
 constexpr int BIG_T = BIG_W * 32;
 constexpr int BIG_NB = 32;             // panel width
 constexpr int BIG_TM = 64;             // trailing-update tile: BIG_TM x BIG_TM, 4 x 4 per thread
@@ -385,8 +387,9 @@ __device__ __noinline__ void big_fallback(double* a, int n, long long lda, const
 }
 
 // Work items: the plan's tasks (one matrix each, p.ntasks of them, taken from p.queue).  Per CTA:
-// a copy of up to bstride doubles in p.fbackup and a slice of p.gscratch (the solve's staging and
-// the fallback's column sums).
+// a copy of up to bstride doubles in p.fbackup and a slice of p.gscratch (warp_scratch_doubles(n)
+// >= n + BIG_W (n | 1): the reciprocals and the warps' solve staging; the fallback's column
+// sums).
 // MINB: resident CTAs per SM the register allocation is bounded for (2: 128 registers, 3: 80).
 template <int MINB, bool MMA>
 __global__ void __launch_bounds__(BIG_T, MINB) getrf_big_fma_kernel(BatchArgs p,
@@ -418,8 +421,17 @@ __global__ void __launch_bounds__(BIG_T, MINB) getrf_big_fma_kernel(BatchArgs p,
       }
       __syncthreads();
     }
-    if (p.nrhs > 0 && tid < 32)
-      getrs_fma<32>(a, n, lda, piv, p.b + p.b_off[mat], n, p.nrhs, slice + n, slice);
+    if (p.nrhs > 0) {
+      // The reciprocals of U's diagonal once (slice[0, n)), then warp w solves right-hand sides
+      // w, w + BIG_W, ... one at a time, staged in slice + n + w (n | 1).
+      for (int i = tid; i < n; i += BIG_T) slice[i] = __drcp_rn(a[(long long)i * lda + i]);
+      __syncthreads();
+      const int warp = tid >> 5;
+      double* xs = slice + n + (long long)warp * (n | 1);
+      for (int r = warp; r < p.nrhs; r += BIG_W)
+        getrs_fma<32, true>(a, n, lda, piv, p.b + p.b_off[mat] + (long long)r * n, n, 1, xs,
+                            slice);
+    }
     if (tid == 0 && !p.solve_only) {
       p.sign[mat] = sign;
       p.info[mat] = info;

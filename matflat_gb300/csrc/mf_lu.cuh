@@ -290,14 +290,17 @@ __device__ void getrs_warp(const typename S::T* lu, int n, long long lda, const 
 // b[piv[i]]), then L y = b' (unit lower) and U x = y, both as column sweeps with fused
 // multiply-adds (column t of the factor is contiguous), U's diagonal applied as its reciprocal.
 // rcp: n doubles of the group's scratch.  b: column-major, leading dimension ldb, overwritten.
-// The solve of the FMA form (lu_fma.cu, lu_big.cu) for every matrix, fallbacks included.
-template <int G>
+// The solve of the FMA form (lu_fma.cu, lu_big.cu) for every matrix, fallbacks included.  Every
+// right-hand side's arithmetic is independent of the others', so any split of them over calls
+// or groups gives the same bits.  RCP: rcp already holds the reciprocals of U's diagonal.
+template <int G, bool RCP = false>
 __device__ void getrs_fma(const double* lu, int n, long long lda, const int* piv, double* b,
                           long long ldb, int nrhs, double* xs, double* rcp) {
   const int lane = group_lane<G>();
   const unsigned gm = group_mask<G>();
   const int ldx = n | 1;
-  for (int t = lane; t < n; t += G) rcp[t] = __drcp_rn(lu[(long long)t * lda + t]);
+  if (!RCP)
+    for (int t = lane; t < n; t += G) rcp[t] = __drcp_rn(lu[(long long)t * lda + t]);
   __syncwarp(gm);
   for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK) {
     const int nr = nrhs - r0 < RHS_CHUNK ? nrhs - r0 : RHS_CHUNK;
