@@ -473,8 +473,8 @@ MFG_API int mfg_dgesv_mixed_batched(mfg_plan* plan, const double* a, const doubl
  * MFG_LU_GROUPS, MFG_QR_GROUP) take precedence over the table for new plans. */
 MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
 
-/* Arithmetic form of a batched Cholesky or QR plan (no counterpart in the reference; MatFlat has
- * one form).  MFG_FORM_EXACT (default): MatFlat's arithmetic, bit-identical factors, info and
+/* Arithmetic form of a batched Cholesky, QR or LU plan (no counterpart in the reference; MatFlat
+ * has one form).  MFG_FORM_EXACT (default): MatFlat's arithmetic, bit-identical factors, info and
  * solutions.  MFG_FORM_FMA, Cholesky (double overload): the same column order and failure test,
  * with fused multiply-adds in any order and the column scaled by the reciprocal of its
  * diagonal: the factor satisfies the Cholesky backward-error bound
@@ -485,13 +485,14 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
  * (double overload): MatFlat's Householder algorithm and storage (no sign choice,
  * rdiag = -norm, the same degenerate-reflector rules) with fused multiply-add dots, norms and
  * updates and the column scaled by the reciprocal of its norm: backward-stable factors and
- * least-squares solutions instead of MatFlat's bits.  MFG_FORM_FMA, LU (double overload, the
- * size-bucketed schedule; orders above 128 in CTA-per-matrix batches stay exact): MatFlat's pivot
- * rule and Crout schedule with fused multiply-add dots and reciprocal column scaling, and a
- * screen at every column that keeps MatFlat's pivots: a matrix whose pivot could depend on
- * rounding (the runner-up within about 1.5e-8 of the pivot, ties, a zero pivot, NaN or infinite
- * candidates) is redone in MatFlat's arithmetic (mfg_plan_form_fallbacks counts them); factors
- * satisfy |PA - LU| <= gamma_n |L| |U|, solutions come from fused multiply-add column sweeps.
+ * least-squares solutions instead of MatFlat's bits.  MFG_FORM_FMA, LU (double overload):
+ * MatFlat's pivot rule with fused multiply-add arithmetic and reciprocal column scaling (the
+ * Crout schedule up to order 176, a blocked right-looking LU with one CTA per matrix above it, or
+ * above 128 in batches with few such matrices), and a screen at every column that keeps MatFlat's
+ * pivots: a matrix whose pivot could depend on rounding (the runner-up within about 1.5e-8 of the
+ * pivot, ties, a zero pivot, NaN or infinite candidates) is redone in MatFlat's arithmetic
+ * (mfg_plan_form_fallbacks counts them); factors satisfy |PA - LU| <= gamma_n |L| |U|, solutions
+ * come from fused multiply-add column sweeps.
  * The screen is not a proof that every pivot is MatFlat's.  MFG_ERR_UNSUPPORTED for other
  * plans.
  * Drops the plan's cached graph. */
