@@ -418,16 +418,21 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   struct Task { int first, cnt, g; };
   std::vector<Task> segs[5];
   // Orders above SMEM_N go to whole CTAs (segment 3) when there are too few of them to give every
-  // SM eight warps, and in the FMA form orders above BIG_FMA_MIN_N always (its blocked CTA kernel
-  // beats 32-lane warp tasks from about there: 68 against 72 ms for 8,192 matrices of order 192,
-  // 66 against 62 ms for 12,288 of order 160); MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
+  // SM eight warps (same bits either way).  The FMA form, whose bits depend on the schedule, sends
+  // orders above BIG_FMA_MIN_N to its blocked CTA kernel whatever the count, so that host-buffer
+  // chunks and device calls agree (the blocked kernel beats 32-lane warp tasks from about there:
+  // 68 against 72 ms for 8,192 matrices of order 192, 66 against 62 ms for 12,288 of order 160).
+  // MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
   constexpr int BIG_FMA_MIN_N = 176;
   long long big = 0;
   for (int i = 0; i < count; i++) big += p->hn[i] > mfg::SMEM_N ? 1 : 0;
   const int cta_env = env_int("MFG_LU_CTA", -1);
   const bool cta = cta_env >= 0 ? cta_env == 1 : big < 8LL * ctx->sm_count;
-  const int cta_from = cta ? mfg::SMEM_N
-                       : (cta_env < 0 && p->args.fma) ? BIG_FMA_MIN_N : INT_MAX;
+  const int cta_from = cta_env == 1 ? mfg::SMEM_N
+                       : cta_env == 0 ? INT_MAX
+                       : p->args.fma  ? BIG_FMA_MIN_N
+                       : cta          ? mfg::SMEM_N
+                                      : INT_MAX;
   for (int i = 0; i < count;) {
     int j = i;
     while (j < count && p->hn[idx[j]] == p->hn[idx[i]]) j++;

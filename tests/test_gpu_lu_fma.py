@@ -136,9 +136,9 @@ def test_lu_fma_host_buffers_and_autotune(mf):
 
 @pytest.mark.parametrize("big", [False, True], ids=["cta-bucket", "task-bucket"])
 def test_lu_fma_padded_and_large_orders(mf, big):
-    """lda > n, and orders above 128: few of them run in the FMA form's blocked CTA kernel;
-    many of them in 32-lane tasks (scratch in global memory) up to order 176 and in the blocked
-    kernel above.  Pivots identical to the oracle's, factors backward stable."""
+    """lda > n, and orders above 128: up to order 176 in 32-lane tasks (scratch in global
+    memory), above it in the blocked CTA kernel, few or many of them.  Pivots identical to the
+    oracle's, factors backward stable."""
     import torch
     rng = np.random.default_rng(320 + big)
     count = 1400 if big else 120
@@ -266,3 +266,35 @@ def test_lu_fma_blocked_large_orders(mf, mma, monkeypatch):
         oracle.lu(ni, ni, oa, li, np.zeros(ni, np.int32))
         assert_bits(ga[a_off[i]:a_off[i] + sz[i]], oa, "exact matrix %d" % i)
     assert batch.form_fallbacks() == 0
+
+
+def test_lu_fma_large_orders_host_buffers(mf, monkeypatch):
+    """Host-buffer calls (four pipelined chunk plans) give the device call's bits in the FMA form
+    for orders on both sides of the blocked kernel's threshold (176)."""
+    monkeypatch.setenv("MFG_PIPE_CHUNKS", "4")
+    rng = np.random.default_rng(340)
+    n = rng.choice([40, 150, 170, 200, 260], size=48).astype(np.int32)
+    sz = n.astype(np.int64) ** 2
+    a_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    a = rng.standard_normal(int(sz.sum()))
+    piv_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))[:-1]]).astype(np.int64)
+    b_off = piv_off * 2
+    b = rng.standard_normal(int(n.sum()) * 2)
+    batch = mf.LuBatch(n, a_off, piv_off, nrhs=2, b_off=b_off)
+    batch.set_form("fma")
+    da, db, dpiv, dsign, dinfo = _run(mf, batch, a, b, n)
+    ha, hb = a.copy(), b.copy()
+    hpiv = np.zeros(int(n.sum()), np.int32)
+    hsign = np.zeros(len(n), np.int32)
+    hinfo = np.zeros(len(n), np.int32)
+    batch.run_host(ha, hpiv, hb, hsign, hinfo)
+    assert_bits(ha, _host(da))
+    assert_bits(hb, _host(db))
+    np.testing.assert_array_equal(hpiv, _host(dpiv))
+    np.testing.assert_array_equal(hsign, _host(dsign))
+    for i in (0, 1, 2, 3):
+        ni = int(n[i])
+        oa = a[a_off[i]:a_off[i] + sz[i]].copy()
+        opiv = np.zeros(ni, np.int32)
+        oracle.lu(ni, ni, oa, ni, opiv)
+        np.testing.assert_array_equal(hpiv[piv_off[i]:piv_off[i] + ni], opiv)
