@@ -24,7 +24,6 @@
 
 namespace mfg {
 
-
 constexpr int BIG_W = 8;               // warps per CTA
 static_assert(2 * RHS_CHUNK >= BIG_W, "solve staging: BIG_W warps of n | 1 doubles per slice");
 constexpr int BIG_T = BIG_W * 32;
