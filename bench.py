@@ -1117,7 +1117,18 @@ def main():
             flops = lu_flops(d["n"], d["nrhs"])
             byts = lu_bytes(d["n"], d["nrhs"])
             table = tuned[2] if tuned is not None else int(os.environ.get("MFG_LU_GROUPS", "2"))
-            kernel_key = "getrf_task_kernel" if table >= 0 else "getrf_batched_kernel"
+            if args.form == "fma":
+                # FMA form: orders above 176 run the blocked CTA kernel
+                big = args.fixed_n is not None and args.fixed_n > 176
+                kernel_key = "getrf_big_fma_kernel" if big else "getrf_task_fma_kernel"
+            else:
+                kernel_key = "getrf_task_kernel" if table >= 0 else "getrf_batched_kernel"
+            # traffic.txt holds per-launch figures of the default batch, and of the blocked
+            # kernel's 2,048 x n=512 batch; other workloads get none
+            if args.fixed_n or args.count:
+                traffic_key = ("getrf_big_fma_kernel_n512x2048"
+                               if kernel_key == "getrf_big_fma_kernel" and args.fixed_n == 512
+                               and count == 2048 else "none")
         elif cfg_name in ("chol", "chol100k"):
             plan = mf.CholeskyBatch(d["n"], d["a_off"], nrhs=d["nrhs"], b_off=d["b_off"])
             plan.set_form(args.form)
