@@ -255,17 +255,75 @@ __device__ __forceinline__ void big_tiles_mma(double* a, int n, long long lda, i
   }
 }
 
+// A22 -= L21 U12 for the BIG_TM x BIG_TM tile at (r0, c0) with fused multiply-adds; U12's block
+// is in sm.bs (big_pos order).  Each thread works on tile rows tx + 16 u, u < UR, and columns
+// ty + 16 v, v < VR: UR (VR) = 2 covers the first 32 rows (columns), for an edge tile with no more
+// valid ones, so that its padding costs no FP64 work.
+template <int UR, int VR>
+__device__ __forceinline__ void big_tile(double* a, int n, long long lda, int j0, int r0, int c0,
+                                         BigSmem& sm) {
+  static_assert((UR == 2 || UR == 4) && (VR == 2 || VR == 4), "2 or 4 rows / columns");
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  double acc[UR][VR];
+#pragma unroll
+  for (int u = 0; u < UR; ++u) {
+#pragma unroll
+    for (int v = 0; v < VR; ++v) {
+      const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+      acc[u][v] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
+    }
+  }
+  constexpr int ROWS = 16 * UR;   // tile rows used
+  for (int e = tid; e < BIG_NB * ROWS; e += BIG_T) {
+    const int k = e / ROWS;
+    const int rr = e - k * ROWS;
+    const int i = r0 + rr;
+    sm.as[k][big_pos(rr)] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int k = 0; k < BIG_NB; ++k) {
+    double av[4], bv[4];
+    const double2 a01 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx]);
+    av[0] = a01.x, av[1] = a01.y;
+    if constexpr (UR == 4) {
+      const double2 a23 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx + 2]);
+      av[2] = a23.x, av[3] = a23.y;
+    }
+    const double2 b01 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty]);
+    bv[0] = b01.x, bv[1] = b01.y;
+    if constexpr (VR == 4) {
+      const double2 b23 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty + 2]);
+      bv[2] = b23.x, bv[3] = b23.y;
+    }
+#pragma unroll
+    for (int u = 0; u < UR; ++u) {
+#pragma unroll
+      for (int v = 0; v < VR; ++v) acc[u][v] = __fma_rn(-av[u], bv[v], acc[u][v]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < UR; ++u) {
+#pragma unroll
+    for (int v = 0; v < VR; ++v) {
+      const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
+      if (i < n && jj < n) a[(long long)jj * lda + i] = acc[u][v];
+    }
+  }
+  __syncthreads();
+}
+
 // U12 = L11^-1 A12 and A22 -= L21 U12 for the rows and columns [j1, n), j1 = j0 + BIG_NB, one
 // block of BIG_TM trailing columns at a time: the block's U12 rows are solved in shared memory
 // (one column per thread of the first BIG_TM, from L11 in shared memory), written back, and kept
 // in shared memory for the block's BIG_TM x BIG_TM update tiles down the trailing rows.
 // MMA: the tiles on the FP64 tensor pipe (each warp 16 x 32 of the tile as 2 x 4 mma tiles of
 // 8 x 8, operands in fragment order, big_frag); otherwise 4 x 4 fused multiply-adds per thread
-// (operands in big_pos order).
+// (operands in big_pos order, big_tile).
 template <bool MMA>
 __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem& sm) {
   const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
   double* asf = &sm.as[0][0];
   double* bsf = &sm.bs[0][0];
   const int j1 = j0 + BIG_NB;
@@ -308,48 +366,15 @@ __device__ void big_u12_update(double* a, int n, long long lda, int j0, BigSmem&
       big_tiles_mma(a, n, lda, j0, j1, c0, mt, asf, bsf);
       continue;
     }
+    // Edge tiles whose valid rows (columns) fit in 32 run 2 of each thread's 4 rows (columns).
+    const int vr = n - c0 > 32 ? 4 : 2;
     for (int rb = 0; rb < mt; ++rb) {
       const int r0 = j1 + rb * BIG_TM;
-      double acc[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
-          acc[u][v] = (i < n && jj < n) ? a[(long long)jj * lda + i] : 0.0;
-        }
-      }
-      for (int e = tid; e < BIG_NB * BIG_TM; e += BIG_T) {
-        const int k = e / BIG_TM;
-        const int rr = e - k * BIG_TM;
-        const int i = r0 + rr;
-        sm.as[k][big_pos(rr)] = i < n ? a[(long long)(j0 + k) * lda + i] : 0.0;
-      }
-      __syncthreads();
-#pragma unroll 4
-      for (int k = 0; k < BIG_NB; ++k) {
-        double av[4], bv[4];
-        const double2 a01 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx]);
-        const double2 a23 = *reinterpret_cast<const double2*>(&sm.as[k][4 * tx + 2]);
-        const double2 b01 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty]);
-        const double2 b23 = *reinterpret_cast<const double2*>(&sm.bs[k][4 * ty + 2]);
-        av[0] = a01.x, av[1] = a01.y, av[2] = a23.x, av[3] = a23.y;
-        bv[0] = b01.x, bv[1] = b01.y, bv[2] = b23.x, bv[3] = b23.y;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-#pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] = __fma_rn(-av[u], bv[v], acc[u][v]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int i = r0 + tx + 16 * u, jj = c0 + ty + 16 * v;
-          if (i < n && jj < n) a[(long long)jj * lda + i] = acc[u][v];
-        }
-      }
-      __syncthreads();
+      const int ur = n - r0 > 32 ? 4 : 2;
+      if (ur == 4 && vr == 4) big_tile<4, 4>(a, n, lda, j0, r0, c0, sm);
+      else if (ur == 4) big_tile<4, 2>(a, n, lda, j0, r0, c0, sm);
+      else if (vr == 4) big_tile<2, 4>(a, n, lda, j0, r0, c0, sm);
+      else big_tile<2, 2>(a, n, lda, j0, r0, c0, sm);
     }
   }
 }
