@@ -1118,8 +1118,8 @@ def main():
             byts = lu_bytes(d["n"], d["nrhs"])
             table = tuned[2] if tuned is not None else int(os.environ.get("MFG_LU_GROUPS", "2"))
             if args.form == "fma":
-                # FMA form: orders above 176 run the blocked CTA kernel
-                big = args.fixed_n is not None and args.fixed_n > 176
+                # FMA form: orders above 152 run the blocked CTA kernel
+                big = args.fixed_n is not None and args.fixed_n > 152
                 kernel_key = "getrf_big_fma_kernel" if big else "getrf_task_fma_kernel"
             else:
                 kernel_key = "getrf_task_kernel" if table >= 0 else "getrf_batched_kernel"

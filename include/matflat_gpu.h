@@ -487,7 +487,7 @@ MFG_API int mfg_plan_autotune(mfg_plan* plan, int* config);
  * updates and the column scaled by the reciprocal of its norm: backward-stable factors and
  * least-squares solutions instead of MatFlat's bits.  MFG_FORM_FMA, LU (double overload):
  * MatFlat's pivot rule with fused multiply-add arithmetic and reciprocal column scaling (the
- * Crout schedule up to order 176, a blocked right-looking LU with one CTA per matrix above it,
+ * Crout schedule up to order 152, a blocked right-looking LU with one CTA per matrix above it,
  * whatever the batch size), and a screen at every column that keeps MatFlat's
  * pivots: a matrix whose pivot could depend on rounding (the runner-up within about 1.5e-8 of the
  * pivot, ties, a zero pivot, NaN or infinite candidates) is redone in MatFlat's arithmetic

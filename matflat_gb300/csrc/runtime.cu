@@ -420,10 +420,11 @@ int getrf_build_tasks(mfg_plan* p, int gsel) {
   // Orders above SMEM_N go to whole CTAs (segment 3) when there are too few of them to give every
   // SM eight warps (same bits either way).  The FMA form, whose bits depend on the schedule, sends
   // orders above BIG_FMA_MIN_N to its blocked CTA kernel whatever the count, so that host-buffer
-  // chunks and device calls agree (the blocked kernel beats 32-lane warp tasks from about there:
-  // 68 against 72 ms for 8,192 matrices of order 192, 66 against 62 ms for 12,288 of order 160).
+  // chunks and device calls agree (the blocked kernel beats 32-lane warp tasks from about there,
+  // 4 right-hand sides: 56.6 against 64.7 ms for 12,288 matrices of order 160, 62.6 against
+  // 62.5 ms for 14,336 of order 152, 63.9 against 53.8 ms for 16,384 of order 136).
   // MFG_LU_CTA = 0 / 1 forces the warp / CTA form.
-  constexpr int BIG_FMA_MIN_N = 176;
+  constexpr int BIG_FMA_MIN_N = 152;
   long long big = 0;
   for (int i = 0; i < count; i++) big += p->hn[i] > mfg::SMEM_N ? 1 : 0;
   const int cta_env = env_int("MFG_LU_CTA", -1);

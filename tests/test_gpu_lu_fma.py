@@ -136,7 +136,7 @@ def test_lu_fma_host_buffers_and_autotune(mf):
 
 @pytest.mark.parametrize("big", [False, True], ids=["cta-bucket", "task-bucket"])
 def test_lu_fma_padded_and_large_orders(mf, big):
-    """lda > n, and orders above 128: up to order 176 in 32-lane tasks (scratch in global
+    """lda > n, and orders above 128: up to order 152 in 32-lane tasks (scratch in global
     memory), above it in the blocked CTA kernel, few or many of them.  Pivots identical to the
     oracle's, factors backward stable."""
     import torch
@@ -270,7 +270,7 @@ def test_lu_fma_blocked_large_orders(mf, mma, monkeypatch):
 
 def test_lu_fma_large_orders_host_buffers(mf, monkeypatch):
     """Host-buffer calls (four pipelined chunk plans) give the device call's bits in the FMA form
-    for orders on both sides of the blocked kernel's threshold (176)."""
+    for orders on both sides of the blocked kernel's threshold (152)."""
     monkeypatch.setenv("MFG_PIPE_CHUNKS", "4")
     rng = np.random.default_rng(340)
     n = rng.choice([40, 150, 170, 200, 260], size=48).astype(np.int32)
