@@ -9,6 +9,9 @@ schedules give MatFlat's values, independently of the GPU:
   * LU in Crout order (csrc/lu.cu): step k finishes row k of U and column k+1 of L, with
     MatFlat's pivot rule (first index of the largest |v| among non-NaN entries; a NaN on the
     diagonal candidate is never displaced).
+The FMA form's blocked LU for large orders (csrc/lu_big.cu) is a different arithmetic, so its
+model is checked by what that form promises instead: MatFlat's pivots and sign where its screen
+passes, a rejection where the choice could depend on rounding, a backward-stable factorization.
 """
 import numpy as np
 import pytest
@@ -161,3 +164,87 @@ def test_lu_crout_schedule_singular():
     np.testing.assert_array_equal(got.view(np.uint64), exp.view(np.uint64))
     np.testing.assert_array_equal(piv_g, piv_e)
     assert sign_g == sign_e
+
+
+# The FMA form's pivot screen (LU_FMA_MARGIN_ULPS in csrc/mf_lu.cuh): the pivot's |v| bits must
+# exceed every other candidate's by 2^26 units in the last place.
+MARGIN_ULPS = 1 << 26
+
+
+def lu_blocked_model(A, nb=32):
+    """The blocked right-looking schedule of getrf_big_fma_kernel on an n-by-n array (numpy
+    float64, separately rounded products and sums instead of fused ones): per panel of nb columns,
+    each column's pivot search with the screen, the whole-row swap, reciprocal scaling and the
+    rank-1 update of the panel's later columns; then U12 = L11^-1 A12 and A22 -= L21 U12.
+    Returns (factors, piv, sign) or None when a column fails the screen."""
+    from scipy.linalg import solve_triangular
+    a = np.array(A, dtype=np.float64)
+    n = a.shape[0]
+    piv = np.arange(n)
+    sign = 1
+    for j0 in range(0, n, nb):
+        j1 = min(n, j0 + nb)
+        for j in range(j0, j1):
+            col = a[j:, j]
+            if not np.isfinite(col).all():
+                return None
+            keys = np.abs(col).view(np.uint64).astype(np.int64)
+            p = int(np.argmax(keys))
+            second = np.max(np.delete(keys, p)) if len(keys) > 1 else 0
+            if keys[p] == 0 or keys[p] - second < MARGIN_ULPS:
+                return None
+            p += j
+            if p != j:
+                a[[j, p], :] = a[[p, j], :]
+                piv[[j, p]] = piv[[p, j]]
+                sign = -sign
+            r = 1.0 / a[j, j]
+            a[j + 1:, j] *= r
+            a[j + 1:, j + 1:j1] -= np.outer(a[j + 1:, j], a[j, j + 1:j1])
+        if j1 < n:
+            a[j0:j1, j1:] = solve_triangular(a[j0:j1, j0:j1], a[j0:j1, j1:], lower=True,
+                                             unit_diagonal=True, check_finite=False)
+            a[j1:, j1:] -= a[j1:, j0:j1] @ a[j0:j1, j1:]
+    return a, piv, sign
+
+
+@pytest.mark.parametrize("n", [40, 129, 200, 333])
+def test_lu_blocked_schedule_pivots(n):
+    """Random N(0,1) matrices: the screen passes and the pivots and sign are MatFlat's; the
+    factors reproduce PA to a normwise backward error within 1e-13 n."""
+    rng = np.random.default_rng(700 + n)
+    A = rng.standard_normal((n, n))
+    out = lu_blocked_model(A)
+    assert out is not None
+    F, piv, sign = out
+    exp = A.flatten(order="F")
+    piv_e = np.zeros(n, np.int32)
+    sign_e = oracle.lu(n, n, exp, n, piv_e)
+    np.testing.assert_array_equal(piv, piv_e)
+    assert sign == sign_e
+    L = np.tril(F, -1) + np.eye(n)
+    U = np.triu(F)
+    assert np.linalg.norm(A[piv, :] - L @ U, 1) / np.linalg.norm(A, 1) <= 1e-13 * n
+
+
+def test_lu_blocked_schedule_screen():
+    """A near-tie (runner-up within 2^26 ulps), an exact tie in a later panel's column, a NaN and
+    a zero column are rejected; a clear gap passes."""
+    rng = np.random.default_rng(710)
+    base = rng.standard_normal((100, 100))
+    near = base.copy()
+    near[5, 0], near[9, 0] = 50.0, -50.0 * (1.0 + 2.0 ** -45)
+    assert lu_blocked_model(near) is None
+    tie = base.copy()
+    tie[60, 40] = tie[70, 40] = 1e6
+    tie[60, :40] = tie[70, :40] = 0.0   # zero multipliers: no update reaches them, an exact tie
+    assert lu_blocked_model(tie) is None
+    nan = base.copy()
+    nan[30, 70] = np.nan
+    assert lu_blocked_model(nan) is None
+    zero = base.copy()
+    zero[:, 0] = 0.0
+    assert lu_blocked_model(zero) is None
+    clear = base.copy()
+    clear[5, 0], clear[9, 0] = 50.0, -49.0
+    assert lu_blocked_model(clear) is not None
